@@ -1,0 +1,194 @@
+/*
+  tmrg.h — C ABI of the GB300 octree-forest adaptation library.
+
+  One opaque forest handle stands for one TMROctForest (TMROctForest.h:46);
+  the octants, nodes and operators live in GPU memory as structure-of-arrays
+  and are produced by CUDA kernels for sm_103a.  Every entry point returns
+  a tmrg_status (0 = success) and never aborts; host pointers are copied
+  in/out with explicit sizes, and *_device variants take device pointers.
+
+  Each declaration names the reference interface it replaces
+  (file:line in the TMR sources).  The reference reports errors by printing
+  to stderr and returning; tmrg returns the status instead and
+  tmrg_last_error() gives the message.
+*/
+#ifndef TMRG_H
+#define TMRG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  TMRG_OK = 0,
+  TMRG_ERR_ARG = 1,         /* bad argument (null, size mismatch, range) */
+  TMRG_ERR_STATE = 2,       /* call out of order (e.g. no octants yet) */
+  TMRG_ERR_CUDA = 3,        /* CUDA runtime error */
+  TMRG_ERR_NOMEM = 4,       /* device allocation failed */
+  TMRG_ERR_KEY_RANGE = 5,   /* blocks x levels exceed the 64-bit sort key */
+  TMRG_ERR_UNSUPPORTED = 6, /* order/interpolation not built */
+  TMRG_ERR_INTERNAL = 7     /* a device-side consistency check failed */
+} tmrg_status;
+
+/* Interpolation types, same values as TMRInterpolationType
+   (TMRBase.h:39-43). */
+enum { TMRG_UNIFORM_POINTS = 0, TMRG_GAUSS_LOBATTO_POINTS = 1,
+       TMRG_BERNSTEIN_POINTS = 2 };
+
+typedef struct tmrg_forest tmrg_forest;
+typedef struct tmrg_interp tmrg_interp;
+typedef struct tmrg_filter tmrg_filter;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *tmrg_last_error(void);
+/* Library version string. */
+const char *tmrg_version(void);
+
+/* ---- forest ---------------------------------------------------------- */
+/* TMROctForest::TMROctForest(MPI_Comm, int order, TMRInterpolationType)
+   (TMROctForest.h:51-52).  `stream` is a cudaStream_t (NULL = default);
+   all work of this forest is ordered on it. */
+int tmrg_forest_create(int order, int interp_type, void *stream,
+                       tmrg_forest **out);
+/* TMREntity::decref reaching zero (TMRBase.cpp:145-156). */
+int tmrg_forest_destroy(tmrg_forest *f);
+/* TMROctForest::setConnectivity (TMROctForest.h:64-65;
+   TMROctForest.cpp:558-590).  block_conn: host, 8 ints per block. */
+int tmrg_forest_set_connectivity(tmrg_forest *f, int num_nodes,
+                                 const int *block_conn, int num_blocks);
+/* TMROctForest::setMeshOrder / getMeshOrder / getInterpType
+   (TMROctForest.h:72-75; TMROctForest.cpp:1389-1440). */
+int tmrg_forest_set_mesh_order(tmrg_forest *f, int order, int interp_type);
+int tmrg_forest_get_mesh_order(tmrg_forest *f, int *order, int *interp_type);
+/* TMROctForest::getInterpKnots (TMROctForest.cpp:1492-1497). */
+int tmrg_forest_get_interp_knots(tmrg_forest *f, double *knots);
+/* TMROctForest::createTrees (TMROctForest.h:79; TMROctForest.cpp:1744). */
+int tmrg_forest_create_trees(tmrg_forest *f, int level);
+/* TMROctForest::refine(const int refinement[], int min, int max)
+   (TMROctForest.h:87; TMROctForest.cpp:2169-2329).  `refinement` is a
+   host array of n = number of octants, or NULL to refine every octant. */
+int tmrg_forest_refine(tmrg_forest *f, const int *refinement, int64_t n,
+                       int min_level, int max_level);
+/* Same, with `refinement` in device memory. */
+int tmrg_forest_refine_device(tmrg_forest *f, const int *d_refinement,
+                              int64_t n, int min_level, int max_level);
+/* TMROctForest::coarsen / duplicate (TMROctForest.h:83-84;
+   TMROctForest.cpp:2097-2164): a new forest owned by the caller. */
+int tmrg_forest_coarsen(tmrg_forest *f, tmrg_forest **out);
+int tmrg_forest_duplicate(tmrg_forest *f, tmrg_forest **out);
+/* TMROctForest::balance(int balance_corner) (TMROctForest.h:91;
+   TMROctForest.cpp:2917-3089). */
+int tmrg_forest_balance(tmrg_forest *f, int balance_corner);
+/* TMROctForest::repartition (TMROctForest.h:80): one GPU holds the whole
+   forest, so this only validates the handle. */
+int tmrg_forest_repartition(tmrg_forest *f, int max_rank);
+/* TMROctForest::createNodes (TMROctForest.h:95; TMROctForest.cpp:4064). */
+int tmrg_forest_create_nodes(tmrg_forest *f);
+
+/* TMROctForest::getOctants (TMROctForest.h:125).  Number of octants, then
+   a host copy: 7 ints per octant {block, x, y, z, tag, level, info}. */
+int tmrg_forest_num_octants(tmrg_forest *f, int64_t *n);
+int tmrg_forest_get_octants(tmrg_forest *f, int *out7, int64_t n);
+/* Device view of the octant arrays (borrowed, valid until the next
+   mutating call): block, x, y, z as int32, level and info as int16. */
+int tmrg_forest_octants_device(tmrg_forest *f, const int **block,
+                               const int **x, const int **y, const int **z,
+                               const int16_t **level, const int16_t **info);
+/* Sizes after createNodes: out[0] num_local_nodes, [1] owned nodes
+   (getOwnedNodeRange, TMROctForest.cpp:1445), [2] dependent nodes
+   (getDepNodeConn return), [3] getExtPreOffset, [4] elements,
+   [5] dependent-CSR entries. */
+int tmrg_forest_node_sizes(tmrg_forest *f, int64_t out6[6]);
+/* TMROctForest::getNodeConn (TMROctForest.cpp:5686): elements x order^3
+   global node numbers, dependent nodes as -k-1.  Host copy. */
+int tmrg_forest_get_node_conn(tmrg_forest *f, int *conn, int64_t n);
+/* TMROctForest::getNodeNumbers (TMROctForest.cpp:1461): sorted. */
+int tmrg_forest_get_node_numbers(tmrg_forest *f, int *out, int64_t n);
+/* TMROctForest::getDepNodeConn (TMROctForest.cpp:5717): host copies of
+   ptr[num_dep+1], conn[nnz], weights[nnz]. */
+int tmrg_forest_get_dep_node_conn(tmrg_forest *f, int *ptr, int *conn,
+                                  double *weights);
+/* Device views of conn and the dependent CSR (borrowed). */
+int tmrg_forest_node_conn_device(tmrg_forest *f, const int **conn);
+int tmrg_forest_dep_node_conn_device(tmrg_forest *f, const int **ptr,
+                                     const int **conn, const double **w);
+
+/* ---- interpolation (prolongation P: coarse -> fine) ------------------- */
+/* TMROctForest::createInterpolation(TMROctForest *coarse, TACSBVecInterp*)
+   (TMROctForest.h:115; TMROctForest.cpp:6611-6793).  Rows are the fine
+   forest's owned nodes, columns the coarse forest's owned nodes. */
+int tmrg_interp_create(tmrg_forest *fine, tmrg_forest *coarse,
+                       tmrg_interp **out);
+int tmrg_interp_destroy(tmrg_interp *I);
+/* out: {rows, cols, nnz} */
+int tmrg_interp_sizes(tmrg_interp *I, int64_t out3[3]);
+/* Row-sorted CSR of P, host copies. */
+int tmrg_interp_get_csr(tmrg_interp *I, int *rowptr, int *cols, double *w);
+/* The TACSBVecInterp applies used at TMRConformFilter.cpp:163 and
+   TMRMatrixFilter.cpp:315 (TACS is not in the reference tree):
+     mult:            y = P x                 (x: cols x nvec, y: rows x nvec)
+     mult_transpose:  y = P^T x               (x: rows x nvec, y: cols x nvec)
+     mult_weight_transpose: y_j = (P^T x)_j / (P^T 1)_j
+   Vectors are node-major (v[node*nvec + k]).  Host pointers; the *_device
+   forms take device pointers and run on the interpolation's stream. */
+int tmrg_interp_mult(tmrg_interp *I, const double *x, double *y, int nvec);
+int tmrg_interp_mult_transpose(tmrg_interp *I, const double *x, double *y,
+                               int nvec);
+int tmrg_interp_mult_weight_transpose(tmrg_interp *I, const double *x,
+                                      double *y, int nvec);
+int tmrg_interp_mult_device(tmrg_interp *I, const double *x, double *y,
+                            int nvec);
+int tmrg_interp_mult_transpose_device(tmrg_interp *I, const double *x,
+                                      double *y, int nvec);
+int tmrg_interp_mult_weight_transpose_device(tmrg_interp *I, const double *x,
+                                             double *y, int nvec);
+
+/* ---- matrix density filter ------------------------------------------ */
+/* TMRMatrixFilter::TMRMatrixFilter(r, N, ...) / initialize_matrix
+   (TMRMatrixFilter.cpp:30-166), on the nodes of `f` (order 2, trilinear
+   elements as TMRMatrixCreator.h:79-80 selects).  The reference takes node
+   coordinates from a TMRTopology; here every block is a cube of side
+   `block_len`, so an element of level l is a cube of side
+   block_len * 2^-l and its consistent mass matrix is exact.  M is
+   assembled with dependent nodes condensed onto their independent nodes. */
+int tmrg_filter_create(tmrg_forest *f, double block_len, double r, int N,
+                       tmrg_filter **out);
+int tmrg_filter_destroy(tmrg_filter *F);
+/* out: {n (owned nodes), nnz of M} */
+int tmrg_filter_sizes(tmrg_filter *F, int64_t out2[2]);
+/* Host copies of M (CSR) and the diagonal scalings Ainv, B, Tinv. */
+int tmrg_filter_get_matrix(tmrg_filter *F, int *rowptr, int *cols,
+                           double *vals, double *Ainv, double *B,
+                           double *Tinv);
+/* TMRMatrixFilter::applyFilter / applyTranspose over `vpn` interleaved
+   components (setDesignVars/addValues, TMRMatrixFilter.cpp:272-368).
+   Host pointers; *_device forms take device pointers. */
+int tmrg_filter_apply(tmrg_filter *F, int vpn, const double *in, double *out);
+int tmrg_filter_apply_transpose(tmrg_filter *F, int vpn, const double *in,
+                                double *out);
+int tmrg_filter_apply_device(tmrg_filter *F, int vpn, const double *in,
+                             double *out);
+int tmrg_filter_apply_transpose_device(tmrg_filter *F, int vpn,
+                                       const double *in, double *out);
+/* FP32 variant of the filter apply (device pointers, float vectors). */
+int tmrg_filter_apply_f32_device(tmrg_filter *F, int vpn, const float *in,
+                                 float *out);
+int tmrg_filter_apply_transpose_f32_device(tmrg_filter *F, int vpn,
+                                           const float *in, float *out);
+
+/* ---- utilities -------------------------------------------------------- */
+/* Seeded refinement indicator used by the synthetic workloads:
+   out[i] = (U(seed, stream, i) < prob) ? 1 : 0, with U the splitmix64
+   uniform shared with the CPU oracle.  Device pointer. */
+int tmrg_random_refinement_device(uint64_t seed, uint64_t stream, double prob,
+                                  int *d_out, int64_t n, void *cuda_stream);
+/* Number of kernels this library has launched in this process. */
+int64_t tmrg_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TMRG_H */

@@ -2082,3 +2082,206 @@ double oo_uniform(uint64_t seed, uint64_t stream, uint64_t index) {
                              (index * 0xD6E8FEB86659FD93ULL));
   return (double)(r >> 11) * (1.0 / 9007199254740992.0);
 }
+
+/* ------------------------------------------------------------------ */
+/* Matrix density filter (TMRMatrixFilter.cpp:30-235).  Parity unpinned:
+   the mass matrix is assembled by TACS in the reference (absent here).
+   Restatement: trilinear elements (TMRMatrixCreator.h:79-80) on blocks that
+   are cubes of side block_len; the exact element mass matrix of a cube of
+   side a is M_ab = a^3 / (27 * 2^k), k = number of local coordinates in
+   which corners a and b differ.  Dependent nodes are condensed: each
+   element merges its expanded 8x8 block over its distinct independent
+   nodes (first-appearance order; products summed in (a, b, p, q) loop
+   order), and the element blocks are summed in element order. */
+struct oo_filter {
+  int n, nnz, N;
+  double r;
+  int *rowptr, *cols;
+  double *vals, *Ainv, *B, *Tinv;
+};
+
+typedef struct {
+  long key;
+  long seq;
+  double v;
+} oo_fent;
+
+static int cmp_fent(const void *a, const void *b) {
+  const oo_fent *x = (const oo_fent *)a, *y = (const oo_fent *)b;
+  if (x->key != y->key) return x->key < y->key ? -1 : 1;
+  return (x->seq > y->seq) - (x->seq < y->seq);
+}
+
+static void filter_horner(oo_filter *F, int tr, int vpn, const double *in,
+                          double *out) {
+  long n = F->n, len = n * (long)vpn;
+  double *t1 = (double *)malloc(sizeof(double) * (size_t)(len ? len : 1));
+  double *cur = (double *)malloc(sizeof(double) * (size_t)(len ? len : 1));
+  double *nxt = (double *)malloc(sizeof(double) * (size_t)(len ? len : 1));
+  const double *pre = tr ? F->Tinv : F->Ainv, *post = tr ? F->Ainv : F->Tinv;
+  for (long i = 0; i < len; i++) t1[i] = pre[i / vpn] * in[i];
+  memcpy(cur, t1, sizeof(double) * (size_t)len);
+  for (int it = 0; it < F->N; it++) {
+    for (long i = 0; i < n; i++)
+      for (int v = 0; v < vpn; v++) {
+        double acc = 0.0;
+        for (int p = F->rowptr[i]; p < F->rowptr[i + 1]; p++) {
+          int j = F->cols[p];
+          double xv = cur[(long)j * vpn + v];
+          if (tr) xv = F->B[j] * xv;
+          acc = acc + F->vals[p] * xv;
+        }
+        double r = tr ? acc + t1[i * vpn + v] : F->B[i] * acc + t1[i * vpn + v];
+        nxt[i * vpn + v] = r;
+      }
+    double *t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+  for (long i = 0; i < len; i++) out[i] = cur[i] * post[i / vpn];
+  free(t1);
+  free(cur);
+  free(nxt);
+}
+
+oo_filter *oo_filter_create(oo_forest *f, double block_len, double r, int N) {
+  if (f->order != 2) return NULL;
+  oo_create_nodes(f);
+  oo_filter *F = (oo_filter *)calloc(1, sizeof(oo_filter));
+  F->n = f->num_owned;
+  F->N = N;
+  F->r = r;
+  long cap = 1 << 16, ne = 0;
+  oo_fent *E = (oo_fent *)malloc(sizeof(oo_fent) * (size_t)cap);
+  for (long e = 0; e < f->noct; e++) {
+    const int *ec = &f->econn[8 * e];
+    int ni[8][4], nc[8], U[27], K = 0;
+    double nw[8][4];
+    for (int a = 0; a < 8; a++) {
+      int g = ec[a];
+      if (g >= 0) {
+        nc[a] = 1;
+        ni[a][0] = g;
+        nw[a][0] = 1.0;
+      } else {
+        int d = -g - 1;
+        nc[a] = f->dep_ptr[d + 1] - f->dep_ptr[d];
+        for (int p = 0; p < nc[a]; p++) {
+          ni[a][p] = f->dep_conn[f->dep_ptr[d] + p];
+          nw[a][p] = f->dep_w[f->dep_ptr[d] + p];
+        }
+      }
+      for (int p = 0; p < nc[a]; p++) {
+        int u = 0;
+        while (u < K && U[u] != ni[a][p]) u++;
+        if (u == K) U[K++] = ni[a][p];
+      }
+    }
+    double L[27][27];
+    for (int u = 0; u < K; u++)
+      for (int v = 0; v < K; v++) L[u][v] = 0.0;
+    double side = block_len / (double)(1 << f->octs[e].level);
+    double s3 = side * side * side;
+    for (int a = 0; a < 8; a++)
+      for (int b = 0; b < 8; b++) {
+        int x = a ^ b;
+        int k = (x & 1) + ((x >> 1) & 1) + (x >> 2);
+        double mab = s3 / (27.0 * (double)(1 << k));
+        for (int p = 0; p < nc[a]; p++) {
+          int u = 0;
+          while (U[u] != ni[a][p]) u++;
+          double t = mab * nw[a][p];
+          for (int q = 0; q < nc[b]; q++) {
+            int v = 0;
+            while (U[v] != ni[b][q]) v++;
+            L[u][v] = L[u][v] + t * nw[b][q];
+          }
+        }
+      }
+    while (ne + K * K > cap) {
+      cap *= 2;
+      E = (oo_fent *)realloc(E, sizeof(oo_fent) * (size_t)cap);
+    }
+    for (int u = 0; u < K; u++)
+      for (int v = 0; v < K; v++) {
+        E[ne].key = (long)U[u] * (long)F->n + U[v];
+        E[ne].seq = ne;
+        E[ne].v = L[u][v];
+        ne++;
+      }
+  }
+  qsort(E, (size_t)ne, sizeof(oo_fent), cmp_fent);
+  F->rowptr = (int *)calloc((size_t)F->n + 1, sizeof(int));
+  F->cols = (int *)malloc(sizeof(int) * (size_t)(ne ? ne : 1));
+  F->vals = (double *)malloc(sizeof(double) * (size_t)(ne ? ne : 1));
+  int nnz = 0;
+  for (long i = 0; i < ne;) {
+    long j = i;
+    double s = E[i].v;
+    while (j + 1 < ne && E[j + 1].key == E[i].key) {
+      j++;
+      s = s + E[j].v;
+    }
+    F->cols[nnz] = (int)(E[i].key % F->n);
+    F->vals[nnz] = s;
+    F->rowptr[E[i].key / F->n + 1]++;
+    nnz++;
+    i = j + 1;
+  }
+  for (int i = 0; i < F->n; i++) F->rowptr[i + 1] += F->rowptr[i];
+  F->nnz = nnz;
+  free(E);
+  F->Ainv = (double *)malloc(sizeof(double) * (size_t)(F->n ? F->n : 1));
+  F->B = (double *)malloc(sizeof(double) * (size_t)(F->n ? F->n : 1));
+  F->Tinv = (double *)malloc(sizeof(double) * (size_t)(F->n ? F->n : 1));
+  for (int i = 0; i < F->n; i++) {
+    double D = 0.0;
+    for (int p = F->rowptr[i]; p < F->rowptr[i + 1]; p++) D = D + F->vals[p];
+    if (D == 0.0) {
+      F->Ainv[i] = 1.0;
+      F->B[i] = 0.0;
+    } else {
+      double t = pow(D, 2.0 / 3.0);
+      F->Ainv[i] = 1.0 / (1.0 + r * r / t);
+      F->B[i] = F->Ainv[i] * r * r / (t * D);
+    }
+    F->Tinv[i] = 1.0;
+  }
+  double *ones = (double *)malloc(sizeof(double) * (size_t)(F->n ? F->n : 1));
+  double *y = (double *)malloc(sizeof(double) * (size_t)(F->n ? F->n : 1));
+  for (int i = 0; i < F->n; i++) ones[i] = 1.0;
+  filter_horner(F, 0, 1, ones, y);
+  for (int i = 0; i < F->n; i++) F->Tinv[i] = (y[i] != 0.0) ? 1.0 / y[i] : 0.0;
+  free(ones);
+  free(y);
+  return F;
+}
+void oo_filter_sizes(oo_filter *F, int *out) {
+  out[0] = F->n;
+  out[1] = F->nnz;
+}
+void oo_filter_get_matrix(oo_filter *F, int *rowptr, int *cols, double *vals,
+                          double *Ainv, double *B, double *Tinv) {
+  memcpy(rowptr, F->rowptr, sizeof(int) * (size_t)(F->n + 1));
+  memcpy(cols, F->cols, sizeof(int) * (size_t)F->nnz);
+  memcpy(vals, F->vals, sizeof(double) * (size_t)F->nnz);
+  memcpy(Ainv, F->Ainv, sizeof(double) * (size_t)F->n);
+  memcpy(B, F->B, sizeof(double) * (size_t)F->n);
+  memcpy(Tinv, F->Tinv, sizeof(double) * (size_t)F->n);
+}
+void oo_filter_apply(oo_filter *F, int vpn, const double *in, double *out) {
+  filter_horner(F, 0, vpn, in, out);
+}
+void oo_filter_apply_t(oo_filter *F, int vpn, const double *in, double *out) {
+  filter_horner(F, 1, vpn, in, out);
+}
+void oo_filter_destroy(oo_filter *F) {
+  if (!F) return;
+  free(F->rowptr);
+  free(F->cols);
+  free(F->vals);
+  free(F->Ainv);
+  free(F->B);
+  free(F->Tinv);
+  free(F);
+}

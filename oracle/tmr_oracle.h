@@ -78,8 +78,7 @@ void oo_csr_mult_wt(int n_rows, int n_cols, const int *rowptr,
 
 /* Matrix density filter (TMRMatrixFilter.cpp:30-235), restated. */
 typedef struct oo_filter oo_filter;
-oo_filter *oo_filter_create(oo_forest *f, const double *block_origin,
-                            double block_len, double r, int N);
+oo_filter *oo_filter_create(oo_forest *f, double block_len, double r, int N);
 void oo_filter_sizes(oo_filter *F, int *out2); /* {n, nnz} */
 void oo_filter_get_matrix(oo_filter *F, int *rowptr, int *cols, double *vals,
                           double *Ainv, double *B, double *Tinv);

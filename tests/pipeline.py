@@ -1,0 +1,142 @@
+"""Runs one adaptation pipeline (createTrees -> refine/balance passes ->
+createNodes -> coarsen/balance/createNodes/createInterpolation per level)
+on the GPU library or on a CPU checker, and returns every product as
+numpy arrays so the two can be compared."""
+import numpy as np
+
+from tmr_gb300 import workloads as W
+
+RTOL = 1e-13  # FP64 tolerance for weights and applies (relative)
+
+
+def indicator(octs, case, p):
+    if case.get("indicator", "random") == "sphere":
+        return W.sphere_indicator(octs)
+    return W.random_indicator(len(octs), case.get("seed", 0), p, case.get("prob", 0.3))
+
+
+def _csr_from_records(rows, ptr, cols, w, nrows):
+    from oracle.oracle import interp_to_csr
+    return interp_to_csr(rows, ptr, cols, w, nrows)
+
+
+def run_gpu(case):
+    from tmr_gb300 import TMR
+    order = case["order"]
+    f = TMR.OctForest(order=order, interp=case.get("interp", TMR.GAUSS_LOBATTO_POINTS))
+    f.setConnectivity(case["conn"])
+    f.createTrees(case["L0"])
+    for p in range(case["passes"]):
+        o = f.getOctantsArray()
+        f.refine(indicator(o, case, p), 0, case["max_level"])
+        f.balance(case.get("corner", 1))
+    f.createNodes()
+    out = dict(oct=f.getOctantsArray(), conn=f.getMeshConn(),
+               nn=f.getNodeNumbers(), dep=f.getDepNodeConn(),
+               sizes=_gpu_sizes(f), levels=[])
+    c = f
+    forests = [f]
+    for _ in range(case.get("coarse_levels", 1)):
+        cc = c.coarsen()
+        cc.balance(case.get("corner", 1))
+        cc.createNodes()
+        I = TMR.VecInterp()
+        c.createInterpolation(cc, I)
+        out["levels"].append(dict(oct=cc.getOctantsArray(), conn=cc.getMeshConn(),
+                                  P=I.getCSR(), I=I))
+        forests.append(cc)
+        c = cc
+    out["forests"] = forests
+    return out
+
+
+def _gpu_sizes(f):
+    s = f._sizes()
+    return dict(num_local=int(s[0]), num_owned=int(s[1]), num_dep=int(s[2]),
+                ext_pre=int(s[3]), num_elements=int(s[4]), dep_nnz=int(s[5]))
+
+
+def run_cpu(case, kind="oracle"):
+    from oracle.oracle import OracleForest, RefForest
+    cls = OracleForest if kind == "oracle" else RefForest
+    order = case["order"]
+    f = cls(order, case.get("interp", 1))
+    f.setConnectivity(case["conn"])
+    f.createTrees(case["L0"])
+    for p in range(case["passes"]):
+        o = f.getOctants()
+        f.refine(indicator(o, case, p), 0, case["max_level"])
+        f.balance(case.get("corner", 1))
+    f.createNodes()
+    out = dict(oct=f.getOctants(), conn=f.getMeshConn(order), nn=f.getNodeNumbers(),
+               dep=f.getDepNodeConn(), sizes=f.nodeSizes(), levels=[])
+    c = f
+    for _ in range(case.get("coarse_levels", 1)):
+        cc = c.coarsen()
+        cc.balance(case.get("corner", 1))
+        cc.createNodes()
+        rows, ptr, cols, w = c.createInterpolation(cc)
+        P = _csr_from_records(rows, ptr, cols, w, c.nodeSizes()["num_owned"])
+        out["levels"].append(dict(oct=cc.getOctants(), conn=cc.getMeshConn(order), P=P))
+        c = cc
+    return out
+
+
+def compare(a, b):
+    """List of mismatch descriptions (empty when a and b agree: integers
+    exactly, floating point within RTOL)."""
+    bad = []
+
+    def ints(name, x, y):
+        x, y = np.asarray(x), np.asarray(y)
+        if x.shape != y.shape:
+            bad.append("%s: shape %s vs %s" % (name, x.shape, y.shape))
+        elif not np.array_equal(x, y):
+            i = np.argwhere(x != y)[0]
+            bad.append("%s: first difference at %s: %s vs %s" % (
+                name, tuple(i), x[tuple(i)], y[tuple(i)]))
+
+    def fps(name, x, y):
+        x, y = np.asarray(x), np.asarray(y)
+        if x.shape != y.shape:
+            bad.append("%s: shape %s vs %s" % (name, x.shape, y.shape))
+        elif x.size and not np.allclose(x, y, rtol=RTOL, atol=RTOL * max(1.0, np.abs(y).max())):
+            bad.append("%s: max abs diff %g" % (name, np.abs(x - y).max()))
+
+    ints("octants", a["oct"], b["oct"])
+    if a["sizes"] != b["sizes"]:
+        bad.append("sizes %s vs %s" % (a["sizes"], b["sizes"]))
+    ints("conn", a["conn"], b["conn"])
+    ints("node_numbers", a["nn"], b["nn"])
+    ints("dep_ptr", a["dep"][0], b["dep"][0])
+    ints("dep_conn", a["dep"][1], b["dep"][1])
+    fps("dep_weights", a["dep"][2], b["dep"][2])
+    for k, (la, lb) in enumerate(zip(a["levels"], b["levels"])):
+        ints("L%d octants" % k, la["oct"], lb["oct"])
+        ints("L%d conn" % k, la["conn"], lb["conn"])
+        ints("L%d P rowptr" % k, la["P"][0], lb["P"][0])
+        ints("L%d P cols" % k, la["P"][1], lb["P"][1])
+        fps("L%d P vals" % k, la["P"][2], lb["P"][2])
+    return bad
+
+
+# Parity cases, small enough for the checker to finish in seconds.
+def cases():
+    return {
+        "c1_small": dict(conn=W.brick(1, 1, 1), order=2, L0=3, passes=3, max_level=6,
+                         indicator="sphere"),
+        "brick_o2": dict(conn=W.brick(3, 2, 2), order=2, L0=1, passes=3, max_level=6,
+                         prob=0.3, seed=7, coarse_levels=2),
+        "brick_o3": dict(conn=W.brick(3, 2, 2), order=3, L0=1, passes=3, max_level=5,
+                         prob=0.3, seed=7, coarse_levels=2),
+        "rot_o2": dict(conn=W.rotate_blocks(W.brick(3, 3, 2), 1), order=2, L0=1, passes=3,
+                       max_level=5, prob=0.3, seed=3),
+        "rot_o3": dict(conn=W.rotate_blocks(W.brick(2, 2, 2), 2), order=3, L0=1, passes=3,
+                       max_level=5, prob=0.3, seed=4, coarse_levels=2),
+        "rot_o4": dict(conn=W.rotate_blocks(W.brick(2, 2, 1), 5), order=4, L0=1, passes=2,
+                       max_level=4, prob=0.3, seed=5, coarse_levels=0),
+        "nocorner": dict(conn=W.rotate_blocks(W.brick(2, 2, 2), 6), order=2, L0=1, passes=3,
+                         max_level=5, prob=0.3, seed=6, corner=0),
+        "uniform_o3": dict(conn=W.brick(2, 1, 1), order=3, L0=2, passes=1, max_level=3,
+                           prob=1.0, seed=1, interp=0),
+    }

@@ -1,0 +1,126 @@
+"""Matrix density filter on the GPU vs the CPU restatement, plus the
+identities the reference documents (F 1 = 1, TMRMatrixFilter.h:48-49) and
+the exactness of the hand-written adjoint."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from tests import pipeline
+
+R_FILTER = 0.08
+N_TERMS = 10
+
+
+def _oracle_filter(case):
+    from oracle.oracle import OracleForest, _lib
+    L = _lib("oracle").lib
+    L.oo_filter_create.restype = ctypes.c_void_p
+    L.oo_filter_create.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int]
+    f = OracleForest(case["order"], 1)
+    f.setConnectivity(case["conn"])
+    f.createTrees(case["L0"])
+    for p in range(case["passes"]):
+        o = f.getOctants()
+        f.refine(pipeline.indicator(o, case, p), 0, case["max_level"])
+        f.balance(1)
+    f.createNodes()
+    F = L.oo_filter_create(ctypes.c_void_p(f.h), 1.0, R_FILTER, N_TERMS)
+    return f, F, L
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["brick_o2", "rot_o2", "c1_small"])
+def test_filter_matches_oracle(gpu_lib, name):
+    import torch
+
+    from tmr_gb300 import TMR
+    case = pipeline.cases()[name]
+    g = pipeline.run_gpu(dict(case, coarse_levels=0))
+    F = TMR.MatrixFilter(R_FILTER, N_TERMS, None, [g["forests"][0]])
+    of, OF, L = _oracle_filter(case)
+    s = np.zeros(2, np.intc)
+    L.oo_filter_sizes(ctypes.c_void_p(OF), _p(s))
+    n, nnz = F.size()
+    assert (n, nnz) == (s[0], s[1])
+    rp, cols, vals, A, B, T = F.getMatrix()
+    orp = np.zeros(n + 1, np.intc)
+    oc = np.zeros(nnz, np.intc)
+    ov = np.zeros(nnz)
+    oA, oB, oT = np.zeros(n), np.zeros(n), np.zeros(n)
+    L.oo_filter_get_matrix(ctypes.c_void_p(OF), _p(orp), _p(oc), _p(ov), _p(oA), _p(oB), _p(oT))
+    np.testing.assert_array_equal(rp, orp)
+    np.testing.assert_array_equal(cols, oc)
+    np.testing.assert_allclose(vals, ov, rtol=1e-13)
+    np.testing.assert_allclose(A, oA, rtol=1e-13)
+    np.testing.assert_allclose(B, oB, rtol=1e-13)
+    np.testing.assert_allclose(T, oT, rtol=1e-13)
+    # forward and adjoint on 3 interleaved components
+    vpn = 3
+    rng = np.random.default_rng(3)
+    x = rng.random(n * vpn)
+    y = np.zeros(n * vpn)
+    F.applyFilter(x, y, vpn)
+    yo = np.zeros(n * vpn)
+    L.oo_filter_apply(ctypes.c_void_p(OF), vpn, _p(x), _p(yo))
+    np.testing.assert_allclose(y, yo, rtol=1e-13, atol=1e-15)
+    yt = np.zeros(n * vpn)
+    F.applyTranspose(x, yt, vpn)
+    yto = np.zeros(n * vpn)
+    L.oo_filter_apply_t(ctypes.c_void_p(OF), vpn, _p(x), _p(yto))
+    np.testing.assert_allclose(yt, yto, rtol=1e-13, atol=1e-15)
+    # F 1 = 1 and <F x, z> = <x, F^T z>
+    one = np.ones(n)
+    f1 = np.zeros(n)
+    F.applyFilter(one, f1, 1)
+    np.testing.assert_allclose(f1, 1.0, rtol=1e-12)
+    z = rng.standard_normal(n * vpn)
+    fz = np.zeros(n * vpn)
+    F.applyTranspose(z, fz, vpn)
+    assert abs(np.dot(y, z) - np.dot(x, fz)) <= 1e-11 * np.abs(np.dot(y, z))
+    # FP32 variant against FP64 (error stated, not a parity claim)
+    xd = torch.tensor(x, dtype=torch.float32, device="cuda")
+    yd = torch.empty_like(xd)
+    F.applyFilter(xd, yd, vpn)
+    err32 = np.abs(yd.cpu().numpy() - y).max() / np.abs(y).max()
+    assert err32 < 1e-5, err32
+    L.oo_filter_destroy(ctypes.c_void_p(OF))
+
+
+@pytest.mark.gpu
+def test_filter_interp_autograd_matches_fd(gpu_lib):
+    import torch
+
+    from tmr_gb300 import TMR
+    from tmr_gb300.autograd import filter_interp
+    case = pipeline.cases()["brick_o2"]
+    g = pipeline.run_gpu(dict(case, coarse_levels=1))
+    fine, coarse = g["forests"][0], g["forests"][1]
+    F = TMR.MatrixFilter(R_FILTER, N_TERMS, None, [coarse])
+    I = g["levels"][0]["I"]
+    n, _ = F.size()
+    rows, cols, _ = I.sizes()
+    assert cols == n
+    vpn = 1
+    gen = torch.Generator(device="cpu").manual_seed(5)
+    x = torch.rand(n * vpn, generator=gen, dtype=torch.float64).cuda().requires_grad_(True)
+    w = torch.rand(rows * vpn, generator=gen, dtype=torch.float64).cuda()
+
+    def obj(v):
+        rho = filter_interp(v, F, I, vpn)
+        return (w * rho ** 3).sum()
+
+    J = obj(x)
+    J.backward()
+    gx = x.grad.detach()
+    h = 1e-6
+    for k in range(20):
+        d = torch.randn(n * vpn, generator=gen, dtype=torch.float64).cuda()
+        with torch.no_grad():
+            fd = (obj(x + h * d) - obj(x - h * d)) / (2 * h)
+        an = torch.dot(gx, d)
+        assert abs(fd.item() - an.item()) <= 1e-6 * max(1.0, abs(an.item())), (k, fd.item(), an.item())

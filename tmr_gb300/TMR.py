@@ -1,0 +1,422 @@
+"""Drop-in for the octree part of the ``tmr.TMR`` Cython module.
+
+Same class and method names as TMR.pyx (OctForest :3393-3790, Octant and
+OctantArray :3270-3392, VecInterp, MatrixFilter :4660-5039), backed by the
+GPU library through its C ABI.  ``comm`` is accepted and ignored: one GPU
+holds the whole forest (the reference's single-rank behaviour).
+
+Vectors passed to VecInterp / MatrixFilter may be numpy arrays (host
+buffers, copied in and out) or CUDA torch tensors (used in place).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import call, lib
+
+UNIFORM_POINTS = 0
+GAUSS_LOBATTO_POINTS = 1
+BERNSTEIN_POINTS = 2
+MAX_LEVEL = 30
+
+_vp = ctypes.c_void_p
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_vp)
+
+
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")
+
+
+class Octant:
+    """TMROctant value (TMROctant.h:36-54)."""
+
+    __slots__ = ("block", "x", "y", "z", "tag", "level", "info")
+
+    def __init__(self, block=0, x=0, y=0, z=0, tag=0, level=0, info=0):
+        self.block, self.x, self.y, self.z = block, x, y, z
+        self.tag, self.level, self.info = tag, level, info
+
+    def __repr__(self):
+        return "Octant(block=%d, x=%d, y=%d, z=%d, tag=%d, level=%d, info=%d)" % (
+            self.block, self.x, self.y, self.z, self.tag, self.level, self.info)
+
+
+class OctantArray:
+    """Host snapshot of a forest's octants (TMR.pyx:3270-3330)."""
+
+    def __init__(self, arr7):
+        self.array = arr7  # (n, 7) int32 {block, x, y, z, tag, level, info}
+
+    def __len__(self):
+        return self.array.shape[0]
+
+    def __getitem__(self, k):
+        n = len(self)
+        if k < 0 or k >= n:
+            raise IndexError("Octant array index %d out of range [0,%d)" % (k, n))
+        r = self.array[k]
+        return Octant(int(r[0]), int(r[1]), int(r[2]), int(r[3]), int(r[4]),
+                      int(r[5]), int(r[6]))
+
+    def __setitem__(self, k, oc):
+        n = len(self)
+        if k < 0 or k >= n:
+            raise IndexError("Octant array index %d out of range [0,%d)" % (k, n))
+        self.array[k] = [oc.block, oc.x, oc.y, oc.z, oc.tag, oc.level, oc.info]
+
+
+class OctForest:
+    """Forest of octrees on one GPU (TMROctForest, TMR.pyx:3393-3790)."""
+
+    def __init__(self, comm=None, order=2, interp=GAUSS_LOBATTO_POINTS, stream=None,
+                 _handle=None):
+        self.comm = comm
+        self._stream = stream
+        if _handle is not None:
+            self.ptr = _handle
+        else:
+            h = _vp()
+            call("tmrg_forest_create", order, interp, _vp(self._stream_ptr()),
+                 ctypes.byref(h))
+            self.ptr = h
+
+    def _stream_ptr(self):
+        s = self._stream
+        if s is None:
+            return None
+        return s.cuda_stream if hasattr(s, "cuda_stream") else int(s)
+
+    def __del__(self):
+        try:
+            if getattr(self, "ptr", None):
+                lib().tmrg_forest_destroy(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+    # -- configuration -------------------------------------------------
+    def setMeshOrder(self, order, interp=GAUSS_LOBATTO_POINTS):
+        call("tmrg_forest_set_mesh_order", self.ptr, order, interp)
+
+    def getMeshOrder(self):
+        o = ctypes.c_int()
+        call("tmrg_forest_get_mesh_order", self.ptr, ctypes.byref(o), None)
+        return o.value
+
+    def getInterpType(self):
+        t = ctypes.c_int()
+        call("tmrg_forest_get_mesh_order", self.ptr, None, ctypes.byref(t))
+        return t.value
+
+    def getInterpKnots(self):
+        k = np.zeros(self.getMeshOrder(), np.float64)
+        call("tmrg_forest_get_interp_knots", self.ptr, _ptr(k))
+        return k
+
+    def setConnectivity(self, conn):
+        conn = np.ascontiguousarray(conn, dtype=np.intc)
+        if conn.ndim != 2 or conn.shape[1] != 8:
+            raise ValueError("Expected array of shape (n, 8)")
+        num_nodes = int(conn.max()) + 1
+        call("tmrg_forest_set_connectivity", self.ptr, num_nodes, _ptr(conn),
+             conn.shape[0])
+
+    def repartition(self, max_rank=-1):
+        call("tmrg_forest_repartition", self.ptr, max_rank)
+
+    # -- octants -------------------------------------------------------
+    def createTrees(self, depth=0):
+        call("tmrg_forest_create_trees", self.ptr, depth)
+
+    def refine(self, refine=None, min_lev=0, max_lev=MAX_LEVEL):
+        if refine is None:
+            call("tmrg_forest_refine", self.ptr, None, 0, min_lev, max_lev)
+        elif _is_torch(refine) and refine.is_cuda:
+            import torch
+            r = refine.to(torch.int32).contiguous()
+            call("tmrg_forest_refine_device", self.ptr, _vp(r.data_ptr()), r.numel(),
+                 min_lev, max_lev)
+        else:
+            r = np.ascontiguousarray(refine, dtype=np.intc)
+            call("tmrg_forest_refine", self.ptr, _ptr(r), r.size, min_lev, max_lev)
+
+    def duplicate(self):
+        h = _vp()
+        call("tmrg_forest_duplicate", self.ptr, ctypes.byref(h))
+        return OctForest(self.comm, stream=self._stream, _handle=h)
+
+    def coarsen(self):
+        h = _vp()
+        call("tmrg_forest_coarsen", self.ptr, ctypes.byref(h))
+        return OctForest(self.comm, stream=self._stream, _handle=h)
+
+    def balance(self, btype=0):
+        call("tmrg_forest_balance", self.ptr, btype)
+
+    def createNodes(self):
+        call("tmrg_forest_create_nodes", self.ptr)
+
+    def getNumOctants(self):
+        n = ctypes.c_int64()
+        call("tmrg_forest_num_octants", self.ptr, ctypes.byref(n))
+        return n.value
+
+    def getOctantsArray(self):
+        """(n, 7) int32 array {block, x, y, z, tag, level, info}."""
+        n = self.getNumOctants()
+        out = np.zeros((n, 7), np.intc)
+        if n:
+            call("tmrg_forest_get_octants", self.ptr, _ptr(out), n)
+        return out
+
+    def getOctants(self):
+        return OctantArray(self.getOctantsArray())
+
+    # -- nodes ---------------------------------------------------------
+    def _sizes(self):
+        s = np.zeros(6, np.int64)
+        call("tmrg_forest_node_sizes", self.ptr, _ptr(s))
+        return s
+
+    def getNodeRange(self):
+        return np.array([0, self._sizes()[1]], dtype=np.intc)
+
+    def getExtPreOffset(self):
+        return int(self._sizes()[3])
+
+    def getMeshConn(self):
+        s = self._sizes()
+        o = self.getMeshOrder()
+        n = int(s[4]) * o ** 3
+        out = np.zeros(n, np.intc)
+        if n:
+            call("tmrg_forest_get_node_conn", self.ptr, _ptr(out), n)
+        return out.reshape(int(s[4]), o ** 3)
+
+    def getNodeNumbers(self):
+        s = self._sizes()
+        out = np.zeros(int(s[0]), np.intc)
+        if out.size:
+            call("tmrg_forest_get_node_numbers", self.ptr, _ptr(out), out.size)
+        return out
+
+    def getDepNodeConn(self):
+        s = self._sizes()
+        ndep, nnz = int(s[2]), int(s[5])
+        ptr = np.zeros(ndep + 1, np.intc)
+        conn = np.zeros(max(nnz, 1), np.intc)
+        w = np.zeros(max(nnz, 1), np.float64)
+        call("tmrg_forest_get_dep_node_conn", self.ptr, _ptr(ptr), _ptr(conn), _ptr(w))
+        return ptr, conn[:nnz], w[:nnz]
+
+    def createInterpolation(self, forest, vec):
+        if forest.ptr.value == self.ptr.value:
+            raise ValueError("Cannot interpolate between the same object")
+        vec._create(self, forest)
+
+    def writeToVTK(self, fname):
+        """Legacy-VTK unstructured grid of the octants (one hexahedron each,
+        block-local integer coordinates)."""
+        o = self.getOctantsArray()
+        h = (1 << (30 - o[:, 5].astype(np.int64)))
+        with open(fname, "w") as fp:
+            fp.write("# vtk DataFile Version 3.0\ntmr_gb300 forest\nASCII\n")
+            fp.write("DATASET UNSTRUCTURED_GRID\nPOINTS %d double\n" % (8 * len(o)))
+            for r, hh in zip(o, h):
+                for c in (0, 1, 3, 2, 4, 5, 7, 6):
+                    fp.write("%g %g %g\n" % ((r[1] + hh * (c & 1)) / 2.0 ** 30 + r[0],
+                                             (r[2] + hh * ((c >> 1) & 1)) / 2.0 ** 30,
+                                             (r[3] + hh * (c >> 2)) / 2.0 ** 30))
+            fp.write("CELLS %d %d\n" % (len(o), 9 * len(o)))
+            for i in range(len(o)):
+                fp.write("8 " + " ".join(str(8 * i + k) for k in range(8)) + "\n")
+            fp.write("CELL_TYPES %d\n" % len(o))
+            fp.write("12\n" * len(o))
+
+
+class VecInterp:
+    """Prolongation operator P (fine rows x coarse columns); the TACS
+    TACSBVecInterp role in TMR (createInterpolation target)."""
+
+    def __init__(self):
+        self.ptr = None
+
+    def _create(self, fine, coarse):
+        h = _vp()
+        call("tmrg_interp_create", fine.ptr, coarse.ptr, ctypes.byref(h))
+        self.ptr = h
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                lib().tmrg_interp_destroy(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+    def sizes(self):
+        s = np.zeros(3, np.int64)
+        call("tmrg_interp_sizes", self.ptr, _ptr(s))
+        return int(s[0]), int(s[1]), int(s[2])
+
+    def getCSR(self):
+        rows, cols, nnz = self.sizes()
+        rp = np.zeros(rows + 1, np.intc)
+        c = np.zeros(max(nnz, 1), np.intc)
+        w = np.zeros(max(nnz, 1), np.float64)
+        call("tmrg_interp_get_csr", self.ptr, _ptr(rp), _ptr(c), _ptr(w))
+        return rp, c[:nnz], w[:nnz]
+
+    def _apply(self, which, x, y):
+        names = ("tmrg_interp_mult", "tmrg_interp_mult_transpose",
+                 "tmrg_interp_mult_weight_transpose")
+        rows, cols, _ = self.sizes()
+        nin = cols if which == 0 else rows
+        if _is_torch(x):
+            nvec = x.numel() // max(nin, 1)
+            call(names[which] + "_device", self.ptr, _vp(x.data_ptr()),
+                 _vp(y.data_ptr()), nvec)
+        else:
+            x = np.ascontiguousarray(x, dtype=np.float64)
+            nvec = x.size // max(nin, 1)
+            out = np.zeros(y.shape, np.float64)
+            call(names[which], self.ptr, _ptr(x), _ptr(out), nvec)
+            y[...] = out
+        return y
+
+    def mult(self, x, y):
+        return self._apply(0, x, y)
+
+    def multTranspose(self, x, y):
+        return self._apply(1, x, y)
+
+    def multWeightTranspose(self, x, y):
+        return self._apply(2, x, y)
+
+
+class MatrixFilter:
+    """Matrix density filter (TMRMatrixFilter, TMR.pyx MatrixFilter).
+
+    ``MatrixFilter(r, N, assemblers, filters)`` as in the reference; the
+    assemblers are ignored (no TACS) and the filter is built on
+    ``filters[0]``, whose blocks are cubes of side ``block_len``.  The
+    remaining forests form the restriction hierarchy used by
+    ``setDesignVars`` (TMRConformFilter.cpp:75-91).
+    """
+
+    def __init__(self, r, N, assemblers=None, filters=None, block_len=1.0, vpn=1):
+        self.filters = list(filters)
+        self.vpn = vpn
+        h = _vp()
+        call("tmrg_filter_create", self.filters[0].ptr, float(block_len), float(r),
+             int(N), ctypes.byref(h))
+        self.ptr = h
+        self.interps = []
+        for k in range(len(self.filters) - 1):
+            I = VecInterp()
+            self.filters[k].createInterpolation(self.filters[k + 1], I)
+            self.interps.append(I)
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                lib().tmrg_filter_destroy(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+    def size(self):
+        s = np.zeros(2, np.int64)
+        call("tmrg_filter_sizes", self.ptr, _ptr(s))
+        return int(s[0]), int(s[1])
+
+    def getMatrix(self):
+        n, nnz = self.size()
+        rp = np.zeros(n + 1, np.intc)
+        c = np.zeros(max(nnz, 1), np.intc)
+        v = np.zeros(max(nnz, 1), np.float64)
+        A = np.zeros(n, np.float64)
+        B = np.zeros(n, np.float64)
+        T = np.zeros(n, np.float64)
+        call("tmrg_filter_get_matrix", self.ptr, _ptr(rp), _ptr(c), _ptr(v), _ptr(A),
+             _ptr(B), _ptr(T))
+        return rp, c[:nnz], v[:nnz], A, B, T
+
+    def _apply(self, transpose, x, y, vpn=None):
+        vpn = vpn or self.vpn
+        if _is_torch(x):
+            import torch
+            if x.dtype == torch.float32:
+                name = "tmrg_filter_apply_transpose_f32_device" if transpose else \
+                    "tmrg_filter_apply_f32_device"
+            else:
+                name = "tmrg_filter_apply_transpose_device" if transpose else \
+                    "tmrg_filter_apply_device"
+            call(name, self.ptr, vpn, _vp(x.data_ptr()), _vp(y.data_ptr()))
+        else:
+            x = np.ascontiguousarray(x, dtype=np.float64)
+            out = np.zeros(x.shape, np.float64)
+            name = "tmrg_filter_apply_transpose" if transpose else "tmrg_filter_apply"
+            call(name, self.ptr, vpn, _ptr(x), _ptr(out))
+            y[...] = out
+        return y
+
+    def applyFilter(self, x, y, vpn=None):
+        return self._apply(False, x, y, vpn)
+
+    def applyTranspose(self, x, y, vpn=None):
+        return self._apply(True, x, y, vpn)
+
+    def setDesignVars(self, x):
+        """Filter x on the finest filter level and restrict it down the
+        hierarchy with the weight-normalised transpose
+        (TMRMatrixFilter.cpp:272-320).  Returns the per-level vectors."""
+        levels = [self._apply(False, x, _like(x))]
+        for I in self.interps:
+            rows, cols, _ = I.sizes()
+            out = _zeros_like(x, cols * self.vpn)
+            I.multWeightTranspose(levels[-1], out)
+            levels.append(out)
+        return levels
+
+    def addValues(self, g):
+        """Gradient with respect to the unfiltered design variables
+        (TMRMatrixFilter.cpp:325-368)."""
+        return self._apply(True, g, _like(g))
+
+
+def _like(x):
+    if _is_torch(x):
+        import torch
+        return torch.empty_like(x)
+    return np.zeros_like(x)
+
+
+def _zeros_like(x, n):
+    if _is_torch(x):
+        import torch
+        return torch.zeros(n, dtype=x.dtype, device=x.device)
+    return np.zeros(n, dtype=np.float64)
+
+
+def kernel_launch_count():
+    return int(lib().tmrg_kernel_launch_count())
+
+
+def version():
+    return lib().tmrg_version().decode()
+
+
+def random_refinement(n, seed, stream, prob, device="cuda"):
+    """Seeded 0/1 refinement indicator on the GPU (the synthetic
+    workloads' U(seed, stream, i) < prob)."""
+    import torch
+    out = torch.empty(n, dtype=torch.int32, device=device)
+    cs = torch.cuda.current_stream().cuda_stream
+    call("tmrg_random_refinement_device", int(seed), int(stream), float(prob),
+         _vp(out.data_ptr()), n, _vp(cs))
+    return out

@@ -1,0 +1,113 @@
+"""ctypes binding of the native library ``libtmrg.so`` (C ABI in include/tmrg.h).
+
+The library is the only compute path: if it has not been built this module
+raises on first use rather than falling back to anything else.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libtmrg.so")
+
+c_int = ctypes.c_int
+c_i64 = ctypes.c_int64
+c_u64 = ctypes.c_uint64
+c_dbl = ctypes.c_double
+c_vp = ctypes.c_void_p
+P = ctypes.POINTER
+
+# name -> argtypes (all return int status unless listed in _RESTYPE)
+_SIGS = {
+    "tmrg_last_error": [],
+    "tmrg_version": [],
+    "tmrg_kernel_launch_count": [],
+    "tmrg_forest_create": [c_int, c_int, c_vp, P(c_vp)],
+    "tmrg_forest_destroy": [c_vp],
+    "tmrg_forest_set_connectivity": [c_vp, c_int, c_vp, c_int],
+    "tmrg_forest_set_mesh_order": [c_vp, c_int, c_int],
+    "tmrg_forest_get_mesh_order": [c_vp, P(c_int), P(c_int)],
+    "tmrg_forest_get_interp_knots": [c_vp, c_vp],
+    "tmrg_forest_create_trees": [c_vp, c_int],
+    "tmrg_forest_refine": [c_vp, c_vp, c_i64, c_int, c_int],
+    "tmrg_forest_refine_device": [c_vp, c_vp, c_i64, c_int, c_int],
+    "tmrg_forest_coarsen": [c_vp, P(c_vp)],
+    "tmrg_forest_duplicate": [c_vp, P(c_vp)],
+    "tmrg_forest_balance": [c_vp, c_int],
+    "tmrg_forest_repartition": [c_vp, c_int],
+    "tmrg_forest_create_nodes": [c_vp],
+    "tmrg_forest_num_octants": [c_vp, P(c_i64)],
+    "tmrg_forest_get_octants": [c_vp, c_vp, c_i64],
+    "tmrg_forest_octants_device": [c_vp, P(c_vp), P(c_vp), P(c_vp), P(c_vp), P(c_vp), P(c_vp)],
+    "tmrg_forest_node_sizes": [c_vp, c_vp],
+    "tmrg_forest_get_node_conn": [c_vp, c_vp, c_i64],
+    "tmrg_forest_get_node_numbers": [c_vp, c_vp, c_i64],
+    "tmrg_forest_get_dep_node_conn": [c_vp, c_vp, c_vp, c_vp],
+    "tmrg_forest_node_conn_device": [c_vp, P(c_vp)],
+    "tmrg_forest_dep_node_conn_device": [c_vp, P(c_vp), P(c_vp), P(c_vp)],
+    "tmrg_interp_create": [c_vp, c_vp, P(c_vp)],
+    "tmrg_interp_destroy": [c_vp],
+    "tmrg_interp_sizes": [c_vp, c_vp],
+    "tmrg_interp_get_csr": [c_vp, c_vp, c_vp, c_vp],
+    "tmrg_interp_mult": [c_vp, c_vp, c_vp, c_int],
+    "tmrg_interp_mult_transpose": [c_vp, c_vp, c_vp, c_int],
+    "tmrg_interp_mult_weight_transpose": [c_vp, c_vp, c_vp, c_int],
+    "tmrg_interp_mult_device": [c_vp, c_vp, c_vp, c_int],
+    "tmrg_interp_mult_transpose_device": [c_vp, c_vp, c_vp, c_int],
+    "tmrg_interp_mult_weight_transpose_device": [c_vp, c_vp, c_vp, c_int],
+    "tmrg_filter_create": [c_vp, c_dbl, c_dbl, c_int, P(c_vp)],
+    "tmrg_filter_destroy": [c_vp],
+    "tmrg_filter_sizes": [c_vp, c_vp],
+    "tmrg_filter_get_matrix": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp],
+    "tmrg_filter_apply": [c_vp, c_int, c_vp, c_vp],
+    "tmrg_filter_apply_transpose": [c_vp, c_int, c_vp, c_vp],
+    "tmrg_filter_apply_device": [c_vp, c_int, c_vp, c_vp],
+    "tmrg_filter_apply_transpose_device": [c_vp, c_int, c_vp, c_vp],
+    "tmrg_filter_apply_f32_device": [c_vp, c_int, c_vp, c_vp],
+    "tmrg_filter_apply_transpose_f32_device": [c_vp, c_int, c_vp, c_vp],
+    "tmrg_random_refinement_device": [c_u64, c_u64, c_dbl, c_vp, c_i64, c_vp],
+}
+_RESTYPE = {
+    "tmrg_last_error": ctypes.c_char_p,
+    "tmrg_version": ctypes.c_char_p,
+    "tmrg_kernel_launch_count": c_i64,
+}
+
+STATUS = {
+    0: "TMRG_OK", 1: "TMRG_ERR_ARG", 2: "TMRG_ERR_STATE", 3: "TMRG_ERR_CUDA",
+    4: "TMRG_ERR_NOMEM", 5: "TMRG_ERR_KEY_RANGE", 6: "TMRG_ERR_UNSUPPORTED",
+    7: "TMRG_ERR_INTERNAL",
+}
+
+
+class TMRGError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    """Load libtmrg.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                "libtmrg.so is not built (%s); run tmr_gb300.build.build()" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = _RESTYPE.get(name, c_int)
+        _lib = L
+    return _lib
+
+
+def check(status):
+    if status != 0:
+        raise TMRGError(status, lib().tmrg_last_error().decode())
+
+
+def call(name, *args):
+    check(getattr(lib(), name)(*args))

@@ -1,0 +1,473 @@
+// The C ABI (include/tmrg.h): status codes in, exceptions never out.
+#include <string.h>
+
+#include <string>
+
+#include "tmrg_internal.h"
+
+using namespace tmrg;
+
+struct tmrg_forest {
+  Forest f;
+};
+struct tmrg_interp {
+  Interp I;
+};
+struct tmrg_filter {
+  Filter F;
+};
+
+static thread_local std::string g_last_error;
+
+template <typename Fn>
+static int guarded(Fn &&fn) {
+  try {
+    fn();
+    g_last_error.clear();
+    return TMRG_OK;
+  } catch (const Error &e) {
+    g_last_error = e.what();
+    return e.status;
+  } catch (const std::bad_alloc &) {
+    g_last_error = "host allocation failed";
+    return TMRG_ERR_NOMEM;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return TMRG_ERR_INTERNAL;
+  }
+}
+#define ARG(cond, msg)                                     \
+  do {                                                     \
+    if (!(cond)) throw Error(TMRG_ERR_ARG, std::string(msg)); \
+  } while (0)
+
+static void copy_d2h(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+  if (!bytes) return;
+  TMRG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+  TMRG_CUDA(cudaStreamSynchronize(s));
+}
+
+extern "C" {
+
+const char *tmrg_last_error(void) { return g_last_error.c_str(); }
+const char *tmrg_version(void) { return "tmr_gb300 0.1 (sm_103a)"; }
+int64_t tmrg_kernel_launch_count(void) { return g_kernel_launches.load(); }
+
+int tmrg_forest_create(int order, int interp_type, void *stream,
+                       tmrg_forest **out) {
+  return guarded([&] {
+    ARG(out, "out is NULL");
+    ARG(interp_type >= 0 && interp_type <= 2, "bad interpolation type");
+    auto *h = new tmrg_forest;
+    h->f.s = (cudaStream_t)stream;
+    h->f.set_order(order, interp_type);
+    *out = h;
+  });
+}
+int tmrg_forest_destroy(tmrg_forest *f) {
+  return guarded([&] {
+    if (!f) return;
+    cudaStreamSynchronize(f->f.s);
+    delete f;
+  });
+}
+int tmrg_forest_set_connectivity(tmrg_forest *f, int num_nodes,
+                                 const int *block_conn, int num_blocks) {
+  return guarded([&] {
+    ARG(f && block_conn, "NULL argument");
+    f->f.free_nodes();
+    f->f.have_octs = false;
+    f->f.n = 0;
+    f->f.conn = build_conn(num_nodes, block_conn, num_blocks, f->f.s);
+  });
+}
+int tmrg_forest_set_mesh_order(tmrg_forest *f, int order, int interp_type) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    ARG(interp_type >= 0 && interp_type <= 2, "bad interpolation type");
+    f->f.set_order(order, interp_type);
+  });
+}
+int tmrg_forest_get_mesh_order(tmrg_forest *f, int *order, int *interp_type) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    if (order) *order = f->f.order;
+    if (interp_type) *interp_type = f->f.interp;
+  });
+}
+int tmrg_forest_get_interp_knots(tmrg_forest *f, double *knots) {
+  return guarded([&] {
+    ARG(f && knots, "NULL argument");
+    memcpy(knots, f->f.knots, sizeof(double) * f->f.order);
+  });
+}
+int tmrg_forest_create_trees(tmrg_forest *f, int level) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    forest_create_trees(f->f, level);
+  });
+}
+int tmrg_forest_refine(tmrg_forest *f, const int *refinement, int64_t n,
+                       int min_level, int max_level) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    if (!refinement) {
+      forest_refine(f->f, nullptr, 0, min_level, max_level);
+      return;
+    }
+    if (!f->f.have_octs) throw Error(TMRG_ERR_STATE, "refine: no octants");
+    ARG(n == f->f.n, "refine: refinement array length != number of octants");
+    DBuf<int> d(n, f->f.s);
+    if (n)
+      TMRG_CUDA(cudaMemcpyAsync(d.p, refinement, n * sizeof(int),
+                                cudaMemcpyHostToDevice, f->f.s));
+    forest_refine(f->f, d.p, n, min_level, max_level);
+  });
+}
+int tmrg_forest_refine_device(tmrg_forest *f, const int *d_refinement,
+                              int64_t n, int min_level, int max_level) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    forest_refine(f->f, d_refinement, d_refinement ? n : 0, min_level,
+                  max_level);
+  });
+}
+int tmrg_forest_coarsen(tmrg_forest *f, tmrg_forest **out) {
+  return guarded([&] {
+    ARG(f && out, "NULL argument");
+    auto *h = new tmrg_forest;
+    h->f.s = f->f.s;
+    try {
+      forest_coarsen(f->f, h->f);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+int tmrg_forest_duplicate(tmrg_forest *f, tmrg_forest **out) {
+  return guarded([&] {
+    ARG(f && out, "NULL argument");
+    auto *h = new tmrg_forest;
+    h->f.s = f->f.s;
+    try {
+      forest_duplicate(f->f, h->f);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+int tmrg_forest_balance(tmrg_forest *f, int balance_corner) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    forest_balance(f->f, balance_corner ? 1 : 0);
+  });
+}
+int tmrg_forest_repartition(tmrg_forest *f, int) {
+  return guarded([&] { ARG(f, "NULL forest"); });
+}
+int tmrg_forest_create_nodes(tmrg_forest *f) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    forest_create_nodes(f->f);
+  });
+}
+int tmrg_forest_num_octants(tmrg_forest *f, int64_t *n) {
+  return guarded([&] {
+    ARG(f && n, "NULL argument");
+    *n = f->f.have_octs ? f->f.n : 0;
+  });
+}
+
+__global__ void k_pack_octants(long long n, const int *b, const int *x,
+                               const int *y, const int *z, const int16_t *l,
+                               const int16_t *info, int *out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int *o = out + 7 * i;
+  o[0] = b[i];
+  o[1] = x[i];
+  o[2] = y[i];
+  o[3] = z[i];
+  o[4] = (int)i;
+  o[5] = l[i];
+  o[6] = info[i];
+}
+
+int tmrg_forest_get_octants(tmrg_forest *f, int *out7, int64_t n) {
+  return guarded([&] {
+    ARG(f && out7, "NULL argument");
+    Forest &F = f->f;
+    if (!F.have_octs) throw Error(TMRG_ERR_STATE, "getOctants: no octants");
+    ARG(n == F.n, "getOctants: buffer length != number of octants");
+    DBuf<int> d(7 * (size_t)n, F.s);
+    launch(k_pack_octants, blocks_for(n, 256), 256, 0, F.s, (long long)n,
+           (const int *)F.block.p, (const int *)F.x.p, (const int *)F.y.p,
+           (const int *)F.z.p, (const int16_t *)F.level.p,
+           (const int16_t *)F.info.p, d.p);
+    copy_d2h(out7, d.p, 7 * sizeof(int) * (size_t)n, F.s);
+  });
+}
+int tmrg_forest_octants_device(tmrg_forest *f, const int **block, const int **x,
+                               const int **y, const int **z,
+                               const int16_t **level, const int16_t **info) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    Forest &F = f->f;
+    if (block) *block = F.block.p;
+    if (x) *x = F.x.p;
+    if (y) *y = F.y.p;
+    if (z) *z = F.z.p;
+    if (level) *level = F.level.p;
+    if (info) *info = F.info.p;
+  });
+}
+int tmrg_forest_node_sizes(tmrg_forest *f, int64_t out6[6]) {
+  return guarded([&] {
+    ARG(f && out6, "NULL argument");
+    Forest &F = f->f;
+    out6[0] = F.num_local;
+    out6[1] = F.num_owned;
+    out6[2] = F.num_dep;
+    out6[3] = F.ext_pre;
+    out6[4] = F.have_octs ? F.n : 0;
+    out6[5] = F.dep_nnz;
+  });
+}
+int tmrg_forest_get_node_conn(tmrg_forest *f, int *conn, int64_t n) {
+  return guarded([&] {
+    ARG(f && conn, "NULL argument");
+    Forest &F = f->f;
+    if (!F.have_nodes) throw Error(TMRG_ERR_STATE, "getNodeConn: no nodes");
+    long long m = F.n * (long long)F.order * F.order * F.order;
+    ARG(n == m, "getNodeConn: buffer length mismatch");
+    copy_d2h(conn, F.econn.p, sizeof(int) * (size_t)m, F.s);
+  });
+}
+int tmrg_forest_get_node_numbers(tmrg_forest *f, int *out, int64_t n) {
+  return guarded([&] {
+    ARG(f && out, "NULL argument");
+    Forest &F = f->f;
+    if (!F.have_nodes) throw Error(TMRG_ERR_STATE, "getNodeNumbers: no nodes");
+    ARG(n == F.num_local, "getNodeNumbers: buffer length mismatch");
+    // sorted: -num_dep .. -1, then 0 .. num_owned-1
+    for (long long i = 0; i < F.num_dep; i++) out[i] = (int)(i - F.num_dep);
+    for (long long i = 0; i < F.num_owned; i++) out[F.num_dep + i] = (int)i;
+  });
+}
+int tmrg_forest_get_dep_node_conn(tmrg_forest *f, int *ptr, int *conn,
+                                  double *weights) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    Forest &F = f->f;
+    if (!F.have_nodes) throw Error(TMRG_ERR_STATE, "getDepNodeConn: no nodes");
+    if (ptr) copy_d2h(ptr, F.dep_ptr.p, sizeof(int) * (F.num_dep + 1), F.s);
+    if (conn) copy_d2h(conn, F.dep_conn.p, sizeof(int) * F.dep_nnz, F.s);
+    if (weights) copy_d2h(weights, F.dep_w.p, sizeof(double) * F.dep_nnz, F.s);
+  });
+}
+int tmrg_forest_node_conn_device(tmrg_forest *f, const int **conn) {
+  return guarded([&] {
+    ARG(f && conn, "NULL argument");
+    *conn = f->f.econn.p;
+  });
+}
+int tmrg_forest_dep_node_conn_device(tmrg_forest *f, const int **ptr,
+                                     const int **conn, const double **w) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    if (ptr) *ptr = f->f.dep_ptr.p;
+    if (conn) *conn = f->f.dep_conn.p;
+    if (w) *w = f->f.dep_w.p;
+  });
+}
+
+// ---- interpolation ----------------------------------------------------
+int tmrg_interp_create(tmrg_forest *fine, tmrg_forest *coarse,
+                       tmrg_interp **out) {
+  return guarded([&] {
+    ARG(fine && coarse && out, "NULL argument");
+    auto *h = new tmrg_interp;
+    try {
+      interp_create(fine->f, coarse->f, h->I);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+int tmrg_interp_destroy(tmrg_interp *I) {
+  return guarded([&] {
+    if (!I) return;
+    cudaStreamSynchronize(I->I.s);
+    delete I;
+  });
+}
+int tmrg_interp_sizes(tmrg_interp *I, int64_t out3[3]) {
+  return guarded([&] {
+    ARG(I && out3, "NULL argument");
+    out3[0] = I->I.rows;
+    out3[1] = I->I.cols;
+    out3[2] = I->I.nnz;
+  });
+}
+int tmrg_interp_get_csr(tmrg_interp *I, int *rowptr, int *cols, double *w) {
+  return guarded([&] {
+    ARG(I, "NULL interp");
+    Interp &P = I->I;
+    if (rowptr) copy_d2h(rowptr, P.rowptr.p, sizeof(int) * (P.rows + 1), P.s);
+    if (cols) copy_d2h(cols, P.colidx.p, sizeof(int) * P.nnz, P.s);
+    if (w) copy_d2h(w, P.vals.p, sizeof(double) * P.nnz, P.s);
+  });
+}
+static int interp_host(tmrg_interp *I, int which, const double *x, double *y,
+                       int nvec) {
+  return guarded([&] {
+    ARG(I && x && y && nvec > 0, "bad argument");
+    Interp &P = I->I;
+    long long nin = (which == 0 ? P.cols : P.rows) * nvec;
+    long long nout = (which == 0 ? P.rows : P.cols) * nvec;
+    DBuf<double> dx(nin, P.s), dy(nout, P.s);
+    TMRG_CUDA(cudaMemcpyAsync(dx.p, x, sizeof(double) * nin,
+                              cudaMemcpyHostToDevice, P.s));
+    interp_apply(P, which, dx.p, dy.p, nvec);
+    copy_d2h(y, dy.p, sizeof(double) * nout, P.s);
+  });
+}
+static int interp_dev(tmrg_interp *I, int which, const double *x, double *y,
+                      int nvec) {
+  return guarded([&] {
+    ARG(I && x && y && nvec > 0, "bad argument");
+    interp_apply(I->I, which, x, y, nvec);
+  });
+}
+int tmrg_interp_mult(tmrg_interp *I, const double *x, double *y, int nvec) {
+  return interp_host(I, 0, x, y, nvec);
+}
+int tmrg_interp_mult_transpose(tmrg_interp *I, const double *x, double *y,
+                               int nvec) {
+  return interp_host(I, 1, x, y, nvec);
+}
+int tmrg_interp_mult_weight_transpose(tmrg_interp *I, const double *x,
+                                      double *y, int nvec) {
+  return interp_host(I, 2, x, y, nvec);
+}
+int tmrg_interp_mult_device(tmrg_interp *I, const double *x, double *y,
+                            int nvec) {
+  return interp_dev(I, 0, x, y, nvec);
+}
+int tmrg_interp_mult_transpose_device(tmrg_interp *I, const double *x,
+                                      double *y, int nvec) {
+  return interp_dev(I, 1, x, y, nvec);
+}
+int tmrg_interp_mult_weight_transpose_device(tmrg_interp *I, const double *x,
+                                             double *y, int nvec) {
+  return interp_dev(I, 2, x, y, nvec);
+}
+
+// ---- matrix filter ----------------------------------------------------
+int tmrg_filter_create(tmrg_forest *f, double block_len, double r, int N,
+                       tmrg_filter **out) {
+  return guarded([&] {
+    ARG(f && out, "NULL argument");
+    ARG(block_len > 0.0 && r >= 0.0 && N >= 0, "bad filter parameters");
+    auto *h = new tmrg_filter;
+    try {
+      filter_create(f->f, block_len, r, N, h->F);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+int tmrg_filter_destroy(tmrg_filter *F) {
+  return guarded([&] {
+    if (!F) return;
+    cudaStreamSynchronize(F->F.s);
+    delete F;
+  });
+}
+int tmrg_filter_sizes(tmrg_filter *F, int64_t out2[2]) {
+  return guarded([&] {
+    ARG(F && out2, "NULL argument");
+    out2[0] = F->F.n;
+    out2[1] = F->F.nnz;
+  });
+}
+int tmrg_filter_get_matrix(tmrg_filter *F, int *rowptr, int *cols,
+                           double *vals, double *Ainv, double *B,
+                           double *Tinv) {
+  return guarded([&] {
+    ARG(F, "NULL filter");
+    Filter &M = F->F;
+    if (rowptr) copy_d2h(rowptr, M.rowptr.p, sizeof(int) * (M.n + 1), M.s);
+    if (cols) copy_d2h(cols, M.colidx.p, sizeof(int) * M.nnz, M.s);
+    if (vals) copy_d2h(vals, M.vals.p, sizeof(double) * M.nnz, M.s);
+    if (Ainv) copy_d2h(Ainv, M.Ainv.p, sizeof(double) * M.n, M.s);
+    if (B) copy_d2h(B, M.B.p, sizeof(double) * M.n, M.s);
+    if (Tinv) copy_d2h(Tinv, M.Tinv.p, sizeof(double) * M.n, M.s);
+  });
+}
+static int filter_host(tmrg_filter *F, bool tr, int vpn, const double *in,
+                       double *out) {
+  return guarded([&] {
+    ARG(F && in && out && vpn > 0, "bad argument");
+    Filter &M = F->F;
+    long long len = M.n * vpn;
+    DBuf<double> a(len, M.s), b(len, M.s);
+    TMRG_CUDA(cudaMemcpyAsync(a.p, in, sizeof(double) * len,
+                              cudaMemcpyHostToDevice, M.s));
+    filter_apply(M, tr, vpn, a.p, b.p);
+    copy_d2h(out, b.p, sizeof(double) * len, M.s);
+  });
+}
+int tmrg_filter_apply(tmrg_filter *F, int vpn, const double *in, double *out) {
+  return filter_host(F, false, vpn, in, out);
+}
+int tmrg_filter_apply_transpose(tmrg_filter *F, int vpn, const double *in,
+                                double *out) {
+  return filter_host(F, true, vpn, in, out);
+}
+int tmrg_filter_apply_device(tmrg_filter *F, int vpn, const double *in,
+                             double *out) {
+  return guarded([&] {
+    ARG(F && in && out && vpn > 0, "bad argument");
+    filter_apply(F->F, false, vpn, in, out);
+  });
+}
+int tmrg_filter_apply_transpose_device(tmrg_filter *F, int vpn,
+                                       const double *in, double *out) {
+  return guarded([&] {
+    ARG(F && in && out && vpn > 0, "bad argument");
+    filter_apply(F->F, true, vpn, in, out);
+  });
+}
+int tmrg_filter_apply_f32_device(tmrg_filter *F, int vpn, const float *in,
+                                 float *out) {
+  return guarded([&] {
+    ARG(F && in && out && vpn > 0, "bad argument");
+    filter_apply_f32(F->F, false, vpn, in, out);
+  });
+}
+int tmrg_filter_apply_transpose_f32_device(tmrg_filter *F, int vpn,
+                                           const float *in, float *out) {
+  return guarded([&] {
+    ARG(F && in && out && vpn > 0, "bad argument");
+    filter_apply_f32(F->F, true, vpn, in, out);
+  });
+}
+
+int tmrg_random_refinement_device(uint64_t seed, uint64_t stream, double prob,
+                                  int *d_out, int64_t n, void *cuda_stream) {
+  return guarded([&] {
+    ARG(d_out || n == 0, "NULL output");
+    random_refinement(seed, stream, prob, d_out, n, (cudaStream_t)cuda_stream);
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,371 @@
+// Matrix density filter (TMRMatrixFilter.cpp:30-235) on the GPU.
+//
+// Setup: the consistent mass matrix M of the trilinear elements of an
+// order-2 forest, with dependent nodes condensed onto the independent
+// nodes they interpolate.  Each element first merges its 8x8 element
+// matrix, expanded through the dependent-node weights, into a dense
+// block over its distinct independent nodes; the blocks of all elements
+// are then sorted by (row, column) and summed in element order.  Then
+// D = M 1, Ainv = 1/(1 + r^2/D^(2/3)), B = Ainv r^2/(D^(2/3) D) and
+// Tinv = 1/(F~ 1).
+//
+// Apply: Horner's recurrence out = B.(M out) + t1 (forward) or
+// out = M(B.out) + t1 (transpose), one fused CSR kernel per term over all
+// `vpn` interleaved design components, so M is read once per term.
+#include "tmrg_tree.cuh"
+
+namespace tmrg {
+
+constexpr int FMAXK = 27;  // distinct independent nodes one element touches
+
+struct FilterCtx {
+  const int *conn;
+  const int *dptr, *dconn;
+  const double *dw;
+  double block_len;
+  const int16_t *lev;
+  int *err;
+};
+
+// Merged element block: distinct nodes U[0..K) in first-appearance order
+// and L[u][v] summed over (a, b, p, q) in loop order.
+__device__ int element_block(const FilterCtx &c, long long e, int *U,
+                             double (*L)[FMAXK]) {
+  const int *ec = c.conn + e * 8;
+  int ni[8][4];
+  double nw[8][4];
+  int nc[8];
+  int K = 0;
+  for (int a = 0; a < 8; a++) {
+    int g = ec[a];
+    if (g >= 0) {
+      nc[a] = 1;
+      ni[a][0] = g;
+      nw[a][0] = 1.0;
+    } else {
+      int d = -g - 1;
+      int p0 = c.dptr[d], p1 = c.dptr[d + 1];
+      nc[a] = p1 - p0;
+      if (nc[a] > 4) {
+        atomicExch(c.err, 1);
+        nc[a] = 4;
+      }
+      for (int p = 0; p < nc[a]; p++) {
+        ni[a][p] = c.dconn[p0 + p];
+        nw[a][p] = c.dw[p0 + p];
+      }
+    }
+    for (int p = 0; p < nc[a]; p++) {
+      int u = 0;
+      while (u < K && U[u] != ni[a][p]) u++;
+      if (u == K) {
+        if (K == FMAXK) {
+          atomicExch(c.err, 1);
+          return K;
+        }
+        U[K++] = ni[a][p];
+      }
+    }
+  }
+  if (!L) return K;
+  for (int u = 0; u < K; u++)
+    for (int v = 0; v < K; v++) L[u][v] = 0.0;
+  double side = c.block_len / (double)(1 << c.lev[e]);
+  double s3 = __dmul_rn(__dmul_rn(side, side), side);
+  for (int a = 0; a < 8; a++)
+    for (int b = 0; b < 8; b++) {
+      int nd = ((a ^ b) & 1) + (((a ^ b) >> 1) & 1) + ((a ^ b) >> 2);
+      double mab = __ddiv_rn(s3, 27.0 * (double)(1 << nd));
+      for (int p = 0; p < nc[a]; p++) {
+        int u = 0;
+        while (U[u] != ni[a][p]) u++;
+        double t = __dmul_rn(mab, nw[a][p]);
+        for (int q = 0; q < nc[b]; q++) {
+          int v = 0;
+          while (U[v] != ni[b][q]) v++;
+          L[u][v] = __dadd_rn(L[u][v], __dmul_rn(t, nw[b][q]));
+        }
+      }
+    }
+  return K;
+}
+
+__global__ void k_fe_count(long long n, FilterCtx c, unsigned *cnt) {
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  int U[FMAXK];
+  int K = element_block(c, e, U, nullptr);
+  cnt[e] = (unsigned)(K * K);
+}
+__global__ void __launch_bounds__(64)
+    k_fe_write(long long n, FilterCtx c, int cb, const unsigned *__restrict__ offs,
+               uint64_t *keys, uint32_t *perm, double *vals) {
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  int U[FMAXK];
+  double L[FMAXK][FMAXK];
+  int K = element_block(c, e, U, L);
+  unsigned o = offs[e];
+  for (int u = 0; u < K; u++)
+    for (int v = 0; v < K; v++) {
+      keys[o] = ((uint64_t)(uint32_t)U[u] << cb) | (uint64_t)(uint32_t)U[v];
+      perm[o] = o;
+      vals[o] = L[u][v];
+      o++;
+    }
+}
+// Sum each run of equal (row, col) keys in element order.
+__global__ void k_fe_reduce(long long E, const uint64_t *__restrict__ keys,
+                            const uint32_t *__restrict__ perm,
+                            const double *__restrict__ v,
+                            const unsigned *__restrict__ pos, int cb,
+                            int *cols, double *out, int *rowcnt) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E || pos[i + 1] == pos[i]) return;
+  uint64_t k = keys[i];
+  double s = v[perm[i]];
+  for (long long j = i + 1; j < E && keys[j] == k; j++) s = __dadd_rn(s, v[perm[j]]);
+  unsigned o = pos[i];
+  cols[o] = (int)(k & ((1ULL << cb) - 1));
+  out[o] = s;
+  atomicAdd(rowcnt + (k >> cb), 1);
+}
+__global__ void k_fe_first(long long E, const uint64_t *__restrict__ keys,
+                           unsigned *flag) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < E) flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+}
+
+// D, Ainv, B (TMRMatrixFilter.cpp:121-147).
+__global__ void k_fe_scalings(long long n, const int *__restrict__ rp,
+                              const double *__restrict__ vals, double r,
+                              double *Ainv, double *B) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double D = 0.0;
+  for (int p = rp[i]; p < rp[i + 1]; p++) D = __dadd_rn(D, vals[p]);
+  if (D == 0.0) {
+    Ainv[i] = 1.0;
+    B[i] = 0.0;
+  } else {
+    double t = pow(D, 2.0 / 3.0);
+    double rr = __dmul_rn(r, r);
+    double a = __ddiv_rn(1.0, __dadd_rn(1.0, __ddiv_rn(rr, t)));
+    Ainv[i] = a;
+    B[i] = __ddiv_rn(__dmul_rn(__dmul_rn(a, r), r), __dmul_rn(t, D));
+  }
+}
+__global__ void k_fe_tinv(long long n, const double *__restrict__ y, double *T) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) T[i] = (y[i] != 0.0) ? __ddiv_rn(1.0, y[i]) : 0.0;
+}
+template <typename T>
+__global__ void k_to_f32(long long n, const double *__restrict__ a, T *b) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (T)a[i];
+}
+
+// ---------------------------------------------------------------------
+__device__ __forceinline__ double fmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double fadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+
+// t1 = s . in ; returns t1 (the first Horner iterate).
+template <typename T>
+__global__ void k_fe_scale(long long n, int vpn, const T *__restrict__ s,
+                           const T *__restrict__ in, T *out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * vpn) return;
+  out[i] = fmul(s[i / vpn], in[i]);
+}
+
+// One Horner term over all components:
+//   forward:   y = B.(M x) + t1
+//   transpose: y = M(B.x) + t1
+// then y *= post (the final Tinv or Ainv) when post != nullptr.
+template <typename T, int VPN, bool TR>
+__global__ void __launch_bounds__(256)
+    k_fe_step(long long n, int vpn_rt, const int *__restrict__ rp,
+              const int *__restrict__ cols, const T *__restrict__ vals,
+              const T *__restrict__ B, const T *__restrict__ t1,
+              const T *__restrict__ x, T *__restrict__ y,
+              const T *__restrict__ post) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int vpn = VPN > 0 ? VPN : vpn_rt;
+  T acc[VPN > 0 ? VPN : 4];
+  for (int c0 = 0; c0 < vpn; c0 += (VPN > 0 ? VPN : 4)) {
+    const int nc = (VPN > 0) ? VPN : min(4, vpn - c0);
+#pragma unroll
+    for (int v = 0; v < (VPN > 0 ? VPN : 4); v++) acc[v] = T(0);
+    for (int p = rp[i]; p < rp[i + 1]; p++) {
+      int j = __ldg(cols + p);
+      T m = __ldg(vals + p);
+      T bj = TR ? __ldg(B + j) : T(1);
+#pragma unroll
+      for (int v = 0; v < (VPN > 0 ? VPN : 4); v++) {
+        if (v < nc) {
+          T xv = __ldg(x + (long long)j * vpn + c0 + v);
+          if (TR) xv = fmul(bj, xv);
+          acc[v] = fadd(acc[v], fmul(m, xv));
+        }
+      }
+    }
+    T bi = TR ? T(1) : B[i];
+    T pi = post ? post[i] : T(1);
+#pragma unroll
+    for (int v = 0; v < (VPN > 0 ? VPN : 4); v++) {
+      if (v < nc) {
+        long long o = i * vpn + c0 + v;
+        T r = TR ? fadd(acc[v], t1[o]) : fadd(fmul(bi, acc[v]), t1[o]);
+        if (post) r = fmul(r, pi);
+        y[o] = r;
+      }
+    }
+  }
+}
+
+template <typename T, bool TR>
+static void launch_step(long long n, int vpn, const int *rp, const int *cols,
+                        const T *vals, const T *B, const T *t1, const T *x, T *y,
+                        const T *post, cudaStream_t s) {
+  unsigned g = blocks_for(n, 256);
+  switch (vpn) {
+    case 1:
+      launch(k_fe_step<T, 1, TR>, g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
+      break;
+    case 2:
+      launch(k_fe_step<T, 2, TR>, g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
+      break;
+    case 3:
+      launch(k_fe_step<T, 3, TR>, g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
+      break;
+    case 4:
+      launch(k_fe_step<T, 4, TR>, g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
+      break;
+    default:
+      launch(k_fe_step<T, 0, TR>, g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
+  }
+}
+
+// applyFilter / applyTranspose (TMRMatrixFilter.cpp:191-235).
+template <typename T>
+static void horner(Filter &F, bool tr, int vpn, const T *in, T *out,
+                   const T *vals, const T *Ainv, const T *B, const T *Tinv) {
+  cudaStream_t s = F.s;
+  long long n = F.n, len = n * vpn;
+  if (n == 0) return;
+  DBuf<T> t1(len, s), tmp(len, s);
+  const T *pre = tr ? Tinv : Ainv;
+  const T *post = tr ? Ainv : Tinv;
+  launch(k_fe_scale<T>, blocks_for(len, 256), 256, 0, s, n, vpn, pre, in, t1.p);
+  if (F.N == 0) {
+    launch(k_fe_scale<T>, blocks_for(len, 256), 256, 0, s, n, vpn, post,
+           (const T *)t1.p, out);
+    return;
+  }
+  // ping-pong so that the last term lands in `out`
+  const T *x = t1.p;
+  for (int k = 0; k < F.N; k++) {
+    bool last = (k == F.N - 1);
+    T *y = ((F.N - 1 - k) % 2 == 0) ? out : tmp.p;
+    if (tr)
+      launch_step<T, true>(n, vpn, F.rowptr.p, F.colidx.p, vals, B, t1.p, x, y,
+                           last ? post : nullptr, s);
+    else
+      launch_step<T, false>(n, vpn, F.rowptr.p, F.colidx.p, vals, B, t1.p, x, y,
+                            last ? post : nullptr, s);
+    x = y;
+  }
+}
+
+void filter_apply(Filter &F, bool tr, int vpn, const double *in, double *out) {
+  horner<double>(F, tr, vpn, in, out, F.vals.p, F.Ainv.p, F.B.p, F.Tinv.p);
+}
+void filter_apply_f32(Filter &F, bool tr, int vpn, const float *in, float *out) {
+  horner<float>(F, tr, vpn, in, out, F.vals32.p, F.Ainv32.p, F.B32.p,
+                F.Tinv32.p);
+}
+
+void filter_create(Forest &f, double len, double r, int N, Filter &F) {
+  if (f.order != 2)
+    throw Error(TMRG_ERR_UNSUPPORTED, "matrix filter: order-2 forests only");
+  forest_create_nodes(f);
+  cudaStream_t s = f.s;
+  F.s = s;
+  F.N = N;
+  F.r = r;
+  const long long n = f.num_owned, ne = f.n;
+  F.n = n;
+  DBuf<int> err(1, s);
+  err.zero();
+  FilterCtx c{f.econn.p, f.dep_ptr.p, f.dep_conn.p, f.dep_w.p, len,
+              f.level.p, err.p};
+  DBuf<unsigned> cnt(ne + 1, s);
+  launch(k_fe_count, blocks_for(ne, 128), 128, 0, s, ne, c, cnt.p);
+  exclusive_scan<unsigned>(cnt.p, cnt.p, ne, s);
+  const long long E = read_scalar(cnt.p + ne, s);
+  const int cb = bits_for(n + 1);
+  if (2 * cb > 64) throw Error(TMRG_ERR_KEY_RANGE, "filter key range");
+  DBuf<uint64_t> keys(E, s);
+  DBuf<uint32_t> perm(E, s);
+  DBuf<double> ev(E, s);
+  launch(k_fe_write, blocks_for(ne, 64), 64, 0, s, ne, c, cb,
+         (const unsigned *)cnt.p, keys.p, perm.p, ev.p);
+  cnt.release();
+  radix_sort(keys, &perm, E, 2 * cb, s);
+  DBuf<unsigned> pos(E + 1, s);
+  launch(k_fe_first, blocks_for(E, 256), 256, 0, s, E, (const uint64_t *)keys.p,
+         pos.p);
+  exclusive_scan<unsigned>(pos.p, pos.p, E, s);
+  const long long nnz = read_scalar(pos.p + E, s);
+  F.nnz = nnz;
+  F.colidx.alloc(nnz + 1, s);
+  F.vals.alloc(nnz + 1, s);
+  F.rowptr.alloc(n + 1, s);
+  F.rowptr.zero();
+  launch(k_fe_reduce, blocks_for(E, 256), 256, 0, s, E, (const uint64_t *)keys.p,
+         (const uint32_t *)perm.p, (const double *)ev.p, (const unsigned *)pos.p,
+         cb, F.colidx.p, F.vals.p, F.rowptr.p);
+  keys.release();
+  perm.release();
+  ev.release();
+  pos.release();
+  exclusive_scan<int>(F.rowptr.p, F.rowptr.p, n, s);
+  if (read_scalar(err.p, s))
+    throw Error(TMRG_ERR_INTERNAL, "matrix filter: element touches too many nodes");
+  F.Ainv.alloc(n, s);
+  F.B.alloc(n, s);
+  F.Tinv.alloc(n, s);
+  launch(k_fe_scalings, blocks_for(n, 256), 256, 0, s, n, (const int *)F.rowptr.p,
+         (const double *)F.vals.p, r, F.Ainv.p, F.B.p);
+  // Tinv = 1 / (F~ 1) with Tinv = 1 during the evaluation.
+  {
+    DBuf<double> ones(n, s), y(n, s);
+    std::vector<double> h1(n, 1.0);
+    TMRG_CUDA(cudaMemcpyAsync(ones.p, h1.data(), n * sizeof(double),
+                              cudaMemcpyHostToDevice, s));
+    TMRG_CUDA(cudaMemcpyAsync(F.Tinv.p, h1.data(), n * sizeof(double),
+                              cudaMemcpyHostToDevice, s));
+    filter_apply(F, false, 1, ones.p, y.p);
+    launch(k_fe_tinv, blocks_for(n, 256), 256, 0, s, n, (const double *)y.p,
+           F.Tinv.p);
+    TMRG_CUDA(cudaStreamSynchronize(s));
+  }
+  F.vals32.alloc(nnz + 1, s);
+  F.Ainv32.alloc(n, s);
+  F.B32.alloc(n, s);
+  F.Tinv32.alloc(n, s);
+  launch(k_to_f32<float>, blocks_for(nnz, 256), 256, 0, s, nnz,
+         (const double *)F.vals.p, F.vals32.p);
+  launch(k_to_f32<float>, blocks_for(n, 256), 256, 0, s, n,
+         (const double *)F.Ainv.p, F.Ainv32.p);
+  launch(k_to_f32<float>, blocks_for(n, 256), 256, 0, s, n,
+         (const double *)F.B.p, F.B32.p);
+  launch(k_to_f32<float>, blocks_for(n, 256), 256, 0, s, n,
+         (const double *)F.Tinv.p, F.Tinv32.p);
+  TMRG_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace tmrg

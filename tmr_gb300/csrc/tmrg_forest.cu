@@ -1,0 +1,662 @@
+// Forest construction and adaptation on the GPU: createTrees, refine,
+// coarsen, duplicate and 2:1 balance.  Octants are kept as a sorted
+// structure of arrays; every set operation is a 64-bit Morton-key radix
+// sort followed by a compaction.
+#include <algorithm>
+#include <vector>
+
+#include "tmrg_tree.cuh"
+
+namespace tmrg {
+
+std::atomic<long long> g_kernel_launches{0};
+
+void Forest::set_order(int o, int it) {
+  free_nodes();
+  if (o < 2) o = 2;
+  if (o > TMRG_MAX_ORDER) o = TMRG_MAX_ORDER;
+  order = o;
+  interp = it;
+  // Knots on [-1, 1] (TMROctForest.cpp:1409-1426); computed with the
+  // host's cos so both sides of a comparison share them.
+  for (int i = 0; i < TMRG_MAX_ORDER; i++) knots[i] = 0.0;
+  knots[0] = -1.0;
+  knots[o - 1] = 1.0;
+  for (int i = 1; i < o - 1; i++) {
+    if (it == TMRG_GAUSS_LOBATTO_POINTS || it == TMRG_BERNSTEIN_POINTS)
+      knots[i] = -cos(M_PI * i / (o - 1));
+    else
+      knots[i] = -1.0 + 2.0 * i / (o - 1);
+  }
+}
+
+OctKey Forest::oct_key() const {
+  OctKey k;
+  k.W = std::max(maxlev, 1);
+  k.bb = conn->block_bits;
+  if (k.total_bits() > 64)
+    throw Error(TMRG_ERR_KEY_RANGE,
+                "octant key needs " + std::to_string(k.total_bits()) +
+                    " bits (blocks x levels too large for 64-bit keys)");
+  return k;
+}
+
+static void alloc_octs(Forest &f, long long n) {
+  f.block.alloc(n, f.s);
+  f.x.alloc(n, f.s);
+  f.y.alloc(n, f.s);
+  f.z.alloc(n, f.s);
+  f.level.alloc(n, f.s);
+  f.info.alloc(n, f.s);
+  f.n = n;
+}
+
+// ---------------------------------------------------------------------
+// createTrees: every block refined uniformly to `level`, generated
+// directly in Morton order (TMROctForest.cpp:1744-1833).
+__global__ void k_create_trees(long long n, int level, int *block, int *x,
+                               int *y, int *z, int16_t *lev, int16_t *info) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  long long per = 1LL << (3 * level);
+  long long b = i / per;
+  uint64_t m = (uint64_t)(i - b * per);
+  int s = TMRG_MAX_LEVEL - level;
+  block[i] = (int)b;
+  x[i] = (int)(compact3(m >> 2) << s);
+  y[i] = (int)(compact3(m >> 1) << s);
+  z[i] = (int)(compact3(m) << s);
+  lev[i] = (int16_t)level;
+  info[i] = 0;
+}
+
+void forest_create_trees(Forest &f, int level) {
+  if (!f.conn) throw Error(TMRG_ERR_STATE, "createTrees: no connectivity");
+  if (level < 0) level = 0;
+  if (level >= TMRG_MAX_LEVEL) level = TMRG_MAX_LEVEL - 1;
+  if (level > 20) throw Error(TMRG_ERR_ARG, "createTrees: level too large");
+  f.free_nodes();
+  long long n = (long long)f.conn->nb << (3 * level);
+  alloc_octs(f, n);
+  launch(k_create_trees, blocks_for(n, 256), 256, 0, f.s, n, level, f.block.p,
+         f.x.p, f.y.p, f.z.p, f.level.p, f.info.p);
+  f.maxlev = level;
+  f.have_octs = true;
+}
+
+// ---------------------------------------------------------------------
+// refine(refinement[], min, max) (TMROctForest.cpp:2169-2329).  Each
+// octant emits itself, its coarsened ancestor or the child-0 seeds of its
+// refinement; the set is made unique on (position, level) keeping the
+// first emitted, then on position keeping the finest.
+struct RefineArgs {
+  const int *ref;  // nullptr: refine every octant by one level
+  int min_level, max_level;
+};
+
+__device__ __forceinline__ int refine_target(const RefineArgs &a, int r,
+                                             int level, int &reps) {
+  reps = 1;
+  if (!a.ref) return (level < a.max_level) ? level + 1 : level;
+  if (r == 0) return level;
+  if (r < 0) {
+    if (level > a.min_level) {
+      int nl = level + r;
+      return nl < a.min_level ? a.min_level : nl;
+    }
+    return level;
+  }
+  if (level < a.max_level) {
+    int nl = level + r;
+    if (nl > a.max_level) nl = a.max_level;
+    int d = nl - level;
+    reps = (d <= 0) ? 1 : (1 << (d - 1));
+    return nl;
+  }
+  return level;
+}
+
+__global__ void k_refine_count(long long n, RefineArgs a,
+                               const int16_t *__restrict__ lev,
+                               unsigned *__restrict__ cnt, int *maxlev) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int ml = 0;
+  if (i < n) {
+    int reps;
+    int nl = refine_target(a, a.ref ? a.ref[i] : 1, lev[i], reps);
+    cnt[i] = (unsigned)(reps * reps * reps);
+    ml = nl;
+  }
+  for (int o = 16; o > 0; o >>= 1) ml = max(ml, __shfl_down_sync(0xffffffffu, ml, o));
+  if ((threadIdx.x & 31) == 0 && ml > 0) atomicMax(maxlev, ml);
+}
+
+// Payload: source index; bit 31 set when the octant keeps its info.
+__global__ void k_refine_emit(long long n, RefineArgs a, OctKey K,
+                              const int *__restrict__ blk,
+                              const int *__restrict__ xs,
+                              const int *__restrict__ ys,
+                              const int *__restrict__ zs,
+                              const int16_t *__restrict__ lev,
+                              const unsigned *__restrict__ offs, uint64_t *keys,
+                              uint32_t *vals) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int level = lev[i];
+  int r = a.ref ? a.ref[i] : 1;
+  int reps;
+  int nl = refine_target(a, r, level, reps);
+  unsigned o = offs[i];
+  int32_t x = xs[i], y = ys[i], z = zs[i];
+  if (nl == level) {
+    keys[o] = K.make(blk[i], x, y, z, level);
+    vals[o] = (uint32_t)i | 0x80000000u;
+    return;
+  }
+  int32_t h = side_of(nl);
+  int32_t x0 = x - x % h, y0 = y - y % h, z0 = z - z % h;
+  for (int ii = 0; ii < reps; ii++)
+    for (int jj = 0; jj < reps; jj++)
+      for (int kk = 0; kk < reps; kk++) {
+        keys[o] = K.make(blk[i], x0 + 2 * ii * h, y0 + 2 * jj * h,
+                         z0 + 2 * kk * h, nl);
+        vals[o] = (uint32_t)i;
+        o++;
+      }
+}
+
+// Keep entry i of the sorted keys if it opens its run of equal keys and
+// that run is the last (finest) one at its position.
+__global__ void k_dedupe_flags(long long n, const uint64_t *__restrict__ keys,
+                               unsigned *__restrict__ flag) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t k = keys[i];
+  unsigned keep = 0;
+  if (i == 0 || keys[i - 1] != k) {
+    long long e = i;
+    while (e + 1 < n && keys[e + 1] == k) e++;
+    keep = (e + 1 == n || (keys[e + 1] >> 5) != (k >> 5)) ? 1u : 0u;
+  }
+  flag[i] = keep;
+}
+
+__global__ void k_compact_octs(long long n, OctKey K,
+                               const uint64_t *__restrict__ keys,
+                               const uint32_t *__restrict__ vals,
+                               const unsigned *__restrict__ pos,
+                               const int16_t *__restrict__ old_info, int *blk,
+                               int *xs, int *ys, int *zs, int16_t *lev,
+                               int16_t *info) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (pos[i + 1] == pos[i]) return;
+  unsigned o = pos[i];
+  Oct q = K.decode(keys[i]);
+  blk[o] = q.block;
+  xs[o] = q.x;
+  ys[o] = q.y;
+  zs[o] = q.z;
+  lev[o] = (int16_t)q.level;
+  uint32_t v = vals ? vals[i] : 0u;
+  info[o] = (vals && old_info && (v & 0x80000000u)) ? old_info[v & 0x7fffffffu]
+                                                   : (int16_t)0;
+}
+
+void forest_refine(Forest &f, const int *d_ref, long long nref, int min_level,
+                   int max_level) {
+  if (!f.have_octs) throw Error(TMRG_ERR_STATE, "refine: no octants");
+  if (d_ref && nref != f.n)
+    throw Error(TMRG_ERR_ARG, "refine: refinement array length " +
+                                  std::to_string(nref) + " != octants " +
+                                  std::to_string(f.n));
+  f.free_nodes();
+  if (min_level < 0) min_level = 0;
+  if (max_level > TMRG_MAX_LEVEL) max_level = TMRG_MAX_LEVEL;
+  if (min_level > max_level) min_level = max_level;
+  long long n = f.n;
+  if (n == 0) return;
+  cudaStream_t s = f.s;
+  RefineArgs a{d_ref, min_level, max_level};
+  DBuf<unsigned> cnt(n + 1, s);
+  DBuf<int> ml(1, s);
+  ml.zero();
+  launch(k_refine_count, blocks_for(n, 256), 256, 0, s, n, a,
+         (const int16_t *)f.level.p, cnt.p, ml.p);
+  exclusive_scan<unsigned>(cnt.p, cnt.p, n, s);
+  unsigned total = read_scalar(cnt.p + n, s);
+  int newmax = read_scalar(ml.p, s);
+  f.maxlev = std::max(newmax, 0);
+  OctKey K = f.oct_key();
+  DBuf<uint64_t> keys(total, s);
+  DBuf<uint32_t> vals(total, s);
+  launch(k_refine_emit, blocks_for(n, 256), 256, 0, s, n, a, K,
+         (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
+         (const int *)f.z.p, (const int16_t *)f.level.p, (const unsigned *)cnt.p,
+         keys.p, vals.p);
+  radix_sort(keys, &vals, total, K.total_bits(), s);
+  DBuf<unsigned> pos(total + 1, s);
+  launch(k_dedupe_flags, blocks_for(total, 256), 256, 0, s, (long long)total,
+         (const uint64_t *)keys.p, pos.p);
+  exclusive_scan<unsigned>(pos.p, pos.p, total, s);
+  unsigned m = read_scalar(pos.p + total, s);
+  DBuf<int16_t> old_info = std::move(f.info);
+  alloc_octs(f, m);
+  launch(k_compact_octs, blocks_for(total, 256), 256, 0, s, (long long)total, K,
+         (const uint64_t *)keys.p, (const uint32_t *)vals.p,
+         (const unsigned *)pos.p, (const int16_t *)old_info.p, f.block.p, f.x.p,
+         f.y.p, f.z.p, f.level.p, f.info.p);
+}
+
+// ---------------------------------------------------------------------
+// coarsen (TMROctForest.cpp:2119-2164): the parent of every child-0,
+// level-0 octants unchanged, in array order.
+__global__ void k_coarsen_flags(long long n, const int *__restrict__ xs,
+                                const int *__restrict__ ys,
+                                const int *__restrict__ zs,
+                                const int16_t *__restrict__ lev,
+                                unsigned *flag) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int l = lev[i];
+  unsigned keep = 1;
+  if (l > 0) {
+    int32_t h = side_of(l);
+    keep = ((xs[i] & h) | (ys[i] & h) | (zs[i] & h)) ? 0u : 1u;
+  }
+  flag[i] = keep;
+}
+__global__ void k_coarsen_emit(long long n, const unsigned *__restrict__ pos,
+                               const int *__restrict__ blk,
+                               const int *__restrict__ xs,
+                               const int *__restrict__ ys,
+                               const int *__restrict__ zs,
+                               const int16_t *__restrict__ lev,
+                               const int16_t *__restrict__ info, int *ob,
+                               int *ox, int *oy, int *oz, int16_t *ol,
+                               int16_t *oi) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || pos[i + 1] == pos[i]) return;
+  unsigned o = pos[i];
+  int l = lev[i];
+  ob[o] = blk[i];
+  if (l > 0) {
+    int32_t h = side_of(l);
+    ox[o] = xs[i] & ~h;
+    oy[o] = ys[i] & ~h;
+    oz[o] = zs[i] & ~h;
+    ol[o] = (int16_t)(l - 1);
+    oi[o] = 0;
+  } else {
+    ox[o] = xs[i];
+    oy[o] = ys[i];
+    oz[o] = zs[i];
+    ol[o] = (int16_t)l;
+    oi[o] = info[i];
+  }
+}
+
+void forest_coarsen(Forest &f, Forest &out) {
+  if (!f.have_octs) throw Error(TMRG_ERR_STATE, "coarsen: no octants");
+  out.conn = f.conn;
+  out.set_order(f.order, f.interp);
+  cudaStream_t s = out.s;
+  TMRG_CUDA(cudaStreamSynchronize(f.s));
+  long long n = f.n;
+  DBuf<unsigned> pos(n + 1, s);
+  launch(k_coarsen_flags, blocks_for(n, 256), 256, 0, s, n, (const int *)f.x.p,
+         (const int *)f.y.p, (const int *)f.z.p, (const int16_t *)f.level.p,
+         pos.p);
+  exclusive_scan<unsigned>(pos.p, pos.p, n, s);
+  unsigned m = n ? read_scalar(pos.p + n, s) : 0;
+  alloc_octs(out, m);
+  launch(k_coarsen_emit, blocks_for(n, 256), 256, 0, s, n,
+         (const unsigned *)pos.p, (const int *)f.block.p, (const int *)f.x.p,
+         (const int *)f.y.p, (const int *)f.z.p, (const int16_t *)f.level.p,
+         (const int16_t *)f.info.p, out.block.p, out.x.p, out.y.p, out.z.p,
+         out.level.p, out.info.p);
+  out.maxlev = std::max(f.maxlev - 1, 0);
+  out.have_octs = true;
+}
+
+void forest_duplicate(Forest &f, Forest &out) {
+  out.conn = f.conn;
+  out.set_order(f.order, f.interp);
+  if (!f.have_octs) return;
+  TMRG_CUDA(cudaStreamSynchronize(f.s));
+  alloc_octs(out, f.n);
+  cudaStream_t s = out.s;
+  size_t n = (size_t)f.n;
+  TMRG_CUDA(cudaMemcpyAsync(out.block.p, f.block.p, n * 4, cudaMemcpyDeviceToDevice, s));
+  TMRG_CUDA(cudaMemcpyAsync(out.x.p, f.x.p, n * 4, cudaMemcpyDeviceToDevice, s));
+  TMRG_CUDA(cudaMemcpyAsync(out.y.p, f.y.p, n * 4, cudaMemcpyDeviceToDevice, s));
+  TMRG_CUDA(cudaMemcpyAsync(out.z.p, f.z.p, n * 4, cudaMemcpyDeviceToDevice, s));
+  TMRG_CUDA(cudaMemcpyAsync(out.level.p, f.level.p, n * 2, cudaMemcpyDeviceToDevice, s));
+  TMRG_CUDA(cudaMemcpyAsync(out.info.p, f.info.p, n * 2, cudaMemcpyDeviceToDevice, s));
+  out.maxlev = f.maxlev;
+  out.have_octs = true;
+}
+
+// ---------------------------------------------------------------------
+// 2:1 balance (TMROctForest.cpp:2525-3089).
+//
+// The reference grows a hash of child-0 octants to a fixed point: every
+// child-0 q at level L > 1 adds the child-0 of each face/edge(/corner)
+// neighbour of its parent, across tree boundaries through the block
+// tables.  That rule only maps level L to level L-1, so the fixed point is
+// reached level by level from the finest down: S_L = seeds_L U gen(S_{L+1}),
+// each level one generate + sort + unique.  The balanced forest is then
+// the set of siblings of all S_L members that are not themselves refined
+// (a sibling s at level L is refined iff S_{L+1} holds a child-0 at s's
+// anchor), which is exactly what the reference's sibling expansion and
+// finest-per-position sort leave.
+
+// Position key of a family: [block | morton(3W)].
+struct PosKey {
+  int W, bb;
+  __device__ __forceinline__ uint64_t make(int32_t b, int32_t x, int32_t y,
+                                           int32_t z) const {
+    int s = TMRG_MAX_LEVEL - W;
+    return ((uint64_t)(uint32_t)b << (3 * W)) |
+           morton3((uint32_t)x >> s, (uint32_t)y >> s, (uint32_t)z >> s);
+  }
+  __device__ __forceinline__ Oct decode(uint64_t k, int level) const {
+    int s = TMRG_MAX_LEVEL - W;
+    uint64_t m = k & ((1ULL << (3 * W)) - 1);
+    Oct o;
+    o.block = (int32_t)(k >> (3 * W));
+    o.x = (int32_t)(compact3(m >> 2) << s);
+    o.y = (int32_t)(compact3(m >> 1) << s);
+    o.z = (int32_t)(compact3(m) << s);
+    o.level = level;
+    return o;
+  }
+};
+
+// Seeds: the child-0 of every octant, keyed level-major.
+__global__ void k_seed_keys(long long n, PosKey P, const int *__restrict__ blk,
+                            const int *__restrict__ xs,
+                            const int *__restrict__ ys,
+                            const int *__restrict__ zs,
+                            const int16_t *__restrict__ lev, uint64_t *keys) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Oct o{blk[i], xs[i], ys[i], zs[i], lev[i]};
+  Oct q = sibling(o, 0);
+  keys[i] = ((uint64_t)o.level << (P.bb + 3 * P.W)) | P.make(q.block, q.x, q.y, q.z);
+}
+
+// Unique flags over sorted keys (first of each run).
+__global__ void k_unique_flags(long long n, const uint64_t *__restrict__ keys,
+                               unsigned *flag) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  flag[i] = (i == 0 || keys[i - 1] != keys[i]) ? 1u : 0u;
+}
+__global__ void k_unique_emit(long long n, const uint64_t *__restrict__ keys,
+                              const unsigned *__restrict__ pos, uint64_t mask,
+                              uint64_t *out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || pos[i + 1] == pos[i]) return;
+  out[pos[i]] = keys[i] & mask;
+}
+__global__ void k_mask_copy(long long n, const uint64_t *__restrict__ in,
+                            uint64_t mask, uint64_t *out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = in[i] & mask;
+}
+__global__ void k_level_starts(long long n, const uint64_t *__restrict__ keys,
+                               int shift, long long *starts) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int l = (int)(keys[i] >> shift);
+  if (i == 0 || (int)(keys[i - 1] >> shift) != l) starts[l] = i;
+}
+
+// Children-0 of the parent's neighbours of family q (level L >= 2).
+template <bool WRITE>
+__device__ __forceinline__ unsigned gen_family(const ConnDev &c, PosKey P,
+                                               const Oct &q, int corner,
+                                               uint64_t *out) {
+  unsigned cnt = 0;
+  Oct p = parent_of(q);
+  int32_t bs = 2 * side_of(p.level);  // side of the generated family's box
+  auto emit = [&](const Oct &r) {
+    if (WRITE) out[cnt] = P.make(r.block, r.x, r.y, r.z);
+    cnt++;
+  };
+  for (int f = 0; f < 6; f++) {
+    Oct r = sibling(face_nbr(p, f), 0);
+    if (in_tree(r))
+      emit(r);
+    else
+      for_images(c, r, bs, false, emit);
+  }
+  for (int e = 0; e < 12; e++) {
+    Oct r = sibling(edge_nbr(p, e), 0);
+    if (in_tree(r))
+      emit(r);
+    else
+      for_images(c, r, bs, false, emit);
+  }
+  if (corner) {
+    for (int k = 0; k < 8; k++) {
+      Oct r = sibling(corner_nbr(p, k), 0);
+      if (in_tree(r))
+        emit(r);
+      else
+        for_images(c, r, bs, true, emit);
+    }
+  }
+  return cnt;
+}
+
+__global__ void k_gen_count(long long n, ConnDev c, PosKey P, int level,
+                            int corner, const uint64_t *__restrict__ cur,
+                            unsigned *cnt) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Oct q = P.decode(cur[i], level);
+  cnt[i] = gen_family<false>(c, P, q, corner, nullptr);
+}
+__global__ void k_gen_write(long long n, ConnDev c, PosKey P, int level,
+                            int corner, const uint64_t *__restrict__ cur,
+                            const unsigned *__restrict__ offs, uint64_t *out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Oct q = P.decode(cur[i], level);
+  gen_family<true>(c, P, q, corner, out + offs[i]);
+}
+
+// Leaves of level L: siblings of each family in S_L whose anchor does not
+// hold a finer family (or the root itself at level 0).
+__global__ void k_leaves(long long n, PosKey P, OctKey K, int level,
+                         const uint64_t *__restrict__ cur,
+                         const uint64_t *__restrict__ finer, long long nfiner,
+                         uint64_t *out, unsigned long long *counter) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t mine[8];
+  int m = 0;
+  if (i < n) {
+    Oct q = P.decode(cur[i], level);
+    int ns = (level == 0) ? 1 : 8;
+    for (int j = 0; j < ns; j++) {
+      Oct sb = (level == 0) ? q : sibling(q, j);
+      uint64_t pk = P.make(sb.block, sb.x, sb.y, sb.z);
+      if (!contains_u64(finer, nfiner, pk))
+        mine[m++] = K.make(sb.block, sb.x, sb.y, sb.z, level);
+    }
+  }
+  // warp-aggregated append
+  int lane = threadIdx.x & 31;
+  int incl = m;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  int tot = __shfl_sync(0xffffffffu, incl, 31);
+  unsigned long long base = 0;
+  if (lane == 31 && tot > 0) base = atomicAdd(counter, (unsigned long long)tot);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  unsigned long long o = base + (incl - m);
+  for (int j = 0; j < m; j++) out[o + j] = mine[j];
+}
+
+__global__ void k_decode_octs(long long n, OctKey K,
+                              const uint64_t *__restrict__ keys, int *blk,
+                              int *xs, int *ys, int *zs, int16_t *lev,
+                              int16_t *info) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Oct q = K.decode(keys[i]);
+  blk[i] = q.block;
+  xs[i] = q.x;
+  ys[i] = q.y;
+  zs[i] = q.z;
+  lev[i] = (int16_t)q.level;
+  info[i] = 0;
+}
+
+// Sort `keys` (n entries, nbits) and keep one of each value (masked).
+static long long sort_unique(DBuf<uint64_t> &keys, long long n, int nbits,
+                             uint64_t mask, DBuf<uint64_t> &out,
+                             cudaStream_t s) {
+  if (n == 0) {
+    out.release();
+    return 0;
+  }
+  radix_sort(keys, nullptr, n, nbits, s);
+  DBuf<unsigned> pos(n + 1, s);
+  launch(k_unique_flags, blocks_for(n, 256), 256, 0, s, n,
+         (const uint64_t *)keys.p, pos.p);
+  exclusive_scan<unsigned>(pos.p, pos.p, n, s);
+  long long m = read_scalar(pos.p + n, s);
+  out.alloc(m, s);
+  launch(k_unique_emit, blocks_for(n, 256), 256, 0, s, n,
+         (const uint64_t *)keys.p, (const unsigned *)pos.p, mask, out.p);
+  return m;
+}
+
+void forest_balance(Forest &f, int corner) {
+  if (!f.have_octs)
+    throw Error(TMRG_ERR_STATE,
+                "Cannot call balance(), no octants have been created");
+  f.free_nodes();
+  long long n = f.n;
+  if (n == 0) return;
+  cudaStream_t s = f.s;
+  OctKey K = f.oct_key();
+  PosKey P{K.W, K.bb};
+  const int pbits = K.bb + 3 * K.W;
+  const uint64_t pmask = (pbits >= 64) ? ~0ULL : ((1ULL << pbits) - 1);
+  ConnDev c = f.conn->dev;
+
+  // Seeds, unique, grouped by level.
+  DBuf<uint64_t> sk(n, s);
+  launch(k_seed_keys, blocks_for(n, 256), 256, 0, s, n, P, (const int *)f.block.p,
+         (const int *)f.x.p, (const int *)f.y.p, (const int *)f.z.p,
+         (const int16_t *)f.level.p, sk.p);
+  DBuf<uint64_t> seeds;
+  long long ns = sort_unique(sk, n, pbits + 5, ~0ULL, seeds, s);
+  sk.release();
+  DBuf<long long> starts(TMRG_MAX_LEVEL + 2, s);
+  starts.fill_bytes(0xff);
+  launch(k_level_starts, blocks_for(ns, 256), 256, 0, s, ns,
+         (const uint64_t *)seeds.p, pbits, starts.p);
+  std::vector<long long> st(TMRG_MAX_LEVEL + 2);
+  TMRG_CUDA(cudaMemcpyAsync(st.data(), starts.p, st.size() * sizeof(long long),
+                            cudaMemcpyDeviceToHost, s));
+  TMRG_CUDA(cudaStreamSynchronize(s));
+  const int L = f.maxlev;
+  std::vector<long long> lo(L + 2, 0), hi(L + 2, 0);
+  {
+    long long next = ns;
+    for (int l = TMRG_MAX_LEVEL + 1; l >= 0; l--) {
+      if (st[l] >= 0) {
+        if (l <= L + 1) {
+          lo[l] = st[l];
+          hi[l] = next;
+        }
+        next = st[l];
+      }
+    }
+  }
+
+  // Fixed point, finest level first.
+  std::vector<DBuf<uint64_t>> S(L + 2);
+  std::vector<long long> Sn(L + 2, 0);
+  DBuf<uint64_t> gen;
+  long long ngen = 0;
+  for (int l = L; l >= 0; l--) {
+    long long nseed = hi[l] - lo[l];
+    long long tot = nseed + ngen;
+    if (tot > 0) {
+      DBuf<uint64_t> cat(tot, s);
+      if (nseed)
+        launch(k_mask_copy, blocks_for(nseed, 256), 256, 0, s, nseed,
+               (const uint64_t *)(seeds.p + lo[l]), pmask, cat.p);
+      if (ngen)
+        TMRG_CUDA(cudaMemcpyAsync(cat.p + nseed, gen.p, ngen * sizeof(uint64_t),
+                                  cudaMemcpyDeviceToDevice, s));
+      Sn[l] = sort_unique(cat, tot, pbits, ~0ULL, S[l], s);
+    }
+    gen.release();
+    ngen = 0;
+    if (l >= 2 && Sn[l] > 0) {
+      DBuf<unsigned> cnt(Sn[l] + 1, s);
+      launch(k_gen_count, blocks_for(Sn[l], 128), 128, 0, s, Sn[l], c, P, l,
+             corner, (const uint64_t *)S[l].p, cnt.p);
+      exclusive_scan<unsigned>(cnt.p, cnt.p, Sn[l], s);
+      ngen = read_scalar(cnt.p + Sn[l], s);
+      gen.alloc(ngen, s);
+      launch(k_gen_write, blocks_for(Sn[l], 128), 128, 0, s, Sn[l], c, P, l,
+             corner, (const uint64_t *)S[l].p, (const unsigned *)cnt.p, gen.p);
+    }
+  }
+  seeds.release();
+
+  // Leaves of every level, then one sort into element order.
+  long long cap = 0;
+  for (int l = 0; l <= L; l++) cap += (l == 0 ? 1 : 8) * Sn[l];
+  DBuf<uint64_t> leaves(cap, s);
+  DBuf<unsigned long long> counter(1, s);
+  counter.zero();
+  for (int l = 0; l <= L; l++) {
+    if (!Sn[l]) continue;
+    launch(k_leaves, blocks_for(Sn[l], 256), 256, 0, s, Sn[l], P, K, l,
+           (const uint64_t *)S[l].p, (const uint64_t *)S[l + 1].p, Sn[l + 1],
+           leaves.p, counter.p);
+  }
+  long long m = (long long)read_scalar(counter.p, s);
+  S.clear();
+  radix_sort(leaves, nullptr, m, K.total_bits(), s);
+  alloc_octs(f, m);
+  launch(k_decode_octs, blocks_for(m, 256), 256, 0, s, m, K,
+         (const uint64_t *)leaves.p, f.block.p, f.x.p, f.y.p, f.z.p, f.level.p,
+         f.info.p);
+}
+
+// ---------------------------------------------------------------------
+__global__ void k_random_refinement(uint64_t seed, uint64_t stream, double prob,
+                                    int *out, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  auto sm = [](uint64_t x) {
+    x += 0x9E3779B97F4A7C15ULL;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+    return x ^ (x >> 31);
+  };
+  uint64_t r = sm(sm(seed * 0x100000001B3ULL + stream) ^
+                  ((uint64_t)i * 0xD6E8FEB86659FD93ULL));
+  double u = (double)(r >> 11) * (1.0 / 9007199254740992.0);
+  out[i] = (u < prob) ? 1 : 0;
+}
+
+void random_refinement(uint64_t seed, uint64_t stream, double prob, int *out,
+                       long long n, cudaStream_t s) {
+  launch(k_random_refinement, blocks_for(n, 256), 256, 0, s, seed, stream, prob,
+         out, n);
+}
+
+}  // namespace tmrg

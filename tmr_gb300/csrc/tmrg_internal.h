@@ -1,0 +1,118 @@
+// Internal object layouts shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <memory>
+#include <vector>
+
+#include "tmrg_common.cuh"
+#include "tmrg_prims.cuh"
+
+namespace tmrg {
+
+// Device view of the block connectivity tables.  CSR entries hold
+// 8*block+corner, 12*block+edge, 6*block+face; the first entry of each
+// list is the lowest-numbered block, which owns the shared entity
+// (TMROctForest.cpp:1090-1143).
+struct ConnDev {
+  int nb;
+  const int *block_conn;  // 8 per block
+  const int *block_edge;  // 12 per block: global edge number
+  const int *block_face;  // 6 per block: global face number
+  const int *face_ids;    // 6 per block: orientation relative to owner
+  const int *node_ptr, *node_ent;
+  const int *edge_ptr, *edge_ent;
+  const int *face_ptr, *face_ent;
+};
+
+// Block connectivity: built on the host (O(blocks)) and mirrored on the
+// device.  Shared by a forest and the forests derived from it.
+struct Conn {
+  int num_nodes = 0, num_edges = 0, num_faces = 0, nb = 0;
+  std::vector<int> block_conn, block_edge, block_face, face_ids;
+  std::vector<int> node_ptr, node_ent, edge_ptr, edge_ent, face_ptr, face_ent;
+  int max_node_val = 1, max_edge_val = 1, max_face_val = 1;
+  DBuf<int> d_all;
+  ConnDev dev{};
+  int block_bits = 1;
+};
+std::shared_ptr<Conn> build_conn(int num_nodes, const int *block_conn,
+                                 int num_blocks, cudaStream_t s);
+
+struct Forest {
+  cudaStream_t s = 0;
+  int order = 2, interp = 1;
+  double knots[TMRG_MAX_ORDER] = {0};
+  std::shared_ptr<Conn> conn;
+
+  // Octants, structure of arrays, sorted in TMR element order.
+  bool have_octs = false;
+  long long n = 0;
+  int maxlev = 0;  // finest level present (key width)
+  DBuf<int> block, x, y, z;
+  DBuf<int16_t> level, info;
+
+  // createNodes products.
+  bool have_nodes = false;
+  long long num_local = 0, num_owned = 0, num_dep = 0, dep_nnz = 0,
+            ext_pre = 0;
+  DBuf<int> econn;  // n * order^3 global node numbers
+  DBuf<int> dep_ptr, dep_conn;
+  DBuf<double> dep_w;
+
+  void free_nodes() {
+    have_nodes = false;
+    econn.release();
+    dep_ptr.release();
+    dep_conn.release();
+    dep_w.release();
+    num_local = num_owned = num_dep = dep_nnz = ext_pre = 0;
+  }
+  void set_order(int o, int it);
+  OctKey oct_key() const;
+};
+
+struct Interp {
+  cudaStream_t s = 0;
+  long long rows = 0, cols = 0, nnz = 0;
+  DBuf<int> rowptr, colidx;  // P, row-sorted CSR
+  DBuf<double> vals;
+  DBuf<int> t_rowptr, t_colidx;  // P^T as CSR (rows = coarse nodes)
+  DBuf<double> t_vals;
+  DBuf<double> colsum;  // P^T 1 (column sums of P)
+};
+
+struct Filter {
+  cudaStream_t s = 0;
+  long long n = 0, nnz = 0;
+  int N = 10;
+  double r = 0.0;
+  DBuf<int> rowptr, colidx;
+  DBuf<double> vals;
+  DBuf<float> vals32;
+  DBuf<double> Ainv, B, Tinv;
+  DBuf<float> Ainv32, B32, Tinv32;
+};
+
+// Operations (tmrg_forest.cu, tmrg_nodes.cu, tmrg_interp.cu,
+// tmrg_filter.cu).
+void forest_create_trees(Forest &f, int level);
+void forest_refine(Forest &f, const int *d_ref, long long nref, int min_level,
+                   int max_level);
+void forest_coarsen(Forest &f, Forest &out);
+void forest_duplicate(Forest &f, Forest &out);
+void forest_balance(Forest &f, int corner);
+void forest_create_nodes(Forest &f);
+void interp_create(Forest &fine, Forest &coarse, Interp &I);
+void interp_apply(Interp &I, int which, const double *x, double *y, int nvec);
+void filter_create(Forest &f, double len, double r, int N, Filter &F);
+void filter_apply(Filter &F, bool transpose, int vpn, const double *in,
+                  double *out);
+void filter_apply_f32(Filter &F, bool transpose, int vpn, const float *in,
+                      float *out);
+void random_refinement(uint64_t seed, uint64_t stream, double prob, int *out,
+                       long long n, cudaStream_t s);
+
+}  // namespace tmrg

@@ -1,0 +1,769 @@
+// createNodes on the GPU (TMROctForest.cpp:3455-5519), hash-free:
+//   1. hanging face/edge flags per octant by binary search in the sorted
+//      octant keys (computeDepFacesAndEdges);
+//   2. every element emits its corner (order 2) or 27 node objects in the
+//      owner tree's frame (transformNode); one radix sort of the node keys
+//      gives the node order of the reference (compareNode), and the unique
+//      run index of each (element, object) entry is its local node;
+//   3. dependent nodes are labelled, then one scan numbers independent
+//      nodes 0.. and dependent nodes -1, -2, .. in node order;
+//   4. the dependent-node CSR is sized by a scan; when several elements
+//      write the same row the last one in element order wins, as in the
+//      reference's sequential loop, resolved with a 64-bit atomicMax.
+#include <vector>
+
+#include "tmrg_tree.cuh"
+
+namespace tmrg {
+
+struct Knots {
+  double k[TMRG_MAX_ORDER];
+};
+
+// Labels distinguish node objects at one position for order > 3
+// (initLabel, TMROctForest.cpp:6798-6811).
+struct Labels {
+  int l[4];
+  int bits;
+};
+static Labels make_labels(int order, int interp) {
+  Labels L;
+  if (order > 3 || (order >= 3 && interp == TMRG_BERNSTEIN_POINTS)) {
+    for (int i = 0; i < 4; i++) L.l[i] = i;
+    L.bits = 2;
+  } else {
+    for (int i = 0; i < 4; i++) L.l[i] = 0;
+    L.bits = 0;
+  }
+  return L;
+}
+
+// ---------------------------------------------------------------------
+// 1. Hanging flags.
+__global__ void k_oct_keys(long long n, OctKey K, const int *__restrict__ blk,
+                           const int *__restrict__ xs, const int *__restrict__ ys,
+                           const int *__restrict__ zs,
+                           const int16_t *__restrict__ lev, uint64_t *keys) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) keys[i] = K.make(blk[i], xs[i], ys[i], zs[i], lev[i]);
+}
+
+__global__ void k_dep_info(long long n, ConnDev c, OctKey K,
+                           const uint64_t *__restrict__ keys,
+                           const int *__restrict__ blk,
+                           const int *__restrict__ xs, const int *__restrict__ ys,
+                           const int *__restrict__ zs,
+                           const int16_t *__restrict__ lev, int16_t *info) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Oct o{blk[i], xs[i], ys[i], zs[i], lev[i]};
+  if (o.level == 0) {
+    info[i] = 0;
+    return;
+  }
+  const int32_t hmax = TMRG_HMAX;
+  auto exists = [&](const Oct &q) {
+    return contains_u64(keys, n, K.make(q.block, q.x, q.y, q.z, q.level));
+  };
+  int id = child_id(o);
+  Oct p = parent_of(o);
+  int bits = 0;
+  for (int k = 0; k < 3; k++) {
+    int fi = child_face(id, k);
+    Oct nb = face_nbr(p, fi);
+    bool hit = false;
+    if (in_tree(nb)) {
+      hit = exists(nb);
+    } else {
+      for_images(c, nb, side_of(nb.level), false, [&](const Oct &q) {
+        if (!hit && exists(q)) hit = true;
+      });
+    }
+    if (hit) bits |= 1 << k;
+  }
+  for (int k = 0; k < 3; k++) {
+    int e = child_edge(id, k);
+    Oct nb = edge_nbr(p, e);
+    bool out = nb.x < 0 || nb.x >= hmax || nb.y < 0 || nb.y >= hmax ||
+               nb.z < 0 || nb.z >= hmax;
+    bool hit = false;
+    if (!out) {
+      hit = exists(nb);
+    } else {
+      for_images(c, nb, side_of(nb.level), false, [&](const Oct &q) {
+        if (!hit && exists(q)) hit = true;
+      });
+    }
+    if (hit) bits |= 1 << (k + 3);
+  }
+  info[i] = (int16_t)bits;
+}
+
+// decode_index_from_info (TMROctForest.cpp:250-276).
+__device__ __forceinline__ void decode_info(int id, int info, int &fbits,
+                                            int &ebits) {
+  fbits = 0;
+  ebits = 0;
+  for (int k = 0; k < 3; k++) {
+    if (info & (1 << k)) {
+      fbits |= 1 << child_face(id, k);
+      ebits |= 1 << child_face_edge(id, k, 0);
+      ebits |= 1 << child_face_edge(id, k, 1);
+    }
+    if (info & (1 << (k + 3))) ebits |= 1 << child_edge(id, k);
+  }
+}
+
+// ---------------------------------------------------------------------
+// 2. Node objects.  Object j of an element: order 2 -> corner j
+// (x fastest); order >= 3 -> (ii, jj, kk) = j % 3, j / 3 % 3, j / 9 on the
+// half-size lattice.
+struct NodeGen {
+  int order, nobj;
+  Labels lab;
+  NodeKey NK;
+};
+
+__device__ __forceinline__ void object_of(const NodeGen &g, const Oct &e, int j,
+                                          int32_t &x, int32_t &y, int32_t &z,
+                                          int &label, int &mult, int &edge_dir) {
+  edge_dir = -1;
+  if (g.order == 2) {
+    int32_t h = side_of(e.level);
+    x = e.x + h * (j & 1);
+    y = e.y + h * ((j >> 1) & 1);
+    z = e.z + h * (j >> 2);
+    label = g.lab.l[0];
+    mult = 1;
+    return;
+  }
+  int32_t h = (int32_t)1 << (TMRG_MAX_LEVEL - e.level - 1);
+  int ii = j % 3, jj = (j / 3) % 3, kk = j / 9;
+  x = e.x + h * ii;
+  y = e.y + h * jj;
+  z = e.z + h * kk;
+  bool fx = ii != 1, fy = jj != 1, fz = kk != 1;
+  int m = g.order - 2;
+  if (fx && fy && fz) {
+    label = g.lab.l[0];
+    mult = 1;
+  } else if ((fy && fz) || (fx && fz) || (fx && fy)) {
+    label = g.lab.l[1];
+    mult = m;
+    edge_dir = !fx ? 0 : (!fy ? 1 : 2);
+  } else if (fx || fy || fz) {
+    label = g.lab.l[2];
+    mult = m * m;
+  } else {
+    label = g.lab.l[3];
+    mult = m * m * m;
+  }
+}
+
+__global__ void k_node_keys(long long n, ConnDev c, NodeGen g,
+                            const int *__restrict__ blk,
+                            const int *__restrict__ xs, const int *__restrict__ ys,
+                            const int *__restrict__ zs,
+                            const int16_t *__restrict__ lev, uint64_t *keys,
+                            uint32_t *vals) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * g.nobj) return;
+  long long e = t / g.nobj;
+  int j = (int)(t - e * g.nobj);
+  Oct o{blk[e], xs[e], ys[e], zs[e], lev[e]};
+  int32_t b = o.block, x, y, z;
+  int label, mult, ed;
+  object_of(g, o, j, x, y, z, label, mult, ed);
+  transform_node(c, b, x, y, z, -1, nullptr, nullptr);
+  keys[t] = g.NK.make(b, x, y, z, label);
+  vals[t] = (uint32_t)t;
+}
+
+// Sorted node-object keys -> run index per (element, object) and the
+// unique keys/multiplicities.
+__global__ void k_node_unique(long long m, const uint64_t *__restrict__ keys,
+                              const uint32_t *__restrict__ vals,
+                              const unsigned *__restrict__ pos, int lab_bits,
+                              int order, uint64_t *ukeys, unsigned *umult,
+                              unsigned *obj_of) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  unsigned idx = pos[i + 1] - 1;  // inclusive count - 1
+  obj_of[vals[i]] = idx;
+  if (pos[i + 1] != pos[i]) {
+    uint64_t k = keys[i];
+    ukeys[idx] = k;
+    int label = lab_bits ? (int)(k & 3) : 0;
+    int mm = order - 2;
+    unsigned mult = (label == 0) ? 1u : (label == 1) ? mm : (label == 2) ? mm * mm : mm * mm * mm;
+    umult[idx] = mult;
+  }
+}
+
+// Flags for the unique pass (first entry of each run).
+__global__ void k_first_of_run(long long m, const uint64_t *__restrict__ keys,
+                               unsigned *flag) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+}
+
+// Element connectivity in local node numbers (createLocalConn,
+// TMROctForest.cpp:4660-4867).
+__global__ void k_local_conn(long long n, ConnDev c, NodeGen g,
+                             const int *__restrict__ blk,
+                             const int *__restrict__ xs,
+                             const int *__restrict__ ys,
+                             const int *__restrict__ zs,
+                             const int16_t *__restrict__ lev,
+                             const unsigned *__restrict__ obj_of,
+                             const unsigned *__restrict__ noff, int *lconn) {
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int o = g.order;
+  const int npe = o * o * o;
+  int *out = lconn + e * npe;
+  const unsigned *ob = obj_of + e * g.nobj;
+  if (o == 2) {
+    for (int j = 0; j < 8; j++) out[j] = (int)noff[ob[j]];
+    return;
+  }
+  if (g.lab.bits == 0) {  // order 3 with one node per object
+    for (int j = 0; j < 27; j++) out[j] = (int)noff[ob[j]];
+    return;
+  }
+  // order >= 4: expand edge/face/interior objects with the owner frame's
+  // edge reversal and face orientation.
+  Oct el{blk[e], xs[e], ys[e], zs[e], lev[e]};
+  int rev[27], fid[27];
+  for (int j = 0; j < 27; j++) {
+    rev[j] = 0;
+    fid[j] = 0;
+    int32_t b = el.block, x, y, z;
+    int label, mult, ed;
+    object_of(g, el, j, x, y, z, label, mult, ed);
+    int ii = j % 3, jj = (j / 3) % 3, kk = j / 9;
+    int nmid = (ii == 1) + (jj == 1) + (kk == 1);
+    if (nmid == 1)
+      transform_node(c, b, x, y, z, ed, &rev[j], nullptr);
+    else if (nmid == 2)
+      transform_node(c, b, x, y, z, -1, nullptr, &fid[j]);
+  }
+  for (int kk = 0; kk < o; kk++)
+    for (int jj = 0; jj < o; jj++)
+      for (int ii = 0; ii < o; ii++) {
+        int ci = (ii == 0) ? 0 : (ii == o - 1) ? 2 : 1;
+        int cj = (jj == 0) ? 0 : (jj == o - 1) ? 2 : 1;
+        int ck = (kk == 0) ? 0 : (kk == o - 1) ? 2 : 1;
+        int j = ci + 3 * cj + 9 * ck;
+        int base = (int)noff[ob[j]];
+        int nmid = (ci == 1) + (cj == 1) + (ck == 1);
+        int add = 0;
+        if (nmid == 1) {
+          int a = (ci == 1) ? ii : (cj == 1) ? jj : kk;
+          add = rev[j] ? (o - 2 - a) : (a - 1);
+        } else if (nmid == 2) {
+          int a, b2;
+          if (ci != 1) {
+            a = jj;
+            b2 = kk;
+          } else if (cj != 1) {
+            a = ii;
+            b2 = kk;
+          } else {
+            a = ii;
+            b2 = jj;
+          }
+          int32_t u, v;
+          face_get(fid[j], o - 1, a, b2, u, v);
+          add = (u - 1) + (v - 1) * (o - 2);
+        } else if (nmid == 3) {
+          add = (ii - 1) + (jj - 1) * (o - 2) + (kk - 1) * (o - 2) * (o - 2);
+        }
+        out[ii + jj * o + kk * o * o] = base + add;
+      }
+}
+
+// ---------------------------------------------------------------------
+// 3. Dependent labels (labelDependentNodes, TMROctForest.cpp:3711-3832).
+__device__ __forceinline__ int edge_off(int o, int ei, int a) {
+  if (ei < 4) return a + (o - 1) * (ei % 2) * o + (o - 1) * (ei / 2) * o * o;
+  if (ei < 8) return (o - 1) * (ei % 2) + a * o + (o - 1) * ((ei - 4) / 2) * o * o;
+  return (o - 1) * (ei % 2) + (o - 1) * ((ei - 8) / 2) * o + a * o * o;
+}
+__device__ __forceinline__ int face_off(int o, int fi, int a, int b) {
+  if (fi < 2) return (o - 1) * (fi % 2) + a * o + b * o * o;
+  if (fi < 4) return a + (o - 1) * (fi % 2) * o + b * o * o;
+  return a + b * o + (o - 1) * (fi % 2) * o * o;
+}
+
+__global__ void k_label_dep(long long n, int order, int bern,
+                            const int *__restrict__ xs,
+                            const int *__restrict__ ys,
+                            const int *__restrict__ zs,
+                            const int16_t *__restrict__ lev,
+                            const int16_t *__restrict__ info,
+                            const int *__restrict__ lconn, unsigned *depflag) {
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  int inf = info[e];
+  if (!inf) return;
+  const int o = order;
+  Oct el{0, xs[e], ys[e], zs[e], lev[e]};
+  int id = child_id(el);
+  int fb, eb;
+  decode_info(id, inf, fb, eb);
+  const int *c = lconn + e * (long long)(o * o * o);
+  for (int fi = 0; fi < 6; fi++)
+    if (fb & (1 << fi))
+      for (int k = 0; k < 4; k++) eb |= 1 << face_edge(fi, k);
+  bool m3 = (o == 3 && !bern);
+  for (int ei = 0; ei < 12; ei++) {
+    if (!(eb & (1 << ei))) continue;
+    int sbit = (ei < 4) ? (id & 1) : (ei < 8) ? ((id >> 1) & 1) : (id >> 2);
+    int st, en;
+    if (sbit == 0) {
+      st = 1;
+      en = m3 ? o - 1 : o;
+    } else {
+      st = m3 ? 1 : 0;
+      en = o - 1;
+    }
+    for (int a = st; a < en; a++) depflag[c[edge_off(o, ei, a)]] = 1u;
+  }
+  for (int fi = 0; fi < 6; fi++) {
+    if (!(fb & (1 << fi))) continue;
+    for (int b = 1; b < o - 1; b++)
+      for (int a = 1; a < o - 1; a++) depflag[c[face_off(o, fi, a, b)]] = 1u;
+  }
+}
+
+// ---------------------------------------------------------------------
+// 4. Dependent CSR (createDependentConn, TMROctForest.cpp:5157-5519).
+struct DepCtx {
+  int order;
+  Labels lab;
+  NodeKey NK;
+  ConnDev c;
+  const uint64_t *ukeys;
+  long long nobj;
+  const unsigned *noff;
+  const unsigned *deprank;  // exclusive scan of dependent flags
+  const unsigned *depflag;
+  int *err;
+};
+
+__device__ __forceinline__ int dep_index(const DepCtx &d, int local) {
+  return d.depflag[local] ? (int)d.deprank[local] : -1;
+}
+
+// Local node number of the object at (b, x, y, z) with `label`; also the
+// owner-frame edge reversal / face orientation.
+__device__ __forceinline__ int find_object(const DepCtx &d, int32_t b, int32_t x,
+                                           int32_t y, int32_t z, int label,
+                                           int edge_dir, int *rev, int *fid) {
+  transform_node(d.c, b, x, y, z, edge_dir, rev, fid);
+  uint64_t k = d.NK.make(b, x, y, z, label);
+  long long i = lower_bound_u64(d.ukeys, d.nobj, k);
+  if (i >= d.nobj || d.ukeys[i] != k) {
+    atomicExch(d.err, 1);
+    return 0;
+  }
+  return (int)d.noff[i];
+}
+
+// getEdgeNodes (TMROctForest.cpp:4886-4963).
+__device__ void parent_edge_nodes(const DepCtx &d, const Oct &p, int ei,
+                                  int *out) {
+  const int o = d.order;
+  int32_t h = (int32_t)1 << (TMRG_MAX_LEVEL - p.level - 1);
+  int32_t hp = side_of(p.level);
+  int np = (o == 2) ? 2 : 3;
+  int32_t step = (o == 2) ? hp : h;
+  for (int ii = 0; ii < np; ii++) {
+    int32_t x, y, z;
+    if (ei < 4) {
+      x = p.x + ii * step;
+      y = p.y + hp * (ei % 2);
+      z = p.z + hp * (ei / 2);
+    } else if (ei < 8) {
+      x = p.x + hp * (ei % 2);
+      y = p.y + ii * step;
+      z = p.z + hp * ((ei - 4) / 2);
+    } else {
+      x = p.x + hp * (ei % 2);
+      y = p.y + hp * ((ei - 8) / 2);
+      z = p.z + ii * step;
+    }
+    if (o == 2 || ii != 1) {
+      int t = find_object(d, p.block, x, y, z, d.lab.l[0], -1, nullptr, nullptr);
+      out[(o == 2) ? ii : (ii / 2) * (o - 1)] = t;
+    } else {
+      int rev = 0;
+      int t = find_object(d, p.block, x, y, z, d.lab.l[1], ei / 4, &rev, nullptr);
+      for (int k = 1; k < o - 1; k++) out[k] = t + (rev ? o - 2 - k : k - 1);
+    }
+  }
+}
+
+// getFaceNodes (TMROctForest.cpp:4984-5146).
+__device__ void parent_face_nodes(const DepCtx &d, const Oct &p, int fi,
+                                  int *out) {
+  const int o = d.order;
+  int32_t h = (int32_t)1 << (TMRG_MAX_LEVEL - p.level - 1);
+  int np = (o == 2) ? 2 : 3;
+  int32_t step = (o == 2) ? 2 * h : h;
+  for (int jj = 0; jj < np; jj++)
+    for (int ii = 0; ii < np; ii++) {
+      int32_t x, y, z;
+      if (fi < 2) {
+        x = p.x + 2 * h * (fi % 2);
+        y = p.y + ii * step;
+        z = p.z + jj * step;
+      } else if (fi < 4) {
+        x = p.x + ii * step;
+        y = p.y + 2 * h * (fi % 2);
+        z = p.z + jj * step;
+      } else {
+        x = p.x + ii * step;
+        y = p.y + jj * step;
+        z = p.z + 2 * h * (fi % 2);
+      }
+      if (o == 2) {
+        out[ii + 2 * jj] =
+            find_object(d, p.block, x, y, z, d.lab.l[0], -1, nullptr, nullptr);
+        continue;
+      }
+      bool ci = (ii != 1), cj = (jj != 1);
+      if (ci && cj) {
+        out[(ii / 2) * (o - 1) + (jj / 2) * (o - 1) * o] =
+            find_object(d, p.block, x, y, z, d.lab.l[0], -1, nullptr, nullptr);
+      } else if (ci || cj) {
+        int e = (ii == 0) ? 0 : (ii == 2) ? 1 : (jj == 0) ? 2 : 3;
+        int rev = 0;
+        int t = find_object(d, p.block, x, y, z, d.lab.l[1],
+                            face_edge(fi, e) / 4, &rev, nullptr);
+        int incr = 1, start = (jj / 2) * (o - 1) * o;
+        if (ii == 0 || ii == 2) {
+          incr = o;
+          start = (ii / 2) * (o - 1);
+        }
+        for (int k = 1; k < o - 1; k++)
+          out[start + k * incr] = t + (rev ? o - 2 - k : k - 1);
+      } else {
+        int fid = 0;
+        int t = find_object(d, p.block, x, y, z, d.lab.l[2], -1, nullptr, &fid);
+        for (int k = 1; k < o - 1; k++)
+          for (int j = 1; j < o - 1; j++) {
+            int32_t u, v;
+            face_get(fid, o - 1, j, k, u, v);
+            out[j + k * o] = t + (u - 1) + (v - 1) * (o - 2);
+          }
+      }
+    }
+}
+
+__device__ __forceinline__ void lagrange(int order, double u, const double *kn,
+                                         double *N) {
+  for (int i = 0; i < order; i++) {
+    double v = 1.0;
+    for (int j = 0; j < order; j++) {
+      if (i != j) {
+        double dd = 1.0 / __dsub_rn(kn[i], kn[j]);
+        v = __dmul_rn(v, __dmul_rn(__dsub_rn(u, kn[j]), dd));
+      }
+    }
+    N[i] = v;
+  }
+}
+
+// Pass A: which dependent nodes sit on a hanging edge (row length order)
+// or only on a hanging face (order^2).  Pass B: last writer per row, as
+// (element, 0..11 for an edge, 16..21 for a face), which orders writers
+// like the reference's loop (elements, then edges, then faces).
+template <int PASS>
+__global__ void k_dep_rows(long long n, DepCtx d, const int *__restrict__ xs,
+                           const int *__restrict__ ys,
+                           const int *__restrict__ zs,
+                           const int16_t *__restrict__ lev,
+                           const int16_t *__restrict__ info,
+                           const int *__restrict__ lconn, unsigned *has_edge,
+                           unsigned *has_face, const int *__restrict__ dptr,
+                           unsigned long long *writer) {
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  int inf = info[e];
+  if (!inf) return;
+  const int o = d.order;
+  Oct el{0, xs[e], ys[e], zs[e], lev[e]};
+  int id = child_id(el);
+  int fb, eb;
+  decode_info(id, inf, fb, eb);
+  const int *c = lconn + e * (long long)(o * o * o);
+  for (int ei = 0; ei < 12; ei++) {
+    if (!(eb & (1 << ei))) continue;
+    for (int k = 0; k < o; k++) {
+      int di = dep_index(d, c[edge_off(o, ei, k)]);
+      if (di < 0) continue;
+      if (PASS == 0) {
+        has_edge[di] = 1u;
+      } else if (dptr[di + 1] - dptr[di] == o) {
+        atomicMax(writer + di, ((unsigned long long)e << 5) | (unsigned)ei);
+      }
+    }
+  }
+  for (int fi = 0; fi < 6; fi++) {
+    if (!(fb & (1 << fi))) continue;
+    for (int b = 0; b < o; b++)
+      for (int a = 0; a < o; a++) {
+        int di = dep_index(d, c[face_off(o, fi, a, b)]);
+        if (di < 0) continue;
+        if (PASS == 0) {
+          has_face[di] = 1u;
+        } else if (dptr[di + 1] - dptr[di] == o * o) {
+          atomicMax(writer + di, ((unsigned long long)e << 5) | 16u | (unsigned)fi);
+        }
+      }
+  }
+}
+
+__global__ void k_dep_len(long long nd, int o, const unsigned *__restrict__ he,
+                          const unsigned *__restrict__ hf, int *len) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nd) len[i] = he[i] ? o : (hf[i] ? o * o : 0);
+}
+
+__global__ void k_dep_write(long long n, DepCtx d, Knots kn,
+                            const int *__restrict__ blk,
+                            const int *__restrict__ xs,
+                            const int *__restrict__ ys,
+                            const int *__restrict__ zs,
+                            const int16_t *__restrict__ lev,
+                            const int16_t *__restrict__ info,
+                            const int *__restrict__ lconn,
+                            const int *__restrict__ dptr,
+                            const unsigned long long *__restrict__ writer,
+                            int *dconn, double *dw) {
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  int inf = info[e];
+  if (!inf) return;
+  const int o = d.order;
+  Oct el{blk[e], xs[e], ys[e], zs[e], lev[e]};
+  int id = child_id(el);
+  int x = id % 2, y = (id % 4) / 2, z = id / 4;
+  int fb, eb;
+  decode_info(id, inf, fb, eb);
+  Oct p = parent_of(el);
+  const int *c = lconn + e * (long long)(o * o * o);
+  int pn[TMRG_MAX_ORDER * TMRG_MAX_ORDER];
+  double Nu[TMRG_MAX_ORDER], Nv[TMRG_MAX_ORDER];
+  for (int ei = 0; ei < 12; ei++) {
+    if (!(eb & (1 << ei))) continue;
+    bool have = false;
+    unsigned long long me = ((unsigned long long)e << 5) | (unsigned)ei;
+    for (int k = 0; k < o; k++) {
+      int di = dep_index(d, c[edge_off(o, ei, k)]);
+      if (di < 0 || dptr[di + 1] - dptr[di] != o || writer[di] != me) continue;
+      if (!have) {
+        parent_edge_nodes(d, p, ei, pn);
+        have = true;
+      }
+      int ptr = dptr[di];
+      for (int j = 0; j < o; j++) dconn[ptr + j] = pn[j];
+      int sb = (ei < 4) ? x : (ei < 8) ? y : z;
+      double u = __dadd_rn(1.0 * (sb - 1), __dmul_rn(0.5, __dadd_rn(1.0, kn.k[k])));
+      lagrange(o, u, kn.k, &dw[ptr]);
+    }
+  }
+  for (int fi = 0; fi < 6; fi++) {
+    if (!(fb & (1 << fi))) continue;
+    bool have = false;
+    unsigned long long me = ((unsigned long long)e << 5) | 16u | (unsigned)fi;
+    for (int jj = 0; jj < o; jj++)
+      for (int ii = 0; ii < o; ii++) {
+        int di = dep_index(d, c[face_off(o, fi, ii, jj)]);
+        if (di < 0 || dptr[di + 1] - dptr[di] != o * o || writer[di] != me) continue;
+        if (!have) {
+          parent_face_nodes(d, p, fi, pn);
+          have = true;
+        }
+        double u = __dadd_rn(-1.0, __dmul_rn(0.5, __dadd_rn(1.0, kn.k[ii])));
+        double v = __dadd_rn(-1.0, __dmul_rn(0.5, __dadd_rn(1.0, kn.k[jj])));
+        if (fi < 2) {
+          u = __dadd_rn(u, 1.0 * y);
+          v = __dadd_rn(v, 1.0 * z);
+        } else if (fi < 4) {
+          u = __dadd_rn(u, 1.0 * x);
+          v = __dadd_rn(v, 1.0 * z);
+        } else {
+          u = __dadd_rn(u, 1.0 * x);
+          v = __dadd_rn(v, 1.0 * y);
+        }
+        lagrange(o, u, kn.k, Nu);
+        lagrange(o, v, kn.k, Nv);
+        int ptr = dptr[di];
+        for (int j = 0; j < o * o; j++) {
+          dconn[ptr + j] = pn[j];
+          dw[ptr + j] = __dmul_rn(Nu[j % o], Nv[j / o]);
+        }
+      }
+  }
+}
+
+// ---------------------------------------------------------------------
+// Numbering and remap.
+__global__ void k_number(long long nl, const unsigned *__restrict__ flag,
+                         const unsigned *__restrict__ rank, int *num) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nl) return;
+  num[i] = flag[i] ? -(int)rank[i] - 1 : (int)(i - (long long)rank[i]);
+}
+__global__ void k_remap(long long m, const int *__restrict__ num, int *a) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) a[i] = num[a[i]];
+}
+
+void forest_create_nodes(Forest &f) {
+  if (!f.have_octs)
+    throw Error(TMRG_ERR_STATE,
+                "Cannot call createNodes(), no octants have been created");
+  if (f.have_nodes) return;
+  if (f.interp == TMRG_BERNSTEIN_POINTS && f.order >= 3)
+    throw Error(TMRG_ERR_UNSUPPORTED,
+                "createNodes: Bernstein interpolation is not built");
+  cudaStream_t s = f.s;
+  const long long n = f.n;
+  const int o = f.order, npe = o * o * o;
+  ConnDev c = f.conn->dev;
+  OctKey K = f.oct_key();
+
+  // 1. hanging flags
+  {
+    DBuf<uint64_t> okeys(n, s);
+    launch(k_oct_keys, blocks_for(n, 256), 256, 0, s, n, K,
+           (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
+           (const int *)f.z.p, (const int16_t *)f.level.p, okeys.p);
+    launch(k_dep_info, blocks_for(n, 128), 128, 0, s, n, c, K,
+           (const uint64_t *)okeys.p, (const int *)f.block.p, (const int *)f.x.p,
+           (const int *)f.y.p, (const int *)f.z.p, (const int16_t *)f.level.p,
+           f.info.p);
+  }
+
+  // 2. node objects
+  NodeGen g;
+  g.order = o;
+  g.nobj = (o == 2) ? 8 : 27;
+  g.lab = make_labels(o, f.interp);
+  g.NK.Lg = f.maxlev + (o == 2 ? 0 : 1);
+  g.NK.bb = f.conn->block_bits;
+  g.NK.lb = g.lab.bits;
+  if (g.NK.total_bits() > 64)
+    throw Error(TMRG_ERR_KEY_RANGE, "node key needs " +
+                                        std::to_string(g.NK.total_bits()) +
+                                        " bits");
+  const long long m = n * g.nobj;
+  if (m >= (1LL << 32)) throw Error(TMRG_ERR_ARG, "createNodes: too many node objects");
+  DBuf<uint64_t> keys(m, s);
+  DBuf<uint32_t> vals(m, s);
+  launch(k_node_keys, blocks_for(m, 256), 256, 0, s, n, c, g,
+         (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
+         (const int *)f.z.p, (const int16_t *)f.level.p, keys.p, vals.p);
+  radix_sort(keys, &vals, m, g.NK.total_bits(), s);
+  DBuf<unsigned> pos(m + 1, s);
+  launch(k_first_of_run, blocks_for(m, 256), 256, 0, s, m,
+         (const uint64_t *)keys.p, pos.p);
+  exclusive_scan<unsigned>(pos.p, pos.p, m, s);
+  const long long nobj = read_scalar(pos.p + m, s);
+  DBuf<uint64_t> ukeys(nobj, s);
+  DBuf<unsigned> noff(nobj + 1, s);
+  DBuf<unsigned> obj_of(m, s);
+  launch(k_node_unique, blocks_for(m, 256), 256, 0, s, m,
+         (const uint64_t *)keys.p, (const uint32_t *)vals.p,
+         (const unsigned *)pos.p, g.lab.bits, o, ukeys.p, noff.p, obj_of.p);
+  keys.release();
+  vals.release();
+  pos.release();
+  exclusive_scan<unsigned>(noff.p, noff.p, nobj, s);
+  const long long nl = read_scalar(noff.p + nobj, s);
+  f.num_local = nl;
+
+  DBuf<int> lconn((size_t)n * npe, s);
+  launch(k_local_conn, blocks_for(n, 128), 128, 0, s, n, c, g,
+         (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
+         (const int *)f.z.p, (const int16_t *)f.level.p,
+         (const unsigned *)obj_of.p, (const unsigned *)noff.p, lconn.p);
+  obj_of.release();
+
+  // 3. labels and numbering
+  DBuf<unsigned> depflag(nl + 1, s);
+  depflag.zero();
+  launch(k_label_dep, blocks_for(n, 128), 128, 0, s, n, o,
+         (int)(f.interp == TMRG_BERNSTEIN_POINTS), (const int *)f.x.p,
+         (const int *)f.y.p, (const int *)f.z.p, (const int16_t *)f.level.p,
+         (const int16_t *)f.info.p, (const int *)lconn.p, depflag.p);
+  DBuf<unsigned> deprank(nl + 1, s);
+  exclusive_scan<unsigned>(depflag.p, deprank.p, nl, s);
+  const long long nd = read_scalar(deprank.p + nl, s);
+  f.num_dep = nd;
+  f.num_owned = nl - nd;
+  f.ext_pre = nd;
+
+  // 4. dependent CSR
+  DBuf<int> err(1, s);
+  err.zero();
+  DepCtx d;
+  d.order = o;
+  d.lab = g.lab;
+  d.NK = g.NK;
+  d.c = c;
+  d.ukeys = ukeys.p;
+  d.nobj = nobj;
+  d.noff = noff.p;
+  d.deprank = deprank.p;
+  d.depflag = depflag.p;
+  d.err = err.p;
+  DBuf<unsigned> he(nd + 1, s), hf(nd + 1, s);
+  he.zero();
+  hf.zero();
+  f.dep_ptr.alloc(nd + 1, s);
+  launch(k_dep_rows<0>, blocks_for(n, 128), 128, 0, s, n, d, (const int *)f.x.p,
+         (const int *)f.y.p, (const int *)f.z.p, (const int16_t *)f.level.p,
+         (const int16_t *)f.info.p, (const int *)lconn.p, he.p, hf.p,
+         (const int *)nullptr, (unsigned long long *)nullptr);
+  launch(k_dep_len, blocks_for(nd, 256), 256, 0, s, nd, o, (const unsigned *)he.p,
+         (const unsigned *)hf.p, f.dep_ptr.p);
+  exclusive_scan<int>(f.dep_ptr.p, f.dep_ptr.p, nd, s);
+  const long long dnnz = read_scalar(f.dep_ptr.p + nd, s);
+  f.dep_nnz = dnnz;
+  DBuf<unsigned long long> writer(nd + 1, s);
+  writer.zero();
+  launch(k_dep_rows<1>, blocks_for(n, 128), 128, 0, s, n, d, (const int *)f.x.p,
+         (const int *)f.y.p, (const int *)f.z.p, (const int16_t *)f.level.p,
+         (const int16_t *)f.info.p, (const int *)lconn.p, he.p, hf.p,
+         (const int *)f.dep_ptr.p, writer.p);
+  f.dep_conn.alloc(dnnz + 1, s);
+  f.dep_w.alloc(dnnz + 1, s);
+  Knots kn;
+  for (int i = 0; i < TMRG_MAX_ORDER; i++) kn.k[i] = f.knots[i];
+  launch(k_dep_write, blocks_for(n, 128), 128, 0, s, n, d, kn,
+         (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
+         (const int *)f.z.p, (const int16_t *)f.level.p,
+         (const int16_t *)f.info.p, (const int *)lconn.p,
+         (const int *)f.dep_ptr.p, (const unsigned long long *)writer.p,
+         f.dep_conn.p, f.dep_w.p);
+
+  // 5. global numbers
+  DBuf<int> num(nl + 1, s);
+  launch(k_number, blocks_for(nl, 256), 256, 0, s, nl, (const unsigned *)depflag.p,
+         (const unsigned *)deprank.p, num.p);
+  launch(k_remap, blocks_for(n * npe, 256), 256, 0, s, n * npe,
+         (const int *)num.p, lconn.p);
+  launch(k_remap, blocks_for(dnnz, 256), 256, 0, s, dnnz, (const int *)num.p,
+         f.dep_conn.p);
+  if (read_scalar(err.p, s))
+    throw Error(TMRG_ERR_INTERNAL, "createNodes: a parent node was not found");
+  f.econn = std::move(lconn);
+  f.have_nodes = true;
+}
+
+}  // namespace tmrg

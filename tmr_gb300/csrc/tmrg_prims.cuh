@@ -1,0 +1,332 @@
+// Device memory, launch accounting and the data-parallel primitives the
+// octree kernels are built from: exclusive scan and a stable LSD radix
+// sort of 64-bit keys with 32-bit payloads.  Header-only templates.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <utility>
+
+#include "tmrg_common.cuh"
+
+namespace tmrg {
+
+extern std::atomic<long long> g_kernel_launches;
+
+// Launch a kernel on `s`, count it and check the launch.
+template <typename... KArgs, typename... Args>
+inline void launch(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                   cudaStream_t s, Args &&...args) {
+  if (grid.x == 0 || grid.y == 0 || grid.z == 0) return;
+  k<<<grid, block, smem, s>>>(std::forward<Args>(args)...);
+  g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
+  TMRG_CHECK_LAUNCH();
+}
+
+inline unsigned blocks_for(long long n, int per_block) {
+  long long b = (n + per_block - 1) / per_block;
+  return (unsigned)(b > 0 ? b : 0);
+}
+
+// Stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync).
+template <typename T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaStream_t s = 0;
+  DBuf() {}
+  DBuf(size_t count, cudaStream_t st) { alloc(count, st); }
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  DBuf(DBuf &&o) noexcept : p(o.p), n(o.n), s(o.s) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  DBuf &operator=(DBuf &&o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      n = o.n;
+      s = o.s;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void alloc(size_t count, cudaStream_t st) {
+    release();
+    s = st;
+    n = count;
+    if (count) {
+      cudaError_t e = cudaMallocAsync((void **)&p, count * sizeof(T), s);
+      if (e != cudaSuccess) {
+        p = nullptr;
+        n = 0;
+        cudaGetLastError();
+        throw Error(TMRG_ERR_NOMEM, std::string("device allocation of ") +
+                                        std::to_string(count * sizeof(T)) +
+                                        " bytes failed");
+      }
+    }
+  }
+  void release() {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+    n = 0;
+  }
+  void zero() {
+    if (n) TMRG_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+  }
+  void fill_bytes(int v) {
+    if (n) TMRG_CUDA(cudaMemsetAsync(p, v, n * sizeof(T), s));
+  }
+  T *get() const { return p; }
+  void swap(DBuf &o) {
+    std::swap(p, o.p);
+    std::swap(n, o.n);
+    std::swap(s, o.s);
+  }
+};
+
+template <typename T>
+inline T read_scalar(const T *d, cudaStream_t s) {
+  T v;
+  TMRG_CUDA(cudaMemcpyAsync(&v, d, sizeof(T), cudaMemcpyDeviceToHost, s));
+  TMRG_CUDA(cudaStreamSynchronize(s));
+  return v;
+}
+
+// ---------------------------------------------------------------------
+// Exclusive scan: out[i] = sum(in[0..i-1]) for i <= n (out has n+1
+// entries; out[n] is the total).  Tiles of 2048 items, reduce-then-scan.
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+template <typename T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T *warp_tot, T &total) {
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = __shfl_up_sync(0xffffffff, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    T w = (lane < SCAN_THREADS / 32) ? warp_tot[lane] : T(0);
+    T ws = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T y = __shfl_up_sync(0xffffffff, ws, o);
+      if (lane >= o) ws += y;
+    }
+    if (lane < SCAN_THREADS / 32) warp_tot[lane] = ws - w;
+    if (lane == SCAN_THREADS / 32 - 1) warp_tot[SCAN_THREADS / 32] = ws;
+  }
+  __syncthreads();
+  T r = x - v + warp_tot[warp];
+  total = warp_tot[SCAN_THREADS / 32];
+  __syncthreads();
+  return r;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS)
+    k_scan_reduce(const T *__restrict__ in, long long n, T *__restrict__ sums) {
+  __shared__ T red[SCAN_THREADS / 32];
+  long long base = (long long)blockIdx.x * SCAN_TILE;
+  T s = 0;
+  for (int i = threadIdx.x; i < SCAN_TILE; i += SCAN_THREADS) {
+    long long idx = base + i;
+    if (idx < n) s += in[idx];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffff, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T t = 0;
+    for (int w = 0; w < SCAN_THREADS / 32; w++) t += red[w];
+    sums[blockIdx.x] = t;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS)
+    k_scan_down(const T *in, T *out, long long n, const T *__restrict__ offs) {
+  __shared__ T tile[SCAN_TILE];
+  __shared__ T warp_tot[SCAN_THREADS / 32 + 1];
+  long long base = (long long)blockIdx.x * SCAN_TILE;
+  for (int i = threadIdx.x; i < SCAN_TILE; i += SCAN_THREADS) {
+    long long idx = base + i;
+    tile[i] = (idx < n) ? in[idx] : T(0);
+  }
+  __syncthreads();
+  T loc[SCAN_ITEMS];
+  T ts = 0;
+#pragma unroll
+  for (int j = 0; j < SCAN_ITEMS; j++) {
+    loc[j] = tile[threadIdx.x * SCAN_ITEMS + j];
+    ts += loc[j];
+  }
+  T total;
+  T pre = block_exclusive_scan<T>(ts, warp_tot, total);
+  T off = offs ? offs[blockIdx.x] : T(0);
+  pre += off;
+#pragma unroll
+  for (int j = 0; j < SCAN_ITEMS; j++) {
+    tile[threadIdx.x * SCAN_ITEMS + j] = pre;
+    pre += loc[j];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < SCAN_TILE; i += SCAN_THREADS) {
+    long long idx = base + i;
+    if (idx < n) out[idx] = tile[i];
+  }
+  if (threadIdx.x == 0 && base + SCAN_TILE >= n) out[n] = off + total;
+}
+
+// out must hold n+1 elements; `in` may alias `out`.
+template <typename T>
+void exclusive_scan(const T *in, T *out, long long n, cudaStream_t s) {
+  if (n <= 0) {
+    TMRG_CUDA(cudaMemsetAsync(out, 0, sizeof(T), s));
+    return;
+  }
+  unsigned nb = blocks_for(n, SCAN_TILE);
+  if (nb == 1) {
+    launch(k_scan_down<T>, 1, SCAN_THREADS, 0, s, in, out, n, (const T *)nullptr);
+    return;
+  }
+  DBuf<T> sums(nb + 1, s);
+  launch(k_scan_reduce<T>, nb, SCAN_THREADS, 0, s, in, n, sums.p);
+  exclusive_scan<T>(sums.p, sums.p, (long long)nb, s);
+  launch(k_scan_down<T>, nb, SCAN_THREADS, 0, s, in, out, n,
+         (const T *)sums.p);
+}
+
+// ---------------------------------------------------------------------
+// Stable LSD radix sort, 8-bit digits.  Tiles of 4096 keys: 8 warps, each
+// owning a contiguous run of 512 keys read lane-striped.  Ranks inside a
+// warp come from __match_any_sync peer groups in key order, across warps
+// from a per-digit prefix in shared memory, across tiles from a
+// digit-major scan of the tile histograms.
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+
+static __global__ void __launch_bounds__(RS_THREADS)
+    k_radix_hist(const uint64_t *__restrict__ kin, long long n, int shift,
+                 uint32_t *__restrict__ hist, unsigned nblocks) {
+  __shared__ uint32_t wh[RS_THREADS / 32][256];
+  for (int i = threadIdx.x; i < (RS_THREADS / 32) * 256; i += RS_THREADS)
+    (&wh[0][0])[i] = 0;
+  __syncthreads();
+  int warp = threadIdx.x >> 5;
+  long long base = (long long)blockIdx.x * RS_TILE;
+  for (int i = threadIdx.x; i < RS_TILE; i += RS_THREADS) {
+    long long idx = base + i;
+    if (idx < n) atomicAdd(&wh[warp][(uint32_t)(kin[idx] >> shift) & 0xFFu], 1u);
+  }
+  __syncthreads();
+  uint32_t t = 0;
+  for (int w = 0; w < RS_THREADS / 32; w++) t += wh[w][threadIdx.x];
+  hist[(size_t)threadIdx.x * nblocks + blockIdx.x] = t;
+}
+
+template <bool VALS>
+__global__ void __launch_bounds__(RS_THREADS)
+    k_radix_scatter(const uint64_t *__restrict__ kin,
+                    const uint32_t *__restrict__ vin, uint64_t *__restrict__ kout,
+                    uint32_t *__restrict__ vout, long long n, int shift,
+                    const uint32_t *__restrict__ offs, unsigned nblocks) {
+  __shared__ uint32_t wcnt[RS_THREADS / 32][256];
+  for (int i = threadIdx.x; i < (RS_THREADS / 32) * 256; i += RS_THREADS)
+    (&wcnt[0][0])[i] = 0;
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  long long base = (long long)blockIdx.x * RS_TILE + (long long)warp * 32 * RS_ITEMS;
+  uint64_t k[RS_ITEMS];
+  uint32_t v[RS_ITEMS];
+  uint32_t rank[RS_ITEMS];
+#pragma unroll
+  for (int j = 0; j < RS_ITEMS; j++) {
+    long long idx = base + j * 32 + lane;
+    k[j] = (idx < n) ? kin[idx] : 0ULL;
+    if (VALS) v[j] = (idx < n) ? vin[idx] : 0u;
+  }
+#pragma unroll
+  for (int j = 0; j < RS_ITEMS; j++) {
+    long long idx = base + j * 32 + lane;
+    bool ok = idx < n;
+    uint32_t d = ok ? ((uint32_t)(k[j] >> shift) & 0xFFu) : (256u + lane);
+    unsigned peers = __match_any_sync(0xffffffffu, d);
+    int leader = __ffs(peers) - 1;
+    uint32_t b = 0;
+    if (ok && lane == leader) {
+      b = wcnt[warp][d];
+      wcnt[warp][d] = b + __popc(peers);
+    }
+    b = __shfl_sync(0xffffffffu, b, leader);
+    rank[j] = b + __popc(peers & lt);
+    __syncwarp();
+  }
+  __syncthreads();
+  {
+    int d = threadIdx.x;  // one thread per digit
+    uint32_t run = 0;
+    for (int w = 0; w < RS_THREADS / 32; w++) {
+      uint32_t c = wcnt[w][d];
+      wcnt[w][d] = run + offs[(size_t)d * nblocks + blockIdx.x];
+      run += c;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < RS_ITEMS; j++) {
+    long long idx = base + j * 32 + lane;
+    if (idx < n) {
+      uint32_t d = (uint32_t)(k[j] >> shift) & 0xFFu;
+      uint32_t pos = wcnt[warp][d] + rank[j];
+      kout[pos] = k[j];
+      if (VALS) vout[pos] = v[j];
+    }
+  }
+}
+
+// Sorts keys[0..n) (and vals alongside, if given) by bits [0, nbits).
+// Buffers are swapped with internal scratch, so the sorted data ends in
+// `keys`/`vals`.  n < 2^32.
+inline void radix_sort(DBuf<uint64_t> &keys, DBuf<uint32_t> *vals, long long n,
+                       int nbits, cudaStream_t s) {
+  if (n <= 1 || nbits <= 0) return;
+  if (n >= (1LL << 32)) throw Error(TMRG_ERR_ARG, "radix sort size >= 2^32");
+  unsigned nb = blocks_for(n, RS_TILE);
+  DBuf<uint64_t> k2(n, s);
+  DBuf<uint32_t> v2;
+  if (vals) v2.alloc(n, s);
+  DBuf<uint32_t> hist((size_t)256 * nb + 1, s);
+  for (int shift = 0; shift < nbits; shift += 8) {
+    launch(k_radix_hist, nb, RS_THREADS, 0, s, (const uint64_t *)keys.p, n,
+           shift, hist.p, nb);
+    exclusive_scan<uint32_t>(hist.p, hist.p, (long long)256 * nb, s);
+    if (vals)
+      launch(k_radix_scatter<true>, nb, RS_THREADS, 0, s,
+             (const uint64_t *)keys.p, (const uint32_t *)vals->p, k2.p, v2.p, n,
+             shift, (const uint32_t *)hist.p, nb);
+    else
+      launch(k_radix_scatter<false>, nb, RS_THREADS, 0, s,
+             (const uint64_t *)keys.p, (const uint32_t *)nullptr, k2.p,
+             (uint32_t *)nullptr, n, shift, (const uint32_t *)hist.p, nb);
+    keys.swap(k2);
+    if (vals) vals->swap(v2);
+  }
+}
+
+}  // namespace tmrg
