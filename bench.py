@@ -1,0 +1,492 @@
+#!/usr/bin/env python
+"""Benchmark of the octree-forest adaptation path on one GB300 per rank.
+
+Workload (the multi-tree configuration): an 8x4x4 brick of unit hexahedra
+(128 trees), createTrees(2), then 5 passes of refine (each octant with
+probability 0.3, seed 7, max level 9) + balance(corner), createNodes with
+order-3 GLL elements, a 4-level hierarchy (coarsen + balance + createNodes
+three times, createInterpolation per level), and P^T / P applied to 16
+seeded N(0,1) FP64 vectors down and back up the hierarchy.
+
+One step = that whole pipeline from the block connectivity to the last
+prolongation.  Units = balanced and numbered octants of the step (all four
+forests of the hierarchy); value = units / second.  `value` keeps every
+input in HBM (the refinement indicator is drawn on the device); `e2e` runs
+the same pipeline through the host-buffer C ABI calls a TMR user makes
+(refinement arrays and vectors in host memory, octants, connectivity and
+vectors copied back).
+
+--impl reference runs the reference's CPU algorithm for the same path on
+the host cores: the single-rank reference build when it exists, else the
+C restatement in oracle/ (one process per core on independent copies of a
+bounded sample: the first 2 refinement passes of the same workload).
+
+Multi-GPU: replicas only (one independent pipeline per rank, no
+collectives on the data path); the reported time is the max over ranks.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="brick8x4x4_L2_p0.3x5_lvl9_order3_gll_4lvl_16vec",
+                nx=8, ny=4, nz=4, L0=2, passes=5, prob=0.3, seed=7, max_level=9,
+                order=3, levels=4, nvec=16, corner=1)
+CPU_SAMPLE_PASSES = 2
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="tmrg", choices=["tmrg", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--profile-step", action="store_true",
+                   help="run the steps only (for ncu launch lists)")
+    return p.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+# ---------------------------------------------------------------------------
+# GPU pipeline
+def gpu_pipeline(TMR, conn, W, x_fine=None, host=False, prefetched=None):
+    """Returns (units, products).  host=True uses host buffers throughout."""
+    import torch
+    f = TMR.OctForest(order=W["order"], interp=TMR.GAUSS_LOBATTO_POINTS)
+    f.setConnectivity(conn)
+    f.createTrees(W["L0"])
+    h2d = d2h = 0
+    for p in range(W["passes"]):
+        n = f.getNumOctants()
+        if host:
+            r = prefetched["refine"][p][:n]
+            h2d += r.nbytes
+            f.refine(r, 0, W["max_level"])
+        else:
+            f.refine(TMR.random_refinement(n, W["seed"], p, W["prob"]), 0, W["max_level"])
+        f.balance(W["corner"])
+    f.createNodes()
+    forests = [f]
+    for _ in range(W["levels"] - 1):
+        c = forests[-1].coarsen()
+        c.balance(W["corner"])
+        c.createNodes()
+        forests.append(c)
+    interps = []
+    for k in range(W["levels"] - 1):
+        I = TMR.VecInterp()
+        forests[k].createInterpolation(forests[k + 1], I)
+        interps.append(I)
+    units = sum(fr.getNumOctants() for fr in forests)
+    nv = W["nvec"]
+    out = {}
+    if host:
+        x = prefetched["x"]
+        bufs = prefetched["buf"]
+        k = 0
+        for I in interps:  # restriction P^T, fine -> coarse (host buffers)
+            rows, cols, _ = I.sizes()
+            y = bufs[k % 2][: cols * nv]
+            I.multTranspose(x[: rows * nv], y)
+            h2d += rows * nv * 8
+            d2h += cols * nv * 8
+            x, k = y, k + 1
+        for I in reversed(interps):  # prolongation P, coarse -> fine
+            rows, cols, _ = I.sizes()
+            y = bufs[k % 2][: rows * nv]
+            I.mult(x[: cols * nv], y)
+            h2d += cols * nv * 8
+            d2h += rows * nv * 8
+            x, k = y, k + 1
+        octs = f.getOctantsArray()
+        conn_f = f.getMeshConn()
+        d2h += octs.nbytes + conn_f.nbytes
+        out["checksum"] = float(x[:16].sum())
+    else:
+        x = x_fine
+        for I in interps:
+            rows, cols, _ = I.sizes()
+            y = torch.empty(cols * nv, dtype=torch.float64, device="cuda")
+            I.multTranspose(x, y)
+            x = y
+        for I in reversed(interps):
+            rows, cols, _ = I.sizes()
+            y = torch.empty(rows * nv, dtype=torch.float64, device="cuda")
+            I.mult(x, y)
+            x = y
+        out["y"] = x
+    out["forests"] = forests
+    out["interps"] = interps
+    out["h2d"] = h2d
+    out["d2h"] = d2h
+    return units, out
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)),
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": float(max(power)) if power else None}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fp:
+            d = json.load(fp)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_step(TMR, conn, W, x_fine):
+    """One untimed step with per-kernel CUDA-event timing in the library."""
+    L = TMR.lib()
+    L.tmrg_profile_begin()
+    gpu_pipeline(TMR, conn, W, x_fine)
+    buf = ctypes.create_string_buffer(1 << 20)
+    rc = L.tmrg_profile_end(buf, len(buf))
+    if rc != 0:
+        return {}
+    return json.loads(buf.value.decode())
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/ncu_traffic.json), scaled to this workload when recorded
+    for a smaller case."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fp:
+        d = json.load(fp)
+    e = d.get(kernel)
+    if not e:
+        return None
+    return e.get("bytes_per_launch_at_workload")
+
+
+def cpu_sample_case():
+    from tmr_gb300 import workloads as Wk
+    W = WORKLOAD
+    return dict(conn=Wk.brick(W["nx"], W["ny"], W["nz"]), order=W["order"], L0=W["L0"],
+                passes=CPU_SAMPLE_PASSES, max_level=W["max_level"], prob=W["prob"],
+                seed=W["seed"], coarse_levels=W["levels"] - 1, indicator="random")
+
+
+def _cpu_sample_worker(kind):
+    sys.path.insert(0, ROOT)
+    from tests import pipeline
+    case = cpu_sample_case()
+    t0 = time.perf_counter()
+    o = pipeline.run_cpu(case, kind)
+    dt = time.perf_counter() - t0
+    units = len(o["oct"]) + sum(len(lv["oct"]) for lv in o["levels"])
+    return units, dt
+
+
+def cpu_kind():
+    from oracle import oracle
+    return "reference" if oracle.ref_available() else "port"
+
+
+def cpu_baseline_single():
+    """The CPU checker on one core, one bounded sample."""
+    from oracle import build as ob
+    ob.build_oracle()
+    kind = cpu_kind()
+    units, dt = _cpu_sample_worker("ref" if kind == "reference" else "oracle")
+    return {"value": units / dt, "unit": "octants/s", "cores": 1, "kind": kind,
+            "sample": "first %d of 5 refinement passes of the workload (%d balanced+"
+                      "numbered octants over 4 levels), %.1f s" % (CPU_SAMPLE_PASSES, units, dt)}
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from oracle import build as ob
+    ob.build_oracle()
+    kind = cpu_kind()
+    pk = "ref" if kind == "reference" else "oracle"
+    ncores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(ncores) as pool:
+        for _ in range(args.warmup):
+            pool.map(_cpu_sample_worker, [pk] * ncores)
+        t0 = time.perf_counter()
+        tot = 0
+        for _ in range(args.steps):
+            res = pool.map(_cpu_sample_worker, [pk] * ncores)
+            tot += sum(u for u, _ in res)
+        dt = time.perf_counter() - t0
+    value = tot / dt
+    line = {
+        "impl": "reference", "metric": "balanced+numbered octants/s", "value": value,
+        "unit": "octants/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32+f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD["name"],
+                   "sample": "first %d of 5 refinement passes, %d independent copies "
+                             "(one per core)" % (CPU_SAMPLE_PASSES, ncores),
+                   "l2": "working set larger than L2"},
+        "cpu_baseline": {"value": value, "unit": "octants/s", "cores": ncores, "kind": kind,
+                         "sample": "first %d of 5 refinement passes of the workload per core"
+                                   % CPU_SAMPLE_PASSES},
+        "e2e": {"value": value, "unit": "octants/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from tmr_gb300 import TMR
+    from tmr_gb300 import build as tb
+    from tmr_gb300 import workloads as Wk
+    tb.build()
+    W = WORKLOAD
+    conn = Wk.brick(W["nx"], W["ny"], W["nz"])
+
+    # the resident input vectors are sized by the finest forest's nodes
+    n_fine = _size_probe(TMR, conn, W)
+    g = torch.Generator(device="cuda").manual_seed(W["seed"])
+    x_fine = torch.randn(n_fine * W["nvec"], dtype=torch.float64, device="cuda", generator=g)
+    for _ in range(args.warmup):
+        gpu_pipeline(TMR, conn, W, x_fine)
+    torch.cuda.synchronize()
+    if args.profile_step:
+        for _ in range(args.steps):
+            gpu_pipeline(TMR, conn, W, x_fine)
+        torch.cuda.synchronize()
+        return
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.3)
+    barrier()
+    launches0 = TMR.kernel_launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    tot_units = 0
+    for _ in range(args.steps):
+        u, _o = gpu_pipeline(TMR, conn, W, x_fine)
+        tot_units += u
+    ev1.record()
+    barrier()
+    clocks = clk.stop()
+    launches = TMR.kernel_launch_count() - launches0
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = tot_units * world / (ms / 1000.0)
+
+    # e2e through the host-buffer C ABI
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(TMR, conn, W, args, barrier, world, x_fine)
+
+    # roofline of the dominant kernel (separate untimed, event-profiled step)
+    prof = profile_step(TMR, conn, W, x_fine)
+    peak, peak_kind = measured_peaks()
+    roof = None
+    p_apply = None
+    if prof:
+        top = max(prof.items(), key=lambda kv: kv[1][1])
+        name, (nl, tms, tbytes) = top
+        achieved = (tbytes / (tms / 1000.0)) / 1e9 if tbytes and tms else None
+        traffic = ncu_traffic(name)
+        roof = {"bound": "hbm", "kernel": name, "launches": nl,
+                "avg_launch_ms": tms / nl,
+                "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None,
+                "traffic": traffic,
+                "algorithmic_bytes_per_launch": tbytes / nl if tbytes else None,
+                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                "step_share": tms / sum(v[1] for v in prof.values())}
+        if "k_csr_apply" in prof:
+            nl2, tms2, tb2 = prof["k_csr_apply"]
+            gbs = tb2 / (tms2 / 1000.0) / 1e9
+            p_apply = {"kernel": "k_csr_apply", "launches": nl2, "ms": tms2,
+                       "achieved_gbs": gbs, "frac": gbs / peak}
+        kernels = {k: {"launches": v[0], "ms": round(v[1], 4),
+                       "gbs": round(v[2] / (v[1] / 1000.0) / 1e9, 1) if v[2] and v[1] else None}
+                   for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:12]}
+    else:
+        kernels = {}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline_single()
+        except Exception as e:  # the baseline must not sink the line
+            cpu = {"value": None, "unit": "octants/s", "cores": 1, "kind": "port",
+                   "sample": "failed: %s" % e}
+
+    if rank == 0:
+        line = {
+            "metric": "balanced+numbered octants/s", "value": value, "unit": "octants/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic (seeded)",
+            "config": {"workload": W["name"], "trees": W["nx"] * W["ny"] * W["nz"],
+                       "octants_per_step": tot_units // args.steps,
+                       "parallelism": "replicas x%d" % world,
+                       "l2": "working set (GBs) larger than L2; no flush"},
+            "e2e": e2e, "gpu_launches": launches, "roofline": roof, "p_apply": p_apply,
+            "cpu_baseline": cpu, "clocks": clocks, "kernels": kernels,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def _size_probe(TMR, conn, W):
+    """Owned nodes of the finest forest (sizes the resident vectors)."""
+    f = TMR.OctForest(order=W["order"], interp=TMR.GAUSS_LOBATTO_POINTS)
+    f.setConnectivity(conn)
+    f.createTrees(W["L0"])
+    for p in range(W["passes"]):
+        n = f.getNumOctants()
+        f.refine(TMR.random_refinement(n, W["seed"], p, W["prob"]), 0, W["max_level"])
+        f.balance(W["corner"])
+    f.createNodes()
+    return int(f.getNodeRange()[1])
+
+
+def run_e2e(TMR, conn, W, args, barrier, world, x_fine):
+    import torch
+
+    from tmr_gb300 import workloads as Wk
+    # host inputs: per-pass refinement arrays and the fine-level vectors,
+    # in pinned memory (sized from a device run of the same pipeline)
+    sizes = []
+    f = TMR.OctForest(order=W["order"], interp=TMR.GAUSS_LOBATTO_POINTS)
+    f.setConnectivity(conn)
+    f.createTrees(W["L0"])
+    for p in range(W["passes"]):
+        n = f.getNumOctants()
+        sizes.append(n)
+        f.refine(TMR.random_refinement(n, W["seed"], p, W["prob"]), 0, W["max_level"])
+        f.balance(W["corner"])
+    del f
+    pin = lambda n, dt: torch.empty(n, dtype=dt, pin_memory=True).numpy()
+    refine = []
+    for p, n in enumerate(sizes):
+        r = pin(n, torch.int32)
+        r[:] = Wk.random_indicator(n, W["seed"], p, W["prob"])
+        refine.append(r)
+    xh = pin(x_fine.numel(), torch.float64)
+    xh[:] = x_fine.cpu().numpy()
+    buf = [pin(x_fine.numel(), torch.float64), pin(x_fine.numel(), torch.float64)]
+    pre = {"refine": refine, "x": xh, "buf": buf}
+    steps = max(1, min(args.steps, 3))
+    gpu_pipeline(TMR, conn, W, host=True, prefetched=pre)
+    barrier()
+    t0 = time.perf_counter()
+    tot = 0
+    h2d = d2h = 0
+    for _ in range(steps):
+        u, o = gpu_pipeline(TMR, conn, W, host=True, prefetched=pre)
+        tot += u
+        h2d, d2h = o["h2d"], o["d2h"]
+    barrier()
+    dt = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([dt], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dt = float(t.item())
+    return {"value": tot * world / dt, "unit": "octants/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "steps": steps, "ms_per_step": 1000 * dt / steps}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

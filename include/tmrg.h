@@ -187,6 +187,12 @@ int tmrg_random_refinement_device(uint64_t seed, uint64_t stream, double prob,
                                   int *d_out, int64_t n, void *cuda_stream);
 /* Number of kernels this library has launched in this process. */
 int64_t tmrg_kernel_launch_count(void);
+/* Per-kernel timing for benchmarks (no counterpart in the reference, which
+   has no GPU code): between begin and end every launch is bracketed by
+   CUDA events on its stream.  end() writes a JSON object
+   {"kernel": [launches, total_ms, algorithmic_bytes], ...} into json[cap]. */
+int tmrg_profile_begin(void);
+int tmrg_profile_end(char *json, int64_t cap);
 
 #ifdef __cplusplus
 }

@@ -283,9 +283,12 @@ class VecInterp:
         else:
             x = np.ascontiguousarray(x, dtype=np.float64)
             nvec = x.size // max(nin, 1)
-            out = np.zeros(y.shape, np.float64)
+            direct = (isinstance(y, np.ndarray) and y.dtype == np.float64
+                      and y.flags.c_contiguous)
+            out = y if direct else np.zeros(y.shape, np.float64)
             call(names[which], self.ptr, _ptr(x), _ptr(out), nvec)
-            y[...] = out
+            if not direct:
+                y[...] = out
         return y
 
     def mult(self, x, y):

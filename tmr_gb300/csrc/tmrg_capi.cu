@@ -1,7 +1,11 @@
 // The C ABI (include/tmrg.h): status codes in, exceptions never out.
+#include <stdio.h>
 #include <string.h>
 
+#include <map>
+#include <mutex>
 #include <string>
+#include <vector>
 
 #include "tmrg_internal.h"
 
@@ -18,6 +22,32 @@ struct tmrg_filter {
 };
 
 static thread_local std::string g_last_error;
+
+// Per-kernel event timing (tmrg_profile_begin / tmrg_profile_end).
+namespace tmrg {
+struct ProfRec {
+  const char *name;
+  cudaEvent_t a, b;
+  long long bytes;
+};
+static std::mutex g_prof_mu;
+static std::vector<ProfRec> g_prof_recs;
+static std::vector<cudaEvent_t> g_prof_pool;
+static size_t g_prof_next = 0;
+cudaEvent_t prof_event() {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  if (g_prof_next == g_prof_pool.size()) {
+    cudaEvent_t e;
+    TMRG_CUDA(cudaEventCreate(&e));
+    g_prof_pool.push_back(e);
+  }
+  return g_prof_pool[g_prof_next++];
+}
+void prof_push(const char *name, cudaEvent_t a, cudaEvent_t b, long long bytes) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof_recs.push_back({name, a, b, bytes});
+}
+}  // namespace tmrg
 
 template <typename Fn>
 static int guarded(Fn &&fn) {
@@ -53,10 +83,72 @@ const char *tmrg_last_error(void) { return g_last_error.c_str(); }
 const char *tmrg_version(void) { return "tmr_gb300 0.1 (sm_103a)"; }
 int64_t tmrg_kernel_launch_count(void) { return g_kernel_launches.load(); }
 
+int tmrg_profile_begin(void) {
+  return guarded([&] {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_prof_recs.clear();
+    g_prof_next = 0;
+    g_profile_on = true;
+  });
+}
+int tmrg_profile_end(char *json, int64_t cap) {
+  return guarded([&] {
+    g_profile_on = false;
+    TMRG_CUDA(cudaDeviceSynchronize());
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    struct Agg {
+      long long n = 0, bytes = 0;
+      double ms = 0;
+    };
+    std::map<std::string, Agg> agg;
+    for (auto &r : g_prof_recs) {
+      float ms = 0;
+      TMRG_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+      Agg &a = agg[r.name];
+      a.n++;
+      a.ms += ms;
+      a.bytes += r.bytes;
+    }
+    std::string s = "{";
+    bool first = true;
+    for (auto &kv : agg) {
+      char buf[512];
+      snprintf(buf, sizeof buf, "%s\"%s\": [%lld, %.6f, %lld]", first ? "" : ", ",
+               kv.first.c_str(), kv.second.n, kv.second.ms, kv.second.bytes);
+      s += buf;
+      first = false;
+    }
+    s += "}";
+    g_prof_recs.clear();
+    g_prof_next = 0;
+    if (json && cap > 0) {
+      snprintf(json, (size_t)cap, "%s", s.c_str());
+      if ((int64_t)s.size() >= cap) throw Error(TMRG_ERR_ARG, "profile buffer too small");
+    }
+  });
+}
+
+// Keep freed stream-ordered allocations in the device's default pool
+// instead of returning them at every synchronisation: the pipeline
+// allocates and frees GB-sized sort buffers at every step.
+static void keep_pool() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  static thread_local int done_dev = -1;
+  if (done_dev == dev) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done_dev = dev;
+}
+
 int tmrg_forest_create(int order, int interp_type, void *stream,
                        tmrg_forest **out) {
   return guarded([&] {
     ARG(out, "out is NULL");
+    keep_pool();
     ARG(interp_type >= 0 && interp_type <= 2, "bad interpolation type");
     auto *h = new tmrg_forest;
     h->f.s = (cudaStream_t)stream;

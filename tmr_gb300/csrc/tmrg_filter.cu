@@ -227,25 +227,29 @@ __global__ void __launch_bounds__(256)
 }
 
 template <typename T, bool TR>
-static void launch_step(long long n, int vpn, const int *rp, const int *cols,
+static void launch_step(long long n, long long nnz, int vpn, const int *rp, const int *cols,
                         const T *vals, const T *B, const T *t1, const T *x, T *y,
                         const T *post, cudaStream_t s) {
   unsigned g = blocks_for(n, 256);
+  // compulsory traffic of one term: M (value + column), row pointers, B,
+  // t1, one read of x and one write of y (all vpn components)
+  prof_bytes((long long)(sizeof(T) + 4) * nnz + 4 * (n + 1) + (long long)sizeof(T) * n +
+             3LL * sizeof(T) * n * vpn + (post ? (long long)sizeof(T) * n : 0));
   switch (vpn) {
     case 1:
-      launch(k_fe_step<T, 1, TR>, g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
+      launch((k_fe_step<T, 1, TR>), g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
       break;
     case 2:
-      launch(k_fe_step<T, 2, TR>, g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
+      launch((k_fe_step<T, 2, TR>), g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
       break;
     case 3:
-      launch(k_fe_step<T, 3, TR>, g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
+      launch((k_fe_step<T, 3, TR>), g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
       break;
     case 4:
-      launch(k_fe_step<T, 4, TR>, g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
+      launch((k_fe_step<T, 4, TR>), g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
       break;
     default:
-      launch(k_fe_step<T, 0, TR>, g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
+      launch((k_fe_step<T, 0, TR>), g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
   }
 }
 
@@ -271,10 +275,10 @@ static void horner(Filter &F, bool tr, int vpn, const T *in, T *out,
     bool last = (k == F.N - 1);
     T *y = ((F.N - 1 - k) % 2 == 0) ? out : tmp.p;
     if (tr)
-      launch_step<T, true>(n, vpn, F.rowptr.p, F.colidx.p, vals, B, t1.p, x, y,
+      launch_step<T, true>(n, F.nnz, vpn, F.rowptr.p, F.colidx.p, vals, B, t1.p, x, y,
                            last ? post : nullptr, s);
     else
-      launch_step<T, false>(n, vpn, F.rowptr.p, F.colidx.p, vals, B, t1.p, x, y,
+      launch_step<T, false>(n, F.nnz, vpn, F.rowptr.p, F.colidx.p, vals, B, t1.p, x, y,
                             last ? post : nullptr, s);
     x = y;
   }

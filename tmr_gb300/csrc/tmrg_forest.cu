@@ -10,6 +10,8 @@
 namespace tmrg {
 
 std::atomic<long long> g_kernel_launches{0};
+std::atomic<bool> g_profile_on{false};
+thread_local long long g_prof_bytes = 0;
 
 void Forest::set_order(int o, int it) {
   free_nodes();

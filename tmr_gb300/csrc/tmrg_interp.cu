@@ -388,6 +388,12 @@ void interp_apply(Interp &I, int which, const double *x, double *y, int nvec) {
   int G = 1;
   while (G < nvec && G < 32) G <<= 1;
   cudaStream_t s = I.s;
+  // compulsory traffic: 12 B per entry, the row pointers, one read of the
+  // input and one write of the output vectors
+  long long nin = (which == 0) ? I.cols : I.rows;
+  long long nout = (which == 0) ? I.rows : I.cols;
+  prof_bytes(12 * I.nnz + 4 * (nout + 1) + 8LL * nvec * (nin + nout) +
+             (which == 2 ? 8 * nout : 0));
   if (which == 0) {
     long long threads = I.rows * G;
     launch(k_csr_apply, blocks_for(threads, 256), 256, 0, s, I.rows, G, nvec,

@@ -15,15 +15,40 @@ namespace tmrg {
 
 extern std::atomic<long long> g_kernel_launches;
 
-// Launch a kernel on `s`, count it and check the launch.
+// Optional per-kernel timing (tmrg_profile_begin/end): CUDA events recorded
+// on the launching stream around each launch, with the launch's
+// algorithmic byte count when the launch site states one.
+extern std::atomic<bool> g_profile_on;
+extern thread_local long long g_prof_bytes;
+cudaEvent_t prof_event();
+void prof_push(const char *name, cudaEvent_t a, cudaEvent_t b, long long bytes);
+inline void prof_bytes(long long b) { g_prof_bytes = b; }
+
+// Launch a kernel on `s`, count it and check the launch.  Use through the
+// `launch(kernel, grid, block, smem, stream, args...)` macro.
 template <typename... KArgs, typename... Args>
-inline void launch(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
-                   cudaStream_t s, Args &&...args) {
+inline void launch_impl(const char *name, void (*k)(KArgs...), dim3 grid,
+                        dim3 block, size_t smem, cudaStream_t s,
+                        Args &&...args) {
+  long long bytes = g_prof_bytes;
+  g_prof_bytes = 0;
   if (grid.x == 0 || grid.y == 0 || grid.z == 0) return;
+  const bool prof = g_profile_on.load(std::memory_order_relaxed);
+  cudaEvent_t a = nullptr;
+  if (prof) {
+    a = prof_event();
+    TMRG_CUDA(cudaEventRecord(a, s));
+  }
   k<<<grid, block, smem, s>>>(std::forward<Args>(args)...);
   g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
   TMRG_CHECK_LAUNCH();
+  if (prof) {
+    cudaEvent_t b = prof_event();
+    TMRG_CUDA(cudaEventRecord(b, s));
+    prof_push(name, a, b, bytes);
+  }
 }
+#define launch(k, ...) ::tmrg::launch_impl(#k, k, __VA_ARGS__)
 
 inline unsigned blocks_for(long long n, int per_block) {
   long long b = (n + per_block - 1) / per_block;
@@ -313,9 +338,11 @@ inline void radix_sort(DBuf<uint64_t> &keys, DBuf<uint32_t> *vals, long long n,
   if (vals) v2.alloc(n, s);
   DBuf<uint32_t> hist((size_t)256 * nb + 1, s);
   for (int shift = 0; shift < nbits; shift += 8) {
+    prof_bytes(8LL * n);
     launch(k_radix_hist, nb, RS_THREADS, 0, s, (const uint64_t *)keys.p, n,
            shift, hist.p, nb);
     exclusive_scan<uint32_t>(hist.p, hist.p, (long long)256 * nb, s);
+    prof_bytes((vals ? 24LL : 16LL) * n);
     if (vals)
       launch(k_radix_scatter<true>, nb, RS_THREADS, 0, s,
              (const uint64_t *)keys.p, (const uint32_t *)vals->p, k2.p, v2.p, n,
