@@ -62,6 +62,13 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
+def aggregate(ms_local, units_local, world, allreduce_max):
+    """Whole-job throughput of `world` identical replicas: every rank
+    processed `units_local` units; the job took the slowest rank's time."""
+    ms = allreduce_max(ms_local) if world > 1 else ms_local
+    return units_local * world / (ms / 1000.0), ms
+
+
 # ---------------------------------------------------------------------------
 # GPU pipeline
 def gpu_pipeline(TMR, conn, W, x_fine=None, host=False, prefetched=None):
@@ -354,12 +361,12 @@ def run_gpu(args):
     barrier()
     clocks = clk.stop()
     launches = TMR.kernel_launch_count() - launches0
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
+    def allreduce_max(v):
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = tot_units * world / (ms / 1000.0)
+        return float(t.item())
+
+    value, ms = aggregate(ev0.elapsed_time(ev1), tot_units, world, allreduce_max)
 
     # e2e through the host-buffer C ABI
     e2e = None

@@ -2,6 +2,9 @@
 createNodes -> coarsen/balance/createNodes/createInterpolation per level)
 on the GPU library or on a CPU checker, and returns every product as
 numpy arrays so the two can be compared."""
+import json
+import os
+
 import numpy as np
 
 from tmr_gb300 import workloads as W
@@ -118,6 +121,38 @@ def compare(a, b):
         ints("L%d P cols" % k, la["P"][1], lb["P"][1])
         fps("L%d P vals" % k, la["P"][2], lb["P"][2])
     return bad
+
+
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load_golden(name):
+    """Products of the reference itself for parity case `name`
+    (tests/golden/<name>.npz, written by tests/golden/make_golden.py), in
+    the format run_gpu/run_cpu return."""
+    z = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
+    s = z["sizes"]
+    out = dict(oct=z["octants"], conn=z["conn"], nn=z["node_numbers"],
+               dep=(z["dep_ptr"], z["dep_conn"], z["dep_w"]),
+               sizes=dict(num_local=int(s[0]), num_owned=int(s[1]), num_dep=int(s[2]),
+                          ext_pre=int(s[3]), num_elements=int(s[4]), dep_nnz=int(s[5])),
+                   levels=[])
+    k = 0
+    while "L%d_octants" % k in z:
+        out["levels"].append(dict(oct=z["L%d_octants" % k], conn=z["L%d_conn" % k],
+                                  P=(z["L%d_P_rowptr" % k], z["L%d_P_cols" % k],
+                                     z["L%d_P_vals" % k])))
+        k += 1
+    return out
+
+
+def golden_case(name):
+    """The parity case as stored with its fixture (block connectivity
+    included), so the fixture alone defines the input."""
+    z = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
+    case = json.loads(str(z["meta"]))
+    case["conn"] = z["block_conn"]
+    return case
 
 
 # Parity cases, small enough for the checker to finish in seconds.

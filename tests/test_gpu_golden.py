@@ -1,0 +1,21 @@
+"""GPU path vs the golden vectors the reference itself produced
+(tests/golden/*.npz, made by tests/golden/make_golden.py from the
+reference's own TMROctant.cpp/TMROctForest.cpp/TMRBase.cpp): bit-exact
+integers, 1e-13 relative FP64, no CPU code in the loop."""
+import os
+
+import pytest
+
+from tests import pipeline
+
+CASES = sorted(f[:-4] for f in os.listdir(pipeline.GOLDEN_DIR) if f.endswith(".npz"))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_gpu_matches_reference_golden(gpu_lib, name):
+    case = pipeline.golden_case(name)
+    g = pipeline.run_gpu(case)
+    ref = pipeline.load_golden(name)
+    bad = pipeline.compare(g, ref)
+    assert not bad, "\n".join(bad)

@@ -1,0 +1,65 @@
+"""The CPU oracle (oracle/tmr_oracle.c) pinned against the golden vectors
+the reference itself produced (tests/golden/*.npz): octants, element
+connectivity, node numbering and dependent-node CSR bit-exact, weights and
+P within 1e-13."""
+import os
+
+import numpy as np
+import pytest
+
+from tests import pipeline
+
+CASES = sorted(f[:-4] for f in os.listdir(pipeline.GOLDEN_DIR) if f.endswith(".npz"))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_matches_reference_golden(name):
+    case = pipeline.golden_case(name)
+    g = pipeline.load_golden(name)
+    o = pipeline.run_cpu(case, "oracle")
+    bad = pipeline.compare(o, g)
+    assert not bad, "\n".join(bad)
+
+
+def test_golden_cases_are_the_parity_cases():
+    # the fixture inputs are exactly the seeded parity cases
+    allc = pipeline.cases()
+    for name in CASES:
+        c = pipeline.golden_case(name)
+        np.testing.assert_array_equal(c["conn"], allc[name]["conn"])
+        for k, v in allc[name].items():
+            if k != "conn":
+                assert c[k] == v, (name, k)
+
+
+def test_golden_properties():
+    # size-independent identities of the reference's own output
+    for name in CASES:
+        g = pipeline.load_golden(name)
+        s = g["sizes"]
+        nn = g["nn"]
+        assert np.array_equal(nn, np.concatenate([np.arange(-s["num_dep"], 0),
+                                                   np.arange(s["num_owned"])]))
+        assert g["conn"].min() >= -s["num_dep"] and g["conn"].max() < s["num_owned"]
+        # dependent weights interpolate constants exactly
+        ptr, _, w = g["dep"]
+        sums = np.add.reduceat(w, ptr[:-1]) if len(w) else np.zeros(0)
+        np.testing.assert_allclose(sums, 1.0, rtol=1e-13)
+        # octants sorted, tags are indices
+        o = g["oct"]
+        assert np.array_equal(o[:, 4], np.arange(len(o)))
+        for lv in g["levels"]:
+            rp, cols, vals = lv["P"]
+            rs = np.add.reduceat(vals, rp[:-1])
+            np.testing.assert_allclose(rs, 1.0, rtol=1e-12)  # P 1 = 1
+
+
+@pytest.mark.skipif(not __import__("oracle.oracle", fromlist=["x"]).ref_available(),
+                    reason="reference sources not built here")
+@pytest.mark.parametrize("name", sorted(pipeline.cases()))
+def test_oracle_matches_live_reference(name):
+    case = pipeline.cases()[name]
+    a = pipeline.run_cpu(case, "oracle")
+    b = pipeline.run_cpu(case, "ref")
+    bad = pipeline.compare(a, b)
+    assert not bad, "\n".join(bad)

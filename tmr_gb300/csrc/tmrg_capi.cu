@@ -167,10 +167,13 @@ int tmrg_forest_set_connectivity(tmrg_forest *f, int num_nodes,
                                  const int *block_conn, int num_blocks) {
   return guarded([&] {
     ARG(f && block_conn, "NULL argument");
+    // validate and build first: a rejected connectivity leaves the forest
+    // as it was
+    auto c = build_conn(num_nodes, block_conn, num_blocks, f->f.s);
     f->f.free_nodes();
     f->f.have_octs = false;
     f->f.n = 0;
-    f->f.conn = build_conn(num_nodes, block_conn, num_blocks, f->f.s);
+    f->f.conn = c;
   });
 }
 int tmrg_forest_set_mesh_order(tmrg_forest *f, int order, int interp_type) {

@@ -16,8 +16,12 @@
 
 namespace tmrg {
 
+// Knots and the reciprocals 1/(k_i - k_j) (rounded once on the host, as
+// the reference rounds them), so the device Lagrange basis needs no FP64
+// division.
 struct Knots {
   double k[TMRG_MAX_ORDER];
+  double r[TMRG_MAX_ORDER][TMRG_MAX_ORDER];
 };
 
 // Labels distinguish node objects at one position for order > 3
@@ -346,6 +350,7 @@ struct DepCtx {
   ConnDev c;
   const uint64_t *ukeys;
   long long nobj;
+  SampledKeys idx;
   const unsigned *noff;
   const unsigned *deprank;  // exclusive scan of dependent flags
   const unsigned *depflag;
@@ -363,7 +368,7 @@ __device__ __forceinline__ int find_object(const DepCtx &d, int32_t b, int32_t x
                                            int edge_dir, int *rev, int *fid) {
   transform_node(d.c, b, x, y, z, edge_dir, rev, fid);
   uint64_t k = d.NK.make(b, x, y, z, label);
-  long long i = lower_bound_u64(d.ukeys, d.nobj, k);
+  long long i = d.idx.lower_bound(k);
   if (i >= d.nobj || d.ukeys[i] != k) {
     atomicExch(d.err, 1);
     return 0;
@@ -462,15 +467,12 @@ __device__ void parent_face_nodes(const DepCtx &d, const Oct &p, int fi,
     }
 }
 
-__device__ __forceinline__ void lagrange(int order, double u, const double *kn,
+__device__ __forceinline__ void lagrange(int order, double u, const Knots &kn,
                                          double *N) {
   for (int i = 0; i < order; i++) {
     double v = 1.0;
     for (int j = 0; j < order; j++) {
-      if (i != j) {
-        double dd = 1.0 / __dsub_rn(kn[i], kn[j]);
-        v = __dmul_rn(v, __dmul_rn(__dsub_rn(u, kn[j]), dd));
-      }
+      if (i != j) v = __dmul_rn(v, __dmul_rn(__dsub_rn(u, kn.k[j]), kn.r[i][j]));
     }
     N[i] = v;
   }
@@ -478,8 +480,10 @@ __device__ __forceinline__ void lagrange(int order, double u, const double *kn,
 
 // Pass A: which dependent nodes sit on a hanging edge (row length order)
 // or only on a hanging face (order^2).  Pass B: last writer per row, as
-// (element, 0..11 for an edge, 16..21 for a face), which orders writers
-// like the reference's loop (elements, then edges, then faces).
+// (element+1) << 11 | (0..11 for an edge, 16..21 for a face) << 6 | position of
+// the node on that edge/face; the maximum is the writer the reference's
+// sequential loop (elements, then edges, then faces) leaves in place, and
+// the position tells the row kernel which node of the edge/face it is.
 template <int PASS>
 __global__ void k_dep_rows(long long n, DepCtx d, const int *__restrict__ xs,
                            const int *__restrict__ ys,
@@ -507,7 +511,7 @@ __global__ void k_dep_rows(long long n, DepCtx d, const int *__restrict__ xs,
       if (PASS == 0) {
         has_edge[di] = 1u;
       } else if (dptr[di + 1] - dptr[di] == o) {
-        atomicMax(writer + di, ((unsigned long long)e << 5) | (unsigned)ei);
+        atomicMax(writer + di, ((unsigned long long)(e + 1) << 11) | ((unsigned)ei << 6) | (unsigned)k);
       }
     }
   }
@@ -520,7 +524,8 @@ __global__ void k_dep_rows(long long n, DepCtx d, const int *__restrict__ xs,
         if (PASS == 0) {
           has_face[di] = 1u;
         } else if (dptr[di + 1] - dptr[di] == o * o) {
-          atomicMax(writer + di, ((unsigned long long)e << 5) | 16u | (unsigned)fi);
+          atomicMax(writer + di, ((unsigned long long)(e + 1) << 11) |
+                                     ((16u + (unsigned)fi) << 6) | (unsigned)(a + b * o));
         }
       }
   }
@@ -543,70 +548,46 @@ __global__ void k_dep_write(long long n, DepCtx d, Knots kn,
                             const int *__restrict__ dptr,
                             const unsigned long long *__restrict__ writer,
                             int *dconn, double *dw) {
-  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n) return;
-  int inf = info[e];
-  if (!inf) return;
+  // One thread per dependent node: its winning writer (element, edge or
+  // face, position) fixes the parent edge/face whose nodes form the row.
+  long long di = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (di >= n) return;
   const int o = d.order;
+  unsigned long long w = writer[di];
+  if (w == 0ULL) return;  // no writer: the row has length 0
+  long long e = (long long)(w >> 11) - 1;
+  int sub = (int)((w >> 6) & 31), pos = (int)(w & 63);
   Oct el{blk[e], xs[e], ys[e], zs[e], lev[e]};
   int id = child_id(el);
   int x = id % 2, y = (id % 4) / 2, z = id / 4;
-  int fb, eb;
-  decode_info(id, inf, fb, eb);
   Oct p = parent_of(el);
-  const int *c = lconn + e * (long long)(o * o * o);
-  int pn[TMRG_MAX_ORDER * TMRG_MAX_ORDER];
-  double Nu[TMRG_MAX_ORDER], Nv[TMRG_MAX_ORDER];
-  for (int ei = 0; ei < 12; ei++) {
-    if (!(eb & (1 << ei))) continue;
-    bool have = false;
-    unsigned long long me = ((unsigned long long)e << 5) | (unsigned)ei;
-    for (int k = 0; k < o; k++) {
-      int di = dep_index(d, c[edge_off(o, ei, k)]);
-      if (di < 0 || dptr[di + 1] - dptr[di] != o || writer[di] != me) continue;
-      if (!have) {
-        parent_edge_nodes(d, p, ei, pn);
-        have = true;
-      }
-      int ptr = dptr[di];
-      for (int j = 0; j < o; j++) dconn[ptr + j] = pn[j];
-      int sb = (ei < 4) ? x : (ei < 8) ? y : z;
-      double u = __dadd_rn(1.0 * (sb - 1), __dmul_rn(0.5, __dadd_rn(1.0, kn.k[k])));
-      lagrange(o, u, kn.k, &dw[ptr]);
+  int ptr = dptr[di];
+  if (dptr[di + 1] - ptr != (sub < 16 ? o : o * o)) return;
+  if (sub < 16) {
+    int ei = sub, k = pos;
+    parent_edge_nodes(d, p, ei, dconn + ptr);
+    int sb = (ei < 4) ? x : (ei < 8) ? y : z;
+    double u = __dadd_rn(1.0 * (sb - 1), __dmul_rn(0.5, __dadd_rn(1.0, kn.k[k])));
+    lagrange(o, u, kn, &dw[ptr]);
+  } else {
+    int fi = sub - 16, ii = pos % o, jj = pos / o;
+    parent_face_nodes(d, p, fi, dconn + ptr);
+    double u = __dadd_rn(-1.0, __dmul_rn(0.5, __dadd_rn(1.0, kn.k[ii])));
+    double v = __dadd_rn(-1.0, __dmul_rn(0.5, __dadd_rn(1.0, kn.k[jj])));
+    if (fi < 2) {
+      u = __dadd_rn(u, 1.0 * y);
+      v = __dadd_rn(v, 1.0 * z);
+    } else if (fi < 4) {
+      u = __dadd_rn(u, 1.0 * x);
+      v = __dadd_rn(v, 1.0 * z);
+    } else {
+      u = __dadd_rn(u, 1.0 * x);
+      v = __dadd_rn(v, 1.0 * y);
     }
-  }
-  for (int fi = 0; fi < 6; fi++) {
-    if (!(fb & (1 << fi))) continue;
-    bool have = false;
-    unsigned long long me = ((unsigned long long)e << 5) | 16u | (unsigned)fi;
-    for (int jj = 0; jj < o; jj++)
-      for (int ii = 0; ii < o; ii++) {
-        int di = dep_index(d, c[face_off(o, fi, ii, jj)]);
-        if (di < 0 || dptr[di + 1] - dptr[di] != o * o || writer[di] != me) continue;
-        if (!have) {
-          parent_face_nodes(d, p, fi, pn);
-          have = true;
-        }
-        double u = __dadd_rn(-1.0, __dmul_rn(0.5, __dadd_rn(1.0, kn.k[ii])));
-        double v = __dadd_rn(-1.0, __dmul_rn(0.5, __dadd_rn(1.0, kn.k[jj])));
-        if (fi < 2) {
-          u = __dadd_rn(u, 1.0 * y);
-          v = __dadd_rn(v, 1.0 * z);
-        } else if (fi < 4) {
-          u = __dadd_rn(u, 1.0 * x);
-          v = __dadd_rn(v, 1.0 * z);
-        } else {
-          u = __dadd_rn(u, 1.0 * x);
-          v = __dadd_rn(v, 1.0 * y);
-        }
-        lagrange(o, u, kn.k, Nu);
-        lagrange(o, v, kn.k, Nv);
-        int ptr = dptr[di];
-        for (int j = 0; j < o * o; j++) {
-          dconn[ptr + j] = pn[j];
-          dw[ptr + j] = __dmul_rn(Nu[j % o], Nv[j / o]);
-        }
-      }
+    double Nu[TMRG_MAX_ORDER], Nv[TMRG_MAX_ORDER];
+    lagrange(o, u, kn, Nu);
+    lagrange(o, v, kn, Nv);
+    for (int j = 0; j < o * o; j++) dw[ptr + j] = __dmul_rn(Nu[j % o], Nv[j / o]);
   }
 }
 
@@ -718,6 +699,12 @@ void forest_create_nodes(Forest &f) {
   d.c = c;
   d.ukeys = ukeys.p;
   d.nobj = nobj;
+  const int S = 6;
+  const long long ntop = (nobj + (1LL << S) - 1) >> S;
+  DBuf<uint64_t> top(ntop, s);
+  launch(k_sample_keys, blocks_for(ntop, 256), 256, 0, s, ntop, S,
+         (const uint64_t *)ukeys.p, top.p);
+  d.idx = SampledKeys{ukeys.p, nobj, top.p, ntop, S};
   d.noff = noff.p;
   d.deprank = deprank.p;
   d.depflag = depflag.p;
@@ -744,8 +731,12 @@ void forest_create_nodes(Forest &f) {
   f.dep_conn.alloc(dnnz + 1, s);
   f.dep_w.alloc(dnnz + 1, s);
   Knots kn;
-  for (int i = 0; i < TMRG_MAX_ORDER; i++) kn.k[i] = f.knots[i];
-  launch(k_dep_write, blocks_for(n, 128), 128, 0, s, n, d, kn,
+  for (int i = 0; i < TMRG_MAX_ORDER; i++) {
+    kn.k[i] = f.knots[i];
+    for (int j = 0; j < TMRG_MAX_ORDER; j++)
+      kn.r[i][j] = (i != j && i < o && j < o) ? 1.0 / (f.knots[i] - f.knots[j]) : 0.0;
+  }
+  launch(k_dep_write, blocks_for(nd, 128), 128, 0, s, nd, d, kn,
          (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
          (const int *)f.z.p, (const int16_t *)f.level.p,
          (const int16_t *)f.info.p, (const int *)lconn.p,

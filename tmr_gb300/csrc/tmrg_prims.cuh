@@ -265,7 +265,7 @@ static __global__ void __launch_bounds__(RS_THREADS)
 }
 
 template <bool VALS>
-__global__ void __launch_bounds__(RS_THREADS)
+__global__ void __launch_bounds__(RS_THREADS, 2)
     k_radix_scatter(const uint64_t *__restrict__ kin,
                     const uint32_t *__restrict__ vin, uint64_t *__restrict__ kout,
                     uint32_t *__restrict__ vout, long long n, int shift,
@@ -303,24 +303,59 @@ __global__ void __launch_bounds__(RS_THREADS)
     __syncwarp();
   }
   __syncthreads();
+  // Per digit (one thread each): prefix over warps, the tile's digit
+  // offsets (block scan) and the digit's global base for this tile.
+  __shared__ uint32_t tile_off[256];
+  __shared__ uint32_t gbase[256];
+  __shared__ uint32_t scan_tmp[RS_THREADS / 32 + 1];
+  __shared__ uint64_t stage[RS_TILE];
+  __shared__ uint8_t stage_d[RS_TILE];
   {
-    int d = threadIdx.x;  // one thread per digit
+    int d = threadIdx.x;
     uint32_t run = 0;
     for (int w = 0; w < RS_THREADS / 32; w++) {
       uint32_t c = wcnt[w][d];
-      wcnt[w][d] = run + offs[(size_t)d * nblocks + blockIdx.x];
+      wcnt[w][d] = run;
       run += c;
     }
+    uint32_t total;
+    uint32_t off = block_exclusive_scan<uint32_t>(run, scan_tmp, total);
+    tile_off[d] = off;
+    gbase[d] = offs[(size_t)d * nblocks + blockIdx.x];
   }
   __syncthreads();
+  long long tile_base = (long long)blockIdx.x * RS_TILE;
+  int cnt = (int)min((long long)RS_TILE, n - tile_base);
+  // Stage keys in tile order of their digit, then write each digit's run
+  // contiguously.
 #pragma unroll
   for (int j = 0; j < RS_ITEMS; j++) {
     long long idx = base + j * 32 + lane;
     if (idx < n) {
       uint32_t d = (uint32_t)(k[j] >> shift) & 0xFFu;
-      uint32_t pos = wcnt[warp][d] + rank[j];
-      kout[pos] = k[j];
-      if (VALS) vout[pos] = v[j];
+      uint32_t tp = tile_off[d] + wcnt[warp][d] + rank[j];
+      rank[j] = tp;
+      stage[tp] = k[j];
+      stage_d[tp] = (uint8_t)d;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < cnt; i += RS_THREADS) {
+    uint32_t d = stage_d[i];
+    kout[gbase[d] + (i - tile_off[d])] = stage[i];
+  }
+  if (VALS) {
+    __syncthreads();
+    uint32_t *vstage = reinterpret_cast<uint32_t *>(stage);
+#pragma unroll
+    for (int j = 0; j < RS_ITEMS; j++) {
+      long long idx = base + j * 32 + lane;
+      if (idx < n) vstage[rank[j]] = v[j];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt; i += RS_THREADS) {
+      uint32_t d = stage_d[i];
+      vout[gbase[d] + (i - tile_off[d])] = vstage[i];
     }
   }
 }

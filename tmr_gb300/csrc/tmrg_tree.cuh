@@ -270,4 +270,44 @@ __device__ __forceinline__ bool contains_u64(const uint64_t *a, long long n,
   return i < n && a[i] == v;
 }
 
+// Two-level search over a large sorted array: `top` samples every
+// 2^S-th key (small enough to stay in L2), so a lookup touches the big
+// array only inside one 2^S-key segment.
+struct SampledKeys {
+  const uint64_t *keys;
+  long long n;
+  const uint64_t *top;
+  long long ntop;
+  int S;
+  __device__ __forceinline__ long long lower_bound(uint64_t v) const {
+    // last sample <= v
+    long long lo = 0, hi = ntop;
+    while (lo < hi) {
+      long long mid = (lo + hi) >> 1;
+      if (__ldg(top + mid) <= v)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    long long seg = lo - 1;
+    if (seg < 0) return 0;
+    long long a = seg << S, b = min(n, (seg + 1) << S);
+    while (a < b) {
+      long long mid = (a + b) >> 1;
+      if (__ldg(keys + mid) < v)
+        a = mid + 1;
+      else
+        b = mid;
+    }
+    return a;
+  }
+};
+
+static __global__ void k_sample_keys(long long ntop, int S,
+                                     const uint64_t *__restrict__ keys,
+                                     uint64_t *top) {
+  long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < ntop) top[j] = keys[j << S];
+}
+
 }  // namespace tmrg
