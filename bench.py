@@ -54,7 +54,13 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--profile-step", action="store_true",
                    help="run the steps only (for ncu launch lists)")
-    return p.parse_args()
+    p.add_argument("--max-level", type=int, default=None,
+                   help="smaller variant of the workload for ncu captures")
+    a = p.parse_args()
+    if a.max_level is not None:
+        WORKLOAD["max_level"] = a.max_level
+        WORKLOAD["name"] = WORKLOAD["name"].replace("lvl9", "lvl%d" % a.max_level)
+    return a
 
 
 def dist_env():

@@ -165,13 +165,65 @@ __device__ __forceinline__ void dir_weights(const InterpCtx &I, int i, int32_t n
 // the run in order (TMRIndexWeight::uniqueSort, TMRBase.h:103-130).
 constexpr int IW_WARPS = 4;
 
-template <bool WRITE>
+// Pass 1 (bound): findEnclosing per row, kept in `trow`, and an upper bound
+// of the row's entries (sum of the box nodes' expansions) in `bound`.
+__global__ void k_interp_bound(long long rows, InterpCtx I, int *trow,
+                               long long *bound) {
+  long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= rows) return;
+  const int mo = I.fo, co = I.co, fnpe = mo * mo * mo;
+  unsigned long long r = I.rep[row];
+  long long e = (long long)(r / fnpe);
+  int info = (int)(r - (unsigned long long)e * fnpe);
+  Oct node{I.fb[e], I.fx[e], I.fy[e], I.fz[e], I.fl[e]};
+  long long t = find_enclosing(I, node, info);
+  trow[row] = (int)t;
+  long long ne = 0;
+  if (t < 0) {
+    atomicExch(I.err, 1);
+  } else {
+    // the box of coarse nodes the row touches (computeElemInterp's
+    // istart..iend per direction), expanded through the dependent rows
+    int4 cq = __ldg(I.c4 + t);
+    int32_t h = side_of(node.level), hc = side_of(cq.x >> 26);
+    int i = info % mo, j = (info % (mo * mo)) / mo, k = info / (mo * mo);
+    int rs[3], re[3];
+    const int ijk[3] = {i, j, k};
+    const int32_t nx[3] = {node.x, node.y, node.z}, ox[3] = {cq.y, cq.z, cq.w};
+    for (int d = 0; d < 3; d++) {
+      int a = ijk[d];
+      if ((a == 0 && ox[d] == nx[d]) || (a == mo - 1 && ox[d] == nx[d] + h)) {
+        rs[d] = 0;
+        re[d] = 1;
+      } else if ((a == 0 && ox[d] + hc == nx[d]) || (a == mo - 1 && ox[d] + hc == nx[d] + h)) {
+        rs[d] = co - 1;
+        re[d] = co;
+      } else {
+        rs[d] = 0;
+        re[d] = co;
+      }
+    }
+    const int *c = I.cconn + t * (long long)(co * co * co);
+    for (int kk = rs[2]; kk < re[2]; kk++)
+      for (int jj = rs[1]; jj < re[1]; jj++)
+        for (int ii = rs[0]; ii < re[0]; ii++) {
+          int cv = __ldg(c + ii + jj * co + kk * co * co);
+          ne += (cv >= 0) ? 1 : (__ldg(I.cdptr - cv) - __ldg(I.cdptr - cv - 1));
+        }
+  }
+  bound[row] = ne;
+}
+
+// Pass 2: the rows, written merged at the bound offsets of a scratch
+// buffer; cnt[row] = merged length.
 __global__ void __launch_bounds__(IW_WARPS * 32)
-    k_interp_rows(long long rows, InterpCtx I, const long long *__restrict__ rowptr64,
-                  int *cnt, int *cols, double *vals) {
+    k_interp_rows(long long rows, InterpCtx I, const int *__restrict__ trow,
+                  const long long *__restrict__ toff, int *cnt, int *cols,
+                  double *vals) {
   __shared__ int s_col[IW_WARPS][IMAX_W];
   __shared__ double s_w[IW_WARPS][IMAX_W];
   __shared__ short s_ord[IW_WARPS][IMAX_W];
+  const bool WRITE = true;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const long long base = ((long long)blockIdx.x * IW_WARPS + warp) * 32;
@@ -188,7 +240,7 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
       long long e = (long long)(r / fnpe);
       int info = (int)(r - (unsigned long long)e * fnpe);
       Oct node{I.fb[e], I.fx[e], I.fy[e], I.fz[e], I.fl[e]};
-      t = find_enclosing(I, node, info);
+      t = trow[row];
       if (t >= 0) {
         int i = info % mo, j = (info % (mo * mo)) / mo, k = info / (mo * mo);
         int4 cq = __ldg(I.c4 + t);
@@ -219,7 +271,7 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
       nw[a] = __shfl_sync(0xffffffffu, Nw[a], q);
     }
     if (tq < 0) {
-      if (!WRITE && lane == 0) cnt[row] = 0;
+      if (lane == 0) cnt[row] = 0;
       continue;
     }
     int is = bq & 3, ie = (bq >> 2) & 3, js = (bq >> 4) & 3, je = (bq >> 6) & 3,
@@ -270,7 +322,7 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
     __syncwarp();
     // merge runs of equal columns
     int run = 0;
-    long long rp = WRITE ? rowptr64[row] : 0;
+    long long rp = toff[row];
     for (int c0 = 0; c0 < ne; c0 += 32) {
       int sidx = c0 + lane;
       bool head = false;
@@ -290,11 +342,26 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
       }
       run += __popc(hm);
     }
-    if (!WRITE && lane == 0) cnt[row] = run;
+    if (lane == 0) cnt[row] = run;
     __syncwarp();
   }
 }
 
+// 8 lanes per row copy a merged row from scratch into the CSR.
+__global__ void k_interp_compact(long long rows, const long long *__restrict__ toff,
+                                 const long long *__restrict__ rp,
+                                 const int *__restrict__ tc, const double *__restrict__ tv,
+                                 int *cols, double *vals) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long r = t >> 3;
+  if (r >= rows) return;
+  int lane = (int)(t & 7);
+  long long s0 = toff[r], d0 = rp[r], n = rp[r + 1] - d0;
+  for (long long k = lane; k < n; k += 8) {
+    cols[d0 + k] = tc[s0 + k];
+    vals[d0 + k] = tv[s0 + k];
+  }
+}
 __global__ void k_ptr32(long long n, const long long *__restrict__ in, int *out) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i <= n) out[i] = (int)in[i];
@@ -408,9 +475,18 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
                         ? 1.0 / (coarse.knots[i] - coarse.knots[j])
                         : 0.0;
   const unsigned rblocks = blocks_for(rows, IW_WARPS * 32);
+  // pass 1: enclosing octants and entry bounds; pass 2: merged rows into
+  // scratch at the bound offsets; pass 3: compact into the CSR
+  DBuf<int> trow(rows + 1, s);
+  DBuf<long long> toff(rows + 1, s);
+  launch(k_interp_bound, blocks_for(rows, 128), 128, 0, s, rows, c, trow.p, toff.p);
+  exclusive_scan<long long>(toff.p, toff.p, rows, s);
+  const long long nbound = read_scalar(toff.p + rows, s);
+  DBuf<int> tcols(nbound + 1, s);
+  DBuf<double> tvals(nbound + 1, s);
   DBuf<int> cnt(rows + 1, s);
-  launch(k_interp_rows<false>, rblocks, IW_WARPS * 32, 0, s, rows, c,
-         (const long long *)nullptr, cnt.p, (int *)nullptr, (double *)nullptr);
+  launch(k_interp_rows, rblocks, IW_WARPS * 32, 0, s, rows, c, (const int *)trow.p,
+         (const long long *)toff.p, cnt.p, tcols.p, tvals.p);
   DBuf<long long> rp64(rows + 1, s);
   launch(k_widen, blocks_for(rows, 256), 256, 0, s, rows, (const int *)cnt.p,
          rp64.p);
@@ -424,8 +500,9 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
          (const long long *)rp64.p, I.rowptr.p);
   I.colidx.alloc(nnz + 1, s);
   I.vals.alloc(nnz + 1, s);
-  launch(k_interp_rows<true>, rblocks, IW_WARPS * 32, 0, s, rows, c,
-         (const long long *)rp64.p, (int *)nullptr, I.colidx.p, I.vals.p);
+  launch(k_interp_compact, blocks_for(rows * 8, 256), 256, 0, s, rows,
+         (const long long *)toff.p, (const long long *)rp64.p, (const int *)tcols.p,
+         (const double *)tvals.p, I.colidx.p, I.vals.p);
   if (read_scalar(err.p, s))
     throw Error(TMRG_ERR_INTERNAL,
                 "createInterpolation: a fine node has no enclosing coarse octant");
@@ -527,10 +604,77 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Split-row form: NG groups of LPR lanes share one row (RPW = 32/(LPR*NG)
+// rows per warp); group g takes entries g, g+NG, ...  The warp runs one
+// trip count (the longest row it holds) with per-entry predicates, so no
+// lane diverges: on GB300 the FP64 pipe is the bound and a diverged or
+// half-masked warp instruction costs the pipe as much as a full one.
+// Group partial sums are combined in a fixed tree order.
+template <int LPR, int NG>
+__global__ void __launch_bounds__(256)
+    k_csr_apply_split(long long rows, int nvec2, const int *__restrict__ rowptr,
+                      const int *__restrict__ cols, const double *__restrict__ vals,
+                      const double2 *__restrict__ x, double2 *__restrict__ y,
+                      const double *__restrict__ scale) {
+  constexpr int RPW = 32 / (LPR * NG);
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int sub = lane / (LPR * NG);       // row slot in the warp
+  const int g = (lane / LPR) % NG;         // group in the row
+  const int v = lane % LPR;                // vector pair
+  const long long r = warp * RPW + sub;
+  if (warp * RPW >= rows) return;          // uniform per warp
+  const bool have = r < rows;
+  const int p0 = have ? __ldg(rowptr + r) : 0;
+  const int p1 = have ? __ldg(rowptr + r + 1) : 0;
+  int trips = (p1 - p0 + NG - 1) / NG;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) trips = max(trips, __shfl_xor_sync(0xffffffffu, trips, o));
+  for (int vb = 0; vb < nvec2; vb += LPR) {
+    const bool act = have && (vb + v < nvec2);
+    double ax = 0.0, ay = 0.0;
+#pragma unroll 4
+    for (int t = 0; t < trips; t++) {
+      int p = p0 + g + t * NG;
+      bool on = act && p < p1;
+      int c = on ? __ldg(cols + p) : 0;
+      double w = on ? __ldg(vals + p) : 0.0;
+      double2 xv = on ? __ldg(x + (long long)c * nvec2 + vb + v) : make_double2(0.0, 0.0);
+      ax = __fma_rn(w, xv.x, ax);
+      ay = __fma_rn(w, xv.y, ay);
+    }
+#pragma unroll
+    for (int o = (NG / 2) * LPR; o >= LPR; o >>= 1) {
+      ax = __dadd_rn(ax, __shfl_down_sync(0xffffffffu, ax, o));
+      ay = __dadd_rn(ay, __shfl_down_sync(0xffffffffu, ay, o));
+    }
+    if (act && g == 0) {
+      if (scale) {
+        double sc = scale[r];
+        ax = (sc != 0.0) ? __ddiv_rn(ax, sc) : 0.0;
+        ay = (sc != 0.0) ? __ddiv_rn(ay, sc) : 0.0;
+      }
+      y[r * nvec2 + vb + v] = make_double2(ax, ay);
+    }
+  }
+}
+
 template <int LPR>
-static void apply2(long long rows, int nvec2, const int *rp, const int *ci,
-                   const double *v, const double *x, double *y,
+static void apply2(long long rows, long long nnz, int nvec2, const int *rp,
+                   const int *ci, const double *v, const double *x, double *y,
                    const double *scale, cudaStream_t s) {
+  // long rows (P^T): the whole warp on one row; short rows (P): two rows
+  // per warp when the lanes allow
+  double avg = rows ? (double)nnz / (double)rows : 0.0;
+  if (LPR == 8) {
+    if (avg >= 48)
+      launch((k_csr_apply_split<8, 4>), blocks_for(rows * 32, 256), 256, 0, s, rows,
+             nvec2, rp, ci, v, (const double2 *)x, (double2 *)y, scale);
+    else
+      launch((k_csr_apply_split<8, 2>), blocks_for((rows + 1) / 2 * 32, 256), 256, 0, s,
+             rows, nvec2, rp, ci, v, (const double2 *)x, (double2 *)y, scale);
+    return;
+  }
   launch(k_csr_apply2<LPR>, blocks_for(rows * LPR, 256), 256, 0, s, rows, nvec2,
          rp, ci, v, (const double2 *)x, (double2 *)y, scale);
 }
@@ -549,13 +693,13 @@ void interp_apply(Interp &I, int which, const double *x, double *y, int nvec) {
     const double *sc = which == 2 ? I.colsum.p : nullptr;
     int n2 = nvec / 2;
     if (n2 >= 8)
-      apply2<8>(nout, n2, rp, ci, v, x, y, sc, s);
+      apply2<8>(nout, I.nnz, n2, rp, ci, v, x, y, sc, s);
     else if (n2 >= 4)
-      apply2<4>(nout, n2, rp, ci, v, x, y, sc, s);
+      apply2<4>(nout, I.nnz, n2, rp, ci, v, x, y, sc, s);
     else if (n2 >= 2)
-      apply2<2>(nout, n2, rp, ci, v, x, y, sc, s);
+      apply2<2>(nout, I.nnz, n2, rp, ci, v, x, y, sc, s);
     else
-      apply2<1>(nout, n2, rp, ci, v, x, y, sc, s);
+      apply2<1>(nout, I.nnz, n2, rp, ci, v, x, y, sc, s);
     return;
   }
   int G = 1;
