@@ -179,6 +179,19 @@ int tmrg_filter_apply_f32_device(tmrg_filter *F, int vpn, const float *in,
 int tmrg_filter_apply_transpose_f32_device(tmrg_filter *F, int vpn,
                                            const float *in, float *out);
 
+/* Allocation-free form of tmrg_filter_apply_device (transpose != 0 gives
+   the applyTranspose form).  No counterpart in the reference: it exists
+   for callers that cannot allocate device memory where they filter (a
+   framework whose allocator owns the GPU's memory, or code that must not
+   call cudaMalloc/cudaFree because they can synchronise the device).  Its
+   work vectors live in a static 16 MiB device array, so nodes x vpn must
+   not exceed 1048576 (TMRG_ERR_ARG otherwise).  The first call on a device
+   looks the array up (call it before any stream capture); calls that
+   overlap on the GPU race on the shared array.  Device pointers; runs on
+   the filter's stream; allocates nothing. */
+int tmrg_filter_apply_static_device(tmrg_filter *F, int transpose, int vpn,
+                                    const double *in, double *out);
+
 /* ---- utilities -------------------------------------------------------- */
 /* Seeded refinement indicator used by the synthetic workloads:
    out[i] = (U(seed, stream, i) < prob) ? 1 : 0, with U the splitmix64

@@ -66,6 +66,7 @@ _SIGS = {
     "tmrg_filter_apply_transpose_device": [c_vp, c_int, c_vp, c_vp],
     "tmrg_filter_apply_f32_device": [c_vp, c_int, c_vp, c_vp],
     "tmrg_filter_apply_transpose_f32_device": [c_vp, c_int, c_vp, c_vp],
+    "tmrg_filter_apply_static_device": [c_vp, c_int, c_int, c_vp, c_vp],
     "tmrg_random_refinement_device": [c_u64, c_u64, c_dbl, c_vp, c_i64, c_vp],
 }
 _RESTYPE = {

@@ -557,6 +557,14 @@ int tmrg_filter_apply_transpose_f32_device(tmrg_filter *F, int vpn,
   });
 }
 
+int tmrg_filter_apply_static_device(tmrg_filter *F, int transpose, int vpn,
+                                    const double *in, double *out) {
+  return guarded([&] {
+    ARG(F && in && out && vpn > 0, "bad argument");
+    filter_apply_static(F->F, transpose != 0, vpn, in, out);
+  });
+}
+
 int tmrg_random_refinement_device(uint64_t seed, uint64_t stream, double prob,
                                   int *d_out, int64_t n, void *cuda_stream) {
   return guarded([&] {

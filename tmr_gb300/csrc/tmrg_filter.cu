@@ -12,6 +12,9 @@
 // Apply: Horner's recurrence out = B.(M out) + t1 (forward) or
 // out = M(B.out) + t1 (transpose), one fused CSR kernel per term over all
 // `vpn` interleaved design components, so M is read once per term.
+#include <mutex>
+#include <string>
+
 #include "tmrg_tree.cuh"
 
 namespace tmrg {
@@ -294,6 +297,78 @@ void filter_apply(Filter &F, bool tr, int vpn, const double *in, double *out) {
 void filter_apply_f32(Filter &F, bool tr, int vpn, const float *in, float *out) {
   horner<float>(F, tr, vpn, in, out, F.vals32.p, F.Ainv32.p, F.B32.p,
                 F.Tinv32.p);
+}
+
+// ---------------------------------------------------------------------
+// Allocation-free apply.  Some callers cannot allocate device memory at
+// the point where they filter: a framework whose caching allocator owns
+// the GPU's memory, or a section that must not call cudaMalloc/cudaFree
+// because those can synchronise the device.  This variant takes its two
+// Horner work vectors (t1 and the ping-pong term) from a static device
+// array instead of the stream-ordered pool.
+//
+// The array holds 2 x FILTER_STATIC_MAX doubles (16 MiB) and stays
+// resident on every GPU that loads the library until the process exits.
+// Every call shares it and it keeps the last call's contents; nothing in
+// it has to start at zero (each call writes t1 and every Horner term in
+// full before reading them).  Calls that overlap on the GPU (different
+// streams, or different filters sharing a device) race on the array.
+constexpr long long FILTER_STATIC_MAX = 1LL << 20;
+static __device__ __align__(256) double g_filter_static[2 * FILTER_STATIC_MAX];
+
+// Device address of the array on the current device, looked up once per
+// device: in host code `g_filter_static` names a host-side stand-in, not
+// device memory.  The first call on a device performs the lookup, so it
+// should come before any stream capture.
+static double *filter_static_scratch() {
+  static std::mutex mu;
+  static double *addr[256] = {nullptr};
+  int dev = 0;
+  TMRG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) throw Error(TMRG_ERR_ARG, "device ordinal out of range");
+  std::lock_guard<std::mutex> lk(mu);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_filter_static);
+    if (e != cudaSuccess)
+      throw Error(TMRG_ERR_CUDA, std::string("cudaGetSymbolAddress(filter scratch): ") +
+                                     cudaGetErrorString(e));
+    addr[dev] = (double *)p;
+  }
+  return addr[dev];
+}
+
+void filter_apply_static(Filter &F, bool tr, int vpn, const double *in, double *out) {
+  const long long n = F.n, len = n * vpn;
+  if (len > FILTER_STATIC_MAX)
+    throw Error(TMRG_ERR_ARG,
+                "allocation-free filter apply: " + std::to_string(len) +
+                    " values (nodes x vpn) exceed the static scratch limit of " +
+                    std::to_string(FILTER_STATIC_MAX));
+  double *t1 = filter_static_scratch();
+  double *tmp = t1 + FILTER_STATIC_MAX;
+  if (n == 0) return;
+  cudaStream_t s = F.s;
+  const double *pre = tr ? F.Tinv.p : F.Ainv.p;
+  const double *post = tr ? F.Ainv.p : F.Tinv.p;
+  launch(k_fe_scale<double>, blocks_for(len, 256), 256, 0, s, n, vpn, pre, in, t1);
+  if (F.N == 0) {
+    launch(k_fe_scale<double>, blocks_for(len, 256), 256, 0, s, n, vpn, post,
+           (const double *)t1, out);
+    return;
+  }
+  const double *x = t1;
+  for (int k = 0; k < F.N; k++) {
+    bool last = (k == F.N - 1);
+    double *y = ((F.N - 1 - k) % 2 == 0) ? out : tmp;
+    if (tr)
+      launch_step<double, true>(n, F.nnz, vpn, F.rowptr.p, F.colidx.p, F.vals.p,
+                                F.B.p, t1, x, y, last ? post : nullptr, s);
+    else
+      launch_step<double, false>(n, F.nnz, vpn, F.rowptr.p, F.colidx.p, F.vals.p,
+                                 F.B.p, t1, x, y, last ? post : nullptr, s);
+    x = y;
+  }
 }
 
 void filter_create(Forest &f, double len, double r, int N, Filter &F) {

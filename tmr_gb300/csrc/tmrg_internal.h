@@ -112,6 +112,8 @@ void filter_apply(Filter &F, bool transpose, int vpn, const double *in,
                   double *out);
 void filter_apply_f32(Filter &F, bool transpose, int vpn, const float *in,
                       float *out);
+void filter_apply_static(Filter &F, bool transpose, int vpn, const double *in,
+                         double *out);
 void random_refinement(uint64_t seed, uint64_t stream, double prob, int *out,
                        long long n, cudaStream_t s);
 
