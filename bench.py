@@ -52,11 +52,18 @@ def parse():
     p.add_argument("--impl", default="tmrg", choices=["tmrg", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-filter", action="store_true",
+                   help="skip the filter -> P chain measurement")
     p.add_argument("--profile-step", action="store_true",
                    help="run the steps only (for ncu launch lists)")
     p.add_argument("--max-level", type=int, default=None,
                    help="smaller variant of the workload for ncu captures")
+    p.add_argument("--passes", type=int, default=None,
+                   help="fewer refinement passes: a smaller case for ncu captures")
     a = p.parse_args()
+    if a.passes is not None:
+        WORKLOAD["passes"] = a.passes
+        WORKLOAD["name"] = WORKLOAD["name"].replace("x5_", "x%d_" % a.passes)
     if a.max_level is not None:
         WORKLOAD["max_level"] = a.max_level
         WORKLOAD["name"] = WORKLOAD["name"].replace("lvl9", "lvl%d" % a.max_level)
@@ -228,6 +235,31 @@ def profile_step(TMR, conn, W, x_fine):
     return json.loads(buf.value.decode())
 
 
+def roofline_entry(name, v, peak, peak_kind, fp64_peak, tot_ms):
+    """Roofline of one kernel from its event profile [launches, ms, bytes,
+    flops]: FP64-pipe bound when its FP64 rate is the larger fraction of
+    its peak, else HBM bound."""
+    nl, tms, tbytes, tflops = v
+    gbs = tbytes / (tms / 1e3) / 1e9 if tbytes and tms else None
+    tfs = tflops / (tms / 1e3) / 1e12 if tflops and tms else None
+    hbm_frac = gbs / peak if gbs else None
+    fp_frac = tfs / fp64_peak if tfs and fp64_peak else None
+    traffic = ncu_traffic(name)
+    e = {"kernel": name, "launches": nl, "avg_launch_ms": tms / nl,
+         "algorithmic_bytes_per_launch": tbytes / nl if tbytes else None,
+         "traffic": traffic, "step_share": tms / tot_ms,
+         "hbm_achieved_gbs": gbs, "hbm_frac": hbm_frac}
+    if fp_frac is not None and (hbm_frac is None or fp_frac > hbm_frac):
+        e.update({"bound": "fp64", "achieved": tfs, "peak": fp64_peak, "unit": "TFLOP/s",
+                  "frac": fp_frac,
+                  "peak_source": "measured live (tmrg_measure_fp64_peak: FP64 FMA chains)"})
+    else:
+        e.update({"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                  "frac": hbm_frac,
+                  "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind})
+    return e
+
+
 def ncu_traffic(kernel):
     """DRAM bytes per launch of `kernel` from the committed ncu summary
     (profiles/ncu_traffic.json), scaled to this workload when recorded
@@ -382,31 +414,40 @@ def run_gpu(args):
     # roofline of the dominant kernel (separate untimed, event-profiled step)
     prof = profile_step(TMR, conn, W, x_fine)
     peak, peak_kind = measured_peaks()
+    fp64 = ctypes.c_double(0.0)
+    TMR.lib().tmrg_measure_fp64_peak(ctypes.byref(fp64))
+    fp64_peak = fp64.value  # TFLOP/s, measured live
     roof = None
     p_apply = None
+    kernels = {}
     if prof:
+        tot_ms = sum(v[1] for v in prof.values())
         top = max(prof.items(), key=lambda kv: kv[1][1])
-        name, (nl, tms, tbytes) = top
-        achieved = (tbytes / (tms / 1000.0)) / 1e9 if tbytes and tms else None
-        traffic = ncu_traffic(name)
-        roof = {"bound": "hbm", "kernel": name, "launches": nl,
-                "avg_launch_ms": tms / nl,
-                "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": (achieved / peak) if achieved else None,
-                "traffic": traffic,
-                "algorithmic_bytes_per_launch": tbytes / nl if tbytes else None,
-                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                "step_share": tms / sum(v[1] for v in prof.values())}
-        if "k_csr_apply" in prof:
-            nl2, tms2, tb2 = prof["k_csr_apply"]
-            gbs = tb2 / (tms2 / 1000.0) / 1e9
-            p_apply = {"kernel": "k_csr_apply", "launches": nl2, "ms": tms2,
-                       "achieved_gbs": gbs, "frac": gbs / peak}
-        kernels = {k: {"launches": v[0], "ms": round(v[1], 4),
-                       "gbs": round(v[2] / (v[1] / 1000.0) / 1e9, 1) if v[2] and v[1] else None}
-                   for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:12]}
-    else:
-        kernels = {}
+        roof = roofline_entry(top[0], top[1], peak, peak_kind, fp64_peak, tot_ms)
+        apply = [(k, v) for k, v in prof.items() if "csr_apply" in k]
+        if apply:
+            nl2 = sum(v[0] for _, v in apply)
+            tms2 = sum(v[1] for _, v in apply)
+            tb2 = sum(v[2] for _, v in apply)
+            tf2 = sum(v[3] for _, v in apply)
+            p_apply = {"kernels": [k for k, _ in apply], "launches": nl2, "ms": tms2,
+                       "achieved_gbs": tb2 / (tms2 / 1e3) / 1e9,
+                       "hbm_frac": tb2 / (tms2 / 1e3) / 1e9 / peak,
+                       "achieved_tflops": tf2 / (tms2 / 1e3) / 1e12,
+                       "fp64_frac": tf2 / (tms2 / 1e3) / 1e12 / fp64_peak,
+                       "bound": "fp64 (2 flops per 12 B of matrix; GB300 FP64 %.2f TFLOP/s)"
+                                % fp64_peak}
+        for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:14]:
+            kernels[k] = {"launches": v[0], "ms": round(v[1], 4), "share": round(v[1] / tot_ms, 4),
+                          "gbs": round(v[2] / (v[1] / 1e3) / 1e9, 1) if v[2] and v[1] else None,
+                          "tflops": round(v[3] / (v[1] / 1e3) / 1e12, 3) if v[3] and v[1] else None}
+
+    chain = None
+    if rank == 0 and not args.no_filter:
+        try:
+            chain = filter_chain_metrics(TMR)
+        except Exception as e:
+            chain = {"failed": str(e)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -427,6 +468,7 @@ def run_gpu(args):
                        "parallelism": "replicas x%d" % world,
                        "l2": "working set (GBs) larger than L2; no flush"},
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "p_apply": p_apply,
+            "filter_chain": chain,
             "cpu_baseline": cpu, "clocks": clocks, "kernels": kernels,
         }
         print(json.dumps(line), flush=True)
@@ -445,6 +487,124 @@ def _size_probe(TMR, conn, W):
         f.balance(W["corner"])
     f.createNodes()
     return int(f.getNodeRange()[1])
+
+
+FILTER_WORKLOAD = dict(name="brick16x8x8_16bumps_sigma0.05_order2_r2h_N10_vpn3",
+                       nx=16, ny=8, nz=8, L0=2, bumps=16, seed=3, sigma=0.05,
+                       target=20_000_000, max_level=9, vpn=3, N=10)
+
+
+def build_filter_chain(TMR, FW):
+    """The differentiable-filter configuration: a 16x8x8 brick refined near
+    16 seeded Gaussian bumps (sigma = 0.05 domain lengths) to ~20M octants
+    (order 2); the filter forest is its coarsened forest; P maps it to the
+    finest forest.  Returns (fine, coarse, interp, filter, r)."""
+    import torch
+
+    from tmr_gb300 import workloads as Wk
+    nx, ny, nz = FW["nx"], FW["ny"], FW["nz"]
+    L = torch.tensor([nx, ny, nz], dtype=torch.float64, device="cuda")
+    cen = torch.tensor(Wk.uniform(FW["seed"], 0, 3 * FW["bumps"]).reshape(-1, 3),
+                       device="cuda") * L
+    sig = FW["sigma"] * L
+    f = TMR.OctForest(order=2, interp=TMR.GAUSS_LOBATTO_POINTS)
+    f.setConnectivity(Wk.brick(nx, ny, nz))
+    f.createTrees(FW["L0"])
+    for _ in range(12):
+        n = f.getNumOctants()
+        if n >= FW["target"]:
+            break
+        o = f.getOctantsDevice()
+        b = o["block"].long()
+        org = torch.stack([b % nx, (b // nx) % ny, b // (nx * ny)], 1).double()
+        lev = o["level"].long()
+        h = torch.pow(2.0, (30 - lev).double())
+        xyz = torch.stack([o["x"], o["y"], o["z"]], 1).double()
+        c = org + (xyz + 0.5 * h[:, None]) / 2.0 ** 30
+        val = torch.zeros(n, dtype=torch.float64, device="cuda")
+        for k in range(cen.shape[0]):
+            val += torch.exp(-0.5 * (((c - cen[k]) / sig) ** 2).sum(1))
+        val[lev >= FW["max_level"]] = -1.0
+        # refine the octants nearest the bumps, as many as take the forest
+        # to about the target size (balance adds ~30%)
+        k = int(min(n, max(1, (FW["target"] - n) / 7 / 1.3)))
+        thr = torch.topk(val, k).values[-1]
+        flags = ((val >= thr) & (val > 0)).int()
+        f.refine(flags, 0, FW["max_level"])
+        f.balance(1)
+    f.createNodes()
+    coarse = f.coarsen()
+    coarse.balance(1)
+    coarse.createNodes()
+    I = TMR.VecInterp()
+    f.createInterpolation(coarse, I)
+    hmin = 1.0 / 2.0 ** int(f.getOctantsDevice()["level"].max().item())
+    r = 2.0 * hmin
+    F = TMR.MatrixFilter(r, FW["N"], None, [coarse], block_len=1.0, vpn=FW["vpn"])
+    return f, coarse, I, F, r
+
+
+def filter_chain_metrics(TMR, steps=5):
+    """Forward + adjoint of filter -> P on 3 design components: time per
+    chain, algorithmic GB/s of the filter and P applies (library profile),
+    and the FP32 filter's error against FP64."""
+    import torch
+    FW = FILTER_WORKLOAD
+    fine, coarse, I, F, r = build_filter_chain(TMR, FW)
+    n, nnz_m = F.size()
+    rows, cols, nnz_p = I.sizes()
+    vpn = FW["vpn"]
+    g = torch.Generator(device="cuda").manual_seed(FW["seed"])
+    x = torch.rand(n * vpn, dtype=torch.float64, device="cuda", generator=g)
+    w = torch.rand(rows * vpn, dtype=torch.float64, device="cuda", generator=g)
+    rho = torch.empty_like(x)
+    y = torch.empty(rows * vpn, dtype=torch.float64, device="cuda")
+    gp = torch.empty_like(x)
+    gx = torch.empty_like(x)
+
+    def chain():
+        F.applyFilter(x, rho, vpn)
+        I.mult(rho, y)
+        gy = 3.0 * w * y * y
+        I.multTranspose(gy, gp)
+        F.applyTranspose(gp, gx, vpn)
+
+    for _ in range(3):
+        chain()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        chain()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    L = TMR.lib()
+    L.tmrg_profile_begin()
+    chain()
+    buf = ctypes.create_string_buffer(1 << 20)
+    L.tmrg_profile_end(buf, len(buf))
+    prof = json.loads(buf.value.decode())
+    fb = sum(v[2] for k, v in prof.items() if k.startswith("(k_fe_step") or k.startswith("k_fe_scale"))
+    fms = sum(v[1] for k, v in prof.items() if k.startswith("(k_fe_step") or k.startswith("k_fe_scale"))
+    pb = sum(v[2] for k, v in prof.items() if "csr_apply" in k)
+    pms = sum(v[1] for k, v in prof.items() if "csr_apply" in k)
+    peak, _ = measured_peaks()
+    x32 = x.float()
+    r32 = torch.empty_like(x32)
+    F.applyFilter(x32, r32, vpn)
+    err32 = float((r32.double() - rho).abs().max() / rho.abs().max())
+    return {
+        "workload": FW["name"], "octants": fine.getNumOctants(),
+        "filter_octants": coarse.getNumOctants(), "filter_nodes": n, "M_nnz": nnz_m,
+        "P_nnz": nnz_p, "r": r, "ms_per_chain": ms,
+        "filter_gbs": fb / (fms / 1e3) / 1e9 if fms else None,
+        "filter_frac": (fb / (fms / 1e3) / 1e9) / peak if fms else None,
+        "p_gbs": pb / (pms / 1e3) / 1e9 if pms else None,
+        "chain_gbs": (fb + pb) / (ms / 1e3) / 1e9,
+        "chain_frac": ((fb + pb) / (ms / 1e3) / 1e9) / peak,
+        "fp32_filter_rel_err": err32,
+    }
 
 
 def run_e2e(TMR, conn, W, args, barrier, world, x_fine):

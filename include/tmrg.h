@@ -203,9 +203,14 @@ int64_t tmrg_kernel_launch_count(void);
 /* Per-kernel timing for benchmarks (no counterpart in the reference, which
    has no GPU code): between begin and end every launch is bracketed by
    CUDA events on its stream.  end() writes a JSON object
-   {"kernel": [launches, total_ms, algorithmic_bytes], ...} into json[cap]. */
+   {"kernel": [launches, total_ms, algorithmic_bytes, flops], ...} into
+   json[cap]. */
 int tmrg_profile_begin(void);
 int tmrg_profile_end(char *json, int64_t cap);
+/* FP64 FMA throughput of the current GPU in TFLOP/s (independent FMA
+   chains, ~20 ms): the roofline denominator for FP64-pipe-bound kernels.
+   No counterpart in the reference. */
+int tmrg_measure_fp64_peak(double *tflops);
 
 #ifdef __cplusplus
 }

@@ -73,3 +73,17 @@ def test_empty_and_edge_inputs(gpu_lib):
     f.refine(np.full(8, 40, np.intc), 0, 2)
     o = f.getOctantsArray()
     assert o[:, 5].max() == 2
+
+
+@pytest.mark.gpu
+def test_device_octant_views_match_host_copy(gpu_lib):
+    from tmr_gb300 import TMR
+    f = TMR.OctForest(order=2)
+    f.setConnectivity(W.brick(2, 2, 1))
+    f.createTrees(2)
+    f.refine(TMR.random_refinement(f.getNumOctants(), 5, 0, 0.4), 0, 5)
+    f.balance(1)
+    d = f.getOctantsDevice()
+    h = f.getOctantsArray()
+    for k, col in (("block", 0), ("x", 1), ("y", 2), ("z", 3), ("level", 5), ("info", 6)):
+        assert np.array_equal(d[k].cpu().numpy().astype(np.int64), h[:, col].astype(np.int64)), k

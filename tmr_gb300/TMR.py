@@ -31,6 +31,15 @@ def _is_torch(a):
     return type(a).__module__.startswith("torch")
 
 
+class _DeviceArray:
+    """Exposes a borrowed device pointer through __cuda_array_interface__."""
+
+    def __init__(self, ptr, n, typestr):
+        self.__cuda_array_interface__ = {
+            "shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 3,
+            "strides": None}
+
+
 class Octant:
     """TMROctant value (TMROctant.h:36-54)."""
 
@@ -175,6 +184,21 @@ class OctForest:
 
     def getOctants(self):
         return OctantArray(self.getOctantsArray())
+
+    def getOctantsDevice(self):
+        """Borrowed CUDA torch views of the octant arrays (block, x, y, z as
+        int32; level, info as int16), valid until the next mutating call."""
+        import torch
+        n = self.getNumOctants()
+        ptrs = [_vp() for _ in range(6)]
+        call("tmrg_forest_octants_device", self.ptr, *[ctypes.byref(p) for p in ptrs])
+        names = ("block", "x", "y", "z", "level", "info")
+        types = ("<i4", "<i4", "<i4", "<i4", "<i2", "<i2")
+        out = {}
+        for name, p, t in zip(names, ptrs, types):
+            out[name] = torch.as_tensor(_DeviceArray(p.value or 0, n, t), device="cuda")
+        out["_owner"] = self
+        return out
 
     # -- nodes ---------------------------------------------------------
     def _sizes(self):

@@ -23,6 +23,7 @@ _SIGS = {
     "tmrg_kernel_launch_count": [],
     "tmrg_profile_begin": [],
     "tmrg_profile_end": [c_vp, c_i64],
+    "tmrg_measure_fp64_peak": [P(c_dbl)],
     "tmrg_forest_create": [c_int, c_int, c_vp, P(c_vp)],
     "tmrg_forest_destroy": [c_vp],
     "tmrg_forest_set_connectivity": [c_vp, c_int, c_vp, c_int],

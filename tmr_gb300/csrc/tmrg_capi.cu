@@ -28,7 +28,7 @@ namespace tmrg {
 struct ProfRec {
   const char *name;
   cudaEvent_t a, b;
-  long long bytes;
+  long long bytes, flops;
 };
 static std::mutex g_prof_mu;
 static std::vector<ProfRec> g_prof_recs;
@@ -43,9 +43,10 @@ cudaEvent_t prof_event() {
   }
   return g_prof_pool[g_prof_next++];
 }
-void prof_push(const char *name, cudaEvent_t a, cudaEvent_t b, long long bytes) {
+void prof_push(const char *name, cudaEvent_t a, cudaEvent_t b, long long bytes,
+               long long flops) {
   std::lock_guard<std::mutex> lk(g_prof_mu);
-  g_prof_recs.push_back({name, a, b, bytes});
+  g_prof_recs.push_back({name, a, b, bytes, flops});
 }
 }  // namespace tmrg
 
@@ -83,6 +84,49 @@ const char *tmrg_last_error(void) { return g_last_error.c_str(); }
 const char *tmrg_version(void) { return "tmr_gb300 0.1 (sm_103a)"; }
 int64_t tmrg_kernel_launch_count(void) { return g_kernel_launches.load(); }
 
+// FP64 FMA throughput of the current device: 8 independent FMA chains per
+// thread over a grid of 8 blocks per SM; the denominator of the roofline of
+// FP64-pipe-bound kernels (no measured FP64 figure exists).
+__global__ void k_fp64_peak(double *out, int iters, double a, double b) {
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4,
+         x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; i++) {
+    x0 = __fma_rn(x0, a, b);
+    x1 = __fma_rn(x1, a, b);
+    x2 = __fma_rn(x2, a, b);
+    x3 = __fma_rn(x3, a, b);
+    x4 = __fma_rn(x4, a, b);
+    x5 = __fma_rn(x5, a, b);
+    x6 = __fma_rn(x6, a, b);
+    x7 = __fma_rn(x7, a, b);
+  }
+  out[(long long)blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+int tmrg_measure_fp64_peak(double *tflops) {
+  return guarded([&] {
+    ARG(tflops, "NULL argument");
+    int dev = 0, sms = 0;
+    TMRG_CUDA(cudaGetDevice(&dev));
+    TMRG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    DBuf<double> out((size_t)blocks * threads, 0);
+    cudaEvent_t e0, e1;
+    TMRG_CUDA(cudaEventCreate(&e0));
+    TMRG_CUDA(cudaEventCreate(&e1));
+    launch(k_fp64_peak, blocks, threads, 0, 0, out.p, 16, 0.999, 0.001);
+    TMRG_CUDA(cudaEventRecord(e0, 0));
+    launch(k_fp64_peak, blocks, threads, 0, 0, out.p, iters, 0.999, 0.001);
+    TMRG_CUDA(cudaEventRecord(e1, 0));
+    TMRG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    TMRG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *tflops = 2.0 * 8 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+  });
+}
+
 int tmrg_profile_begin(void) {
   return guarded([&] {
     std::lock_guard<std::mutex> lk(g_prof_mu);
@@ -97,7 +141,7 @@ int tmrg_profile_end(char *json, int64_t cap) {
     TMRG_CUDA(cudaDeviceSynchronize());
     std::lock_guard<std::mutex> lk(g_prof_mu);
     struct Agg {
-      long long n = 0, bytes = 0;
+      long long n = 0, bytes = 0, flops = 0;
       double ms = 0;
     };
     std::map<std::string, Agg> agg;
@@ -108,13 +152,15 @@ int tmrg_profile_end(char *json, int64_t cap) {
       a.n++;
       a.ms += ms;
       a.bytes += r.bytes;
+      a.flops += r.flops;
     }
     std::string s = "{";
     bool first = true;
     for (auto &kv : agg) {
       char buf[512];
-      snprintf(buf, sizeof buf, "%s\"%s\": [%lld, %.6f, %lld]", first ? "" : ", ",
-               kv.first.c_str(), kv.second.n, kv.second.ms, kv.second.bytes);
+      snprintf(buf, sizeof buf, "%s\"%s\": [%lld, %.6f, %lld, %lld]", first ? "" : ", ",
+               kv.first.c_str(), kv.second.n, kv.second.ms, kv.second.bytes,
+               kv.second.flops);
       s += buf;
       first = false;
     }

@@ -242,6 +242,7 @@ static void launch_step(long long n, long long nnz, int vpn, const int *rp, cons
   // t1, one read of x and one write of y (all vpn components)
   prof_bytes((long long)(sizeof(T) + 4) * nnz + 4 * (n + 1) + (long long)sizeof(T) * n +
              3LL * sizeof(T) * n * vpn + (post ? (long long)sizeof(T) * n : 0));
+  prof_flops(2LL * vpn * nnz);
   switch (vpn) {
     case 1:
       launch((k_fe_step<T, 1, TR>), g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
@@ -270,6 +271,7 @@ static void horner(Filter &F, bool tr, int vpn, const T *in, T *out,
   DBuf<T> t1(len, s), tmp(len, s);
   const T *pre = tr ? Tinv : Ainv;
   const T *post = tr ? Ainv : Tinv;
+  prof_bytes(2LL * sizeof(T) * len + (long long)sizeof(T) * n);
   launch(k_fe_scale<T>, blocks_for(len, 256), 256, 0, s, n, vpn, pre, in, t1.p);
   if (F.N == 0) {
     launch(k_fe_scale<T>, blocks_for(len, 256), 256, 0, s, n, vpn, post,
@@ -292,6 +294,7 @@ static void horner(Filter &F, bool tr, int vpn, const T *in, T *out,
 }
 
 void filter_apply(Filter &F, bool tr, int vpn, const double *in, double *out) {
+  Stage st(tr ? "tmrg_filter_apply_transpose" : "tmrg_filter_apply");
   horner<double>(F, tr, vpn, in, out, F.vals.p, F.Ainv.p, F.B.p, F.Tinv.p);
 }
 void filter_apply_f32(Filter &F, bool tr, int vpn, const float *in, float *out) {
@@ -372,6 +375,7 @@ void filter_apply_static(Filter &F, bool tr, int vpn, const double *in, double *
 }
 
 void filter_create(Forest &f, double len, double r, int N, Filter &F) {
+  Stage st("tmrg_filter_create");
   if (f.order != 2)
     throw Error(TMRG_ERR_UNSUPPORTED, "matrix filter: order-2 forests only");
   forest_create_nodes(f);

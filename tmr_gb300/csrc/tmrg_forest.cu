@@ -12,6 +12,7 @@ namespace tmrg {
 std::atomic<long long> g_kernel_launches{0};
 std::atomic<bool> g_profile_on{false};
 thread_local long long g_prof_bytes = 0;
+thread_local long long g_prof_flops = 0;
 
 void Forest::set_order(int o, int it) {
   free_nodes();
@@ -207,6 +208,7 @@ __global__ void k_compact_octs(long long n, OctKey K,
 
 void forest_refine(Forest &f, const int *d_ref, long long nref, int min_level,
                    int max_level) {
+  Stage st("tmrg_refine");
   if (!f.have_octs) throw Error(TMRG_ERR_STATE, "refine: no octants");
   if (d_ref && nref != f.n)
     throw Error(TMRG_ERR_ARG, "refine: refinement array length " +
@@ -540,6 +542,7 @@ static long long sort_unique(DBuf<uint64_t> &keys, long long n, int nbits,
 }
 
 void forest_balance(Forest &f, int corner) {
+  Stage stage("tmrg_balance");
   if (!f.have_octs)
     throw Error(TMRG_ERR_STATE,
                 "Cannot call balance(), no octants have been created");

@@ -418,6 +418,7 @@ __global__ void k_rowsum(long long rows, const int *__restrict__ rowptr,
 }
 
 void interp_create(Forest &fine, Forest &coarse, Interp &I) {
+  Stage st("tmrg_create_interpolation");
   if (&fine == &coarse)
     throw Error(TMRG_ERR_ARG, "Cannot interpolate between the same object");
   if (fine.interp != coarse.interp)
@@ -508,6 +509,7 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
                 "createInterpolation: a fine node has no enclosing coarse octant");
 
   // P^T by a stable sort on the column (rows stay ascending per column).
+  Stage st_t("tmrg_transpose");
   const int cbits = bits_for(I.cols + 1);
   DBuf<uint64_t> tk(nnz, s);
   DBuf<uint32_t> tp(nnz, s);
@@ -680,6 +682,7 @@ static void apply2(long long rows, long long nnz, int nvec2, const int *rp,
 }
 
 void interp_apply(Interp &I, int which, const double *x, double *y, int nvec) {
+  Stage st(which == 0 ? "tmrg_interp_mult" : "tmrg_interp_mult_transpose");
   if (nvec <= 0) throw Error(TMRG_ERR_ARG, "interp apply: nvec <= 0");
   cudaStream_t s = I.s;
   if (nvec % 2 == 0 && ((uintptr_t)x % 16) == 0 && ((uintptr_t)y % 16) == 0) {
@@ -687,6 +690,7 @@ void interp_apply(Interp &I, int which, const double *x, double *y, int nvec) {
     long long nout = (which == 0) ? I.rows : I.cols;
     prof_bytes(12 * I.nnz + 4 * (nout + 1) + 8LL * nvec * (nin + nout) +
                (which == 2 ? 8 * nout : 0));
+    prof_flops(2LL * nvec * I.nnz);
     const int *rp = which == 0 ? I.rowptr.p : I.t_rowptr.p;
     const int *ci = which == 0 ? I.colidx.p : I.t_colidx.p;
     const double *v = which == 0 ? I.vals.p : I.t_vals.p;
@@ -710,6 +714,7 @@ void interp_apply(Interp &I, int which, const double *x, double *y, int nvec) {
   long long nout = (which == 0) ? I.rows : I.cols;
   prof_bytes(12 * I.nnz + 4 * (nout + 1) + 8LL * nvec * (nin + nout) +
              (which == 2 ? 8 * nout : 0));
+  prof_flops(2LL * nvec * I.nnz);
   if (which == 0) {
     long long threads = I.rows * G;
     launch(k_csr_apply, blocks_for(threads, 256), 256, 0, s, I.rows, G, nvec,

@@ -605,6 +605,7 @@ __global__ void k_remap(long long m, const int *__restrict__ num, int *a) {
 }
 
 void forest_create_nodes(Forest &f) {
+  Stage st("tmrg_create_nodes");
   if (!f.have_octs)
     throw Error(TMRG_ERR_STATE,
                 "Cannot call createNodes(), no octants have been created");

@@ -6,12 +6,21 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <atomic>
 #include <utility>
 
 #include "tmrg_common.cuh"
 
 namespace tmrg {
+
+// NVTX range for a pipeline stage (visible to ncu --nvtx and profilers;
+// a no-op when no tool is attached).
+struct Stage {
+  explicit Stage(const char *name) { nvtxRangePushA(name); }
+  ~Stage() { nvtxRangePop(); }
+};
 
 extern std::atomic<long long> g_kernel_launches;
 
@@ -20,9 +29,12 @@ extern std::atomic<long long> g_kernel_launches;
 // algorithmic byte count when the launch site states one.
 extern std::atomic<bool> g_profile_on;
 extern thread_local long long g_prof_bytes;
+extern thread_local long long g_prof_flops;
 cudaEvent_t prof_event();
-void prof_push(const char *name, cudaEvent_t a, cudaEvent_t b, long long bytes);
+void prof_push(const char *name, cudaEvent_t a, cudaEvent_t b, long long bytes,
+               long long flops);
 inline void prof_bytes(long long b) { g_prof_bytes = b; }
+inline void prof_flops(long long f) { g_prof_flops = f; }
 
 // Launch a kernel on `s`, count it and check the launch.  Use through the
 // `launch(kernel, grid, block, smem, stream, args...)` macro.
@@ -30,8 +42,9 @@ template <typename... KArgs, typename... Args>
 inline void launch_impl(const char *name, void (*k)(KArgs...), dim3 grid,
                         dim3 block, size_t smem, cudaStream_t s,
                         Args &&...args) {
-  long long bytes = g_prof_bytes;
+  long long bytes = g_prof_bytes, flops = g_prof_flops;
   g_prof_bytes = 0;
+  g_prof_flops = 0;
   if (grid.x == 0 || grid.y == 0 || grid.z == 0) return;
   const bool prof = g_profile_on.load(std::memory_order_relaxed);
   cudaEvent_t a = nullptr;
@@ -45,7 +58,7 @@ inline void launch_impl(const char *name, void (*k)(KArgs...), dim3 grid,
   if (prof) {
     cudaEvent_t b = prof_event();
     TMRG_CUDA(cudaEventRecord(b, s));
-    prof_push(name, a, b, bytes);
+    prof_push(name, a, b, bytes, flops);
   }
 }
 #define launch(k, ...) ::tmrg::launch_impl(#k, k, __VA_ARGS__)
