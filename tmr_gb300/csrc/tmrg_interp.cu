@@ -5,32 +5,45 @@
 // order (TMROctForest.cpp:6654-6688): the reference's findEnclosing search
 // over the sorted coarse octants, computeElemInterp's tensor-product
 // Lagrange weights with the coarse dependent-node expansion, and a sort and
-// merge of the entries by column (TMRIndexWeight::uniqueSort), one warp per
-// row.  Rows are made in two passes (count, then write at the scanned
-// offsets).  P^T is the same matrix re-sorted by
-// (column, row), so transpose applies gather without atomics and sum in a
-// fixed order.
+// merge of the entries by column (TMRIndexWeight::uniqueSort).
+//
+// The sort is done once per coarse element instead of once per row.  The
+// entries of a row are, in computeElemInterp's order (kk, jj, ii, then the
+// dependent entries in CSR order), the in-box subsequence of its element's
+// full expansion sequence.  A stable sort by column commutes with taking a
+// subsequence, so each coarse element's expansion is stably sorted by
+// column once, and a row is the in-box filter of that list with adjacent
+// equal columns summed in order.  Rows are written in two passes (exact
+// count, then write at the scanned offsets).  P^T is the zero-free matrix
+// re-sorted by (column, row), so transpose applies gather without atomics
+// and sum in a fixed order.
 #include "tmrg_tree.cuh"
 
 namespace tmrg {
 
-constexpr int IMAX_CO = 3;  // coarse orders built for createInterpolation
-constexpr int IMAX_W = IMAX_CO * IMAX_CO * IMAX_CO * IMAX_CO * IMAX_CO;
+constexpr int IMAX_CO = 3;   // coarse orders built for createInterpolation
+constexpr int IMAX_E = 256;  // entries of one coarse element's expansion
+constexpr uint8_t KEY_INDEP = 0x80;  // list entry is an independent node
 
 struct InterpCtx {
   int fo, co;  // fine / coarse order
-  double fk[TMRG_MAX_ORDER], ck[TMRG_MAX_ORDER];
-  double crk[TMRG_MAX_ORDER][TMRG_MAX_ORDER];  // 1/(ck_i - ck_j)
+  double fk1[TMRG_MAX_ORDER], ck[TMRG_MAX_ORDER];  // 1 + fine knot, coarse knot
+  double crk[TMRG_MAX_ORDER][TMRG_MAX_ORDER];     // 1/(ck_i - ck_j)
   // fine octants
   const int *fb, *fx, *fy, *fz;
   const int16_t *fl;
-  // coarse octants {block | level << 26, x, y, z}, connectivity and
-  // dependent CSR
+  // coarse octants {block | level << 26, x, y, z}
   long long cn;
   const int4 *c4;
-  const int *cconn;
-  const int *cdptr, *cdconn;
-  const double *cdw;
+  // per coarse element: offsets of its sorted expansion list, the list
+  // (column, dependent weight, local node | KEY_INDEP) and its kind
+  // (0: co^3 independent distinct nodes, 1: dependent entries, 2: a
+  // column repeats)
+  const long long *eoff;
+  const int *lcol;
+  const double *ldw;
+  const uint8_t *lkey;
+  const uint8_t *ekind;
   const unsigned long long *rep;  // fine node -> element*npe + local index
   int *err;
 };
@@ -52,24 +65,115 @@ __global__ void k_first_ref(long long m, int npe, long long nowned,
   if (c >= 0 && c < nowned) atomicMin(rep + c, (unsigned long long)t);
 }
 
-// 1-D Lagrange basis (TMRInterpolation.h:40-52).  rk[i][j] holds
-// 1/(k_i - k_j), rounded once on the host exactly as the reference rounds
-// it, so no FP64 division runs here (FP64 is a scarce pipe on GB300).
-__device__ __forceinline__ void lagrange_w(int order, double u, const double *kn,
-                                           const double (*rk)[TMRG_MAX_ORDER],
-                                           double *N) {
-  for (int i = 0; i < order; i++) {
-    double v = 1.0;
-    for (int j = 0; j < order; j++) {
-      if (i != j) v = __dmul_rn(v, __dmul_rn(__dsub_rn(u, kn[j]), rk[i][j]));
-    }
-    N[i] = v;
+// ---------------------------------------------------------------------
+// Coarse element expansion lists.
+__global__ void k_elist_count(long long n, int cnpe, const int *__restrict__ conn,
+                              const int *__restrict__ dptr, long long *cnt) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int *c = conn + t * cnpe;
+  long long e = 0;
+  for (int l = 0; l < cnpe; l++) {
+    int cv = __ldg(c + l);
+    e += (cv >= 0) ? 1 : (__ldg(dptr - cv) - __ldg(dptr - cv - 1));
   }
+  cnt[t] = e;
 }
-// 1/2^e for an octant side 2^e, exact (same value as 1.0/h).
-__device__ __forceinline__ double inv_side(int level) {
-  return __hiloint2double((1023 - (TMRG_MAX_LEVEL - level)) << 20, 0);
+
+// One warp per coarse element: lane l expands local node l (l = ii + jj*co
+// + kk*co^2, so lanes run in computeElemInterp's loop order) into shared
+// memory, then a stable rank sort by column writes the list.
+constexpr int EL_WARPS = 4;
+__global__ void __launch_bounds__(EL_WARPS * 32)
+    k_elist_fill(long long n, int cnpe, const int *__restrict__ conn,
+                 const int *__restrict__ dptr, const int *__restrict__ dconn,
+                 const double *__restrict__ dw, const long long *__restrict__ eoff,
+                 int *lcol, double *ldw, uint8_t *lkey, uint8_t *ekind, int *err) {
+  __shared__ int s_col[EL_WARPS][IMAX_E];
+  __shared__ double s_dw[EL_WARPS][IMAX_E];
+  __shared__ uint8_t s_key[EL_WARPS][IMAX_E];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long t = (long long)blockIdx.x * EL_WARPS + warp;
+  if (t >= n) return;
+  const long long eo = eoff[t];
+  const int E = (int)(eoff[t + 1] - eo);
+  if (E > IMAX_E) {
+    if (lane == 0) atomicExch(err, 2);
+    return;
+  }
+  int cv = 0, myn = 0, d0 = 0;
+  if (lane < cnpe) {
+    cv = __ldg(conn + t * cnpe + lane);
+    if (cv >= 0) {
+      myn = 1;
+    } else {
+      d0 = __ldg(dptr - cv - 1);
+      myn = __ldg(dptr - cv) - d0;
+    }
+  }
+  int incl = myn;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int off = incl - myn;
+  if (lane < cnpe) {
+    if (cv >= 0) {
+      s_col[warp][off] = cv;
+      s_dw[warp][off] = 1.0;
+      s_key[warp][off] = (uint8_t)(lane | KEY_INDEP);
+    } else {
+      for (int p = 0; p < myn; p++) {
+        s_col[warp][off + p] = __ldg(dconn + d0 + p);
+        s_dw[warp][off + p] = __ldg(dw + d0 + p);
+        s_key[warp][off + p] = (uint8_t)lane;
+      }
+    }
+  }
+  const bool anydep = __any_sync(0xffffffffu, lane < cnpe && cv < 0);
+  __syncwarp();
+  bool dup = false;
+  for (int a = lane; a < E; a += 32) {
+    const int col = s_col[warp][a];
+    int rk = 0;
+    for (int b = 0; b < E; b++) {
+      const int cb = s_col[warp][b];
+      rk += (cb < col) || (cb == col && b < a);
+      dup |= (cb == col && b != a);
+    }
+    lcol[eo + rk] = col;
+    ldw[eo + rk] = s_dw[warp][a];
+    lkey[eo + rk] = s_key[warp][a];
+  }
+  const bool anydup = __any_sync(0xffffffffu, dup);
+  if (lane == 0) ekind[t] = anydup ? 2 : (anydep ? 1 : 0);
 }
+
+// ---------------------------------------------------------------------
+// 1-D Lagrange basis (TMRInterpolation.h:40-52) for two or three knots:
+// N_i = prod_{j != i, ascending} (u - k_j) * rk[i][j], where rk[i][j] holds
+// 1/(k_i - k_j), rounded once on the host exactly as the reference rounds
+// it.  The product starts from its first factor (1.0 * f == f exactly), so
+// an order-3 basis takes 12 FP64 operations (FP64 is a scarce pipe on
+// GB300).
+__device__ __forceinline__ void lagrange3(int order, double u, const double *kn,
+                                          const double (*rk)[TMRG_MAX_ORDER],
+                                          double &n0, double &n1, double &n2) {
+  const double d0 = __dsub_rn(u, kn[0]), d1 = __dsub_rn(u, kn[1]);
+  if (order == 2) {
+    n0 = __dmul_rn(d1, rk[0][1]);
+    n1 = __dmul_rn(d0, rk[1][0]);
+    n2 = 1.0;
+    return;
+  }
+  const double d2 = __dsub_rn(u, kn[2]);
+  n0 = __dmul_rn(__dmul_rn(d1, rk[0][1]), __dmul_rn(d2, rk[0][2]));
+  n1 = __dmul_rn(__dmul_rn(d0, rk[1][0]), __dmul_rn(d2, rk[1][2]));
+  n2 = __dmul_rn(__dmul_rn(d0, rk[2][0]), __dmul_rn(d1, rk[2][1]));
+}
+// 2^e as a double from its exponent (exact; e >= -1022).
+__device__ __forceinline__ double pow2(int e) { return __hiloint2double((1023 + e) << 20, 0); }
 
 // findEnclosing (TMROctForest.cpp:6228-6377): binary search for the node's
 // element octant, then a forward scan up to the bounding position.
@@ -91,10 +195,13 @@ __device__ long long find_enclosing(const InterpCtx &I, const Oct &node, int inf
     zi = node.z + (kk / (order - 1)) * h;
   else if (order % 2 == 1 && kk == order / 2)
     zi = node.z + h / 2;
-  double hd = (double)h;
-  double xd = __dadd_rn((double)node.x, __dmul_rn(__dmul_rn(0.5, hd), __dadd_rn(1.0, I.fk[ii])));
-  double yd = __dadd_rn((double)node.y, __dmul_rn(__dmul_rn(0.5, hd), __dadd_rn(1.0, I.fk[jj])));
-  double zd = __dadd_rn((double)node.z, __dmul_rn(__dmul_rn(0.5, hd), __dadd_rn(1.0, I.fk[kk])));
+  // node position at knots that are not octant-grid points (none below
+  // order 4): x + (0.5 h)(1 + k), with 0.5 h = 2^(29 - level) exact
+  const double half = pow2(TMRG_MAX_LEVEL - 1 - node.level);
+  double xd = 0.0, yd = 0.0, zd = 0.0;
+  if (xi < 0) xd = __dadd_rn((double)node.x, __dmul_rn(half, I.fk1[ii]));
+  if (yi < 0) yd = __dadd_rn((double)node.y, __dmul_rn(half, I.fk1[jj]));
+  if (zi < 0) zd = __dadd_rn((double)node.z, __dmul_rn(half, I.fk1[kk]));
   long long low = 0, high = I.cn - 1, mid = low + (high - low) / 2;
   while (mid != low) {
     int4 q = __ldg(I.c4 + mid);
@@ -132,243 +239,359 @@ __device__ long long find_enclosing(const InterpCtx &I, const Oct &node, int inf
   return -1;
 }
 
-// One coordinate direction of computeElemInterp (TMROctForest.cpp:
-// 6497-6548, Lagrange branch): exact face hits short-circuit to one weight.
-__device__ __forceinline__ void dir_weights(const InterpCtx &I, int i, int32_t nx,
-                                            int32_t h, int32_t ox, int32_t hc,
-                                            double ihc, int &s, int &e, double *N) {
-  const int mo = I.fo, co = I.co;
-  if ((i == 0 && ox == nx) || (i == mo - 1 && ox == nx + h)) {
-    s = 0;
-    e = 1;
-    N[0] = 1.0;
-  } else if ((i == 0 && ox + hc == nx) || (i == mo - 1 && ox + hc == nx + h)) {
-    s = co - 1;
-    e = co;
-    N[s] = 1.0;
-  } else {
-    s = 0;
-    e = co;
-    double t = __dadd_rn((double)nx,
-                         __dmul_rn(__dmul_rn(0.5, (double)h), __dadd_rn(1.0, I.fk[i])));
-    // division by the power of two hc is an exact scaling
-    double u = __dadd_rn(-1.0, __dmul_rn(__dmul_rn(2.0, __dsub_rn(t, (double)ox)), ihc));
-    lagrange_w(co, u, I.ck, I.crk, N);
+// The index range [s, e) of one coordinate direction of computeElemInterp
+// (TMROctForest.cpp:6497-6548, Lagrange branch) as s | e << 2: an exact
+// face hit keeps one coarse index.
+__device__ __forceinline__ int dir_range(int i, int mo, int co, int32_t nx, int32_t h,
+                                         int32_t ox, int32_t hc) {
+  if ((i == 0 && ox == nx) || (i == mo - 1 && ox == nx + h)) return 0 | (1 << 2);
+  if ((i == 0 && ox + hc == nx) || (i == mo - 1 && ox + hc == nx + h))
+    return (co - 1) | (co << 2);
+  return 0 | (co << 2);
+}
+// The weights of that direction (1.0 at a face hit).
+// u = -1 + 2 (x + 0.5 h (1 + k_i) - ox) / hc as the reference rounds it:
+// 0.5 h and 2 / hc are powers of two, so those scalings are exact.
+__device__ __forceinline__ void dir_weights(const InterpCtx &I, int i, int range,
+                                            int32_t nx, double half, int32_t ox,
+                                            double two_ihc, double &n0, double &n1,
+                                            double &n2) {
+  if (((range >> 2) - (range & 3)) == 1) {
+    n0 = n1 = n2 = 1.0;
+    return;
   }
+  double t = __dadd_rn((double)nx, __dmul_rn(half, I.fk1[i]));
+  double u = __dadd_rn(-1.0, __dmul_rn(__dsub_rn(t, (double)ox), two_ihc));
+  lagrange3(I.co, u, I.ck, I.crk, n0, n1, n2);
+}
+// Bit l of the mask is set when local coarse node l = ii + jj*co + kk*co^2
+// lies in the row's box.
+__device__ __forceinline__ unsigned box_mask(int co, int rx, int ry, int rz) {
+  unsigned mu = ((1u << (rx >> 2)) - 1u) & ~((1u << (rx & 3)) - 1u);
+  unsigned m = 0;
+  for (int kk = rz & 3; kk < (rz >> 2); kk++)
+    for (int jj = ry & 3; jj < (ry >> 2); jj++) m |= mu << (jj * co + kk * co * co);
+  return m;
 }
 
-// Rows of P, one warp per row, 32 rows per warp.  Phase A: each lane runs
-// findEnclosing and the per-direction weights of one row.  Phase B, row by
-// row: lane i expands box node i (ii fastest, as computeElemInterp loops)
-// through the coarse dependent CSR into shared memory; a stable rank sort
-// orders the entries by column and the first entry of each column run sums
-// the run in order (TMRIndexWeight::uniqueSort, TMRBase.h:103-130).
-constexpr int IW_WARPS = 4;
-
-// Pass 1 (bound): findEnclosing per row, kept in `trow`, and an upper bound
-// of the row's entries (sum of the box nodes' expansions) in `bound`.
-__global__ void k_interp_bound(long long rows, InterpCtx I, int *trow,
-                               long long *bound) {
-  long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= rows) return;
+// The row's element and box.  Returns the element (or -1 with the error
+// flag set) and the box mask in `bm`.
+__device__ __forceinline__ long long row_box(const InterpCtx &I, long long row,
+                                             Oct &node, int &info, int4 &cq,
+                                             int r[3], unsigned &bm) {
   const int mo = I.fo, co = I.co, fnpe = mo * mo * mo;
-  unsigned long long r = I.rep[row];
-  long long e = (long long)(r / fnpe);
-  int info = (int)(r - (unsigned long long)e * fnpe);
-  Oct node{I.fb[e], I.fx[e], I.fy[e], I.fz[e], I.fl[e]};
+  unsigned long long rr = I.rep[row];
+  long long e = (long long)(rr / fnpe);
+  info = (int)(rr - (unsigned long long)e * fnpe);
+  node = Oct{I.fb[e], I.fx[e], I.fy[e], I.fz[e], I.fl[e]};
   long long t = find_enclosing(I, node, info);
-  trow[row] = (int)t;
-  long long ne = 0;
+  bm = 0;
   if (t < 0) {
     atomicExch(I.err, 1);
-  } else {
-    // the box of coarse nodes the row touches (computeElemInterp's
-    // istart..iend per direction), expanded through the dependent rows
-    int4 cq = __ldg(I.c4 + t);
-    int32_t h = side_of(node.level), hc = side_of(cq.x >> 26);
-    int i = info % mo, j = (info % (mo * mo)) / mo, k = info / (mo * mo);
-    int rs[3], re[3];
-    const int ijk[3] = {i, j, k};
-    const int32_t nx[3] = {node.x, node.y, node.z}, ox[3] = {cq.y, cq.z, cq.w};
-    for (int d = 0; d < 3; d++) {
-      int a = ijk[d];
-      if ((a == 0 && ox[d] == nx[d]) || (a == mo - 1 && ox[d] == nx[d] + h)) {
-        rs[d] = 0;
-        re[d] = 1;
-      } else if ((a == 0 && ox[d] + hc == nx[d]) || (a == mo - 1 && ox[d] + hc == nx[d] + h)) {
-        rs[d] = co - 1;
-        re[d] = co;
-      } else {
-        rs[d] = 0;
-        re[d] = co;
-      }
-    }
-    const int *c = I.cconn + t * (long long)(co * co * co);
-    for (int kk = rs[2]; kk < re[2]; kk++)
-      for (int jj = rs[1]; jj < re[1]; jj++)
-        for (int ii = rs[0]; ii < re[0]; ii++) {
-          int cv = __ldg(c + ii + jj * co + kk * co * co);
-          ne += (cv >= 0) ? 1 : (__ldg(I.cdptr - cv) - __ldg(I.cdptr - cv - 1));
-        }
+    return -1;
   }
-  bound[row] = ne;
+  cq = __ldg(I.c4 + t);
+  int32_t h = side_of(node.level), hc = side_of(cq.x >> 26);
+  int i = info % mo, j = (info % (mo * mo)) / mo, k = info / (mo * mo);
+  r[0] = dir_range(i, mo, co, node.x, h, cq.y, hc);
+  r[1] = dir_range(j, mo, co, node.y, h, cq.z, hc);
+  r[2] = dir_range(k, mo, co, node.z, h, cq.w, hc);
+  bm = box_mask(co, r[0], r[1], r[2]);
+  return t;
 }
 
-// Pass 2: the rows, written merged at the bound offsets of a scratch
-// buffer; cnt[row] = merged length.
+// Pass 1, one lane per row: findEnclosing, kept in `trow`, and the exact
+// number of merged entries of the row in `cnt`.
+__global__ void k_interp_count(long long rows, InterpCtx I, int *trow, long long *cnt) {
+  long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= rows) return;
+  Oct node;
+  int info, r[3];
+  int4 cq;
+  unsigned bm;
+  long long t = row_box(I, row, node, info, cq, r, bm);
+  trow[row] = (int)t;
+  long long ne = 0;
+  if (t >= 0) {
+    const int kind = I.ekind[t];
+    if (kind == 0) {
+      ne = __popc(bm);
+    } else {
+      const long long eo = I.eoff[t], e1 = I.eoff[t + 1];
+      int prev = -1;
+      for (long long j = eo; j < e1; j++) {
+        int key = I.lkey[j];
+        if ((bm >> (key & 31)) & 1u) {
+          if (kind == 1) {
+            ne++;
+          } else {
+            int col = I.lcol[j];
+            ne += (col != prev);
+            prev = col;
+          }
+        }
+      }
+    }
+  }
+  cnt[row] = ne;
+}
+
+__device__ __forceinline__ int nonzero_bits(double v) {
+  return (__double_as_longlong(v) << 1) != 0;
+}
+
+// Pass 2, 32 consecutive rows per warp; their entries form one contiguous
+// segment of the CSR.  Phase A, one lane per row: the element, its list
+// range, the box mask and the direction weights, with the products
+// Nu[ii]*Nv[jj] formed once per row (computeElemInterp multiplies Nu*Nv
+// first).  Phase B walks the 32 rows' element lists as one concatenated
+// sequence, 64 entries per step with all loads independent, and stages the
+// in-box entries in order (ballot + popc) in shared memory.  A flush forms
+// the staged weights on full warps (a masked FP64 warp instruction costs
+// the GB300 FP64 pipe as much as a full one), sums each run of equal
+// (row, column) in order and writes the run heads in order; the last run
+// of a non-final flush stays staged because it may continue.  *nzcount
+// gets the number of nonzero values written.
+constexpr int IW_WARPS = 4;
+constexpr int IW_CAP = 256;  // staged entries per warp
 __global__ void __launch_bounds__(IW_WARPS * 32)
     k_interp_rows(long long rows, InterpCtx I, const int *__restrict__ trow,
-                  const long long *__restrict__ toff, int *cnt, int *cols,
-                  double *vals) {
-  __shared__ int s_col[IW_WARPS][IMAX_W];
-  __shared__ double s_w[IW_WARPS][IMAX_W];
-  __shared__ short s_ord[IW_WARPS][IMAX_W];
-  const bool WRITE = true;
+                  const long long *__restrict__ roff, int *cols, double *vals,
+                  unsigned long long *nzcount) {
+  __shared__ double s_uv[IW_WARPS][32][IMAX_CO * IMAX_CO];
+  __shared__ double s_nw[IW_WARPS][32][IMAX_CO];
+  __shared__ long long s_eo[IW_WARPS][32];
+  __shared__ int s_vs[IW_WARPS][33];  // start of each row's list in the sequence
+  __shared__ unsigned s_bm[IW_WARPS][32];
+  __shared__ int s_c[IW_WARPS][IW_CAP];
+  __shared__ double s_v[IW_WARPS][IW_CAP];
+  __shared__ uint16_t s_k[IW_WARPS][IW_CAP];  // row slot << 8 | kk << 4 | ii + co*jj
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const long long base = ((long long)blockIdx.x * IW_WARPS + warp) * 32;
   if (base >= rows) return;
-  const int mo = I.fo, co = I.co, fnpe = mo * mo * mo;
+  const int mo = I.fo, co = I.co, co2 = co * co, fnpe = mo * mo * mo;
   // phase A
-  long long t = -1;
-  int box = 0;  // is | ie<<2 | js<<4 | je<<6 | ks<<8 | ke<<10
-  double Nu[IMAX_CO] = {0, 0, 0}, Nv[IMAX_CO] = {0, 0, 0}, Nw[IMAX_CO] = {0, 0, 0};
   {
     long long row = base + lane;
+    int E = 0;
+    long long eo = 0;
+    unsigned bm = 0;
     if (row < rows) {
-      unsigned long long r = I.rep[row];
-      long long e = (long long)(r / fnpe);
-      int info = (int)(r - (unsigned long long)e * fnpe);
-      Oct node{I.fb[e], I.fx[e], I.fy[e], I.fz[e], I.fl[e]};
-      t = trow[row];
+      const int t = trow[row];
       if (t >= 0) {
-        int i = info % mo, j = (info % (mo * mo)) / mo, k = info / (mo * mo);
+        eo = I.eoff[t];
+        E = (int)(I.eoff[t + 1] - eo);
+        unsigned long long rr = I.rep[row];
+        long long e = (long long)(rr / fnpe);
+        int info = (int)(rr - (unsigned long long)e * fnpe);
+        Oct node{I.fb[e], I.fx[e], I.fy[e], I.fz[e], I.fl[e]};
         int4 cq = __ldg(I.c4 + t);
         int cl = cq.x >> 26;
         int32_t h = side_of(node.level), hc = side_of(cl);
-        double ihc = inv_side(cl);
-        int is, ie, js, je, ks, ke;
-        dir_weights(I, i, node.x, h, cq.y, hc, ihc, is, ie, Nu);
-        dir_weights(I, j, node.y, h, cq.z, hc, ihc, js, je, Nv);
-        dir_weights(I, k, node.z, h, cq.w, hc, ihc, ks, ke, Nw);
-        box = is | (ie << 2) | (js << 4) | (je << 6) | (ks << 8) | (ke << 10);
-      } else {
-        atomicExch(I.err, 1);
-      }
-    }
-  }
-  // phase B
-  for (int q = 0; q < 32; q++) {
-    long long row = base + q;
-    if (row >= rows) break;
-    long long tq = __shfl_sync(0xffffffffu, t, q);
-    int bq = __shfl_sync(0xffffffffu, box, q);
-    double nu[IMAX_CO], nv[IMAX_CO], nw[IMAX_CO];
+        const double half = pow2(TMRG_MAX_LEVEL - 1 - node.level);
+        const double two_ihc = pow2(cl + 1 - TMRG_MAX_LEVEL);
+        int i = info % mo, j = (info % (mo * mo)) / mo, k = info / (mo * mo);
+        int rx = dir_range(i, mo, co, node.x, h, cq.y, hc);
+        int ry = dir_range(j, mo, co, node.y, h, cq.z, hc);
+        int rz = dir_range(k, mo, co, node.z, h, cq.w, hc);
+        bm = box_mask(co, rx, ry, rz);
+        double u0, u1, u2, v0, v1, v2, w0, w1, w2;
+        dir_weights(I, i, rx, node.x, half, cq.y, two_ihc, u0, u1, u2);
+        dir_weights(I, j, ry, node.y, half, cq.z, two_ihc, v0, v1, v2);
+        dir_weights(I, k, rz, node.z, half, cq.w, two_ihc, w0, w1, w2);
+        const double nu[3] = {u0, u1, u2}, nv[3] = {v0, v1, v2};
 #pragma unroll
-    for (int a = 0; a < IMAX_CO; a++) {
-      nu[a] = __shfl_sync(0xffffffffu, Nu[a], q);
-      nv[a] = __shfl_sync(0xffffffffu, Nv[a], q);
-      nw[a] = __shfl_sync(0xffffffffu, Nw[a], q);
-    }
-    if (tq < 0) {
-      if (lane == 0) cnt[row] = 0;
-      continue;
-    }
-    int is = bq & 3, ie = (bq >> 2) & 3, js = (bq >> 4) & 3, je = (bq >> 6) & 3,
-        ks = (bq >> 8) & 3, ke = (bq >> 10) & 3;
-    int di = ie - is, dj = je - js, nb = di * dj * (ke - ks);
-    int cv = 0, myn = 0, dp0 = 0;
-    double wt = 0.0;
-    if (lane < nb) {
-      int ii = is + lane % di, jj = js + (lane / di) % dj, kk = ks + lane / (di * dj);
-      cv = __ldg(I.cconn + tq * (long long)(co * co * co) + ii + jj * co + kk * co * co);
-      wt = __dmul_rn(__dmul_rn(nu[ii], nv[jj]), nw[kk]);
-      if (cv >= 0) {
-        myn = 1;
-      } else {
-        int d = -cv - 1;
-        dp0 = __ldg(I.cdptr + d);
-        myn = __ldg(I.cdptr + d + 1) - dp0;
+        for (int b = 0; b < IMAX_CO; b++)
+#pragma unroll
+          for (int a = 0; a < IMAX_CO; a++)
+            if (a < co && b < co) s_uv[warp][lane][a + co * b] = __dmul_rn(nu[a], nv[b]);
+        s_nw[warp][lane][0] = w0;
+        s_nw[warp][lane][1] = w1;
+        s_nw[warp][lane][2] = w2;
       }
     }
-    int incl = myn;
+    int incl = E;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       int y = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += y;
     }
-    const int ne = __shfl_sync(0xffffffffu, incl, 31);
-    int off = incl - myn;
-    if (myn == 1 && cv >= 0) {
-      s_col[warp][off] = cv;
-      s_w[warp][off] = wt;
-    } else {
-      for (int p = 0; p < myn; p++) {
-        s_col[warp][off + p] = __ldg(I.cdconn + dp0 + p);
-        s_w[warp][off + p] = __dmul_rn(wt, __ldg(I.cdw + dp0 + p));
-      }
-    }
-    __syncwarp();
-    // stable ranks
-    for (int a = lane; a < ne; a += 32) {
-      int col = s_col[warp][a];
-      int rk = 0;
-      for (int b = 0; b < ne; b++) {
-        int cb = s_col[warp][b];
-        rk += (cb < col) || (cb == col && b < a);
-      }
-      s_ord[warp][rk] = (short)a;
-    }
-    __syncwarp();
-    // merge runs of equal columns
-    int run = 0;
-    long long rp = toff[row];
-    for (int c0 = 0; c0 < ne; c0 += 32) {
-      int sidx = c0 + lane;
-      bool head = false;
-      int col = 0;
-      if (sidx < ne) {
-        col = s_col[warp][s_ord[warp][sidx]];
-        head = (sidx == 0) || (s_col[warp][s_ord[warp][sidx - 1]] != col);
-      }
-      unsigned hm = __ballot_sync(0xffffffffu, head);
-      if (WRITE && head) {
-        double acc = s_w[warp][s_ord[warp][sidx]];
-        for (int n2 = sidx + 1; n2 < ne && s_col[warp][s_ord[warp][n2]] == col; n2++)
-          acc = __dadd_rn(acc, s_w[warp][s_ord[warp][n2]]);
-        long long o = rp + run + __popc(hm & lt);
-        cols[o] = col;
-        vals[o] = acc;
-      }
-      run += __popc(hm);
-    }
-    if (lane == 0) cnt[row] = run;
-    __syncwarp();
+    s_vs[warp][lane] = incl - E;
+    if (lane == 31) s_vs[warp][32] = incl;
+    s_eo[warp][lane] = eo;
+    s_bm[warp][lane] = bm;
   }
+  __syncwarp();
+  const int vtot = s_vs[warp][32];
+  // phase B
+  const long long lim = roff[min(base + 32, rows)];  // end of the warp's segment
+  long long out = roff[base];
+  int nbuf = 0, nzc = 0;
+  auto flush = [&](bool final) {
+    __syncwarp();
+    int end = nbuf;
+    if (!final && nbuf > 0) {
+      // keep the last run (at most co^3 entries: one per local node)
+      const int c1 = s_c[warp][nbuf - 1], q1 = s_k[warp][nbuf - 1] >> 8;
+      while (end > 1 && s_c[warp][end - 2] == c1 && (s_k[warp][end - 2] >> 8) == q1) end--;
+      end--;
+    }
+    for (int k = lane; k < end; k += 32) {
+      const int sk = s_k[warp][k];
+      const int q = sk >> 8;
+      s_v[warp][k] = __dmul_rn(__dmul_rn(s_uv[warp][q][sk & 15], s_nw[warp][q][(sk >> 4) & 15]),
+                               s_v[warp][k]);
+    }
+    __syncwarp();
+    for (int c0 = 0; c0 < end; c0 += 32) {
+      const int k = c0 + lane;
+      bool head = false;
+      int col = 0, q = 0;
+      if (k < end) {
+        col = s_c[warp][k];
+        q = s_k[warp][k] >> 8;
+        head = (k == 0) || (s_c[warp][k - 1] != col) || ((s_k[warp][k - 1] >> 8) != q);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, head);
+      if (head) {
+        double acc = s_v[warp][k];
+        for (int k2 = k + 1;
+             k2 < end && s_c[warp][k2] == col && (s_k[warp][k2] >> 8) == q; k2++)
+          acc = __dadd_rn(acc, s_v[warp][k2]);
+        const long long o = out + __popc(m & lt);
+        if (o < lim) {
+          cols[o] = col;
+          vals[o] = acc;
+          nzc += nonzero_bits(acc);
+        } else {
+          atomicExch(I.err, 3);
+        }
+      }
+      out += __popc(m);
+    }
+    // move the kept run (shorter than the flushed part) to the front
+    int keep = nbuf - end;
+    if (keep > 32) {  // a run has at most one entry per local node
+      atomicExch(I.err, 3);
+      keep = 0;
+    }
+    int kc = 0, kk = 0;
+    double kv = 0.0;
+    if (lane < keep) {
+      kc = s_c[warp][end + lane];
+      kk = s_k[warp][end + lane];
+      kv = s_v[warp][end + lane];
+    }
+    __syncwarp();
+    if (lane < keep) {
+      s_c[warp][lane] = kc;
+      s_k[warp][lane] = (uint16_t)kk;
+      s_v[warp][lane] = kv;
+    }
+    __syncwarp();
+    nbuf = keep;
+  };
+  // the row slot of sequence position v: the last q with s_vs[q] <= v
+  auto slot = [&](int v) {
+    int q = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1)
+      if (q + step < 32 && s_vs[warp][q + step] <= v) q += step;
+    return q;
+  };
+  for (int v0 = 0; v0 < vtot; v0 += 64) {
+    int key[2] = {0, 0}, col[2] = {0, 0}, qs[2] = {0, 0};
+    double dw[2] = {0.0, 0.0};
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      const int v = v0 + 32 * u + lane;
+      if (v < vtot) {
+        const int q = slot(v);
+        const long long a = s_eo[warp][q] + (v - s_vs[warp][q]);
+        qs[u] = q;
+        key[u] = I.lkey[a];
+        col[u] = I.lcol[a];
+        dw[u] = I.ldw[a];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      const int v = v0 + 32 * u + lane;
+      const bool in = v < vtot && ((s_bm[warp][qs[u]] >> (key[u] & 31)) & 1u);
+      const unsigned m = __ballot_sync(0xffffffffu, in);
+      if (in) {
+        const int li = key[u] & 31;
+        const int kk = li >= 2 * co2 ? 2 : (li >= co2 ? 1 : 0);
+        const int o = nbuf + __popc(m & lt);
+        s_c[warp][o] = col[u];
+        // (Nu Nv Nw) * 1.0 is the independent node's weight exactly
+        s_v[warp][o] = (key[u] & KEY_INDEP) ? 1.0 : dw[u];
+        s_k[warp][o] = (uint16_t)((qs[u] << 8) | (kk << 4) | (li - kk * co2));
+      }
+      nbuf += __popc(m);
+    }
+    if (nbuf > IW_CAP - 64) flush(false);
+  }
+  flush(true);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nzc += __shfl_xor_sync(0xffffffffu, nzc, o);
+  if (lane == 0 && nzc) atomicAdd(nzcount, (unsigned long long)nzc);
 }
 
-// 8 lanes per row copy a merged row from scratch into the CSR.
-__global__ void k_interp_compact(long long rows, const long long *__restrict__ toff,
-                                 const long long *__restrict__ rp,
-                                 const int *__restrict__ tc, const double *__restrict__ tv,
-                                 int *cols, double *vals) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long r = t >> 3;
-  if (r >= rows) return;
-  int lane = (int)(t & 7);
-  long long s0 = toff[r], d0 = rp[r], n = rp[r + 1] - d0;
-  for (long long k = lane; k < n; k += 8) {
-    cols[d0 + k] = tc[s0 + k];
-    vals[d0 + k] = tv[s0 + k];
-  }
+// Nonzero values per row (8 lanes per row).
+__global__ void k_nz_count(long long rows, const int *__restrict__ rp,
+                           const double *__restrict__ v, long long *cnt) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long r = t >> 3;
+  const int g8 = threadIdx.x & 7;
+  int c = 0;
+  if (r < rows)
+    for (int p = __ldg(rp + r) + g8; p < __ldg(rp + r + 1); p += 8) c += nonzero_bits(__ldg(v + p));
+  c += __shfl_xor_sync(0xffffffffu, c, 1);
+  c += __shfl_xor_sync(0xffffffffu, c, 2);
+  c += __shfl_xor_sync(0xffffffffu, c, 4);
+  if (r < rows && g8 == 0) cnt[r] = c;
 }
+
 __global__ void k_ptr32(long long n, const long long *__restrict__ in, int *out) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i <= n) out[i] = (int)in[i];
 }
-__global__ void k_widen(long long n, const int *__restrict__ in, long long *out) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = in[i];
+
+// Zero-free copy of P: 8 lanes per row keep the nonzero entries in order.
+__global__ void k_nz_fill(long long rows, const int *__restrict__ rp,
+                          const int *__restrict__ ci, const double *__restrict__ v,
+                          const long long *__restrict__ nzoff, int *nrp, int *nci,
+                          double *nv) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long r = t >> 3;
+  const int lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
+  if (((t >> 5) << 2) >= rows) return;  // uniform per warp
+  const bool have = r < rows;
+  const int p0 = have ? __ldg(rp + r) : 0, p1 = have ? __ldg(rp + r + 1) : 0;
+  int trips = (p1 - p0 + 7) >> 3;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) trips = max(trips, __shfl_xor_sync(0xffffffffu, trips, o));
+  long long o = have ? nzoff[r] : 0;
+  const long long lim = have ? nzoff[r + 1] : 0;
+  for (int it = 0; it < trips; it++) {
+    const int p = p0 + it * 8 + g8;
+    const bool on = have && p < p1;
+    const double w = on ? __ldg(v + p) : 0.0;
+    const bool nz = on && nonzero_bits(w);
+    const unsigned mg = (__ballot_sync(0xffffffffu, nz) >> (grp * 8)) & 0xffu;
+    if (nz) {
+      const long long d = o + __popc(mg & ((1u << g8) - 1u));
+      if (d < lim) {
+        nci[d] = __ldg(ci + p);
+        nv[d] = w;
+      }
+    }
+    o += __popc(mg);
+  }
+  if (have && g8 == 0) nrp[r] = (int)nzoff[r];
+  if (have && g8 == 0 && r == rows - 1) nrp[rows] = (int)nzoff[rows];
 }
 
 // Transpose support.  Entries are keyed row << 32 | column; the stable
@@ -432,7 +655,10 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   TMRG_CUDA(cudaStreamSynchronize(coarse.s));
   cudaStream_t s = fine.s;
   I.s = s;
+  I.have_colsum = false;
+  I.colsum.release();
   const int fnpe = fine.order * fine.order * fine.order;
+  const int cnpe = coarse.order * coarse.order * coarse.order;
   const long long rows = fine.num_owned;
   I.rows = rows;
   I.cols = coarse.num_owned;
@@ -447,7 +673,7 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   c.fo = fine.order;
   c.co = coarse.order;
   for (int i = 0; i < TMRG_MAX_ORDER; i++) {
-    c.fk[i] = fine.knots[i];
+    c.fk1[i] = 1.0 + fine.knots[i];
     c.ck[i] = coarse.knots[i];
   }
   c.fb = fine.block.p;
@@ -464,10 +690,24 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
          (const int *)coarse.y.p, (const int *)coarse.z.p,
          (const int16_t *)coarse.level.p, c4.p);
   c.c4 = c4.p;
-  c.cconn = coarse.econn.p;
-  c.cdptr = coarse.dep_ptr.p;
-  c.cdconn = coarse.dep_conn.p;
-  c.cdw = coarse.dep_w.p;
+  // sorted expansion list of every coarse element
+  DBuf<long long> eoff(coarse.n + 1, s);
+  launch(k_elist_count, blocks_for(coarse.n, 256), 256, 0, s, coarse.n, cnpe,
+         (const int *)coarse.econn.p, (const int *)coarse.dep_ptr.p, eoff.p);
+  exclusive_scan<long long>(eoff.p, eoff.p, coarse.n, s);
+  const long long ne = read_scalar(eoff.p + coarse.n, s);
+  DBuf<int> lcol(ne + 1, s);
+  DBuf<double> ldw(ne + 1, s);
+  DBuf<uint8_t> lkey(ne + 1, s), ekind(coarse.n + 1, s);
+  launch(k_elist_fill, blocks_for(coarse.n, EL_WARPS), EL_WARPS * 32, 0, s, coarse.n,
+         cnpe, (const int *)coarse.econn.p, (const int *)coarse.dep_ptr.p,
+         (const int *)coarse.dep_conn.p, (const double *)coarse.dep_w.p,
+         (const long long *)eoff.p, lcol.p, ldw.p, lkey.p, ekind.p, err.p);
+  c.eoff = eoff.p;
+  c.lcol = lcol.p;
+  c.ldw = ldw.p;
+  c.lkey = lkey.p;
+  c.ekind = ekind.p;
   c.rep = rep.p;
   c.err = err.p;
   for (int i = 0; i < TMRG_MAX_ORDER; i++)
@@ -475,59 +715,88 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
       c.crk[i][j] = (i != j && i < coarse.order && j < coarse.order)
                         ? 1.0 / (coarse.knots[i] - coarse.knots[j])
                         : 0.0;
-  const unsigned rblocks = blocks_for(rows, IW_WARPS * 32);
-  // pass 1: enclosing octants and entry bounds; pass 2: merged rows into
-  // scratch at the bound offsets; pass 3: compact into the CSR
+  // pass 1: enclosing octants and exact row lengths; pass 2: the rows
   DBuf<int> trow(rows + 1, s);
-  DBuf<long long> toff(rows + 1, s);
-  launch(k_interp_bound, blocks_for(rows, 128), 128, 0, s, rows, c, trow.p, toff.p);
-  exclusive_scan<long long>(toff.p, toff.p, rows, s);
-  const long long nbound = read_scalar(toff.p + rows, s);
-  DBuf<int> tcols(nbound + 1, s);
-  DBuf<double> tvals(nbound + 1, s);
-  DBuf<int> cnt(rows + 1, s);
-  launch(k_interp_rows, rblocks, IW_WARPS * 32, 0, s, rows, c, (const int *)trow.p,
-         (const long long *)toff.p, cnt.p, tcols.p, tvals.p);
-  DBuf<long long> rp64(rows + 1, s);
-  launch(k_widen, blocks_for(rows, 256), 256, 0, s, rows, (const int *)cnt.p,
-         rp64.p);
-  exclusive_scan<long long>(rp64.p, rp64.p, rows, s);
-  const long long nnz = read_scalar(rp64.p + rows, s);
+  DBuf<long long> roff(rows + 1, s);
+  launch(k_interp_count, blocks_for(rows, 128), 128, 0, s, rows, c, trow.p, roff.p);
+  exclusive_scan<long long>(roff.p, roff.p, rows, s);
+  const long long nnz = read_scalar(roff.p + rows, s);
+  const int e = read_scalar(err.p, s);
+  if (e == 2)
+    throw Error(TMRG_ERR_INTERNAL,
+                "createInterpolation: a coarse element expands to more than 256 entries");
+  if (e)
+    throw Error(TMRG_ERR_INTERNAL,
+                "createInterpolation: a fine node has no enclosing coarse octant");
   if (nnz >= (1LL << 31) - 1)
     throw Error(TMRG_ERR_ARG, "createInterpolation: more than 2^31 entries");
   I.nnz = nnz;
   I.rowptr.alloc(rows + 1, s);
-  launch(k_ptr32, blocks_for(rows + 1, 256), 256, 0, s, rows,
-         (const long long *)rp64.p, I.rowptr.p);
+  launch(k_ptr32, blocks_for(rows + 1, 256), 256, 0, s, rows, (const long long *)roff.p,
+         I.rowptr.p);
   I.colidx.alloc(nnz + 1, s);
   I.vals.alloc(nnz + 1, s);
-  launch(k_interp_compact, blocks_for(rows * 8, 256), 256, 0, s, rows,
-         (const long long *)toff.p, (const long long *)rp64.p, (const int *)tcols.p,
-         (const double *)tvals.p, I.colidx.p, I.vals.p);
+  DBuf<unsigned long long> nzcount(1, s);
+  nzcount.zero();
+  launch(k_interp_rows, blocks_for(rows, IW_WARPS * 32), IW_WARPS * 32, 0, s, rows, c,
+         (const int *)trow.p, (const long long *)roff.p, I.colidx.p, I.vals.p, nzcount.p);
+  trow.release();
+  roff.release();
+  eoff.release();
+  lcol.release();
+  ldw.release();
+  lkey.release();
+  ekind.release();
+  c4.release();
+  rep.release();
+
+  // zero-free copy for the applies, when P has exact zeros
+  const long long nonzeros = (long long)read_scalar(nzcount.p, s);
   if (read_scalar(err.p, s))
-    throw Error(TMRG_ERR_INTERNAL,
-                "createInterpolation: a fine node has no enclosing coarse octant");
+    throw Error(TMRG_ERR_INTERNAL, "createInterpolation: a row outgrew its counted length");
+  // worth a second copy only when zeros are a good part of P
+  I.nnz_nz = (nnz - nonzeros) * 8 >= nnz ? nonzeros : nnz;
+  const long long nnz_nz = I.nnz_nz;
+  if (I.nnz_nz < nnz) {
+    DBuf<long long> nzoff(rows + 1, s);
+    launch(k_nz_count, blocks_for(rows * 8, 256), 256, 0, s, rows, (const int *)I.rowptr.p,
+           (const double *)I.vals.p, nzoff.p);
+    exclusive_scan<long long>(nzoff.p, nzoff.p, rows, s);
+    I.nz_rowptr.alloc(rows + 1, s);
+    I.nz_colidx.alloc(nnz_nz + 1, s);
+    I.nz_vals.alloc(nnz_nz + 1, s);
+    if (rows == 0) TMRG_CUDA(cudaMemsetAsync(I.nz_rowptr.p, 0, sizeof(int), s));
+    launch(k_nz_fill, blocks_for(((rows + 3) / 4) * 32, 256), 256, 0, s, rows,
+           (const int *)I.rowptr.p, (const int *)I.colidx.p, (const double *)I.vals.p,
+           (const long long *)nzoff.p, I.nz_rowptr.p, I.nz_colidx.p, I.nz_vals.p);
+  }
 
   // P^T by a stable sort on the column (rows stay ascending per column).
   Stage st_t("tmrg_transpose");
   const int cbits = bits_for(I.cols + 1);
-  DBuf<uint64_t> tk(nnz, s);
-  DBuf<uint32_t> tp(nnz, s);
+  DBuf<uint64_t> tk(nnz_nz, s);
+  DBuf<uint32_t> tp(nnz_nz, s);
   launch(k_t_keys, blocks_for(rows * 8, 256), 256, 0, s, rows,
-         (const int *)I.rowptr.p, (const int *)I.colidx.p, tk.p, tp.p);
-  radix_sort(tk, &tp, nnz, cbits, s);
-  I.t_colidx.alloc(nnz + 1, s);
-  I.t_vals.alloc(nnz + 1, s);
+         I.ap_rowptr(), I.ap_colidx(), tk.p, tp.p);
+  radix_sort(tk, &tp, nnz_nz, cbits, s);
+  I.t_colidx.alloc(nnz_nz + 1, s);
+  I.t_vals.alloc(nnz_nz + 1, s);
   I.t_rowptr.alloc(I.cols + 1, s);
-  launch(k_t_fill, blocks_for(nnz, 256), 256, 0, s, nnz, (const uint64_t *)tk.p,
-         (const uint32_t *)tp.p, (const double *)I.vals.p, I.t_colidx.p, I.t_vals.p,
+  launch(k_t_fill, blocks_for(nnz_nz, 256), 256, 0, s, nnz_nz, (const uint64_t *)tk.p,
+         (const uint32_t *)tp.p, I.ap_vals(), I.t_colidx.p, I.t_vals.p,
          I.t_rowptr.p);
-  launch(k_t_tail, blocks_for(I.cols + 1, 256), 256, 0, s, I.cols, nnz,
+  launch(k_t_tail, blocks_for(I.cols + 1, 256), 256, 0, s, I.cols, nnz_nz,
          (const uint64_t *)tk.p, I.t_rowptr.p);
-  I.colsum.alloc(I.cols + 1, s);
-  launch(k_rowsum, blocks_for(I.cols, 256), 256, 0, s, I.cols,
-         (const int *)I.t_rowptr.p, (const double *)I.t_vals.p, I.colsum.p);
   TMRG_CUDA(cudaStreamSynchronize(s));
+}
+
+// Column sums of P for the weight-normalised transpose, on first use.
+static void interp_colsum(Interp &I) {
+  if (I.have_colsum) return;
+  I.colsum.alloc(I.cols + 1, I.s);
+  launch(k_rowsum, blocks_for(I.cols, 256), 256, 0, I.s, I.cols,
+         (const int *)I.t_rowptr.p, (const double *)I.t_vals.p, I.colsum.p);
+  I.have_colsum = true;
 }
 
 // ---------------------------------------------------------------------
@@ -669,7 +938,7 @@ static void apply2(long long rows, long long nnz, int nvec2, const int *rp,
   // per warp when the lanes allow
   double avg = rows ? (double)nnz / (double)rows : 0.0;
   if (LPR == 8) {
-    if (avg >= 48)
+    if (avg >= 24)
       launch((k_csr_apply_split<8, 4>), blocks_for(rows * 32, 256), 256, 0, s, rows,
              nvec2, rp, ci, v, (const double2 *)x, (double2 *)y, scale);
     else
@@ -685,48 +954,37 @@ void interp_apply(Interp &I, int which, const double *x, double *y, int nvec) {
   Stage st(which == 0 ? "tmrg_interp_mult" : "tmrg_interp_mult_transpose");
   if (nvec <= 0) throw Error(TMRG_ERR_ARG, "interp apply: nvec <= 0");
   cudaStream_t s = I.s;
+  if (which == 2) interp_colsum(I);
+  const long long nin = (which == 0) ? I.cols : I.rows;
+  const long long nout = (which == 0) ? I.rows : I.cols;
+  const int *rp = which == 0 ? I.ap_rowptr() : I.t_rowptr.p;
+  const int *ci = which == 0 ? I.ap_colidx() : I.t_colidx.p;
+  const double *v = which == 0 ? I.ap_vals() : I.t_vals.p;
+  const double *sc = which == 2 ? (const double *)I.colsum.p : (const double *)nullptr;
+  // compulsory traffic: 12 B per nonzero entry, the row pointers, one read
+  // of the input and one write of the output vectors
+  const long long bytes = 12 * I.nnz_nz + 4 * (nout + 1) + 8LL * nvec * (nin + nout) +
+                          (which == 2 ? 8 * nout : 0);
   if (nvec % 2 == 0 && ((uintptr_t)x % 16) == 0 && ((uintptr_t)y % 16) == 0) {
-    long long nin = (which == 0) ? I.cols : I.rows;
-    long long nout = (which == 0) ? I.rows : I.cols;
-    prof_bytes(12 * I.nnz + 4 * (nout + 1) + 8LL * nvec * (nin + nout) +
-               (which == 2 ? 8 * nout : 0));
-    prof_flops(2LL * nvec * I.nnz);
-    const int *rp = which == 0 ? I.rowptr.p : I.t_rowptr.p;
-    const int *ci = which == 0 ? I.colidx.p : I.t_colidx.p;
-    const double *v = which == 0 ? I.vals.p : I.t_vals.p;
-    const double *sc = which == 2 ? I.colsum.p : nullptr;
+    prof_bytes(bytes);
+    prof_flops(2LL * nvec * I.nnz_nz);
     int n2 = nvec / 2;
     if (n2 >= 8)
-      apply2<8>(nout, I.nnz, n2, rp, ci, v, x, y, sc, s);
+      apply2<8>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, s);
     else if (n2 >= 4)
-      apply2<4>(nout, I.nnz, n2, rp, ci, v, x, y, sc, s);
+      apply2<4>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, s);
     else if (n2 >= 2)
-      apply2<2>(nout, I.nnz, n2, rp, ci, v, x, y, sc, s);
+      apply2<2>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, s);
     else
-      apply2<1>(nout, I.nnz, n2, rp, ci, v, x, y, sc, s);
+      apply2<1>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, s);
     return;
   }
   int G = 1;
   while (G < nvec && G < 32) G <<= 1;
-  // compulsory traffic: 12 B per entry, the row pointers, one read of the
-  // input and one write of the output vectors
-  long long nin = (which == 0) ? I.cols : I.rows;
-  long long nout = (which == 0) ? I.rows : I.cols;
-  prof_bytes(12 * I.nnz + 4 * (nout + 1) + 8LL * nvec * (nin + nout) +
-             (which == 2 ? 8 * nout : 0));
-  prof_flops(2LL * nvec * I.nnz);
-  if (which == 0) {
-    long long threads = I.rows * G;
-    launch(k_csr_apply, blocks_for(threads, 256), 256, 0, s, I.rows, G, nvec,
-           (const int *)I.rowptr.p, (const int *)I.colidx.p,
-           (const double *)I.vals.p, x, y, (const double *)nullptr);
-  } else {
-    long long threads = I.cols * G;
-    launch(k_csr_apply, blocks_for(threads, 256), 256, 0, s, I.cols, G, nvec,
-           (const int *)I.t_rowptr.p, (const int *)I.t_colidx.p,
-           (const double *)I.t_vals.p, x, y,
-           which == 2 ? (const double *)I.colsum.p : (const double *)nullptr);
-  }
+  prof_bytes(bytes);
+  prof_flops(2LL * nvec * I.nnz_nz);
+  launch(k_csr_apply, blocks_for(nout * G, 256), 256, 0, s, nout, G, nvec, rp, ci, v, x,
+         y, sc);
 }
 
 }  // namespace tmrg
