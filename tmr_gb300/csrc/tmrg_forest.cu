@@ -61,9 +61,8 @@ __global__ void k_create_trees(long long n, int level, int *block, int *x,
                                int *y, int *z, int16_t *lev, int16_t *info) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  long long per = 1LL << (3 * level);
-  long long b = i / per;
-  uint64_t m = (uint64_t)(i - b * per);
+  long long b = i >> (3 * level);  // 8^level octants per block
+  uint64_t m = (uint64_t)(i - (b << (3 * level)));
   int s = TMRG_MAX_LEVEL - level;
   block[i] = (int)b;
   x[i] = (int)(compact3(m >> 2) << s);

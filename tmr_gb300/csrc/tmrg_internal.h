@@ -89,6 +89,7 @@ struct Interp {
   const int *ap_rowptr() const { return nnz_nz < nnz ? nz_rowptr.p : rowptr.p; }
   const int *ap_colidx() const { return nnz_nz < nnz ? nz_colidx.p : colidx.p; }
   const double *ap_vals() const { return nnz_nz < nnz ? nz_vals.p : vals.p; }
+  DBuf<int> perm;  // apply rows ordered by length inside windows
   DBuf<int> t_rowptr, t_colidx;  // P^T (zero-free) as CSR, rows = coarse nodes
   DBuf<double> t_vals;
   bool have_colsum = false;

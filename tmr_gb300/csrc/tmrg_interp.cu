@@ -56,13 +56,19 @@ __global__ void k_pack_octs(long long n, const int *__restrict__ b,
   if (i < n) out[i] = make_int4(b[i] | ((int)l[i] << 26), x[i], y[i], z[i]);
 }
 
-__global__ void k_first_ref(long long m, int npe, long long nowned,
+// First reference of every owned fine node in (element, local index)
+// order, packed element << 8 | local (npe <= 216): decoding takes shifts,
+// not a 64-bit division (which GB300 runs on its scarce FP64 pipe).
+__global__ void k_first_ref(long long n, int npe, long long nowned,
                             const int *__restrict__ conn,
                             unsigned long long *rep) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= m) return;
-  int c = conn[t];
-  if (c >= 0 && c < nowned) atomicMin(rep + c, (unsigned long long)t);
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int *c = conn + e * npe;
+  for (int l = 0; l < npe; l++) {
+    int v = __ldg(c + l);
+    if (v >= 0 && v < nowned) atomicMin(rep + v, ((unsigned long long)e << 8) | (unsigned)l);
+  }
 }
 
 // ---------------------------------------------------------------------
@@ -279,10 +285,10 @@ __device__ __forceinline__ unsigned box_mask(int co, int rx, int ry, int rz) {
 __device__ __forceinline__ long long row_box(const InterpCtx &I, long long row,
                                              Oct &node, int &info, int4 &cq,
                                              int r[3], unsigned &bm) {
-  const int mo = I.fo, co = I.co, fnpe = mo * mo * mo;
+  const int mo = I.fo, co = I.co;
   unsigned long long rr = I.rep[row];
-  long long e = (long long)(rr / fnpe);
-  info = (int)(rr - (unsigned long long)e * fnpe);
+  long long e = (long long)(rr >> 8);
+  info = (int)(rr & 255u);
   node = Oct{I.fb[e], I.fx[e], I.fy[e], I.fz[e], I.fl[e]};
   long long t = find_enclosing(I, node, info);
   bm = 0;
@@ -370,7 +376,7 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
   const unsigned lt = (1u << lane) - 1u;
   const long long base = ((long long)blockIdx.x * IW_WARPS + warp) * 32;
   if (base >= rows) return;
-  const int mo = I.fo, co = I.co, co2 = co * co, fnpe = mo * mo * mo;
+  const int mo = I.fo, co = I.co, co2 = co * co;
   // phase A
   {
     long long row = base + lane;
@@ -383,8 +389,8 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
         eo = I.eoff[t];
         E = (int)(I.eoff[t + 1] - eo);
         unsigned long long rr = I.rep[row];
-        long long e = (long long)(rr / fnpe);
-        int info = (int)(rr - (unsigned long long)e * fnpe);
+        long long e = (long long)(rr >> 8);
+        int info = (int)(rr & 255u);
         Oct node{I.fb[e], I.fx[e], I.fy[e], I.fz[e], I.fl[e]};
         int4 cq = __ldg(I.c4 + t);
         int cl = cq.x >> 26;
@@ -631,6 +637,40 @@ __global__ void k_t_tail(long long ncols, long long nnz, const uint64_t *__restr
   int clast = nnz ? (int)(keys[nnz - 1] & 0xffffffffu) : -1;
   if (j > clast && j <= ncols) trowptr[j] = (int)nnz;
 }
+// Rows ordered by length inside windows of LO_WIN rows (one block per
+// window, counting sort on min(length, LO_BUCKETS - 1)); the order inside a
+// bucket does not matter, each row's sum is independent of it.
+constexpr int LO_WIN = 4096, LO_BUCKETS = 64, LO_THREADS = 256;
+__global__ void __launch_bounds__(LO_THREADS)
+    k_len_order(long long rows, const int *__restrict__ rp, int *perm) {
+  __shared__ int s_cnt[LO_BUCKETS], s_off[LO_BUCKETS];
+  const long long w0 = (long long)blockIdx.x * LO_WIN;
+  if (threadIdx.x < LO_BUCKETS) s_cnt[threadIdx.x] = 0;
+  __syncthreads();
+  int b[LO_WIN / LO_THREADS];
+#pragma unroll
+  for (int k = 0; k < LO_WIN / LO_THREADS; k++) {
+    const long long r = w0 + threadIdx.x + k * LO_THREADS;
+    b[k] = -1;
+    if (r < rows) {
+      b[k] = min(__ldg(rp + r + 1) - __ldg(rp + r), LO_BUCKETS - 1);
+      atomicAdd(&s_cnt[b[k]], 1);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int a = 0;
+    for (int i = 0; i < LO_BUCKETS; i++) {
+      s_off[i] = a;
+      a += s_cnt[i];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < LO_WIN / LO_THREADS; k++)
+    if (b[k] >= 0)
+      perm[w0 + atomicAdd(&s_off[b[k]], 1)] = (int)(w0 + threadIdx.x + k * LO_THREADS);
+}
 __global__ void k_rowsum(long long rows, const int *__restrict__ rowptr,
                          const double *__restrict__ vals, double *sum) {
   long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -664,8 +704,7 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   I.cols = coarse.num_owned;
   DBuf<unsigned long long> rep(rows + 1, s);
   rep.fill_bytes(0xff);
-  long long m = fine.n * fnpe;
-  launch(k_first_ref, blocks_for(m, 256), 256, 0, s, m, fnpe, rows,
+  launch(k_first_ref, blocks_for(fine.n, 256), 256, 0, s, fine.n, fnpe, rows,
          (const int *)fine.econn.p, rep.p);
   DBuf<int> err(1, s);
   err.zero();
@@ -771,17 +810,21 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
            (const long long *)nzoff.p, I.nz_rowptr.p, I.nz_colidx.p, I.nz_vals.p);
   }
 
+  I.perm.alloc(rows + 1, s);
+  launch(k_len_order, blocks_for(rows, LO_WIN), LO_THREADS, 0, s, rows, I.ap_rowptr(),
+         I.perm.p);
+
   // P^T by a stable sort on the column (rows stay ascending per column).
   Stage st_t("tmrg_transpose");
+  I.t_colidx.alloc(nnz_nz + 1, s);
+  I.t_vals.alloc(nnz_nz + 1, s);
+  I.t_rowptr.alloc(I.cols + 1, s);
   const int cbits = bits_for(I.cols + 1);
   DBuf<uint64_t> tk(nnz_nz, s);
   DBuf<uint32_t> tp(nnz_nz, s);
   launch(k_t_keys, blocks_for(rows * 8, 256), 256, 0, s, rows,
          I.ap_rowptr(), I.ap_colidx(), tk.p, tp.p);
   radix_sort(tk, &tp, nnz_nz, cbits, s);
-  I.t_colidx.alloc(nnz_nz + 1, s);
-  I.t_vals.alloc(nnz_nz + 1, s);
-  I.t_rowptr.alloc(I.cols + 1, s);
   launch(k_t_fill, blocks_for(nnz_nz, 256), 256, 0, s, nnz_nz, (const uint64_t *)tk.p,
          (const uint32_t *)tp.p, I.ap_vals(), I.t_colidx.p, I.t_vals.p,
          I.t_rowptr.p);
@@ -880,22 +923,25 @@ __global__ void __launch_bounds__(256)
 // trip count (the longest row it holds) with per-entry predicates, so no
 // lane diverges: on GB300 the FP64 pipe is the bound and a diverged or
 // half-masked warp instruction costs the pipe as much as a full one.
-// Group partial sums are combined in a fixed tree order.
+// Group partial sums are combined in a fixed tree order.  With `perm` the
+// warp takes rows perm[slot] (rows ordered by length inside windows, so the
+// rows sharing a warp have equal trip counts).
 template <int LPR, int NG>
 __global__ void __launch_bounds__(256)
     k_csr_apply_split(long long rows, int nvec2, const int *__restrict__ rowptr,
                       const int *__restrict__ cols, const double *__restrict__ vals,
                       const double2 *__restrict__ x, double2 *__restrict__ y,
-                      const double *__restrict__ scale) {
+                      const double *__restrict__ scale, const int *__restrict__ perm) {
   constexpr int RPW = 32 / (LPR * NG);
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int sub = lane / (LPR * NG);       // row slot in the warp
   const int g = (lane / LPR) % NG;         // group in the row
   const int v = lane % LPR;                // vector pair
-  const long long r = warp * RPW + sub;
+  const long long slot = warp * RPW + sub;
   if (warp * RPW >= rows) return;          // uniform per warp
-  const bool have = r < rows;
+  const bool have = slot < rows;
+  const long long r = (have && perm) ? (long long)__ldg(perm + slot) : slot;
   const int p0 = have ? __ldg(rowptr + r) : 0;
   const int p1 = have ? __ldg(rowptr + r + 1) : 0;
   int trips = (p1 - p0 + NG - 1) / NG;
@@ -933,17 +979,18 @@ __global__ void __launch_bounds__(256)
 template <int LPR>
 static void apply2(long long rows, long long nnz, int nvec2, const int *rp,
                    const int *ci, const double *v, const double *x, double *y,
-                   const double *scale, cudaStream_t s) {
+                   const double *scale, const int *perm, cudaStream_t s) {
   // long rows (P^T): the whole warp on one row; short rows (P): two rows
   // per warp when the lanes allow
   double avg = rows ? (double)nnz / (double)rows : 0.0;
   if (LPR == 8) {
     if (avg >= 24)
       launch((k_csr_apply_split<8, 4>), blocks_for(rows * 32, 256), 256, 0, s, rows,
-             nvec2, rp, ci, v, (const double2 *)x, (double2 *)y, scale);
+             nvec2, rp, ci, v, (const double2 *)x, (double2 *)y, scale,
+             (const int *)nullptr);
     else
       launch((k_csr_apply_split<8, 2>), blocks_for((rows + 1) / 2 * 32, 256), 256, 0, s,
-             rows, nvec2, rp, ci, v, (const double2 *)x, (double2 *)y, scale);
+             rows, nvec2, rp, ci, v, (const double2 *)x, (double2 *)y, scale, perm);
     return;
   }
   launch(k_csr_apply2<LPR>, blocks_for(rows * LPR, 256), 256, 0, s, rows, nvec2,
@@ -961,6 +1008,7 @@ void interp_apply(Interp &I, int which, const double *x, double *y, int nvec) {
   const int *ci = which == 0 ? I.ap_colidx() : I.t_colidx.p;
   const double *v = which == 0 ? I.ap_vals() : I.t_vals.p;
   const double *sc = which == 2 ? (const double *)I.colsum.p : (const double *)nullptr;
+  const int *perm = which == 0 ? (const int *)I.perm.p : (const int *)nullptr;
   // compulsory traffic: 12 B per nonzero entry, the row pointers, one read
   // of the input and one write of the output vectors
   const long long bytes = 12 * I.nnz_nz + 4 * (nout + 1) + 8LL * nvec * (nin + nout) +
@@ -970,13 +1018,13 @@ void interp_apply(Interp &I, int which, const double *x, double *y, int nvec) {
     prof_flops(2LL * nvec * I.nnz_nz);
     int n2 = nvec / 2;
     if (n2 >= 8)
-      apply2<8>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, s);
+      apply2<8>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, perm, s);
     else if (n2 >= 4)
-      apply2<4>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, s);
+      apply2<4>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, perm, s);
     else if (n2 >= 2)
-      apply2<2>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, s);
+      apply2<2>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, perm, s);
     else
-      apply2<1>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, s);
+      apply2<1>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, perm, s);
     return;
   }
   int G = 1;

@@ -172,8 +172,10 @@ __global__ void k_node_keys(long long n, ConnDev c, NodeGen g,
                             uint32_t *vals) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * g.nobj) return;
-  long long e = t / g.nobj;
-  int j = (int)(t - e * g.nobj);
+  // t < 2^32 (it is stored as a 32-bit value): a 32-bit division
+  const unsigned tu = (unsigned)t;
+  long long e = tu / (unsigned)g.nobj;
+  int j = (int)(tu - (unsigned)e * (unsigned)g.nobj);
   Oct o{blk[e], xs[e], ys[e], zs[e], lev[e]};
   int32_t b = o.block, x, y, z;
   int label, mult, ed;

@@ -254,16 +254,16 @@ void exclusive_scan(const T *in, T *out, long long n, cudaStream_t s) {
 // warp come from __match_any_sync peer groups in key order, across warps
 // from a per-digit prefix in shared memory, across tiles from a
 // digit-major scan of the tile histograms.
-constexpr int RS_THREADS = 256;
-constexpr int RS_ITEMS = 16;
+constexpr int RS_THREADS = 512;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_ITEMS = 8;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 
 static __global__ void __launch_bounds__(RS_THREADS)
     k_radix_hist(const uint64_t *__restrict__ kin, long long n, int shift,
                  uint32_t *__restrict__ hist, unsigned nblocks) {
-  __shared__ uint32_t wh[RS_THREADS / 32][256];
-  for (int i = threadIdx.x; i < (RS_THREADS / 32) * 256; i += RS_THREADS)
-    (&wh[0][0])[i] = 0;
+  __shared__ uint32_t wh[RS_WARPS][256];
+  for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) (&wh[0][0])[i] = 0;
   __syncthreads();
   int warp = threadIdx.x >> 5;
   long long base = (long long)blockIdx.x * RS_TILE;
@@ -272,24 +272,35 @@ static __global__ void __launch_bounds__(RS_THREADS)
     if (idx < n) atomicAdd(&wh[warp][(uint32_t)(kin[idx] >> shift) & 0xFFu], 1u);
   }
   __syncthreads();
-  uint32_t t = 0;
-  for (int w = 0; w < RS_THREADS / 32; w++) t += wh[w][threadIdx.x];
-  hist[(size_t)threadIdx.x * nblocks + blockIdx.x] = t;
+  for (int d = threadIdx.x; d < 256; d += RS_THREADS) {
+    uint32_t t = 0;
+    for (int w = 0; w < RS_WARPS; w++) t += wh[w][d];
+    hist[(size_t)d * nblocks + blockIdx.x] = t;
+  }
 }
 
+// One tile of RS_TILE keys per block, 16 warps x 8 keys per lane (64
+// registers a thread, two blocks per SM).  Ranks inside the tile come from
+// __match_any_sync per warp-row and per-warp digit counters; keys (and
+// values) are staged in tile order of their digit and written out as one
+// contiguous run per digit.
 template <bool VALS>
 __global__ void __launch_bounds__(RS_THREADS, 2)
     k_radix_scatter(const uint64_t *__restrict__ kin,
                     const uint32_t *__restrict__ vin, uint64_t *__restrict__ kout,
                     uint32_t *__restrict__ vout, long long n, int shift,
                     const uint32_t *__restrict__ offs, unsigned nblocks) {
-  __shared__ uint32_t wcnt[RS_THREADS / 32][256];
-  for (int i = threadIdx.x; i < (RS_THREADS / 32) * 256; i += RS_THREADS)
-    (&wcnt[0][0])[i] = 0;
+  __shared__ uint16_t wcnt[RS_WARPS][256];
+  __shared__ uint32_t tile_off[256];
+  __shared__ uint32_t gbase[256];
+  __shared__ uint32_t wsum[8];
+  __shared__ uint64_t stage[RS_TILE];
+  __shared__ uint8_t stage_d[RS_TILE];
+  for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) (&wcnt[0][0])[i] = 0;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  long long base = (long long)blockIdx.x * RS_TILE + (long long)warp * 32 * RS_ITEMS;
+  const long long base = (long long)blockIdx.x * RS_TILE + (long long)warp * 32 * RS_ITEMS;
   uint64_t k[RS_ITEMS];
   uint32_t v[RS_ITEMS];
   uint32_t rank[RS_ITEMS];
@@ -309,38 +320,41 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
     uint32_t b = 0;
     if (ok && lane == leader) {
       b = wcnt[warp][d];
-      wcnt[warp][d] = b + __popc(peers);
+      wcnt[warp][d] = (uint16_t)(b + __popc(peers));
     }
     b = __shfl_sync(0xffffffffu, b, leader);
     rank[j] = b + __popc(peers & lt);
     __syncwarp();
   }
   __syncthreads();
-  // Per digit (one thread each): prefix over warps, the tile's digit
-  // offsets (block scan) and the digit's global base for this tile.
-  __shared__ uint32_t tile_off[256];
-  __shared__ uint32_t gbase[256];
-  __shared__ uint32_t scan_tmp[RS_THREADS / 32 + 1];
-  __shared__ uint64_t stage[RS_TILE];
-  __shared__ uint8_t stage_d[RS_TILE];
-  {
-    int d = threadIdx.x;
-    uint32_t run = 0;
-    for (int w = 0; w < RS_THREADS / 32; w++) {
+  // Per digit (threads 0..255): prefix over warps, then the tile's digit
+  // offsets (exclusive scan over digits) and the digit's global base.
+  uint32_t run = 0, incl = 0;
+  if (threadIdx.x < 256) {
+    const int d = threadIdx.x;
+    for (int w = 0; w < RS_WARPS; w++) {
       uint32_t c = wcnt[w][d];
-      wcnt[w][d] = run;
+      wcnt[w][d] = (uint16_t)run;
       run += c;
     }
-    uint32_t total;
-    uint32_t off = block_exclusive_scan<uint32_t>(run, scan_tmp, total);
-    tile_off[d] = off;
-    gbase[d] = offs[(size_t)d * nblocks + blockIdx.x];
+    incl = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[warp] = incl;
   }
   __syncthreads();
-  long long tile_base = (long long)blockIdx.x * RS_TILE;
-  int cnt = (int)min((long long)RS_TILE, n - tile_base);
-  // Stage keys in tile order of their digit, then write each digit's run
-  // contiguously.
+  if (threadIdx.x < 256) {
+    uint32_t pre = 0;
+    for (int w = 0; w < warp; w++) pre += wsum[w];
+    tile_off[threadIdx.x] = pre + incl - run;
+    gbase[threadIdx.x] = offs[(size_t)threadIdx.x * nblocks + blockIdx.x];
+  }
+  __syncthreads();
+  const long long tile_base = (long long)blockIdx.x * RS_TILE;
+  const int cnt = (int)min((long long)RS_TILE, n - tile_base);
 #pragma unroll
   for (int j = 0; j < RS_ITEMS; j++) {
     long long idx = base + j * 32 + lane;
