@@ -133,9 +133,11 @@ def gpu_pipeline(TMR, conn, W, x_fine=None, host=False, prefetched=None):
             h2d += cols * nv * 8
             d2h += rows * nv * 8
             x, k = y, k + 1
-        octs = f.getOctantsArray()
-        conn_f = f.getMeshConn()
-        d2h += octs.nbytes + conn_f.nbytes
+        # the reference getters' borrowed views (TMROctForest::getOctants,
+        # getNodeConn): page-locked host copies owned by the forest
+        octs = f.getOctants()
+        conn_f = f.getMeshConn(copy=False)
+        d2h += octs.array.nbytes + conn_f.nbytes
         out["checksum"] = float(x[:16].sum())
     else:
         x = x_fine

@@ -116,6 +116,31 @@ int tmrg_forest_node_conn_device(tmrg_forest *f, const int **conn);
 int tmrg_forest_dep_node_conn_device(tmrg_forest *f, const int **ptr,
                                      const int **conn, const double **w);
 
+/* Borrowed host views, the reference getters' own semantics: pointers into
+   page-locked host memory owned by the forest, valid until the next call
+   that changes the forest (setConnectivity, setMeshOrder, createTrees,
+   refine, balance, createNodes) or its destruction.  Built on first
+   request after a change.
+   TMROctForest::getOctants (TMROctForest.h:128; TMROctForest.cpp:1452):
+   octants in TMROctant layout, tag = index. */
+typedef struct {
+  int32_t block, x, y, z, tag;
+  int16_t level, info;
+} tmrg_octant; /* TMROctant field layout (TMROctant.h:47-52), 24 bytes */
+int tmrg_forest_octants_host(tmrg_forest *f, const tmrg_octant **octs,
+                             int64_t *n);
+/* TMROctForest::getNodeConn (TMROctForest.h:108; TMROctForest.cpp:5686). */
+int tmrg_forest_node_conn_host(tmrg_forest *f, const int **conn,
+                               int64_t *num_elements);
+/* TMROctForest::getDepNodeConn (TMROctForest.h:110;
+   TMROctForest.cpp:5717); *num_dep is the reference's return value. */
+int tmrg_forest_dep_node_conn_host(tmrg_forest *f, const int **ptr,
+                                   const int **conn, const double **weights,
+                                   int64_t *num_dep);
+/* Returns the page-locked blocks kept for reuse by host views to the
+   system (no reference counterpart). */
+int tmrg_host_pool_trim(void);
+
 /* ---- interpolation (prolongation P: coarse -> fine) ------------------- */
 /* TMROctForest::createInterpolation(TMROctForest *coarse, TACSBVecInterp*)
    (TMROctForest.h:115; TMROctForest.cpp:6611-6793).  Rows are the fine

@@ -37,14 +37,20 @@ class TMROctant {
   int16_t level, info;
 };
 
-// Host snapshot of the octants (TMROctantArray, TMROctant.h:65-81).
+static_assert(sizeof(TMROctant) == sizeof(tmrg_octant), "TMROctant layout");
+
+// The octants (TMROctantArray, TMROctant.h:65-81): a view of the forest's
+// page-locked host octants, which the forest owns, valid until the forest
+// changes (the reference's getOctants hands out its own array the same
+// way).
 class TMROctantArray {
  public:
   void getArray(TMROctant **a, int *size) {
-    if (a) *a = array.data();
-    if (size) *size = (int)array.size();
+    if (a) *a = ptr;
+    if (size) *size = (int)n;
   }
-  std::vector<TMROctant> array;
+  TMROctant *ptr = nullptr;
+  int64_t n = 0;
 };
 
 class TMRGEntity {
@@ -155,22 +161,14 @@ class TMROctForest : public TMRGEntity {
   void createNodes() { tmrg_report(tmrg_forest_create_nodes(f), "createNodes"); }
 
   void getOctants(TMROctantArray **octs) {
+    const tmrg_octant *p = nullptr;
     int64_t n = 0;
-    tmrg_forest_num_octants(f, &n);
-    std::vector<int> raw(7 * (size_t)n);
-    if (n && !tmrg_report(tmrg_forest_get_octants(f, raw.data(), n), "getOctants"))
+    if (!tmrg_report(tmrg_forest_octants_host(f, &p, &n), "getOctants")) {
+      p = nullptr;
       n = 0;
-    octants_.array.resize((size_t)n);
-    for (int64_t i = 0; i < n; i++) {
-      TMROctant &o = octants_.array[(size_t)i];
-      o.block = raw[7 * i];
-      o.x = raw[7 * i + 1];
-      o.y = raw[7 * i + 2];
-      o.z = raw[7 * i + 3];
-      o.tag = raw[7 * i + 4];
-      o.level = (int16_t)raw[7 * i + 5];
-      o.info = (int16_t)raw[7 * i + 6];
     }
+    octants_.ptr = reinterpret_cast<TMROctant *>(const_cast<tmrg_octant *>(p));
+    octants_.n = n;
     if (octs) *octs = &octants_;
   }
   void getNodeConn(const int **conn = nullptr, int *num_elements = nullptr,
@@ -178,28 +176,27 @@ class TMROctForest : public TMRGEntity {
                    int *num_local_nodes = nullptr) {
     int64_t s[6] = {0};
     tmrg_forest_node_sizes(f, s);
-    int o = getMeshOrder();
-    conn_.resize((size_t)(s[4] * o * o * o));
-    if (conn && !conn_.empty())
-      tmrg_report(tmrg_forest_get_node_conn(f, conn_.data(), (int64_t)conn_.size()),
-                  "getNodeConn");
-    if (conn) *conn = conn_.data();
+    if (conn) {
+      const int *p = nullptr;
+      *conn = tmrg_report(tmrg_forest_node_conn_host(f, &p, nullptr), "getNodeConn")
+                  ? p
+                  : nullptr;
+    }
     if (num_elements) *num_elements = (int)s[4];
     if (num_owned_nodes) *num_owned_nodes = (int)s[1];
     if (num_local_nodes) *num_local_nodes = (int)s[0];
   }
   int getDepNodeConn(const int **ptr = nullptr, const int **conn = nullptr,
                      const double **weights = nullptr) {
-    int64_t s[6] = {0};
-    tmrg_forest_node_sizes(f, s);
-    dptr_.resize((size_t)s[2] + 1);
-    dconn_.resize((size_t)s[5]);
-    dw_.resize((size_t)s[5]);
-    tmrg_forest_get_dep_node_conn(f, dptr_.data(), dconn_.data(), dw_.data());
-    if (ptr) *ptr = dptr_.data();
-    if (conn) *conn = dconn_.data();
-    if (weights) *weights = dw_.data();
-    return (int)s[2];
+    const int *p = nullptr, *c = nullptr;
+    const double *w = nullptr;
+    int64_t nd = 0;
+    if (!tmrg_report(tmrg_forest_dep_node_conn_host(f, &p, &c, &w, &nd), "getDepNodeConn"))
+      nd = 0;
+    if (ptr) *ptr = p;
+    if (conn) *conn = c;
+    if (weights) *weights = w;
+    return (int)nd;
   }
   int getOwnedNodeRange(const int **node_range) {
     int64_t s[6] = {0};
@@ -247,8 +244,8 @@ class TMROctForest : public TMRGEntity {
   tmrg_forest *f;
   void *stream;
   TMROctantArray octants_;
-  std::vector<int> conn_, dptr_, dconn_, nn_;
-  std::vector<double> dw_, knots_;
+  std::vector<int> nn_;
+  std::vector<double> knots_;
   int range_[2];
 };
 

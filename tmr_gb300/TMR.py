@@ -27,6 +27,18 @@ def _ptr(a):
     return a.ctypes.data_as(_vp)
 
 
+def _host_view(addr, n, dtype):
+    """Read-only numpy view of n items at a host address owned by the
+    library (empty when n == 0)."""
+    dt = np.dtype(dtype)
+    if n <= 0 or not addr:
+        return np.zeros(0, dt)
+    buf = (ctypes.c_char * (n * dt.itemsize)).from_address(addr)
+    a = np.frombuffer(buf, dtype=dt, count=n)
+    a.flags.writeable = False
+    return a
+
+
 def _is_torch(a):
     return type(a).__module__.startswith("torch")
 
@@ -54,28 +66,53 @@ class Octant:
             self.block, self.x, self.y, self.z, self.tag, self.level, self.info)
 
 
-class OctantArray:
-    """Host snapshot of a forest's octants (TMR.pyx:3270-3330)."""
+# TMROctant layout (TMROctant.h:47-52): five int32 then two int16, 24 bytes
+OCTANT_DTYPE = np.dtype([("block", "<i4"), ("x", "<i4"), ("y", "<i4"), ("z", "<i4"),
+                         ("tag", "<i4"), ("level", "<i2"), ("info", "<i2")])
 
-    def __init__(self, arr7):
-        self.array = arr7  # (n, 7) int32 {block, x, y, z, tag, level, info}
+
+class OctantArray:
+    """A forest's octants (TMR.pyx:3270-3330).  Built over an (n, 7) int32
+    array {block, x, y, z, tag, level, info} or over a structured
+    OCTANT_DTYPE array; OctForest.getOctants() returns the latter as a
+    borrowed view of the forest's host octants (valid until the forest
+    changes, like the reference's OctantArray that does not own its
+    array)."""
+
+    def __init__(self, arr, owner=None):
+        self.array = arr
+        self._owner = owner  # keeps the forest (and its host view) alive
 
     def __len__(self):
         return self.array.shape[0]
+
+    def _fields(self):
+        a = self.array
+        if a.dtype.names:
+            return a["block"], a["x"], a["y"], a["z"], a["tag"], a["level"], a["info"]
+        return tuple(a[:, j] for j in range(7))
+
+    def asArray7(self):
+        """(n, 7) int32 copy {block, x, y, z, tag, level, info}."""
+        if not self.array.dtype.names:
+            return np.array(self.array, dtype=np.intc)
+        return np.stack(self._fields(), axis=1).astype(np.intc)
 
     def __getitem__(self, k):
         n = len(self)
         if k < 0 or k >= n:
             raise IndexError("Octant array index %d out of range [0,%d)" % (k, n))
         r = self.array[k]
-        return Octant(int(r[0]), int(r[1]), int(r[2]), int(r[3]), int(r[4]),
-                      int(r[5]), int(r[6]))
+        return Octant(*(int(v) for v in (tuple(r) if self.array.dtype.names else r)))
 
     def __setitem__(self, k, oc):
         n = len(self)
         if k < 0 or k >= n:
             raise IndexError("Octant array index %d out of range [0,%d)" % (k, n))
-        self.array[k] = [oc.block, oc.x, oc.y, oc.z, oc.tag, oc.level, oc.info]
+        if not self.array.flags.writeable:
+            raise ValueError("borrowed octant view is read-only")
+        v = (oc.block, oc.x, oc.y, oc.z, oc.tag, oc.level, oc.info)
+        self.array[k] = v if self.array.dtype.names else list(v)
 
 
 class OctForest:
@@ -183,7 +220,13 @@ class OctForest:
         return out
 
     def getOctants(self):
-        return OctantArray(self.getOctantsArray())
+        """Borrowed view of the octants in page-locked host memory
+        (TMROctForest::getOctants, TMROctForest.cpp:1452), valid until the
+        next call that changes this forest."""
+        p = _vp()
+        n = ctypes.c_int64()
+        call("tmrg_forest_octants_host", self.ptr, ctypes.byref(p), ctypes.byref(n))
+        return OctantArray(_host_view(p.value, n.value, OCTANT_DTYPE), owner=self)
 
     def getOctantsDevice(self):
         """Borrowed CUDA torch views of the octant arrays (block, x, y, z as
@@ -212,9 +255,18 @@ class OctForest:
     def getExtPreOffset(self):
         return int(self._sizes()[3])
 
-    def getMeshConn(self):
-        s = self._sizes()
+    def getMeshConn(self, copy=True):
+        """(elements, order^3) global node numbers, dependent nodes -k-1.
+        copy=False returns the borrowed read-only view of the forest's
+        page-locked host connectivity (TMROctForest::getNodeConn,
+        TMROctForest.cpp:5686), valid until the forest changes."""
         o = self.getMeshOrder()
+        if not copy:
+            p = _vp()
+            ne = ctypes.c_int64()
+            call("tmrg_forest_node_conn_host", self.ptr, ctypes.byref(p), ctypes.byref(ne))
+            return _host_view(p.value, ne.value * o ** 3, np.intc).reshape(ne.value, o ** 3)
+        s = self._sizes()
         n = int(s[4]) * o ** 3
         out = np.zeros(n, np.intc)
         if n:
@@ -228,7 +280,18 @@ class OctForest:
             call("tmrg_forest_get_node_numbers", self.ptr, _ptr(out), out.size)
         return out
 
-    def getDepNodeConn(self):
+    def getDepNodeConn(self, copy=True):
+        """(ptr, conn, weights) of the dependent nodes; copy=False returns
+        borrowed read-only views (TMROctForest::getDepNodeConn,
+        TMROctForest.cpp:5717)."""
+        if not copy:
+            p, c, w = _vp(), _vp(), _vp()
+            nd = ctypes.c_int64()
+            call("tmrg_forest_dep_node_conn_host", self.ptr, ctypes.byref(p), ctypes.byref(c),
+                 ctypes.byref(w), ctypes.byref(nd))
+            ptr = _host_view(p.value, nd.value + 1, np.intc)
+            nnz = int(ptr[-1]) if nd.value >= 0 else 0
+            return ptr, _host_view(c.value, nnz, np.intc), _host_view(w.value, nnz, np.float64)
         s = self._sizes()
         ndep, nnz = int(s[2]), int(s[5])
         ptr = np.zeros(ndep + 1, np.intc)

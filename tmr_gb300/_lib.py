@@ -47,6 +47,10 @@ _SIGS = {
     "tmrg_forest_get_dep_node_conn": [c_vp, c_vp, c_vp, c_vp],
     "tmrg_forest_node_conn_device": [c_vp, P(c_vp)],
     "tmrg_forest_dep_node_conn_device": [c_vp, P(c_vp), P(c_vp), P(c_vp)],
+    "tmrg_forest_octants_host": [c_vp, P(c_vp), P(c_i64)],
+    "tmrg_forest_node_conn_host": [c_vp, P(c_vp), P(c_i64)],
+    "tmrg_forest_dep_node_conn_host": [c_vp, P(c_vp), P(c_vp), P(c_vp), P(c_i64)],
+    "tmrg_host_pool_trim": [],
     "tmrg_interp_create": [c_vp, c_vp, P(c_vp)],
     "tmrg_interp_destroy": [c_vp],
     "tmrg_interp_sizes": [c_vp, c_vp],

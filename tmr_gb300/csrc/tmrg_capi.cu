@@ -11,8 +11,76 @@
 
 using namespace tmrg;
 
+// ---------------------------------------------------------------------
+// Pinned host memory, pooled.  Borrowed host views of a forest (octants,
+// connectivity, dependent CSR) live in page-locked memory so that the
+// device writes them at the host link's full rate; a fresh pageable buffer
+// is first touched page by page during the copy, an order of magnitude
+// slower.  Blocks come in power-of-two sizes from 1 MiB and go back to the
+// pool when a forest is destroyed or its views are rebuilt;
+// tmrg_host_pool_trim() returns them to the system.
+namespace {
+struct PinnedBlock {
+  void *p = nullptr;
+  size_t cap = 0;
+};
+std::mutex g_pin_mu;
+std::multimap<size_t, void *> g_pin_free;
+
+PinnedBlock pin_get(size_t bytes) {
+  size_t cap = size_t(1) << 20;
+  while (cap < bytes) cap <<= 1;
+  {
+    std::lock_guard<std::mutex> g(g_pin_mu);
+    auto it = g_pin_free.find(cap);
+    if (it != g_pin_free.end()) {
+      PinnedBlock b{it->second, cap};
+      g_pin_free.erase(it);
+      return b;
+    }
+  }
+  void *p = nullptr;
+  if (cudaMallocHost(&p, cap) != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(TMRG_ERR_NOMEM,
+                "pinned host allocation of " + std::to_string(cap) + " bytes failed");
+  }
+  return PinnedBlock{p, cap};
+}
+void pin_put(PinnedBlock &b) {
+  if (!b.p) return;
+  std::lock_guard<std::mutex> g(g_pin_mu);
+  g_pin_free.emplace(b.cap, b.p);
+  b = PinnedBlock{};
+}
+void pin_ensure(PinnedBlock &b, size_t bytes) {
+  if (b.p && b.cap >= bytes) return;
+  pin_put(b);
+  b = pin_get(bytes);
+}
+
+// Host views of one forest and the forest generation they were made from.
+struct HostMirror {
+  uint64_t oct_gen = ~0ULL, conn_gen = ~0ULL, dep_gen = ~0ULL;
+  PinnedBlock octs, conn, dptr, dconn, dw;
+  void release() {
+    pin_put(octs);
+    pin_put(conn);
+    pin_put(dptr);
+    pin_put(dconn);
+    pin_put(dw);
+    oct_gen = conn_gen = dep_gen = ~0ULL;
+  }
+};
+}  // namespace
+
 struct tmrg_forest {
   Forest f;
+  // bumped by every call that changes the octants or nodes; a host view
+  // made from an older generation is rebuilt on request
+  uint64_t gen = 0;
+  HostMirror m;
+  ~tmrg_forest() { m.release(); }
 };
 struct tmrg_interp {
   Interp I;
@@ -72,6 +140,16 @@ static int guarded(Fn &&fn) {
     if (!(cond)) throw Error(TMRG_ERR_ARG, std::string(msg)); \
   } while (0)
 
+// Device-usable address of page-locked host memory (cudaMallocHost,
+// cudaHostAlloc, registered), or null for any other pointer.
+static void *host_mapped(void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (a.type == cudaMemoryTypeHost) ? a.devicePointer : nullptr;
+}
 static void copy_d2h(void *dst, const void *src, size_t bytes, cudaStream_t s) {
   if (!bytes) return;
   TMRG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
@@ -213,6 +291,7 @@ int tmrg_forest_set_connectivity(tmrg_forest *f, int num_nodes,
                                  const int *block_conn, int num_blocks) {
   return guarded([&] {
     ARG(f && block_conn, "NULL argument");
+    f->gen++;
     // validate and build first: a rejected connectivity leaves the forest
     // as it was
     auto c = build_conn(num_nodes, block_conn, num_blocks, f->f.s);
@@ -225,6 +304,7 @@ int tmrg_forest_set_connectivity(tmrg_forest *f, int num_nodes,
 int tmrg_forest_set_mesh_order(tmrg_forest *f, int order, int interp_type) {
   return guarded([&] {
     ARG(f, "NULL forest");
+    f->gen++;
     ARG(interp_type >= 0 && interp_type <= 2, "bad interpolation type");
     f->f.set_order(order, interp_type);
   });
@@ -245,6 +325,7 @@ int tmrg_forest_get_interp_knots(tmrg_forest *f, double *knots) {
 int tmrg_forest_create_trees(tmrg_forest *f, int level) {
   return guarded([&] {
     ARG(f, "NULL forest");
+    f->gen++;
     forest_create_trees(f->f, level);
   });
 }
@@ -252,6 +333,7 @@ int tmrg_forest_refine(tmrg_forest *f, const int *refinement, int64_t n,
                        int min_level, int max_level) {
   return guarded([&] {
     ARG(f, "NULL forest");
+    f->gen++;
     if (!refinement) {
       forest_refine(f->f, nullptr, 0, min_level, max_level);
       return;
@@ -269,6 +351,7 @@ int tmrg_forest_refine_device(tmrg_forest *f, const int *d_refinement,
                               int64_t n, int min_level, int max_level) {
   return guarded([&] {
     ARG(f, "NULL forest");
+    f->gen++;
     forest_refine(f->f, d_refinement, d_refinement ? n : 0, min_level,
                   max_level);
   });
@@ -304,6 +387,7 @@ int tmrg_forest_duplicate(tmrg_forest *f, tmrg_forest **out) {
 int tmrg_forest_balance(tmrg_forest *f, int balance_corner) {
   return guarded([&] {
     ARG(f, "NULL forest");
+    f->gen++;
     forest_balance(f->f, balance_corner ? 1 : 0);
   });
 }
@@ -313,6 +397,7 @@ int tmrg_forest_repartition(tmrg_forest *f, int) {
 int tmrg_forest_create_nodes(tmrg_forest *f) {
   return guarded([&] {
     ARG(f, "NULL forest");
+    f->gen++;
     forest_create_nodes(f->f);
   });
 }
@@ -366,6 +451,108 @@ int tmrg_forest_octants_device(tmrg_forest *f, const int **block, const int **x,
     if (info) *info = F.info.p;
   });
 }
+__global__ void k_pack_octants24(long long n, const int *__restrict__ b,
+                                 const int *__restrict__ x, const int *__restrict__ y,
+                                 const int *__restrict__ z, const int16_t *__restrict__ l,
+                                 const int16_t *__restrict__ info, tmrg_octant *out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  tmrg_octant o;
+  o.block = b[i];
+  o.x = x[i];
+  o.y = y[i];
+  o.z = z[i];
+  o.tag = (int32_t)i;
+  o.level = l[i];
+  o.info = info[i];
+  out[i] = o;
+}
+static_assert(sizeof(tmrg_octant) == 24, "TMROctant layout");
+
+int tmrg_forest_octants_host(tmrg_forest *f, const tmrg_octant **octs, int64_t *n) {
+  return guarded([&] {
+    ARG(f && octs, "NULL argument");
+    Forest &F = f->f;
+    if (!F.have_octs) throw Error(TMRG_ERR_STATE, "getOctants: no octants");
+    if (f->m.oct_gen != f->gen) {
+      f->m.oct_gen = ~0ULL;
+      pin_ensure(f->m.octs, sizeof(tmrg_octant) * (size_t)F.n);
+      // packed in HBM, then one bulk copy (24-byte stores straight over the
+      // host link run at a fraction of the copy rate)
+      DBuf<tmrg_octant> d(F.n, F.s);
+      launch(k_pack_octants24, blocks_for(F.n, 256), 256, 0, F.s, F.n,
+             (const int *)F.block.p, (const int *)F.x.p, (const int *)F.y.p,
+             (const int *)F.z.p, (const int16_t *)F.level.p, (const int16_t *)F.info.p,
+             d.p);
+      if (F.n)
+        TMRG_CUDA(cudaMemcpyAsync(f->m.octs.p, d.p, sizeof(tmrg_octant) * (size_t)F.n,
+                                  cudaMemcpyDeviceToHost, F.s));
+      TMRG_CUDA(cudaStreamSynchronize(F.s));
+      f->m.oct_gen = f->gen;
+    }
+    *octs = (const tmrg_octant *)f->m.octs.p;
+    if (n) *n = F.n;
+  });
+}
+static void conn_mirror(tmrg_forest *f) {
+  Forest &F = f->f;
+  if (!F.have_nodes) throw Error(TMRG_ERR_STATE, "no nodes: call createNodes first");
+  if (f->m.conn_gen == f->gen) return;
+  f->m.conn_gen = ~0ULL;
+  const size_t nconn = (size_t)F.n * F.order * F.order * F.order;
+  pin_ensure(f->m.conn, sizeof(int) * nconn);
+  if (nconn)
+    TMRG_CUDA(cudaMemcpyAsync(f->m.conn.p, F.econn.p, sizeof(int) * nconn,
+                              cudaMemcpyDeviceToHost, F.s));
+  TMRG_CUDA(cudaStreamSynchronize(F.s));
+  f->m.conn_gen = f->gen;
+}
+static void dep_mirror(tmrg_forest *f) {
+  Forest &F = f->f;
+  if (!F.have_nodes) throw Error(TMRG_ERR_STATE, "no nodes: call createNodes first");
+  if (f->m.dep_gen == f->gen) return;
+  f->m.dep_gen = ~0ULL;
+  pin_ensure(f->m.dptr, sizeof(int) * ((size_t)F.num_dep + 1));
+  pin_ensure(f->m.dconn, sizeof(int) * (size_t)F.dep_nnz + 1);
+  pin_ensure(f->m.dw, sizeof(double) * (size_t)F.dep_nnz + 1);
+  TMRG_CUDA(cudaMemcpyAsync(f->m.dptr.p, F.dep_ptr.p, sizeof(int) * ((size_t)F.num_dep + 1),
+                            cudaMemcpyDeviceToHost, F.s));
+  if (F.dep_nnz) {
+    TMRG_CUDA(cudaMemcpyAsync(f->m.dconn.p, F.dep_conn.p, sizeof(int) * (size_t)F.dep_nnz,
+                              cudaMemcpyDeviceToHost, F.s));
+    TMRG_CUDA(cudaMemcpyAsync(f->m.dw.p, F.dep_w.p, sizeof(double) * (size_t)F.dep_nnz,
+                              cudaMemcpyDeviceToHost, F.s));
+  }
+  TMRG_CUDA(cudaStreamSynchronize(F.s));
+  f->m.dep_gen = f->gen;
+}
+int tmrg_forest_node_conn_host(tmrg_forest *f, const int **conn, int64_t *num_elements) {
+  return guarded([&] {
+    ARG(f && conn, "NULL argument");
+    conn_mirror(f);
+    *conn = (const int *)f->m.conn.p;
+    if (num_elements) *num_elements = f->f.n;
+  });
+}
+int tmrg_forest_dep_node_conn_host(tmrg_forest *f, const int **ptr, const int **conn,
+                                   const double **weights, int64_t *num_dep) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    dep_mirror(f);
+    if (ptr) *ptr = (const int *)f->m.dptr.p;
+    if (conn) *conn = (const int *)f->m.dconn.p;
+    if (weights) *weights = (const double *)f->m.dw.p;
+    if (num_dep) *num_dep = f->f.num_dep;
+  });
+}
+int tmrg_host_pool_trim(void) {
+  return guarded([&] {
+    std::lock_guard<std::mutex> g(g_pin_mu);
+    for (auto &kv : g_pin_free) cudaFreeHost(kv.second);
+    g_pin_free.clear();
+  });
+}
+
 int tmrg_forest_node_sizes(tmrg_forest *f, int64_t out6[6]) {
   return guarded([&] {
     ARG(f && out6, "NULL argument");
@@ -472,9 +659,17 @@ static int interp_host(tmrg_interp *I, int which, const double *x, double *y,
     Interp &P = I->I;
     long long nin = (which == 0 ? P.cols : P.rows) * nvec;
     long long nout = (which == 0 ? P.rows : P.cols) * nvec;
-    DBuf<double> dx(nin, P.s), dy(nout, P.s);
+    DBuf<double> dx(nin, P.s);
     TMRG_CUDA(cudaMemcpyAsync(dx.p, x, sizeof(double) * nin,
                               cudaMemcpyHostToDevice, P.s));
+    if (double *ym = (double *)host_mapped(y)) {
+      // page-locked output: the apply writes it over the host link while
+      // it computes, instead of a copy after it
+      interp_apply(P, which, dx.p, ym, nvec);
+      TMRG_CUDA(cudaStreamSynchronize(P.s));
+      return;
+    }
+    DBuf<double> dy(nout, P.s);
     interp_apply(P, which, dx.p, dy.p, nvec);
     copy_d2h(y, dy.p, sizeof(double) * nout, P.s);
   });
