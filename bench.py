@@ -159,6 +159,15 @@ def gpu_pipeline(TMR, conn, W, x_fine=None, host=False, prefetched=None):
     return units, out
 
 
+def hierarchy(out):
+    """Octants of each level and the sizes of each level's P."""
+    lv = [{"octants": fr.getNumOctants()} for fr in out["forests"]]
+    for k, I in enumerate(out["interps"]):
+        rows, cols, nnz = I.sizes()
+        lv[k].update({"P_rows": rows, "P_cols": cols, "P_nnz": nnz})
+    return lv
+
+
 class ClockSampler:
     """nvidia-smi clocks/throttle reasons sampled every 200 ms."""
 
@@ -246,7 +255,7 @@ def roofline_entry(name, v, peak, peak_kind, fp64_peak, tot_ms):
     tfs = tflops / (tms / 1e3) / 1e12 if tflops and tms else None
     hbm_frac = gbs / peak if gbs else None
     fp_frac = tfs / fp64_peak if tfs and fp64_peak else None
-    traffic = ncu_traffic(name)
+    traffic = ncu_traffic(name, tbytes / nl if tbytes else None)
     e = {"kernel": name, "launches": nl, "avg_launch_ms": tms / nl,
          "algorithmic_bytes_per_launch": tbytes / nl if tbytes else None,
          "traffic": traffic, "step_share": tms / tot_ms,
@@ -262,19 +271,27 @@ def roofline_entry(name, v, peak, peak_kind, fp64_peak, tot_ms):
     return e
 
 
-def ncu_traffic(kernel):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary
-    (profiles/ncu_traffic.json), scaled to this workload when recorded
-    for a smaller case."""
+def base_name(k):
+    """Kernel name without template arguments or parentheses."""
+    k = k.strip("()")
+    return k.split("<")[0]
+
+
+def ncu_traffic(kernel, alg_bytes_per_launch):
+    """DRAM bytes per launch of `kernel`: the ratio of ncu-measured DRAM
+    traffic to algorithmic bytes of a captured launch (committed in
+    profiles/ncu_traffic.json, captured on a smaller case of the same
+    workload) times this run's algorithmic bytes per launch, i.e. scaled
+    by the work the launch does."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if not os.path.exists(p):
+    if not os.path.exists(p) or not alg_bytes_per_launch:
         return None
     with open(p) as fp:
         d = json.load(fp)
     e = d.get(kernel)
-    if not e:
+    if not e or not e.get("dram_over_algorithmic"):
         return None
-    return e.get("bytes_per_launch_at_workload")
+    return e["dram_over_algorithmic"] * alg_bytes_per_launch
 
 
 def cpu_sample_case():
@@ -376,8 +393,10 @@ def run_gpu(args):
     torch.cuda.synchronize()
     if args.profile_step:
         for _ in range(args.steps):
-            gpu_pipeline(TMR, conn, W, x_fine)
+            _u, o = gpu_pipeline(TMR, conn, W, x_fine)
         torch.cuda.synchronize()
+        if rank == 0:
+            print(json.dumps({"workload": W["name"], "hierarchy": hierarchy(o)}), flush=True)
         return
 
     def barrier():
@@ -395,12 +414,14 @@ def run_gpu(args):
     ev0.record()
     tot_units = 0
     for _ in range(args.steps):
-        u, _o = gpu_pipeline(TMR, conn, W, x_fine)
+        u, last = gpu_pipeline(TMR, conn, W, x_fine)
         tot_units += u
     ev1.record()
     barrier()
     clocks = clk.stop()
     launches = TMR.kernel_launch_count() - launches0
+    levels = hierarchy(last)
+    del last
     def allreduce_max(v):
         t = torch.tensor([v], dtype=torch.float64, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -424,7 +445,15 @@ def run_gpu(args):
     kernels = {}
     if prof:
         tot_ms = sum(v[1] for v in prof.values())
-        top = max(prof.items(), key=lambda kv: kv[1][1])
+        # instantiations of one kernel template (launch shapes of the same
+        # source) count as one kernel
+        fam = {}
+        for k, v in prof.items():
+            b = base_name(k)
+            a = fam.setdefault(b, [0, 0.0, 0, 0])
+            for i in range(4):
+                a[i] += v[i]
+        top = max(fam.items(), key=lambda kv: kv[1][1])
         roof = roofline_entry(top[0], top[1], peak, peak_kind, fp64_peak, tot_ms)
         apply = [(k, v) for k, v in prof.items() if "csr_apply" in k]
         if apply:
@@ -467,6 +496,7 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic (seeded)",
             "config": {"workload": W["name"], "trees": W["nx"] * W["ny"] * W["nz"],
                        "octants_per_step": tot_units // args.steps,
+                       "hierarchy": levels,
                        "parallelism": "replicas x%d" % world,
                        "l2": "working set (GBs) larger than L2; no flush"},
             "e2e": e2e, "gpu_launches": launches, "roofline": roof, "p_apply": p_apply,

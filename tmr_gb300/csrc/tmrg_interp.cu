@@ -777,6 +777,9 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   I.vals.alloc(nnz + 1, s);
   DBuf<unsigned long long> nzcount(1, s);
   nzcount.zero();
+  // compulsory traffic: the CSR entries written (12 B each) and per row
+  // its first reference, element, and offset (20 B)
+  prof_bytes(12 * nnz + 20 * rows);
   launch(k_interp_rows, blocks_for(rows, IW_WARPS * 32), IW_WARPS * 32, 0, s, rows, c,
          (const int *)trow.p, (const long long *)roff.p, I.colidx.p, I.vals.p, nzcount.p);
   trow.release();
