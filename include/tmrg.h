@@ -59,6 +59,39 @@ int tmrg_forest_destroy(tmrg_forest *f);
    TMROctForest.cpp:558-590).  block_conn: host, 8 ints per block. */
 int tmrg_forest_set_connectivity(tmrg_forest *f, int num_nodes,
                                  const int *block_conn, int num_blocks);
+/* TMROctForest::setFullConnectivity (TMROctForest.h:66-69;
+   TMROctForest.cpp:596-637): corners, edges and faces of every block given
+   (8, 12 and 6 ints per block, host); adjacency follows the given edge and
+   face numbers. */
+int tmrg_forest_set_full_connectivity(tmrg_forest *f, int num_nodes,
+                                      int num_edges, int num_faces,
+                                      int num_blocks, const int *block_conn,
+                                      const int *block_edge_conn,
+                                      const int *block_face_conn);
+/* TMROctForest::getConnectivity (TMROctForest.h:142-145;
+   TMROctForest.cpp:1633-1692): borrowed host arrays, 8 / 6 / 12 / 6 ints
+   per block; edges and faces numbered in order of first use as the
+   reference numbers them.  Valid until the connectivity is replaced. */
+int tmrg_forest_get_connectivity(tmrg_forest *f, int *nblocks, int *nfaces,
+                                 int *nedges, int *nnodes,
+                                 const int **block_conn,
+                                 const int **block_face_conn,
+                                 const int **block_edge_conn,
+                                 const int **block_face_ids);
+/* TMROctForest::getInverseConnectivity (TMROctForest.h:146-151;
+   TMROctForest.cpp:1694-1740): CSR lists of 8*block+corner,
+   12*block+edge and 6*block+face entries in block order (borrowed). */
+int tmrg_forest_get_inverse_connectivity(
+    tmrg_forest *f, const int **node_block_conn, const int **node_block_ptr,
+    const int **edge_block_conn, const int **edge_block_ptr,
+    const int **face_block_conn, const int **face_block_ptr);
+/* TMROctForest::createRandomTrees (TMROctForest.h:81;
+   TMROctForest.cpp:1838-1917): nrand octants per block at random levels in
+   [min_level, max_level] and random anchors, sorted and unique by position
+   (finest kept).  The reference draws from libc rand(); here octant i of
+   block b draws a seeded splitmix64 uniform U(seed, b, 4i+k). */
+int tmrg_forest_create_random_trees(tmrg_forest *f, int nrand, int min_level,
+                                    int max_level, uint64_t seed);
 /* TMROctForest::setMeshOrder / getMeshOrder / getInterpType
    (TMROctForest.h:72-75; TMROctForest.cpp:1389-1440). */
 int tmrg_forest_set_mesh_order(tmrg_forest *f, int order, int interp_type);
@@ -140,6 +173,55 @@ int tmrg_forest_dep_node_conn_host(tmrg_forest *f, const int **ptr,
 /* Returns the page-locked blocks kept for reuse by host views to the
    system (no reference counterpart). */
 int tmrg_host_pool_trim(void);
+
+/* TMROctForest::getLocalNodeNumber (TMROctForest.cpp:1486-1496): index of
+   global node number `node` in getNodeNumbers, or -1. */
+int tmrg_forest_get_local_node_number(tmrg_forest *f, int node, int *local);
+/* TMROctForest::getPoints (TMROctForest.cpp:1476-1482) with the node
+   locations of evaluateNodeLocations (:5524-5680): X[3*num_local_nodes],
+   each node placed by the first element (in element order) that uses it.
+   The reference evaluates a TMRTopology volume and leaves every point at 0
+   without one; here the geometry is an optional axis-aligned box per block
+   (tmrg_forest_set_block_boxes: origin xyz, extent xyz), mapping the
+   block's parameter cube linearly; without boxes every point is 0. */
+int tmrg_forest_set_block_boxes(tmrg_forest *f, const double *boxes,
+                                int num_blocks);
+int tmrg_forest_get_points(tmrg_forest *f, double *X, int64_t n);
+/* TMROctForest::evalInterp (TMROctForest.h:131-138;
+   TMROctForest.cpp:1510-1631): tensor-product shape functions of the
+   forest's order and interpolation at a parametric point pt[3] in
+   [-1,1]^3, ii fastest; N1..N3 (all or none) the first derivatives.  The
+   *_eval_interp forms take the order, type and knots explicitly. */
+int tmrg_eval_interp(int order, int interp_type, const double *knots,
+                     const double *pt, double *N, double *N1, double *N2,
+                     double *N3);
+int tmrg_forest_eval_interp(tmrg_forest *f, const double *pt, double *N,
+                            double *N1, double *N2, double *N3);
+/* Second-derivative form.  Reproduces the reference: N33 ends holding the
+   mixed (1,2) derivative and N12 is not written
+   (TMROctForest.cpp:1614-1615). */
+int tmrg_eval_interp2(int order, int interp_type, const double *knots,
+                      const double *pt, double *N, double *N1, double *N2,
+                      double *N3, double *N11, double *N22, double *N33,
+                      double *N23, double *N13, double *N12);
+int tmrg_forest_eval_interp2(tmrg_forest *f, const double *pt, double *N,
+                             double *N1, double *N2, double *N3, double *N11,
+                             double *N22, double *N33, double *N23,
+                             double *N13, double *N12);
+/* TMROctForest::findEnclosing (TMROctForest.h:155-156;
+   TMROctForest.cpp:6228-6377) for n nodes (host): each node is an element
+   octant whose `info` is the local node index in an element of `order`
+   with `knots`; index[i] = the octant of this forest the reference
+   returns, or -1 where it returns NULL.  Single rank: mpi_owner is 0. */
+int tmrg_forest_find_enclosing(tmrg_forest *f, int order, const double *knots,
+                               const tmrg_octant *nodes, int64_t n,
+                               int64_t *index);
+/* TMROctForest::transformNode (TMROctForest.h:160-161;
+   TMROctForest.cpp:3847-4039) on n nodes in place (host); edge_reversed and
+   src_face_id (optional, n ints each) as the reference reports them. */
+int tmrg_forest_transform_nodes(tmrg_forest *f, tmrg_octant *octs, int64_t n,
+                                int edge_dir, int *edge_reversed,
+                                int *src_face_id);
 
 /* ---- interpolation (prolongation P: coarse -> fine) ------------------- */
 /* TMROctForest::createInterpolation(TMROctForest *coarse, TACSBVecInterp*)

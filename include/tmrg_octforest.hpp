@@ -53,6 +53,12 @@ class TMROctantArray {
   int64_t n = 0;
 };
 
+// Node location (TMRPoint, TMRBase.h).
+class TMRPoint {
+ public:
+  double x, y, z;
+};
+
 class TMRGEntity {
  public:
   TMRGEntity() : ref_count(0) {}
@@ -119,6 +125,30 @@ class TMROctForest : public TMRGEntity {
                                              num_blocks),
                 "setConnectivity");
   }
+  void setFullConnectivity(int num_nodes, int num_edges, int num_faces, int num_blocks,
+                           const int *block_conn, const int *block_edge_conn,
+                           const int *block_face_conn) {
+    tmrg_report(tmrg_forest_set_full_connectivity(f, num_nodes, num_edges, num_faces,
+                                                  num_blocks, block_conn, block_edge_conn,
+                                                  block_face_conn),
+                "setFullConnectivity");
+  }
+  void getConnectivity(int *nblocks, int *nfaces, int *nedges, int *nnodes,
+                       const int **block_conn, const int **block_face_conn,
+                       const int **block_edge_conn, const int **block_face_ids) {
+    tmrg_report(tmrg_forest_get_connectivity(f, nblocks, nfaces, nedges, nnodes, block_conn,
+                                             block_face_conn, block_edge_conn,
+                                             block_face_ids),
+                "getConnectivity");
+  }
+  void getInverseConnectivity(const int **node_block_conn, const int **node_block_ptr,
+                              const int **edge_block_conn, const int **edge_block_ptr,
+                              const int **face_block_conn, const int **face_block_ptr) {
+    tmrg_report(tmrg_forest_get_inverse_connectivity(f, node_block_conn, node_block_ptr,
+                                                     edge_block_conn, edge_block_ptr,
+                                                     face_block_conn, face_block_ptr),
+                "getInverseConnectivity");
+  }
   void setMeshOrder(int order,
                     TMRInterpolationType t = TMR_GAUSS_LOBATTO_POINTS) {
     tmrg_report(tmrg_forest_set_mesh_order(f, order, t), "setMeshOrder");
@@ -142,6 +172,13 @@ class TMROctForest : public TMRGEntity {
   }
   void createTrees(int refine_level) {
     tmrg_report(tmrg_forest_create_trees(f, refine_level), "createTrees");
+  }
+  // The reference draws from libc rand(); this draws from a seeded
+  // generator (tmrg_forest_create_random_trees).
+  void createRandomTrees(int nrand = 10, int min_level = 0, int max_level = 8,
+                         uint64_t seed = 0) {
+    tmrg_report(tmrg_forest_create_random_trees(f, nrand, min_level, max_level, seed),
+                "createRandomTrees");
   }
   void repartition(int max_rank = -1) {
     tmrg_report(tmrg_forest_repartition(f, max_rank), "repartition");
@@ -214,6 +251,91 @@ class TMROctForest : public TMRGEntity {
     if (node_numbers) *node_numbers = nn_.data();
     return (int)s[0];
   }
+  int getLocalNodeNumber(int node) {
+    int li = -1;
+    if (!tmrg_report(tmrg_forest_get_local_node_number(f, node, &li), "getLocalNodeNumber"))
+      return -1;
+    return li;
+  }
+  // Node locations (zeros unless block boxes were set with
+  // tmrg_forest_set_block_boxes, as the reference without a topology).
+  int getPoints(TMRPoint **X) {
+    int64_t s[6] = {0};
+    tmrg_forest_node_sizes(f, s);
+    points_.resize((size_t)s[0]);
+    if (!points_.empty() &&
+        !tmrg_report(tmrg_forest_get_points(f, &points_[0].x, s[0]), "getPoints"))
+      points_.clear();
+    if (X) *X = points_.data();
+    return (int)points_.size();
+  }
+  void evalInterp(const double pt[], double N[]) {
+    tmrg_report(tmrg_forest_eval_interp(f, pt, N, nullptr, nullptr, nullptr), "evalInterp");
+  }
+  void evalInterp(const double pt[], double N[], double Nxi[], double Neta[],
+                  double Nzeta[]) {
+    tmrg_report(tmrg_forest_eval_interp(f, pt, N, Nxi, Neta, Nzeta), "evalInterp");
+  }
+  void evalInterp(const double pt[], double N[], double N1[], double N2[], double N3[],
+                  double N11[], double N22[], double N33[], double N23[], double N13[],
+                  double N12[]) {
+    tmrg_report(tmrg_forest_eval_interp2(f, pt, N, N1, N2, N3, N11, N22, N33, N23, N13, N12),
+                "evalInterp");
+  }
+  // Returns the enclosing octant inside the borrowed host octants
+  // (getOctants), or nullptr.
+  TMROctant *findEnclosing(const int order, const double *knots, TMROctant *node,
+                           int *mpi_owner = nullptr) {
+    if (mpi_owner) *mpi_owner = 0;
+    int64_t idx = -1;
+    if (!tmrg_report(tmrg_forest_find_enclosing(f, order, knots,
+                                                reinterpret_cast<const tmrg_octant *>(node),
+                                                1, &idx),
+                     "findEnclosing") ||
+        idx < 0)
+      return nullptr;
+    TMROctantArray *a = nullptr;
+    getOctants(&a);
+    return (a && idx < a->n) ? a->ptr + idx : nullptr;
+  }
+  void transformNode(TMROctant *oct, int edge_dir = -1, int *edge_reversed = nullptr,
+                     int *src_face_id = nullptr) {
+    tmrg_report(tmrg_forest_transform_nodes(f, reinterpret_cast<tmrg_octant *>(oct), 1,
+                                            edge_dir, edge_reversed, src_face_id),
+                "transformNode");
+  }
+  // Legacy VTK unstructured grid of the elements' corner points
+  // (writeToVTK, TMROctForest.cpp), from getPoints and getNodeConn.
+  void writeToVTK(const char *filename) {
+    TMRPoint *X = nullptr;
+    int np = getPoints(&X);
+    const int *conn = nullptr;
+    int ne = 0;
+    getNodeConn(&conn, &ne);
+    int64_t s[6] = {0};
+    tmrg_forest_node_sizes(f, s);
+    const int o = getMeshOrder(), nd = (int)s[2];
+    FILE *fp = filename ? fopen(filename, "w") : nullptr;
+    if (!fp || !conn) {
+      if (fp) fclose(fp);
+      fprintf(stderr, "TMROctForest: writeToVTK failed for %s\n", filename ? filename : "(null)");
+      return;
+    }
+    fprintf(fp, "# vtk DataFile Version 3.0\nvtk output\nASCII\nDATASET UNSTRUCTURED_GRID\n");
+    fprintf(fp, "POINTS %d float\n", np);
+    for (int i = 0; i < np; i++) fprintf(fp, "%e %e %e\n", X[i].x, X[i].y, X[i].z);
+    fprintf(fp, "CELLS %d %d\n", ne, 9 * ne);
+    const int c[8] = {0, o - 1, o * o - 1, o * (o - 1), o * o * (o - 1),
+                      o * o * (o - 1) + o - 1, o * o * o - 1, o * o * o - o};
+    for (int e = 0; e < ne; e++) {
+      fprintf(fp, "8");
+      for (int k = 0; k < 8; k++) fprintf(fp, " %d", conn[o * o * o * e + c[k]] + nd);
+      fprintf(fp, "\n");
+    }
+    fprintf(fp, "CELL_TYPES %d\n", ne);
+    for (int e = 0; e < ne; e++) fprintf(fp, "%d\n", 12);
+    fclose(fp);
+  }
   int getExtPreOffset() {
     int64_t s[6] = {0};
     tmrg_forest_node_sizes(f, s);
@@ -245,6 +367,7 @@ class TMROctForest : public TMRGEntity {
   void *stream;
   TMROctantArray octants_;
   std::vector<int> nn_;
+  std::vector<TMRPoint> points_;
   std::vector<double> knots_;
   int range_[2];
 };

@@ -161,4 +161,107 @@ void tmrref_interp_get(void *h, int *rows, int *end_ptr, int *cols,
 }
 void tmrref_interp_destroy(void *h) { delete (TACSBVecInterp *)h; }
 
+// evalInterp (TMROctForest.cpp:1510-1631); N1 == NULL selects the
+// values-only form.
+void tmrref_eval_interp(void *f, const double *pt, double *N, double *N1,
+                        double *N2, double *N3) {
+  if (N1)
+    ((TMROctForest *)f)->evalInterp(pt, N, N1, N2, N3);
+  else
+    ((TMROctForest *)f)->evalInterp(pt, N);
+}
+void tmrref_eval_interp2(void *f, const double *pt, double *N, double *N1,
+                         double *N2, double *N3, double *N11, double *N22,
+                         double *N33, double *N23, double *N13, double *N12) {
+  ((TMROctForest *)f)->evalInterp(pt, N, N1, N2, N3, N11, N22, N33, N23, N13,
+                                  N12);
+}
+// getConnectivity (TMROctForest.cpp:1633-1692): sizes[4] = blocks, faces,
+// edges, nodes; arrays copied out when the buffers are given.
+void tmrref_get_connectivity(void *f, int *sizes, int *block_conn,
+                             int *block_face, int *block_edge, int *face_ids) {
+  int nb, nf, ne, nn;
+  const int *bc, *bf, *be, *fi;
+  ((TMROctForest *)f)->getConnectivity(&nb, &nf, &ne, &nn, &bc, &bf, &be, &fi);
+  sizes[0] = nb;
+  sizes[1] = nf;
+  sizes[2] = ne;
+  sizes[3] = nn;
+  if (block_conn) memcpy(block_conn, bc, sizeof(int) * 8 * nb);
+  if (block_face) memcpy(block_face, bf, sizeof(int) * 6 * nb);
+  if (block_edge) memcpy(block_edge, be, sizeof(int) * 12 * nb);
+  if (face_ids) memcpy(face_ids, fi, sizeof(int) * 6 * nb);
+}
+// getInverseConnectivity (TMROctForest.cpp:1694-1740) copied out; the
+// pointer arrays have nodes+1, edges+1, faces+1 entries.
+void tmrref_get_inverse_connectivity(void *f, int *node_conn, int *node_ptr,
+                                     int *edge_conn, int *edge_ptr,
+                                     int *face_conn, int *face_ptr) {
+  int nb, nf, ne, nn;
+  ((TMROctForest *)f)->getConnectivity(&nb, &nf, &ne, &nn, NULL, NULL, NULL,
+                                       NULL);
+  const int *a, *b, *c, *d, *e, *g;
+  ((TMROctForest *)f)->getInverseConnectivity(&a, &b, &c, &d, &e, &g);
+  memcpy(node_ptr, b, sizeof(int) * (nn + 1));
+  memcpy(node_conn, a, sizeof(int) * b[nn]);
+  memcpy(edge_ptr, d, sizeof(int) * (ne + 1));
+  memcpy(edge_conn, c, sizeof(int) * d[ne]);
+  memcpy(face_ptr, g, sizeof(int) * (nf + 1));
+  memcpy(face_conn, e, sizeof(int) * g[nf]);
+}
+// findEnclosing (TMROctForest.cpp:6228-6377) for nodes given as 7 ints
+// {block, x, y, z, tag, level, info}: index of the returned octant, or -1.
+void tmrref_find_enclosing(void *f, int order, const double *knots, int n,
+                           const int *nodes7, long *out) {
+  TMROctForest *F = (TMROctForest *)f;
+  TMROctantArray *arr;
+  F->getOctants(&arr);
+  TMROctant *base;
+  int size;
+  arr->getArray(&base, &size);
+  for (int i = 0; i < n; i++) {
+    TMROctant q;
+    q.block = nodes7[7 * i];
+    q.x = nodes7[7 * i + 1];
+    q.y = nodes7[7 * i + 2];
+    q.z = nodes7[7 * i + 3];
+    q.tag = nodes7[7 * i + 4];
+    q.level = (int16_t)nodes7[7 * i + 5];
+    q.info = (int16_t)nodes7[7 * i + 6];
+    TMROctant *t = F->findEnclosing(order, knots, &q);
+    out[i] = t ? (long)(t - base) : -1;
+  }
+}
+// transformNode (TMROctForest.cpp:3847-4039) in place on 7-int nodes.
+void tmrref_transform_nodes(void *f, int n, int *nodes7, int edge_dir,
+                            int *rev, int *fid) {
+  TMROctForest *F = (TMROctForest *)f;
+  for (int i = 0; i < n; i++) {
+    TMROctant q;
+    q.block = nodes7[7 * i];
+    q.x = nodes7[7 * i + 1];
+    q.y = nodes7[7 * i + 2];
+    q.z = nodes7[7 * i + 3];
+    q.tag = nodes7[7 * i + 4];
+    q.level = (int16_t)nodes7[7 * i + 5];
+    q.info = (int16_t)nodes7[7 * i + 6];
+    int r = 0, id = 0;
+    F->transformNode(&q, edge_dir, rev ? &r : NULL, fid ? &id : NULL);
+    nodes7[7 * i] = q.block;
+    nodes7[7 * i + 1] = q.x;
+    nodes7[7 * i + 2] = q.y;
+    nodes7[7 * i + 3] = q.z;
+    if (rev) rev[i] = r;
+    if (fid) fid[i] = id;
+  }
+}
+void tmrref_get_knots(void *f, double *out) {
+  const double *k;
+  int n = ((TMROctForest *)f)->getInterpKnots(&k);
+  memcpy(out, k, sizeof(double) * n);
+}
+int tmrref_get_local_node_number(void *f, int node) {
+  return ((TMROctForest *)f)->getLocalNodeNumber(node);
+}
+
 }  // extern "C"

@@ -56,8 +56,42 @@ int main() {
   const int *dp, *dc;
   const double *dw;
   int nd = f->getDepNodeConn(&dp, &dc, &dw);
-  printf("elements %d owned %d dep %d conn_sum %lld P_rows %lld P_nnz %lld P1_sum %.12f\n",
-         ne, nown, nd, csum, (long long)rows, (long long)nnz, s);
+  // the rest of the surface: connectivity getters, local numbers, shape
+  // functions (partition of unity), findEnclosing, transformNode
+  int nb, nf, ned, nn;
+  const int *bc, *bf, *be, *fi;
+  f->getConnectivity(&nb, &nf, &ned, &nn, &bc, &bf, &be, &fi);
+  const int *npt, *nco, *ept, *eco, *fpt, *fco;
+  f->getInverseConnectivity(&nco, &npt, &eco, &ept, &fco, &fpt);
+  const int *nums;
+  int nl = f->getNodeNumbers(&nums);
+  int local_ok = f->getLocalNodeNumber(nums[nl / 2]) == nl / 2;
+  double pt[3] = {0.25, -0.5, 0.75}, N[27], N1[27], N2[27], N3[27];
+  f->evalInterp(pt, N, N1, N2, N3);
+  double pu = 0.0, du = 0.0;
+  for (int i = 0; i < 27; i++) {
+    pu += N[i];
+    du += N1[i];
+  }
+  TMROctantArray *octs;
+  f->getOctants(&octs);
+  TMROctant *a;
+  int na;
+  octs->getArray(&a, &na);
+  TMROctant node = a[na / 2];
+  node.info = 13;  // element centre: enclosed by the element itself
+  const double *kn;
+  f->getInterpKnots(&kn);
+  TMROctant *enc = f->findEnclosing(3, kn, &node);
+  TMROctant corner = a[0];
+  corner.x = corner.y = corner.z = 0;
+  int rev = -1, fid = -1;
+  f->transformNode(&corner, -1, &rev, &fid);
+  printf("elements %d owned %d dep %d conn_sum %lld P_rows %lld P_nnz %lld P1_sum %.12f "
+         "blocks %d faces %d edges %d nodes %d node_refs %d local_ok %d pu %.15f du %.15f "
+         "enclosed_self %d corner_block %d\n",
+         ne, nown, nd, csum, (long long)rows, (long long)nnz, s, nb, nf, ned, nn, npt[nn],
+         local_ok, pu, du, enc == &a[na / 2], corner.block);
   I->decref();
   c->decref();
   f->decref();

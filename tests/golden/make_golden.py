@@ -59,5 +59,111 @@ def main():
         print(name, len(r["oct"]), "octants ->", out, os.path.getsize(out), "bytes")
 
 
+def make_api_golden():
+    """tests/golden/api.npz: evalInterp tables, block connectivity getters,
+    findEnclosing and transformNode results of the reference."""
+    import ctypes
+    from oracle.oracle import RefForest, _lib
+    from tmr_gb300 import workloads as W
+    L = _lib("ref").lib
+    vp = ctypes.c_void_p
+    L.tmrref_forest_create.restype = vp
+    P = lambda a: a.ctypes.data_as(vp)
+    arrs = {}
+    # evalInterp: orders 2-4, uniform / GLL / Bernstein, five points
+    pts = np.array([[0.0, 0.0, 0.0], [0.3, -0.7, 0.9], [-1.0, 1.0, 0.25],
+                    [0.123456789, 0.5, -0.333], [0.99, -0.01, 0.6]])
+    for order in (2, 3, 4):
+        for it in (0, 1, 2):
+            f = L.tmrref_forest_create(order, it)
+            kn = np.zeros(16)
+            L.tmrref_get_knots(vp(f), P(kn))
+            arrs["ev_o%d_t%d_knots" % (order, it)] = kn[:order]
+            n = order ** 3
+            for ip_, pt in enumerate(pts):
+                pt = np.ascontiguousarray(pt)
+                N = np.zeros(n)
+                L.tmrref_eval_interp(vp(f), P(pt), P(N), None, None, None)
+                d1 = [np.zeros(n) for _ in range(4)]
+                L.tmrref_eval_interp(vp(f), P(pt), *[P(a) for a in d1])
+                d2 = [np.zeros(n) for _ in range(10)] + [np.full(n, -7.0)]
+                L.tmrref_eval_interp2(vp(f), P(pt), *[P(a) for a in d2])
+                key = "ev_o%d_t%d_p%d" % (order, it, ip_)
+                arrs[key + "_N"] = N
+                arrs[key + "_d1"] = np.stack(d1)
+                arrs[key + "_d2"] = np.stack(d2)
+            L.tmrref_forest_destroy(vp(f))
+    arrs["ev_points"] = pts
+    # connectivity of randomly rotated blocks
+    conn = W.rotate_blocks(W.brick(3, 2, 2), 2)
+    ref = RefForest(2, 1)
+    ref.setConnectivity(conn)
+    sizes = np.zeros(4, np.int32)
+    L.tmrref_get_connectivity(vp(ref.h), P(sizes), None, None, None, None)
+    nb, nf, ne, nn = (int(v) for v in sizes)
+    bc, bf, be, fi = (np.zeros(nb * w, np.int32) for w in (8, 6, 12, 6))
+    L.tmrref_get_connectivity(vp(ref.h), P(sizes), P(bc), P(bf), P(be), P(fi))
+    ncn, ncp = np.zeros(8 * nb, np.int32), np.zeros(nn + 1, np.int32)
+    ecn, ecp = np.zeros(12 * nb, np.int32), np.zeros(ne + 1, np.int32)
+    fcn, fcp = np.zeros(6 * nb, np.int32), np.zeros(nf + 1, np.int32)
+    L.tmrref_get_inverse_connectivity(vp(ref.h), P(ncn), P(ncp), P(ecn), P(ecp), P(fcn), P(fcp))
+    arrs.update({"cn_block_conn_in": conn, "cn_sizes": sizes, "cn_block_conn": bc,
+                 "cn_block_face": bf, "cn_block_edge": be, "cn_face_ids": fi,
+                 "cn_node_conn": ncn, "cn_node_ptr": ncp, "cn_edge_conn": ecn,
+                 "cn_edge_ptr": ecp, "cn_face_conn": fcn, "cn_face_ptr": fcp})
+    # transformNode on nodes at block corners, edges, faces and interiors
+    rng = np.random.default_rng(3)
+    hmax = 1 << 30
+    m = 3000
+    nodes = np.zeros((m, 7), np.int32)
+    nodes[:, 0] = rng.integers(0, nb, m)
+    for c in (1, 2, 3):
+        pick = rng.integers(0, 3, m)
+        val = rng.integers(0, 1 << 10, m) << 20
+        nodes[:, c] = np.where(pick == 0, 0, np.where(pick == 1, hmax, val))
+    for ed in (-1, 0, 1, 2):
+        out = nodes.copy()
+        rev, fid = np.zeros(m, np.int32), np.zeros(m, np.int32)
+        L.tmrref_transform_nodes(vp(ref.h), m, P(out), ed, P(rev), P(fid))
+        arrs["tn_out_e%d" % (ed + 1)] = out
+        arrs["tn_rev_e%d" % (ed + 1)] = rev
+        arrs["tn_fid_e%d" % (ed + 1)] = fid
+    arrs["tn_nodes"] = nodes
+    # findEnclosing: every local node of a small refined order-3 forest
+    # searched in its coarsened forest
+    case = dict(pipeline.cases()["rot_o3"])
+    case["passes"] = 2
+    fine = RefForest(3, 1)
+    fine.setConnectivity(case["conn"])
+    fine.createTrees(case["L0"])
+    for p in range(case["passes"]):
+        o = fine.getOctants()
+        fine.refine(pipeline.indicator(o, case, p), 0, case["max_level"])
+        fine.balance(1)
+    coarse = fine.coarsen()
+    coarse.balance(1)
+    fo = fine.getOctants()
+    q = np.repeat(fo, 27, axis=0)
+    q[:, 6] = np.tile(np.arange(27), len(fo))
+    idx = np.zeros(len(q), np.int64)
+    L.tmrref_find_enclosing(vp(coarse.h), 3, P(_ref_knots(fine)), len(q),
+                            P(np.ascontiguousarray(q)), P(idx))
+    arrs.update({"fe_conn": case["conn"], "fe_case": np.array(json.dumps(
+        {k: v for k, v in case.items() if k != "conn"}, sort_keys=True)),
+        "fe_nodes": q, "fe_index": idx, "fe_coarse_octants": coarse.getOctants()})
+    out = os.path.join(HERE, "api.npz")
+    np.savez_compressed(out, **arrs)
+    print("api ->", out, os.path.getsize(out), "bytes")
+
+
+def _ref_knots(f):
+    import ctypes
+    from oracle.oracle import _lib
+    k = np.zeros(16)
+    _lib("ref").lib.tmrref_get_knots(ctypes.c_void_p(f.h), k.ctypes.data_as(ctypes.c_void_p))
+    return k
+
+
 if __name__ == "__main__":
     main()
+    make_api_golden()

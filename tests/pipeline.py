@@ -126,6 +126,13 @@ def compare(a, b):
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
+def golden_cases():
+    """Names of the pipeline fixtures in tests/golden (api.npz holds the
+    single-call getters and is read by its own tests)."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN_DIR)
+                  if f.endswith(".npz") and f != "api.npz")
+
+
 def load_golden(name):
     """Products of the reference itself for parity case `name`
     (tests/golden/<name>.npz, written by tests/golden/make_golden.py), in

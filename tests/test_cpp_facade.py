@@ -55,3 +55,12 @@ def test_facade_matches_python_binding(gpu_lib, tmp_path):
     assert int(vals["conn_sum"]) == int(conn.astype(np.int64).sum())
     assert int(vals["P_rows"]) == rows and int(vals["P_nnz"]) == nnz
     assert float(vals["P1_sum"]) == pytest.approx(y.sum(), rel=1e-12)
+    bc, bf, be, fi, nn, ne, nf = f.getConnectivity()
+    assert int(vals["blocks"]) == bc.shape[0] and int(vals["nodes"]) == nn
+    assert int(vals["edges"]) == ne and int(vals["faces"]) == nf
+    assert int(vals["node_refs"]) == 8 * bc.shape[0]
+    assert int(vals["local_ok"]) == 1
+    assert float(vals["pu"]) == pytest.approx(1.0, abs=1e-14)
+    assert float(vals["du"]) == pytest.approx(0.0, abs=1e-13)
+    assert int(vals["enclosed_self"]) == 1
+    assert int(vals["corner_block"]) == 0

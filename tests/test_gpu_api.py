@@ -1,0 +1,191 @@
+"""The rest of TMROctForest's public surface on the GPU library, against
+the reference's own results (tests/golden/api.npz, from the reference build)
+or restatements in this file: getConnectivity / getInverseConnectivity,
+setFullConnectivity, createRandomTrees, findEnclosing, transformNode,
+getLocalNodeNumber, getPoints, evalInterp through a forest."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from tests import pipeline
+from tmr_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _golden():
+    return np.load(os.path.join(HERE, "golden", "api.npz"))
+
+
+def test_connectivity_getters_match_reference(gpu_lib):
+    from tmr_gb300 import TMR
+    z = _golden()
+    f = TMR.OctForest(order=2)
+    f.setConnectivity(z["cn_block_conn_in"])
+    bc, bf, be, fi, nn, ne, nf = f.getConnectivity()
+    nb = bc.shape[0]
+    assert [nb, nf, ne, nn] == list(z["cn_sizes"])
+    np.testing.assert_array_equal(bc.ravel(), z["cn_block_conn"])
+    np.testing.assert_array_equal(bf.ravel(), z["cn_block_face"])
+    np.testing.assert_array_equal(be.ravel(), z["cn_block_edge"])
+    np.testing.assert_array_equal(fi.ravel(), z["cn_face_ids"])
+    inv = f.getInverseConnectivity()
+    np.testing.assert_array_equal(inv["node"][0], z["cn_node_ptr"])
+    np.testing.assert_array_equal(inv["node"][1], z["cn_node_conn"])
+    np.testing.assert_array_equal(inv["edge"][0], z["cn_edge_ptr"])
+    np.testing.assert_array_equal(inv["edge"][1], z["cn_edge_conn"])
+    np.testing.assert_array_equal(inv["face"][0], z["cn_face_ptr"])
+    np.testing.assert_array_equal(inv["face"][1], z["cn_face_conn"])
+
+
+def test_full_connectivity_gives_the_same_forest(gpu_lib):
+    from tmr_gb300 import TMR
+    z = _golden()
+    conn = z["cn_block_conn_in"]
+    nb = conn.shape[0]
+    ref = pipeline.run_gpu(dict(conn=conn, order=3, L0=1, passes=2, max_level=4, prob=0.4,
+                                seed=9, coarse_levels=1))
+    f = TMR.OctForest(order=3)
+    f.setFullConnectivity(conn, z["cn_block_edge"].reshape(nb, 12),
+                          z["cn_block_face"].reshape(nb, 6))
+    bc, bf, be, fi, nn, ne, nf = f.getConnectivity()
+    np.testing.assert_array_equal(fi.ravel(), z["cn_face_ids"])
+    f.createTrees(1)
+    case = dict(conn=conn, order=3, L0=1, passes=2, max_level=4, prob=0.4, seed=9)
+    for p in range(2):
+        o = f.getOctantsArray()
+        f.refine(pipeline.indicator(o, case, p), 0, 4)
+        f.balance(1)
+    f.createNodes()
+    np.testing.assert_array_equal(f.getOctantsArray(), ref["oct"])
+    np.testing.assert_array_equal(f.getMeshConn(), ref["conn"])
+    with pytest.raises(TMR._lib.TMRGError):
+        bad = z["cn_block_edge"].reshape(nb, 12).copy()
+        bad[0, 0] = ne + 5
+        f.setFullConnectivity(conn, bad, z["cn_block_face"].reshape(nb, 6), num_edges=ne)
+
+
+def _morton_key(o):
+    """Sort key of TMROctant::compare: block, then the x-most-significant
+    interleave of the coordinates, then the level."""
+    b, x, y, z, lev = (int(v) for v in o)
+    m = 0
+    for bit in range(29, -1, -1):
+        m = (m << 3) | (((x >> bit) & 1) << 2) | (((y >> bit) & 1) << 1) | ((z >> bit) & 1)
+    return (b, m, lev)
+
+
+def test_random_trees_match_restatement(gpu_lib):
+    from tmr_gb300 import TMR
+    conn = W.brick(2, 2, 1)
+    nrand, lo, hi, seed = 40, 1, 5, 17
+    f = TMR.OctForest(order=2)
+    f.setConnectivity(conn)
+    f.createRandomTrees(nrand, lo, hi, seed)
+    got = f.getOctantsArray()
+    # restatement: U(seed, block, 4i + k) draws, sort, keep the finest per position
+    cand = []
+    for b in range(conn.shape[0]):
+        u = W.uniform(seed, b, 4 * nrand)
+        for i in range(nrand):
+            lev = min(lo + int(u[4 * i] * (hi - lo + 1)), hi)
+            h = 1 << (30 - lev)
+            xyz = [h * min(int(u[4 * i + 1 + k] * (1 << lev)), (1 << lev) - 1) for k in range(3)]
+            cand.append((b, *xyz, lev))
+    cand.sort(key=_morton_key)
+    keep = [c for i, c in enumerate(cand)
+            if i + 1 == len(cand) or _morton_key(cand[i + 1])[:2] != _morton_key(c)[:2]]
+    exp = np.array([[c[0], c[1], c[2], c[3], i, c[4], 0] for i, c in enumerate(keep)], np.intc)
+    np.testing.assert_array_equal(got, exp)
+
+
+def test_transform_nodes_match_reference(gpu_lib):
+    from tmr_gb300 import TMR
+    z = _golden()
+    f = TMR.OctForest(order=2)
+    f.setConnectivity(z["cn_block_conn_in"])
+    nodes = z["tn_nodes"]
+    for ed in (-1, 0, 1, 2):
+        out, rev, fid = f.transformNodes(nodes, edge_dir=ed)
+        exp = z["tn_out_e%d" % (ed + 1)]
+        for j, name in enumerate(("block", "x", "y", "z")):
+            np.testing.assert_array_equal(out[name], exp[:, j])
+        np.testing.assert_array_equal(rev, z["tn_rev_e%d" % (ed + 1)])
+        np.testing.assert_array_equal(fid, z["tn_fid_e%d" % (ed + 1)])
+
+
+def test_find_enclosing_matches_reference(gpu_lib):
+    from tmr_gb300 import TMR
+    z = _golden()
+    case = json.loads(str(z["fe_case"]))
+    case["conn"] = z["fe_conn"]
+    fine = TMR.OctForest(order=3)
+    fine.setConnectivity(case["conn"])
+    fine.createTrees(case["L0"])
+    for p in range(case["passes"]):
+        o = fine.getOctantsArray()
+        fine.refine(pipeline.indicator(o, case, p), 0, case["max_level"])
+        fine.balance(1)
+    coarse = fine.coarsen()
+    coarse.balance(1)
+    np.testing.assert_array_equal(coarse.getOctantsArray(), z["fe_coarse_octants"])
+    idx = coarse.findEnclosing(3, fine.getInterpKnots(), z["fe_nodes"])
+    np.testing.assert_array_equal(idx, z["fe_index"])
+
+
+def test_local_node_numbers_and_points(gpu_lib):
+    from tmr_gb300 import TMR
+    conn = W.brick(2, 1, 1)
+    f = TMR.OctForest(order=3)
+    f.setConnectivity(conn)
+    f.createTrees(1)
+    n = f.getNumOctants()
+    f.refine(W.random_indicator(n, 4, 0, 0.5), 0, 3)
+    f.balance(1)
+    f.createNodes()
+    nn = f.getNodeNumbers()
+    for k in (0, len(nn) // 2, len(nn) - 1):
+        assert f.getLocalNodeNumber(int(nn[k])) == k
+    assert f.getLocalNodeNumber(int(nn[-1]) + 1) == -1
+    # no geometry: every point is 0, as the reference without a topology
+    assert not f.getPoints().any()
+    boxes = np.array([[0.0, 0.0, 0.0, 1.0, 2.0, 0.5], [1.0, 0.0, 0.0, 1.0, 2.0, 0.5]])
+    f.setBlockBoxes(boxes)
+    X = f.getPoints()
+    # restatement: the first (element, local index) using each node places it
+    octs = f.getOctantsArray()
+    mc = f.getMeshConn()
+    kn = f.getInterpKnots()
+    exp = np.full((len(nn), 3), np.nan)
+    num_dep = int(f._sizes()[2])
+    s = 1.0 / (1 << 30)
+    for e in range(len(octs)):
+        b, x, y, zc, _, lev, _ = octs[e]
+        d = (1 << (30 - lev)) * s
+        for l in range(27):
+            li = int(mc[e, l]) + num_dep
+            if not np.isnan(exp[li, 0]):
+                continue
+            ijk = (l % 3, (l // 3) % 3, l // 9)
+            for a, c in enumerate((x, y, zc)):
+                u = c * s + 0.5 * d * (1.0 + kn[ijk[a]])
+                exp[li, a] = boxes[b, a] + boxes[b, 3 + a] * u
+    np.testing.assert_array_equal(X, exp)
+
+
+def test_forest_eval_interp_matches_reference(gpu_lib):
+    from tmr_gb300 import TMR
+    z = _golden()
+    for order in (2, 3):
+        for itype in (0, 1):
+            f = TMR.OctForest(order=order, interp=itype)
+            np.testing.assert_array_equal(f.getInterpKnots(), z["ev_o%d_t%d_knots" % (order, itype)])
+            for ip, pt in enumerate(z["ev_points"]):
+                key = "ev_o%d_t%d_p%d" % (order, itype, ip)
+                np.testing.assert_array_equal(f.evalInterp(pt), z[key + "_N"])
+                np.testing.assert_array_equal(np.stack(f.evalInterp(pt, 1)), z[key + "_d1"])
+                d2 = np.stack(f.evalInterp(pt, 2))
+                np.testing.assert_array_equal(d2[:10], z[key + "_d2"][:10])

@@ -9,7 +9,7 @@ import pytest
 
 from tests import pipeline
 
-CASES = sorted(f[:-4] for f in os.listdir(pipeline.GOLDEN_DIR) if f.endswith(".npz"))
+CASES = pipeline.golden_cases()
 
 
 @pytest.mark.parametrize("name", CASES)

@@ -39,6 +39,21 @@ def _host_view(addr, n, dtype):
     return a
 
 
+def _octant_struct(nodes):
+    """Contiguous OCTANT_DTYPE array from an OctantArray, an (n, 7) int
+    array or a structured octant array."""
+    if isinstance(nodes, OctantArray):
+        nodes = nodes.array
+    a = np.asarray(nodes)
+    if a.dtype.names:
+        return np.ascontiguousarray(a.astype(OCTANT_DTYPE))
+    a = a.reshape(-1, 7)
+    out = np.zeros(a.shape[0], OCTANT_DTYPE)
+    for j, name in enumerate(OCTANT_DTYPE.names):
+        out[name] = a[:, j]
+    return out
+
+
 def _is_torch(a):
     return type(a).__module__.startswith("torch")
 
@@ -171,12 +186,59 @@ class OctForest:
         call("tmrg_forest_set_connectivity", self.ptr, num_nodes, _ptr(conn),
              conn.shape[0])
 
+    def setFullConnectivity(self, conn, edge_conn, face_conn, num_nodes=None,
+                            num_edges=None, num_faces=None):
+        """TMROctForest::setFullConnectivity (TMROctForest.cpp:596-637):
+        corner (n, 8), edge (n, 12) and face (n, 6) numbers of every block."""
+        conn = np.ascontiguousarray(conn, dtype=np.intc)
+        ec = np.ascontiguousarray(edge_conn, dtype=np.intc)
+        fc = np.ascontiguousarray(face_conn, dtype=np.intc)
+        nb = conn.shape[0]
+        if conn.shape != (nb, 8) or ec.shape != (nb, 12) or fc.shape != (nb, 6):
+            raise ValueError("Expected arrays of shape (n, 8), (n, 12), (n, 6)")
+        nn = int(conn.max()) + 1 if num_nodes is None else num_nodes
+        ne = int(ec.max()) + 1 if num_edges is None else num_edges
+        nf = int(fc.max()) + 1 if num_faces is None else num_faces
+        call("tmrg_forest_set_full_connectivity", self.ptr, nn, ne, nf, nb, _ptr(conn),
+             _ptr(ec), _ptr(fc))
+
+    def getConnectivity(self):
+        """(block_conn (n,8), block_face_conn (n,6), block_edge_conn (n,12),
+        block_face_ids (n,6), num_nodes, num_edges, num_faces) of the block
+        connectivity (TMROctForest::getConnectivity); copies."""
+        nb, nf, ne, nn = (ctypes.c_int() for _ in range(4))
+        p = [_vp() for _ in range(4)]
+        call("tmrg_forest_get_connectivity", self.ptr, ctypes.byref(nb), ctypes.byref(nf),
+             ctypes.byref(ne), ctypes.byref(nn), *[ctypes.byref(q) for q in p])
+        n = nb.value
+        arr = [np.array(_host_view(q.value, n * w, np.intc)).reshape(n, w)
+               for q, w in zip(p, (8, 6, 12, 6))]
+        return (*arr, nn.value, ne.value, nf.value)
+
+    def getInverseConnectivity(self):
+        """{node,edge,face}_block (ptr, conn) CSR copies
+        (TMROctForest::getInverseConnectivity)."""
+        _, _, _, _, nn, ne, nf = self.getConnectivity()
+        p = [_vp() for _ in range(6)]
+        call("tmrg_forest_get_inverse_connectivity", self.ptr, *[ctypes.byref(q) for q in p])
+        out = {}
+        for (name, nitems), (pc, pp) in zip((("node", nn), ("edge", ne), ("face", nf)),
+                                            ((p[0], p[1]), (p[2], p[3]), (p[4], p[5]))):
+            ptr = np.array(_host_view(pp.value, nitems + 1, np.intc))
+            out[name] = (ptr, np.array(_host_view(pc.value, int(ptr[-1]), np.intc)))
+        return out
+
     def repartition(self, max_rank=-1):
         call("tmrg_forest_repartition", self.ptr, max_rank)
 
     # -- octants -------------------------------------------------------
     def createTrees(self, depth=0):
         call("tmrg_forest_create_trees", self.ptr, depth)
+
+    def createRandomTrees(self, nrand=10, min_lev=0, max_lev=8, seed=0):
+        """TMROctForest::createRandomTrees (TMROctForest.cpp:1838-1917) with a
+        seeded generator in place of libc rand()."""
+        call("tmrg_forest_create_random_trees", self.ptr, nrand, min_lev, max_lev, seed)
 
     def refine(self, refine=None, min_lev=0, max_lev=MAX_LEVEL):
         if refine is None:
@@ -248,6 +310,69 @@ class OctForest:
         s = np.zeros(6, np.int64)
         call("tmrg_forest_node_sizes", self.ptr, _ptr(s))
         return s
+
+    def getLocalNodeNumber(self, node):
+        """TMROctForest::getLocalNodeNumber (TMROctForest.cpp:1486-1496)."""
+        li = ctypes.c_int()
+        call("tmrg_forest_get_local_node_number", self.ptr, int(node), ctypes.byref(li))
+        return li.value
+
+    def setBlockBoxes(self, boxes):
+        """Axis-aligned box (origin xyz, extent xyz) of every block: the
+        geometry getPoints maps node positions through; None removes it."""
+        if boxes is None:
+            call("tmrg_forest_set_block_boxes", self.ptr, None, 0)
+            return
+        b = np.ascontiguousarray(boxes, dtype=np.float64)
+        if b.ndim != 2 or b.shape[1] != 6:
+            raise ValueError("Expected array of shape (n, 6)")
+        call("tmrg_forest_set_block_boxes", self.ptr, _ptr(b), b.shape[0])
+
+    def getPoints(self):
+        """Node locations (num_local_nodes, 3) (TMROctForest::getPoints):
+        zeros without block boxes, as the reference without a topology."""
+        n = int(self._sizes()[0])
+        X = np.zeros((n, 3), np.float64)
+        if n:
+            call("tmrg_forest_get_points", self.ptr, _ptr(X), n)
+        return X
+
+    def evalInterp(self, pt, derivs=0):
+        """TMROctForest::evalInterp (TMROctForest.cpp:1510-1631): N, or
+        (N, N1, N2, N3) with derivs=1, or the ten arrays of the
+        second-derivative form with derivs=2."""
+        o = self.getMeshOrder()
+        pt = np.ascontiguousarray(pt, dtype=np.float64)
+        arrs = [np.zeros(o ** 3) for _ in range({0: 1, 1: 4, 2: 11}[derivs])]
+        if derivs == 2:
+            call("tmrg_forest_eval_interp2", self.ptr, _ptr(pt), *[_ptr(a) for a in arrs])
+            return tuple(arrs)
+        ptrs = [_ptr(a) for a in arrs] + [None] * (4 - len(arrs))
+        call("tmrg_forest_eval_interp", self.ptr, _ptr(pt), *ptrs)
+        return arrs[0] if derivs == 0 else tuple(arrs)
+
+    def findEnclosing(self, order, knots, nodes):
+        """TMROctForest::findEnclosing for nodes given as an OctantArray,
+        an (n, 7) int array or a structured octant array; returns the index
+        of the enclosing octant of this forest per node (-1: none)."""
+        a = _octant_struct(nodes)
+        k = np.ascontiguousarray(knots, dtype=np.float64)
+        idx = np.zeros(len(a), np.int64)
+        if len(a):
+            call("tmrg_forest_find_enclosing", self.ptr, int(order), _ptr(k), _ptr(a), len(a),
+                 _ptr(idx))
+        return idx
+
+    def transformNodes(self, nodes, edge_dir=-1):
+        """TMROctForest::transformNode on every node (copy): returns the
+        transformed structured octants, edge reversal flags and face ids."""
+        a = _octant_struct(nodes).copy()
+        rev = np.zeros(len(a), np.intc)
+        fid = np.zeros(len(a), np.intc)
+        if len(a):
+            call("tmrg_forest_transform_nodes", self.ptr, _ptr(a), len(a), int(edge_dir),
+                 _ptr(rev), _ptr(fid))
+        return a, rev, fid
 
     def getNodeRange(self):
         return np.array([0, self._sizes()[1]], dtype=np.intc)

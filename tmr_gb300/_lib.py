@@ -51,6 +51,21 @@ _SIGS = {
     "tmrg_forest_node_conn_host": [c_vp, P(c_vp), P(c_i64)],
     "tmrg_forest_dep_node_conn_host": [c_vp, P(c_vp), P(c_vp), P(c_vp), P(c_i64)],
     "tmrg_host_pool_trim": [],
+    "tmrg_forest_set_full_connectivity": [c_vp, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp],
+    "tmrg_forest_get_connectivity": [c_vp, P(c_int), P(c_int), P(c_int), P(c_int),
+                                     P(c_vp), P(c_vp), P(c_vp), P(c_vp)],
+    "tmrg_forest_get_inverse_connectivity": [c_vp, P(c_vp), P(c_vp), P(c_vp), P(c_vp),
+                                             P(c_vp), P(c_vp)],
+    "tmrg_forest_create_random_trees": [c_vp, c_int, c_int, c_int, c_u64],
+    "tmrg_forest_get_local_node_number": [c_vp, c_int, P(c_int)],
+    "tmrg_forest_set_block_boxes": [c_vp, c_vp, c_int],
+    "tmrg_forest_get_points": [c_vp, c_vp, c_i64],
+    "tmrg_eval_interp": [c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp],
+    "tmrg_forest_eval_interp": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp],
+    "tmrg_eval_interp2": [c_int, c_int, c_vp, c_vp] + [c_vp] * 10,
+    "tmrg_forest_eval_interp2": [c_vp, c_vp] + [c_vp] * 10,
+    "tmrg_forest_find_enclosing": [c_vp, c_int, c_vp, c_vp, c_i64, c_vp],
+    "tmrg_forest_transform_nodes": [c_vp, c_vp, c_i64, c_int, c_vp, c_vp],
     "tmrg_interp_create": [c_vp, c_vp, P(c_vp)],
     "tmrg_interp_destroy": [c_vp],
     "tmrg_interp_sizes": [c_vp, c_vp],

@@ -156,6 +156,106 @@ static void copy_d2h(void *dst, const void *src, size_t bytes, cudaStream_t s) {
   TMRG_CUDA(cudaStreamSynchronize(s));
 }
 
+// ---------------------------------------------------------------------
+// 1-D bases of evalInterp (host; TMRInterpolation.h).  Each evaluates in
+// the reference's operation order so the values agree bit for bit.
+namespace {
+// Lagrange values, and first derivatives when Nd is given
+// (lagrange_shape_functions :40-52, lagrange_shape_func_derivative :66-93).
+void basis_lagrange(int o, double u, const double *kn, double *N, double *Nd) {
+  for (int i = 0; i < o; i++) {
+    double v = 1.0, dv = 0.0;
+    for (int j = 0; j < o; j++) {
+      if (j == i) continue;
+      double t = 1.0 / (kn[i] - kn[j]);
+      v *= (u - kn[j]) * t;
+      if (Nd) {
+        for (int m = 0; m < o; m++)
+          if (m != i && m != j) t *= (u - kn[m]) / (kn[i] - kn[m]);
+        dv += t;
+      }
+    }
+    N[i] = v;
+    if (Nd) Nd[i] = dv;
+  }
+}
+// Lagrange values, first and second derivatives
+// (lagrange_shape_func_second_derivative :107-148); note the value product
+// associates as (N (u - k_j)) d_j here.
+void basis_lagrange2(int o, double u, const double *kn, double *N, double *Nd,
+                     double *Ndd) {
+  for (int i = 0; i < o; i++) {
+    double v = 1.0, dv = 0.0, ddv = 0.0;
+    for (int j = 0; j < o; j++) {
+      if (j == i) continue;
+      const double rj = 1.0 / (kn[i] - kn[j]);
+      double a = rj;
+      v = v * (u - kn[j]) * a;
+      for (int k = 0; k < o; k++) {
+        if (k == i || k == j) continue;
+        double b = 1.0 / (kn[i] - kn[k]);
+        a *= (u - kn[k]) * b;
+        b *= rj;
+        for (int m = 0; m < o; m++)
+          if (m != i && m != j && m != k) b *= (u - kn[m]) / (kn[i] - kn[m]);
+        ddv += b;
+      }
+      dv += a;
+    }
+    N[i] = v;
+    Nd[i] = dv;
+    Ndd[i] = ddv;
+  }
+}
+// Bernstein values of degree o-1 by the de Casteljau-style recurrence
+// (bernstein_shape_functions :164-178).
+void basis_bernstein(int o, double u, double *N) {
+  const double a = 0.5 * (1.0 - u), b = 0.5 * (u + 1.0);
+  N[0] = 1.0;
+  for (int j = 1; j < o; j++) {
+    double carry = 0.0;
+    for (int k = 0; k < j; k++) {
+      const double t = N[k];
+      N[k] = carry + a * t;
+      carry = b * t;
+    }
+    N[j] = carry;
+  }
+}
+// Derivative from the degree o-2 basis (bernstein_shape_func_derivative
+// :194-223).
+void basis_bernstein_d1(int o, double u, double *N, double *Nd) {
+  basis_bernstein(o - 1, u, N);
+  const double c = 0.5 * (o - 1);
+  for (int j = 0; j < o; j++) {
+    double v = 0.0;
+    if (j > 0) v += c * N[j - 1];
+    if (j < o - 1) v -= c * N[j];
+    Nd[j] = v;
+  }
+  basis_bernstein(o, u, N);
+}
+// Second derivative from the degree o-3 basis
+// (bernstein_shape_func_second_derivative :240-275).
+void basis_bernstein_d2(int o, double u, double *N, double *Nd, double *Ndd) {
+  basis_bernstein(o - 2, u, N);
+  const double c2 = 0.5 * (o - 2), c1 = 0.5 * (o - 1);
+  for (int j = 0; j < o - 1; j++) {
+    double v = 0.0;
+    if (j > 0) v += c2 * N[j - 1];
+    if (j < o - 2) v -= c2 * N[j];
+    Nd[j] = v;
+  }
+  for (int j = 0; j < o; j++) {
+    double v = 0.0;
+    if (j > 0) v += c1 * Nd[j - 1];
+    if (j < o - 1) v -= c1 * Nd[j];
+    Ndd[j] = v;
+  }
+  basis_bernstein_d1(o, u, N, Nd);
+}
+}  // namespace
+
 extern "C" {
 
 const char *tmrg_last_error(void) { return g_last_error.c_str(); }
@@ -301,6 +401,138 @@ int tmrg_forest_set_connectivity(tmrg_forest *f, int num_nodes,
     f->f.conn = c;
   });
 }
+int tmrg_forest_set_full_connectivity(tmrg_forest *f, int num_nodes, int num_edges,
+                                      int num_faces, int num_blocks, const int *block_conn,
+                                      const int *block_edge_conn,
+                                      const int *block_face_conn) {
+  return guarded([&] {
+    ARG(f && block_conn && block_edge_conn && block_face_conn, "NULL argument");
+    f->gen++;
+    auto c = build_conn(num_nodes, block_conn, num_blocks, f->f.s, num_edges,
+                        block_edge_conn, num_faces, block_face_conn);
+    f->f.free_nodes();
+    f->f.have_octs = false;
+    f->f.n = 0;
+    f->f.conn = c;
+  });
+}
+int tmrg_forest_get_connectivity(tmrg_forest *f, int *nblocks, int *nfaces, int *nedges,
+                                 int *nnodes, const int **block_conn,
+                                 const int **block_face_conn, const int **block_edge_conn,
+                                 const int **block_face_ids) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    const Conn *c = f->f.conn.get();
+    if (nblocks) *nblocks = c ? c->nb : 0;
+    if (nfaces) *nfaces = c ? c->num_faces : 0;
+    if (nedges) *nedges = c ? c->num_edges : 0;
+    if (nnodes) *nnodes = c ? c->num_nodes : 0;
+    if (block_conn) *block_conn = c ? c->block_conn.data() : nullptr;
+    if (block_face_conn) *block_face_conn = c ? c->block_face.data() : nullptr;
+    if (block_edge_conn) *block_edge_conn = c ? c->block_edge.data() : nullptr;
+    if (block_face_ids) *block_face_ids = c ? c->face_ids.data() : nullptr;
+  });
+}
+int tmrg_forest_get_inverse_connectivity(tmrg_forest *f, const int **node_block_conn,
+                                         const int **node_block_ptr,
+                                         const int **edge_block_conn,
+                                         const int **edge_block_ptr,
+                                         const int **face_block_conn,
+                                         const int **face_block_ptr) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    const Conn *c = f->f.conn.get();
+    if (node_block_conn) *node_block_conn = c ? c->node_ent.data() : nullptr;
+    if (node_block_ptr) *node_block_ptr = c ? c->node_ptr.data() : nullptr;
+    if (edge_block_conn) *edge_block_conn = c ? c->edge_ent.data() : nullptr;
+    if (edge_block_ptr) *edge_block_ptr = c ? c->edge_ptr.data() : nullptr;
+    if (face_block_conn) *face_block_conn = c ? c->face_ent.data() : nullptr;
+    if (face_block_ptr) *face_block_ptr = c ? c->face_ptr.data() : nullptr;
+  });
+}
+int tmrg_forest_create_random_trees(tmrg_forest *f, int nrand, int min_level,
+                                    int max_level, uint64_t seed) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    f->gen++;
+    forest_create_random_trees(f->f, nrand, min_level, max_level, seed);
+  });
+}
+int tmrg_forest_get_local_node_number(tmrg_forest *f, int node, int *local) {
+  return guarded([&] {
+    ARG(f && local, "NULL argument");
+    const Forest &F = f->f;
+    if (!F.have_nodes) throw Error(TMRG_ERR_STATE, "getLocalNodeNumber: no nodes");
+    // node numbers are -num_dep .. -1, 0 .. num_owned-1, sorted
+    long long li = (long long)node + F.num_dep;
+    *local = (li >= 0 && li < F.num_local) ? (int)li : -1;
+  });
+}
+int tmrg_forest_find_enclosing(tmrg_forest *f, int order, const double *knots,
+                               const tmrg_octant *nodes, int64_t n, int64_t *index) {
+  return guarded([&] {
+    ARG(f && knots && (n == 0 || (nodes && index)), "NULL argument");
+    ARG(n >= 0, "findEnclosing: n < 0");
+    if (!n) return;
+    Forest &F = f->f;
+    DBuf<tmrg_octant> d(n, F.s);
+    DBuf<long long> r(n, F.s);
+    TMRG_CUDA(cudaMemcpyAsync(d.p, nodes, sizeof(tmrg_octant) * n, cudaMemcpyHostToDevice, F.s));
+    forest_find_enclosing(F, order, knots, d.p, n, r.p);
+    static_assert(sizeof(long long) == sizeof(int64_t), "int64");
+    copy_d2h(index, r.p, sizeof(int64_t) * n, F.s);
+  });
+}
+int tmrg_forest_transform_nodes(tmrg_forest *f, tmrg_octant *octs, int64_t n, int edge_dir,
+                                int *edge_reversed, int *src_face_id) {
+  return guarded([&] {
+    ARG(f && (n == 0 || octs), "NULL argument");
+    ARG(n >= 0 && edge_dir >= -1 && edge_dir <= 2, "transformNode: bad argument");
+    if (!n) return;
+    Forest &F = f->f;
+    DBuf<tmrg_octant> d(n, F.s);
+    DBuf<int> r(edge_reversed ? n : 0, F.s), id(src_face_id ? n : 0, F.s);
+    TMRG_CUDA(cudaMemcpyAsync(d.p, octs, sizeof(tmrg_octant) * n, cudaMemcpyHostToDevice, F.s));
+    forest_transform_nodes(F, d.p, n, edge_dir, edge_reversed ? r.p : nullptr,
+                           src_face_id ? id.p : nullptr);
+    if (edge_reversed)
+      TMRG_CUDA(cudaMemcpyAsync(edge_reversed, r.p, sizeof(int) * n, cudaMemcpyDeviceToHost, F.s));
+    if (src_face_id)
+      TMRG_CUDA(cudaMemcpyAsync(src_face_id, id.p, sizeof(int) * n, cudaMemcpyDeviceToHost, F.s));
+    copy_d2h(octs, d.p, sizeof(tmrg_octant) * n, F.s);
+  });
+}
+int tmrg_forest_set_block_boxes(tmrg_forest *f, const double *boxes, int num_blocks) {
+  return guarded([&] {
+    ARG(f, "NULL forest");
+    Conn *c = f->f.conn.get();
+    if (!c) throw Error(TMRG_ERR_STATE, "setBlockBoxes: no connectivity");
+    if (!boxes) {
+      c->boxes.clear();
+      c->d_boxes.release();
+      return;
+    }
+    ARG(num_blocks == c->nb, "setBlockBoxes: one box per block");
+    c->boxes.assign(boxes, boxes + 6LL * num_blocks);
+    c->d_boxes.alloc(6LL * num_blocks, f->f.s);
+    TMRG_CUDA(cudaMemcpyAsync(c->d_boxes.p, c->boxes.data(), sizeof(double) * 6 * num_blocks,
+                              cudaMemcpyHostToDevice, f->f.s));
+    TMRG_CUDA(cudaStreamSynchronize(f->f.s));
+  });
+}
+int tmrg_forest_get_points(tmrg_forest *f, double *X, int64_t n) {
+  return guarded([&] {
+    ARG(f && X, "NULL argument");
+    Forest &F = f->f;
+    if (!F.have_nodes) throw Error(TMRG_ERR_STATE, "getPoints: no nodes");
+    ARG(n == F.num_local, "getPoints: buffer length != number of local nodes");
+    DBuf<double> d(3 * (size_t)n + 1, F.s);
+    forest_get_points(F, F.conn->boxes.empty() ? nullptr : (const double *)F.conn->d_boxes.p,
+                      d.p);
+    copy_d2h(X, d.p, sizeof(double) * 3 * (size_t)n, F.s);
+  });
+}
+
 int tmrg_forest_set_mesh_order(tmrg_forest *f, int order, int interp_type) {
   return guarded([&] {
     ARG(f, "NULL forest");
@@ -545,6 +777,95 @@ int tmrg_forest_dep_node_conn_host(tmrg_forest *f, const int **ptr, const int **
     if (num_dep) *num_dep = f->f.num_dep;
   });
 }
+// evalInterp (TMROctForest.cpp:1510-1631): tensor-product shape functions
+// at a parametric point, ii fastest, with optional first derivatives.
+int tmrg_eval_interp(int order, int interp_type, const double *knots, const double *pt,
+                     double *N, double *N1, double *N2, double *N3) {
+  return guarded([&] {
+    ARG(pt && N && order >= 2 && order <= TMRG_MAX_ORDER, "bad argument");
+    ARG(interp_type == TMRG_BERNSTEIN_POINTS || knots, "knots are NULL");
+    const bool d1 = N1 && N2 && N3;
+    double B[3][TMRG_MAX_ORDER], D[3][TMRG_MAX_ORDER];
+    for (int a = 0; a < 3; a++) {
+      if (interp_type == TMRG_BERNSTEIN_POINTS) {
+        if (d1)
+          basis_bernstein_d1(order, pt[a], B[a], D[a]);
+        else
+          basis_bernstein(order, pt[a], B[a]);
+      } else {
+        basis_lagrange(order, pt[a], knots, B[a], d1 ? D[a] : nullptr);
+      }
+    }
+    int p = 0;
+    for (int k = 0; k < order; k++)
+      for (int j = 0; j < order; j++)
+        for (int i = 0; i < order; i++, p++) {
+          N[p] = B[0][i] * B[1][j] * B[2][k];
+          if (d1) {
+            N1[p] = D[0][i] * B[1][j] * B[2][k];
+            N2[p] = B[0][i] * D[1][j] * B[2][k];
+            N3[p] = B[0][i] * B[1][j] * D[2][k];
+          }
+        }
+  });
+}
+// The second-derivative form (TMROctForest.cpp:1572-1631).  As in the
+// reference, N33 receives the mixed (1,2) derivative after the (3,3) one
+// and N12 is not written (TMROctForest.cpp:1614-1615).
+int tmrg_eval_interp2(int order, int interp_type, const double *knots, const double *pt,
+                      double *N, double *N1, double *N2, double *N3, double *N11,
+                      double *N22, double *N33, double *N23, double *N13, double *N12) {
+  return guarded([&] {
+    ARG(pt && N && N1 && N2 && N3 && N11 && N22 && N33 && N23 && N13 && order >= 2 &&
+            order <= TMRG_MAX_ORDER,
+        "bad argument");
+    ARG(interp_type == TMRG_BERNSTEIN_POINTS || knots, "knots are NULL");
+    (void)N12;
+    double B[3][TMRG_MAX_ORDER], D[3][TMRG_MAX_ORDER], DD[3][TMRG_MAX_ORDER];
+    for (int a = 0; a < 3; a++) {
+      if (interp_type == TMRG_BERNSTEIN_POINTS)
+        basis_bernstein_d2(order, pt[a], B[a], D[a], DD[a]);
+      else
+        basis_lagrange2(order, pt[a], knots, B[a], D[a], DD[a]);
+    }
+    int p = 0;
+    for (int k = 0; k < order; k++)
+      for (int j = 0; j < order; j++)
+        for (int i = 0; i < order; i++, p++) {
+          const double u = B[0][i], v = B[1][j], w = B[2][k];
+          const double du = D[0][i], dv = D[1][j], dw = D[2][k];
+          N[p] = u * v * w;
+          N1[p] = du * v * w;
+          N2[p] = u * dv * w;
+          N3[p] = u * v * dw;
+          N11[p] = DD[0][i] * v * w;
+          N22[p] = u * DD[1][j] * w;
+          N33[p] = u * v * DD[2][k];
+          N23[p] = u * dv * dw;
+          N13[p] = du * v * dw;
+          N33[p] = du * dv * w;
+        }
+  });
+}
+int tmrg_forest_eval_interp(tmrg_forest *f, const double *pt, double *N, double *N1,
+                            double *N2, double *N3) {
+  if (!f) {
+    g_last_error = "NULL forest";
+    return TMRG_ERR_ARG;
+  }
+  return tmrg_eval_interp(f->f.order, f->f.interp, f->f.knots, pt, N, N1, N2, N3);
+}
+int tmrg_forest_eval_interp2(tmrg_forest *f, const double *pt, double *N, double *N1,
+                             double *N2, double *N3, double *N11, double *N22, double *N33,
+                             double *N23, double *N13, double *N12) {
+  if (!f) {
+    g_last_error = "NULL forest";
+    return TMRG_ERR_ARG;
+  }
+  return tmrg_eval_interp2(f->f.order, f->f.interp, f->f.knots, pt, N, N1, N2, N3, N11, N22,
+                           N33, N23, N13, N12);
+}
+
 int tmrg_host_pool_trim(void) {
   return guarded([&] {
     std::lock_guard<std::mutex> g(g_pin_mu);

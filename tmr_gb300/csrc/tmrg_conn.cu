@@ -29,7 +29,8 @@ static void make_csr(int nitems, const std::vector<int> &item_of,
 }
 
 std::shared_ptr<Conn> build_conn(int num_nodes, const int *bc, int nb,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, int num_edges, const int *be,
+                                 int num_faces, const int *bf) {
   if (nb <= 0 || num_nodes <= 0 || !bc)
     throw Error(TMRG_ERR_ARG, "setConnectivity: empty connectivity");
   for (long long i = 0; i < 8LL * nb; i++)
@@ -44,10 +45,18 @@ std::shared_ptr<Conn> build_conn(int num_nodes, const int *bc, int nb,
   // Corner -> blocks.
   make_csr(num_nodes, c->block_conn, c->node_ptr, c->node_ent);
 
-  // Edges: keyed by their unordered node pair, numbered by first use.
+  // Edges: keyed by their unordered node pair, numbered by first use
+  // (computeEdgesFromNodes, TMROctForest.cpp:791-862), or as given
+  // (setFullConnectivity, :596-637).
   std::map<std::pair<int, int>, int> edges;
   c->block_edge.assign(12LL * nb, 0);
-  for (int b = 0; b < nb; b++)
+  if (be) {
+    for (long long i = 0; i < 12LL * nb; i++)
+      if (be[i] < 0 || be[i] >= num_edges)
+        throw Error(TMRG_ERR_ARG, "setFullConnectivity: edge index out of range");
+    c->block_edge.assign(be, be + 12LL * nb);
+  }
+  for (int b = 0; b < nb && !be; b++)
     for (int e = 0; e < 12; e++) {
       int a1, a2;
       edge_corners(e, a1, a2);
@@ -63,14 +72,20 @@ std::shared_ptr<Conn> build_conn(int num_nodes, const int *bc, int nb,
       }
       c->block_edge[12 * b + e] = id;
     }
-  c->num_edges = (int)edges.size();
+  c->num_edges = be ? num_edges : (int)edges.size();
   make_csr(c->num_edges, c->block_edge, c->edge_ptr, c->edge_ent);
 
   // Faces: keyed by their sorted node 4-tuple; orientation is checked
   // against the owner's corner order below.
   std::map<std::tuple<int, int, int, int>, int> faces;
   c->block_face.assign(6LL * nb, 0);
-  for (int b = 0; b < nb; b++)
+  if (bf) {
+    for (long long i = 0; i < 6LL * nb; i++)
+      if (bf[i] < 0 || bf[i] >= num_faces)
+        throw Error(TMRG_ERR_ARG, "setFullConnectivity: face index out of range");
+    c->block_face.assign(bf, bf + 6LL * nb);
+  }
+  for (int b = 0; b < nb && !bf; b++)
     for (int f = 0; f < 6; f++) {
       int q[4];
       for (int k = 0; k < 4; k++) q[k] = bc[8 * b + face_corner(f, k)];
@@ -86,7 +101,7 @@ std::shared_ptr<Conn> build_conn(int num_nodes, const int *bc, int nb,
       }
       c->block_face[6 * b + f] = id;
     }
-  c->num_faces = (int)faces.size();
+  c->num_faces = bf ? num_faces : (int)faces.size();
   make_csr(c->num_faces, c->block_face, c->face_ptr, c->face_ent);
 
   // Orientation of each block face relative to the face owner: the first

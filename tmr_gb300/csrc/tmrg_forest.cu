@@ -641,20 +641,110 @@ void forest_balance(Forest &f, int corner) {
 }
 
 // ---------------------------------------------------------------------
-__global__ void k_random_refinement(uint64_t seed, uint64_t stream, double prob,
-                                    int *out, long long n) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+// Seeded uniform U(seed, stream, i) in [0, 1): splitmix64 of the seed and
+// stream, mixed with the index (same function as oo_uniform and
+// workloads.uniform).
+__device__ __forceinline__ double seeded_uniform(uint64_t seed, uint64_t stream, uint64_t i) {
   auto sm = [](uint64_t x) {
     x += 0x9E3779B97F4A7C15ULL;
     x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
     x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
     return x ^ (x >> 31);
   };
-  uint64_t r = sm(sm(seed * 0x100000001B3ULL + stream) ^
-                  ((uint64_t)i * 0xD6E8FEB86659FD93ULL));
-  double u = (double)(r >> 11) * (1.0 / 9007199254740992.0);
-  out[i] = (u < prob) ? 1 : 0;
+  uint64_t r = sm(sm(seed * 0x100000001B3ULL + stream) ^ (i * 0xD6E8FEB86659FD93ULL));
+  return (double)(r >> 11) * (1.0 / 9007199254740992.0);
+}
+
+__global__ void k_random_refinement(uint64_t seed, uint64_t stream, double prob,
+                                    int *out, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = (seeded_uniform(seed, stream, (uint64_t)i) < prob) ? 1 : 0;
+}
+
+// ---------------------------------------------------------------------
+// createRandomTrees (TMROctForest.cpp:1838-1917): nrand octants per block
+// at a random level in [min_level, max_level] and a random anchor of that
+// level, sorted, and made unique on position keeping the finest (the
+// reference's TMROctantArray::sort).  The reference draws from libc rand();
+// here octant i of block b draws U(seed, b, 4i + k), k = 0..3.
+__global__ void k_random_octs(long long total, int nrand, int min_level, int max_level,
+                              uint64_t seed, OctKey K, uint64_t *keys) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const unsigned tu = (unsigned)t;  // total < 2^32
+  const int b = (int)(tu / (unsigned)nrand), i = (int)(tu - (unsigned)b * (unsigned)nrand);
+  const uint64_t base = 4ULL * (uint64_t)i;
+  int level = min_level + (int)(seeded_uniform(seed, b, base) * (max_level - min_level + 1));
+  if (level > max_level) level = max_level;
+  const int32_t h = side_of(level);
+  const double cells = (double)(1 << level);
+  int32_t c[3];
+  for (int k = 0; k < 3; k++) {
+    int32_t q = (int32_t)(seeded_uniform(seed, b, base + 1 + k) * cells);
+    if (q >= (1 << level)) q = (1 << level) - 1;
+    c[k] = h * q;
+  }
+  keys[t] = K.make(b, c[0], c[1], c[2], level);
+}
+
+void forest_create_random_trees(Forest &f, int nrand, int min_level, int max_level,
+                                uint64_t seed) {
+  Stage st("tmrg_create_random_trees");
+  if (!f.conn) throw Error(TMRG_ERR_STATE, "createRandomTrees: no connectivity");
+  if (nrand < 0) throw Error(TMRG_ERR_ARG, "createRandomTrees: nrand < 0");
+  if (min_level < 0) min_level = 0;
+  if (max_level >= TMRG_MAX_LEVEL) max_level = TMRG_MAX_LEVEL - 1;
+  if (min_level > max_level) min_level = max_level;
+  f.free_nodes();
+  cudaStream_t s = f.s;
+  const long long total = (long long)f.conn->nb * nrand;
+  if (total >= (1LL << 32)) throw Error(TMRG_ERR_ARG, "createRandomTrees: too many octants");
+  f.maxlev = max_level;
+  OctKey K = f.oct_key();
+  DBuf<uint64_t> keys(total, s);
+  launch(k_random_octs, blocks_for(total, 256), 256, 0, s, total, nrand, min_level,
+         max_level, seed, K, keys.p);
+  radix_sort(keys, nullptr, total, K.total_bits(), s);
+  DBuf<unsigned> pos(total + 1, s);
+  launch(k_dedupe_flags, blocks_for(total, 256), 256, 0, s, total, (const uint64_t *)keys.p,
+         pos.p);
+  exclusive_scan<unsigned>(pos.p, pos.p, total, s);
+  const unsigned m = total ? read_scalar(pos.p + total, s) : 0u;
+  alloc_octs(f, m);
+  launch(k_compact_octs, blocks_for(total, 256), 256, 0, s, total, K,
+         (const uint64_t *)keys.p, (const uint32_t *)nullptr, (const unsigned *)pos.p,
+         (const int16_t *)nullptr, f.block.p, f.x.p, f.y.p, f.z.p, f.level.p, f.info.p);
+  f.have_octs = true;
+  TMRG_CUDA(cudaStreamSynchronize(s));
+}
+
+// ---------------------------------------------------------------------
+// transformNode (TMROctForest.cpp:3847-4039) on a batch of nodes in place:
+// block, x, y, z of each node become those of its owner frame; edge_dir
+// as in the reference; optional per-node edge reversal and face id.
+__global__ void k_transform_nodes(long long n, ConnDev c, tmrg_octant *o, int edge_dir,
+                                  int *rev, int *fid) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  tmrg_octant q = o[i];
+  int32_t b = q.block, x = q.x, y = q.y, z = q.z;
+  int r = 0, id = 0;
+  transform_node(c, b, x, y, z, edge_dir, rev ? &r : nullptr, fid ? &id : nullptr);
+  q.block = b;
+  q.x = x;
+  q.y = y;
+  q.z = z;
+  o[i] = q;
+  if (rev) rev[i] = r;
+  if (fid) fid[i] = id;
+}
+
+void forest_transform_nodes(Forest &f, tmrg_octant *d_octs, long long n, int edge_dir,
+                            int *d_rev, int *d_fid) {
+  if (!f.conn) throw Error(TMRG_ERR_STATE, "transformNode: no connectivity");
+  launch(k_transform_nodes, blocks_for(n, 256), 256, 0, f.s, n, f.conn->dev, d_octs,
+         edge_dir, d_rev, d_fid);
 }
 
 void random_refinement(uint64_t seed, uint64_t stream, double prob, int *out,

@@ -37,9 +37,15 @@ struct Conn {
   DBuf<int> d_all;
   ConnDev dev{};
   int block_bits = 1;
+  // optional axis-aligned box of every block (origin xyz, extent xyz): the
+  // geometry getPoints maps nodes through; empty = no geometry
+  std::vector<double> boxes;
+  DBuf<double> d_boxes;
 };
 std::shared_ptr<Conn> build_conn(int num_nodes, const int *block_conn,
-                                 int num_blocks, cudaStream_t s);
+                                 int num_blocks, cudaStream_t s, int num_edges = 0,
+                                 const int *block_edge = nullptr, int num_faces = 0,
+                                 const int *block_face = nullptr);
 
 struct Forest {
   cudaStream_t s = 0;
@@ -128,5 +134,12 @@ void filter_apply_static(Filter &F, bool transpose, int vpn, const double *in,
                          double *out);
 void random_refinement(uint64_t seed, uint64_t stream, double prob, int *out,
                        long long n, cudaStream_t s);
+void forest_create_random_trees(Forest &f, int nrand, int min_level, int max_level,
+                                uint64_t seed);
+void forest_transform_nodes(Forest &f, tmrg_octant *d_octs, long long n, int edge_dir,
+                            int *d_rev, int *d_fid);
+void forest_find_enclosing(Forest &f, int order, const double *knots,
+                           const tmrg_octant *d_nodes, long long n, long long *d_index);
+void forest_get_points(Forest &f, const double *boxes, double *d_X);
 
 }  // namespace tmrg

@@ -680,6 +680,40 @@ __global__ void k_rowsum(long long rows, const int *__restrict__ rowptr,
   sum[r] = s;
 }
 
+// findEnclosing (TMROctForest.cpp:6228-6377) for a batch of nodes: each
+// node is an element octant with `info` = its local node index in an
+// element of `order` with `knots`; the result is the index of the octant of
+// this forest the reference returns, or -1 where it returns NULL.
+__global__ void k_find_enclosing_batch(long long n, InterpCtx I, const tmrg_octant *nodes,
+                                       long long *out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const tmrg_octant q = nodes[i];
+  const Oct node{q.block, q.x, q.y, q.z, q.level};
+  out[i] = find_enclosing(I, node, q.info);
+}
+
+void forest_find_enclosing(Forest &f, int order, const double *knots,
+                           const tmrg_octant *d_nodes, long long n, long long *d_index) {
+  if (!f.have_octs) throw Error(TMRG_ERR_STATE, "findEnclosing: no octants");
+  if (order < 2 || order > TMRG_MAX_ORDER)
+    throw Error(TMRG_ERR_ARG, "findEnclosing: order out of range");
+  if (f.conn->nb >= (1 << 26))
+    throw Error(TMRG_ERR_KEY_RANGE, "findEnclosing: more than 2^26 blocks");
+  cudaStream_t s = f.s;
+  InterpCtx c{};
+  c.fo = order;
+  for (int k = 0; k < TMRG_MAX_ORDER; k++) c.fk1[k] = k < order ? 1.0 + knots[k] : 0.0;
+  c.cn = f.n;
+  DBuf<int4> c4(f.n + 1, s);
+  launch(k_pack_octs, blocks_for(f.n, 256), 256, 0, s, f.n, (const int *)f.block.p,
+         (const int *)f.x.p, (const int *)f.y.p, (const int *)f.z.p,
+         (const int16_t *)f.level.p, c4.p);
+  c.c4 = c4.p;
+  launch(k_find_enclosing_batch, blocks_for(n, 256), 256, 0, s, n, c, d_nodes, d_index);
+  TMRG_CUDA(cudaStreamSynchronize(s));
+}
+
 void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   Stage st("tmrg_create_interpolation");
   if (&fine == &coarse)

@@ -606,6 +606,70 @@ __global__ void k_remap(long long m, const int *__restrict__ num, int *a) {
   if (i < m) a[i] = num[a[i]];
 }
 
+// ---------------------------------------------------------------------
+// getPoints (TMROctForest.cpp:1476-1482, evaluateNodeLocations :5524-5680):
+// each local node takes the position of its first (element, local index)
+// in element order.  Without a geometry the reference leaves every point
+// at 0; here a block may carry an axis-aligned box (origin, extent), the
+// stand-in for TMRVolume::evalPoint on a box volume:
+// X = origin + extent * (u + 0.5 d (1 + knot)), u = x / 2^30, d = h / 2^30.
+__global__ void k_points_first_ref(long long n, int npe, long long num_dep,
+                                   long long nlocal, const int *__restrict__ conn,
+                                   unsigned long long *rep) {
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int *c = conn + e * npe;
+  for (int l = 0; l < npe; l++) {
+    long long li = (long long)__ldg(c + l) + num_dep;
+    if (li >= 0 && li < nlocal)
+      atomicMin(rep + li, ((unsigned long long)e << 8) | (unsigned)l);
+  }
+}
+__global__ void k_points_eval(long long nlocal, int order, Knots kn,
+                              const unsigned long long *__restrict__ rep,
+                              const int *__restrict__ blk, const int *__restrict__ xs,
+                              const int *__restrict__ ys, const int *__restrict__ zs,
+                              const int16_t *__restrict__ lev,
+                              const double *__restrict__ boxes, double *X) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nlocal) return;
+  const unsigned long long r = rep[i];
+  double p[3] = {0.0, 0.0, 0.0};
+  if (r != ~0ULL && boxes) {
+    const long long e = (long long)(r >> 8);
+    const int l = (int)(r & 255u);
+    const int ijk[3] = {l % order, (l / order) % order, l / (order * order)};
+    const int32_t c[3] = {xs[e], ys[e], zs[e]};
+    const double scale = 1.0 / (double)(1 << TMRG_MAX_LEVEL);
+    const double d = (double)side_of(lev[e]) * scale;
+    const double *bx = boxes + 6 * (long long)blk[e];
+    for (int k = 0; k < 3; k++) {
+      const double u = (double)c[k] * scale + 0.5 * d * (1.0 + kn.k[ijk[k]]);
+      p[k] = bx[k] + bx[3 + k] * u;
+    }
+  }
+  X[3 * i] = p[0];
+  X[3 * i + 1] = p[1];
+  X[3 * i + 2] = p[2];
+}
+
+void forest_get_points(Forest &f, const double *d_boxes, double *d_X) {
+  if (!f.have_nodes) throw Error(TMRG_ERR_STATE, "getPoints: no nodes");
+  cudaStream_t s = f.s;
+  const int o = f.order, npe = o * o * o;
+  const long long nlocal = f.num_local;
+  DBuf<unsigned long long> rep(nlocal + 1, s);
+  rep.fill_bytes(0xff);
+  launch(k_points_first_ref, blocks_for(f.n, 256), 256, 0, s, f.n, npe, f.num_dep, nlocal,
+         (const int *)f.econn.p, rep.p);
+  Knots kn{};
+  for (int i = 0; i < TMRG_MAX_ORDER; i++) kn.k[i] = i < o ? f.knots[i] : 0.0;
+  launch(k_points_eval, blocks_for(nlocal, 256), 256, 0, s, nlocal, o, kn,
+         (const unsigned long long *)rep.p, (const int *)f.block.p, (const int *)f.x.p,
+         (const int *)f.y.p, (const int *)f.z.p, (const int16_t *)f.level.p, d_boxes, d_X);
+  TMRG_CUDA(cudaStreamSynchronize(s));
+}
+
 void forest_create_nodes(Forest &f) {
   Stage st("tmrg_create_nodes");
   if (!f.have_octs)
