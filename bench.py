@@ -60,6 +60,9 @@ def parse():
                    help="smaller variant of the workload for ncu captures")
     p.add_argument("--passes", type=int, default=None,
                    help="fewer refinement passes: a smaller case for ncu captures")
+    p.add_argument("--workload", default="c2", choices=["c2", "c5"],
+                   help="c2: the multi-tree order-3 workload (default, the headline); "
+                        "c5: the 200M-octant adaptive workload (one JSON line of its own)")
     a = p.parse_args()
     if a.passes is not None:
         WORKLOAD["passes"] = a.passes
@@ -576,6 +579,190 @@ def build_filter_chain(TMR, FW):
     return f, coarse, I, F, r
 
 
+# ---------------------------------------------------------------------------
+# The large adaptive configuration: 16x16x8 brick (2048 trees) refined near
+# 32 Gaussian bumps and coarsened away from them to ~200M octants, order 2,
+# a 5-level hierarchy with P / P^T, and the matrix filter chained with P.
+C5_WORKLOAD = dict(name="brick16x16x8_32bumps_refine+coarsen_200M_order2_5lvl_vpn3",
+                   nx=16, ny=16, nz=8, L0=2, bumps=32, seed=5, sigma=0.05,
+                   target=200_000_000, min_level=2, max_level=10, max_passes=10,
+                   t_coarsen=1e-3, order=2, levels=5, vpn=3, N=10)
+
+
+def _c5_setup(TMR, CW):
+    import torch
+
+    from tmr_gb300 import workloads as Wk
+    nx, ny, nz = CW["nx"], CW["ny"], CW["nz"]
+    conn = Wk.brick(nx, ny, nz)
+    nb = conn.shape[0]
+    boxes = np.zeros((nb, 6))
+    b = np.arange(nb)
+    boxes[:, 0], boxes[:, 1], boxes[:, 2] = b % nx, (b // nx) % ny, b // (nx * ny)
+    boxes[:, 3:] = 1.0
+    L = np.array([nx, ny, nz], np.float64)
+    cen = torch.tensor(Wk.uniform(CW["seed"], 0, 3 * CW["bumps"]).reshape(-1, 3) * L,
+                       device="cuda")
+    return conn, boxes, cen, CW["sigma"] * L
+
+
+def _c5_forest(TMR, CW, conn, boxes):
+    f = TMR.OctForest(order=CW["order"], interp=TMR.GAUSS_LOBATTO_POINTS)
+    f.setConnectivity(conn)
+    f.setBlockBoxes(boxes)
+    f.createTrees(CW["L0"])
+    return f
+
+
+def c5_thresholds(TMR, CW):
+    """Untimed plan: per pass, the bump-sum threshold above which refining
+    takes the forest toward the target (refine ~ (target - n) / 9 octants;
+    balance adds about a third), from the kernel's own indicator values."""
+    import torch
+    conn, boxes, cen, sig = _c5_setup(TMR, CW)
+    f = _c5_forest(TMR, CW, conn, boxes)
+    thr = []
+    for _ in range(CW["max_passes"]):
+        n = f.getNumOctants()
+        if n >= 0.9 * CW["target"]:
+            break
+        # indicator values: the kernel flags at decreasing thresholds would
+        # need many launches; recompute the sums here once per pass
+        o = f.getOctantsDevice()
+        bl = o["block"].long()
+        org = torch.tensor(boxes[:, :3], device="cuda")[bl]
+        lev = o["level"].long()
+        h = torch.pow(2.0, (30 - lev).double())
+        xyz = torch.stack([o["x"], o["y"], o["z"]], 1).double()
+        c = org + (xyz + 0.5 * h[:, None]) / 2.0 ** 30
+        val = torch.zeros(n, dtype=torch.float64, device="cuda")
+        for k in range(cen.shape[0]):
+            val += torch.exp(-0.5 * (((c - cen[k]) / torch.tensor(sig, device="cuda")) ** 2).sum(1))
+        val[lev >= CW["max_level"]] = -1.0
+        k = int(min(n, max(1, (CW["target"] - n) / 9)))
+        t = float(torch.topk(val, k).values[-1])
+        thr.append(t)
+        del o, bl, org, lev, h, xyz, c, val
+        flags = TMR.bump_indicator(f, cen, sig, t, CW["t_coarsen"], CW["min_level"],
+                                   CW["max_level"])
+        f.refine(flags, CW["min_level"], CW["max_level"])
+        f.balance(1)
+    return thr
+
+
+def c5_step(TMR, CW, thr, setup):
+    """Adaptation + numbering + hierarchy + interpolation of one step."""
+    conn, boxes, cen, sig = setup
+    f = _c5_forest(TMR, CW, conn, boxes)
+    for t in thr:
+        flags = TMR.bump_indicator(f, cen, sig, t, CW["t_coarsen"], CW["min_level"],
+                                   CW["max_level"])
+        f.refine(flags, CW["min_level"], CW["max_level"])
+        f.balance(1)
+    f.createNodes()
+    forests = [f]
+    for _ in range(CW["levels"] - 1):
+        c = forests[-1].coarsen()
+        c.balance(1)
+        c.createNodes()
+        forests.append(c)
+    interps = []
+    for k in range(CW["levels"] - 1):
+        I = TMR.VecInterp()
+        forests[k].createInterpolation(forests[k + 1], I)
+        interps.append(I)
+    return forests, interps
+
+
+def run_c5(args):
+    """One JSON line for the large adaptive configuration."""
+    import torch
+    from tmr_gb300 import TMR
+    from tmr_gb300 import build as tb
+    tb.build()
+    CW = C5_WORKLOAD
+    thr = c5_thresholds(TMR, CW)
+    setup = _c5_setup(TMR, CW)
+    for _ in range(args.warmup):
+        fo, it = c5_step(TMR, CW, thr, setup)
+        del fo, it
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    units = 0
+    for _ in range(args.steps):
+        forests, interps = c5_step(TMR, CW, thr, setup)
+        units += sum(fr.getNumOctants() for fr in forests)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    levels = [{"octants": fr.getNumOctants()} for fr in forests]
+    for k, I in enumerate(interps):
+        r, c, z = I.sizes()
+        levels[k].update({"P_rows": r, "P_cols": c, "P_nnz": z})
+    # P^T down / P up on vpn vectors, then filter -> P forward + adjoint on level 1
+    vpn = CW["vpn"]
+    g = torch.Generator(device="cuda").manual_seed(CW["seed"])
+    nf = interps[0].sizes()[0]
+    x0 = torch.rand(nf * vpn, dtype=torch.float64, device="cuda", generator=g)
+
+    def hierarchy_applies():
+        x = x0
+        for I in interps:
+            y = torch.empty(I.sizes()[1] * vpn, dtype=torch.float64, device="cuda")
+            I.multTranspose(x, y)
+            x = y
+        for I in reversed(interps):
+            y = torch.empty(I.sizes()[0] * vpn, dtype=torch.float64, device="cuda")
+            I.mult(x, y)
+            x = y
+        return x
+    hierarchy_applies()
+    torch.cuda.synchronize()
+    e0.record()
+    hierarchy_applies()
+    e1.record()
+    torch.cuda.synchronize()
+    apply_ms = e0.elapsed_time(e1)
+    hmin = 1.0 / 2.0 ** int(forests[1].getOctantsDevice()["level"].max().item())
+    F = TMR.MatrixFilter(2.0 * hmin, CW["N"], None, [forests[1]], block_len=1.0, vpn=vpn)
+    n, nnz_m = F.size()
+    x = torch.rand(n * vpn, dtype=torch.float64, device="cuda", generator=g)
+    w = torch.rand(nf * vpn, dtype=torch.float64, device="cuda", generator=g)
+    rho, gp, gx = torch.empty_like(x), torch.empty_like(x), torch.empty_like(x)
+    y = torch.empty(nf * vpn, dtype=torch.float64, device="cuda")
+
+    def chain():
+        F.applyFilter(x, rho, vpn)
+        interps[0].mult(rho, y)
+        interps[0].multTranspose(3.0 * w * y * y, gp)
+        F.applyTranspose(gp, gx, vpn)
+    chain()
+    torch.cuda.synchronize()
+    e0.record()
+    chain()
+    e1.record()
+    torch.cuda.synchronize()
+    chain_ms = e0.elapsed_time(e1)
+    x32 = x.float()
+    r32 = torch.empty_like(x32)
+    F.applyFilter(x32, r32, vpn)
+    err32 = float((r32.double() - rho).abs().max() / rho.abs().max())
+    line = {"metric": "balanced+numbered octants/s", "value": units / (ms * args.steps / 1e3),
+            "unit": "octants/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "dtype": "int32+f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": CW["name"], "refine_thresholds": thr,
+                       "octants_per_step": units // args.steps, "hierarchy": levels},
+            "hierarchy_applies_ms": apply_ms, "filter_chain_ms": chain_ms,
+            "filter_nodes": n, "M_nnz": nnz_m, "fp32_filter_rel_err": err32,
+            # the library's stream-ordered pool keeps what it used: in use now
+            # is about the peak of the run
+            "device_mem_in_use_gb": (lambda fr_to: (fr_to[1] - fr_to[0]) / 1e9)(
+                torch.cuda.mem_get_info())}
+    print(json.dumps(line), flush=True)
+
+
 def filter_chain_metrics(TMR, steps=5):
     """Forward + adjoint of filter -> P on 3 design components: time per
     chain, algorithmic GB/s of the filter and P applies (library profile),
@@ -689,6 +876,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c5":
+        run_c5(args)
     else:
         run_gpu(args)
 

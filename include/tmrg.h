@@ -305,6 +305,17 @@ int tmrg_filter_apply_static_device(tmrg_filter *F, int transpose, int vpn,
    uniform shared with the CPU oracle.  Device pointer. */
 int tmrg_random_refinement_device(uint64_t seed, uint64_t stream, double prob,
                                   int *d_out, int64_t n, void *cuda_stream);
+/* Refinement array of the large adaptive workload (no reference
+   counterpart): per octant the sum of Gaussian bumps
+   exp(-|(p - c_k) / sigma|^2 / 2) at its centre p (physical, through the
+   block boxes of tmrg_forest_set_block_boxes); +1 where the sum exceeds
+   t_refine and the level is below max_level, -1 where it is under
+   t_coarsen and the level is above min_level, else 0.  d_centres: device,
+   3 doubles per bump; d_out: device, one int per octant. */
+int tmrg_bump_indicator_device(tmrg_forest *f, const double *d_centres,
+                               int num_bumps, const double *sigma,
+                               double t_refine, double t_coarsen,
+                               int min_level, int max_level, int *d_out);
 /* Number of kernels this library has launched in this process. */
 int64_t tmrg_kernel_launch_count(void);
 /* Per-kernel timing for benchmarks (no counterpart in the reference, which

@@ -22,7 +22,7 @@ from oracle import build as ob  # noqa: E402
 from tests import pipeline  # noqa: E402
 
 CASES = ["c1_small", "brick_o2", "brick_o3", "rot_o2", "rot_o3", "rot_o4", "nocorner",
-         "uniform_o3"]
+         "uniform_o3", "mixed_o2"]
 
 
 def case_meta(case):

@@ -15,6 +15,9 @@ RTOL = 1e-13  # FP64 tolerance for weights and applies (relative)
 def indicator(octs, case, p):
     if case.get("indicator", "random") == "sphere":
         return W.sphere_indicator(octs)
+    if case.get("indicator") == "mixed":
+        return W.mixed_indicator(len(octs), case.get("seed", 0), p, case.get("prob", 0.3),
+                                 case.get("coarsen_prob", 0.3))
     return W.random_indicator(len(octs), case.get("seed", 0), p, case.get("prob", 0.3))
 
 
@@ -181,4 +184,8 @@ def cases():
                          max_level=5, prob=0.3, seed=6, corner=0),
         "uniform_o3": dict(conn=W.brick(2, 1, 1), order=3, L0=2, passes=1, max_level=3,
                            prob=1.0, seed=1, interp=0),
+        # refinement arrays with -1 entries: coarsening inside refine
+        "mixed_o2": dict(conn=W.rotate_blocks(W.brick(3, 2, 2), 8), order=2, L0=2, passes=3,
+                         max_level=4, indicator="mixed", prob=0.35, coarsen_prob=0.3, seed=12,
+                         coarse_levels=2),
     }

@@ -635,3 +635,19 @@ def random_refinement(n, seed, stream, prob, device="cuda"):
     call("tmrg_random_refinement_device", int(seed), int(stream), float(prob),
          _vp(out.data_ptr()), n, _vp(cs))
     return out
+
+
+def bump_indicator(forest, centres, sigma, t_refine, t_coarsen, min_level, max_level):
+    """Refine (+1) / coarsen (-1) / keep (0) flags of `forest`'s octants
+    from a sum of Gaussian bumps at CUDA `centres` (K x 3, float64) with
+    widths `sigma` (3), through the forest's block boxes.  Returns a CUDA
+    int32 tensor; ordered on the forest's stream."""
+    import torch
+    n = forest.getNumOctants()
+    out = torch.empty(max(n, 1), dtype=torch.int32, device="cuda")
+    c = centres.contiguous()
+    sg = np.ascontiguousarray(sigma, dtype=np.float64)
+    call("tmrg_bump_indicator_device", forest.ptr, _vp(c.data_ptr()), int(c.shape[0]),
+         _ptr(sg), float(t_refine), float(t_coarsen), int(min_level), int(max_level),
+         _vp(out.data_ptr()))
+    return out[:n]

@@ -1127,6 +1127,16 @@ int tmrg_filter_apply_static_device(tmrg_filter *F, int transpose, int vpn,
   });
 }
 
+int tmrg_bump_indicator_device(tmrg_forest *f, const double *d_centres, int num_bumps,
+                               const double *sigma, double t_refine, double t_coarsen,
+                               int min_level, int max_level, int *d_out) {
+  return guarded([&] {
+    ARG(f && sigma && (d_out || f->f.n == 0) && (d_centres || num_bumps == 0),
+        "NULL argument");
+    bump_indicator(f->f, d_centres, num_bumps, sigma, t_refine, t_coarsen, min_level,
+                   max_level, d_out);
+  });
+}
 int tmrg_random_refinement_device(uint64_t seed, uint64_t stream, double prob,
                                   int *d_out, int64_t n, void *cuda_stream) {
   return guarded([&] {

@@ -747,6 +747,46 @@ void forest_transform_nodes(Forest &f, tmrg_octant *d_octs, long long n, int edg
          edge_dir, d_rev, d_fid);
 }
 
+// Refinement indicator of the large adaptive workload: the sum of K
+// Gaussian bumps at the octant centre (physical position through the
+// per-block boxes) gives +1 above t_refine (below max_level), -1 below
+// t_coarsen (above min_level), 0 otherwise.
+__global__ void k_bump_indicator(long long n, const int *__restrict__ blk,
+                                 const int *__restrict__ xs, const int *__restrict__ ys,
+                                 const int *__restrict__ zs, const int16_t *__restrict__ lev,
+                                 const double *__restrict__ boxes,
+                                 const double *__restrict__ centres, int K, double sx,
+                                 double sy, double sz, double t_refine, double t_coarsen,
+                                 int min_level, int max_level, int *out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double *bx = boxes + 6 * (long long)blk[i];
+  const int l = lev[i];
+  const double half = 0.5 * (double)side_of(l);
+  const double sc = 1.0 / (double)(1 << TMRG_MAX_LEVEL);
+  const double px = bx[0] + bx[3] * (((double)xs[i] + half) * sc);
+  const double py = bx[1] + bx[4] * (((double)ys[i] + half) * sc);
+  const double pz = bx[2] + bx[5] * (((double)zs[i] + half) * sc);
+  double v = 0.0;
+  for (int k = 0; k < K; k++) {
+    const double dx = (px - centres[3 * k]) / sx, dy = (py - centres[3 * k + 1]) / sy,
+                 dz = (pz - centres[3 * k + 2]) / sz;
+    v += exp(-0.5 * (dx * dx + dy * dy + dz * dz));
+  }
+  out[i] = (v > t_refine && l < max_level) ? 1 : ((v < t_coarsen && l > min_level) ? -1 : 0);
+}
+
+void bump_indicator(Forest &f, const double *d_centres, int K, const double sigma[3],
+                    double t_refine, double t_coarsen, int min_level, int max_level,
+                    int *d_out) {
+  if (!f.have_octs) throw Error(TMRG_ERR_STATE, "bump indicator: no octants");
+  if (f.conn->boxes.empty()) throw Error(TMRG_ERR_STATE, "bump indicator: no block boxes");
+  launch(k_bump_indicator, blocks_for(f.n, 256), 256, 0, f.s, f.n, (const int *)f.block.p,
+         (const int *)f.x.p, (const int *)f.y.p, (const int *)f.z.p,
+         (const int16_t *)f.level.p, (const double *)f.conn->d_boxes.p, d_centres, K,
+         sigma[0], sigma[1], sigma[2], t_refine, t_coarsen, min_level, max_level, d_out);
+}
+
 void random_refinement(uint64_t seed, uint64_t stream, double prob, int *out,
                        long long n, cudaStream_t s) {
   launch(k_random_refinement, blocks_for(n, 256), 256, 0, s, seed, stream, prob,

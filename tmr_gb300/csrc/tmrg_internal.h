@@ -136,6 +136,9 @@ void random_refinement(uint64_t seed, uint64_t stream, double prob, int *out,
                        long long n, cudaStream_t s);
 void forest_create_random_trees(Forest &f, int nrand, int min_level, int max_level,
                                 uint64_t seed);
+void bump_indicator(Forest &f, const double *d_centres, int K, const double sigma[3],
+                    double t_refine, double t_coarsen, int min_level, int max_level,
+                    int *d_out);
 void forest_transform_nodes(Forest &f, tmrg_octant *d_octs, long long n, int edge_dir,
                             int *d_rev, int *d_fid);
 void forest_find_enclosing(Forest &f, int order, const double *knots,

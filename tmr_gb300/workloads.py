@@ -94,6 +94,16 @@ def random_indicator(n, seed, stream, prob):
     return (uniform(seed, stream, n) < prob).astype(np.intc)
 
 
+def mixed_indicator(n, seed, stream, prob, coarsen_prob):
+    """+1 (refine) where U < prob, -1 (coarsen) where U >= 1 - coarsen_prob,
+    0 elsewhere."""
+    u = uniform(seed, stream, n)
+    out = np.zeros(n, np.intc)
+    out[u < prob] = 1
+    out[u >= 1.0 - coarsen_prob] = -1
+    return out
+
+
 # ---- the benchmark configurations ----------------------------------------
 # C1: one tree, uniform level 4, 3 sphere passes to level 7, order 2.
 C1 = dict(conn=lambda: brick(1, 1, 1), L0=4, passes=3, max_level=7, order=2,
