@@ -60,8 +60,9 @@ def parse():
                    help="smaller variant of the workload for ncu captures")
     p.add_argument("--passes", type=int, default=None,
                    help="fewer refinement passes: a smaller case for ncu captures")
-    p.add_argument("--workload", default="c2", choices=["c2", "c5"],
+    p.add_argument("--workload", default="c2", choices=["c2", "c4", "c5"],
                    help="c2: the multi-tree order-3 workload (default, the headline); "
+                        "c4: 256 forests batched as one; "
                         "c5: the 200M-octant adaptive workload (one JSON line of its own)")
     a = p.parse_args()
     if a.passes is not None:
@@ -763,6 +764,115 @@ def run_c5(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# The batched configuration: 256 independent forests of 1, 8 or 27 trees,
+# target sizes log-uniform in [1k, 2M] octants, refinement probability
+# U(0.1, 0.5) per forest, max level 10, order 2, 3-level hierarchy.  The
+# batch runs as one forest over the disjoint union of the forests' blocks
+# (tmr_gb300.batch); the comparison is the plain loop over the forests.
+C4_WORKLOAD = dict(name="256forests_1-8-27trees_1k-2M_p0.1-0.5_lvl10_order2_3lvl",
+                   forests=256, seed=11, min_size=1e3, max_size=2e6, max_level=10,
+                   order=2, levels=3, L0=1, max_passes=12)
+
+
+def c4_specs(CW):
+    from tmr_gb300 import workloads as Wk
+    u = Wk.uniform(CW["seed"], 0, 3 * CW["forests"]).reshape(-1, 3)
+    shapes = 1 + (u[:, 0] * 3).astype(int).clip(0, 2)
+    lo, hi = np.log(CW["min_size"]), np.log(CW["max_size"])
+    targets = np.exp(lo + (hi - lo) * u[:, 1]).astype(np.int64)
+    probs = 0.1 + 0.4 * u[:, 2]
+    conns = [Wk.brick(int(s), int(s), int(s)) for s in shapes]
+    return conns, targets, probs
+
+
+def _c4_hierarchy(TMR, f, CW):
+    f.createNodes()
+    forests = [f]
+    for _ in range(CW["levels"] - 1):
+        c = forests[-1].coarsen()
+        c.balance(1)
+        c.createNodes()
+        forests.append(c)
+    interps = []
+    for k in range(CW["levels"] - 1):
+        I = TMR.VecInterp()
+        forests[k].createInterpolation(forests[k + 1], I)
+        interps.append(I)
+    return forests, interps
+
+
+def c4_loop(TMR, CW, conns, targets, probs):
+    units = 0
+    for k, conn in enumerate(conns):
+        f = TMR.OctForest(order=CW["order"], interp=TMR.GAUSS_LOBATTO_POINTS)
+        f.setConnectivity(conn)
+        f.createTrees(CW["L0"])
+        for p in range(CW["max_passes"]):
+            n = f.getNumOctants()
+            if n >= targets[k]:
+                break
+            f.refine(TMR.random_refinement(n, CW["seed"], k * 1024 + p, probs[k]), 0,
+                     CW["max_level"])
+            f.balance(1)
+        forests, interps = _c4_hierarchy(TMR, f, CW)
+        units += sum(fr.getNumOctants() for fr in forests)
+    return units
+
+
+def c4_batched(TMR, CW, conns, targets, probs):
+    from tmr_gb300.batch import ForestBatch
+    B = ForestBatch(conns, order=CW["order"])
+    f = B.forest
+    f.createTrees(CW["L0"])
+    for p in range(CW["max_passes"]):
+        active = np.diff(B.octant_starts()) < targets
+        if not active.any():
+            break
+        f.refine(B.random_refinement(CW["seed"], p, probs, active), 0, CW["max_level"])
+        f.balance(1)
+    forests, interps = _c4_hierarchy(TMR, f, CW)
+    return sum(fr.getNumOctants() for fr in forests), B, forests
+
+
+def run_c4(args):
+    """One JSON line for the batched configuration (batched and looped)."""
+    import torch
+    from tmr_gb300 import TMR
+    from tmr_gb300 import build as tb
+    tb.build()
+    CW = C4_WORKLOAD
+    conns, targets, probs = c4_specs(CW)
+    for _ in range(args.warmup):
+        c4_batched(TMR, CW, conns, targets, probs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        units, B, forests = c4_batched(TMR, CW, conns, targets, probs)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    sizes = np.diff(B.octant_starts())
+    c4_loop(TMR, CW, conns, targets, probs)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loop_units = c4_loop(TMR, CW, conns, targets, probs)
+    torch.cuda.synchronize()
+    loop_ms = (time.perf_counter() - t0) * 1e3
+    line = {"metric": "balanced+numbered octants/s", "value": units / (ms / 1e3),
+            "unit": "octants/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "dtype": "int32+f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": CW["name"], "forests": len(conns),
+                       "trees": int(sum(c.shape[0] for c in conns)),
+                       "octants_per_step": units,
+                       "finest_sizes": {"min": int(sizes.min()), "median": int(np.median(sizes)),
+                                        "max": int(sizes.max())}},
+            "loop_over_forests": {"ms": loop_ms, "value": loop_units / (loop_ms / 1e3),
+                                  "octants": loop_units},
+            "same_octants": bool(loop_units == units)}
+    print(json.dumps(line), flush=True)
+
+
 def filter_chain_metrics(TMR, steps=5):
     """Forward + adjoint of filter -> P on 3 design components: time per
     chain, algorithmic GB/s of the filter and P applies (library profile),
@@ -878,6 +988,8 @@ def main():
         run_reference(args)
     elif args.workload == "c5":
         run_c5(args)
+    elif args.workload == "c4":
+        run_c4(args)
     else:
         run_gpu(args)
 

@@ -305,6 +305,19 @@ int tmrg_filter_apply_static_device(tmrg_filter *F, int transpose, int vpn,
    uniform shared with the CPU oracle.  Device pointer. */
 int tmrg_random_refinement_device(uint64_t seed, uint64_t stream, double prob,
                                   int *d_out, int64_t n, void *cuda_stream);
+/* Refinement array of a batch of independent forests held as one forest
+   over the disjoint union of their blocks (no reference counterpart):
+   forest k owns blocks [d_first_block[k], d_first_block[k+1]) (num_forests
+   + 1 entries), d_block_forest maps a block to its forest; d_start
+   (num_forests + 1, device) receives each forest's first octant; octant j
+   of forest k gets U(seed, k * 1024 + pass, j) < d_prob[k] when
+   d_active[k] is nonzero, else 0 -- the draws that forest alone gets from
+   tmrg_random_refinement_device(seed, k * 1024 + pass, prob). */
+int tmrg_batch_refinement_device(tmrg_forest *f, int num_forests,
+                                 const int *d_first_block,
+                                 const int *d_block_forest, const double *d_prob,
+                                 const int *d_active, uint64_t seed,
+                                 uint64_t pass, int64_t *d_start, int *d_out);
 /* Refinement array of the large adaptive workload (no reference
    counterpart): per octant the sum of Gaussian bumps
    exp(-|(p - c_k) / sigma|^2 / 2) at its centre p (physical, through the

@@ -67,6 +67,8 @@ _SIGS = {
     "tmrg_forest_find_enclosing": [c_vp, c_int, c_vp, c_vp, c_i64, c_vp],
     "tmrg_forest_transform_nodes": [c_vp, c_vp, c_i64, c_int, c_vp, c_vp],
     "tmrg_bump_indicator_device": [c_vp, c_vp, c_int, c_vp, c_dbl, c_dbl, c_int, c_int, c_vp],
+    "tmrg_batch_refinement_device": [c_vp, c_int, c_vp, c_vp, c_vp, c_vp, c_u64, c_u64, c_vp,
+                                     c_vp],
     "tmrg_interp_create": [c_vp, c_vp, P(c_vp)],
     "tmrg_interp_destroy": [c_vp],
     "tmrg_interp_sizes": [c_vp, c_vp],

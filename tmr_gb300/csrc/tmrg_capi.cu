@@ -1127,6 +1127,19 @@ int tmrg_filter_apply_static_device(tmrg_filter *F, int transpose, int vpn,
   });
 }
 
+int tmrg_batch_refinement_device(tmrg_forest *f, int num_forests, const int *d_first_block,
+                                 const int *d_block_forest, const double *d_prob,
+                                 const int *d_active, uint64_t seed, uint64_t pass,
+                                 int64_t *d_start, int *d_out) {
+  return guarded([&] {
+    ARG(f && num_forests > 0 && d_first_block && d_block_forest && d_prob && d_active &&
+            d_start && (d_out || f->f.n == 0),
+        "NULL argument");
+    static_assert(sizeof(long long) == sizeof(int64_t), "int64");
+    batch_refinement(f->f, num_forests, d_first_block, d_block_forest, d_prob, d_active, seed,
+                     pass, (long long *)d_start, d_out);
+  });
+}
 int tmrg_bump_indicator_device(tmrg_forest *f, const double *d_centres, int num_bumps,
                                const double *sigma, double t_refine, double t_coarsen,
                                int min_level, int max_level, int *d_out) {

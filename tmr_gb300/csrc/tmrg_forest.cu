@@ -787,6 +787,50 @@ void bump_indicator(Forest &f, const double *d_centres, int K, const double sigm
          sigma[0], sigma[1], sigma[2], t_refine, t_coarsen, min_level, max_level, d_out);
 }
 
+// Batched forests (several independent forests as one forest over the
+// disjoint union of their blocks): the first octant of each forest, and a
+// per-forest seeded refinement array in which octant j of forest k draws
+// U(seed, k * 1024 + pass, j) < prob[k] (zero for inactive forests), the
+// same draws the forest alone gets from random_refinement.
+__global__ void k_forest_starts(int nforests, const int *__restrict__ first_block,
+                                long long n, const int *__restrict__ blk,
+                                long long *start) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k > nforests) return;
+  const int b = first_block[k];
+  long long lo = 0, hi = n;
+  while (lo < hi) {
+    long long mid = (lo + hi) >> 1;
+    if (blk[mid] < b)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  start[k] = lo;
+}
+__global__ void k_batch_refinement(long long n, const int *__restrict__ blk,
+                                   const int *__restrict__ block_forest,
+                                   const long long *__restrict__ start,
+                                   const double *__restrict__ prob,
+                                   const int *__restrict__ active, uint64_t seed,
+                                   uint64_t pass, int *out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int k = block_forest[blk[i]];
+  const uint64_t j = (uint64_t)(i - start[k]);
+  out[i] = (active[k] && seeded_uniform(seed, (uint64_t)k * 1024 + pass, j) < prob[k]) ? 1 : 0;
+}
+
+void batch_refinement(Forest &f, int nforests, const int *d_first_block,
+                      const int *d_block_forest, const double *d_prob, const int *d_active,
+                      uint64_t seed, uint64_t pass, long long *d_start, int *d_out) {
+  if (!f.have_octs) throw Error(TMRG_ERR_STATE, "batch refinement: no octants");
+  launch(k_forest_starts, blocks_for(nforests + 1, 128), 128, 0, f.s, nforests, d_first_block,
+         f.n, (const int *)f.block.p, d_start);
+  launch(k_batch_refinement, blocks_for(f.n, 256), 256, 0, f.s, f.n, (const int *)f.block.p,
+         d_block_forest, (const long long *)d_start, d_prob, d_active, seed, pass, d_out);
+}
+
 void random_refinement(uint64_t seed, uint64_t stream, double prob, int *out,
                        long long n, cudaStream_t s) {
   launch(k_random_refinement, blocks_for(n, 256), 256, 0, s, seed, stream, prob,

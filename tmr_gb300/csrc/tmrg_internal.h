@@ -136,6 +136,9 @@ void random_refinement(uint64_t seed, uint64_t stream, double prob, int *out,
                        long long n, cudaStream_t s);
 void forest_create_random_trees(Forest &f, int nrand, int min_level, int max_level,
                                 uint64_t seed);
+void batch_refinement(Forest &f, int nforests, const int *d_first_block,
+                      const int *d_block_forest, const double *d_prob, const int *d_active,
+                      uint64_t seed, uint64_t pass, long long *d_start, int *d_out);
 void bump_indicator(Forest &f, const double *d_centres, int K, const double sigma[3],
                     double t_refine, double t_coarsen, int min_level, int max_level,
                     int *d_out);
