@@ -230,6 +230,17 @@ int tmrg_forest_transform_nodes(tmrg_forest *f, tmrg_octant *octs, int64_t n,
 int tmrg_interp_create(tmrg_forest *fine, tmrg_forest *coarse,
                        tmrg_interp **out);
 int tmrg_interp_destroy(tmrg_interp *I);
+/* Design -> analysis weights (TMROctTACSTopoCreator::computeWeights,
+   TMR_TACSTopoCreator.cpp:55-122, per element as createElements calls it,
+   :163-183): one row per analysis-forest element, one column per owned
+   filter node; the row holds the filter's shape functions at the element
+   centre (located with findEnclosing), expanded through the filter's
+   dependent nodes and merged by column.  The result is an interpolation
+   object: tmrg_interp_mult maps filter design values to element values.
+   The reference copies a fixed filter_order^3 slots per element; rows here
+   hold every merged entry. */
+int tmrg_topo_weights_create(tmrg_forest *filter, tmrg_forest *analysis,
+                             tmrg_interp **out);
 /* out: {rows, cols, nnz} */
 int tmrg_interp_sizes(tmrg_interp *I, int64_t out3[3]);
 /* Row-sorted CSR of P, host copies. */

@@ -10,6 +10,8 @@
 */
 #include <stdio.h>
 
+#include <vector>
+
 #include "TMROctForest.h"
 
 // The reference's TMROctForest.cpp reaches these only with a topology
@@ -259,6 +261,70 @@ void tmrref_get_knots(void *f, double *out) {
   const double *k;
   int n = ((TMROctForest *)f)->getInterpKnots(&k);
   memcpy(out, k, sizeof(double) * n);
+}
+// TMROctTACSTopoCreator::computeWeights (TMR_TACSTopoCreator.cpp:55-122) as
+// createElements calls it per element (:163-183), written out over the
+// reference's own forest methods (the creator itself needs TACS): rows of
+// merged (index, weight) pairs per analysis element.  With cols == NULL
+// only the number of entries is returned.
+long tmrref_topo_weights(void *filt, void *ana, int *rowptr, int *cols,
+                         double *w) {
+  TMROctForest *filter = (TMROctForest *)filt, *forest = (TMROctForest *)ana;
+  TMROctantArray *arr;
+  forest->getOctants(&arr);
+  TMROctant *octs;
+  int n;
+  arr->getArray(&octs, &n);
+  const int order = filter->getMeshOrder(), np = order * order * order;
+  const int *dep_ptr, *dep_conn;
+  const double *dep_w;
+  filter->getDepNodeConn(&dep_ptr, &dep_conn, &dep_w);
+  const int *conn;
+  filter->getNodeConn(&conn);
+  const double node_knots[] = {-1.0, 0.0, 1.0};
+  std::vector<TMRIndexWeight> wt(np * order * order + 8);
+  std::vector<double> N(np);
+  long nnz = 0;
+  if (rowptr) rowptr[0] = 0;
+  for (int i = 0; i < n; i++) {
+    TMROctant node = octs[i];
+    node.info = 13;
+    TMROctant *oct = filter->findEnclosing(3, node_knots, &node);
+    if (oct) {
+      const int32_t h = 1 << (TMR_MAX_LEVEL - node.level);
+      const int32_t hoct = 1 << (TMR_MAX_LEVEL - oct->level);
+      double pt[3];
+      pt[0] = -1.0 + 2.0 * ((node.x % hoct) + 0.5 * h * (1.0 + node_knots[1])) / hoct;
+      pt[1] = -1.0 + 2.0 * ((node.y % hoct) + 0.5 * h * (1.0 + node_knots[1])) / hoct;
+      pt[2] = -1.0 + 2.0 * ((node.z % hoct) + 0.5 * h * (1.0 + node_knots[1])) / hoct;
+      filter->evalInterp(pt, N.data());
+      const int *c = &conn[np * oct->tag];
+      int m = 0;
+      for (int off = 0; off < np; off++) {
+        if (c[off] >= 0) {
+          wt[m].index = c[off];
+          wt[m].weight = N[off];
+          m++;
+        } else {
+          int d = -c[off] - 1;
+          for (int jp = dep_ptr[d]; jp < dep_ptr[d + 1]; jp++) {
+            wt[m].index = dep_conn[jp];
+            wt[m].weight = N[off] * dep_w[jp];
+            m++;
+          }
+        }
+      }
+      m = TMRIndexWeight::uniqueSort(wt.data(), m);
+      if (cols)
+        for (int k = 0; k < m; k++) {
+          cols[nnz + k] = wt[k].index;
+          w[nnz + k] = wt[k].weight;
+        }
+      nnz += m;
+    }
+    if (rowptr) rowptr[i + 1] = (int)nnz;
+  }
+  return nnz;
 }
 int tmrref_get_local_node_number(void *f, int node) {
   return ((TMROctForest *)f)->getLocalNodeNumber(node);

@@ -151,6 +151,31 @@ def make_api_golden():
     arrs.update({"fe_conn": case["conn"], "fe_case": np.array(json.dumps(
         {k: v for k, v in case.items() if k != "conn"}, sort_keys=True)),
         "fe_nodes": q, "fe_index": idx, "fe_coarse_octants": coarse.getOctants()})
+    # design -> analysis weights: analysis forest = a refined forest, filter
+    # forest = its coarsened forest (orders 2 and 3)
+    L.tmrref_topo_weights.restype = ctypes.c_long
+    for name in ("brick_o2", "rot_o3"):
+        case = dict(pipeline.cases()[name])
+        case["passes"] = 2
+        ana = RefForest(case["order"], 1)
+        ana.setConnectivity(case["conn"])
+        ana.createTrees(case["L0"])
+        for p in range(case["passes"]):
+            o = ana.getOctants()
+            ana.refine(pipeline.indicator(o, case, p), 0, case["max_level"])
+            ana.balance(1)
+        filt = ana.coarsen()
+        filt.balance(1)
+        filt.createNodes()
+        n = len(ana.getOctants())
+        rp = np.zeros(n + 1, np.int32)
+        nnz = L.tmrref_topo_weights(vp(filt.h), vp(ana.h), P(rp), None, None)
+        cols, w = np.zeros(max(nnz, 1), np.int32), np.zeros(max(nnz, 1))
+        L.tmrref_topo_weights(vp(filt.h), vp(ana.h), P(rp), P(cols), P(w))
+        arrs.update({"tw_%s_case" % name: np.array(json.dumps(
+            {k: v for k, v in case.items() if k != "conn"}, sort_keys=True)),
+            "tw_%s_conn" % name: case["conn"], "tw_%s_rowptr" % name: rp,
+            "tw_%s_cols" % name: cols[:nnz], "tw_%s_w" % name: w[:nnz]})
     out = os.path.join(HERE, "api.npz")
     np.savez_compressed(out, **arrs)
     print("api ->", out, os.path.getsize(out), "bytes")

@@ -189,3 +189,53 @@ def test_forest_eval_interp_matches_reference(gpu_lib):
                 np.testing.assert_array_equal(np.stack(f.evalInterp(pt, 1)), z[key + "_d1"])
                 d2 = np.stack(f.evalInterp(pt, 2))
                 np.testing.assert_array_equal(d2[:10], z[key + "_d2"][:10])
+
+
+@pytest.mark.parametrize("name", ["brick_o2", "rot_o3"])
+def test_topo_weights_match_reference(gpu_lib, name):
+    """Design -> analysis weights of every element against the reference's
+    computeWeights steps run on the reference forests."""
+    from tmr_gb300 import TMR
+    z = _golden()
+    case = json.loads(str(z["tw_%s_case" % name]))
+    case["conn"] = z["tw_%s_conn" % name]
+    ana = TMR.OctForest(order=case["order"])
+    ana.setConnectivity(case["conn"])
+    ana.createTrees(case["L0"])
+    for p in range(case["passes"]):
+        o = ana.getOctantsArray()
+        ana.refine(pipeline.indicator(o, case, p), 0, case["max_level"])
+        ana.balance(1)
+    filt = ana.coarsen()
+    filt.balance(1)
+    filt.createNodes()
+    W_ = TMR.createTopoWeights(filt, ana)
+    rp, ci, w = W_.getCSR()
+    np.testing.assert_array_equal(rp, z["tw_%s_rowptr" % name])
+    np.testing.assert_array_equal(ci, z["tw_%s_cols" % name])
+    np.testing.assert_array_equal(w, z["tw_%s_w" % name])
+    # the element values of a constant design field are that constant
+    rows, cols, _ = W_.sizes()
+    y = np.zeros(rows)
+    W_.mult(np.full(cols, 0.7), y)
+    np.testing.assert_allclose(y, 0.7, rtol=1e-13)
+
+
+def test_interpolate_design_vec_keeps_constants(gpu_lib):
+    from tmr_gb300 import TMR
+    case = dict(pipeline.cases()["brick_o2"])
+    f = TMR.OctForest(order=2)
+    f.setConnectivity(case["conn"])
+    f.createTrees(1)
+    f.refine(W.random_indicator(f.getNumOctants(), 3, 0, 0.5), 0, 4)
+    f.balance(1)
+    f.createNodes()
+    g = f.duplicate()
+    g.refine(W.random_indicator(g.getNumOctants(), 3, 1, 0.3), 0, 5)
+    g.balance(1)
+    g.createNodes()
+    nf, ng = f.getNodeRange()[1], g.getNodeRange()[1]
+    x = np.tile([1.5, -2.0], nf)
+    y = np.zeros(2 * ng)
+    TMR.interpolateDesignVec(f, x, g, y)
+    np.testing.assert_allclose(y.reshape(-1, 2), np.tile([1.5, -2.0], (ng, 1)), rtol=1e-12)

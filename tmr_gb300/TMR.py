@@ -604,6 +604,102 @@ class MatrixFilter:
         return self._apply(True, g, _like(g))
 
 
+class ConformFilter:
+    """TMRConformFilter (TMRConformFilter.cpp:33-168; TMR.pyx
+    ConformFilter): the design variables live on the finest filter forest
+    and are restricted level by level with the weight-normalised P^T
+    (setDesignVars, :144-156).  ``assemblers`` are accepted and ignored
+    (no TACS); ``filters`` is the list of forests, finest first, each
+    balanced with nodes created.  applyFilter / applyTranspose are not
+    implemented by the reference for this filter (TMRTopoFilter.h: message
+    on stderr, no output), and likewise here."""
+
+    _name = "TMRConformFilter"
+
+    def __init__(self, assemblers=None, filters=None, vpn=1):
+        if assemblers is not None and len(assemblers) != len(filters):
+            raise ValueError("%s must have equal number of objects in lists" %
+                             type(self).__name__)
+        self.filters = list(filters)
+        self.vpn = vpn
+        self.interps = []
+        for k in range(len(self.filters) - 1):
+            I = VecInterp()
+            self.filters[k].createInterpolation(self.filters[k + 1], I)
+            self.interps.append(I)
+        self.x = None
+
+    def getFilter(self):
+        return self.filters[0]
+
+    def getNumLevels(self):
+        return len(self.filters)
+
+    def setDesignVars(self, x):
+        """x on the finest level, then x[k+1] = P_k^T-weighted x[k]; returns
+        the per-level vectors (the reference hands each to its level's
+        assembler)."""
+        levels = [x]
+        for I in self.interps:
+            rows, cols, _ = I.sizes()
+            out = _zeros_like(x, cols * self.vpn)
+            I.multWeightTranspose(levels[-1], out)
+            levels.append(out)
+        self.x = levels
+        return levels
+
+    def getDesignVars(self):
+        return None if self.x is None else self.x[0]
+
+    def addValues(self, g):
+        """The gradient with respect to the finest-level variables: for this
+        filter the reference only completes the vector's parallel
+        assembly (addValues, :161-164), so it is returned unchanged."""
+        return g
+
+    def setValues(self, g):
+        return g
+
+    def applyFilter(self, x, y, vpn=None):
+        import sys
+        sys.stderr.write("TMR Filter Error: applyFilter() method is not implemented!\n")
+
+    def applyTranspose(self, x, y, vpn=None):
+        import sys
+        sys.stderr.write("TMR Filter Error: applyTranspose() method is not implemented!\n")
+
+
+class LagrangeFilter(ConformFilter):
+    """TMRLagrangeFilter (TMRLagrangeFilter.cpp:31-150; TMR.pyx
+    LagrangeFilter): the same level-by-level weight-normalised restriction
+    of the design variables as ConformFilter (setDesignVars, :130-139)."""
+
+    _name = "TMRLagrangeFilter"
+
+
+def createTopoWeights(filter, forest):
+    """Design -> analysis weights of TMROctTACSTopoCreator
+    (TMR_TACSTopoCreator.cpp:55-183) as a VecInterp: rows = elements of
+    `forest`, columns = owned nodes of `filter`; mult maps filter design
+    values to element values."""
+    I = VecInterp()
+    h = _vp()
+    call("tmrg_topo_weights_create", filter.ptr, forest.ptr, ctypes.byref(h))
+    I.ptr = h
+    return I
+
+
+def interpolateDesignVec(orig_filter, orig_x, new_filter, new_x):
+    """interpolateDesignVec (TopOptUtils.py:270-307): the design values on
+    `orig_filter`'s nodes carried to `new_filter`'s nodes through
+    new_filter.createInterpolation(orig_filter); vectors node-major with
+    any number of values per node."""
+    I = VecInterp()
+    new_filter.createInterpolation(orig_filter, I)
+    I.mult(orig_x, new_x)
+    return new_x
+
+
 def _like(x):
     if _is_torch(x):
         import torch

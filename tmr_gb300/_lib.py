@@ -71,6 +71,7 @@ _SIGS = {
                                      c_vp],
     "tmrg_interp_create": [c_vp, c_vp, P(c_vp)],
     "tmrg_interp_destroy": [c_vp],
+    "tmrg_topo_weights_create": [c_vp, c_vp, P(c_vp)],
     "tmrg_interp_sizes": [c_vp, c_vp],
     "tmrg_interp_get_csr": [c_vp, c_vp, c_vp, c_vp],
     "tmrg_interp_mult": [c_vp, c_vp, c_vp, c_int],

@@ -949,6 +949,19 @@ int tmrg_interp_create(tmrg_forest *fine, tmrg_forest *coarse,
     *out = h;
   });
 }
+int tmrg_topo_weights_create(tmrg_forest *filter, tmrg_forest *analysis, tmrg_interp **out) {
+  return guarded([&] {
+    ARG(filter && analysis && out, "NULL argument");
+    auto *h = new tmrg_interp;
+    try {
+      topo_weights_create(filter->f, analysis->f, h->I);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
 int tmrg_interp_destroy(tmrg_interp *I) {
   return guarded([&] {
     if (!I) return;

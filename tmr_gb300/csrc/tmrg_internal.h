@@ -125,6 +125,7 @@ void forest_balance(Forest &f, int corner);
 void forest_create_nodes(Forest &f);
 void interp_create(Forest &fine, Forest &coarse, Interp &I);
 void interp_apply(Interp &I, int which, const double *x, double *y, int nvec);
+void topo_weights_create(Forest &filter, Forest &analysis, Interp &I);
 void filter_create(Forest &f, double len, double r, int N, Filter &F);
 void filter_apply(Filter &F, bool transpose, int vpn, const double *in,
                   double *out);

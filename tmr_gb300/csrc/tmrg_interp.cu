@@ -714,6 +714,31 @@ void forest_find_enclosing(Forest &f, int order, const double *knots,
   TMRG_CUDA(cudaStreamSynchronize(s));
 }
 
+// Sorted expansion lists of every element of `coarse` (k_elist_*).
+struct ElemLists {
+  DBuf<long long> eoff;
+  DBuf<int> lcol;
+  DBuf<double> ldw;
+  DBuf<uint8_t> lkey, ekind;
+};
+static void build_elists(Forest &coarse, ElemLists &L, int *err, cudaStream_t s) {
+  const int cnpe = coarse.order * coarse.order * coarse.order;
+  L.eoff.alloc(coarse.n + 1, s);
+  launch(k_elist_count, blocks_for(coarse.n, 256), 256, 0, s, coarse.n, cnpe,
+         (const int *)coarse.econn.p, (const int *)coarse.dep_ptr.p, L.eoff.p);
+  exclusive_scan<long long>(L.eoff.p, L.eoff.p, coarse.n, s);
+  const long long ne = read_scalar(L.eoff.p + coarse.n, s);
+  L.lcol.alloc(ne + 1, s);
+  L.ldw.alloc(ne + 1, s);
+  L.lkey.alloc(ne + 1, s);
+  L.ekind.alloc(coarse.n + 1, s);
+  launch(k_elist_fill, blocks_for(coarse.n, EL_WARPS), EL_WARPS * 32, 0, s, coarse.n, cnpe,
+         (const int *)coarse.econn.p, (const int *)coarse.dep_ptr.p,
+         (const int *)coarse.dep_conn.p, (const double *)coarse.dep_w.p,
+         (const long long *)L.eoff.p, L.lcol.p, L.ldw.p, L.lkey.p, L.ekind.p, err);
+}
+static void interp_finish(Interp &I, long long nonzeros, cudaStream_t s);
+
 void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   Stage st("tmrg_create_interpolation");
   if (&fine == &coarse)
@@ -764,23 +789,13 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
          (const int16_t *)coarse.level.p, c4.p);
   c.c4 = c4.p;
   // sorted expansion list of every coarse element
-  DBuf<long long> eoff(coarse.n + 1, s);
-  launch(k_elist_count, blocks_for(coarse.n, 256), 256, 0, s, coarse.n, cnpe,
-         (const int *)coarse.econn.p, (const int *)coarse.dep_ptr.p, eoff.p);
-  exclusive_scan<long long>(eoff.p, eoff.p, coarse.n, s);
-  const long long ne = read_scalar(eoff.p + coarse.n, s);
-  DBuf<int> lcol(ne + 1, s);
-  DBuf<double> ldw(ne + 1, s);
-  DBuf<uint8_t> lkey(ne + 1, s), ekind(coarse.n + 1, s);
-  launch(k_elist_fill, blocks_for(coarse.n, EL_WARPS), EL_WARPS * 32, 0, s, coarse.n,
-         cnpe, (const int *)coarse.econn.p, (const int *)coarse.dep_ptr.p,
-         (const int *)coarse.dep_conn.p, (const double *)coarse.dep_w.p,
-         (const long long *)eoff.p, lcol.p, ldw.p, lkey.p, ekind.p, err.p);
-  c.eoff = eoff.p;
-  c.lcol = lcol.p;
-  c.ldw = ldw.p;
-  c.lkey = lkey.p;
-  c.ekind = ekind.p;
+  ElemLists EL;
+  build_elists(coarse, EL, err.p, s);
+  c.eoff = EL.eoff.p;
+  c.lcol = EL.lcol.p;
+  c.ldw = EL.ldw.p;
+  c.lkey = EL.lkey.p;
+  c.ekind = EL.ekind.p;
   c.rep = rep.p;
   c.err = err.p;
   for (int i = 0; i < TMRG_MAX_ORDER; i++)
@@ -818,19 +833,21 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
          (const int *)trow.p, (const long long *)roff.p, I.colidx.p, I.vals.p, nzcount.p);
   trow.release();
   roff.release();
-  eoff.release();
-  lcol.release();
-  ldw.release();
-  lkey.release();
-  ekind.release();
+  EL = ElemLists();
   c4.release();
   rep.release();
-
-  // zero-free copy for the applies, when P has exact zeros
   const long long nonzeros = (long long)read_scalar(nzcount.p, s);
   if (read_scalar(err.p, s))
     throw Error(TMRG_ERR_INTERNAL, "createInterpolation: a row outgrew its counted length");
-  // worth a second copy only when zeros are a good part of P
+  interp_finish(I, nonzeros, s);
+}
+
+// The apply structures of a finished P (rows, cols, nnz, rowptr, colidx,
+// vals set): the zero-free copy when P has exact zeros, the length-ordered
+// row permutation and P^T.
+static void interp_finish(Interp &I, long long nonzeros, cudaStream_t s) {
+  const long long rows = I.rows, nnz = I.nnz;
+  // zero-free copy for the applies, when P has exact zeros  // worth a second copy only when zeros are a good part of P
   I.nnz_nz = (nnz - nonzeros) * 8 >= nnz ? nonzeros : nnz;
   const long long nnz_nz = I.nnz_nz;
   if (I.nnz_nz < nnz) {
@@ -868,6 +885,161 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   launch(k_t_tail, blocks_for(I.cols + 1, 256), 256, 0, s, I.cols, nnz_nz,
          (const uint64_t *)tk.p, I.t_rowptr.p);
   TMRG_CUDA(cudaStreamSynchronize(s));
+}
+
+// ---------------------------------------------------------------------
+// Design -> analysis weights (TMROctTACSTopoCreator::computeWeights,
+// TMR_TACSTopoCreator.cpp:55-122, called per element at :163-183): the
+// centre of every analysis element (an order-3 node with knots -1, 0, 1
+// and local index 13) is located in the filter forest with findEnclosing;
+// the filter's shape functions at that point, expanded through the filter's
+// dependent nodes and merged by column (uniqueSort), are the element's
+// row.  The merge follows the filter element's sorted expansion list, in
+// the reference's loop order.
+__global__ void k_tw_count(long long n, InterpCtx I, const int *__restrict__ ab,
+                           const int *__restrict__ ax, const int *__restrict__ ay,
+                           const int *__restrict__ az, const int16_t *__restrict__ al,
+                           int *trow, long long *cnt) {
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const Oct node{ab[e], ax[e], ay[e], az[e], al[e]};
+  const long long t = find_enclosing(I, node, 13);
+  trow[e] = (int)t;
+  long long m = 0;
+  if (t < 0) {
+    atomicExch(I.err, 1);
+  } else {
+    int prev = -1;
+    for (long long j = I.eoff[t]; j < I.eoff[t + 1]; j++) {
+      const int col = I.lcol[j];
+      m += (col != prev);
+      prev = col;
+    }
+  }
+  cnt[e] = m;
+}
+__global__ void k_tw_rows(long long n, InterpCtx I, const int *__restrict__ ax,
+                          const int *__restrict__ ay, const int *__restrict__ az,
+                          const int16_t *__restrict__ al, const int *__restrict__ trow,
+                          const long long *__restrict__ roff, int *cols, double *vals) {
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int t = trow[e];
+  if (t < 0) return;
+  const int co = I.co, co2 = co * co;
+  const int4 cq = __ldg(I.c4 + t);
+  const int32_t hoct = side_of(cq.x >> 26), h = side_of(al[e]);
+  const int32_t xyz[3] = {ax[e], ay[e], az[e]};
+  double N[3][IMAX_CO];
+  for (int a = 0; a < 3; a++) {
+    // -1 + 2 ((x mod hoct) + 0.5 h (1 + 0)) / hoct, as the reference rounds it
+    const double u = -1.0 + 2.0 * ((double)(xyz[a] % hoct) + 0.5 * (double)h * 1.0) /
+                                (double)hoct;
+    lagrange3(co, u, I.ck, I.crk, N[a][0], N[a][1], N[a][2]);
+  }
+  long long o = roff[e];
+  const long long lim = roff[e + 1];
+  int prev = -1;
+  double acc = 0.0;
+  bool open = false;
+  for (long long j = I.eoff[t]; j < I.eoff[t + 1]; j++) {
+    const int key = I.lkey[j], li = key & 31, col = I.lcol[j];
+    const int kk = li / co2, jj = (li - kk * co2) / co, ii = li - kk * co2 - jj * co;
+    double w = __dmul_rn(__dmul_rn(N[0][ii], N[1][jj]), N[2][kk]);
+    if (!(key & KEY_INDEP)) w = __dmul_rn(w, I.ldw[j]);
+    if (open && col == prev) {
+      acc = __dadd_rn(acc, w);
+    } else {
+      if (open && o < lim) {
+        cols[o] = prev;
+        vals[o] = acc;
+        o++;
+      }
+      acc = w;
+      prev = col;
+      open = true;
+    }
+  }
+  if (open && o < lim) {
+    cols[o] = prev;
+    vals[o] = acc;
+  }
+}
+
+void topo_weights_create(Forest &filter, Forest &analysis, Interp &I) {
+  Stage st("tmrg_topo_weights");
+  if (filter.order > IMAX_CO)
+    throw Error(TMRG_ERR_UNSUPPORTED, "topo weights: filter order > 3 is not built");
+  if (filter.interp == TMRG_BERNSTEIN_POINTS)
+    throw Error(TMRG_ERR_UNSUPPORTED, "topo weights: Bernstein filter is not built");
+  if (!analysis.have_octs) throw Error(TMRG_ERR_STATE, "topo weights: no analysis octants");
+  forest_create_nodes(filter);
+  if (filter.conn->nb >= (1 << 26))
+    throw Error(TMRG_ERR_KEY_RANGE, "topo weights: more than 2^26 blocks");
+  cudaStream_t s = analysis.s;
+  TMRG_CUDA(cudaStreamSynchronize(filter.s));
+  I.s = s;
+  I.have_colsum = false;
+  I.colsum.release();
+  const long long rows = analysis.n;
+  I.rows = rows;
+  I.cols = filter.num_owned;
+  DBuf<int> err(1, s);
+  err.zero();
+  InterpCtx c{};
+  c.fo = 3;  // the element centre is an order-3 node with knots -1, 0, 1
+  c.fk1[0] = 0.0;
+  c.fk1[1] = 1.0;
+  c.fk1[2] = 2.0;
+  c.co = filter.order;
+  for (int i = 0; i < TMRG_MAX_ORDER; i++) c.ck[i] = filter.knots[i];
+  for (int i = 0; i < TMRG_MAX_ORDER; i++)
+    for (int j = 0; j < TMRG_MAX_ORDER; j++)
+      c.crk[i][j] = (i != j && i < filter.order && j < filter.order)
+                        ? 1.0 / (filter.knots[i] - filter.knots[j])
+                        : 0.0;
+  c.cn = filter.n;
+  DBuf<int4> c4(filter.n + 1, s);
+  launch(k_pack_octs, blocks_for(filter.n, 256), 256, 0, s, filter.n,
+         (const int *)filter.block.p, (const int *)filter.x.p, (const int *)filter.y.p,
+         (const int *)filter.z.p, (const int16_t *)filter.level.p, c4.p);
+  c.c4 = c4.p;
+  ElemLists EL;
+  build_elists(filter, EL, err.p, s);
+  c.eoff = EL.eoff.p;
+  c.lcol = EL.lcol.p;
+  c.ldw = EL.ldw.p;
+  c.lkey = EL.lkey.p;
+  c.ekind = EL.ekind.p;
+  c.err = err.p;
+  DBuf<int> trow(rows + 1, s);
+  DBuf<long long> roff(rows + 1, s);
+  launch(k_tw_count, blocks_for(rows, 128), 128, 0, s, rows, c,
+         (const int *)analysis.block.p, (const int *)analysis.x.p, (const int *)analysis.y.p,
+         (const int *)analysis.z.p, (const int16_t *)analysis.level.p, trow.p, roff.p);
+  exclusive_scan<long long>(roff.p, roff.p, rows, s);
+  const long long nnz = read_scalar(roff.p + rows, s);
+  const int e = read_scalar(err.p, s);
+  if (e == 2)
+    throw Error(TMRG_ERR_INTERNAL, "topo weights: a filter element expands to more than 256 entries");
+  if (e)
+    throw Error(TMRG_ERR_INTERNAL, "topo weights: an element centre has no enclosing filter octant");
+  if (nnz >= (1LL << 31) - 1) throw Error(TMRG_ERR_ARG, "topo weights: more than 2^31 entries");
+  I.nnz = nnz;
+  I.rowptr.alloc(rows + 1, s);
+  launch(k_ptr32, blocks_for(rows + 1, 256), 256, 0, s, rows, (const long long *)roff.p,
+         I.rowptr.p);
+  I.colidx.alloc(nnz + 1, s);
+  I.vals.alloc(nnz + 1, s);
+  launch(k_tw_rows, blocks_for(rows, 128), 128, 0, s, rows, c, (const int *)analysis.x.p,
+         (const int *)analysis.y.p, (const int *)analysis.z.p,
+         (const int16_t *)analysis.level.p, (const int *)trow.p, (const long long *)roff.p,
+         I.colidx.p, I.vals.p);
+  trow.release();
+  roff.release();
+  EL = ElemLists();
+  c4.release();
+  interp_finish(I, nnz, s);
 }
 
 // Column sums of P for the weight-normalised transpose, on first use.
