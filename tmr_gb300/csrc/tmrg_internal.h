@@ -97,6 +97,7 @@ struct Interp {
   const double *ap_vals() const { return nnz_nz < nnz ? nz_vals.p : vals.p; }
   DBuf<int> perm;  // apply rows ordered by length inside windows
   DBuf<int> t_rowptr, t_colidx;  // P^T (zero-free) as CSR, rows = coarse nodes
+  DBuf<int> t_perm;              // P^T rows ordered by length inside windows
   DBuf<double> t_vals;
   bool have_colsum = false;
   DBuf<double> colsum;  // P^T 1 (column sums of P), made on first use

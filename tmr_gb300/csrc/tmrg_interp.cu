@@ -640,12 +640,12 @@ __global__ void k_t_tail(long long ncols, long long nnz, const uint64_t *__restr
 // Rows ordered by length inside windows of LO_WIN rows (one block per
 // window, counting sort on min(length, LO_BUCKETS - 1)); the order inside a
 // bucket does not matter, each row's sum is independent of it.
-constexpr int LO_WIN = 4096, LO_BUCKETS = 64, LO_THREADS = 256;
+constexpr int LO_WIN = 4096, LO_BUCKETS = 256, LO_THREADS = 256;
 __global__ void __launch_bounds__(LO_THREADS)
     k_len_order(long long rows, const int *__restrict__ rp, int *perm) {
   __shared__ int s_cnt[LO_BUCKETS], s_off[LO_BUCKETS];
   const long long w0 = (long long)blockIdx.x * LO_WIN;
-  if (threadIdx.x < LO_BUCKETS) s_cnt[threadIdx.x] = 0;
+  for (int i = threadIdx.x; i < LO_BUCKETS; i += LO_THREADS) s_cnt[i] = 0;
   __syncthreads();
   int b[LO_WIN / LO_THREADS];
 #pragma unroll
@@ -884,6 +884,9 @@ static void interp_finish(Interp &I, long long nonzeros, cudaStream_t s) {
          I.t_rowptr.p);
   launch(k_t_tail, blocks_for(I.cols + 1, 256), 256, 0, s, I.cols, nnz_nz,
          (const uint64_t *)tk.p, I.t_rowptr.p);
+  I.t_perm.alloc(I.cols + 1, s);
+  launch(k_len_order, blocks_for(I.cols, LO_WIN), LO_THREADS, 0, s, I.cols,
+         (const int *)I.t_rowptr.p, I.t_perm.p);
   TMRG_CUDA(cudaStreamSynchronize(s));
 }
 
@@ -1189,11 +1192,15 @@ template <int LPR>
 static void apply2(long long rows, long long nnz, int nvec2, const int *rp,
                    const int *ci, const double *v, const double *x, double *y,
                    const double *scale, const int *perm, cudaStream_t s) {
-  // long rows (P^T): the whole warp on one row; short rows (P): two rows
-  // per warp when the lanes allow
+  // with rows ordered by length: four rows per warp, one group of 8 lanes
+  // each (no partial sums to combine); otherwise long rows take a whole
+  // warp and short rows two rows per warp
   double avg = rows ? (double)nnz / (double)rows : 0.0;
   if (LPR == 8) {
-    if (avg >= 24)
+    if (perm)
+      launch((k_csr_apply_split<8, 1>), blocks_for((rows + 3) / 4 * 32, 256), 256, 0, s,
+             rows, nvec2, rp, ci, v, (const double2 *)x, (double2 *)y, scale, perm);
+    else if (avg >= 24)
       launch((k_csr_apply_split<8, 4>), blocks_for(rows * 32, 256), 256, 0, s, rows,
              nvec2, rp, ci, v, (const double2 *)x, (double2 *)y, scale,
              (const int *)nullptr);
@@ -1217,7 +1224,7 @@ void interp_apply(Interp &I, int which, const double *x, double *y, int nvec) {
   const int *ci = which == 0 ? I.ap_colidx() : I.t_colidx.p;
   const double *v = which == 0 ? I.ap_vals() : I.t_vals.p;
   const double *sc = which == 2 ? (const double *)I.colsum.p : (const double *)nullptr;
-  const int *perm = which == 0 ? (const int *)I.perm.p : (const int *)nullptr;
+  const int *perm = which == 0 ? (const int *)I.perm.p : (const int *)I.t_perm.p;
   // compulsory traffic: 12 B per nonzero entry, the row pointers, one read
   // of the input and one write of the output vectors
   const long long bytes = 12 * I.nnz_nz + 4 * (nout + 1) + 8LL * nvec * (nin + nout) +
