@@ -180,6 +180,30 @@ __device__ __forceinline__ void lagrange3(int order, double u, const double *kn,
 }
 // 2^e as a double from its exponent (exact; e >= -1022).
 __device__ __forceinline__ double pow2(int e) { return __hiloint2double((1023 + e) << 20, 0); }
+// A non-negative int32 as a double, assembled from its bits with integer
+// operations (exactly (double)v): GB300 issues int-to-double conversions on
+// its FP64 pipe.
+__device__ __forceinline__ double exact_double(int32_t v) {
+  if (v <= 0) return 0.0;
+  const int e = 31 - __clz(v);  // leading bit
+  const unsigned long long m = ((unsigned long long)(uint32_t)v << (52 - e)) &
+                               ((1ULL << 52) - 1ULL);
+  return __longlong_as_double((long long)(((unsigned long long)(1023 + e) << 52) | m));
+}
+
+// Integer bounds [lo, hi] of a node coordinate at a knot that is not an
+// octant-grid point (orders >= 4): x + (0.5 h)(1 + k) in double as the
+// reference rounds it, with 0.5 h = 2^(29 - level) exact.  An integer a
+// satisfies a <= xd iff a <= floor(xd), and xd <= b iff ceil(xd) <= b, so
+// the containment tests below stay in integers.  Kept out of line: GB300
+// runs integer-to-double conversions on its FP64 pipe, and the exact
+// (grid-point) case must not pay for them.
+__device__ __noinline__ void knot_bounds(int32_t x, int level, double fk1, int32_t &lo,
+                                         int32_t &hi) {
+  const double xd = __dadd_rn((double)x, __dmul_rn(pow2(TMRG_MAX_LEVEL - 1 - level), fk1));
+  lo = (int32_t)floor(xd);
+  hi = (int32_t)ceil(xd);
+}
 
 // findEnclosing (TMROctForest.cpp:6228-6377): binary search for the node's
 // element octant, then a forward scan up to the bounding position.
@@ -201,13 +225,10 @@ __device__ long long find_enclosing(const InterpCtx &I, const Oct &node, int inf
     zi = node.z + (kk / (order - 1)) * h;
   else if (order % 2 == 1 && kk == order / 2)
     zi = node.z + h / 2;
-  // node position at knots that are not octant-grid points (none below
-  // order 4): x + (0.5 h)(1 + k), with 0.5 h = 2^(29 - level) exact
-  const double half = pow2(TMRG_MAX_LEVEL - 1 - node.level);
-  double xd = 0.0, yd = 0.0, zd = 0.0;
-  if (xi < 0) xd = __dadd_rn((double)node.x, __dmul_rn(half, I.fk1[ii]));
-  if (yi < 0) yd = __dadd_rn((double)node.y, __dmul_rn(half, I.fk1[jj]));
-  if (zi < 0) zd = __dadd_rn((double)node.z, __dmul_rn(half, I.fk1[kk]));
+  int32_t xl = xi, xh = xi, yl = yi, yh = yi, zl = zi, zh = zi;
+  if (xi < 0) knot_bounds(node.x, node.level, I.fk1[ii], xl, xh);
+  if (yi < 0) knot_bounds(node.y, node.level, I.fk1[jj], yl, yh);
+  if (zi < 0) knot_bounds(node.z, node.level, I.fk1[kk], zl, zh);
   long long low = 0, high = I.cn - 1, mid = low + (high - low) / 2;
   while (mid != low) {
     int4 q = __ldg(I.c4 + mid);
@@ -232,12 +253,9 @@ __device__ long long find_enclosing(const InterpCtx &I, const Oct &node, int inf
     if (ab == node.block) {
       int32_t hm = side_of(q.x >> 26);
       int32_t ax = q.y, ay = q.z, az = q.w;
-      bool xin = (xi >= 0) ? (ax <= xi && xi <= ax + hm)
-                           : ((double)ax <= xd && xd <= (double)(ax + hm));
-      bool yin = (yi >= 0) ? (ay <= yi && yi <= ay + hm)
-                           : ((double)ay <= yd && yd <= (double)(ay + hm));
-      bool zin = (zi >= 0) ? (az <= zi && zi <= az + hm)
-                           : ((double)az <= zd && zd <= (double)(az + hm));
+      const bool xin = ax <= xl && xh <= ax + hm;
+      const bool yin = ay <= yl && yh <= ay + hm;
+      const bool zin = az <= zl && zh <= az + hm;
       if (xin && yin && zin) return mid;
     }
     mid++;
@@ -266,8 +284,8 @@ __device__ __forceinline__ void dir_weights(const InterpCtx &I, int i, int range
     n0 = n1 = n2 = 1.0;
     return;
   }
-  double t = __dadd_rn((double)nx, __dmul_rn(half, I.fk1[i]));
-  double u = __dadd_rn(-1.0, __dmul_rn(__dsub_rn(t, (double)ox), two_ihc));
+  double t = __dadd_rn(exact_double(nx), __dmul_rn(half, I.fk1[i]));
+  double u = __dadd_rn(-1.0, __dmul_rn(__dsub_rn(t, exact_double(ox)), two_ihc));
   lagrange3(I.co, u, I.ck, I.crk, n0, n1, n2);
 }
 // Bit l of the mask is set when local coarse node l = ii + jj*co + kk*co^2
@@ -372,6 +390,8 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
   __shared__ int s_c[IW_WARPS][IW_CAP];
   __shared__ double s_v[IW_WARPS][IW_CAP];
   __shared__ uint16_t s_k[IW_WARPS][IW_CAP];  // row slot << 8 | kk << 4 | ii + co*jj
+  __shared__ uint16_t s_rs[IW_WARPS][IW_CAP / 2];  // start and length of each
+  __shared__ uint8_t s_rl[IW_WARPS][IW_CAP / 2];   // run to sum
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const long long base = ((long long)blockIdx.x * IW_WARPS + warp) * 32;
@@ -450,21 +470,48 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
                                s_v[warp][k]);
     }
     __syncwarp();
+    // runs of equal (row, column) longer than one entry, listed densely so
+    // that their in-order sums run on as many lanes as there are runs
+    int nruns = 0;
+    for (int c0 = 0; c0 < end; c0 += 32) {
+      const int k = c0 + lane;
+      int len = 0;
+      if (k < end) {
+        const int col = s_c[warp][k], q = s_k[warp][k] >> 8;
+        if ((k == 0) || (s_c[warp][k - 1] != col) || ((s_k[warp][k - 1] >> 8) != q)) {
+          len = 1;
+          while (k + len < end && s_c[warp][k + len] == col && (s_k[warp][k + len] >> 8) == q)
+            len++;
+        }
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, len > 1);
+      if (len > 1) {
+        const int r = nruns + __popc(m & lt);
+        s_rs[warp][r] = (uint16_t)k;
+        s_rl[warp][r] = (uint8_t)len;
+      }
+      nruns += __popc(m);
+    }
+    __syncwarp();
+    for (int r = lane; r < nruns; r += 32) {
+      const int st = s_rs[warp][r], len = s_rl[warp][r];
+      double acc = s_v[warp][st];
+      for (int i = 1; i < len; i++) acc = __dadd_rn(acc, s_v[warp][st + i]);
+      s_v[warp][st] = acc;
+    }
+    __syncwarp();
     for (int c0 = 0; c0 < end; c0 += 32) {
       const int k = c0 + lane;
       bool head = false;
-      int col = 0, q = 0;
+      int col = 0;
       if (k < end) {
         col = s_c[warp][k];
-        q = s_k[warp][k] >> 8;
+        const int q = s_k[warp][k] >> 8;
         head = (k == 0) || (s_c[warp][k - 1] != col) || ((s_k[warp][k - 1] >> 8) != q);
       }
       const unsigned m = __ballot_sync(0xffffffffu, head);
       if (head) {
-        double acc = s_v[warp][k];
-        for (int k2 = k + 1;
-             k2 < end && s_c[warp][k2] == col && (s_k[warp][k2] >> 8) == q; k2++)
-          acc = __dadd_rn(acc, s_v[warp][k2]);
+        const double acc = s_v[warp][k];
         const long long o = out + __popc(m & lt);
         if (o < lim) {
           cols[o] = col;
