@@ -91,3 +91,30 @@ def test_apply_into_page_locked_output(gpu_lib):
     I.multTranspose(xt, z_page)
     I.multTranspose(xt, z_pin)
     np.testing.assert_array_equal(z_page, z_pin)
+
+
+def test_staged_transpose_matches_device_apply(gpu_lib):
+    """Host-input restriction (input copied in pieces overlapped with the
+    rows they complete) equals the device-resident apply bit for bit."""
+    import torch
+    from tmr_gb300 import TMR
+    f = _forest(TMR, passes=3)
+    f.createNodes()
+    c = f.coarsen()
+    c.balance(1)
+    c.createNodes()
+    I = TMR.VecInterp()
+    f.createInterpolation(c, I)
+    rows, cols, _ = I.sizes()
+    nv = 16
+    x = np.random.default_rng(8).standard_normal(rows * nv)
+    xd = torch.tensor(x, device="cuda")
+    for name in ("multTranspose", "multWeightTranspose"):
+        yd = torch.zeros(cols * nv, dtype=torch.float64, device="cuda")
+        getattr(I, name)(xd, yd)
+        y_page = np.zeros(cols * nv)
+        getattr(I, name)(x, y_page)
+        y_pin = torch.zeros(cols * nv, dtype=torch.float64, pin_memory=True).numpy()
+        getattr(I, name)(x, y_pin)
+        np.testing.assert_array_equal(y_page, yd.cpu().numpy())
+        np.testing.assert_array_equal(y_pin, yd.cpu().numpy())

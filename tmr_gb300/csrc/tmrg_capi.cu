@@ -994,9 +994,20 @@ static int interp_host(tmrg_interp *I, int which, const double *x, double *y,
     long long nin = (which == 0 ? P.cols : P.rows) * nvec;
     long long nout = (which == 0 ? P.rows : P.cols) * nvec;
     DBuf<double> dx(nin, P.s);
+    double *ym = (double *)host_mapped(y);
+    if (which != 0) {
+      // restriction: copy the input in pieces overlapped with the rows
+      // they complete
+      DBuf<double> dy;
+      if (!ym) dy.alloc(nout, P.s);
+      if (interp_apply_transpose_staged(P, which, x, dx.p, ym ? ym : dy.p, nvec)) {
+        if (!ym) copy_d2h(y, dy.p, sizeof(double) * nout, P.s);
+        return;
+      }
+    }
     TMRG_CUDA(cudaMemcpyAsync(dx.p, x, sizeof(double) * nin,
                               cudaMemcpyHostToDevice, P.s));
-    if (double *ym = (double *)host_mapped(y)) {
+    if (ym) {
       // page-locked output: the apply writes it over the host link while
       // it computes, instead of a copy after it
       interp_apply(P, which, dx.p, ym, nvec);

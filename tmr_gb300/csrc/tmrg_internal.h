@@ -97,7 +97,8 @@ struct Interp {
   const double *ap_vals() const { return nnz_nz < nnz ? nz_vals.p : vals.p; }
   DBuf<int> perm;  // apply rows ordered by length inside windows
   DBuf<int> t_rowptr, t_colidx;  // P^T (zero-free) as CSR, rows = coarse nodes
-  DBuf<int> t_perm;              // P^T rows ordered by length inside windows
+  DBuf<int> t_perm;  // P^T rows by input chunk of their last entry, then length
+  std::vector<long long> t_chunk;  // t_perm range of each input chunk
   DBuf<double> t_vals;
   bool have_colsum = false;
   DBuf<double> colsum;  // P^T 1 (column sums of P), made on first use
@@ -126,6 +127,8 @@ void forest_balance(Forest &f, int corner);
 void forest_create_nodes(Forest &f);
 void interp_create(Forest &fine, Forest &coarse, Interp &I);
 void interp_apply(Interp &I, int which, const double *x, double *y, int nvec);
+bool interp_apply_transpose_staged(Interp &I, int which, const double *xh, double *dx,
+                                   double *y, int nvec);
 void topo_weights_create(Forest &filter, Forest &analysis, Interp &I);
 void filter_create(Forest &f, double len, double r, int N, Filter &F);
 void filter_apply(Filter &F, bool transpose, int vpn, const double *in,

@@ -17,6 +17,8 @@
 // count, then write at the scanned offsets).  P^T is the zero-free matrix
 // re-sorted by (column, row), so transpose applies gather without atomics
 // and sum in a fixed order.
+#include <algorithm>
+
 #include "tmrg_tree.cuh"
 
 namespace tmrg {
@@ -688,8 +690,12 @@ __global__ void k_t_tail(long long ncols, long long nnz, const uint64_t *__restr
 // window, counting sort on min(length, LO_BUCKETS - 1)); the order inside a
 // bucket does not matter, each row's sum is independent of it.
 constexpr int LO_WIN = 4096, LO_BUCKETS = 256, LO_THREADS = 256;
+// input chunks of a host-buffer transpose apply: the copy of chunk k+1
+// overlaps the rows whose inputs lie in chunks <= k
+constexpr int TC_CHUNKS = 8;
 __global__ void __launch_bounds__(LO_THREADS)
-    k_len_order(long long rows, const int *__restrict__ rp, int *perm) {
+    k_len_order(long long rows, const int *__restrict__ rp, const int *__restrict__ list,
+                int *perm) {
   __shared__ int s_cnt[LO_BUCKETS], s_off[LO_BUCKETS];
   const long long w0 = (long long)blockIdx.x * LO_WIN;
   for (int i = threadIdx.x; i < LO_BUCKETS; i += LO_THREADS) s_cnt[i] = 0;
@@ -700,7 +706,8 @@ __global__ void __launch_bounds__(LO_THREADS)
     const long long r = w0 + threadIdx.x + k * LO_THREADS;
     b[k] = -1;
     if (r < rows) {
-      b[k] = min(__ldg(rp + r + 1) - __ldg(rp + r), LO_BUCKETS - 1);
+      const int row = list ? __ldg(list + r) : (int)r;
+      b[k] = min(__ldg(rp + row + 1) - __ldg(rp + row), LO_BUCKETS - 1);
       atomicAdd(&s_cnt[b[k]], 1);
     }
   }
@@ -715,8 +722,21 @@ __global__ void __launch_bounds__(LO_THREADS)
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < LO_WIN / LO_THREADS; k++)
-    if (b[k] >= 0)
-      perm[w0 + atomicAdd(&s_off[b[k]], 1)] = (int)(w0 + threadIdx.x + k * LO_THREADS);
+    if (b[k] >= 0) {
+      const long long r = w0 + threadIdx.x + k * LO_THREADS;
+      perm[w0 + atomicAdd(&s_off[b[k]], 1)] = list ? __ldg(list + r) : (int)r;
+    }
+}
+// P^T rows keyed by the input chunk holding their last (largest) input
+// row: chunk = last_row * TC_CHUNKS / n_in, empty rows in chunk 0.
+__global__ void k_t_chunk_keys(long long ncols, long long nin, const int *__restrict__ trp,
+                               const int *__restrict__ tci, uint64_t *keys, uint32_t *vals) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncols) return;
+  const int p0 = trp[c], p1 = trp[c + 1];
+  const long long last = p1 > p0 ? tci[p1 - 1] : 0;
+  keys[c] = (uint64_t)((last * TC_CHUNKS) / (nin > 0 ? nin : 1));
+  vals[c] = (uint32_t)c;
 }
 __global__ void k_rowsum(long long rows, const int *__restrict__ rowptr,
                          const double *__restrict__ vals, double *sum) {
@@ -913,7 +933,7 @@ static void interp_finish(Interp &I, long long nonzeros, cudaStream_t s) {
 
   I.perm.alloc(rows + 1, s);
   launch(k_len_order, blocks_for(rows, LO_WIN), LO_THREADS, 0, s, rows, I.ap_rowptr(),
-         I.perm.p);
+         (const int *)nullptr, I.perm.p);
 
   // P^T by a stable sort on the column (rows stay ascending per column).
   Stage st_t("tmrg_transpose");
@@ -931,9 +951,29 @@ static void interp_finish(Interp &I, long long nonzeros, cudaStream_t s) {
          I.t_rowptr.p);
   launch(k_t_tail, blocks_for(I.cols + 1, 256), 256, 0, s, I.cols, nnz_nz,
          (const uint64_t *)tk.p, I.t_rowptr.p);
-  I.t_perm.alloc(I.cols + 1, s);
-  launch(k_len_order, blocks_for(I.cols, LO_WIN), LO_THREADS, 0, s, I.cols,
-         (const int *)I.t_rowptr.p, I.t_perm.p);
+  // P^T rows ordered by the input chunk their last entry needs (stable),
+  // then by length inside 4096-row windows of each chunk
+  {
+    DBuf<uint64_t> ck(I.cols + 1, s);
+    DBuf<uint32_t> cv(I.cols + 1, s);
+    launch(k_t_chunk_keys, blocks_for(I.cols, 256), 256, 0, s, I.cols, rows,
+           (const int *)I.t_rowptr.p, (const int *)I.t_colidx.p, ck.p, cv.p);
+    radix_sort(ck, &cv, I.cols, bits_for(TC_CHUNKS), s);
+    std::vector<uint64_t> hk(I.cols > 0 ? I.cols : 1);
+    if (I.cols)
+      TMRG_CUDA(cudaMemcpyAsync(hk.data(), ck.p, sizeof(uint64_t) * I.cols,
+                                cudaMemcpyDeviceToHost, s));
+    TMRG_CUDA(cudaStreamSynchronize(s));
+    I.t_chunk.assign(TC_CHUNKS + 1, 0);
+    for (int k = 0; k <= TC_CHUNKS; k++)
+      I.t_chunk[k] = std::lower_bound(hk.begin(), hk.begin() + I.cols, (uint64_t)k) - hk.begin();
+    I.t_perm.alloc(I.cols + 1, s);
+    for (int k = 0; k < TC_CHUNKS; k++) {
+      const long long a = I.t_chunk[k], n = I.t_chunk[k + 1] - a;
+      launch(k_len_order, blocks_for(n, LO_WIN), LO_THREADS, 0, s, n,
+             (const int *)I.t_rowptr.p, (const int *)(cv.p + a), I.t_perm.p + a);
+    }
+  }
   TMRG_CUDA(cudaStreamSynchronize(s));
 }
 
@@ -1258,6 +1298,52 @@ static void apply2(long long rows, long long nnz, int nvec2, const int *rp,
   }
   launch(k_csr_apply2<LPR>, blocks_for(rows * LPR, 256), 256, 0, s, rows, nvec2,
          rp, ci, v, (const double2 *)x, (double2 *)y, scale);
+}
+
+// Transpose apply with the input in host memory: the input rows are copied
+// in TC_CHUNKS pieces on a second stream, and after piece k arrives the
+// output rows whose inputs all lie in pieces <= k are computed (t_perm
+// holds the rows grouped that way), so the copy of the next piece overlaps
+// them.  Same kernel, rows and summation order as the single apply.
+// Returns false (nothing done) where the grouped kernel does not apply.
+bool interp_apply_transpose_staged(Interp &I, int which, const double *xh, double *dx,
+                                   double *y, int nvec) {
+  if ((which != 1 && which != 2) || nvec % 2 != 0 || nvec / 2 < 8 ||
+      ((uintptr_t)dx % 16) != 0 || ((uintptr_t)y % 16) != 0 ||
+      (long long)I.t_chunk.size() != TC_CHUNKS + 1)
+    return false;
+  Stage st("tmrg_interp_mult_transpose_staged");
+  cudaStream_t s = I.s;
+  if (which == 2) interp_colsum(I);
+  cudaStream_t cs;
+  TMRG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaEvent_t ev[TC_CHUNKS + 1];
+  for (int k = 0; k <= TC_CHUNKS; k++)
+    TMRG_CUDA(cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming));
+  // the copies start after the work already queued on the forest stream
+  TMRG_CUDA(cudaEventRecord(ev[TC_CHUNKS], s));
+  TMRG_CUDA(cudaStreamWaitEvent(cs, ev[TC_CHUNKS], 0));
+  const long long nin = I.rows;
+  for (int k = 0; k < TC_CHUNKS; k++) {
+    const long long r0 = (k * nin + TC_CHUNKS - 1) / TC_CHUNKS;
+    const long long r1 = ((k + 1) * nin + TC_CHUNKS - 1) / TC_CHUNKS;
+    if (r1 > r0)
+      TMRG_CUDA(cudaMemcpyAsync(dx + r0 * nvec, xh + r0 * nvec, sizeof(double) * (r1 - r0) * nvec,
+                                cudaMemcpyHostToDevice, cs));
+    TMRG_CUDA(cudaEventRecord(ev[k], cs));
+  }
+  const double *sc = which == 2 ? (const double *)I.colsum.p : (const double *)nullptr;
+  for (int k = 0; k < TC_CHUNKS; k++) {
+    TMRG_CUDA(cudaStreamWaitEvent(s, ev[k], 0));
+    const long long a = I.t_chunk[k], n = I.t_chunk[k + 1] - a;
+    if (n > 0)
+      apply2<8>(n, I.nnz_nz, nvec / 2, I.t_rowptr.p, I.t_colidx.p, I.t_vals.p, dx, y, sc,
+                I.t_perm.p + a, s);
+  }
+  TMRG_CUDA(cudaStreamSynchronize(s));
+  for (int k = 0; k <= TC_CHUNKS; k++) cudaEventDestroy(ev[k]);
+  cudaStreamDestroy(cs);
+  return true;
 }
 
 void interp_apply(Interp &I, int which, const double *x, double *y, int nvec) {
