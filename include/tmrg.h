@@ -41,6 +41,7 @@ enum { TMRG_UNIFORM_POINTS = 0, TMRG_GAUSS_LOBATTO_POINTS = 1,
 typedef struct tmrg_forest tmrg_forest;
 typedef struct tmrg_interp tmrg_interp;
 typedef struct tmrg_filter tmrg_filter;
+typedef struct tmrg_helmholtz tmrg_helmholtz;
 
 /* Message of the last failed call on this thread ("" if none). */
 const char *tmrg_last_error(void);
@@ -309,6 +310,48 @@ int tmrg_filter_apply_transpose_f32_device(tmrg_filter *F, int vpn,
    the filter's stream; allocates nothing. */
 int tmrg_filter_apply_static_device(tmrg_filter *F, int transpose, int vpn,
                                     const double *in, double *out);
+
+/* ---- Helmholtz PDE filter ------------------------------------------- */
+/* TMRHelmholtzFilter::TMRHelmholtzFilter(r, nlevels, assemblers, filters)
+   (TMRHelmholtzFilter.cpp:29-33, initialize_helmholtz :48-111): the
+   Helmholtz operator K = int(r^2 grad N . grad N + N N) and mass M on each
+   forest of `filters` (finest first; each nested in the previous one,
+   nodes created, block boxes set; order 2 or 3 with the element bases of
+   TMRMatrixCreator.h:76-92), the createInterpolation operators between
+   consecutive forests, and the multigrid-preconditioned solver.  The
+   reference's TACS assemblers have no counterpart: the geometry is the
+   forests' block boxes (tmrg_forest_set_block_boxes). */
+int tmrg_helmholtz_create(tmrg_forest *const *filters, int nlevels, double r,
+                          tmrg_helmholtz **out);
+int tmrg_helmholtz_destroy(tmrg_helmholtz *H);
+/* out3[3 * k + {0, 1, 2}] = independent nodes, elements and dependent
+   nodes of level k, for k < nlevels. */
+int tmrg_helmholtz_sizes(tmrg_helmholtz *H, int *nlevels, int64_t *out3);
+/* applyFilter (TMRHelmholtzFilter.cpp:126-196): out = K^-1 M in, and
+   applyTranspose (:199-247): out = M K^-1 in, for `vpn` (1..16)
+   interleaved components over the finest forest's independent nodes.
+   Host pointers; *_device forms take device pointers on the filter's
+   stream. */
+int tmrg_helmholtz_apply(tmrg_helmholtz *H, int vpn, const double *in, double *out);
+int tmrg_helmholtz_apply_transpose(tmrg_helmholtz *H, int vpn, const double *in,
+                                   double *out);
+int tmrg_helmholtz_apply_device(tmrg_helmholtz *H, int vpn, const double *in,
+                                double *out);
+int tmrg_helmholtz_apply_transpose_device(tmrg_helmholtz *H, int vpn,
+                                          const double *in, double *out);
+/* Solver tolerances (the reference's KSM setTolerances(1e-12, 1e-30) with
+   at most 300 iterations, TMRHelmholtzFilter.cpp:91-101, are the
+   defaults): a component stops when |r| <= max(rtol |b|, atol). */
+int tmrg_helmholtz_set_tolerances(tmrg_helmholtz *H, double rtol, double atol,
+                                  int max_iters);
+/* Iterations and final residual norms (one per component, at most `n`)
+   of the last solve. */
+int tmrg_helmholtz_last_solve(tmrg_helmholtz *H, int *iters, double *res, int n);
+/* out = K in (which = 0) or M in (which = 1) on level `level`, the
+   assembled operators with dependent nodes condensed (device pointers,
+   nvec interleaved components). */
+int tmrg_helmholtz_mult_device(tmrg_helmholtz *H, int level, int which, int nvec,
+                               const double *in, double *out);
 
 /* ---- utilities -------------------------------------------------------- */
 /* Seeded refinement indicator used by the synthetic workloads:

@@ -677,6 +677,92 @@ class LagrangeFilter(ConformFilter):
     _name = "TMRLagrangeFilter"
 
 
+class HelmholtzFilter(ConformFilter):
+    """TMRHelmholtzFilter (TMRHelmholtzFilter.cpp:29-276; TMR.pyx
+    HelmholtzFilter(radius, assemblers, filters)): the Helmholtz PDE filter
+    psi = K^-1 M x on the finest filter forest, solved with conjugate
+    gradients preconditioned by a multigrid V-cycle over the filter
+    forests.  ``assemblers`` are accepted and ignored (no TACS); every
+    forest needs its nodes and block boxes (``setBlockBoxes``): the boxes
+    are the geometry the element integrals use."""
+
+    _name = "TMRHelmholtzFilter"
+
+    def __init__(self, r, assemblers=None, filters=None, vpn=1):
+        ConformFilter.__init__(self, assemblers, filters, vpn)
+        arr = (ctypes.c_void_p * len(self.filters))(*[f.ptr for f in self.filters])
+        h = _vp()
+        call("tmrg_helmholtz_create", arr, len(self.filters), float(r), ctypes.byref(h))
+        self.ptr = h
+        self.r = r
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                lib().tmrg_helmholtz_destroy(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+    def sizes(self):
+        """Per level (independent nodes, elements, dependent nodes)."""
+        n = ctypes.c_int(0)
+        out = np.zeros(3 * len(self.filters), np.int64)
+        call("tmrg_helmholtz_sizes", self.ptr, ctypes.byref(n), _ptr(out))
+        return out.reshape(-1, 3)[: n.value]
+
+    def setTolerances(self, rtol=1e-12, atol=1e-30, max_iters=300):
+        call("tmrg_helmholtz_set_tolerances", self.ptr, float(rtol), float(atol),
+             int(max_iters))
+
+    def lastSolve(self):
+        """(iterations, residual norm per component) of the last solve."""
+        it = ctypes.c_int(0)
+        res = np.zeros(16)
+        call("tmrg_helmholtz_last_solve", self.ptr, ctypes.byref(it), _ptr(res), 16)
+        return it.value, res
+
+    def _apply(self, transpose, x, y, vpn=None):
+        vpn = vpn or self.vpn
+        if _is_torch(x):
+            name = ("tmrg_helmholtz_apply_transpose_device" if transpose
+                    else "tmrg_helmholtz_apply_device")
+            call(name, self.ptr, vpn, _vp(x.data_ptr()), _vp(y.data_ptr()))
+        else:
+            x = np.ascontiguousarray(x, dtype=np.float64)
+            out = np.zeros(x.shape, np.float64)
+            name = "tmrg_helmholtz_apply_transpose" if transpose else "tmrg_helmholtz_apply"
+            call(name, self.ptr, vpn, _ptr(x), _ptr(out))
+            y[...] = out
+        return y
+
+    def applyFilter(self, x, y, vpn=None):
+        """applyFilter (:126-196): y = K^-1 M x per component."""
+        return self._apply(False, x, y, vpn)
+
+    def applyTranspose(self, x, y, vpn=None):
+        """applyTranspose (:199-247): y = M K^-1 x per component."""
+        return self._apply(True, x, y, vpn)
+
+    def mult(self, level, which, x, y, nvec=1):
+        """y = K x (which = 0) or M x (which = 1) on filter level `level`
+        (torch CUDA tensors)."""
+        call("tmrg_helmholtz_mult_device", self.ptr, int(level), int(which), int(nvec),
+             _vp(x.data_ptr()), _vp(y.data_ptr()))
+        return y
+
+    def setDesignVars(self, x):
+        """setDesignVars (:252-262): filter x, then restrict it level by
+        level with the weight-normalised P^T; returns the per-level
+        vectors."""
+        return ConformFilter.setDesignVars(self, self._apply(False, x, _like(x)))
+
+    def addValues(self, g):
+        """addValues (:267-272): the gradient with respect to the unfiltered
+        variables, applyTranspose of g."""
+        return self._apply(True, g, _like(g))
+
+
 def createTopoWeights(filter, forest):
     """Design -> analysis weights of TMROctTACSTopoCreator
     (TMR_TACSTopoCreator.cpp:55-183) as a VecInterp: rows = elements of

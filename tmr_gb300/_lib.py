@@ -91,6 +91,16 @@ _SIGS = {
     "tmrg_filter_apply_f32_device": [c_vp, c_int, c_vp, c_vp],
     "tmrg_filter_apply_transpose_f32_device": [c_vp, c_int, c_vp, c_vp],
     "tmrg_filter_apply_static_device": [c_vp, c_int, c_int, c_vp, c_vp],
+    "tmrg_helmholtz_create": [c_vp, c_int, c_dbl, P(c_vp)],
+    "tmrg_helmholtz_destroy": [c_vp],
+    "tmrg_helmholtz_sizes": [c_vp, c_vp, c_vp],
+    "tmrg_helmholtz_apply": [c_vp, c_int, c_vp, c_vp],
+    "tmrg_helmholtz_apply_transpose": [c_vp, c_int, c_vp, c_vp],
+    "tmrg_helmholtz_apply_device": [c_vp, c_int, c_vp, c_vp],
+    "tmrg_helmholtz_apply_transpose_device": [c_vp, c_int, c_vp, c_vp],
+    "tmrg_helmholtz_set_tolerances": [c_vp, c_dbl, c_dbl, c_int],
+    "tmrg_helmholtz_last_solve": [c_vp, c_vp, c_vp, c_int],
+    "tmrg_helmholtz_mult_device": [c_vp, c_int, c_int, c_int, c_vp, c_vp],
     "tmrg_random_refinement_device": [c_u64, c_u64, c_dbl, c_vp, c_i64, c_vp],
 }
 _RESTYPE = {

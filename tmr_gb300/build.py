@@ -22,6 +22,7 @@ SOURCES = [
     "tmrg_nodes.cu",
     "tmrg_interp.cu",
     "tmrg_filter.cu",
+    "tmrg_helmholtz.cu",
     "tmrg_capi.cu",
 ]
 

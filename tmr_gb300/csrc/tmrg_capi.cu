@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "tmrg_internal.h"
+#include "tmrg_helmholtz.h"
 
 using namespace tmrg;
 
@@ -87,6 +88,9 @@ struct tmrg_interp {
 };
 struct tmrg_filter {
   Filter F;
+};
+struct tmrg_helmholtz {
+  Helmholtz H;
 };
 
 static thread_local std::string g_last_error;
@@ -1148,6 +1152,105 @@ int tmrg_filter_apply_static_device(tmrg_filter *F, int transpose, int vpn,
   return guarded([&] {
     ARG(F && in && out && vpn > 0, "bad argument");
     filter_apply_static(F->F, transpose != 0, vpn, in, out);
+  });
+}
+
+// ---- Helmholtz filter ---------------------------------------------------
+int tmrg_helmholtz_create(tmrg_forest *const *filters, int nlevels, double r,
+                          tmrg_helmholtz **out) {
+  return guarded([&] {
+    ARG(filters && out && nlevels > 0, "bad argument");
+    ARG(r >= 0.0, "Helmholtz radius must be >= 0");
+    std::vector<Forest *> fs(nlevels);
+    for (int k = 0; k < nlevels; k++) {
+      ARG(filters[k], "NULL forest");
+      fs[k] = &filters[k]->f;
+    }
+    auto *h = new tmrg_helmholtz;
+    try {
+      helmholtz_create(fs.data(), nlevels, r, h->H);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+int tmrg_helmholtz_destroy(tmrg_helmholtz *H) {
+  return guarded([&] {
+    if (!H) return;
+    cudaStreamSynchronize(H->H.s);
+    delete H;
+  });
+}
+int tmrg_helmholtz_sizes(tmrg_helmholtz *H, int *nlevels, int64_t *out3) {
+  return guarded([&] {
+    ARG(H, "NULL filter");
+    if (nlevels) *nlevels = H->H.nlevels;
+    if (out3)
+      for (int k = 0; k < H->H.nlevels; k++) {
+        out3[3 * k] = H->H.L[k]->nn;
+        out3[3 * k + 1] = H->H.L[k]->ne;
+        out3[3 * k + 2] = H->H.L[k]->ndep;
+      }
+  });
+}
+static int helmholtz_host(tmrg_helmholtz *H, bool tr, int vpn, const double *in,
+                          double *out) {
+  return guarded([&] {
+    ARG(H && in && out && vpn > 0, "bad argument");
+    Helmholtz &M = H->H;
+    long long len = M.L[0]->nn * vpn;
+    DBuf<double> a(std::max(1LL, len), M.s), b(std::max(1LL, len), M.s);
+    if (len)
+      TMRG_CUDA(cudaMemcpyAsync(a.p, in, sizeof(double) * len, cudaMemcpyHostToDevice, M.s));
+    helmholtz_apply(M, tr, vpn, a.p, b.p);
+    copy_d2h(out, b.p, sizeof(double) * len, M.s);
+  });
+}
+int tmrg_helmholtz_apply(tmrg_helmholtz *H, int vpn, const double *in, double *out) {
+  return helmholtz_host(H, false, vpn, in, out);
+}
+int tmrg_helmholtz_apply_transpose(tmrg_helmholtz *H, int vpn, const double *in,
+                                   double *out) {
+  return helmholtz_host(H, true, vpn, in, out);
+}
+int tmrg_helmholtz_apply_device(tmrg_helmholtz *H, int vpn, const double *in,
+                                double *out) {
+  return guarded([&] {
+    ARG(H && in && out && vpn > 0, "bad argument");
+    helmholtz_apply(H->H, false, vpn, in, out);
+  });
+}
+int tmrg_helmholtz_apply_transpose_device(tmrg_helmholtz *H, int vpn,
+                                          const double *in, double *out) {
+  return guarded([&] {
+    ARG(H && in && out && vpn > 0, "bad argument");
+    helmholtz_apply(H->H, true, vpn, in, out);
+  });
+}
+int tmrg_helmholtz_set_tolerances(tmrg_helmholtz *H, double rtol, double atol,
+                                  int max_iters) {
+  return guarded([&] {
+    ARG(H && rtol >= 0.0 && atol >= 0.0 && max_iters > 0, "bad argument");
+    H->H.rtol = rtol;
+    H->H.atol = atol;
+    H->H.max_iters = max_iters;
+  });
+}
+int tmrg_helmholtz_last_solve(tmrg_helmholtz *H, int *iters, double *res, int n) {
+  return guarded([&] {
+    ARG(H, "NULL filter");
+    if (iters) *iters = H->H.last_iters;
+    if (res)
+      for (int k = 0; k < n && k < (int)H->H.last_res.size(); k++) res[k] = H->H.last_res[k];
+  });
+}
+int tmrg_helmholtz_mult_device(tmrg_helmholtz *H, int level, int which, int nvec,
+                               const double *in, double *out) {
+  return guarded([&] {
+    ARG(H && in && out && nvec > 0 && (which == 0 || which == 1), "bad argument");
+    helmholtz_operator(H->H, level, which == 0, nvec, in, out);
   });
 }
 

@@ -1,0 +1,1080 @@
+// Helmholtz PDE density filter (TMRHelmholtzFilter.cpp:29-247) on the GPU.
+//
+// The filter solves, per design component,
+//     K psi = M x,   K = int(r^2 grad N . grad N + N N),  M = int(N N)
+// on the finest filter forest (applyFilter, :126-196) and applies
+// M K^-1 for the transpose (applyTranspose, :199-247).  The element weak
+// form is TMRHexaHelmholtzModel's (TMRHelmholtzModel.cpp:67-97); the
+// element basis is the one TMROctTACSMatrixCreator picks for the forest
+// order (TMRMatrixCreator.h:76-92): the linear hexahedron for order 2 and
+// the quadratic Bernstein hexahedron for order 3.
+//
+// Design:
+// * Matrix-free operator.  Forest geometry is a box per block, so every
+//   element is an axis-aligned box and its matrices are tensor products of
+//   exact 1-D reference matrices: K_e = V (cx Kx My Mz + cy Mx Ky Mz +
+//   cz Mx My Kz + Mx My Mz) with V the element's Jacobian determinant and
+//   c_d = r^2 / s_d^2 (s_d the half side).  One thread per element gathers
+//   its node values (dependent nodes through their weights), applies K_e
+//   by sum factorisation (7 one-dimensional contractions) and writes one
+//   value per element slot; a node-ordered scatter list then sums the slot
+//   values of every independent node in a fixed order (deterministic, no
+//   atomics).  The same scatter list gives the Jacobi diagonal and, on the
+//   coarsest level, the dense matrix.
+// * Solver.  The reference runs GMRES(50) preconditioned by TACS
+//   multigrid (symmetric SOR smoothing, direct coarse solve) to a relative
+//   residual of 1e-12.  The operator is SPD, so here the Krylov method is
+//   conjugate gradients in FP64 (two reductions an iteration, Polak-Ribiere
+//   form so that the preconditioner may vary slightly) and the
+//   preconditioner is one multigrid V-cycle computed in FP32: GB300 runs
+//   FP32 at 64 times its FP64 rate, and the FP64 outer iteration still
+//   drives the true residual to the reference's tolerance.  The smoother is
+//   Chebyshev on D^-1 K over [0.1, 1.1] lmax (lmax from Lanczos; degree 3
+//   for order-2 levels, 6 for order 3), which is parallel where SOR is
+//   sequential.  Restriction and prolongation are the forests' own
+//   createInterpolation operators (P^T and P); coarse levels are
+//   rediscretised, as in the reference (use_galerkin = 0).  The coarsest
+//   level is solved with its explicit dense inverse (Gauss-Jordan on the
+//   GPU) when it has at most HM_DENSE_MAX nodes, else by Chebyshev sweeps.
+// * All design components are solved together: vectors are node-major
+//   with `nvec` interleaved components and every scalar of the iteration is
+//   kept per component.
+#include <algorithm>
+#include <cmath>
+#include <string>
+
+#include "tmrg_helmholtz.h"
+
+namespace tmrg {
+
+constexpr int HM_THREADS = 128;
+constexpr int HM_RED_BLOCKS = 304;  // 2 per SM
+constexpr int HM_MAXVEC = 16;
+
+// ---------------------------------------------------------------------
+// 1-D reference matrices of the element basis on [-1, 1], by Gauss
+// quadrature with `o` points (the element's own rule).
+static void make_basis(int o, HBasisT<double> &B) {
+  B.o = o;
+  double pts[3], wts[3];
+  if (o == 2) {
+    pts[0] = -1.0 / std::sqrt(3.0);
+    pts[1] = 1.0 / std::sqrt(3.0);
+    wts[0] = wts[1] = 1.0;
+  } else {
+    pts[0] = -std::sqrt(0.6);
+    pts[1] = 0.0;
+    pts[2] = std::sqrt(0.6);
+    wts[0] = wts[2] = 5.0 / 9.0;
+    wts[1] = 8.0 / 9.0;
+  }
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++) B.M[a][b] = B.K[a][b] = 0.0;
+  for (int q = 0; q < o; q++) {
+    double u = pts[q], N[3], D[3];
+    if (o == 2) {
+      N[0] = 0.5 * (1.0 - u);
+      N[1] = 0.5 * (1.0 + u);
+      D[0] = -0.5;
+      D[1] = 0.5;
+    } else {
+      N[0] = 0.25 * (1.0 - u) * (1.0 - u);
+      N[1] = 0.5 * (1.0 - u) * (1.0 + u);
+      N[2] = 0.25 * (1.0 + u) * (1.0 + u);
+      D[0] = -0.5 * (1.0 - u);
+      D[1] = -u;
+      D[2] = 0.5 * (1.0 + u);
+    }
+    for (int a = 0; a < o; a++)
+      for (int b = 0; b < o; b++) {
+        B.M[a][b] += wts[q] * N[a] * N[b];
+        B.K[a][b] += wts[q] * D[a] * D[b];
+      }
+  }
+}
+
+// Element factors: V = sx sy sz, c_d = r^2 / s_d^2, s_d the half side of
+// the element in direction d (block box extent x 2^-level / 2).
+__global__ void k_h_geom(long long ne, const int *__restrict__ block,
+                         const int16_t *__restrict__ level,
+                         const double *__restrict__ boxes, double r2, HGeoT<double> *geo,
+                         HGeoT<float> *geo32) {
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const double *bx = boxes + 6LL * block[e];
+  int l = level[e];
+  double sx = ldexp(bx[3], -l - 1), sy = ldexp(bx[4], -l - 1), sz = ldexp(bx[5], -l - 1);
+  HGeoT<double> g{sx * sy * sz, r2 / (sx * sx), r2 / (sy * sy), r2 / (sz * sz)};
+  geo[e] = g;
+  geo32[e] = HGeoT<float>{(float)g.x, (float)g.y, (float)g.z, (float)g.w};
+}
+
+// Element matrix entry K_e[a][b] (stiff) or M_e[a][b].
+__device__ __forceinline__ double h_entry(const HBasisT<double> &B, int o, HGeoT<double> G,
+                                          int a, int b, bool stiff) {
+  int ax = a % o, ay = (a / o) % o, az = a / (o * o);
+  int bx = b % o, by = (b / o) % o, bz = b / (o * o);
+  double mx = B.M[ax][bx], my = B.M[ay][by], mz = B.M[az][bz];
+  double v = mx * my * mz;
+  if (stiff)
+    v += G.y * B.K[ax][bx] * my * mz + G.z * mx * B.K[ay][by] * mz +
+         G.w * mx * my * B.K[az][bz];
+  return G.x * v;
+}
+
+// ---------------------------------------------------------------------
+// Scatter list: for every independent node, the element slots that add
+// into it (slot-major index a*ne + e) with their weights, in slot order.
+__global__ void k_h_scount(long long nslot, const int *__restrict__ econn,
+                           const int *__restrict__ dptr, unsigned *cnt) {
+  long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nslot) return;
+  int g = econn[s];
+  cnt[s] = g >= 0 ? 1u : (unsigned)(dptr[-g] - dptr[-g - 1]);
+}
+__global__ void k_h_sfill(long long nslot, long long ne, int npe,
+                          const int *__restrict__ econn, const int *__restrict__ dptr,
+                          const int *__restrict__ dconn, const double *__restrict__ dw,
+                          const unsigned *__restrict__ off, uint64_t *keys,
+                          uint32_t *pay, int *ent_slot, double *ent_w) {
+  long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nslot) return;
+  long long e = s / npe;
+  int a = (int)(s - e * npe);
+  int q = (int)(a * ne + e);
+  unsigned o = off[s];
+  int g = econn[s];
+  if (g >= 0) {
+    keys[o] = (uint64_t)g;
+    pay[o] = o;
+    ent_slot[o] = q;
+    ent_w[o] = 1.0;
+    return;
+  }
+  for (int p = dptr[-g - 1]; p < dptr[-g]; p++, o++) {
+    keys[o] = (uint64_t)dconn[p];
+    pay[o] = o;
+    ent_slot[o] = q;
+    ent_w[o] = dw[p];
+  }
+}
+__global__ void k_h_sfinish(long long E, const uint32_t *__restrict__ pay,
+                            const int *__restrict__ ent_slot,
+                            const double *__restrict__ ent_w, int *slot, double *w,
+                            float *w32) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E) return;
+  uint32_t p = pay[i];
+  slot[i] = ent_slot[p];
+  w[i] = ent_w[p];
+  w32[i] = (float)ent_w[p];
+}
+// rp[j] = first sorted entry with node >= j.
+__global__ void k_h_srowptr(long long nn, long long E, const uint64_t *__restrict__ keys,
+                            int *rp) {
+  long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > nn) return;
+  long long lo = 0, hi = E;
+  while (lo < hi) {
+    long long m = (lo + hi) >> 1;
+    if (keys[m] < (uint64_t)j)
+      lo = m + 1;
+    else
+      hi = m;
+  }
+  rp[j] = (int)lo;
+}
+
+// Inverse Jacobi diagonal: diag_j = sum over elements e touching j of
+// sum_{(a,wa),(b,wb) in e} wa wb K_e[a][b].
+__global__ void k_h_diag(long long nn, long long ne, int o, HBasisT<double> B,
+                         const int *__restrict__ rp, const int *__restrict__ slot,
+                         const double *__restrict__ w,
+                         const HGeoT<double> *__restrict__ geo, double *dinv,
+                         float *dinv32, int *err) {
+  long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nn) return;
+  double d = 0.0;
+  int p = rp[j], p1 = rp[j + 1];
+  while (p < p1) {
+    unsigned e = (unsigned)slot[p] % (unsigned)ne;
+    int q = p + 1;
+    while (q < p1 && (unsigned)slot[q] % (unsigned)ne == e) q++;
+    HGeoT<double> G = geo[e];
+    for (int i = p; i < q; i++) {
+      int a = (int)((unsigned)slot[i] / (unsigned)ne);
+      for (int k = p; k < q; k++) {
+        int b = (int)((unsigned)slot[k] / (unsigned)ne);
+        d += w[i] * w[k] * h_entry(B, o, G, a, b, true);
+      }
+    }
+    p = q;
+  }
+  if (!(d > 0.0)) {
+    atomicExch(err, 1);
+    d = 1.0;
+  }
+  dinv[j] = 1.0 / d;
+  dinv32[j] = (float)(1.0 / d);
+}
+
+template <typename A, typename B>
+__global__ void k_h_cvt(long long n, const A *__restrict__ a, B *b) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (B)a[i];
+}
+
+// ---------------------------------------------------------------------
+// Operator: xd = dependent values, yE = element products, y = scatter.
+template <typename T>
+__global__ void k_h_dep(long long ndep, int nvec, const int *__restrict__ dptr,
+                        const int *__restrict__ dconn, const T *__restrict__ dw,
+                        const T *__restrict__ x, T *xd) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ndep * nvec) return;
+  long long d = i / nvec;
+  int v = (int)(i - d * nvec);
+  T s = T(0);
+  for (int p = dptr[d]; p < dptr[d + 1]; p++) s = fma(dw[p], x[(long long)dconn[p] * nvec + v], s);
+  xd[i] = s;
+}
+
+// One thread per element: gather, sum-factorised K_e (STIFF) or M_e,
+// slot-major output yE[(a*ne + e)*nvec + v].
+template <int O, bool STIFF, typename T>
+__global__ void __launch_bounds__(HM_THREADS)
+    k_h_elem(long long ne, int nvec, const int *__restrict__ econn,
+             const HGeoT<T> *__restrict__ geo, const T *__restrict__ x,
+             const T *__restrict__ xd, T *__restrict__ yE, HBasisT<T> B) {
+  constexpr int N = O * O * O;
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  int g[N];
+#pragma unroll
+  for (int a = 0; a < N; a++) g[a] = econn[e * N + a];
+  const HGeoT<T> G = geo[e];
+  for (int v = 0; v < nvec; v++) {
+    T u[N];
+#pragma unroll
+    for (int a = 0; a < N; a++)
+      u[a] = g[a] >= 0 ? __ldg(x + (long long)g[a] * nvec + v)
+                       : __ldg(xd + (long long)(-g[a] - 1) * nvec + v);
+    // z direction
+    T zm[N], zk[STIFF ? N : 1];
+#pragma unroll
+    for (int i = 0; i < O * O; i++)
+#pragma unroll
+      for (int bz = 0; bz < O; bz++) {
+        T sm = T(0), sk = T(0);
+#pragma unroll
+        for (int az = 0; az < O; az++) {
+          sm = fma(B.M[bz][az], u[i + O * O * az], sm);
+          if (STIFF) sk = fma(B.K[bz][az], u[i + O * O * az], sk);
+        }
+        zm[i + O * O * bz] = sm;
+        if (STIFF) zk[i + O * O * bz] = sk;
+      }
+    // y direction: ym = My zm, and in = cy Ky zm + cz My zk + My zm
+    T ym[N], in[N];
+#pragma unroll
+    for (int ix = 0; ix < O; ix++)
+#pragma unroll
+      for (int bz = 0; bz < O; bz++)
+#pragma unroll
+        for (int by = 0; by < O; by++) {
+          T sm = T(0), sk = T(0), sz = T(0);
+#pragma unroll
+          for (int ay = 0; ay < O; ay++) {
+            T t = zm[ix + O * ay + O * O * bz];
+            sm = fma(B.M[by][ay], t, sm);
+            if (STIFF) {
+              sk = fma(B.K[by][ay], t, sk);
+              sz = fma(B.M[by][ay], zk[ix + O * ay + O * O * bz], sz);
+            }
+          }
+          int c = ix + O * by + O * O * bz;
+          ym[c] = sm;
+          in[c] = STIFF ? fma(G.z, sk, fma(G.w, sz, sm)) : sm;
+        }
+    // x direction: y = V (Mx in + cx Kx ym)
+#pragma unroll
+    for (int bz = 0; bz < O; bz++)
+#pragma unroll
+      for (int by = 0; by < O; by++)
+#pragma unroll
+        for (int bx = 0; bx < O; bx++) {
+          T sm = T(0), sk = T(0);
+#pragma unroll
+          for (int ax = 0; ax < O; ax++) {
+            sm = fma(B.M[bx][ax], in[ax + O * by + O * O * bz], sm);
+            if (STIFF) sk = fma(B.K[bx][ax], ym[ax + O * by + O * O * bz], sk);
+          }
+          int b = bx + O * by + O * O * bz;
+          T r = STIFF ? fma(G.y, sk, sm) : sm;
+          yE[((long long)b * ne + e) * nvec + v] = G.x * r;
+        }
+  }
+}
+
+// y_j = sum of w yE[slot] over j's scatter list; mode 0: out = y,
+// 1: out = b - y, 2: out -= y.
+template <typename T>
+__global__ void k_h_scatter(long long nn, int nvec, const int *__restrict__ rp,
+                            const int *__restrict__ slot, const T *__restrict__ w,
+                            const T *__restrict__ yE, const T *__restrict__ b, T *out,
+                            int mode) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn * nvec) return;
+  long long j = i / nvec;
+  int v = (int)(i - j * nvec);
+  T s = T(0);
+  for (int p = rp[j]; p < rp[j + 1]; p++) s = fma(w[p], yE[(long long)slot[p] * nvec + v], s);
+  if (mode == 0)
+    out[i] = s;
+  else if (mode == 1)
+    out[i] = b[i] - s;
+  else
+    out[i] -= s;
+}
+
+// y = A x for a CSR matrix (thread per row and component).
+template <typename T>
+__global__ void k_h_csr(long long nrows, int nvec, const int *__restrict__ rp,
+                        const int *__restrict__ ci, const T *__restrict__ v,
+                        const T *__restrict__ x, T *y) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrows * nvec) return;
+  long long j = i / nvec;
+  int c = (int)(i - j * nvec);
+  T s = T(0);
+  for (int p = rp[j]; p < rp[j + 1]; p++) s = fma(v[p], x[(long long)ci[p] * nvec + c], s);
+  y[i] = s;
+}
+
+// ---------------------------------------------------------------------
+// Coarsest level: dense matrix (thread per row), Gauss-Jordan inverse,
+// dense product.
+__global__ void k_h_dense(long long nn, long long ne, int o, HBasisT<double> B,
+                          const int *__restrict__ rp, const int *__restrict__ slot,
+                          const double *__restrict__ w, const int *__restrict__ econn,
+                          const int *__restrict__ dptr, const int *__restrict__ dconn,
+                          const double *__restrict__ dw,
+                          const HGeoT<double> *__restrict__ geo, double *A) {
+  long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nn) return;
+  const int npe = o * o * o;
+  double *row = A + j * nn;
+  for (int p = rp[j]; p < rp[j + 1]; p++) {
+    unsigned e = (unsigned)slot[p] % (unsigned)ne;
+    int a = (int)((unsigned)slot[p] / (unsigned)ne);
+    HGeoT<double> G = geo[e];
+    for (int b = 0; b < npe; b++) {
+      double kab = w[p] * h_entry(B, o, G, a, b, true);
+      int g = econn[(long long)e * npe + b];
+      if (g >= 0) {
+        row[g] += kab;
+      } else {
+        for (int q = dptr[-g - 1]; q < dptr[-g]; q++) row[dconn[q]] += kab * dw[q];
+      }
+    }
+  }
+}
+__global__ void k_h_gj_copy(long long n, const double *__restrict__ A, long long k,
+                            double *rowk, double *colk) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  rowk[i] = A[k * n + i];
+  colk[i] = A[i * n + k];
+}
+// In-place Gauss-Jordan step k (no pivoting: the matrix is SPD).
+__global__ void k_h_gj_update(long long n, double *A, long long k,
+                              const double *__restrict__ rowk,
+                              const double *__restrict__ colk) {
+  long long jj = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long i = blockIdx.y;
+  if (jj >= n) return;
+  double p = 1.0 / rowk[k];
+  double v;
+  if (i == k && jj == k)
+    v = p;
+  else if (i == k)
+    v = rowk[jj] * p;
+  else if (jj == k)
+    v = -colk[i] * p;
+  else
+    v = A[i * n + jj] - colk[i] * rowk[jj] * p;
+  A[i * n + jj] = v;
+}
+// y = A x, warp per row, nvec interleaved components.
+template <typename T>
+__global__ void k_h_dense_mv(long long n, int nvec, const T *__restrict__ A,
+                             const T *__restrict__ x, T *y) {
+  long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (wid >= n * nvec) return;
+  long long i = wid / nvec;
+  int v = (int)(wid - i * nvec);
+  T s = T(0);
+  for (long long j = lane; j < n; j += 32) s = fma(A[i * n + j], x[j * nvec + v], s);
+#pragma unroll
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) y[wid] = s;
+}
+
+// ---------------------------------------------------------------------
+// Chebyshev smoother steps.
+// first:  d = c dinv r_in; x = d (zero guess: r_out = r_in) or x += d
+template <typename T>
+__global__ void k_h_cheb_first(long long n, int nvec, const T *__restrict__ dinv,
+                               const T *rin, T *rout, T *d, T *x, T c, int zero) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * nvec) return;
+  T r = rin[i];
+  T di = c * dinv[i / nvec] * r;
+  d[i] = di;
+  if (zero) {
+    x[i] = di;
+    if (rout != rin) rout[i] = r;
+  } else {
+    x[i] += di;
+  }
+}
+// d = a d + c dinv r; x += d
+template <typename T>
+__global__ void k_h_cheb_step(long long n, int nvec, const T *__restrict__ dinv,
+                              const T *__restrict__ r, T *d, T *x, T a, T c) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * nvec) return;
+  T di = fma(a, d[i], c * dinv[i / nvec] * r[i]);
+  d[i] = di;
+  x[i] += di;
+}
+template <typename T>
+__global__ void k_h_add(long long n, T *x, const T *__restrict__ t) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] += t[i];
+}
+
+// ---------------------------------------------------------------------
+// Reductions: per-component sums of a.b (and c.d) in a fixed order:
+// block partials, then one block combines them.
+__global__ void __launch_bounds__(256)
+    k_h_dot2(long long n, int nvec, const double *__restrict__ a,
+             const double *__restrict__ b, const double *__restrict__ c,
+             const double *__restrict__ d, double *part) {
+  __shared__ double sh[2][HM_MAXVEC][8];
+  double s1[HM_MAXVEC], s2[HM_MAXVEC];
+  for (int v = 0; v < nvec; v++) s1[v] = s2[v] = 0.0;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n;
+       j += (long long)gridDim.x * blockDim.x) {
+    for (int v = 0; v < nvec; v++) {
+      long long i = j * nvec + v;
+      s1[v] = fma(a[i], b[i], s1[v]);
+      if (c) s2[v] = fma(c[i], d[i], s2[v]);
+    }
+  }
+  int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  for (int v = 0; v < nvec; v++) {
+    double x1 = s1[v], x2 = s2[v];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      x1 += __shfl_xor_sync(0xffffffffu, x1, o);
+      x2 += __shfl_xor_sync(0xffffffffu, x2, o);
+    }
+    if (lane == 0) {
+      sh[0][v][wp] = x1;
+      sh[1][v][wp] = x2;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 2 * nvec) {
+    int k = threadIdx.x / nvec, v = threadIdx.x % nvec;
+    double t = 0.0;
+    for (int q = 0; q < 8; q++) t += sh[k][v][q];
+    part[((long long)blockIdx.x * 2 + k) * nvec + v] = t;
+  }
+}
+// out[k*nvec + v] = sum over blocks of part (k = 0, 1)
+__global__ void k_h_dot_final(int nblocks, int nvec, const double *__restrict__ part,
+                              double *out) {
+  int t = threadIdx.x;
+  if (t >= 2 * nvec) return;
+  int k = t / nvec, v = t % nvec;
+  double s = 0.0;
+  for (int b = 0; b < nblocks; b++) s += part[((long long)b * 2 + k) * nvec + v];
+  out[k * nvec + v] = s;
+}
+
+// Conjugate-gradient scalars, per component v at sc[8v]: [0] r.z, [2]
+// alpha, [3] beta, [4] done flag, [5] thr^2.
+// alpha = rz / pq (0 once the component has converged)
+__global__ void k_h_cg_alpha(int nvec, const double *__restrict__ dots, double *sc) {
+  int v = threadIdx.x;
+  if (v >= nvec) return;
+  double *c = sc + 8 * v;
+  double pq = dots[v];
+  c[2] = (c[4] != 0.0 || pq == 0.0) ? 0.0 : c[0] / pq;
+}
+// a component is done once r.r <= thr^2 (alpha and beta are 0 from then on)
+__global__ void k_h_cg_check(int nvec, const double *__restrict__ dots, double *sc) {
+  int v = threadIdx.x;
+  if (v >= nvec) return;
+  if (dots[v] <= sc[8 * v + 5]) sc[8 * v + 4] = 1.0;
+}
+// after the preconditioner: dots = (r.z_new, r.z_old); Polak-Ribiere
+// beta = (r.z_new - r.z_old) / rz, then rz = r.z_new
+__global__ void k_h_cg_beta(int nvec, const double *__restrict__ dots, double *sc) {
+  int v = threadIdx.x;
+  if (v >= nvec) return;
+  double *c = sc + 8 * v;
+  double rz = dots[v], rzo = dots[nvec + v];
+  c[3] = (c[4] != 0.0 || c[0] == 0.0) ? 0.0 : (rz - rzo) / c[0];
+  c[0] = rz;
+}
+// x += alpha p; r -= alpha q
+__global__ void k_h_cg_update(long long n, int nvec, const double *__restrict__ sc,
+                              const double *__restrict__ p, const double *__restrict__ q,
+                              double *x, double *r) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * nvec) return;
+  double al = sc[8 * (i % nvec) + 2];
+  x[i] = fma(al, p[i], x[i]);
+  r[i] = fma(-al, q[i], r[i]);
+}
+// p = z + beta p
+__global__ void k_h_cg_dir(long long n, int nvec, const double *__restrict__ sc,
+                           const double *__restrict__ z, double *p) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * nvec) return;
+  p[i] = fma(sc[8 * (i % nvec) + 3], p[i], z[i]);
+}
+
+// Lanczos helpers on D^-1/2 K D^-1/2.
+__global__ void k_h_scale_sqrt(long long n, const double *__restrict__ dinv,
+                               const double *v, double *u) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) u[i] = sqrt(dinv[i]) * v[i];
+}
+// w = w - alpha v - beta vp
+__global__ void k_h_lanczos_orth(long long n, double *w, const double *__restrict__ v,
+                                 const double *__restrict__ vp, double alpha, double beta) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) w[i] = w[i] - alpha * v[i] - beta * vp[i];
+}
+__global__ void k_h_scale(long long n, double *v, const double *w, double c) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = c * w[i];
+}
+// deterministic start vector in (0.5, 1.5)
+__global__ void k_h_start(long long n, double *v) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t h = (uint64_t)i * 0x9E3779B97F4A7C15ULL + 0x632BE59BD9B4E019ULL;
+  h ^= h >> 31;
+  h *= 0xBF58476D1CE4E5B9ULL;
+  h ^= h >> 29;
+  v[i] = 0.5 + (double)(h >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// ---------------------------------------------------------------------
+template <typename T>
+static void ensure(DBuf<T> &b, long long n, cudaStream_t s) {
+  if ((long long)b.n < n) b.alloc(n, s);
+}
+
+template <typename T>
+static void ensure_work(HLevel &L, HWork<T> &W, int nvec, cudaStream_t s) {
+  if (nvec <= W.cap) return;
+  W.cap = nvec;
+  for (DBuf<T> *b : {&W.x, &W.b, &W.r, &W.d, &W.t}) b->alloc(std::max(1LL, L.nn * nvec), s);
+  W.xd.alloc(std::max(1LL, L.ndep * nvec), s);
+  W.yE.alloc(std::max(1LL, L.ne * L.npe * nvec), s);
+}
+
+template <typename T>
+struct LevelData;
+template <>
+struct LevelData<double> {
+  static HWork<double> &work(HLevel &L) { return L.w64; }
+  static const double *dw(HLevel &L) { return L.dw.p; }
+  static const double *sw(HLevel &L) { return L.sw.p; }
+  static const double *dinv(HLevel &L) { return L.dinv.p; }
+  static const HGeoT<double> *geo(HLevel &L) { return (const HGeoT<double> *)L.geo.p; }
+  static const HBasisT<double> &bas(HLevel &L) { return L.bas; }
+};
+template <>
+struct LevelData<float> {
+  static HWork<float> &work(HLevel &L) { return L.w32; }
+  static const float *dw(HLevel &L) { return L.dw32.p; }
+  static const float *sw(HLevel &L) { return L.sw32.p; }
+  static const float *dinv(HLevel &L) { return L.dinv32.p; }
+  static const HGeoT<float> *geo(HLevel &L) { return (const HGeoT<float> *)L.geo32.p; }
+  static const HBasisT<float> &bas(HLevel &L) { return L.bas32; }
+};
+
+// y = op x with op = K (stiff) or M; mode as k_h_scatter.  Uses the
+// level's work vectors of precision T (xd, yE).
+template <typename T>
+static void h_apply(HLevel &L, bool stiff, int nvec, const T *x, T *y, const T *b, int mode,
+                    cudaStream_t s) {
+  using D = LevelData<T>;
+  HWork<T> &W = D::work(L);
+  ensure_work(L, W, nvec, s);
+  const long long sz = sizeof(T);
+  if (L.ndep) {
+    prof_bytes((4 + sz) * L.dnnz + 4 * (L.ndep + 1) + sz * L.ndep * nvec);
+    launch(k_h_dep<T>, blocks_for(L.ndep * nvec, 256), 256, 0, s, L.ndep, nvec,
+           (const int *)L.dptr.p, (const int *)L.dconn.p, D::dw(L), x, W.xd.p);
+  }
+  const int npe = L.npe;
+  // compulsory: element connectivity and factors, node values once, slot
+  // values written
+  prof_bytes(4LL * L.ne * npe + 4 * sz * L.ne + sz * (L.nn + L.ndep) * nvec +
+             sz * L.ne * npe * nvec);
+  prof_flops((stiff ? 14LL : 6LL) * L.ne * npe * L.o * nvec);
+  unsigned g = blocks_for(L.ne, HM_THREADS);
+  const HGeoT<T> *geo = D::geo(L);
+  const int *ec = L.econn.p;
+  if (L.o == 2) {
+    if (stiff)
+      launch((k_h_elem<2, true, T>), g, HM_THREADS, 0, s, L.ne, nvec, ec, geo, x,
+             (const T *)W.xd.p, W.yE.p, D::bas(L));
+    else
+      launch((k_h_elem<2, false, T>), g, HM_THREADS, 0, s, L.ne, nvec, ec, geo, x,
+             (const T *)W.xd.p, W.yE.p, D::bas(L));
+  } else {
+    if (stiff)
+      launch((k_h_elem<3, true, T>), g, HM_THREADS, 0, s, L.ne, nvec, ec, geo, x,
+             (const T *)W.xd.p, W.yE.p, D::bas(L));
+    else
+      launch((k_h_elem<3, false, T>), g, HM_THREADS, 0, s, L.ne, nvec, ec, geo, x,
+             (const T *)W.xd.p, W.yE.p, D::bas(L));
+  }
+  prof_bytes((4 + sz) * L.snnz + 4 * (L.nn + 1) + sz * L.snnz * nvec +
+             sz * L.nn * nvec * (mode == 0 ? 1 : 2));
+  launch(k_h_scatter<T>, blocks_for(L.nn * nvec, 256), 256, 0, s, L.nn, nvec,
+         (const int *)L.srp.p, (const int *)L.sslot.p, D::sw(L), (const T *)W.yE.p, b, y,
+         mode);
+}
+
+// per-component dot products (a.b, c.d) into dev_out[0..2 nvec)
+static void h_dots(Helmholtz &H, long long n, int nvec, const double *a, const double *b,
+                   const double *c, const double *d, double *dev_out) {
+  cudaStream_t s = H.s;
+  prof_bytes(8LL * n * nvec * (c ? 4 : 2));
+  launch(k_h_dot2, HM_RED_BLOCKS, 256, 0, s, n, nvec, a, b, c, d, H.part.p);
+  launch(k_h_dot_final, 1, 64, 0, s, HM_RED_BLOCKS, nvec, (const double *)H.part.p, dev_out);
+}
+
+// Largest eigenvalue of the symmetric tridiagonal (alpha, beta) by
+// bisection on the Sturm sequence count.
+static double tridiag_max_eig(const std::vector<double> &al, const std::vector<double> &be) {
+  int m = (int)al.size();
+  double lo = 1e300, hi = -1e300;
+  for (int i = 0; i < m; i++) {
+    double r = (i > 0 ? std::fabs(be[i - 1]) : 0.0) + (i + 1 < m ? std::fabs(be[i]) : 0.0);
+    lo = std::min(lo, al[i] - r);
+    hi = std::max(hi, al[i] + r);
+  }
+  auto count_below = [&](double x) {
+    int c = 0;
+    double q = 1.0;
+    for (int i = 0; i < m; i++) {
+      double b2 = i > 0 ? be[i - 1] * be[i - 1] : 0.0;
+      q = al[i] - x - (i > 0 ? b2 / q : 0.0);
+      if (q == 0.0) q = 1e-300;
+      if (q < 0) c++;
+    }
+    return c;
+  };
+  for (int it = 0; it < 200 && hi - lo > 1e-12 * std::max(1.0, std::fabs(hi)); it++) {
+    double mid = 0.5 * (lo + hi);
+    if (count_below(mid) >= m)
+      hi = mid;
+    else
+      lo = mid;
+  }
+  return hi;
+}
+
+// lmax of D^-1 K by Lanczos on D^-1/2 K D^-1/2 (FP64).
+static void lanczos_lmax(Helmholtz &H, HLevel &L) {
+  cudaStream_t s = H.s;
+  const long long n = L.nn;
+  const int steps = (int)std::min<long long>(H.lanczos_steps, n);
+  DBuf<double> v(n, s), vp(n, s), w(n, s), u(n, s), dots(2 * HM_MAXVEC, s);
+  vp.zero();
+  launch(k_h_start, blocks_for(n, 256), 256, 0, s, n, v.p);
+  double h2[2];
+  h_dots(H, n, 1, v.p, v.p, nullptr, nullptr, dots.p);
+  TMRG_CUDA(cudaMemcpyAsync(h2, dots.p, sizeof(h2), cudaMemcpyDeviceToHost, s));
+  TMRG_CUDA(cudaStreamSynchronize(s));
+  launch(k_h_scale, blocks_for(n, 256), 256, 0, s, n, v.p, (const double *)v.p,
+         1.0 / std::sqrt(h2[0]));
+  std::vector<double> al, be;
+  double beta = 0.0;
+  for (int k = 0; k < steps; k++) {
+    launch(k_h_scale_sqrt, blocks_for(n, 256), 256, 0, s, n, (const double *)L.dinv.p,
+           (const double *)v.p, u.p);
+    h_apply<double>(L, true, 1, u.p, w.p, nullptr, 0, s);
+    launch(k_h_scale_sqrt, blocks_for(n, 256), 256, 0, s, n, (const double *)L.dinv.p,
+           (const double *)w.p, w.p);
+    h_dots(H, n, 1, w.p, v.p, nullptr, nullptr, dots.p);
+    TMRG_CUDA(cudaMemcpyAsync(h2, dots.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    TMRG_CUDA(cudaStreamSynchronize(s));
+    double alpha = h2[0];
+    al.push_back(alpha);
+    launch(k_h_lanczos_orth, blocks_for(n, 256), 256, 0, s, n, w.p, (const double *)v.p,
+           (const double *)vp.p, alpha, beta);
+    h_dots(H, n, 1, w.p, w.p, nullptr, nullptr, dots.p);
+    TMRG_CUDA(cudaMemcpyAsync(h2, dots.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    TMRG_CUDA(cudaStreamSynchronize(s));
+    beta = std::sqrt(std::max(h2[0], 0.0));
+    if (k + 1 == steps || beta <= 1e-14 * std::fabs(alpha)) break;
+    be.push_back(beta);
+    vp.swap(v);
+    launch(k_h_scale, blocks_for(n, 256), 256, 0, s, n, v.p, (const double *)w.p, 1.0 / beta);
+  }
+  be.resize(al.empty() ? 0 : al.size() - 1);
+  double lm = tridiag_max_eig(al, be);
+  L.lmax = H.cheb_upper * lm;
+  L.lmin = H.cheb_lower * lm;
+  // the FP64 work vectors of coarse levels are not needed after this
+  L.w64 = HWork<double>();
+}
+
+// Chebyshev smoothing of level L in FP32: on entry r = b - A x (zero: x = 0
+// and r = rin = b); keeps r = b - A x on exit when keep_r.
+static void chebyshev(Helmholtz &H, HLevel &L, int nvec, const float *rin, bool zero,
+                      bool keep_r) {
+  cudaStream_t s = H.s;
+  HWork<float> &W = L.w32;
+  const long long n = L.nn;
+  const unsigned g = blocks_for(n * nvec, 256);
+  const double theta = 0.5 * (L.lmax + L.lmin), delta = 0.5 * (L.lmax - L.lmin);
+  const double sigma = theta / delta;
+  double rho = 1.0 / sigma;
+  prof_bytes(4LL * n * nvec * 4 + 4LL * n);
+  launch(k_h_cheb_first<float>, g, 256, 0, s, n, nvec, (const float *)L.dinv32.p, rin, W.r.p,
+         W.d.p, W.x.p, (float)(1.0 / theta), zero ? 1 : 0);
+  for (int k = 1; k < L.degree; k++) {
+    h_apply<float>(L, true, nvec, W.d.p, W.r.p, nullptr, 2, s);
+    double rn = 1.0 / (2.0 * sigma - rho);
+    prof_bytes(4LL * n * nvec * 5 + 4LL * n);
+    launch(k_h_cheb_step<float>, g, 256, 0, s, n, nvec, (const float *)L.dinv32.p,
+           (const float *)W.r.p, W.d.p, W.x.p, (float)(rn * rho), (float)(2.0 * rn / delta));
+    rho = rn;
+  }
+  if (keep_r) h_apply<float>(L, true, nvec, W.d.p, W.r.p, nullptr, 2, s);
+}
+
+static void p_apply32(Helmholtz &H, int k, bool transpose, int nvec, const float *x, float *y) {
+  Interp &I = *H.P[k];
+  HInterp32 &F = *H.P32[k];
+  const long long nout = transpose ? I.cols : I.rows;
+  prof_bytes(8LL * I.nnz_nz + 4 * (nout + 1) + 4LL * nvec * (I.rows + I.cols));
+  if (transpose)
+    launch(k_h_csr<float>, blocks_for(nout * nvec, 256), 256, 0, H.s, nout, nvec,
+           (const int *)I.t_rowptr.p, (const int *)I.t_colidx.p, (const float *)F.pt.p, x, y);
+  else
+    launch(k_h_csr<float>, blocks_for(nout * nvec, 256), 256, 0, H.s, nout, nvec,
+           I.ap_rowptr(), I.ap_colidx(), (const float *)F.p.p, x, y);
+}
+
+// x_k = B_k b in FP32 (one V-cycle from a zero guess); the result is left
+// in level k's w32.x.
+static void vcycle(Helmholtz &H, int k, int nvec, const float *b) {
+  cudaStream_t s = H.s;
+  HLevel &L = *H.L[k];
+  HWork<float> &W = L.w32;
+  const long long n = L.nn;
+  if (k == H.nlevels - 1) {
+    if (H.dense) {
+      prof_bytes(4LL * n * n + 8LL * n * nvec);
+      launch(k_h_dense_mv<float>, blocks_for(n * nvec * 32, 256), 256, 0, s, n, nvec,
+             (const float *)H.Ainv32.p, b, W.x.p);
+    } else {
+      chebyshev(H, L, nvec, b, true, false);
+      for (int it = 1; it < H.coarse_sweeps; it++) {
+        h_apply<float>(L, true, nvec, W.x.p, W.r.p, b, 1, s);
+        chebyshev(H, L, nvec, W.r.p, false, false);
+      }
+    }
+    return;
+  }
+  HLevel &C = *H.L[k + 1];
+  chebyshev(H, L, nvec, b, true, true);
+  p_apply32(H, k, true, nvec, W.r.p, C.w32.b.p);
+  vcycle(H, k + 1, nvec, C.w32.b.p);
+  p_apply32(H, k, false, nvec, C.w32.x.p, W.t.p);
+  prof_bytes(12LL * n * nvec);
+  launch(k_h_add<float>, blocks_for(n * nvec, 256), 256, 0, s, n * nvec, W.x.p,
+         (const float *)W.t.p);
+  h_apply<float>(L, true, nvec, W.x.p, W.r.p, b, 1, s);
+  chebyshev(H, L, nvec, W.r.p, false, false);
+}
+
+// z = B r: r (FP64) to FP32, V-cycle, result back to FP64.
+static void precondition(Helmholtz &H, int nvec, const double *r, double *z) {
+  HLevel &L = *H.L[0];
+  const long long len = L.nn * nvec;
+  prof_bytes(12LL * len);
+  launch((k_h_cvt<double, float>), blocks_for(len, 256), 256, 0, H.s, len, r, L.w32.b.p);
+  vcycle(H, 0, nvec, L.w32.b.p);
+  prof_bytes(12LL * len);
+  launch((k_h_cvt<float, double>), blocks_for(len, 256), 256, 0, H.s, len,
+         (const float *)L.w32.x.p, z);
+}
+
+// Solve K x = b on the finest level (all components), flexible PCG with
+// the FP32 V-cycle; x and b are nvec-interleaved FP64 device vectors.
+static void solve(Helmholtz &H, int nvec, const double *b, double *x) {
+  cudaStream_t s = H.s;
+  HLevel &L = *H.L[0];
+  const long long n = L.nn;
+  const long long len = n * nvec;
+  const unsigned g = blocks_for(len, 256);
+  for (auto &lv : H.L) ensure_work(*lv, lv->w32, nvec, s);
+  for (DBuf<double> *v : {&H.cg_r, &H.cg_p, &H.cg_q, &H.cg_z, &H.cg_zo}) ensure(*v, len, s);
+  TMRG_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * len, s));
+  TMRG_CUDA(cudaMemcpyAsync(H.cg_r.p, b, sizeof(double) * len, cudaMemcpyDeviceToDevice, s));
+  // thresholds from |b|
+  std::vector<double> hd(2 * nvec), hsc(8 * nvec, 0.0);
+  h_dots(H, n, nvec, b, b, nullptr, nullptr, H.dots.p);
+  TMRG_CUDA(cudaMemcpyAsync(hd.data(), H.dots.p, sizeof(double) * 2 * nvec,
+                            cudaMemcpyDeviceToHost, s));
+  TMRG_CUDA(cudaStreamSynchronize(s));
+  std::vector<double> thr2(nvec);
+  std::vector<int> done(nvec, 0);
+  bool all_done = true;
+  H.last_res.assign(nvec, 0.0);
+  for (int v = 0; v < nvec; v++) {
+    double t = std::max(H.rtol * std::sqrt(hd[v]), H.atol);
+    thr2[v] = t * t;
+    hsc[8 * v + 5] = thr2[v];
+    H.last_res[v] = std::sqrt(hd[v]);
+    done[v] = hd[v] <= thr2[v];
+    hsc[8 * v + 4] = done[v] ? 1.0 : 0.0;
+    all_done = all_done && done[v];
+  }
+  H.last_iters = 0;
+  if (all_done) return;
+  TMRG_CUDA(cudaMemcpyAsync(H.sc.p, hsc.data(), sizeof(double) * 8 * nvec,
+                            cudaMemcpyHostToDevice, s));
+  // z = B r ; p = z ; rz = r.z
+  precondition(H, nvec, H.cg_r.p, H.cg_z.p);
+  TMRG_CUDA(cudaMemcpyAsync(H.cg_p.p, H.cg_z.p, sizeof(double) * len, cudaMemcpyDeviceToDevice,
+                            s));
+  TMRG_CUDA(cudaMemsetAsync(H.cg_zo.p, 0, sizeof(double) * len, s));
+  h_dots(H, n, nvec, H.cg_r.p, H.cg_z.p, H.cg_r.p, H.cg_zo.p, H.dots.p);
+  launch(k_h_cg_beta, 1, 32, 0, s, nvec, (const double *)H.dots.p, H.sc.p);
+  for (int it = 1; it <= H.max_iters; it++) {
+    h_apply<double>(L, true, nvec, H.cg_p.p, H.cg_q.p, nullptr, 0, s);
+    h_dots(H, n, nvec, H.cg_p.p, H.cg_q.p, nullptr, nullptr, H.dots.p);
+    launch(k_h_cg_alpha, 1, 32, 0, s, nvec, (const double *)H.dots.p, H.sc.p);
+    prof_bytes(8LL * len * 6);
+    launch(k_h_cg_update, g, 256, 0, s, n, nvec, (const double *)H.sc.p,
+           (const double *)H.cg_p.p, (const double *)H.cg_q.p, x, H.cg_r.p);
+    h_dots(H, n, nvec, H.cg_r.p, H.cg_r.p, nullptr, nullptr, H.dots.p);
+    launch(k_h_cg_check, 1, 32, 0, s, nvec, (const double *)H.dots.p, H.sc.p);
+    TMRG_CUDA(cudaMemcpyAsync(hd.data(), H.dots.p, sizeof(double) * nvec,
+                              cudaMemcpyDeviceToHost, s));
+    TMRG_CUDA(cudaStreamSynchronize(s));
+    H.last_iters = it;
+    bool fin = true;
+    for (int v = 0; v < nvec; v++) {
+      if (!done[v]) {
+        H.last_res[v] = std::sqrt(std::max(hd[v], 0.0));
+        if (hd[v] <= thr2[v]) done[v] = 1;
+      }
+      fin = fin && done[v];
+    }
+    if (fin) break;
+    H.cg_zo.swap(H.cg_z);
+    precondition(H, nvec, H.cg_r.p, H.cg_z.p);
+    h_dots(H, n, nvec, H.cg_r.p, H.cg_z.p, H.cg_r.p, H.cg_zo.p, H.dots.p);
+    launch(k_h_cg_beta, 1, 32, 0, s, nvec, (const double *)H.dots.p, H.sc.p);
+    prof_bytes(8LL * len * 3);
+    launch(k_h_cg_dir, g, 256, 0, s, n, nvec, (const double *)H.sc.p,
+           (const double *)H.cg_z.p, H.cg_p.p);
+  }
+}
+
+// ---------------------------------------------------------------------
+static void build_level(Helmholtz &H, Forest &f, HLevel &L) {
+  cudaStream_t s = H.s;
+  if (!f.have_nodes) forest_create_nodes(f);
+  if (f.order != 2 && f.order != 3)
+    throw Error(TMRG_ERR_UNSUPPORTED, "Helmholtz filter: forest order must be 2 or 3");
+  if (!f.conn || f.conn->boxes.empty())
+    throw Error(TMRG_ERR_ARG,
+                "Helmholtz filter: the forest has no geometry (set the block boxes)");
+  L.o = f.order;
+  L.npe = f.order * f.order * f.order;
+  L.degree = L.o == 2 ? 3 : 6;
+  make_basis(L.o, L.bas);
+  L.bas32.o = L.o;
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++) {
+      L.bas32.M[a][b] = (float)L.bas.M[a][b];
+      L.bas32.K[a][b] = (float)L.bas.K[a][b];
+    }
+  L.ne = f.n;
+  L.nn = f.num_owned;
+  L.ndep = f.num_dep;
+  L.dnnz = f.dep_nnz;
+  if (L.ne * L.npe >= (1LL << 31))
+    throw Error(TMRG_ERR_ARG, "Helmholtz filter: too many element slots");
+  const long long nslot = L.ne * L.npe;
+  L.econn.alloc(std::max(1LL, nslot), s);
+  TMRG_CUDA(cudaMemcpyAsync(L.econn.p, f.econn.p, sizeof(int) * nslot,
+                            cudaMemcpyDeviceToDevice, s));
+  L.dptr.alloc(L.ndep + 1, s);
+  L.dconn.alloc(std::max(1LL, L.dnnz), s);
+  L.dw.alloc(std::max(1LL, L.dnnz), s);
+  L.dw32.alloc(std::max(1LL, L.dnnz), s);
+  if (L.ndep) {
+    TMRG_CUDA(cudaMemcpyAsync(L.dptr.p, f.dep_ptr.p, sizeof(int) * (L.ndep + 1),
+                              cudaMemcpyDeviceToDevice, s));
+    TMRG_CUDA(cudaMemcpyAsync(L.dconn.p, f.dep_conn.p, sizeof(int) * L.dnnz,
+                              cudaMemcpyDeviceToDevice, s));
+    TMRG_CUDA(cudaMemcpyAsync(L.dw.p, f.dep_w.p, sizeof(double) * L.dnnz,
+                              cudaMemcpyDeviceToDevice, s));
+    launch((k_h_cvt<double, float>), blocks_for(L.dnnz, 256), 256, 0, s, L.dnnz,
+           (const double *)L.dw.p, L.dw32.p);
+  } else {
+    L.dptr.zero();
+  }
+  L.geo.alloc(4 * std::max(1LL, L.ne), s);
+  L.geo32.alloc(4 * std::max(1LL, L.ne), s);
+  launch(k_h_geom, blocks_for(L.ne, 256), 256, 0, s, L.ne, (const int *)f.block.p,
+         (const int16_t *)f.level.p, (const double *)f.conn->d_boxes.p, H.r * H.r,
+         (HGeoT<double> *)L.geo.p, (HGeoT<float> *)L.geo32.p);
+  // scatter list
+  DBuf<unsigned> cnt(nslot + 1, s);
+  launch(k_h_scount, blocks_for(nslot, 256), 256, 0, s, nslot, (const int *)L.econn.p,
+         (const int *)L.dptr.p, cnt.p);
+  exclusive_scan<unsigned>(cnt.p, cnt.p, nslot, s);
+  const long long E = read_scalar(cnt.p + nslot, s);
+  L.snnz = E;
+  DBuf<uint64_t> keys(std::max(1LL, E), s);
+  DBuf<uint32_t> pay(std::max(1LL, E), s);
+  DBuf<int> eslot(std::max(1LL, E), s);
+  DBuf<double> ew(std::max(1LL, E), s);
+  launch(k_h_sfill, blocks_for(nslot, 256), 256, 0, s, nslot, L.ne, L.npe,
+         (const int *)L.econn.p, (const int *)L.dptr.p, (const int *)L.dconn.p,
+         (const double *)L.dw.p, (const unsigned *)cnt.p, keys.p, pay.p, eslot.p, ew.p);
+  cnt.release();
+  radix_sort(keys, &pay, E, bits_for(L.nn + 1), s);
+  L.sslot.alloc(std::max(1LL, E), s);
+  L.sw.alloc(std::max(1LL, E), s);
+  L.sw32.alloc(std::max(1LL, E), s);
+  launch(k_h_sfinish, blocks_for(E, 256), 256, 0, s, E, (const uint32_t *)pay.p,
+         (const int *)eslot.p, (const double *)ew.p, L.sslot.p, L.sw.p, L.sw32.p);
+  L.srp.alloc(L.nn + 1, s);
+  launch(k_h_srowptr, blocks_for(L.nn + 1, 256), 256, 0, s, L.nn, E, (const uint64_t *)keys.p,
+         L.srp.p);
+  keys.release();
+  pay.release();
+  eslot.release();
+  ew.release();
+  DBuf<int> err(1, s);
+  err.zero();
+  L.dinv.alloc(std::max(1LL, L.nn), s);
+  L.dinv32.alloc(std::max(1LL, L.nn), s);
+  launch(k_h_diag, blocks_for(L.nn, 128), 128, 0, s, L.nn, L.ne, L.o, L.bas,
+         (const int *)L.srp.p, (const int *)L.sslot.p, (const double *)L.sw.p,
+         (const HGeoT<double> *)L.geo.p, L.dinv.p, L.dinv32.p, err.p);
+  if (read_scalar(err.p, s))
+    throw Error(TMRG_ERR_ARG, "Helmholtz filter: a node has a non-positive diagonal "
+                              "(degenerate element geometry)");
+}
+
+void helmholtz_create(Forest *const *forests, int nlevels, double r, Helmholtz &H) {
+  Stage st("tmrg_helmholtz_create");
+  if (nlevels < 1) throw Error(TMRG_ERR_ARG, "Helmholtz filter: no forests");
+  H.s = forests[0]->s;
+  H.r = r;
+  H.nlevels = nlevels;
+  cudaStream_t s = H.s;
+  H.part.alloc((size_t)HM_RED_BLOCKS * 2 * HM_MAXVEC, s);
+  H.dots.alloc(2 * HM_MAXVEC, s);
+  H.sc.alloc(8 * HM_MAXVEC, s);
+  for (int k = 0; k < nlevels; k++) {
+    H.L.emplace_back(new HLevel);
+    build_level(H, *forests[k], *H.L.back());
+  }
+  for (int k = 0; k + 1 < nlevels; k++) {
+    H.P.emplace_back(new Interp);
+    Interp &I = *H.P.back();
+    interp_create(*forests[k], *forests[k + 1], I);
+    I.s = s;
+    if (I.rows != H.L[k]->nn || I.cols != H.L[k + 1]->nn)
+      throw Error(TMRG_ERR_INTERNAL, "Helmholtz filter: interpolation size mismatch");
+    H.P32.emplace_back(new HInterp32);
+    HInterp32 &F = *H.P32.back();
+    F.p.alloc(std::max(1LL, I.nnz_nz), s);
+    F.pt.alloc(std::max(1LL, I.nnz_nz), s);
+    launch((k_h_cvt<double, float>), blocks_for(I.nnz_nz, 256), 256, 0, s, I.nnz_nz,
+           I.ap_vals(), F.p.p);
+    launch((k_h_cvt<double, float>), blocks_for(I.nnz_nz, 256), 256, 0, s, I.nnz_nz,
+           (const double *)I.t_vals.p, F.pt.p);
+  }
+  // coarsest level
+  HLevel &C = *H.L.back();
+  H.nc = C.nn;
+  H.dense = C.nn <= HM_DENSE_MAX;
+  if (H.dense) {
+    const long long n = C.nn;
+    DBuf<double> A(std::max(1LL, n * n), s);
+    A.zero();
+    launch(k_h_dense, blocks_for(n, 64), 64, 0, s, n, C.ne, C.o, C.bas, (const int *)C.srp.p,
+           (const int *)C.sslot.p, (const double *)C.sw.p, (const int *)C.econn.p,
+           (const int *)C.dptr.p, (const int *)C.dconn.p, (const double *)C.dw.p,
+           (const HGeoT<double> *)C.geo.p, A.p);
+    DBuf<double> rowk(std::max(1LL, n), s), colk(std::max(1LL, n), s);
+    for (long long k = 0; k < n; k++) {
+      launch(k_h_gj_copy, blocks_for(n, 256), 256, 0, s, n, (const double *)A.p, k, rowk.p,
+             colk.p);
+      launch(k_h_gj_update, dim3(blocks_for(n, 256), (unsigned)n), 256, 0, s, n, A.p, k,
+             (const double *)rowk.p, (const double *)colk.p);
+    }
+    H.Ainv32.alloc(std::max(1LL, n * n), s);
+    launch((k_h_cvt<double, float>), blocks_for(n * n, 256), 256, 0, s, n * n,
+           (const double *)A.p, H.Ainv32.p);
+  }
+  for (int k = 0; k < nlevels; k++)
+    if (!(H.dense && k == nlevels - 1)) lanczos_lmax(H, *H.L[k]);
+  TMRG_CUDA(cudaStreamSynchronize(s));
+}
+
+void helmholtz_apply(Helmholtz &H, bool transpose, int vpn, const double *in, double *out) {
+  Stage st(transpose ? "tmrg_helmholtz_apply_transpose" : "tmrg_helmholtz_apply");
+  if (vpn < 1 || vpn > HM_MAXVEC)
+    throw Error(TMRG_ERR_ARG, "Helmholtz filter: vars per node must be 1.." +
+                                  std::to_string(HM_MAXVEC));
+  cudaStream_t s = H.s;
+  HLevel &L = *H.L[0];
+  const long long len = L.nn * vpn;
+  if (len == 0) return;
+  ensure(H.rhs, len, s);
+  if (!transpose) {
+    // rhs = M x, psi = K^-1 rhs
+    h_apply<double>(L, false, vpn, in, H.rhs.p, nullptr, 0, s);
+    solve(H, vpn, H.rhs.p, out);
+  } else {
+    // psi = K^-1 x, out = M psi
+    ensure(H.psi, len, s);
+    solve(H, vpn, in, H.psi.p);
+    h_apply<double>(L, false, vpn, H.psi.p, out, nullptr, 0, s);
+  }
+}
+
+void helmholtz_operator(Helmholtz &H, int level, bool stiff, int nvec, const double *in,
+                        double *out) {
+  if (level < 0 || level >= H.nlevels) throw Error(TMRG_ERR_ARG, "level out of range");
+  if (nvec < 1 || nvec > HM_MAXVEC) throw Error(TMRG_ERR_ARG, "nvec out of range");
+  h_apply<double>(*H.L[level], stiff, nvec, in, out, nullptr, 0, H.s);
+}
+
+}  // namespace tmrg
