@@ -60,10 +60,11 @@ def parse():
                    help="smaller variant of the workload for ncu captures")
     p.add_argument("--passes", type=int, default=None,
                    help="fewer refinement passes: a smaller case for ncu captures")
-    p.add_argument("--workload", default="c2", choices=["c2", "c4", "c5"],
+    p.add_argument("--workload", default="c2", choices=["c2", "c4", "c5", "helmholtz"],
                    help="c2: the multi-tree order-3 workload (default, the headline); "
                         "c4: 256 forests batched as one; "
-                        "c5: the 200M-octant adaptive workload (one JSON line of its own)")
+                        "c5: the 200M-octant adaptive workload (one JSON line of its own); "
+                        "helmholtz: the Helmholtz PDE filter on a 5-level filter hierarchy")
     a = p.parse_args()
     if a.passes is not None:
         WORKLOAD["passes"] = a.passes
@@ -530,11 +531,10 @@ FILTER_WORKLOAD = dict(name="brick16x8x8_16bumps_sigma0.05_order2_r2h_N10_vpn3",
                        target=20_000_000, max_level=9, vpn=3, N=10)
 
 
-def build_filter_chain(TMR, FW):
-    """The differentiable-filter configuration: a 16x8x8 brick refined near
-    16 seeded Gaussian bumps (sigma = 0.05 domain lengths) to ~20M octants
-    (order 2); the filter forest is its coarsened forest; P maps it to the
-    finest forest.  Returns (fine, coarse, interp, filter, r)."""
+def bump_forest(TMR, FW):
+    """A brick of FW's size refined near FW["bumps"] seeded Gaussian bumps
+    (sigma = FW["sigma"] domain lengths) to about FW["target"] octants,
+    order 2, balanced, nodes created."""
     import torch
 
     from tmr_gb300 import workloads as Wk
@@ -569,6 +569,15 @@ def build_filter_chain(TMR, FW):
         f.refine(flags, 0, FW["max_level"])
         f.balance(1)
     f.createNodes()
+    return f
+
+
+def build_filter_chain(TMR, FW):
+    """The differentiable-filter configuration: a 16x8x8 brick refined near
+    16 seeded Gaussian bumps (sigma = 0.05 domain lengths) to ~20M octants
+    (order 2); the filter forest is its coarsened forest; P maps it to the
+    finest forest.  Returns (fine, coarse, interp, filter, r)."""
+    f = bump_forest(TMR, FW)
     coarse = f.coarsen()
     coarse.balance(1)
     coarse.createNodes()
@@ -578,6 +587,185 @@ def build_filter_chain(TMR, FW):
     r = 2.0 * hmin
     F = TMR.MatrixFilter(r, FW["N"], None, [coarse], block_len=1.0, vpn=FW["vpn"])
     return f, coarse, I, F, r
+
+
+# ---------------------------------------------------------------------------
+# The Helmholtz PDE filter configuration: the filter forest of the bump
+# workload (the coarsened ~20M-octant analysis forest) and four more
+# coarsened levels; unit-cube block boxes; r = 2 x the finest element side;
+# one step = applyFilter + applyTranspose on vpn design components.
+HELMHOLTZ_WORKLOAD = dict(name="brick16x8x8_16bumps_20M_filter-forest_order2_5lvl_r2h_vpn1",
+                          nx=16, ny=8, nz=8, L0=2, bumps=16, seed=3, sigma=0.05,
+                          target=20_000_000, max_level=9, levels=5, vpn=1,
+                          cpu_sample=dict(nx=4, ny=2, nz=2, L0=2, bumps=4, seed=3,
+                                          sigma=0.05, target=25_000, max_level=7))
+
+
+def helmholtz_setup(TMR, HW):
+    f = bump_forest(TMR, HW)
+    filters = [f.coarsen()]
+    filters[0].balance(1)
+    filters[0].createNodes()
+    for _ in range(HW["levels"] - 1):
+        c = filters[-1].coarsen()
+        c.balance(1)
+        c.createNodes()
+        filters.append(c)
+    nx, ny, nz = HW["nx"], HW["ny"], HW["nz"]
+    boxes = np.array([[i, j, k, 1.0, 1.0, 1.0] for k in range(nz) for j in range(ny)
+                      for i in range(nx)], np.float64)
+    for c in filters:
+        c.setBlockBoxes(boxes)
+    hmin = 1.0 / 2.0 ** int(filters[0].getOctantsDevice()["level"].max().item())
+    return f, filters, boxes, 2.0 * hmin
+
+
+def helmholtz_cpu_baseline(HW):
+    """The oracle (scipy sparse direct solve of the assembled K, M) on a
+    bounded sample of the same kind of forest; filtered nodes per second of
+    the solve alone (assembly excluded), one core."""
+    import time
+
+    from oracle import helmholtz as HO
+    from oracle.oracle import OracleForest
+    from tmr_gb300 import workloads as Wk
+    S = HW["cpu_sample"]
+    nx, ny, nz = S["nx"], S["ny"], S["nz"]
+    f = OracleForest(2, 1)
+    f.setConnectivity(Wk.brick(nx, ny, nz))
+    f.createTrees(S["L0"])
+    cen = Wk.uniform(S["seed"], 0, 3 * S["bumps"]).reshape(-1, 3) * np.array([nx, ny, nz])
+    sig = S["sigma"] * np.array([nx, ny, nz])
+    for _ in range(12):
+        o = f.getOctants()
+        if len(o) >= S["target"]:
+            break
+        h = 2.0 ** (30 - o[:, 5])
+        c = np.stack([o[:, 0] % nx, (o[:, 0] // nx) % ny, o[:, 0] // (nx * ny)], 1) + \
+            (o[:, 1:4] + 0.5 * h[:, None]) / 2.0 ** 30
+        val = sum(np.exp(-0.5 * (((c - cen[k]) / sig) ** 2).sum(1)) for k in range(len(cen)))
+        val[o[:, 5] >= S["max_level"]] = -1.0
+        k = int(min(len(o), max(1, (S["target"] - len(o)) / 7 / 1.3)))
+        thr = np.sort(val)[-k]
+        f.refine(((val >= thr) & (val > 0)).astype(np.intc), 0, S["max_level"])
+        f.balance(1)
+    f.createNodes()
+    n = f.nodeSizes()["num_owned"]
+    dp, dc, dw = f.getDepNodeConn()
+    boxes = np.array([[i, j, k, 1.0, 1.0, 1.0] for k in range(nz) for j in range(ny)
+                      for i in range(nx)], np.float64)
+    hmin = 1.0 / 2.0 ** int(f.getOctants()[:, 5].max())
+    K, M = HO.assemble(f.getOctants(), f.getMeshConn(2), dp, dc, dw, n, 2, [-1.0, 1.0],
+                       boxes, 2.0 * hmin)
+    import scipy.sparse.linalg as sla
+    x = np.random.default_rng(0).uniform(0.0, 1.0, n)
+    t = time.perf_counter()
+    lu = sla.splu(K.tocsc())
+    lu.solve(M @ x)
+    M @ lu.solve(x)
+    dt = time.perf_counter() - t
+    return {"value": 2 * n / dt, "unit": "filtered nodes/s", "cores": 1, "kind": "port",
+            "sample": "oracle scipy sparse LU of the Helmholtz matrix and two solves "
+                      "(forward + adjoint) on a %dx%dx%d brick refined near %d bumps (%d "
+                      "octants, %d nodes), assembly excluded" % (
+                          nx, ny, nz, S["bumps"], len(f.getOctants()), n)}
+
+
+def run_helmholtz(args):
+    """One JSON line for the Helmholtz filter configuration."""
+    import time
+
+    import torch
+    from tmr_gb300 import TMR
+    from tmr_gb300 import build as tb
+    tb.build()
+    HW = HELMHOLTZ_WORKLOAD
+    f, filters, boxes, r = helmholtz_setup(TMR, HW)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    H = TMR.HelmholtzFilter(r, None, filters, vpn=HW["vpn"])
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    sizes = H.sizes()
+    n = int(sizes[0][0])
+    vpn = HW["vpn"]
+    g = torch.Generator(device="cuda").manual_seed(HW["seed"])
+    x = torch.rand(n * vpn, dtype=torch.float64, device="cuda", generator=g)
+    w = torch.rand(n * vpn, dtype=torch.float64, device="cuda", generator=g)
+    rho, gx = torch.empty_like(x), torch.empty_like(x)
+    iters = []
+
+    def step():
+        H.applyFilter(x, rho)
+        iters.append(H.lastSolve()[0])
+        H.applyTranspose(w, gx)
+        iters.append(H.lastSolve()[0])
+    for _ in range(args.warmup):
+        step()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    tot = 0.0
+    iters.clear()
+    lc0 = TMR.kernel_launch_count()
+    for _ in range(args.steps):
+        flush.zero_()
+        e0.record()
+        step()
+        e1.record()
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1)
+    launches = (TMR.kernel_launch_count() - lc0) // args.steps
+    ms = tot / args.steps
+    # per-kernel profile of one step: the dominant kernel's roofline
+    L = TMR.lib()
+    L.tmrg_profile_begin()
+    step()
+    buf = ctypes.create_string_buffer(1 << 20)
+    L.tmrg_profile_end(buf, len(buf))
+    prof = json.loads(buf.value.decode())
+    # kernels keyed by their full launch name (precision and order kept apart)
+    fam = {k.strip("()"): v for k, v in prof.items()}
+    tot_ms = sum(v[1] for v in fam.values())
+    top = max(fam.items(), key=lambda kv: kv[1][1])
+    peak, peak_kind = measured_peaks()
+    fp64 = ctypes.c_double(0.0)
+    L.tmrg_measure_fp64_peak(ctypes.byref(fp64))
+    roof = roofline_entry(top[0], top[1], peak, peak_kind, fp64.value, tot_ms)
+    shares = {k: round(v[1] / tot_ms, 4) for k, v in sorted(fam.items(), key=lambda kv: -kv[1][1])[:8]}
+    # end to end through the host API: host vectors in, host vectors out
+    xh = x.cpu().numpy()
+    wh = w.cpu().numpy()
+    rh, gh = np.zeros_like(xh), np.zeros_like(wh)
+    H.applyFilter(xh, rh)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        H.applyFilter(xh, rh)
+        H.applyTranspose(wh, gh)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    err = float(np.abs(rh - rho.cpu().numpy()).max() / np.abs(rho.cpu().numpy()).max())
+    line = {"metric": "Helmholtz-filtered design nodes/s (forward + adjoint)",
+            "value": 2 * n * vpn / (ms / 1e3), "unit": "nodes/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 (Krylov) + f32 (multigrid preconditioner)",
+            "data": "synthetic (seeded)",
+            "config": {"workload": HW["name"], "analysis_octants": f.getNumOctants(),
+                       "levels": [{"nodes": int(a), "elements": int(b), "dependent": int(c)}
+                                  for a, b, c in sizes],
+                       "r": r, "vpn": vpn, "l2": "flushed (256 MiB write) before each step"},
+            "solver_iterations": iters, "setup_s": setup_s, "gpu_launches": launches,
+            "roofline": {k: roof[k] for k in ("bound", "achieved", "peak", "unit", "frac",
+                                              "traffic")},
+            "top_kernel": roof, "kernel_shares": shares,
+            "e2e": {"value": 2 * n * vpn / e2e_s, "unit": "nodes/s",
+                    "h2d_bytes_per_step": 2 * 8 * n * vpn,
+                    "d2h_bytes_per_step": 2 * 8 * n * vpn},
+            "e2e_vs_device_rel_err": err}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = helmholtz_cpu_baseline(HW)
+    print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -990,6 +1178,8 @@ def main():
         run_c5(args)
     elif args.workload == "c4":
         run_c4(args)
+    elif args.workload == "helmholtz":
+        run_helmholtz(args)
     else:
         run_gpu(args)
 

@@ -344,6 +344,16 @@ int tmrg_helmholtz_apply_transpose_device(tmrg_helmholtz *H, int vpn,
    defaults): a component stops when |r| <= max(rtol |b|, atol). */
 int tmrg_helmholtz_set_tolerances(tmrg_helmholtz *H, double rtol, double atol,
                                   int max_iters);
+/* Multigrid smoother of the preconditioner: Chebyshev polynomials of
+   degree `degree_order2` over [lower_order2, upper] x lam on order-2
+   levels and `degree_order3` over [lower_order3, upper] x lam on order-3
+   levels, lam the Lanczos estimate of the largest eigenvalue of D^-1 K.
+   Defaults 5, 6, 0.05, 0.1, 1.1.  The reference's TACS multigrid uses
+   symmetric SOR or, optionally, degree-3 Chebyshev over [1/30, 1.1]
+   (TMR_RefinementTools.cpp:44-50); the smoother changes only the iteration
+   count, not the converged result. */
+int tmrg_helmholtz_set_smoother(tmrg_helmholtz *H, int degree_order2, int degree_order3,
+                                double lower_order2, double lower_order3, double upper);
 /* Iterations and final residual norms (one per component, at most `n`)
    of the last solve. */
 int tmrg_helmholtz_last_solve(tmrg_helmholtz *H, int *iters, double *res, int n);

@@ -715,6 +715,14 @@ class HelmholtzFilter(ConformFilter):
         call("tmrg_helmholtz_set_tolerances", self.ptr, float(rtol), float(atol),
              int(max_iters))
 
+    def setSmoother(self, degree_order2=5, degree_order3=6, lower_order2=0.05,
+                    lower_order3=0.1, upper=1.1):
+        """Chebyshev smoother of the multigrid preconditioner (degree and
+        interval, as fractions of the largest eigenvalue estimate of
+        D^-1 K, per level order); changes the iteration count only."""
+        call("tmrg_helmholtz_set_smoother", self.ptr, int(degree_order2), int(degree_order3),
+             float(lower_order2), float(lower_order3), float(upper))
+
     def lastSolve(self):
         """(iterations, residual norm per component) of the last solve."""
         it = ctypes.c_int(0)

@@ -100,6 +100,7 @@ _SIGS = {
     "tmrg_helmholtz_apply_transpose_device": [c_vp, c_int, c_vp, c_vp],
     "tmrg_helmholtz_set_tolerances": [c_vp, c_dbl, c_dbl, c_int],
     "tmrg_helmholtz_last_solve": [c_vp, c_vp, c_vp, c_int],
+    "tmrg_helmholtz_set_smoother": [c_vp, c_int, c_int, c_dbl, c_dbl, c_dbl],
     "tmrg_helmholtz_mult_device": [c_vp, c_int, c_int, c_int, c_vp, c_vp],
     "tmrg_random_refinement_device": [c_u64, c_u64, c_dbl, c_vp, c_i64, c_vp],
 }

@@ -1238,6 +1238,22 @@ int tmrg_helmholtz_set_tolerances(tmrg_helmholtz *H, double rtol, double atol,
     H->H.max_iters = max_iters;
   });
 }
+int tmrg_helmholtz_set_smoother(tmrg_helmholtz *H, int degree_order2, int degree_order3,
+                                double lower_order2, double lower_order3, double upper) {
+  return guarded([&] {
+    ARG(H && degree_order2 >= 1 && degree_order3 >= 1 && degree_order2 <= 64 &&
+            degree_order3 <= 64,
+        "bad smoother degree");
+    ARG(lower_order2 > 0.0 && lower_order3 > 0.0 && upper > lower_order2 &&
+            upper > lower_order3,
+        "bad smoother interval");
+    H->H.cheb_degree2 = degree_order2;
+    H->H.cheb_degree3 = degree_order3;
+    H->H.cheb_lower2 = lower_order2;
+    H->H.cheb_lower3 = lower_order3;
+    H->H.cheb_upper = upper;
+  });
+}
 int tmrg_helmholtz_last_solve(tmrg_helmholtz *H, int *iters, double *res, int n) {
   return guarded([&] {
     ARG(H, "NULL filter");

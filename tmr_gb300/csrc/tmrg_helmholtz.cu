@@ -29,9 +29,10 @@
 //   preconditioner is one multigrid V-cycle computed in FP32: GB300 runs
 //   FP32 at 64 times its FP64 rate, and the FP64 outer iteration still
 //   drives the true residual to the reference's tolerance.  The smoother is
-//   Chebyshev on D^-1 K over [0.1, 1.1] lmax (lmax from Lanczos; degree 3
-//   for order-2 levels, 6 for order 3), which is parallel where SOR is
-//   sequential.  Restriction and prolongation are the forests' own
+//   Chebyshev on D^-1 K over [lower, 1.1] lmax (lmax from Lanczos; degree
+//   5 and lower 0.05 for order-2 levels, degree 6 and lower 0.1 for order
+//   3, the settings that solved the measured filter hierarchies fastest),
+//   which is parallel where SOR is sequential.  Restriction and prolongation are the forests' own
 //   createInterpolation operators (P^T and P); coarse levels are
 //   rediscretised, as in the reference (use_galerkin = 0).  The coarsest
 //   level is solved with its explicit dense inverse (Gauss-Jordan on the
@@ -42,6 +43,7 @@
 #include <algorithm>
 #include <cmath>
 #include <string>
+#include <type_traits>
 
 #include "tmrg_helmholtz.h"
 
@@ -494,15 +496,19 @@ __global__ void __launch_bounds__(256)
     part[((long long)blockIdx.x * 2 + k) * nvec + v] = t;
   }
 }
-// out[k*nvec + v] = sum over blocks of part (k = 0, 1)
+// out[k*nvec + v] = sum over blocks of part (k = 0, 1): one warp per
+// output, lanes strided over the blocks, then a fixed shuffle tree.
 __global__ void k_h_dot_final(int nblocks, int nvec, const double *__restrict__ part,
                               double *out) {
-  int t = threadIdx.x;
-  if (t >= 2 * nvec) return;
-  int k = t / nvec, v = t % nvec;
-  double s = 0.0;
-  for (int b = 0; b < nblocks; b++) s += part[((long long)b * 2 + k) * nvec + v];
-  out[k * nvec + v] = s;
+  const int lane = threadIdx.x & 31;
+  for (int t = threadIdx.x >> 5; t < 2 * nvec; t += blockDim.x >> 5) {
+    int k = t / nvec, v = t % nvec;
+    double s = 0.0;
+    for (int b = lane; b < nblocks; b += 32) s += part[((long long)b * 2 + k) * nvec + v];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[k * nvec + v] = s;
+  }
 }
 
 // Conjugate-gradient scalars, per component v at sc[8v]: [0] r.z, [2]
@@ -621,40 +627,58 @@ static void h_apply(HLevel &L, bool stiff, int nvec, const T *x, T *y, const T *
   HWork<T> &W = D::work(L);
   ensure_work(L, W, nvec, s);
   const long long sz = sizeof(T);
+  // (kernels are named with their precision so that per-kernel profiles
+  // keep the FP64 and FP32 operators apart)
   if (L.ndep) {
     prof_bytes((4 + sz) * L.dnnz + 4 * (L.ndep + 1) + sz * L.ndep * nvec);
-    launch(k_h_dep<T>, blocks_for(L.ndep * nvec, 256), 256, 0, s, L.ndep, nvec,
-           (const int *)L.dptr.p, (const int *)L.dconn.p, D::dw(L), x, W.xd.p);
+    const unsigned gd = blocks_for(L.ndep * nvec, 256);
+    if constexpr (std::is_same<T, double>::value)
+      launch(k_h_dep<double>, gd, 256, 0, s, L.ndep, nvec, (const int *)L.dptr.p,
+             (const int *)L.dconn.p, D::dw(L), x, W.xd.p);
+    else
+      launch(k_h_dep<float>, gd, 256, 0, s, L.ndep, nvec, (const int *)L.dptr.p,
+             (const int *)L.dconn.p, D::dw(L), x, W.xd.p);
   }
   const int npe = L.npe;
   // compulsory: element connectivity and factors, node values once, slot
   // values written
   prof_bytes(4LL * L.ne * npe + 4 * sz * L.ne + sz * (L.nn + L.ndep) * nvec +
              sz * L.ne * npe * nvec);
-  prof_flops((stiff ? 14LL : 6LL) * L.ne * npe * L.o * nvec);
-  unsigned g = blocks_for(L.ne, HM_THREADS);
+  // FP64 operations of the sum factorisation (7 or 3 contractions of
+  // o^4 multiply-adds, x2 flops)
+  if constexpr (std::is_same<T, double>::value)
+    prof_flops((stiff ? 14LL : 6LL) * L.ne * npe * L.o * nvec);
+  const unsigned g = blocks_for(L.ne, HM_THREADS);
   const HGeoT<T> *geo = D::geo(L);
   const int *ec = L.econn.p;
-  if (L.o == 2) {
-    if (stiff)
-      launch((k_h_elem<2, true, T>), g, HM_THREADS, 0, s, L.ne, nvec, ec, geo, x,
-             (const T *)W.xd.p, W.yE.p, D::bas(L));
-    else
-      launch((k_h_elem<2, false, T>), g, HM_THREADS, 0, s, L.ne, nvec, ec, geo, x,
-             (const T *)W.xd.p, W.yE.p, D::bas(L));
+  const T *xd = W.xd.p;
+  T *yE = W.yE.p;
+#define H_ELEM(O, ST, TT)                                                                  \
+  launch((k_h_elem<O, ST, TT>), g, HM_THREADS, 0, s, L.ne, nvec, ec, geo, x, xd, yE, \
+         D::bas(L))
+  if constexpr (std::is_same<T, double>::value) {
+    if (L.o == 2) {
+      if (stiff) H_ELEM(2, true, double); else H_ELEM(2, false, double);
+    } else {
+      if (stiff) H_ELEM(3, true, double); else H_ELEM(3, false, double);
+    }
   } else {
-    if (stiff)
-      launch((k_h_elem<3, true, T>), g, HM_THREADS, 0, s, L.ne, nvec, ec, geo, x,
-             (const T *)W.xd.p, W.yE.p, D::bas(L));
-    else
-      launch((k_h_elem<3, false, T>), g, HM_THREADS, 0, s, L.ne, nvec, ec, geo, x,
-             (const T *)W.xd.p, W.yE.p, D::bas(L));
+    if (L.o == 2) {
+      if (stiff) H_ELEM(2, true, float); else H_ELEM(2, false, float);
+    } else {
+      if (stiff) H_ELEM(3, true, float); else H_ELEM(3, false, float);
+    }
   }
+#undef H_ELEM
   prof_bytes((4 + sz) * L.snnz + 4 * (L.nn + 1) + sz * L.snnz * nvec +
              sz * L.nn * nvec * (mode == 0 ? 1 : 2));
-  launch(k_h_scatter<T>, blocks_for(L.nn * nvec, 256), 256, 0, s, L.nn, nvec,
-         (const int *)L.srp.p, (const int *)L.sslot.p, D::sw(L), (const T *)W.yE.p, b, y,
-         mode);
+  const unsigned gs = blocks_for(L.nn * nvec, 256);
+  if constexpr (std::is_same<T, double>::value)
+    launch(k_h_scatter<double>, gs, 256, 0, s, L.nn, nvec, (const int *)L.srp.p,
+           (const int *)L.sslot.p, D::sw(L), (const T *)yE, b, y, mode);
+  else
+    launch(k_h_scatter<float>, gs, 256, 0, s, L.nn, nvec, (const int *)L.srp.p,
+           (const int *)L.sslot.p, D::sw(L), (const T *)yE, b, y, mode);
 }
 
 // per-component dot products (a.b, c.d) into dev_out[0..2 nvec)
@@ -663,7 +687,7 @@ static void h_dots(Helmholtz &H, long long n, int nvec, const double *a, const d
   cudaStream_t s = H.s;
   prof_bytes(8LL * n * nvec * (c ? 4 : 2));
   launch(k_h_dot2, HM_RED_BLOCKS, 256, 0, s, n, nvec, a, b, c, d, H.part.p);
-  launch(k_h_dot_final, 1, 64, 0, s, HM_RED_BLOCKS, nvec, (const double *)H.part.p, dev_out);
+  launch(k_h_dot_final, 1, 256, 0, s, HM_RED_BLOCKS, nvec, (const double *)H.part.p, dev_out);
 }
 
 // Largest eigenvalue of the symmetric tridiagonal (alpha, beta) by
@@ -736,9 +760,7 @@ static void lanczos_lmax(Helmholtz &H, HLevel &L) {
     launch(k_h_scale, blocks_for(n, 256), 256, 0, s, n, v.p, (const double *)w.p, 1.0 / beta);
   }
   be.resize(al.empty() ? 0 : al.size() - 1);
-  double lm = tridiag_max_eig(al, be);
-  L.lmax = H.cheb_upper * lm;
-  L.lmin = H.cheb_lower * lm;
+  L.lam = tridiag_max_eig(al, be);
   // the FP64 work vectors of coarse levels are not needed after this
   L.w64 = HWork<double>();
 }
@@ -751,13 +773,16 @@ static void chebyshev(Helmholtz &H, HLevel &L, int nvec, const float *rin, bool 
   HWork<float> &W = L.w32;
   const long long n = L.nn;
   const unsigned g = blocks_for(n * nvec, 256);
-  const double theta = 0.5 * (L.lmax + L.lmin), delta = 0.5 * (L.lmax - L.lmin);
+  const double lmax = H.cheb_upper * L.lam,
+               lmin = (L.o == 2 ? H.cheb_lower2 : H.cheb_lower3) * L.lam;
+  const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
   const double sigma = theta / delta;
   double rho = 1.0 / sigma;
   prof_bytes(4LL * n * nvec * 4 + 4LL * n);
   launch(k_h_cheb_first<float>, g, 256, 0, s, n, nvec, (const float *)L.dinv32.p, rin, W.r.p,
          W.d.p, W.x.p, (float)(1.0 / theta), zero ? 1 : 0);
-  for (int k = 1; k < L.degree; k++) {
+  const int degree = L.o == 2 ? H.cheb_degree2 : H.cheb_degree3;
+  for (int k = 1; k < degree; k++) {
     h_apply<float>(L, true, nvec, W.d.p, W.r.p, nullptr, 2, s);
     double rn = 1.0 / (2.0 * sigma - rho);
     prof_bytes(4LL * n * nvec * 5 + 4LL * n);
@@ -911,7 +936,6 @@ static void build_level(Helmholtz &H, Forest &f, HLevel &L) {
                 "Helmholtz filter: the forest has no geometry (set the block boxes)");
   L.o = f.order;
   L.npe = f.order * f.order * f.order;
-  L.degree = L.o == 2 ? 3 : 6;
   make_basis(L.o, L.bas);
   L.bas32.o = L.o;
   for (int a = 0; a < 3; a++)

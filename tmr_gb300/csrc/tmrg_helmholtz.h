@@ -35,8 +35,8 @@ struct HWork {
 
 // One level of the filter hierarchy: the forest's element connectivity
 // and dependent weights, per-element factors, the node-ordered scatter
-// list of element slots, the inverse Jacobi diagonal and the Chebyshev
-// smoother's interval and degree.  The operator data is held in FP64 (the
+// list of element slots, the inverse Jacobi diagonal and the largest
+// eigenvalue estimate the Chebyshev smoother scales its interval by.  The operator data is held in FP64 (the
 // Krylov iteration, the filter's mass products) and FP32 (the multigrid
 // preconditioner).
 struct HLevel {
@@ -47,8 +47,7 @@ struct HLevel {
   DBuf<int> econn, dptr, dconn, srp, sslot;
   DBuf<double> dw, geo, sw, dinv;
   DBuf<float> dw32, geo32, sw32, dinv32;
-  double lmin = 0.0, lmax = 0.0;
-  int degree = 3;
+  double lam = 0.0;  // Lanczos estimate of the largest eigenvalue of D^-1 K
   HWork<double> w64;
   HWork<float> w32;
 };
@@ -72,7 +71,10 @@ struct Helmholtz {
   // TMRHelmholtzFilter.cpp:95-101)
   double rtol = 1e-12, atol = 1e-30;
   int max_iters = 300;
-  double cheb_lower = 0.1, cheb_upper = 1.1;
+  // Chebyshev smoother: interval [lower, upper] x lam; degree and lower
+  // bound by level order
+  double cheb_lower2 = 0.05, cheb_lower3 = 0.1, cheb_upper = 1.1;
+  int cheb_degree2 = 5, cheb_degree3 = 6;
   int lanczos_steps = 16;
   int coarse_sweeps = 4;
   // last solve
