@@ -60,6 +60,8 @@ def parse():
                    help="smaller variant of the workload for ncu captures")
     p.add_argument("--passes", type=int, default=None,
                    help="fewer refinement passes: a smaller case for ncu captures")
+    p.add_argument("--target", type=int, default=None,
+                   help="helmholtz workload: analysis-forest octants (smaller case for ncu)")
     p.add_argument("--workload", default="c2", choices=["c2", "c4", "c5", "helmholtz"],
                    help="c2: the multi-tree order-3 workload (default, the headline); "
                         "c4: 256 forests batched as one; "
@@ -679,13 +681,26 @@ def run_helmholtz(args):
     from tmr_gb300 import TMR
     from tmr_gb300 import build as tb
     tb.build()
-    HW = HELMHOLTZ_WORKLOAD
+    HW = dict(HELMHOLTZ_WORKLOAD)
+    if args.target:
+        HW["target"] = args.target
+        HW["name"] = HW["name"].replace("_20M_", "_%dM_" % (args.target // 1_000_000))
     f, filters, boxes, r = helmholtz_setup(TMR, HW)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     H = TMR.HelmholtzFilter(r, None, filters, vpn=HW["vpn"])
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t0
+    if args.profile_step:
+        # one filter application on the built hierarchy (ncu captures)
+        n = int(H.sizes()[0][0]) * HW["vpn"]
+        x = torch.rand(n, dtype=torch.float64, device="cuda")
+        y = torch.empty_like(x)
+        H.applyFilter(x, y)
+        torch.cuda.synchronize()
+        print(json.dumps({"workload": HW["name"], "levels": H.sizes().tolist(),
+                          "iterations": H.lastSolve()[0]}), flush=True)
+        return
     sizes = H.sizes()
     n = int(sizes[0][0])
     vpn = HW["vpn"]
@@ -752,8 +767,8 @@ def run_helmholtz(args):
             "dtype": "f64 (Krylov) + f32 (multigrid preconditioner)",
             "data": "synthetic (seeded)",
             "config": {"workload": HW["name"], "analysis_octants": f.getNumOctants(),
-                       "levels": [{"nodes": int(a), "elements": int(b), "dependent": int(c)}
-                                  for a, b, c in sizes],
+                       "levels": [{"nodes": int(a), "elements": int(b), "dependent": int(c),
+                                   "scatter_entries": int(d)} for a, b, c, d in sizes],
                        "r": r, "vpn": vpn, "l2": "flushed (256 MiB write) before each step"},
             "solver_iterations": iters, "setup_s": setup_s, "gpu_launches": launches,
             "roofline": {k: roof[k] for k in ("bound", "achieved", "peak", "unit", "frac",

@@ -324,9 +324,10 @@ int tmrg_filter_apply_static_device(tmrg_filter *F, int transpose, int vpn,
 int tmrg_helmholtz_create(tmrg_forest *const *filters, int nlevels, double r,
                           tmrg_helmholtz **out);
 int tmrg_helmholtz_destroy(tmrg_helmholtz *H);
-/* out3[3 * k + {0, 1, 2}] = independent nodes, elements and dependent
-   nodes of level k, for k < nlevels. */
-int tmrg_helmholtz_sizes(tmrg_helmholtz *H, int *nlevels, int64_t *out3);
+/* out4[4 * k + {0, 1, 2, 3}] = independent nodes, elements, dependent
+   nodes and scatter-list entries (element slots expanded through the
+   dependent weights) of level k, for k < nlevels. */
+int tmrg_helmholtz_sizes(tmrg_helmholtz *H, int *nlevels, int64_t *out4);
 /* applyFilter (TMRHelmholtzFilter.cpp:126-196): out = K^-1 M in, and
    applyTranspose (:199-247): out = M K^-1 in, for `vpn` (1..16)
    interleaved components over the finest forest's independent nodes.

@@ -69,7 +69,7 @@ def test_operators_match_oracle(gpu_lib, name):
     Hf.mult(0, 1, xd, y)
     assert _rel(y.cpu().numpy(), M @ x) <= 1e-12
     # K 1 = M 1 on every level
-    for lev, (nn, _, _) in enumerate(Hf.sizes()):
+    for lev, (nn, _, _, _) in enumerate(Hf.sizes()):
         one = torch.ones(int(nn), dtype=torch.float64, device="cuda")
         a = torch.empty_like(one)
         b = torch.empty_like(one)

@@ -705,11 +705,12 @@ class HelmholtzFilter(ConformFilter):
             pass
 
     def sizes(self):
-        """Per level (independent nodes, elements, dependent nodes)."""
+        """Per level (independent nodes, elements, dependent nodes,
+        scatter-list entries)."""
         n = ctypes.c_int(0)
-        out = np.zeros(3 * len(self.filters), np.int64)
+        out = np.zeros(4 * len(self.filters), np.int64)
         call("tmrg_helmholtz_sizes", self.ptr, ctypes.byref(n), _ptr(out))
-        return out.reshape(-1, 3)[: n.value]
+        return out.reshape(-1, 4)[: n.value]
 
     def setTolerances(self, rtol=1e-12, atol=1e-30, max_iters=300):
         call("tmrg_helmholtz_set_tolerances", self.ptr, float(rtol), float(atol),

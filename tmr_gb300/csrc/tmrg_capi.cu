@@ -1183,15 +1183,16 @@ int tmrg_helmholtz_destroy(tmrg_helmholtz *H) {
     delete H;
   });
 }
-int tmrg_helmholtz_sizes(tmrg_helmholtz *H, int *nlevels, int64_t *out3) {
+int tmrg_helmholtz_sizes(tmrg_helmholtz *H, int *nlevels, int64_t *out4) {
   return guarded([&] {
     ARG(H, "NULL filter");
     if (nlevels) *nlevels = H->H.nlevels;
-    if (out3)
+    if (out4)
       for (int k = 0; k < H->H.nlevels; k++) {
-        out3[3 * k] = H->H.L[k]->nn;
-        out3[3 * k + 1] = H->H.L[k]->ne;
-        out3[3 * k + 2] = H->H.L[k]->ndep;
+        out4[4 * k] = H->H.L[k]->nn;
+        out4[4 * k + 1] = H->H.L[k]->ne;
+        out4[4 * k + 2] = H->H.L[k]->ndep;
+        out4[4 * k + 3] = H->H.L[k]->snnz;
       }
   });
 }
