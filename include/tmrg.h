@@ -311,6 +311,34 @@ int tmrg_filter_apply_transpose_f32_device(tmrg_filter *F, int vpn,
 int tmrg_filter_apply_static_device(tmrg_filter *F, int transpose, int vpn,
                                     const double *in, double *out);
 
+/* ---- iso-surface STL ----------------------------------------------------- */
+/* TMR_GenerateSTLTriangles(root, filter, x, x_offset, cutoff, &ntris,
+   &tris) (TMR_STLTools.h:44-46, TMR_STLTools.cpp:639-902): the
+   triangles of the level set x[x_offset] = cutoff over every element of
+   `f` (marching cubes on the (order-1)^3 cells of each element, plus the
+   part of every domain-boundary cell face where x >= cutoff), in the
+   reference's element / cell / face order.  x holds `vpn` interleaved
+   values per independent node (host pointer; the _device form takes a
+   device pointer and writes device memory).  *ntris is always set; the
+   triangles (9 doubles each: three points x, y, z) are written only when
+   `tris` is non-NULL and max_tris >= *ntris.  Node positions are the
+   forest's points (tmrg_forest_get_points; zero without block boxes, as
+   the reference without a topology).  Crossing points are bit-equal to
+   the reference's; each cell's polygon loops are the reference's, split
+   into triangles from each loop's lowest edge. */
+int tmrg_stl_triangles(tmrg_forest *f, const double *x, int vpn, int x_offset, double cutoff,
+                       int64_t *ntris, double *tris, int64_t max_tris);
+int tmrg_stl_triangles_device(tmrg_forest *f, const double *x, int vpn, int x_offset,
+                              double cutoff, int64_t *ntris, double *tris, int64_t max_tris);
+/* TMR_GenerateBinFile (TMR_STLTools.cpp:904-966): int32 triangle count,
+   then 9 doubles per triangle, native byte order. */
+int tmrg_generate_bin_file(const char *filename, tmrg_forest *f, const double *x, int vpn,
+                           int x_offset, double cutoff);
+/* TMR_ConvertBinToSTL (TMR_STLTools.cpp:968-993): the ASCII STL of a
+   binary triangle file ("solid topology", one facet per triangle with
+   its unit normal, "%e" fields). */
+int tmrg_convert_bin_to_stl(const char *binfile, const char *stlfile);
+
 /* ---- Helmholtz PDE filter ------------------------------------------- */
 /* TMRHelmholtzFilter::TMRHelmholtzFilter(r, nlevels, assemblers, filters)
    (TMRHelmholtzFilter.cpp:29-33, initialize_helmholtz :48-111): the

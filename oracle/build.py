@@ -3,7 +3,7 @@
 * ``oracle/_build/libtmr_oracle.so`` — the C restatement (tmr_oracle.c),
   built wherever the repository is built.
 * ``oracle/_ref/libtmrref.so`` — the reference's own TMROctant.cpp,
-  TMROctForest.cpp and TMRBase.cpp compiled in place from the reference
+  TMROctForest.cpp, TMRBase.cpp and TMR_STLTools.cpp compiled in place from the reference
   source tree with the single-rank shims in ``oracle/ref_shim``; built only
   when that tree is present (``TMR_REFERENCE_SRC`` or the default path).
 """
@@ -37,7 +37,7 @@ def build_oracle(force=False):
 def build_ref(force=False):
     """Compile the reference octree core for one rank, if its sources exist."""
     srcs = [os.path.join(REF_SRC, f) for f in
-            ("TMROctant.cpp", "TMROctForest.cpp", "TMRBase.cpp")]
+            ("TMROctant.cpp", "TMROctForest.cpp", "TMRBase.cpp", "TMR_STLTools.cpp")]
     if not all(os.path.exists(s) for s in srcs):
         return None
     shim = os.path.join(HERE, "ref_shim")

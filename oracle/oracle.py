@@ -157,6 +157,47 @@ class OracleForest(_Forest):
 class RefForest(_Forest):
     kind = "ref"
 
+    def stlTriangles(self, X, x, vpn, offset, cutoff):
+        """The reference's TMR_GenerateSTLTriangles with node points X
+        (num_local x 3) and design values x (vpn per independent node):
+        (ntris, 3, 3)."""
+        X = np.ascontiguousarray(X, np.float64)
+        x = np.ascontiguousarray(x, np.float64)
+        self.L.stl_triangles.argtypes = [_V, _V, _V, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_double]
+        n = self.L.stl_triangles(_V(self.h), _p(X), _p(x), vpn, offset, cutoff)
+        out = np.zeros(max(n, 1) * 9, np.float64)
+        if n:
+            self.L.stl_get(_p(out))
+        return out[: 9 * n].reshape(-1, 3, 3)
+
+    def stlFiles(self, X, x, vpn, offset, cutoff, binfile, stlfile):
+        """TMR_GenerateBinFile then TMR_ConvertBinToSTL; returns fail."""
+        X = np.ascontiguousarray(X, np.float64)
+        x = np.ascontiguousarray(x, np.float64)
+        self.L.stl_files.argtypes = [_V, _V, _V, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_char_p, ctypes.c_char_p]
+        return self.L.stl_files(_V(self.h), _p(X), _p(x), vpn, offset, cutoff,
+                                binfile.encode(), stlfile.encode() if stlfile else None)
+
+    def getConnectivityTables(self):
+        """(block_face (nb x 6), face_ptr) from getConnectivity /
+        getInverseConnectivity."""
+        nb = len(self.conn)
+        sizes = np.zeros(4, np.int32)
+        bc = np.zeros(8 * nb, np.int32)
+        bf = np.zeros(6 * nb, np.int32)
+        be = np.zeros(12 * nb, np.int32)
+        fi = np.zeros(6 * nb, np.int32)
+        self.L.get_connectivity(_V(self.h), _p(sizes), _p(bc), _p(bf), _p(be), _p(fi))
+        nf, ne, nn = int(sizes[1]), int(sizes[2]), int(sizes[3])
+        ncon, nptr = np.zeros(8 * nb, np.int32), np.zeros(nn + 1, np.int32)
+        econ, eptr = np.zeros(12 * nb, np.int32), np.zeros(ne + 1, np.int32)
+        fcon, fptr = np.zeros(6 * nb, np.int32), np.zeros(nf + 1, np.int32)
+        self.L.get_inverse_connectivity(_V(self.h), _p(ncon), _p(nptr), _p(econ), _p(eptr),
+                                        _p(fcon), _p(fptr))
+        return bf.reshape(nb, 6), fptr
+
 
 def interp_to_csr(rows, ptr, cols, w, n_rows):
     """Sort the addInterp records by row into CSR (rowptr, cols, vals)."""

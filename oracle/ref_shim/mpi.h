@@ -1,7 +1,7 @@
 /*
   Single-rank stand-in for <mpi.h>, used only to compile the reference
-  TMR octree core (TMROctant.cpp, TMROctForest.cpp, TMRBase.cpp) as a CPU
-  checker.  It is test infrastructure: nothing in the tmr_gb300 product
+  TMR octree core (TMROctant.cpp, TMROctForest.cpp, TMRBase.cpp,
+  TMR_STLTools.cpp) as a CPU checker.  It is test infrastructure: nothing in the tmr_gb300 product
   links it.
 
   Semantics: the communicator has exactly one rank (rank 0, size 1).
@@ -94,5 +94,56 @@ static inline int MPI_Type_create_struct(int n, const int *counts,
 static inline int MPI_Type_commit(MPI_Datatype *) { return 0; }
 static inline int MPI_Type_free(MPI_Datatype *) { return 0; }
 static inline double MPI_Wtime() { return 0.0; }
+static inline int MPI_Gatherv(const void *s, int n, MPI_Datatype t, void *r, const int *,
+                              const int *displs, MPI_Datatype, int, MPI_Comm) {
+  memmove((char *)r + (size_t)displs[0] * (size_t)t, s, (size_t)n * (size_t)t);
+  return 0;
+}
+
+/* MPI-IO on one rank: a stdio file; a view's displacement is where the
+   next collective write lands. */
+typedef struct {
+  FILE *fp;
+  long disp;
+  MPI_Datatype etype;
+} TMRG_MPI_File;
+typedef TMRG_MPI_File *MPI_File;
+typedef int MPI_Info;
+#define MPI_INFO_NULL ((MPI_Info)0)
+#define MPI_MODE_WRONLY 4
+#define MPI_MODE_CREATE 1
+static inline int MPI_File_open(MPI_Comm, const char *name, int, MPI_Info, MPI_File *f) {
+  FILE *fp = fopen(name, "wb");
+  if (!fp) {
+    *f = 0;
+    return 1;
+  }
+  *f = (MPI_File)calloc(1, sizeof(TMRG_MPI_File));
+  (*f)->fp = fp;
+  return 0;
+}
+static inline int MPI_File_write(MPI_File f, const void *b, int n, MPI_Datatype t,
+                                 MPI_Status *) {
+  fwrite(b, (size_t)t, (size_t)n, f->fp);
+  return 0;
+}
+static inline int MPI_File_set_view(MPI_File f, long disp, MPI_Datatype etype, MPI_Datatype,
+                                    const char *, MPI_Info) {
+  f->disp = disp;
+  f->etype = etype;
+  return 0;
+}
+static inline int MPI_File_write_at_all(MPI_File f, long off, const void *b, int n,
+                                        MPI_Datatype t, MPI_Status *) {
+  fseek(f->fp, f->disp + off * (long)f->etype, SEEK_SET);
+  fwrite(b, (size_t)t, (size_t)n, f->fp);
+  return 0;
+}
+static inline int MPI_File_close(MPI_File *f) {
+  fclose((*f)->fp);
+  free(*f);
+  *f = 0;
+  return 0;
+}
 
 #endif

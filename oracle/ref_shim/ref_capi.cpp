@@ -1,7 +1,7 @@
 /*
   C entry points over the reference TMR octree core, compiled from the
-  reference's own sources (TMROctant.cpp, TMROctForest.cpp, TMRBase.cpp)
-  with the single-rank shims in this folder.  Test infrastructure only:
+  reference's own sources (TMROctant.cpp, TMROctForest.cpp, TMRBase.cpp,
+  TMR_STLTools.cpp) with the single-rank shims in this folder.  Test infrastructure only:
   it produces golden vectors and pins the C restatement in oracle/.
 
   Every function mirrors one public TMROctForest method
@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "TMROctForest.h"
+#include "TMR_STLTools.h"
 
 // The reference's TMROctForest.cpp reaches these only with a topology
 // attached or with Bernstein interpolation plus a topology; the checker
@@ -328,6 +329,61 @@ long tmrref_topo_weights(void *filt, void *ana, int *rowptr, int *cols,
 }
 int tmrref_get_local_node_number(void *f, int node) {
   return ((TMROctForest *)f)->getLocalNodeNumber(node);
+}
+
+// TMR_GenerateSTLTriangles (TMR_STLTools.cpp:854-902) with the forest's
+// node points set to X (num_local x 3; the checker attaches no topology,
+// so the reference's own points are zero) and the design values x
+// (vpn per independent node).  The triangles are kept until
+// tmrref_stl_get copies them out.
+static std::vector<double> g_stl;
+int tmrref_stl_triangles(void *f, const double *X, const double *x, int vpn, int offset,
+                         double cutoff) {
+  if (!TMRIsInitialized()) TMRInitialize();
+  TMROctForest *F = (TMROctForest *)f;
+  TMRPoint *P;
+  int nl = F->getPoints(&P);
+  for (int i = 0; i < nl; i++) {
+    P[i].x = X[3 * i];
+    P[i].y = X[3 * i + 1];
+    P[i].z = X[3 * i + 2];
+  }
+  TACSBVec vec(x, vpn);
+  int ntris = 0;
+  TMR_STLTriangle *tris = NULL;
+  TMR_GenerateSTLTriangles(0, F, &vec, offset, cutoff, &ntris, &tris);
+  g_stl.assign((size_t)ntris * 9, 0.0);
+  for (int i = 0; i < ntris; i++)
+    for (int k = 0; k < 3; k++) {
+      g_stl[9 * i + 3 * k] = tris[i].p[k].x;
+      g_stl[9 * i + 3 * k + 1] = tris[i].p[k].y;
+      g_stl[9 * i + 3 * k + 2] = tris[i].p[k].z;
+    }
+  delete[] tris;
+  return ntris;
+}
+void tmrref_stl_get(double *out) {
+  for (size_t i = 0; i < g_stl.size(); i++) out[i] = g_stl[i];
+}
+int tmrref_convert_bin_to_stl(const char *binfile, const char *stlfile) {
+  return TMR_ConvertBinToSTL(binfile, stlfile);
+}
+// TMR_GenerateBinFile + TMR_ConvertBinToSTL (TMR_STLTools.cpp:904-993).
+int tmrref_stl_files(void *f, const double *X, const double *x, int vpn, int offset,
+                     double cutoff, const char *binfile, const char *stlfile) {
+  if (!TMRIsInitialized()) TMRInitialize();
+  TMROctForest *F = (TMROctForest *)f;
+  TMRPoint *P;
+  int nl = F->getPoints(&P);
+  for (int i = 0; i < nl; i++) {
+    P[i].x = X[3 * i];
+    P[i].y = X[3 * i + 1];
+    P[i].z = X[3 * i + 2];
+  }
+  TACSBVec vec(x, vpn);
+  int fail = TMR_GenerateBinFile(binfile, F, &vec, offset, cutoff);
+  if (!fail && stlfile) fail = TMR_ConvertBinToSTL(binfile, stlfile);
+  return fail;
 }
 
 }  // extern "C"

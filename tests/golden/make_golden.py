@@ -189,6 +189,40 @@ def _ref_knots(f):
     return k
 
 
+def make_stl_golden():
+    """tests/golden/api_stl.npz: the reference's own TMR_GenerateSTLTriangles
+    output (oracle/_ref) on parity forests with block boxes and a seeded
+    field (tests/pipeline.py STL_CASES)."""
+    from oracle.oracle import RefForest
+    arrs = {}
+    for name, sc in pipeline.STL_CASES.items():
+        case = pipeline.cases()[name]
+        o = case["order"]
+        f = RefForest(o, case.get("interp", 1))
+        f.setConnectivity(case["conn"])
+        f.createTrees(case["L0"])
+        for p in range(case["passes"]):
+            oc = f.getOctants()
+            f.refine(pipeline.indicator(oc, case, p), 0, case["max_level"])
+            f.balance(case.get("corner", 1))
+        f.createNodes()
+        s = f.nodeSizes()
+        knots = [-1.0, 1.0] if o == 2 else ([-1.0, -np.cos(np.pi / 2), 1.0]
+                                            if case.get("interp", 1) == 1 else [-1.0, 0.0, 1.0])
+        boxes = pipeline.brick_boxes(*sc["grid"])
+        X = pipeline.node_points(f.getOctants(), f.getMeshConn(o), s["num_dep"], s["num_local"],
+                                 o, knots, boxes)
+        x = pipeline.stl_field(X[s["num_dep"]:], sc["vpn"])
+        tris = f.stlTriangles(X, x, sc["vpn"], sc["offset"], sc["cutoff"])
+        arrs[name + "_tris"] = tris
+        arrs[name + "_octants"] = f.getOctants()
+        print(name, len(tris), "reference triangles")
+    out = os.path.join(HERE, "api_stl.npz")
+    np.savez_compressed(out, **arrs)
+    print("->", out, os.path.getsize(out), "bytes")
+
+
 if __name__ == "__main__":
     main()
     make_api_golden()
+    make_stl_golden()

@@ -130,10 +130,11 @@ GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def golden_cases():
-    """Names of the pipeline fixtures in tests/golden (api.npz holds the
-    single-call getters and is read by its own tests)."""
+    """Names of the pipeline fixtures in tests/golden (api*.npz hold the
+    single-call getters and the STL output and are read by their own
+    tests)."""
     return sorted(f[:-4] for f in os.listdir(GOLDEN_DIR)
-                  if f.endswith(".npz") and f != "api.npz")
+                  if f.endswith(".npz") and not f.startswith("api"))
 
 
 def load_golden(name):
@@ -189,3 +190,45 @@ def cases():
                          max_level=4, indicator="mixed", prob=0.35, coarsen_prob=0.3, seed=12,
                          coarse_levels=2),
     }
+
+
+# ---------------------------------------------------------------------------
+# Iso-surface (STL) cases: the parity forests with unit-cube block boxes,
+# node points by the box map, and a smooth seeded design field.
+STL_CASES = {
+    "brick_o2": dict(cutoff=0.1, vpn=2, offset=0, grid=(3, 2, 2)),
+    "uniform_o3": dict(cutoff=0.05, vpn=2, offset=1, grid=(2, 1, 1)),
+}
+
+
+def brick_boxes(nx, ny, nz, ext=(1.0, 1.0, 1.0)):
+    """Block boxes (origin xyz, extent xyz) of W.brick(nx, ny, nz)."""
+    return np.array([[i * ext[0], j * ext[1], k * ext[2], *ext] for k in range(nz)
+                     for j in range(ny) for i in range(nx)], np.float64)
+
+
+def node_points(octs, conn, num_dep, num_local, order, knots, boxes):
+    """getPoints with block boxes: each node placed by the first (element,
+    local index) that uses it (local index of node g: g + num_dep)."""
+    X = np.full((num_local, 3), np.nan)
+    s = 1.0 / (1 << 30)
+    for e in range(len(octs)):
+        b, x, y, z, _, lev, _ = (int(v) for v in octs[e])
+        d = (1 << (30 - lev)) * s
+        for l in range(order ** 3):
+            li = int(conn[e, l]) + num_dep
+            if not np.isnan(X[li, 0]):
+                continue
+            ijk = (l % order, (l // order) % order, l // (order * order))
+            for a, c in enumerate((x, y, z)):
+                u = c * s + 0.5 * d * (1.0 + knots[ijk[a]])
+                X[li, a] = boxes[b, a] + boxes[b, 3 + a] * u
+    return X
+
+
+def stl_field(P, vpn):
+    """Design values at the independent nodes' points P: component 0 is
+    sin(2x) cos(1.5y) + 0.3z, component 1 its negative plus 0.2."""
+    f = np.sin(2.0 * P[:, 0]) * np.cos(1.5 * P[:, 1]) + 0.3 * P[:, 2]
+    comps = [f, 0.2 - f][:vpn]
+    return np.stack(comps, 1).ravel()

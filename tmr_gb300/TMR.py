@@ -660,6 +660,14 @@ class ConformFilter:
     def setValues(self, g):
         return g
 
+    def writeSTLFile(self, k, cutoff, filename):
+        """writeSTLFile (TMRConformFilter.h:58-61): the binary STL file of
+        design component k of the finest-level design variables (set by
+        setDesignVars) at level `cutoff`."""
+        if self.x is not None:
+            writeSTLToBin(filename, self.filters[0], self.x[0], index=k, cutoff=cutoff,
+                          vpn=self.vpn)
+
     def applyFilter(self, x, y, vpn=None):
         import sys
         sys.stderr.write("TMR Filter Error: applyFilter() method is not implemented!\n")
@@ -770,6 +778,62 @@ class HelmholtzFilter(ConformFilter):
         """addValues (:267-272): the gradient with respect to the unfiltered
         variables, applyTranspose of g."""
         return self._apply(True, g, _like(g))
+
+
+def _stl_values(forest, x, vpn):
+    n = forest.getNodeRange()[1]
+    if vpn is None:
+        vpn = max(1, len(x) // max(n, 1))
+    if len(x) != n * vpn:
+        raise ValueError("design vector length %d is not %d nodes x %d values" %
+                         (len(x), n, vpn))
+    return vpn
+
+
+def getSTLTriangles(forest, x, offset=0, cutoff=0.5, root=0, vpn=None):
+    """getSTLTriangles (TMR.pyx; TMR_GenerateSTLTriangles,
+    TMR_STLTools.cpp:639-902): the points (3 ntris, 3) of the triangles of
+    the level set x[offset] = cutoff, or np.array([[]]) when there are
+    none.  x: numpy or torch CUDA array of vpn interleaved values per
+    independent node of `forest`; `root` is accepted (one process)."""
+    vpn = _stl_values(forest, x, vpn)
+    n = ctypes.c_int64(0)
+    if _is_torch(x):
+        import torch
+        fn, xp = "tmrg_stl_triangles_device", _vp(x.data_ptr())
+        call(fn, forest.ptr, xp, vpn, int(offset), float(cutoff), ctypes.byref(n), None, 0)
+        out = torch.empty(max(n.value, 1) * 9, dtype=torch.float64, device=x.device)
+        call(fn, forest.ptr, xp, vpn, int(offset), float(cutoff), ctypes.byref(n),
+             _vp(out.data_ptr()), n.value)
+        pts = out[: 9 * n.value].reshape(-1, 3).cpu().numpy()
+    else:
+        xh = np.ascontiguousarray(x, dtype=np.float64)
+        call("tmrg_stl_triangles", forest.ptr, _ptr(xh), vpn, int(offset), float(cutoff),
+             ctypes.byref(n), None, 0)
+        pts = np.zeros(max(n.value, 1) * 9)
+        call("tmrg_stl_triangles", forest.ptr, _ptr(xh), vpn, int(offset), float(cutoff),
+             ctypes.byref(n), _ptr(pts), n.value)
+        pts = pts[: 9 * n.value].reshape(-1, 3)
+    if n.value == 0:
+        return np.array([[]])
+    return pts
+
+
+def writeSTLToBin(fname, forest, x, index=0, cutoff=0.5, vpn=None):
+    """writeSTLToBin (TMR.pyx; TMR_GenerateBinFile): the triangles of the
+    level set x[index] = cutoff to a binary file (int32 count, then 9
+    doubles a triangle)."""
+    xh = x.detach().cpu().numpy() if _is_torch(x) else x
+    xh = np.ascontiguousarray(xh, dtype=np.float64)
+    vpn = _stl_values(forest, xh, vpn)
+    call("tmrg_generate_bin_file", str(fname).encode(), forest.ptr, _ptr(xh), vpn, int(index),
+         float(cutoff))
+
+
+def convertBinToSTL(binfile, stlfile):
+    """TMR_ConvertBinToSTL (the reference's bstltostl converter): the ASCII
+    STL file of a binary triangle file."""
+    call("tmrg_convert_bin_to_stl", str(binfile).encode(), str(stlfile).encode())
 
 
 def createTopoWeights(filter, forest):

@@ -91,6 +91,10 @@ _SIGS = {
     "tmrg_filter_apply_f32_device": [c_vp, c_int, c_vp, c_vp],
     "tmrg_filter_apply_transpose_f32_device": [c_vp, c_int, c_vp, c_vp],
     "tmrg_filter_apply_static_device": [c_vp, c_int, c_int, c_vp, c_vp],
+    "tmrg_stl_triangles": [c_vp, c_vp, c_int, c_int, c_dbl, c_vp, c_vp, c_i64],
+    "tmrg_stl_triangles_device": [c_vp, c_vp, c_int, c_int, c_dbl, c_vp, c_vp, c_i64],
+    "tmrg_generate_bin_file": [ctypes.c_char_p, c_vp, c_vp, c_int, c_int, c_dbl],
+    "tmrg_convert_bin_to_stl": [ctypes.c_char_p, ctypes.c_char_p],
     "tmrg_helmholtz_create": [c_vp, c_int, c_dbl, P(c_vp)],
     "tmrg_helmholtz_destroy": [c_vp],
     "tmrg_helmholtz_sizes": [c_vp, c_vp, c_vp],

@@ -23,6 +23,7 @@ SOURCES = [
     "tmrg_interp.cu",
     "tmrg_filter.cu",
     "tmrg_helmholtz.cu",
+    "tmrg_stl.cu",
     "tmrg_capi.cu",
 ]
 

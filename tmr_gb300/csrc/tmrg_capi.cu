@@ -1155,6 +1155,102 @@ int tmrg_filter_apply_static_device(tmrg_filter *F, int transpose, int vpn,
   });
 }
 
+// ---- iso-surface STL ----------------------------------------------------
+static long long stl_run(tmrg_forest *f, const double *x, bool device, int vpn,
+                         int x_offset, double cutoff, DBuf<double> &tris) {
+  Forest &F = f->f;
+  if (!F.have_nodes) forest_create_nodes(F);
+  const long long len = F.num_owned * vpn;
+  if (device) return stl_triangles(F, x, vpn, x_offset, cutoff, tris);
+  DBuf<double> dx(std::max(1LL, len), F.s);
+  if (len)
+    TMRG_CUDA(cudaMemcpyAsync(dx.p, x, sizeof(double) * len, cudaMemcpyHostToDevice, F.s));
+  return stl_triangles(F, dx.p, vpn, x_offset, cutoff, tris);
+}
+static int stl_entry(tmrg_forest *f, const double *x, bool device, int vpn, int x_offset,
+                     double cutoff, int64_t *ntris, double *tris, int64_t max_tris) {
+  return guarded([&] {
+    ARG(f && x && ntris && vpn > 0, "bad argument");
+    DBuf<double> d;
+    const long long n = stl_run(f, x, device, vpn, x_offset, cutoff, d);
+    *ntris = n;
+    if (tris && max_tris >= n && n) {
+      if (device) {
+        TMRG_CUDA(cudaMemcpyAsync(tris, d.p, sizeof(double) * 9 * n, cudaMemcpyDeviceToDevice,
+                                  f->f.s));
+        TMRG_CUDA(cudaStreamSynchronize(f->f.s));
+      } else {
+        copy_d2h(tris, d.p, sizeof(double) * 9 * n, f->f.s);
+      }
+    }
+  });
+}
+int tmrg_stl_triangles(tmrg_forest *f, const double *x, int vpn, int x_offset, double cutoff,
+                       int64_t *ntris, double *tris, int64_t max_tris) {
+  return stl_entry(f, x, false, vpn, x_offset, cutoff, ntris, tris, max_tris);
+}
+int tmrg_stl_triangles_device(tmrg_forest *f, const double *x, int vpn, int x_offset,
+                              double cutoff, int64_t *ntris, double *tris, int64_t max_tris) {
+  return stl_entry(f, x, true, vpn, x_offset, cutoff, ntris, tris, max_tris);
+}
+int tmrg_generate_bin_file(const char *filename, tmrg_forest *f, const double *x, int vpn,
+                           int x_offset, double cutoff) {
+  return guarded([&] {
+    ARG(filename && f && x && vpn > 0, "bad argument");
+    DBuf<double> d;
+    const long long n = stl_run(f, x, false, vpn, x_offset, cutoff, d);
+    ARG(n < (1LL << 31), "more triangles than the binary format's int count holds");
+    std::vector<double> h((size_t)9 * n);
+    copy_d2h(h.data(), d.p, sizeof(double) * h.size(), f->f.s);
+    FILE *fp = fopen(filename, "wb");
+    if (!fp) throw Error(TMRG_ERR_ARG, std::string("cannot open ") + filename);
+    int32_t cnt = (int32_t)n;
+    bool ok = fwrite(&cnt, sizeof(cnt), 1, fp) == 1 &&
+              (n == 0 || fwrite(h.data(), sizeof(double), h.size(), fp) == h.size());
+    ok = (fclose(fp) == 0) && ok;
+    if (!ok) throw Error(TMRG_ERR_ARG, std::string("write failed: ") + filename);
+  });
+}
+int tmrg_convert_bin_to_stl(const char *binfile, const char *stlfile) {
+  return guarded([&] {
+    ARG(binfile && stlfile, "NULL file name");
+    FILE *fp = fopen(binfile, "rb");
+    if (!fp) throw Error(TMRG_ERR_ARG, std::string("cannot open ") + binfile);
+    int32_t n = 0;
+    std::vector<double> t;
+    bool ok = fread(&n, sizeof(n), 1, fp) == 1 && n >= 0;
+    if (ok) {
+      t.resize((size_t)9 * n);
+      ok = n == 0 || fread(t.data(), sizeof(double), t.size(), fp) == t.size();
+    }
+    fclose(fp);
+    if (!ok) throw Error(TMRG_ERR_ARG, std::string("bad STL binary file: ") + binfile);
+    FILE *out = fopen(stlfile, "w");
+    if (!out) throw Error(TMRG_ERR_ARG, std::string("cannot open ") + stlfile);
+    // the reference's text layout and facet normal (writeSTLFile and
+    // compute_normal, TMR_STLTools.cpp:440-461, 544-574)
+    fprintf(out, "solid topology\n");
+    for (int32_t i = 0; i < n; i++) {
+      const double *p = t.data() + 9 * (size_t)i;
+      double a[3] = {p[3] - p[0], p[4] - p[1], p[5] - p[2]};
+      double b[3] = {p[6] - p[0], p[7] - p[1], p[8] - p[2]};
+      double nn[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2],
+                      a[0] * b[1] - a[1] * b[0]};
+      double norm = sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+      nn[0] /= norm;
+      nn[1] /= norm;
+      nn[2] /= norm;
+      fprintf(out, "facet normal %e %e %e\n", nn[0], nn[1], nn[2]);
+      fprintf(out, "outer loop\n");
+      for (int k = 0; k < 3; k++)
+        fprintf(out, "vertex %e %e %e\n", p[3 * k], p[3 * k + 1], p[3 * k + 2]);
+      fprintf(out, "endloop\nendfacet\n");
+    }
+    fprintf(out, "endsolid topology\n");
+    if (fclose(out) != 0) throw Error(TMRG_ERR_ARG, std::string("write failed: ") + stlfile);
+  });
+}
+
 // ---- Helmholtz filter ---------------------------------------------------
 int tmrg_helmholtz_create(tmrg_forest *const *filters, int nlevels, double r,
                           tmrg_helmholtz **out) {

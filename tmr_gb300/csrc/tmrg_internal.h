@@ -152,5 +152,7 @@ void forest_transform_nodes(Forest &f, tmrg_octant *d_octs, long long n, int edg
 void forest_find_enclosing(Forest &f, int order, const double *knots,
                            const tmrg_octant *d_nodes, long long n, long long *d_index);
 void forest_get_points(Forest &f, const double *boxes, double *d_X);
+long long stl_triangles(Forest &f, const double *d_x, int vpn, int offset, double cutoff,
+                        DBuf<double> &tris);
 
 }  // namespace tmrg
