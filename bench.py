@@ -62,11 +62,12 @@ def parse():
                    help="fewer refinement passes: a smaller case for ncu captures")
     p.add_argument("--target", type=int, default=None,
                    help="helmholtz workload: analysis-forest octants (smaller case for ncu)")
-    p.add_argument("--workload", default="c2", choices=["c2", "c4", "c5", "helmholtz"],
+    p.add_argument("--workload", default="c2", choices=["c2", "c4", "c5", "helmholtz", "stl"],
                    help="c2: the multi-tree order-3 workload (default, the headline); "
                         "c4: 256 forests batched as one; "
                         "c5: the 200M-octant adaptive workload (one JSON line of its own); "
-                        "helmholtz: the Helmholtz PDE filter on a 5-level filter hierarchy")
+                        "helmholtz: the Helmholtz PDE filter on a 5-level filter hierarchy; "
+                        "stl: iso-surface triangles of a smoothed density")
     a = p.parse_args()
     if a.passes is not None:
         WORKLOAD["passes"] = a.passes
@@ -673,6 +674,133 @@ def helmholtz_cpu_baseline(HW):
                           nx, ny, nz, S["bumps"], len(f.getOctants()), n)}
 
 
+# The iso-surface configuration: the Helmholtz workload's filter forest
+# (2.6M order-2 elements), a density field made smooth by the Helmholtz
+# filter (a seeded uniform field filtered with r = 8 h_min), triangles of
+# its 0.5 level set with the closing boundary faces.
+STL_WORKLOAD = dict(name="brick16x8x8_16bumps_20M_filter-forest_order2_helmholtz-smoothed_cut0.5",
+                    cutoff=0.5, r_factor=8.0,
+                    cpu_sample=dict(nx=4, ny=2, nz=2, L0=3, seed=3, max_level=7))
+
+
+def stl_cpu_baseline(SW):
+    """The oracle's triangles (Python) on a bounded sample: elements per
+    second, one core."""
+    import time
+
+    from oracle import stl as Sx
+    from oracle.oracle import OracleForest
+    from tmr_gb300 import workloads as Wk
+    S = SW["cpu_sample"]
+    nx, ny, nz = S["nx"], S["ny"], S["nz"]
+    f = OracleForest(2, 1)
+    f.setConnectivity(Wk.brick(nx, ny, nz))
+    f.createTrees(S["L0"])
+    f.refine(Wk.random_indicator(len(f.getOctants()), S["seed"], 0, 0.5), 0, S["max_level"])
+    f.balance(1)
+    f.createNodes()
+    s = f.nodeSizes()
+    boxes = np.array([[i, j, k, 1.0, 1.0, 1.0] for k in range(nz) for j in range(ny)
+                      for i in range(nx)], np.float64)
+    octs, conn = f.getOctants(), f.getMeshConn(2)
+    from tests import pipeline as tp
+    X = tp.node_points(octs, conn, s["num_dep"], s["num_local"], 2, [-1.0, 1.0], boxes)
+    x = 0.5 + 0.5 * np.sin(3.0 * X[s["num_dep"]:, 0]) * np.cos(2.0 * X[s["num_dep"]:, 1])
+    bface = np.array([[i == 0, i == nx - 1, j == 0, j == ny - 1, k == 0, k == nz - 1]
+                      for k in range(nz) for j in range(ny) for i in range(nx)], bool)
+    t = time.perf_counter()
+    tris = Sx.triangles(octs, conn, f.getDepNodeConn(), X, x, 1, 0, SW["cutoff"], 2, bface)
+    dt = time.perf_counter() - t
+    return {"value": len(octs) / dt, "unit": "elements/s", "cores": 1, "kind": "port",
+            "sample": "oracle (Python) triangles of a smooth field's 0.5 level set on a "
+                      "%dx%dx%d brick, %d order-2 elements, %d triangles" % (
+                          nx, ny, nz, len(octs), len(tris))}
+
+
+def run_stl(args):
+    """One JSON line for the iso-surface configuration."""
+    import time
+
+    import torch
+    from tmr_gb300 import TMR
+    from tmr_gb300 import build as tb
+    tb.build()
+    SW = STL_WORKLOAD
+    HW = dict(HELMHOLTZ_WORKLOAD)
+    f, filters, boxes, r = helmholtz_setup(TMR, HW)
+    F = filters[0]
+    n = int(F.getNodeRange()[1])
+    H = TMR.HelmholtzFilter(SW["r_factor"] * r / 2.0, None, filters)
+    g = torch.Generator(device="cuda").manual_seed(7)
+    x0 = torch.rand(n, dtype=torch.float64, device="cuda", generator=g)
+    x = torch.empty_like(x0)
+    H.applyFilter(x0, x)
+    del H
+    ne = int(F.getNumOctants())
+    cnt = ctypes.c_int64(0)
+    L = TMR.lib()
+    xp = ctypes.c_void_p(x.data_ptr())
+    TMR.call("tmrg_stl_triangles_device", F.ptr, xp, 1, 0, SW["cutoff"], ctypes.byref(cnt),
+             None, 0)
+    ntri = cnt.value
+    out = torch.empty(max(ntri, 1) * 9, dtype=torch.float64, device="cuda")
+    op = ctypes.c_void_p(out.data_ptr())
+
+    def step():
+        TMR.call("tmrg_stl_triangles_device", F.ptr, xp, 1, 0, SW["cutoff"], ctypes.byref(cnt),
+                 op, ntri)
+    for _ in range(args.warmup):
+        step()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    tot = 0.0
+    lc0 = TMR.kernel_launch_count()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0.record()
+        step()
+        e1.record()
+        torch.cuda.synchronize()
+        tot += e0.elapsed_time(e1)
+    launches = (TMR.kernel_launch_count() - lc0) // args.steps
+    ms = tot / args.steps
+    L.tmrg_profile_begin()
+    step()
+    buf = ctypes.create_string_buffer(1 << 20)
+    L.tmrg_profile_end(buf, len(buf))
+    prof = {k.strip("()"): v for k, v in json.loads(buf.value.decode()).items()}
+    tot_ms = sum(v[1] for v in prof.values())
+    top = max(prof.items(), key=lambda kv: kv[1][1])
+    peak, peak_kind = measured_peaks()
+    roof = roofline_entry(top[0], top[1], peak, peak_kind, None, tot_ms)
+    # end to end: host values in, host triangles out (two calls: count, copy)
+    xh = x.cpu().numpy()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        pts = TMR.getSTLTriangles(F, xh, cutoff=SW["cutoff"])
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    line = {"metric": "iso-surface elements/s", "value": ne / (ms / 1e3), "unit": "elements/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": SW["name"], "elements": ne, "nodes": n, "triangles": ntri,
+                       "l2": "flushed (256 MiB write) before each step"},
+            "gpu_launches": launches,
+            "roofline": {k: roof[k] for k in ("bound", "achieved", "peak", "unit", "frac",
+                                              "traffic")},
+            "top_kernel": roof,
+            "kernel_shares": {k: round(v[1] / tot_ms, 4) for k, v in prof.items()},
+            "e2e": {"value": ne / e2e_s, "unit": "elements/s",
+                    "h2d_bytes_per_step": 2 * 8 * n, "d2h_bytes_per_step": 2 * 72 * ntri + 16},
+            "e2e_triangles_equal_device": bool(
+                len(pts) == 3 * ntri and np.array_equal(
+                    pts.reshape(-1), out[: 9 * ntri].cpu().numpy()))}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = stl_cpu_baseline(SW)
+    print(json.dumps(line), flush=True)
+
+
 def run_helmholtz(args):
     """One JSON line for the Helmholtz filter configuration."""
     import time
@@ -1195,6 +1323,8 @@ def main():
         run_c4(args)
     elif args.workload == "helmholtz":
         run_helmholtz(args)
+    elif args.workload == "stl":
+        run_stl(args)
     else:
         run_gpu(args)
 

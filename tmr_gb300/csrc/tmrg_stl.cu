@@ -12,7 +12,8 @@
 // an element, a cell's iso-surface triangles before its boundary-face
 // triangles (faces in the order -x, +x, -y, +y, -z, +z): the reference's
 // output order.  Two passes: a count per element, a scan, then each element
-// writes its triangles at its offset.
+// writes its triangles at its offset (staged in shared memory, so that
+// the output is stored block by block in full lines).
 //
 // Case tables are built here, on the host, by one construction rule rather
 // than taken from a published table:
@@ -262,16 +263,12 @@ __device__ long long stl_element(const StlCtx &c, long long e, double *out) {
         const int nv = c_stl.vn[ci];
         if (out) {
           double vp[12][3];
-          for (int ed = 0; ed < 12; ed++) {
-            bool used = false;
-            for (int t = 0; t < nv; t++)
-              used = used || c_stl.vt[ci][t][0] == ed || c_stl.vt[ci][t][1] == ed ||
-                     c_stl.vt[ci][t][2] == ed;
-            if (used) {
-              const int a = c_stl.edge[ed][0], bb = c_stl.edge[ed][1];
+          // crossing points of the edges the level set cuts
+          for (int ed = 0; ed < 12 && nv; ed++) {
+            const int a = c_stl.edge[ed][0], bb = c_stl.edge[ed][1];
+            if (((ci >> a) ^ (ci >> bb)) & 1)
               vinterp(c.cutoff, c.X + 3LL * li[off[a]], c.X + 3LL * li[off[bb]], val[a], val[bb],
                       vp[ed]);
-            }
           }
           for (int t = 0; t < nv; t++) {
             double *w = out + 9 * (cnt + t);
@@ -319,11 +316,27 @@ __global__ void k_stl_count(StlCtx c, long long *cnt) {
   if (e >= c.n) return;
   cnt[e] = stl_element<O>(c, e, nullptr);
 }
+// The block's triangles are one contiguous run of the output: each thread
+// writes its element's triangles into a shared-memory copy of that run,
+// then the block stores the run with consecutive threads on consecutive
+// doubles.  A block whose run exceeds the staging area writes directly.
+constexpr int STL_THREADS = 128;
+constexpr int STL_STAGE = 640;  // triangles (46 KB)
 template <int O>
-__global__ void k_stl_write(StlCtx c, const long long *__restrict__ off, double *tris) {
-  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= c.n) return;
-  stl_element<O>(c, e, tris + 9 * off[e]);
+__global__ void __launch_bounds__(STL_THREADS)
+    k_stl_write(StlCtx c, const long long *__restrict__ off, double *tris) {
+  extern __shared__ double st[];
+  const long long e0 = (long long)blockIdx.x * blockDim.x;
+  const long long e = e0 + threadIdx.x;
+  const long long e1 = min(e0 + (long long)blockDim.x, c.n);
+  const long long base = off[e0], end = off[e1];
+  const bool staged = end - base <= STL_STAGE;
+  if (e < c.n) stl_element<O>(c, e, staged ? st + 9 * (off[e] - base) : tris + 9 * off[e]);
+  if (staged) {
+    __syncthreads();
+    double *dst = tris + 9 * base;
+    for (long long i = threadIdx.x; i < 9 * (end - base); i += blockDim.x) dst[i] = st[i];
+  }
 }
 
 
@@ -411,6 +424,11 @@ long long stl_triangles(Forest &f, const double *d_x, int vpn, int offset, doubl
            bern ? 1 : 0, NB.p};
   const long long n = f.n;
   DBuf<long long> cnt(n + 1, s);
+  // compulsory traffic of a pass: element connectivity and octant fields,
+  // the design values and dependent weights once, the per-element count
+  const long long base = (4LL * npe + 18) * n + 8LL * f.num_owned * vpn +
+                         16LL * f.dep_nnz + 4 * (f.num_dep + 1);
+  prof_bytes(base + 8 * n);
   if (o == 2)
     launch(k_stl_count<2>, blocks_for(n, 128), 128, 0, s, c, cnt.p);
   else
@@ -419,10 +437,15 @@ long long stl_triangles(Forest &f, const double *d_x, int vpn, int offset, doubl
   const long long ntri = read_scalar(cnt.p + n, s);
   tris.alloc(9 * std::max(1LL, ntri), s);
   if (ntri) {
+    // plus the node points once and the triangles written
+    prof_bytes(base + 8 * n + 24LL * f.num_local + 72LL * ntri);
+    const size_t sm = sizeof(double) * 9 * STL_STAGE;
     if (o == 2)
-      launch(k_stl_write<2>, blocks_for(n, 128), 128, 0, s, c, (const long long *)cnt.p, tris.p);
+      launch(k_stl_write<2>, blocks_for(n, STL_THREADS), STL_THREADS, sm, s, c,
+             (const long long *)cnt.p, tris.p);
     else
-      launch(k_stl_write<3>, blocks_for(n, 128), 128, 0, s, c, (const long long *)cnt.p, tris.p);
+      launch(k_stl_write<3>, blocks_for(n, STL_THREADS), STL_THREADS, sm, s, c,
+             (const long long *)cnt.p, tris.p);
   }
   TMRG_CUDA(cudaStreamSynchronize(s));
   return ntri;
