@@ -42,6 +42,7 @@ typedef struct tmrg_forest tmrg_forest;
 typedef struct tmrg_interp tmrg_interp;
 typedef struct tmrg_filter tmrg_filter;
 typedef struct tmrg_helmholtz tmrg_helmholtz;
+typedef struct tmrg_qforest tmrg_qforest;
 
 /* Message of the last failed call on this thread ("" if none). */
 const char *tmrg_last_error(void);
@@ -310,6 +311,59 @@ int tmrg_filter_apply_transpose_f32_device(tmrg_filter *F, int vpn,
    the filter's stream; allocates nothing. */
 int tmrg_filter_apply_static_device(tmrg_filter *F, int transpose, int vpn,
                                     const double *in, double *out);
+
+/* ---- quadtree forest (the 2-D twin) ------------------------------------ */
+/* TMRQuadForest (TMRQuadForest.h:43-161) on the GPU: orders 2 and 3 with
+   Gauss-Lobatto or uniform knots (TMRG_ERR_UNSUPPORTED otherwise). */
+int tmrg_qforest_create(int order, int interp, void *cuda_stream, tmrg_qforest **out);
+int tmrg_qforest_destroy(tmrg_qforest *f);
+/* setConnectivity (TMRQuadForest.cpp:318-349): 4 nodes per face, corners
+   x fastest; edges numbered from the nodes. */
+int tmrg_qforest_set_connectivity(tmrg_qforest *f, int num_nodes, const int *face_conn,
+                                  int num_faces);
+/* setFullConnectivity (:351-386): edge numbers given (4 per face). */
+int tmrg_qforest_set_full_connectivity(tmrg_qforest *f, int num_nodes, int num_edges,
+                                       int num_faces, const int *face_conn,
+                                       const int *face_edge_conn);
+/* getConnectivity (:1162-1201): sizes3 = {faces, edges, nodes}. */
+int tmrg_qforest_get_connectivity(tmrg_qforest *f, int *sizes3, int *face_conn,
+                                  int *face_edge_conn);
+/* setMeshOrder / getMeshOrder / getInterpType / getInterpKnots
+   (:948-1067). */
+int tmrg_qforest_set_mesh_order(tmrg_qforest *f, int order, int interp);
+int tmrg_qforest_get_mesh_order(tmrg_qforest *f, int *order, int *interp, double *knots);
+/* createTrees (:1239-1325), refine (:1644-1800; host or device array, NULL
+   refines every quadrant by one level), coarsen (:1594-1640), duplicate
+   (:1572-1592), balance (:2237-2410), createNodes (:2996-3216). */
+int tmrg_qforest_create_trees(tmrg_qforest *f, int level);
+int tmrg_qforest_refine(tmrg_qforest *f, const int *refine, int64_t n, int min_level,
+                        int max_level);
+int tmrg_qforest_refine_device(tmrg_qforest *f, const int *d_refine, int64_t n, int min_level,
+                               int max_level);
+int tmrg_qforest_coarsen(tmrg_qforest *f, tmrg_qforest **out);
+int tmrg_qforest_duplicate(tmrg_qforest *f, tmrg_qforest **out);
+int tmrg_qforest_balance(tmrg_qforest *f, int corner);
+int tmrg_qforest_create_nodes(tmrg_qforest *f);
+/* getQuadrants (:1011-1018): 6 ints per quadrant {face, x, y, tag, level,
+   info}, in element order. */
+int tmrg_qforest_num_quadrants(tmrg_qforest *f, int64_t *n);
+int tmrg_qforest_get_quadrants(tmrg_qforest *f, int *out);
+/* out6 = {local nodes, owned nodes, dependent nodes, ext_pre_offset,
+   elements, dependent-weight entries}. */
+int tmrg_qforest_sizes(tmrg_qforest *f, int64_t *out6);
+/* getNodeConn (:4005-4032): order^2 nodes per element; getDepNodeConn
+   (:4034-4063): `order` entries per dependent node. */
+int tmrg_qforest_get_node_conn(tmrg_qforest *f, int *conn);
+int tmrg_qforest_get_dep_node_conn(tmrg_qforest *f, int *ptr, int *conn, double *w);
+/* createInterpolation (:4660-4845): P from `coarse` to `fine`, applied with
+   the tmrg_interp_* functions. */
+int tmrg_qforest_create_interpolation(tmrg_qforest *fine, tmrg_qforest *coarse,
+                                      tmrg_interp **out);
+/* Geometry stand-in for the topology: a box per face (origin x, y,
+   extent x, y); getPoints (:1035-1043) then gives num_local x 3 points
+   (z = 0), zero without boxes. */
+int tmrg_qforest_set_face_boxes(tmrg_qforest *f, const double *boxes, int nboxes);
+int tmrg_qforest_get_points(tmrg_qforest *f, double *X);
 
 /* ---- iso-surface STL ----------------------------------------------------- */
 /* TMR_GenerateSTLTriangles(root, filter, x, x_offset, cutoff, &ntris,

@@ -3,7 +3,8 @@
 * ``oracle/_build/libtmr_oracle.so`` — the C restatement (tmr_oracle.c),
   built wherever the repository is built.
 * ``oracle/_ref/libtmrref.so`` — the reference's own TMROctant.cpp,
-  TMROctForest.cpp, TMRBase.cpp and TMR_STLTools.cpp compiled in place from the reference
+  TMROctForest.cpp, TMRBase.cpp, TMR_STLTools.cpp and the quadtree core
+  (TMRQuadrant.cpp, TMRQuadForest.cpp) compiled in place from the reference
   source tree with the single-rank shims in ``oracle/ref_shim``; built only
   when that tree is present (``TMR_REFERENCE_SRC`` or the default path).
 """
@@ -37,7 +38,8 @@ def build_oracle(force=False):
 def build_ref(force=False):
     """Compile the reference octree core for one rank, if its sources exist."""
     srcs = [os.path.join(REF_SRC, f) for f in
-            ("TMROctant.cpp", "TMROctForest.cpp", "TMRBase.cpp", "TMR_STLTools.cpp")]
+            ("TMROctant.cpp", "TMROctForest.cpp", "TMRBase.cpp", "TMR_STLTools.cpp",
+             "TMRQuadrant.cpp", "TMRQuadForest.cpp")]
     if not all(os.path.exists(s) for s in srcs):
         return None
     shim = os.path.join(HERE, "ref_shim")
@@ -48,6 +50,7 @@ def build_ref(force=False):
         # without including it
         subprocess.run(["g++", *CFLAGS, "-w", "-include", "math.h", "-I", shim,
                         "-I", REF_SRC, *srcs, os.path.join(shim, "ref_capi.cpp"),
+                        os.path.join(shim, "ref_quad.cpp"),
                         "-o", REF_SO], check=True)
     return REF_SO
 

@@ -223,3 +223,111 @@ def uniform(seed, stream, n):
     L.oo_uniform.restype = ctypes.c_double
     L.oo_uniform.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
     return np.array([L.oo_uniform(seed, stream, i) for i in range(n)])
+
+
+class RefQuadForest:
+    """The reference's own TMRQuadForest (oracle/_ref/libtmrref.so), the
+    checker of the quadtree twin."""
+
+    def __init__(self, order=2, interp=1, _handle=None, _conn=None):
+        self.L = _lib("ref")
+        for name in ("qforest_create", "qcoarsen", "qduplicate", "qcreate_interp"):
+            getattr(self.L.lib, "tmrref_" + name).restype = _V
+        self.h = _handle if _handle is not None else self.L.qforest_create(order, interp)
+        self.conn = _conn
+        self.order = order
+
+    def __del__(self):
+        try:
+            self.L.qforest_destroy(_V(self.h))
+        except Exception:
+            pass
+
+    def setConnectivity(self, conn):
+        conn = np.ascontiguousarray(conn, dtype=np.int32)
+        self.conn = conn
+        self.L.qset_connectivity(_V(self.h), int(conn.max()) + 1, _p(conn), conn.shape[0])
+
+    def createTrees(self, level):
+        self.L.qcreate_trees(_V(self.h), level)
+
+    def refine(self, refine=None, min_lev=0, max_lev=30):
+        if refine is None:
+            self.L.qrefine(_V(self.h), None, min_lev, max_lev)
+        else:
+            r = np.ascontiguousarray(refine, dtype=np.int32)
+            self.L.qrefine(_V(self.h), _p(r), min_lev, max_lev)
+
+    def balance(self, corner=1):
+        self.L.qbalance(_V(self.h), corner)
+
+    def coarsen(self):
+        return RefQuadForest(self.order, _handle=self.L.qcoarsen(_V(self.h)), _conn=self.conn)
+
+    def duplicate(self):
+        return RefQuadForest(self.order, _handle=self.L.qduplicate(_V(self.h)), _conn=self.conn)
+
+    def setMeshOrder(self, order, interp=1):
+        self.order = order
+        self.L.qset_mesh_order(_V(self.h), order, interp)
+
+    def createNodes(self):
+        self.L.qcreate_nodes(_V(self.h))
+
+    def getQuadrants(self):
+        """(n, 6) int32 array of {face, x, y, tag, level, info}."""
+        n = self.L.qnum_quads(_V(self.h))
+        out = np.zeros((n, 6), np.int32)
+        if n:
+            self.L.qget_quads(_V(self.h), _p(out))
+        return out
+
+    def nodeSizes(self):
+        s = np.zeros(6, np.int32)
+        self.L.qnode_sizes(_V(self.h), _p(s))
+        return dict(num_local=int(s[0]), num_owned=int(s[1]), num_dep=int(s[2]),
+                    ext_pre=int(s[3]), num_elements=int(s[4]), dep_nnz=int(s[5]))
+
+    def getMeshConn(self):
+        s = self.nodeSizes()
+        out = np.zeros(s["num_elements"] * self.order ** 2, np.int32)
+        if out.size:
+            self.L.qget_conn(_V(self.h), _p(out))
+        return out.reshape(s["num_elements"], self.order ** 2)
+
+    def getNodeNumbers(self):
+        s = self.nodeSizes()
+        out = np.zeros(s["num_local"], np.int32)
+        if out.size:
+            self.L.qget_node_numbers(_V(self.h), _p(out))
+        return out
+
+    def getDepNodeConn(self):
+        s = self.nodeSizes()
+        ptr = np.zeros(s["num_dep"] + 1, np.int32)
+        conn = np.zeros(max(s["dep_nnz"], 1), np.int32)
+        w = np.zeros(max(s["dep_nnz"], 1), np.float64)
+        self.L.qget_dep(_V(self.h), _p(ptr), _p(conn), _p(w))
+        return ptr, conn[: s["dep_nnz"]], w[: s["dep_nnz"]]
+
+    def getConnectivity(self):
+        nf = len(self.conn)
+        sizes = np.zeros(3, np.int32)
+        fc = np.zeros(4 * nf, np.int32)
+        fe = np.zeros(4 * nf, np.int32)
+        self.L.qget_connectivity(_V(self.h), _p(sizes), _p(fc), _p(fe))
+        return sizes, fc.reshape(nf, 4), fe.reshape(nf, 4)
+
+    def createInterpolation(self, coarse):
+        """(rows, ptr, cols, weights) records of the addInterp calls."""
+        h = self.L.qcreate_interp(_V(self.h), _V(coarse.h))
+        s = np.zeros(2, np.int32)
+        self.L.interp_sizes(_V(h), _p(s))
+        rows = np.zeros(max(s[0], 1), np.int32)
+        end = np.zeros(max(s[0], 1), np.int32)
+        cols = np.zeros(max(s[1], 1), np.int32)
+        w = np.zeros(max(s[1], 1), np.float64)
+        self.L.interp_get(_V(h), _p(rows), _p(end), _p(cols), _p(w))
+        self.L.interp_destroy(_V(h))
+        ptr = np.concatenate([[0], end[: s[0]]]).astype(np.int32)
+        return rows[: s[0]], ptr, cols[: s[1]], w[: s[1]]

@@ -222,7 +222,27 @@ def make_stl_golden():
     print("->", out, os.path.getsize(out), "bytes")
 
 
+def make_quad_golden():
+    """tests/golden/quad_<case>.npz: the reference's own TMRQuadForest
+    (oracle/_ref) on the quadtree parity cases (tests/pipeline.py
+    quad_cases)."""
+    for name, case in pipeline.quad_cases().items():
+        r = pipeline.run_quad_ref(case)
+        arrs = {"meta": np.array(case_meta(case)), "face_conn": case["conn"],
+                "quads": r["quads"], "conn": r["conn"], "dep_ptr": r["dep"][0],
+                "dep_conn": r["dep"][1], "dep_w": r["dep"][2]}
+        for k, lv in enumerate(r["levels"]):
+            arrs["L%d_quads" % k] = lv["quads"]
+            arrs["L%d_conn" % k] = lv["conn"]
+            arrs["L%d_dep_ptr" % k], arrs["L%d_dep_conn" % k], arrs["L%d_dep_w" % k] = lv["dep"]
+            arrs["L%d_P_rowptr" % k], arrs["L%d_P_cols" % k], arrs["L%d_P_vals" % k] = lv["P"]
+        out = os.path.join(HERE, "quad_" + name + ".npz")
+        np.savez_compressed(out, **arrs)
+        print("quad", name, len(r["quads"]), "quadrants ->", os.path.getsize(out), "bytes")
+
+
 if __name__ == "__main__":
     main()
     make_api_golden()
     make_stl_golden()
+    make_quad_golden()

@@ -134,7 +134,7 @@ def golden_cases():
     single-call getters and the STL output and are read by their own
     tests)."""
     return sorted(f[:-4] for f in os.listdir(GOLDEN_DIR)
-                  if f.endswith(".npz") and not f.startswith("api"))
+                  if f.endswith(".npz") and not f.startswith(("api", "quad_")))
 
 
 def load_golden(name):
@@ -232,3 +232,136 @@ def stl_field(P, vpn):
     f = np.sin(2.0 * P[:, 0]) * np.cos(1.5 * P[:, 1]) + 0.3 * P[:, 2]
     comps = [f, 0.2 - f][:vpn]
     return np.stack(comps, 1).ravel()
+
+
+# ---------------------------------------------------------------------------
+# Quadtree (2-D twin) parity cases.
+def quad_cases():
+    return {
+        "brick_o2": dict(conn=W.brick2d(4, 3), order=2, L0=1, passes=4, max_level=8,
+                         prob=0.3, seed=7, coarse_levels=2),
+        "brick_o3": dict(conn=W.brick2d(3, 2), order=3, L0=1, passes=4, max_level=7,
+                         prob=0.3, seed=8, coarse_levels=2),
+        "rot_o2": dict(conn=W.rotate_faces(W.brick2d(4, 4), 3), order=2, L0=1, passes=4,
+                       max_level=7, prob=0.3, seed=9, coarse_levels=1),
+        "rot_o3": dict(conn=W.rotate_faces(W.brick2d(3, 3), 4), order=3, L0=1, passes=3,
+                       max_level=6, prob=0.35, seed=10, coarse_levels=2),
+        "nocorner_o2": dict(conn=W.rotate_faces(W.brick2d(3, 3), 5), order=2, L0=1,
+                            passes=4, max_level=7, prob=0.3, seed=11, corner=0,
+                            coarse_levels=1),
+        "uniform_o3": dict(conn=W.brick2d(2, 2), order=3, L0=2, passes=3, max_level=6,
+                           prob=0.3, seed=12, interp=0, coarse_levels=1),
+        "mixed_o2": dict(conn=W.rotate_faces(W.brick2d(4, 3), 6), order=2, L0=2, passes=3,
+                         max_level=6, indicator="mixed", prob=0.35, coarsen_prob=0.3, seed=13,
+                         coarse_levels=2),
+    }
+
+
+def _quad_run(f, case, make_interp):
+    for p in range(case["passes"]):
+        q = f.getQuadrantsArray() if hasattr(f, "getQuadrantsArray") else f.getQuadrants()
+        f.refine(indicator(q, case, p), 0, case["max_level"])
+        f.balance(case.get("corner", 1))
+    f.createNodes()
+    out = dict(quads=_quads(f), conn=f.getMeshConn(), dep=f.getDepNodeConn(), levels=[])
+    c = f
+    for _ in range(case.get("coarse_levels", 1)):
+        cc = c.coarsen()
+        cc.balance(case.get("corner", 1))
+        cc.createNodes()
+        out["levels"].append(dict(quads=_quads(cc), conn=cc.getMeshConn(),
+                                  dep=cc.getDepNodeConn(), P=make_interp(c, cc)))
+        c = cc
+    return out
+
+
+def _quads(f):
+    q = f.getQuadrantsArray() if hasattr(f, "getQuadrantsArray") else f.getQuadrants()
+    q = np.array(q, np.int32).copy()
+    q[:, 3] = 0  # the tag column is bookkeeping (element index on the GPU)
+    return q
+
+
+def run_quad_gpu(case):
+    from tmr_gb300 import TMR
+    f = TMR.QuadForest(order=case["order"], interp=case.get("interp", 1))
+    f.setConnectivity(case["conn"])
+    f.createTrees(case["L0"])
+
+    def interp(fine, coarse):
+        I = TMR.VecInterp()
+        fine.createInterpolation(coarse, I)
+        return I.getCSR()
+    return _quad_run(f, case, interp)
+
+
+def run_quad_ref(case):
+    from oracle.oracle import RefQuadForest
+    f = RefQuadForest(case["order"], case.get("interp", 1))
+    f.setConnectivity(case["conn"])
+    f.createTrees(case["L0"])
+
+    def interp(fine, coarse):
+        rows, ptr, cols, w = fine.createInterpolation(coarse)
+        return _csr_from_records(rows, ptr, cols, w, fine.nodeSizes()["num_owned"])
+    return _quad_run(f, case, interp)
+
+
+def load_quad_golden(name):
+    z = np.load(os.path.join(GOLDEN_DIR, "quad_" + name + ".npz"))
+    out = dict(quads=z["quads"], conn=z["conn"], dep=(z["dep_ptr"], z["dep_conn"], z["dep_w"]),
+               levels=[])
+    k = 0
+    while "L%d_quads" % k in z:
+        out["levels"].append(dict(quads=z["L%d_quads" % k], conn=z["L%d_conn" % k],
+                                  dep=(z["L%d_dep_ptr" % k], z["L%d_dep_conn" % k],
+                                       z["L%d_dep_w" % k]),
+                                  P=(z["L%d_P_rowptr" % k], z["L%d_P_cols" % k],
+                                     z["L%d_P_vals" % k])))
+        k += 1
+    return out
+
+
+def compare_quad(a, b):
+    """Differences between two quadtree pipeline results (empty = equal):
+    integers bit-exact, weights within 1e-13 relative (observed equal)."""
+    bad = []
+
+    def arr(name, x, y, tol=None):
+        x, y = np.asarray(x), np.asarray(y)
+        if x.shape != y.shape:
+            bad.append("%s shape %s != %s" % (name, x.shape, y.shape))
+        elif tol is None:
+            if not np.array_equal(x, y):
+                bad.append("%s differs at %d entries" % (name, int((x != y).sum())))
+        elif x.size and np.abs(x - y).max() > tol * max(1.0, np.abs(y).max()):
+            bad.append("%s max diff %g" % (name, np.abs(x - y).max()))
+
+    def level(pfx, A, B):
+        arr(pfx + "quads", A["quads"], B["quads"])
+        arr(pfx + "conn", A["conn"], B["conn"])
+        for j, nm in enumerate(("dep_ptr", "dep_conn")):
+            arr(pfx + nm, A["dep"][j], B["dep"][j])
+        arr(pfx + "dep_w", A["dep"][2], B["dep"][2], 1e-13)
+    level("", a, b)
+    if len(a["levels"]) != len(b["levels"]):
+        bad.append("levels %d != %d" % (len(a["levels"]), len(b["levels"])))
+    for k, (A, B) in enumerate(zip(a["levels"], b["levels"])):
+        level("L%d_" % k, A, B)
+        arr("L%d_P_rowptr" % k, A["P"][0], B["P"][0])
+        arr("L%d_P_cols" % k, A["P"][1], B["P"][1])
+        arr("L%d_P_vals" % k, A["P"][2], B["P"][2], 1e-13)
+    return bad
+
+
+def quad_golden_case(name):
+    """The quadtree parity case as stored with its fixture."""
+    z = np.load(os.path.join(GOLDEN_DIR, "quad_" + name + ".npz"))
+    case = json.loads(str(z["meta"]))
+    case["conn"] = z["face_conn"]
+    return case
+
+
+def quad_golden_names():
+    return sorted(f[5:-4] for f in os.listdir(GOLDEN_DIR)
+                  if f.startswith("quad_") and f.endswith(".npz"))

@@ -450,6 +450,246 @@ class OctForest:
             fp.write("12\n" * len(o))
 
 
+class Quadrant:
+    """TMRQuadrant value (TMRQuadrant.h:36-52)."""
+
+    __slots__ = ("face", "x", "y", "tag", "level", "info")
+
+    def __init__(self, face=0, x=0, y=0, tag=0, level=0, info=0):
+        self.face, self.x, self.y = face, x, y
+        self.tag, self.level, self.info = tag, level, info
+
+    def __repr__(self):
+        return "Quadrant(face=%d, x=%d, y=%d, tag=%d, level=%d, info=%d)" % (
+            self.face, self.x, self.y, self.tag, self.level, self.info)
+
+
+class QuadrantArray:
+    """A forest's quadrants (TMR.pyx QuadrantArray) over an (n, 6) int32
+    array {face, x, y, tag, level, info}."""
+
+    def __init__(self, arr):
+        self.array = arr
+
+    def __len__(self):
+        return self.array.shape[0]
+
+    def __getitem__(self, k):
+        n = len(self)
+        if k < 0 or k >= n:
+            raise IndexError("Quadrant array index %d out of range [0,%d)" % (k, n))
+        return Quadrant(*(int(v) for v in self.array[k]))
+
+
+class QuadForest:
+    """Forest of quadtrees on one GPU (TMRQuadForest, TMR.pyx QuadForest):
+    mesh orders 2 and 3, Gauss-Lobatto or uniform knots."""
+
+    def __init__(self, comm=None, order=2, interp=GAUSS_LOBATTO_POINTS, stream=None,
+                 _handle=None):
+        self.comm = comm
+        self._stream = stream
+        if _handle is not None:
+            self.ptr = _handle
+        else:
+            h = _vp()
+            st = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
+            call("tmrg_qforest_create", order, interp, _vp(st), ctypes.byref(h))
+            self.ptr = h
+
+    def __del__(self):
+        try:
+            if getattr(self, "ptr", None):
+                lib().tmrg_qforest_destroy(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+    def _child(self, name):
+        h = _vp()
+        call(name, self.ptr, ctypes.byref(h))
+        return QuadForest(self.comm, stream=self._stream, _handle=h)
+
+    def setMeshOrder(self, order, interp=GAUSS_LOBATTO_POINTS):
+        call("tmrg_qforest_set_mesh_order", self.ptr, order, interp)
+
+    def _order(self):
+        o, t = ctypes.c_int(), ctypes.c_int()
+        k = np.zeros(3)
+        call("tmrg_qforest_get_mesh_order", self.ptr, ctypes.byref(o), ctypes.byref(t), _ptr(k))
+        return o.value, t.value, k[: o.value]
+
+    def getMeshOrder(self):
+        return self._order()[0]
+
+    def getInterpType(self):
+        return self._order()[1]
+
+    def getInterpKnots(self):
+        return self._order()[2]
+
+    def setConnectivity(self, conn):
+        conn = np.ascontiguousarray(conn, dtype=np.intc)
+        if conn.ndim != 2 or conn.shape[1] != 4:
+            raise ValueError("Expected array of shape (n, 4)")
+        call("tmrg_qforest_set_connectivity", self.ptr, int(conn.max()) + 1, _ptr(conn),
+             conn.shape[0])
+
+    def setFullConnectivity(self, conn, edge_conn, num_nodes=None, num_edges=None):
+        conn = np.ascontiguousarray(conn, dtype=np.intc)
+        ec = np.ascontiguousarray(edge_conn, dtype=np.intc)
+        if conn.shape != ec.shape or conn.shape[1] != 4:
+            raise ValueError("Expected arrays of shape (n, 4)")
+        nn = int(conn.max()) + 1 if num_nodes is None else num_nodes
+        ne = int(ec.max()) + 1 if num_edges is None else num_edges
+        call("tmrg_qforest_set_full_connectivity", self.ptr, nn, ne, conn.shape[0], _ptr(conn),
+             _ptr(ec))
+
+    def getConnectivity(self):
+        """(face_conn (n, 4), face_edge_conn (n, 4), num_nodes, num_edges)."""
+        sz = np.zeros(3, np.intc)
+        call("tmrg_qforest_get_connectivity", self.ptr, _ptr(sz), None, None)
+        fc = np.zeros((sz[0], 4), np.intc)
+        fe = np.zeros((sz[0], 4), np.intc)
+        call("tmrg_qforest_get_connectivity", self.ptr, _ptr(sz), _ptr(fc), _ptr(fe))
+        return fc, fe, int(sz[2]), int(sz[1])
+
+    def createTrees(self, depth=0):
+        call("tmrg_qforest_create_trees", self.ptr, depth)
+
+    def refine(self, refine=None, min_lev=0, max_lev=MAX_LEVEL):
+        if refine is None:
+            call("tmrg_qforest_refine", self.ptr, None, 0, min_lev, max_lev)
+        elif _is_torch(refine) and refine.is_cuda:
+            import torch
+            r = refine.to(torch.int32).contiguous()
+            call("tmrg_qforest_refine_device", self.ptr, _vp(r.data_ptr()), r.numel(),
+                 min_lev, max_lev)
+        else:
+            r = np.ascontiguousarray(refine, dtype=np.intc)
+            call("tmrg_qforest_refine", self.ptr, _ptr(r), r.size, min_lev, max_lev)
+
+    def duplicate(self):
+        return self._child("tmrg_qforest_duplicate")
+
+    def coarsen(self):
+        return self._child("tmrg_qforest_coarsen")
+
+    def balance(self, btype=0):
+        call("tmrg_qforest_balance", self.ptr, btype)
+
+    def createNodes(self):
+        call("tmrg_qforest_create_nodes", self.ptr)
+
+    def getNumQuadrants(self):
+        n = ctypes.c_int64(0)
+        call("tmrg_qforest_num_quadrants", self.ptr, ctypes.byref(n))
+        return n.value
+
+    def getQuadrantsArray(self):
+        """(n, 6) int32 {face, x, y, tag, level, info} in element order."""
+        n = self.getNumQuadrants()
+        out = np.zeros((n, 6), np.intc)
+        if n:
+            call("tmrg_qforest_get_quadrants", self.ptr, _ptr(out))
+        return out
+
+    def getQuadrants(self):
+        return QuadrantArray(self.getQuadrantsArray())
+
+    def _sizes(self):
+        s = np.zeros(6, np.int64)
+        call("tmrg_qforest_sizes", self.ptr, _ptr(s))
+        return s
+
+    def getNodeRange(self):
+        return np.array([0, int(self._sizes()[1])], np.intc)
+
+    def getExtPreOffset(self):
+        return int(self._sizes()[3])
+
+    def getMeshConn(self):
+        s = self._sizes()
+        o = self.getMeshOrder()
+        out = np.zeros((int(s[4]), o * o), np.intc)
+        call("tmrg_qforest_get_node_conn", self.ptr, _ptr(out))
+        return out
+
+    def getDepNodeConn(self):
+        s = self._sizes()
+        nd, nnz = int(s[2]), int(s[5])
+        ptr = np.zeros(nd + 1, np.intc)
+        conn = np.zeros(max(nnz, 1), np.intc)
+        w = np.zeros(max(nnz, 1), np.float64)
+        call("tmrg_qforest_get_dep_node_conn", self.ptr, _ptr(ptr), _ptr(conn), _ptr(w))
+        return ptr, conn[:nnz], w[:nnz]
+
+    def getNodeNumbers(self):
+        """The local node numbers, sorted (dependent nodes negative)."""
+        s = self._sizes()
+        return np.arange(-int(s[2]), int(s[1]), dtype=np.intc)
+
+    def getLocalNodeNumber(self, node):
+        s = self._sizes()
+        return int(node) + int(s[2]) if -int(s[2]) <= node < int(s[1]) else -1
+
+    def createInterpolation(self, forest, vec):
+        """P from `forest` (coarse) to this forest, into the VecInterp `vec`."""
+        h = _vp()
+        call("tmrg_qforest_create_interpolation", self.ptr, forest.ptr, ctypes.byref(h))
+        vec.ptr = h
+        return vec
+
+    def setFaceBoxes(self, boxes):
+        """A box (origin x, y, extent x, y) per face: the geometry getPoints
+        maps nodes through; None removes it."""
+        if boxes is None:
+            call("tmrg_qforest_set_face_boxes", self.ptr, None, 0)
+            return
+        b = np.ascontiguousarray(boxes, dtype=np.float64)
+        if b.ndim != 2 or b.shape[1] != 4:
+            raise ValueError("Expected array of shape (n, 4)")
+        call("tmrg_qforest_set_face_boxes", self.ptr, _ptr(b), b.shape[0])
+
+    def getPoints(self):
+        s = self._sizes()
+        X = np.zeros((int(s[0]), 3))
+        call("tmrg_qforest_get_points", self.ptr, _ptr(X))
+        return X
+
+    def evalInterp(self, pt, derivs=0):
+        """TMRQuadForest::evalInterp (:1069-1160) for the Lagrange knots:
+        N (and the d/du, d/dv tables with derivs=1) at the parametric point
+        pt in [-1, 1]^2, N[i + j order] = Nu[i] Nv[j]."""
+        o = self.getMeshOrder()
+        k = self.getInterpKnots()
+
+        def lag(u):
+            # lagrange_shape_func_derivative (TMRInterpolation.h), same
+            # operation order
+            N = [1.0] * o
+            D = [0.0] * o
+            for i in range(o):
+                for j in range(o):
+                    if i != j:
+                        d = 1.0 / (k[i] - k[j])
+                        N[i] *= (u - k[j]) * d
+                        for m in range(o):
+                            if m != i and m != j:
+                                d *= (u - k[m]) / (k[i] - k[m])
+                        D[i] += d
+            return N, D
+        k = [float(v) for v in k]
+        Nu, Du = lag(float(pt[0]))
+        Nv, Dv = lag(float(pt[1]))
+        N = np.array([Nu[i] * Nv[j] for j in range(o) for i in range(o)])
+        if not derivs:
+            return N
+        N1 = np.array([Du[i] * Nv[j] for j in range(o) for i in range(o)])
+        N2 = np.array([Nu[i] * Dv[j] for j in range(o) for i in range(o)])
+        return N, N1, N2
+
+
 class VecInterp:
     """Prolongation operator P (fine rows x coarse columns); the TACS
     TACSBVecInterp role in TMR (createInterpolation target)."""

@@ -91,6 +91,28 @@ _SIGS = {
     "tmrg_filter_apply_f32_device": [c_vp, c_int, c_vp, c_vp],
     "tmrg_filter_apply_transpose_f32_device": [c_vp, c_int, c_vp, c_vp],
     "tmrg_filter_apply_static_device": [c_vp, c_int, c_int, c_vp, c_vp],
+    "tmrg_qforest_create": [c_int, c_int, c_vp, P(c_vp)],
+    "tmrg_qforest_destroy": [c_vp],
+    "tmrg_qforest_set_connectivity": [c_vp, c_int, c_vp, c_int],
+    "tmrg_qforest_set_full_connectivity": [c_vp, c_int, c_int, c_int, c_vp, c_vp],
+    "tmrg_qforest_get_connectivity": [c_vp, c_vp, c_vp, c_vp],
+    "tmrg_qforest_set_mesh_order": [c_vp, c_int, c_int],
+    "tmrg_qforest_get_mesh_order": [c_vp, c_vp, c_vp, c_vp],
+    "tmrg_qforest_create_trees": [c_vp, c_int],
+    "tmrg_qforest_refine": [c_vp, c_vp, c_i64, c_int, c_int],
+    "tmrg_qforest_refine_device": [c_vp, c_vp, c_i64, c_int, c_int],
+    "tmrg_qforest_coarsen": [c_vp, P(c_vp)],
+    "tmrg_qforest_duplicate": [c_vp, P(c_vp)],
+    "tmrg_qforest_balance": [c_vp, c_int],
+    "tmrg_qforest_create_nodes": [c_vp],
+    "tmrg_qforest_num_quadrants": [c_vp, c_vp],
+    "tmrg_qforest_get_quadrants": [c_vp, c_vp],
+    "tmrg_qforest_sizes": [c_vp, c_vp],
+    "tmrg_qforest_get_node_conn": [c_vp, c_vp],
+    "tmrg_qforest_get_dep_node_conn": [c_vp, c_vp, c_vp, c_vp],
+    "tmrg_qforest_create_interpolation": [c_vp, c_vp, P(c_vp)],
+    "tmrg_qforest_set_face_boxes": [c_vp, c_vp, c_int],
+    "tmrg_qforest_get_points": [c_vp, c_vp],
     "tmrg_stl_triangles": [c_vp, c_vp, c_int, c_int, c_dbl, c_vp, c_vp, c_i64],
     "tmrg_stl_triangles_device": [c_vp, c_vp, c_int, c_int, c_dbl, c_vp, c_vp, c_i64],
     "tmrg_generate_bin_file": [ctypes.c_char_p, c_vp, c_vp, c_int, c_int, c_dbl],

@@ -24,6 +24,7 @@ SOURCES = [
     "tmrg_filter.cu",
     "tmrg_helmholtz.cu",
     "tmrg_stl.cu",
+    "tmrg_quad.cu",
     "tmrg_capi.cu",
 ]
 

@@ -9,6 +9,7 @@
 
 #include "tmrg_internal.h"
 #include "tmrg_helmholtz.h"
+#include "tmrg_quad.h"
 
 using namespace tmrg;
 
@@ -91,6 +92,9 @@ struct tmrg_filter {
 };
 struct tmrg_helmholtz {
   Helmholtz H;
+};
+struct tmrg_qforest {
+  QForest f;
 };
 
 static thread_local std::string g_last_error;
@@ -1152,6 +1156,246 @@ int tmrg_filter_apply_static_device(tmrg_filter *F, int transpose, int vpn,
   return guarded([&] {
     ARG(F && in && out && vpn > 0, "bad argument");
     filter_apply_static(F->F, transpose != 0, vpn, in, out);
+  });
+}
+
+// ---- quadtree forest ----------------------------------------------------
+static QForest &QF(tmrg_qforest *f) {
+  if (!f) throw Error(TMRG_ERR_ARG, "NULL quadtree forest");
+  return f->f;
+}
+int tmrg_qforest_create(int order, int interp, void *cuda_stream, tmrg_qforest **out) {
+  return guarded([&] {
+    ARG(out, "NULL argument");
+    auto *h = new tmrg_qforest;
+    h->f.s = (cudaStream_t)cuda_stream;
+    try {
+      h->f.set_order(order, interp);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+int tmrg_qforest_destroy(tmrg_qforest *f) {
+  return guarded([&] {
+    if (!f) return;
+    cudaStreamSynchronize(f->f.s);
+    delete f;
+  });
+}
+int tmrg_qforest_set_connectivity(tmrg_qforest *f, int num_nodes, const int *face_conn,
+                                  int num_faces) {
+  return guarded([&] {
+    ARG(face_conn, "NULL connectivity");
+    QForest &F = QF(f);
+    F.free_nodes();
+    F.have_quads = false;
+    F.n = 0;
+    F.conn = qconn_build(num_nodes, face_conn, num_faces, nullptr, 0, F.s);
+  });
+}
+int tmrg_qforest_set_full_connectivity(tmrg_qforest *f, int num_nodes, int num_edges,
+                                       int num_faces, const int *face_conn,
+                                       const int *face_edge_conn) {
+  return guarded([&] {
+    ARG(face_conn && face_edge_conn && num_edges > 0, "bad argument");
+    QForest &F = QF(f);
+    F.free_nodes();
+    F.have_quads = false;
+    F.n = 0;
+    F.conn = qconn_build(num_nodes, face_conn, num_faces, face_edge_conn, num_edges, F.s);
+  });
+}
+int tmrg_qforest_get_connectivity(tmrg_qforest *f, int *sizes3, int *face_conn,
+                                  int *face_edge_conn) {
+  return guarded([&] {
+    QForest &F = QF(f);
+    ARG(F.conn, "no connectivity");
+    const QConn &C = *F.conn;
+    if (sizes3) {
+      sizes3[0] = C.nf;
+      sizes3[1] = C.num_edges;
+      sizes3[2] = C.num_nodes;
+    }
+    if (face_conn) memcpy(face_conn, C.face_conn.data(), sizeof(int) * C.face_conn.size());
+    if (face_edge_conn)
+      memcpy(face_edge_conn, C.face_edge.data(), sizeof(int) * C.face_edge.size());
+  });
+}
+int tmrg_qforest_set_mesh_order(tmrg_qforest *f, int order, int interp) {
+  return guarded([&] { QF(f).set_order(order, interp); });
+}
+int tmrg_qforest_get_mesh_order(tmrg_qforest *f, int *order, int *interp, double *knots) {
+  return guarded([&] {
+    QForest &F = QF(f);
+    if (order) *order = F.order;
+    if (interp) *interp = F.interp;
+    if (knots)
+      for (int i = 0; i < F.order; i++) knots[i] = F.knots[i];
+  });
+}
+int tmrg_qforest_create_trees(tmrg_qforest *f, int level) {
+  return guarded([&] { qforest_create_trees(QF(f), level); });
+}
+int tmrg_qforest_refine(tmrg_qforest *f, const int *refine, int64_t n, int min_level,
+                        int max_level) {
+  return guarded([&] {
+    QForest &F = QF(f);
+    if (!refine) {
+      qforest_refine(F, nullptr, 0, min_level, max_level);
+      return;
+    }
+    DBuf<int> d(std::max<int64_t>(n, 1), F.s);
+    if (n)
+      TMRG_CUDA(cudaMemcpyAsync(d.p, refine, sizeof(int) * n, cudaMemcpyHostToDevice, F.s));
+    qforest_refine(F, d.p, n, min_level, max_level);
+  });
+}
+int tmrg_qforest_refine_device(tmrg_qforest *f, const int *d_refine, int64_t n,
+                               int min_level, int max_level) {
+  return guarded([&] { qforest_refine(QF(f), d_refine, d_refine ? n : 0, min_level, max_level); });
+}
+int tmrg_qforest_coarsen(tmrg_qforest *f, tmrg_qforest **out) {
+  return guarded([&] {
+    ARG(out, "NULL argument");
+    QForest &F = QF(f);
+    auto *h = new tmrg_qforest;
+    h->f.s = F.s;
+    try {
+      qforest_coarsen(F, h->f);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+int tmrg_qforest_duplicate(tmrg_qforest *f, tmrg_qforest **out) {
+  return guarded([&] {
+    ARG(out, "NULL argument");
+    QForest &F = QF(f);
+    auto *h = new tmrg_qforest;
+    h->f.s = F.s;
+    try {
+      qforest_duplicate(F, h->f);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+int tmrg_qforest_balance(tmrg_qforest *f, int corner) {
+  return guarded([&] { qforest_balance(QF(f), corner); });
+}
+int tmrg_qforest_create_nodes(tmrg_qforest *f) {
+  return guarded([&] {
+    QForest &F = QF(f);
+    if (!F.have_quads)
+      throw Error(TMRG_ERR_STATE, "Cannot call createNodes(), no quadrants have been created");
+    qforest_create_nodes(F);
+  });
+}
+int tmrg_qforest_num_quadrants(tmrg_qforest *f, int64_t *n) {
+  return guarded([&] {
+    ARG(n, "NULL argument");
+    *n = QF(f).have_quads ? QF(f).n : 0;
+  });
+}
+// out: 6 ints per quadrant {face, x, y, tag, level, info}
+int tmrg_qforest_get_quadrants(tmrg_qforest *f, int *out) {
+  return guarded([&] {
+    QForest &F = QF(f);
+    ARG(out, "NULL argument");
+    const long long n = F.n;
+    std::vector<int> b(n), x(n), y(n);
+    std::vector<int16_t> l(n), in(n);
+    copy_d2h(b.data(), F.block.p, 4 * n, F.s);
+    copy_d2h(x.data(), F.x.p, 4 * n, F.s);
+    copy_d2h(y.data(), F.y.p, 4 * n, F.s);
+    copy_d2h(l.data(), F.level.p, 2 * n, F.s);
+    copy_d2h(in.data(), F.info.p, 2 * n, F.s);
+    for (long long i = 0; i < n; i++) {
+      int *o = out + 6 * i;
+      o[0] = b[i];
+      o[1] = x[i];
+      o[2] = y[i];
+      o[3] = (int)i;
+      o[4] = l[i];
+      o[5] = in[i];
+    }
+  });
+}
+// out6: {local nodes, owned nodes, dependent nodes, ext_pre, elements, dep nnz}
+int tmrg_qforest_sizes(tmrg_qforest *f, int64_t *out6) {
+  return guarded([&] {
+    QForest &F = QF(f);
+    ARG(out6, "NULL argument");
+    out6[0] = F.num_local;
+    out6[1] = F.num_owned;
+    out6[2] = F.num_dep;
+    out6[3] = F.num_dep;
+    out6[4] = F.have_quads ? F.n : 0;
+    out6[5] = F.dep_nnz;
+  });
+}
+int tmrg_qforest_get_node_conn(tmrg_qforest *f, int *conn) {
+  return guarded([&] {
+    QForest &F = QF(f);
+    ARG(conn && F.have_nodes, "no nodes (call createNodes)");
+    copy_d2h(conn, F.econn.p, sizeof(int) * F.n * F.order * F.order, F.s);
+  });
+}
+int tmrg_qforest_get_dep_node_conn(tmrg_qforest *f, int *ptr, int *conn, double *w) {
+  return guarded([&] {
+    QForest &F = QF(f);
+    ARG(F.have_nodes, "no nodes (call createNodes)");
+    if (ptr) copy_d2h(ptr, F.dep_ptr.p, sizeof(int) * (F.num_dep + 1), F.s);
+    if (conn) copy_d2h(conn, F.dep_conn.p, sizeof(int) * F.dep_nnz, F.s);
+    if (w) copy_d2h(w, F.dep_w.p, sizeof(double) * F.dep_nnz, F.s);
+  });
+}
+int tmrg_qforest_create_interpolation(tmrg_qforest *fine, tmrg_qforest *coarse,
+                                      tmrg_interp **out) {
+  return guarded([&] {
+    ARG(fine && coarse && out, "NULL argument");
+    auto *h = new tmrg_interp;
+    try {
+      qinterp_create(fine->f, coarse->f, h->I);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+int tmrg_qforest_set_face_boxes(tmrg_qforest *f, const double *boxes, int nboxes) {
+  return guarded([&] {
+    QForest &F = QF(f);
+    ARG(F.conn, "no connectivity");
+    QConn &C = *F.conn;
+    if (!boxes) {
+      C.boxes.clear();
+      C.d_boxes.release();
+      return;
+    }
+    ARG(nboxes == C.nf, "one box per face expected");
+    C.boxes.assign(boxes, boxes + 4 * (size_t)nboxes);
+    C.d_boxes.alloc(C.boxes.size(), F.s);
+    TMRG_CUDA(cudaMemcpyAsync(C.d_boxes.p, C.boxes.data(), sizeof(double) * C.boxes.size(),
+                              cudaMemcpyHostToDevice, F.s));
+    TMRG_CUDA(cudaStreamSynchronize(F.s));
+  });
+}
+int tmrg_qforest_get_points(tmrg_qforest *f, double *X) {
+  return guarded([&] {
+    QForest &F = QF(f);
+    ARG(X && F.have_nodes, "no nodes (call createNodes)");
+    DBuf<double> d(3 * std::max(1LL, F.num_local), F.s);
+    qforest_get_points(F, d.p);
+    copy_d2h(X, d.p, sizeof(double) * 3 * F.num_local, F.s);
   });
 }
 

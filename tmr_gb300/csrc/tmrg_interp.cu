@@ -804,7 +804,7 @@ static void build_elists(Forest &coarse, ElemLists &L, int *err, cudaStream_t s)
          (const int *)coarse.dep_conn.p, (const double *)coarse.dep_w.p,
          (const long long *)L.eoff.p, L.lcol.p, L.ldw.p, L.lkey.p, L.ekind.p, err);
 }
-static void interp_finish(Interp &I, long long nonzeros, cudaStream_t s);
+void interp_finish(Interp &I, long long nonzeros, cudaStream_t s);
 
 void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   Stage st("tmrg_create_interpolation");
@@ -912,7 +912,7 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
 // The apply structures of a finished P (rows, cols, nnz, rowptr, colidx,
 // vals set): the zero-free copy when P has exact zeros, the length-ordered
 // row permutation and P^T.
-static void interp_finish(Interp &I, long long nonzeros, cudaStream_t s) {
+void interp_finish(Interp &I, long long nonzeros, cudaStream_t s) {
   const long long rows = I.rows, nnz = I.nnz;
   // zero-free copy for the applies, when P has exact zeros  // worth a second copy only when zeros are a good part of P
   I.nnz_nz = (nnz - nonzeros) * 8 >= nnz ? nonzeros : nnz;

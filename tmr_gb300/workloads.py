@@ -112,3 +112,37 @@ C1 = dict(conn=lambda: brick(1, 1, 1), L0=4, passes=3, max_level=7, order=2,
 # to level 9, order 3, 4-level hierarchy, P/P^T on 16 vectors.
 C2 = dict(conn=lambda: brick(8, 4, 4), L0=2, passes=5, max_level=9, order=3,
           indicator="random", prob=0.3, seed=7, levels=4, nvec=16)
+
+
+def brick2d(nx, ny):
+    """Face connectivity of an nx x ny grid of unit squares: node (i, j) is
+    numbered i + (nx+1) j, face corners x fastest (the corner order of
+    TMRQuadForest.cpp:24-31)."""
+    conn = []
+    for j in range(ny):
+        for i in range(nx):
+            n0 = i + (nx + 1) * j
+            conn.append([n0, n0 + 1, n0 + nx + 1, n0 + nx + 2])
+    return np.array(conn, dtype=np.intc)
+
+
+def rotate_faces(conn, seed):
+    """Relabel each face's corners by a seeded symmetry of the square
+    (rotations and reflections), so that neighbouring faces meet with
+    reversed edges."""
+    # corner (a, b) of the square -> index a + 2b; the 8 symmetries as maps
+    # of (a, b)
+    maps = [lambda a, b: (a, b), lambda a, b: (1 - b, a), lambda a, b: (1 - a, 1 - b),
+            lambda a, b: (b, 1 - a), lambda a, b: (b, a), lambda a, b: (1 - a, b),
+            lambda a, b: (a, 1 - b), lambda a, b: (1 - b, 1 - a)]
+    rng = np.random.default_rng(seed)
+    out = np.array(conn, dtype=np.intc).copy()
+    for f in range(len(out)):
+        m = maps[int(rng.integers(0, 8))]
+        new = np.empty(4, np.intc)
+        for c in range(4):
+            a, b = c & 1, c >> 1
+            na, nb = m(a, b)
+            new[na + 2 * nb] = out[f, c]
+        out[f] = new
+    return out
