@@ -62,12 +62,13 @@ def parse():
                    help="fewer refinement passes: a smaller case for ncu captures")
     p.add_argument("--target", type=int, default=None,
                    help="helmholtz workload: analysis-forest octants (smaller case for ncu)")
-    p.add_argument("--workload", default="c2", choices=["c2", "c4", "c5", "helmholtz", "stl"],
+    p.add_argument("--workload", default="c2", choices=["c2", "c4", "c5", "helmholtz", "stl", "quad"],
                    help="c2: the multi-tree order-3 workload (default, the headline); "
                         "c4: 256 forests batched as one; "
                         "c5: the 200M-octant adaptive workload (one JSON line of its own); "
                         "helmholtz: the Helmholtz PDE filter on a 5-level filter hierarchy; "
-                        "stl: iso-surface triangles of a smoothed density")
+                        "stl: iso-surface triangles of a smoothed density; "
+                        "quad: the quadtree twin's pipeline")
     a = p.parse_args()
     if a.passes is not None:
         WORKLOAD["passes"] = a.passes
@@ -801,6 +802,120 @@ def run_stl(args):
     print(json.dumps(line), flush=True)
 
 
+# The quadtree configuration: a 64 x 64 grid of faces (4096 trees), three
+# uniform levels, five random refinement passes (p = 0.3) to level 11,
+# order 3 GLL, a 4-level hierarchy with P / P^T applied to 16 vectors.
+QUAD_WORKLOAD = dict(name="quad64x64_L3_p0.3x5_lvl11_order3_gll_4lvl_16vec",
+                     nx=64, ny=64, L0=3, passes=5, prob=0.3, seed=7, max_level=11, order=3,
+                     levels=4, nvec=16, corner=1)
+
+
+def quad_pipeline(TMR, conn, QW, x_fine):
+    f = TMR.QuadForest(order=QW["order"], interp=TMR.GAUSS_LOBATTO_POINTS)
+    f.setConnectivity(conn)
+    f.createTrees(QW["L0"])
+    for p in range(QW["passes"]):
+        n = f.getNumQuadrants()
+        f.refine(TMR.random_refinement(n, QW["seed"], p, QW["prob"]), 0, QW["max_level"])
+        f.balance(QW["corner"])
+    f.createNodes()
+    forests = [f]
+    for _ in range(QW["levels"] - 1):
+        c = forests[-1].coarsen()
+        c.balance(QW["corner"])
+        c.createNodes()
+        forests.append(c)
+    interps = []
+    for k in range(QW["levels"] - 1):
+        I = TMR.VecInterp()
+        forests[k].createInterpolation(forests[k + 1], I)
+        interps.append(I)
+    import torch
+    nv = QW["nvec"]
+    x = x_fine[: forests[0].getNodeRange()[1] * nv] if x_fine is not None else None
+    if x is not None:
+        for I in interps:
+            rows, cols, _ = I.sizes()
+            y = torch.empty(cols * nv, dtype=torch.float64, device="cuda")
+            I.multTranspose(x, y)
+            x = y
+        for I in reversed(interps):
+            rows, cols, _ = I.sizes()
+            y = torch.empty(rows * nv, dtype=torch.float64, device="cuda")
+            I.mult(x, y)
+            x = y
+    return sum(fr.getNumQuadrants() for fr in forests), forests, interps
+
+
+def run_quad(args):
+    """One JSON line for the quadtree configuration."""
+    import torch
+    from tmr_gb300 import TMR
+    from tmr_gb300 import build as tb
+    from tmr_gb300 import workloads as Wk
+    tb.build()
+    QW = QUAD_WORKLOAD
+    conn = Wk.brick2d(QW["nx"], QW["ny"])
+    # size the prolongation input once
+    _, fs, _ = quad_pipeline(TMR, conn, QW, None)
+    nfine = int(fs[0].getNodeRange()[1])
+    del fs
+    g = torch.Generator(device="cuda").manual_seed(QW["seed"])
+    x_fine = torch.rand(nfine * QW["nvec"], dtype=torch.float64, device="cuda", generator=g)
+    for _ in range(args.warmup):
+        quad_pipeline(TMR, conn, QW, x_fine)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    lc0 = TMR.kernel_launch_count()
+    e0.record()
+    units = 0
+    for _ in range(args.steps):
+        u, forests, interps = quad_pipeline(TMR, conn, QW, x_fine)
+        units += u
+    e1.record()
+    torch.cuda.synchronize()
+    launches = (TMR.kernel_launch_count() - lc0) // args.steps
+    ms = e0.elapsed_time(e1) / args.steps
+    L = TMR.lib()
+    L.tmrg_profile_begin()
+    quad_pipeline(TMR, conn, QW, x_fine)
+    buf = ctypes.create_string_buffer(1 << 20)
+    L.tmrg_profile_end(buf, len(buf))
+    prof = {k.strip("()"): v for k, v in json.loads(buf.value.decode()).items()}
+    tot_ms = sum(v[1] for v in prof.values())
+    top = max(prof.items(), key=lambda kv: kv[1][1])
+    peak, peak_kind = measured_peaks()
+    fp64 = ctypes.c_double(0.0)
+    L.tmrg_measure_fp64_peak(ctypes.byref(fp64))
+    roof = roofline_entry(top[0], top[1], peak, peak_kind, fp64.value, tot_ms)
+    levels = []
+    for k, fr in enumerate(forests):
+        e = {"quadrants": int(fr.getNumQuadrants()), "nodes": int(fr.getNodeRange()[1])}
+        if k < len(interps):
+            r, c, z = interps[k].sizes()
+            e["P_nnz"] = int(z)
+        levels.append(e)
+    line = {"metric": "balanced+numbered quadrants/s", "value": units / (ms * args.steps / 1e3)
+            * args.steps, "unit": "quadrants/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": QW["name"], "quadrants_per_step": units // args.steps,
+                       "hierarchy": levels},
+            "gpu_launches": launches,
+            "roofline": {k: roof[k] for k in ("bound", "achieved", "peak", "unit", "frac",
+                                              "traffic")},
+            "top_kernel": roof,
+            "kernel_shares": {k: round(v[1] / tot_ms, 4)
+                              for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:10]},
+            "cpu_baseline": {"unavailable": "the quadtree checker is the reference's own "
+                             "TMRQuadForest, built only where its sources are (not on the GPU "
+                             "host); its timing on the build host is recorded with the design "
+                             "notes"}}
+    line["value"] = units / (ms * args.steps / 1e3)
+    print(json.dumps(line), flush=True)
+
+
 def run_helmholtz(args):
     """One JSON line for the Helmholtz filter configuration."""
     import time
@@ -1325,6 +1440,8 @@ def main():
         run_helmholtz(args)
     elif args.workload == "stl":
         run_stl(args)
+    elif args.workload == "quad":
+        run_quad(args)
     else:
         run_gpu(args)
 

@@ -1155,7 +1155,18 @@ __global__ void k_q_pack(long long n, const int *__restrict__ b, const int *__re
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = make_int4(b[i] | ((int)l[i] << 26), x[i], y[i], 0);
 }
+// 2^e as a double from its exponent (exact; e >= -1022).
 __device__ __forceinline__ double q_pow2(int e) { return __hiloint2double((1023 + e) << 20, 0); }
+// A non-negative int32 as a double assembled from its bits with integer
+// operations (exactly (double)v): GB300 issues int-to-double conversions on
+// its FP64 pipe.
+__device__ __forceinline__ double q_exact(int32_t v) {
+  if (v <= 0) return 0.0;
+  const int e = 31 - __clz(v);
+  const unsigned long long m =
+      ((unsigned long long)(uint32_t)v << (52 - e)) & ((1ULL << 52) - 1ULL);
+  return __longlong_as_double((long long)(((unsigned long long)(1023 + e) << 52) | m));
+}
 // findEnclosing (:4338-4440)
 __device__ long long q_find_enclosing(const QInterpCtx &I, const Quad &node, int info) {
   const int order = I.fo;
@@ -1172,12 +1183,12 @@ __device__ long long q_find_enclosing(const QInterpCtx &I, const Quad &node, int
     yi = node.y + h / 2;
   int32_t xl = xi, xh = xi, yl = yi, yh = yi;
   if (xi < 0) {
-    double xd = __dadd_rn((double)node.x, __dmul_rn(q_pow2(TMRG_MAX_LEVEL - 1 - node.level), I.fk1[ii]));
+    double xd = __dadd_rn(q_exact(node.x), __dmul_rn(q_pow2(TMRG_MAX_LEVEL - 1 - node.level), I.fk1[ii]));
     xl = (int32_t)floor(xd);
     xh = (int32_t)ceil(xd);
   }
   if (yi < 0) {
-    double yd = __dadd_rn((double)node.y, __dmul_rn(q_pow2(TMRG_MAX_LEVEL - 1 - node.level), I.fk1[jj]));
+    double yd = __dadd_rn(q_exact(node.y), __dmul_rn(q_pow2(TMRG_MAX_LEVEL - 1 - node.level), I.fk1[jj]));
     yl = (int32_t)floor(yd);
     yh = (int32_t)ceil(yd);
   }
@@ -1211,8 +1222,9 @@ __device__ long long q_find_enclosing(const QInterpCtx &I, const Quad &node, int
   return -1;
 }
 // one direction of computeElemInterp (:4486-4640, Lagrange branch)
-__device__ __forceinline__ void q_dir(const QInterpCtx &I, int i, int32_t nx, int32_t h,
-                                      int32_t ox, int32_t hc, int &s, int &e, double *N) {
+__device__ __forceinline__ void q_dir(const QInterpCtx &I, int i, int32_t nx, int nlev,
+                                      int32_t ox, int clev, int &s, int &e, double *N) {
+  const int32_t h = side_of(nlev), hc = side_of(clev);
   const int mo = I.fo, co = I.co;
   if ((i == 0 && ox == nx) || (i == mo - 1 && ox == nx + h)) {
     s = 0;
@@ -1226,9 +1238,10 @@ __device__ __forceinline__ void q_dir(const QInterpCtx &I, int i, int32_t nx, in
     s = 0;
     e = co;
     // u = -1 + 2 (x + 0.5 h (1 + k_i) - ox) / hc: the scalings by 0.5 h and
-    // 2 / hc are powers of two, so they round as the reference's division
-    double t = __dadd_rn((double)nx, __dmul_rn(__dmul_rn(0.5, (double)h), I.fk1[i]));
-    double u = __dadd_rn(-1.0, __ddiv_rn(__dmul_rn(2.0, __dsub_rn(t, (double)ox)), (double)hc));
+    // 2 / hc are powers of two, so the products round as the reference's
+    // expression does
+    double t = __dadd_rn(q_exact(nx), __dmul_rn(q_pow2(TMRG_MAX_LEVEL - 1 - nlev), I.fk1[i]));
+    double u = __dadd_rn(-1.0, __dmul_rn(__dsub_rn(t, q_exact(ox)), q_pow2(clev - TMRG_MAX_LEVEL + 1)));
     for (int a = 0; a < co; a++) {
       double v = 1.0;
       for (int b = 0; b < co; b++)
@@ -1238,24 +1251,28 @@ __device__ __forceinline__ void q_dir(const QInterpCtx &I, int i, int32_t nx, in
   }
 }
 // the row's entries (uniqueSort: stable by column, duplicates summed in
-// order); returns the count, writes when cols != nullptr
-__device__ int q_row(const QInterpCtx &I, long long row, int *cols, double *w) {
+// order); returns the count, writes when cols != nullptr.  The enclosing
+// coarse element is searched when *tp < 0 and returned in *tp.
+__device__ int q_row(const QInterpCtx &I, long long row, int *tp, int *cols, double *w) {
   unsigned long long rr = I.rep[row];
   long long e = (long long)(rr >> 8);
   int info = (int)(rr & 255u);
   Quad node{I.fb[e], I.fx[e], I.fy[e], I.fl[e]};
-  long long t = q_find_enclosing(I, node, info);
+  long long t = *tp;
   if (t < 0) {
-    atomicExch(I.err, 1);
-    return 0;
+    t = q_find_enclosing(I, node, info);
+    if (t < 0) {
+      atomicExch(I.err, 1);
+      return 0;
+    }
+    *tp = (int)t;
   }
   int4 cq = I.c4[t];
-  const int32_t h = side_of(node.level), hc = side_of(cq.x >> 26);
   const int mo = I.fo, co = I.co;
   double Nu[3], Nv[3];
   int is, ie, js, je;
-  q_dir(I, info % mo, node.x, h, cq.y, hc, is, ie, Nu);
-  q_dir(I, info / mo, node.y, h, cq.z, hc, js, je, Nv);
+  q_dir(I, info % mo, node.x, node.level, cq.y, cq.x >> 26, is, ie, Nu);
+  q_dir(I, info / mo, node.y, node.level, cq.z, cq.x >> 26, js, je, Nv);
   int ic[27];
   double iw[27];
   int m = 0;
@@ -1300,18 +1317,26 @@ __device__ int q_row(const QInterpCtx &I, long long row, int *cols, double *w) {
   }
   return k;
 }
-__global__ void k_q_row_count(long long rows, QInterpCtx I, int *cnt) {
-  long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < rows) cnt[r] = q_row(I, r, nullptr, nullptr);
-}
-__global__ void k_q_row_fill(long long rows, QInterpCtx I, const int *__restrict__ rp, int *cols,
-                             double *w, unsigned long long *nonzero) {
+__global__ void k_q_row_count(long long rows, QInterpCtx I, int *cnt, int *encl) {
   long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= rows) return;
-  int k = q_row(I, r, cols + rp[r], w + rp[r]);
+  int t = -1;
+  cnt[r] = q_row(I, r, &t, nullptr, nullptr);
+  encl[r] = t;
+}
+__global__ void k_q_row_fill(long long rows, QInterpCtx I, const int *__restrict__ rp,
+                             const int *__restrict__ encl, int *cols, double *w,
+                             unsigned long long *nonzero) {
+  long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned nz = 0;
-  for (int a = 0; a < k; a++) nz += (w[rp[r] + a] != 0.0);
-  if (nz) atomicAdd(nonzero, (unsigned long long)nz);
+  if (r < rows) {
+    int t = encl[r];
+    int k = q_row(I, r, &t, cols + rp[r], w + rp[r]);
+    for (int a = 0; a < k; a++) nz += (w[rp[r] + a] != 0.0);
+  }
+  // one atomic per warp
+  for (int o = 16; o; o >>= 1) nz += __shfl_xor_sync(0xffffffffu, nz, o);
+  if ((threadIdx.x & 31) == 0 && nz) atomicAdd(nonzero, (unsigned long long)nz);
 }
 
 void qinterp_create(QForest &fine, QForest &coarse, Interp &I) {
@@ -1365,7 +1390,13 @@ void qinterp_create(QForest &fine, QForest &coarse, Interp &I) {
   c.rep = rep.p;
   c.err = err.p;
   DBuf<int> cnt(rows + 1, s);
-  launch(k_q_row_count, blocks_for(rows, 128), 128, 0, s, rows, c, cnt.p);
+  // compulsory per row: its reference entry, the fine element fields, the
+  // coarse element it lands in (packed quad and connectivity) and the row
+  // count (the fill pass adds 12 bytes per entry written)
+  const long long row_bytes = rows * (8LL + 14 + 16 + 4LL * coarse.order * coarse.order + 8);
+  prof_bytes(row_bytes);
+  DBuf<int> encl(std::max(1LL, rows), s);
+  launch(k_q_row_count, blocks_for(rows, 128), 128, 0, s, rows, c, cnt.p, encl.p);
   exclusive_scan<int>(cnt.p, cnt.p, rows, s);
   const long long nnz = read_scalar(cnt.p + rows, s);
   if (read_scalar(err.p, s))
@@ -1376,8 +1407,9 @@ void qinterp_create(QForest &fine, QForest &coarse, Interp &I) {
   I.vals.alloc(std::max(1LL, nnz), s);
   DBuf<unsigned long long> nzc(1, s);
   nzc.zero();
+  prof_bytes(row_bytes + 12 * nnz);
   launch(k_q_row_fill, blocks_for(rows, 128), 128, 0, s, rows, c, (const int *)I.rowptr.p,
-         I.colidx.p, I.vals.p, nzc.p);
+         (const int *)encl.p, I.colidx.p, I.vals.p, nzc.p);
   const long long nonzeros = (long long)read_scalar(nzc.p, s);
   interp_finish(I, nonzeros, s);
   TMRG_CUDA(cudaStreamSynchronize(s));
