@@ -728,6 +728,8 @@ def run_stl(args):
     tb.build()
     SW = STL_WORKLOAD
     HW = dict(HELMHOLTZ_WORKLOAD)
+    if args.target:
+        HW["target"] = args.target
     f, filters, boxes, r = helmholtz_setup(TMR, HW)
     F = filters[0]
     n = int(F.getNodeRange()[1])
@@ -750,6 +752,11 @@ def run_stl(args):
     def step():
         TMR.call("tmrg_stl_triangles_device", F.ptr, xp, 1, 0, SW["cutoff"], ctypes.byref(cnt),
                  op, ntri)
+    if args.profile_step:
+        step()
+        torch.cuda.synchronize()
+        print(json.dumps({"workload": SW["name"], "elements": ne, "triangles": ntri}))
+        return
     for _ in range(args.warmup):
         step()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -854,7 +861,10 @@ def run_quad(args):
     from tmr_gb300 import build as tb
     from tmr_gb300 import workloads as Wk
     tb.build()
-    QW = QUAD_WORKLOAD
+    QW = dict(QUAD_WORKLOAD)
+    if args.passes is not None:
+        QW["passes"] = args.passes
+        QW["name"] = QW["name"].replace("x5_", "x%d_" % args.passes)
     conn = Wk.brick2d(QW["nx"], QW["ny"])
     # size the prolongation input once
     _, fs, _ = quad_pipeline(TMR, conn, QW, None)
@@ -862,6 +872,11 @@ def run_quad(args):
     del fs
     g = torch.Generator(device="cuda").manual_seed(QW["seed"])
     x_fine = torch.rand(nfine * QW["nvec"], dtype=torch.float64, device="cuda", generator=g)
+    if args.profile_step:
+        u, _, _ = quad_pipeline(TMR, conn, QW, x_fine)
+        torch.cuda.synchronize()
+        print(json.dumps({"workload": QW["name"], "quadrants": u}))
+        return
     for _ in range(args.warmup):
         quad_pipeline(TMR, conn, QW, x_fine)
     torch.cuda.synchronize()
@@ -1411,21 +1426,28 @@ def run_e2e(TMR, conn, W, args, barrier, world, x_fine):
     steps = max(1, min(args.steps, 3))
     gpu_pipeline(TMR, conn, W, host=True, prefetched=pre)
     barrier()
-    t0 = time.perf_counter()
-    tot = 0
+    each = []
+    units = 0
     h2d = d2h = 0
     for _ in range(steps):
+        # every step bracketed by a barrier (host-synchronous API: the
+        # results are in host memory when the call returns)
+        t0 = time.perf_counter()
         u, o = gpu_pipeline(TMR, conn, W, host=True, prefetched=pre)
-        tot += u
+        barrier()
+        each.append(time.perf_counter() - t0)
+        units = u
         h2d, d2h = o["h2d"], o["d2h"]
-    barrier()
-    dt = time.perf_counter() - t0
     if world > 1:
-        t = torch.tensor([dt], device="cuda")
+        t = torch.tensor(each, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dt = float(t.item())
-    return {"value": tot * world / dt, "unit": "octants/s", "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "steps": steps, "ms_per_step": 1000 * dt / steps}
+        each = [float(v) for v in t.cpu()]
+    # the median step: the host link is shared with other jobs on the
+    # machine, so single steps can stall
+    dt = float(np.median(each))
+    return {"value": units * world / dt, "unit": "octants/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "steps": steps, "ms_per_step": 1000 * dt,
+            "statistic": "median step", "ms_each": [round(1000 * v, 2) for v in each]}
 
 
 def main():

@@ -1221,6 +1221,23 @@ __device__ long long q_find_enclosing(const QInterpCtx &I, const Quad &node, int
   }
   return -1;
 }
+// the coarse index range [s, e) of one direction (an exact hit of the
+// element's side keeps one index)
+__device__ __forceinline__ void q_range(const QInterpCtx &I, int i, int32_t nx, int nlev,
+                                        int32_t ox, int clev, int &s, int &e) {
+  const int mo = I.fo, co = I.co;
+  const int32_t h = side_of(nlev), hc = side_of(clev);
+  if ((i == 0 && ox == nx) || (i == mo - 1 && ox == nx + h)) {
+    s = 0;
+    e = 1;
+  } else if ((i == 0 && ox + hc == nx) || (i == mo - 1 && ox + hc == nx + h)) {
+    s = co - 1;
+    e = co;
+  } else {
+    s = 0;
+    e = co;
+  }
+}
 // one direction of computeElemInterp (:4486-4640, Lagrange branch)
 __device__ __forceinline__ void q_dir(const QInterpCtx &I, int i, int32_t nx, int nlev,
                                       int32_t ox, int clev, int &s, int &e, double *N) {
@@ -1251,8 +1268,10 @@ __device__ __forceinline__ void q_dir(const QInterpCtx &I, int i, int32_t nx, in
   }
 }
 // the row's entries (uniqueSort: stable by column, duplicates summed in
-// order); returns the count, writes when cols != nullptr.  The enclosing
-// coarse element is searched when *tp < 0 and returned in *tp.
+// order); returns the count, and with WEIGHTS writes the columns and
+// weights (the count pass needs only the columns).  The enclosing coarse
+// element is searched when *tp < 0 and returned in *tp.
+template <bool WEIGHTS>
 __device__ int q_row(const QInterpCtx &I, long long row, int *tp, int *cols, double *w) {
   unsigned long long rr = I.rep[row];
   long long e = (long long)(rr >> 8);
@@ -1271,47 +1290,57 @@ __device__ int q_row(const QInterpCtx &I, long long row, int *tp, int *cols, dou
   const int mo = I.fo, co = I.co;
   double Nu[3], Nv[3];
   int is, ie, js, je;
-  q_dir(I, info % mo, node.x, node.level, cq.y, cq.x >> 26, is, ie, Nu);
-  q_dir(I, info / mo, node.y, node.level, cq.z, cq.x >> 26, js, je, Nv);
+  if (WEIGHTS) {
+    q_dir(I, info % mo, node.x, node.level, cq.y, cq.x >> 26, is, ie, Nu);
+    q_dir(I, info / mo, node.y, node.level, cq.z, cq.x >> 26, js, je, Nv);
+  } else {
+    q_range(I, info % mo, node.x, node.level, cq.y, cq.x >> 26, is, ie);
+    q_range(I, info / mo, node.y, node.level, cq.z, cq.x >> 26, js, je);
+  }
   int ic[27];
-  double iw[27];
+  double iw[WEIGHTS ? 27 : 1];
   int m = 0;
   const int *c = I.cconn + t * co * co;
   for (int jj = js; jj < je; jj++)
     for (int ii = is; ii < ie; ii++) {
-      double wt = __dmul_rn(Nu[ii], Nv[jj]);
+      double wt = WEIGHTS ? __dmul_rn(Nu[ii], Nv[jj]) : 0.0;
       int g = c[ii + jj * co];
       if (g >= 0) {
         ic[m] = g;
-        iw[m++] = wt;
+        if (WEIGHTS) iw[m] = wt;
+        m++;
       } else {
         int d = -g - 1;
         for (int p = I.cdptr[d]; p < I.cdptr[d + 1] && m < 27; p++) {
           ic[m] = I.cdconn[p];
-          iw[m++] = __dmul_rn(wt, I.cdw[p]);
+          if (WEIGHTS) iw[m] = __dmul_rn(wt, I.cdw[p]);
+          m++;
         }
       }
     }
   // stable insertion sort by column
   for (int a = 1; a < m; a++) {
     int kc = ic[a];
-    double kw = iw[a];
+    double kw = WEIGHTS ? iw[a] : 0.0;
     int b = a - 1;
     while (b >= 0 && ic[b] > kc) {
       ic[b + 1] = ic[b];
-      iw[b + 1] = iw[b];
+      if (WEIGHTS) iw[b + 1] = iw[b];
       b--;
     }
     ic[b + 1] = kc;
-    iw[b + 1] = kw;
+    if (WEIGHTS) iw[b + 1] = kw;
   }
   int k = 0;
   for (int a = 0; a < m; a++) {
-    double s = iw[a];
-    while (a + 1 < m && ic[a + 1] == ic[a]) s = __dadd_rn(s, iw[++a]);
-    if (cols) {
+    double sum = WEIGHTS ? iw[a] : 0.0;
+    while (a + 1 < m && ic[a + 1] == ic[a]) {
+      ++a;
+      if (WEIGHTS) sum = __dadd_rn(sum, iw[a]);
+    }
+    if (WEIGHTS) {
       cols[k] = ic[a];
-      w[k] = s;
+      w[k] = sum;
     }
     k++;
   }
@@ -1321,7 +1350,7 @@ __global__ void k_q_row_count(long long rows, QInterpCtx I, int *cnt, int *encl)
   long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= rows) return;
   int t = -1;
-  cnt[r] = q_row(I, r, &t, nullptr, nullptr);
+  cnt[r] = q_row<false>(I, r, &t, nullptr, nullptr);
   encl[r] = t;
 }
 __global__ void k_q_row_fill(long long rows, QInterpCtx I, const int *__restrict__ rp,
@@ -1331,7 +1360,7 @@ __global__ void k_q_row_fill(long long rows, QInterpCtx I, const int *__restrict
   unsigned nz = 0;
   if (r < rows) {
     int t = encl[r];
-    int k = q_row(I, r, &t, cols + rp[r], w + rp[r]);
+    int k = q_row<true>(I, r, &t, cols + rp[r], w + rp[r]);
     for (int a = 0; a < k; a++) nz += (w[rp[r] + a] != 0.0);
   }
   // one atomic per warp
