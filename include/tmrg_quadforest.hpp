@@ -1,0 +1,259 @@
+/*
+  tmrg_quadforest.hpp — C++ host facade with the TMRQuadForest interface
+  (TMRQuadForest.h:43-161, TMRQuadrant.h:36-52), the STL tools
+  (TMR_STLTools.h:44-77) and TMRHelmholtzFilter (TMRHelmholtzFilter.h:31-61)
+  over the tmrg C ABI.  Header only; include after (or instead of)
+  tmrg_octforest.hpp, whose TMRGEntity, TMRGVecInterp, TMRPoint and error
+  reporting it shares.
+*/
+#ifndef TMRG_QUADFOREST_HPP
+#define TMRG_QUADFOREST_HPP
+
+#include <stdint.h>
+#include <stdio.h>
+
+#include <vector>
+
+#include "tmrg.h"
+#include "tmrg_octforest.hpp"
+
+// Same field layout as TMRQuadrant (TMRQuadrant.h:46-51).
+class TMRQuadrant {
+ public:
+  int32_t face, x, y, tag;
+  int16_t level, info;
+};
+
+// The quadrants (TMRQuadrantArray): a copy owned by the forest, valid until
+// the forest changes.
+class TMRQuadrantArray {
+ public:
+  void getArray(TMRQuadrant **a, int *size) {
+    if (a) *a = quads.data();
+    if (size) *size = (int)quads.size();
+  }
+  std::vector<TMRQuadrant> quads;
+};
+
+class TMRQuadForest : public TMRGEntity {
+ public:
+  explicit TMRQuadForest(int comm = 0, int mesh_order = 2,
+                         TMRInterpolationType interp_type = TMR_GAUSS_LOBATTO_POINTS,
+                         void *cuda_stream = nullptr)
+      : f(nullptr), stream(cuda_stream) {
+    (void)comm;
+    tmrg_report(tmrg_qforest_create(mesh_order, interp_type, stream, &f), "TMRQuadForest");
+  }
+  ~TMRQuadForest() { tmrg_qforest_destroy(f); }
+
+  void setConnectivity(int num_nodes, const int *face_conn, int num_faces) {
+    tmrg_report(tmrg_qforest_set_connectivity(f, num_nodes, face_conn, num_faces),
+                "setConnectivity");
+  }
+  void setFullConnectivity(int num_nodes, int num_edges, int num_faces, const int *face_conn,
+                           const int *face_edge_conn) {
+    tmrg_report(tmrg_qforest_set_full_connectivity(f, num_nodes, num_edges, num_faces,
+                                                   face_conn, face_edge_conn),
+                "setFullConnectivity");
+  }
+  void getConnectivity(int *nfaces, int *nedges, int *nnodes, const int **face_conn,
+                       const int **face_edge_conn) {
+    int sz[3] = {0, 0, 0};
+    tmrg_qforest_get_connectivity(f, sz, nullptr, nullptr);
+    fc_.assign(4 * (size_t)sz[0], 0);
+    fe_.assign(4 * (size_t)sz[0], 0);
+    tmrg_report(tmrg_qforest_get_connectivity(f, sz, fc_.data(), fe_.data()), "getConnectivity");
+    if (nfaces) *nfaces = sz[0];
+    if (nedges) *nedges = sz[1];
+    if (nnodes) *nnodes = sz[2];
+    if (face_conn) *face_conn = fc_.data();
+    if (face_edge_conn) *face_edge_conn = fe_.data();
+  }
+  void setMeshOrder(int mesh_order, TMRInterpolationType interp = TMR_GAUSS_LOBATTO_POINTS) {
+    tmrg_report(tmrg_qforest_set_mesh_order(f, mesh_order, interp), "setMeshOrder");
+  }
+  int getMeshOrder() {
+    int o = 2;
+    tmrg_qforest_get_mesh_order(f, &o, nullptr, nullptr);
+    return o;
+  }
+  TMRInterpolationType getInterpType() {
+    int t = 1;
+    tmrg_qforest_get_mesh_order(f, nullptr, &t, nullptr);
+    return (TMRInterpolationType)t;
+  }
+  int getInterpKnots(const double **knots) {
+    knots_.assign(3, 0.0);
+    int o = 2;
+    tmrg_qforest_get_mesh_order(f, &o, nullptr, knots_.data());
+    if (knots) *knots = knots_.data();
+    return o;
+  }
+  void createTrees(int refine_level) {
+    tmrg_report(tmrg_qforest_create_trees(f, refine_level), "createTrees");
+  }
+  void refine(const int refinement[] = nullptr, int min_level = 0,
+              int max_level = TMR_MAX_LEVEL) {
+    int64_t n = 0;
+    tmrg_qforest_num_quadrants(f, &n);
+    tmrg_report(tmrg_qforest_refine(f, refinement, refinement ? n : 0, min_level, max_level),
+                "refine");
+  }
+  TMRQuadForest *duplicate() { return derived(tmrg_qforest_duplicate, "duplicate"); }
+  TMRQuadForest *coarsen() { return derived(tmrg_qforest_coarsen, "coarsen"); }
+  void balance(int balance_corner = 0) {
+    tmrg_report(tmrg_qforest_balance(f, balance_corner), "balance");
+  }
+  void createNodes() { tmrg_report(tmrg_qforest_create_nodes(f), "createNodes"); }
+
+  void getQuadrants(TMRQuadrantArray **quads) {
+    int64_t n = 0;
+    tmrg_qforest_num_quadrants(f, &n);
+    std::vector<int> raw(6 * (size_t)n);
+    if (n && !tmrg_report(tmrg_qforest_get_quadrants(f, raw.data()), "getQuadrants")) n = 0;
+    quads_.quads.resize((size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+      TMRQuadrant &q = quads_.quads[i];
+      q.face = raw[6 * i];
+      q.x = raw[6 * i + 1];
+      q.y = raw[6 * i + 2];
+      q.tag = raw[6 * i + 3];
+      q.level = (int16_t)raw[6 * i + 4];
+      q.info = (int16_t)raw[6 * i + 5];
+    }
+    if (quads) *quads = &quads_;
+  }
+  void getNodeConn(const int **conn = nullptr, int *num_elements = nullptr,
+                   int *num_owned_nodes = nullptr, int *num_local_nodes = nullptr) {
+    int64_t s[6] = {0};
+    tmrg_qforest_sizes(f, s);
+    const int o = getMeshOrder();
+    conn_.assign((size_t)s[4] * o * o, 0);
+    if (conn) {
+      *conn = (s[4] && tmrg_report(tmrg_qforest_get_node_conn(f, conn_.data()), "getNodeConn"))
+                  ? conn_.data()
+                  : nullptr;
+    }
+    if (num_elements) *num_elements = (int)s[4];
+    if (num_owned_nodes) *num_owned_nodes = (int)s[1];
+    if (num_local_nodes) *num_local_nodes = (int)s[0];
+  }
+  int getDepNodeConn(const int **ptr = nullptr, const int **conn = nullptr,
+                     const double **weights = nullptr) {
+    int64_t s[6] = {0};
+    tmrg_qforest_sizes(f, s);
+    dptr_.assign((size_t)s[2] + 1, 0);
+    dconn_.assign((size_t)s[5] + 1, 0);
+    dw_.assign((size_t)s[5] + 1, 0.0);
+    if (!tmrg_report(tmrg_qforest_get_dep_node_conn(f, dptr_.data(), dconn_.data(), dw_.data()),
+                     "getDepNodeConn"))
+      return 0;
+    if (ptr) *ptr = dptr_.data();
+    if (conn) *conn = dconn_.data();
+    if (weights) *weights = dw_.data();
+    return (int)s[2];
+  }
+  int getOwnedNodeRange(const int **node_range) {
+    int64_t s[6] = {0};
+    tmrg_qforest_sizes(f, s);
+    range_[0] = 0;
+    range_[1] = (int)s[1];
+    if (node_range) *node_range = range_;
+    return 1;
+  }
+  void createInterpolation(TMRQuadForest *coarse, TMRGVecInterp *interp) {
+    if (coarse == this) {
+      fprintf(stderr, "TMRQuadForest Error: Cannot interpolate between the same object\n");
+      return;
+    }
+    tmrg_interp_destroy(interp->I);
+    interp->I = nullptr;
+    tmrg_report(tmrg_qforest_create_interpolation(f, coarse->f, &interp->I),
+                "createInterpolation");
+  }
+  tmrg_qforest *handle() { return f; }
+
+ private:
+  TMRQuadForest *derived(int (*fn)(tmrg_qforest *, tmrg_qforest **), const char *w) {
+    TMRQuadForest *d = new TMRQuadForest(0, getMeshOrder(), getInterpType(), stream);
+    tmrg_qforest_destroy(d->f);
+    d->f = nullptr;
+    if (!tmrg_report(fn(f, &d->f), w)) tmrg_qforest_create(getMeshOrder(), getInterpType(), stream, &d->f);
+    return d;
+  }
+  tmrg_qforest *f;
+  void *stream;
+  TMRQuadrantArray quads_;
+  std::vector<int> fc_, fe_, conn_, dptr_, dconn_;
+  std::vector<double> dw_, knots_;
+  int range_[2];
+};
+
+// STL triangle (TMR_STLTriangle, TMRBase.h:79-82).
+class TMR_STLTriangle {
+ public:
+  TMRPoint p[3];
+};
+
+// TMR_GenerateSTLTriangles (TMR_STLTools.h:44-46) with the design vector
+// given as `vpn` interleaved values per independent node (host pointer)
+// in place of a TACSBVec; *tris is allocated with new[] (delete[] it).
+inline int TMR_GenerateSTLTriangles(int root, TMROctForest *filter, const double *x, int vpn,
+                                    int x_offset, double cutoff, int *ntris,
+                                    TMR_STLTriangle **tris) {
+  (void)root;
+  int64_t n = 0;
+  *ntris = 0;
+  *tris = nullptr;
+  if (!tmrg_report(tmrg_stl_triangles(filter->handle(), x, vpn, x_offset, cutoff, &n, nullptr, 0),
+                   "TMR_GenerateSTLTriangles"))
+    return 1;
+  *tris = new TMR_STLTriangle[n > 0 ? n : 1];
+  if (!tmrg_report(tmrg_stl_triangles(filter->handle(), x, vpn, x_offset, cutoff, &n,
+                                      reinterpret_cast<double *>(*tris), n),
+                   "TMR_GenerateSTLTriangles")) {
+    delete[] * tris;
+    *tris = nullptr;
+    return 1;
+  }
+  *ntris = (int)n;
+  return 0;
+}
+inline int TMR_GenerateBinFile(const char *filename, TMROctForest *filter, const double *x,
+                               int vpn, int x_offset, double cutoff) {
+  return tmrg_report(tmrg_generate_bin_file(filename, filter->handle(), x, vpn, x_offset, cutoff),
+                     "TMR_GenerateBinFile")
+             ? 0
+             : 1;
+}
+inline int TMR_ConvertBinToSTL(const char *binfile, const char *stlfile) {
+  return tmrg_report(tmrg_convert_bin_to_stl(binfile, stlfile), "TMR_ConvertBinToSTL") ? 0 : 1;
+}
+
+// TMRHelmholtzFilter over octree filter forests (finest first, block boxes
+// set); applyFilter / applyTranspose on host vectors of vpn interleaved
+// components.  The TACS assemblers of the reference's constructor have no
+// counterpart here.
+class TMRHelmholtzFilter : public TMRGEntity {
+ public:
+  TMRHelmholtzFilter(double helmholtz_radius, int nlevels, TMROctForest *filter[])
+      : H(nullptr) {
+    std::vector<tmrg_forest *> fs(nlevels);
+    for (int k = 0; k < nlevels; k++) fs[k] = filter[k]->handle();
+    tmrg_report(tmrg_helmholtz_create(fs.data(), nlevels, helmholtz_radius, &H),
+                "TMRHelmholtzFilter");
+  }
+  ~TMRHelmholtzFilter() { tmrg_helmholtz_destroy(H); }
+  void applyFilter(const double *in, double *out, int vpn = 1) {
+    tmrg_report(tmrg_helmholtz_apply(H, vpn, in, out), "applyFilter");
+  }
+  void applyTranspose(const double *in, double *out, int vpn = 1) {
+    tmrg_report(tmrg_helmholtz_apply_transpose(H, vpn, in, out), "applyTranspose");
+  }
+  tmrg_helmholtz *handle() { return H; }
+
+ private:
+  tmrg_helmholtz *H;
+};
+
+#endif

@@ -1,0 +1,91 @@
+// Drives the C++ TMRQuadForest facade (include/tmrg_quadforest.hpp) the
+// way TMR code drives TMRQuadForest, then the STL tools on a small octree
+// forest.  Prints counts and checksums for the test to compare with the
+// Python binding on the same input.
+#include <stdio.h>
+
+#include <vector>
+
+#include "tmrg_quadforest.hpp"
+
+int main() {
+  const int nx = 3, ny = 2;
+  std::vector<int> conn;
+  for (int j = 0; j < ny; j++)
+    for (int i = 0; i < nx; i++) {
+      int n0 = i + (nx + 1) * j;
+      conn.insert(conn.end(), {n0, n0 + 1, n0 + nx + 1, n0 + nx + 2});
+    }
+  TMRQuadForest *f = new TMRQuadForest(0, 3, TMR_GAUSS_LOBATTO_POINTS);
+  f->incref();
+  f->setConnectivity((nx + 1) * (ny + 1), conn.data(), nx * ny);
+  f->createTrees(1);
+  for (int pass = 0; pass < 3; pass++) {
+    TMRQuadrantArray *quads;
+    f->getQuadrants(&quads);
+    int n;
+    TMRQuadrant *a;
+    quads->getArray(&a, &n);
+    std::vector<int> ref(n);
+    for (int i = 0; i < n; i++) ref[i] = ((a[i].x >> 20) + (a[i].y >> 21) + a[i].face + pass) % 3 == 0;
+    f->refine(ref.data(), 0, 6);
+    f->balance(1);
+  }
+  f->createNodes();
+  TMRQuadForest *c = f->coarsen();
+  c->incref();
+  c->balance(1);
+  c->createNodes();
+  TMRGVecInterp *I = new TMRGVecInterp();
+  I->incref();
+  f->createInterpolation(c, I);
+  int64_t rows, cols, nnz;
+  I->getSizes(&rows, &cols, &nnz);
+  std::vector<double> x(cols, 1.0), y(rows, 0.0);
+  I->mult(x.data(), y.data());
+  double s = 0.0;
+  for (double v : y) s += v;
+  const int *ec;
+  int ne, nown;
+  f->getNodeConn(&ec, &ne, &nown);
+  long long csum = 0;
+  for (long long i = 0; i < (long long)ne * 9; i++) csum += ec[i];
+  const int *dp, *dc;
+  const double *dw;
+  int nd = f->getDepNodeConn(&dp, &dc, &dw);
+  int nfaces, nedges, nnodes;
+  const int *fc, *fe;
+  f->getConnectivity(&nfaces, &nedges, &nnodes, &fc, &fe);
+  printf("elements %d owned %d dep %d conn_sum %lld P_rows %lld P_nnz %lld P1_sum %.17g "
+         "faces %d edges %d nodes %d\n",
+         ne, nown, nd, csum, (long long)rows, (long long)nnz, s, nfaces, nedges, nnodes);
+  // STL tools on a one-block octree forest with a linear field in x
+  std::vector<int> bconn = {0, 1, 2, 3, 4, 5, 6, 7};
+  TMROctForest *o = new TMROctForest(0, 2, TMR_GAUSS_LOBATTO_POINTS);
+  o->incref();
+  o->setConnectivity(8, bconn.data(), 1);
+  o->createTrees(2);
+  o->createNodes();
+  int nl;
+  const int *nums;
+  nl = o->getNodeNumbers(&nums);
+  int no;
+  o->getNodeConn(nullptr, nullptr, &no);
+  std::vector<double> xv(no);
+  // value = node number parity: a ragged level set, enough to produce
+  // triangles
+  for (int i = 0; i < no; i++) xv[i] = (i % 3) * 0.5;
+  int ntris = 0;
+  TMR_STLTriangle *tris = nullptr;
+  TMR_GenerateSTLTriangles(0, o, xv.data(), 1, 0, 0.4, &ntris, &tris);
+  double tsum = 0.0;
+  for (int i = 0; i < ntris; i++)
+    for (int k = 0; k < 3; k++) tsum += tris[i].p[k].x + tris[i].p[k].y + tris[i].p[k].z;
+  delete[] tris;
+  printf("stl_tris %d stl_sum %.17g local %d\n", ntris, tsum, nl);
+  I->decref();
+  c->decref();
+  f->decref();
+  o->decref();
+  return 0;
+}

@@ -9,21 +9,23 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "cpp", "facade_pipeline.cpp")
+SRC_QUAD = os.path.join(ROOT, "tests", "cpp", "facade_quad.cpp")
 
 
-def _build(tmp_path):
+def _build(tmp_path, src=SRC):
     from tmr_gb300 import build
     lib = build.build()
-    exe = str(tmp_path / "facade_pipeline")
+    exe = str(tmp_path / os.path.basename(src)[:-4])
     cuda_inc = "/usr/local/cuda/include"
     subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"),
-                    "-I", cuda_inc, SRC, "-o", exe, "-L", os.path.dirname(lib), "-ltmrg",
+                    "-I", cuda_inc, src, "-o", exe, "-L", os.path.dirname(lib), "-ltmrg",
                     "-Wl,-rpath," + os.path.dirname(lib)], check=True)
     return exe
 
 
 def test_facade_compiles_and_links(tmp_path):
     assert os.path.exists(_build(tmp_path))
+    assert os.path.exists(_build(tmp_path, SRC_QUAD))
 
 
 @pytest.mark.gpu
@@ -64,3 +66,46 @@ def test_facade_matches_python_binding(gpu_lib, tmp_path):
     assert float(vals["du"]) == pytest.approx(0.0, abs=1e-13)
     assert int(vals["enclosed_self"]) == 1
     assert int(vals["corner_block"]) == 0
+
+
+@pytest.mark.gpu
+def test_quad_facade_matches_python_binding(gpu_lib, tmp_path):
+    exe = _build(tmp_path, SRC_QUAD)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
+    vals = dict(zip(out[0::2], out[1::2]))
+    from tmr_gb300 import TMR
+    from tmr_gb300 import workloads as W
+    f = TMR.QuadForest(order=3)
+    f.setConnectivity(W.brick2d(3, 2))
+    f.createTrees(1)
+    for p in range(3):
+        q = f.getQuadrantsArray()
+        ref = (((q[:, 1] >> 20) + (q[:, 2] >> 21) + q[:, 0] + p) % 3 == 0).astype(np.intc)
+        f.refine(ref, 0, 6)
+        f.balance(1)
+    f.createNodes()
+    c = f.coarsen()
+    c.balance(1)
+    c.createNodes()
+    I = TMR.VecInterp()
+    f.createInterpolation(c, I)
+    rows, cols, nnz = I.sizes()
+    y = np.zeros(rows)
+    I.mult(np.ones(cols), y)
+    conn = f.getMeshConn()
+    assert int(vals["elements"]) == conn.shape[0]
+    assert int(vals["conn_sum"]) == int(conn.astype(np.int64).sum())
+    assert int(vals["dep"]) == len(f.getDepNodeConn()[0]) - 1
+    assert int(vals["P_rows"]) == rows and int(vals["P_nnz"]) == nnz
+    assert float(vals["P1_sum"]) == pytest.approx(y.sum(), rel=1e-12)
+    assert (int(vals["faces"]), int(vals["edges"]), int(vals["nodes"])) == (6, 17, 12)
+    # STL tools through the facade = the Python binding
+    o = TMR.OctForest(order=2)
+    o.setConnectivity(np.arange(8, dtype=np.intc).reshape(1, 8))
+    o.createTrees(2)
+    o.createNodes()
+    no = o.getNodeRange()[1]
+    xv = (np.arange(no) % 3) * 0.5
+    pts = TMR.getSTLTriangles(o, xv, offset=0, cutoff=0.4, vpn=1)
+    assert int(vals["stl_tris"]) == len(pts) // 3 > 0
+    assert float(vals["stl_sum"]) == pytest.approx(float(pts.sum()), rel=1e-13)
