@@ -405,6 +405,11 @@ int tmrg_convert_bin_to_stl(const char *binfile, const char *stlfile);
    forests' block boxes (tmrg_forest_set_block_boxes). */
 int tmrg_helmholtz_create(tmrg_forest *const *filters, int nlevels, double r,
                           tmrg_helmholtz **out);
+/* The same filter over quadtree forests (TMRHelmholtzFilter.cpp:35-40,
+   TMRQuadHelmholtzModel :23-59): bilinear (order 2) or quadratic Bernstein
+   (order 3) quadrilaterals, face boxes from tmrg_qforest_set_face_boxes. */
+int tmrg_helmholtz_create_quad(tmrg_qforest *const *filters, int nlevels, double r,
+                               tmrg_helmholtz **out);
 int tmrg_helmholtz_destroy(tmrg_helmholtz *H);
 /* out4[4 * k + {0, 1, 2, 3}] = independent nodes, elements, dependent
    nodes and scatter-list entries (element slots expanded through the

@@ -230,7 +230,7 @@ inline int TMR_ConvertBinToSTL(const char *binfile, const char *stlfile) {
   return tmrg_report(tmrg_convert_bin_to_stl(binfile, stlfile), "TMR_ConvertBinToSTL") ? 0 : 1;
 }
 
-// TMRHelmholtzFilter over octree filter forests (finest first, block boxes
+// TMRHelmholtzFilter over octree or quadtree filter forests (finest first, boxes
 // set); applyFilter / applyTranspose on host vectors of vpn interleaved
 // components.  The TACS assemblers of the reference's constructor have no
 // counterpart here.
@@ -241,6 +241,15 @@ class TMRHelmholtzFilter : public TMRGEntity {
     std::vector<tmrg_forest *> fs(nlevels);
     for (int k = 0; k < nlevels; k++) fs[k] = filter[k]->handle();
     tmrg_report(tmrg_helmholtz_create(fs.data(), nlevels, helmholtz_radius, &H),
+                "TMRHelmholtzFilter");
+  }
+  // The 2-D filter (TMRHelmholtzFilter.cpp:35-40): quadtree forests with
+  // face boxes.
+  TMRHelmholtzFilter(double helmholtz_radius, int nlevels, TMRQuadForest *filter[])
+      : H(nullptr) {
+    std::vector<tmrg_qforest *> fs(nlevels);
+    for (int k = 0; k < nlevels; k++) fs[k] = filter[k]->handle();
+    tmrg_report(tmrg_helmholtz_create_quad(fs.data(), nlevels, helmholtz_radius, &H),
                 "TMRHelmholtzFilter");
   }
   ~TMRHelmholtzFilter() { tmrg_helmholtz_destroy(H); }

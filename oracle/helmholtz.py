@@ -154,3 +154,65 @@ def apply_transpose(K, M, x, vpn=1):
     x = np.asarray(x, np.float64).reshape(-1, vpn)
     lu = sla.splu(K.tocsc())
     return np.stack([M @ lu.solve(x[:, k]) for k in range(vpn)], axis=1).ravel()
+
+
+# ---------------------------------------------------------------------------
+# The 2-D filter on quadtree forests (TMRQuadHelmholtzModel,
+# TMRHelmholtzModel.cpp:23-59; TMRQuadTACSMatrixCreator's bilinear /
+# quadratic Bernstein quadrilaterals).
+def element_points2d(quad_row, order, knots, boxes):
+    """Node coordinates of one quadrilateral (order^2 x 2), x fastest."""
+    f, x, y = int(quad_row[0]), int(quad_row[1]), int(quad_row[2])
+    lev = int(quad_row[4])
+    s = 1.0 / (1 << 30)
+    d = (1 << (30 - lev)) * s
+    X = np.zeros((order ** 2, 2))
+    for j in range(order):
+        for i in range(order):
+            u = (x * s + 0.5 * d * (1.0 + knots[i]), y * s + 0.5 * d * (1.0 + knots[j]))
+            for a in range(2):
+                X[i + order * j, a] = boxes[f, a] + boxes[f, 2 + a] * u[a]
+    return X
+
+
+def element_matrices2d(Xpts, order, r):
+    pts, wts = _GAUSS[order]
+    n = order ** 2
+    Ke = np.zeros((n, n))
+    Me = np.zeros((n, n))
+    for jq in range(order):
+        for iq in range(order):
+            Nx, Dx = basis_1d(order, pts[iq])
+            Ny, Dy = basis_1d(order, pts[jq])
+            wt = wts[iq] * wts[jq]
+            N = np.einsum("j,i->ji", Ny, Nx).ravel()
+            dN = np.stack([np.einsum("j,i->ji", Ny, Dx).ravel(),
+                           np.einsum("j,i->ji", Dy, Nx).ravel()], axis=1)
+            Xd = Xpts.T @ dN
+            detJ = np.linalg.det(Xd)
+            G = dN @ np.linalg.inv(Xd)
+            h = wt * detJ
+            Ke += h * (r * r * (G @ G.T) + np.outer(N, N))
+            Me += h * np.outer(N, N)
+    return Ke, Me
+
+
+def assemble2d(quads, conn, dep_ptr, dep_conn, dep_w, num_nodes, order, knots, boxes, r):
+    """Global K and M of a quadtree forest (scipy CSR)."""
+    import scipy.sparse as sp
+    npe = order ** 2
+    ne = len(quads)
+    Ks = np.zeros((ne, npe, npe))
+    Ms = np.zeros((ne, npe, npe))
+    cache = {}
+    for e in range(ne):
+        X = element_points2d(quads[e], order, knots, boxes)
+        key = (X - X[0]).tobytes()
+        if key not in cache:
+            cache[key] = element_matrices2d(X, order, r)
+        Ks[e], Ms[e] = cache[key]
+    S = slot_matrix(conn, dep_ptr, dep_conn, dep_w, num_nodes)
+    ip = np.arange(ne + 1)
+    Kb = sp.bsr_matrix((Ks, np.arange(ne), ip), shape=(ne * npe, ne * npe))
+    Mb = sp.bsr_matrix((Ms, np.arange(ne), ip), shape=(ne * npe, ne * npe))
+    return (S @ Kb @ S.T).tocsr(), (S @ Mb @ S.T).tocsr()

@@ -146,3 +146,69 @@ def test_no_geometry_is_an_error(gpu_lib):
     f.createNodes()
     with pytest.raises(TMR._lib.TMRGError, match="geometry"):
         TMR.HelmholtzFilter(0.1, None, [f])
+
+
+def _quad_forests(name):
+    """The quadtree forests of a quad fixture case (finest first), checked
+    against the fixture's mesh."""
+    from tmr_gb300 import TMR
+    case = pipeline.quad_golden_case(name)
+    gold = pipeline.load_quad_golden(name)
+    f = TMR.QuadForest(order=case["order"], interp=case.get("interp", 1))
+    f.setConnectivity(case["conn"])
+    f.createTrees(case["L0"])
+    for p in range(case["passes"]):
+        f.refine(pipeline.indicator(f.getQuadrantsArray(), case, p), 0, case["max_level"])
+        f.balance(case.get("corner", 1))
+    f.createNodes()
+    np.testing.assert_array_equal(f.getMeshConn(), gold["conn"])
+    forests = [f]
+    for _ in range(case.get("coarse_levels", 1)):
+        c = forests[-1].coarsen()
+        c.balance(case.get("corner", 1))
+        c.createNodes()
+        forests.append(c)
+    return case, gold, forests
+
+
+# faces per row / column of the brick2d grids of the quad fixtures
+QUAD_GRID = {"brick_o2": (4, 3), "brick_o3": (3, 2)}
+
+
+@pytest.mark.parametrize("name", ["brick_o2", "brick_o3"])
+@pytest.mark.parametrize("r", [0.02, 0.1])
+def test_quad_filter_matches_direct_solve(gpu_lib, name, r):
+    """The 2-D filter on the reference's quadtree forests: K x, M x and
+    the filtered field against the assembled direct solve."""
+    import torch
+    from tmr_gb300 import TMR
+    case, gold, forests = _quad_forests(name)
+    nx, ny = QUAD_GRID[name]
+    boxes = np.array([[i * 1.0, j * 0.6, 1.0, 0.6] for j in range(ny) for i in range(nx)])
+    for g in forests:
+        g.setFaceBoxes(boxes)
+    Hf = TMR.HelmholtzFilter(r, None, forests)
+    sizes = Hf.sizes()
+    assert len(sizes) == len(forests)
+    n = int(sizes[0][0])
+    dp, dc, dw = gold["dep"]
+    K, M = HO.assemble2d(gold["quads"], gold["conn"], dp, dc, dw, n, case["order"],
+                         forests[0].getInterpKnots(), boxes, r)
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal(n)
+    xd = torch.tensor(x, device="cuda")
+    y = torch.empty_like(xd)
+    Hf.mult(0, 0, xd, y)
+    assert _rel(y.cpu().numpy(), K @ x) <= 1e-12
+    Hf.mult(0, 1, xd, y)
+    assert _rel(y.cpu().numpy(), M @ x) <= 1e-12
+    u = rng.uniform(0.0, 1.0, n)
+    out = np.zeros(n)
+    Hf.applyFilter(u, out)
+    assert _rel(out, HO.apply_filter(K, M, u)) <= 1e-9
+    it, res = Hf.lastSolve()
+    assert 1 <= it <= 60
+    Hf.applyTranspose(u, out)
+    assert _rel(out, HO.apply_transpose(K, M, u)) <= 1e-9
+    Hf.applyFilter(np.ones(n), out)
+    np.testing.assert_allclose(out, 1.0, rtol=1e-10)

@@ -79,3 +79,23 @@ def test_assembled_operators_properties():
     a = y @ H.apply_filter(K, M, x)
     b = H.apply_transpose(K, M, y) @ x
     assert a == pytest.approx(b, rel=1e-10)
+
+
+def test_quad_element_matrices_closed_form():
+    """Bilinear square of side h: M = h^2/36 [4 2 2 1; ...], K 1 = M 1."""
+    X = np.array([[0, 0], [0.5, 0], [0, 0.5], [0.5, 0.5]], float)
+    Ke, Me = H.element_matrices2d(X, 2, 0.3)
+    exp = np.array([[4, 2, 2, 1], [2, 4, 1, 2], [2, 1, 4, 2], [1, 2, 2, 4]]) * 0.25 / 36
+    np.testing.assert_allclose(Me, exp, rtol=1e-14)
+    np.testing.assert_allclose(Ke.sum(1), Me.sum(1), atol=1e-16)
+    # stiffness part: r^2 times the Laplacian of a square (scale-free in 2-D)
+    L = (Ke - Me) / 0.09
+    exp_l = np.array([[4, -1, -1, -2], [-1, 4, -2, -1], [-1, -2, 4, -1], [-2, -1, -1, 4]]) / 6
+    np.testing.assert_allclose(L, exp_l, rtol=1e-13, atol=1e-15)
+    # quadratic Bernstein: partition of unity, mass sums to the area of the
+    # level-1 element of a 2 x 1 face (1 x 0.5)
+    X3 = H.element_points2d(np.array([0, 0, 0, 0, 1, 0]), 3, np.array([-1.0, 0.0, 1.0]),
+                             np.array([[0.0, 0.0, 2.0, 1.0]]))
+    K3, M3 = H.element_matrices2d(X3, 3, 0.1)
+    assert M3.sum() == pytest.approx(0.5, rel=1e-13)
+    np.testing.assert_allclose(K3.sum(1), M3.sum(1), atol=1e-15)

@@ -930,9 +930,10 @@ class HelmholtzFilter(ConformFilter):
     HelmholtzFilter(radius, assemblers, filters)): the Helmholtz PDE filter
     psi = K^-1 M x on the finest filter forest, solved with conjugate
     gradients preconditioned by a multigrid V-cycle over the filter
-    forests.  ``assemblers`` are accepted and ignored (no TACS); every
-    forest needs its nodes and block boxes (``setBlockBoxes``): the boxes
-    are the geometry the element integrals use."""
+    forests (OctForests, or QuadForests for the 2-D filter).
+    ``assemblers`` are accepted and ignored (no TACS); every forest needs
+    its nodes and block boxes (``setBlockBoxes`` / ``setFaceBoxes``): the
+    boxes are the geometry the element integrals use."""
 
     _name = "TMRHelmholtzFilter"
 
@@ -940,7 +941,9 @@ class HelmholtzFilter(ConformFilter):
         ConformFilter.__init__(self, assemblers, filters, vpn)
         arr = (ctypes.c_void_p * len(self.filters))(*[f.ptr for f in self.filters])
         h = _vp()
-        call("tmrg_helmholtz_create", arr, len(self.filters), float(r), ctypes.byref(h))
+        name = ("tmrg_helmholtz_create_quad" if isinstance(self.filters[0], QuadForest)
+                else "tmrg_helmholtz_create")
+        call(name, arr, len(self.filters), float(r), ctypes.byref(h))
         self.ptr = h
         self.r = r
 

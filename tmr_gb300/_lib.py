@@ -118,6 +118,7 @@ _SIGS = {
     "tmrg_generate_bin_file": [ctypes.c_char_p, c_vp, c_vp, c_int, c_int, c_dbl],
     "tmrg_convert_bin_to_stl": [ctypes.c_char_p, ctypes.c_char_p],
     "tmrg_helmholtz_create": [c_vp, c_int, c_dbl, P(c_vp)],
+    "tmrg_helmholtz_create_quad": [c_vp, c_int, c_dbl, P(c_vp)],
     "tmrg_helmholtz_destroy": [c_vp],
     "tmrg_helmholtz_sizes": [c_vp, c_vp, c_vp],
     "tmrg_helmholtz_apply": [c_vp, c_int, c_vp, c_vp],

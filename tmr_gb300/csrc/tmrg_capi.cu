@@ -1516,6 +1516,26 @@ int tmrg_helmholtz_create(tmrg_forest *const *filters, int nlevels, double r,
     *out = h;
   });
 }
+int tmrg_helmholtz_create_quad(tmrg_qforest *const *filters, int nlevels, double r,
+                               tmrg_helmholtz **out) {
+  return guarded([&] {
+    ARG(filters && out && nlevels > 0, "bad argument");
+    ARG(r >= 0.0, "Helmholtz radius must be >= 0");
+    std::vector<QForest *> fs(nlevels);
+    for (int k = 0; k < nlevels; k++) {
+      ARG(filters[k], "NULL forest");
+      fs[k] = &filters[k]->f;
+    }
+    auto *h = new tmrg_helmholtz;
+    try {
+      helmholtz_create_quad(fs.data(), nlevels, r, h->H);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
 int tmrg_helmholtz_destroy(tmrg_helmholtz *H) {
   return guarded([&] {
     if (!H) return;

@@ -46,6 +46,7 @@
 #include <type_traits>
 
 #include "tmrg_helmholtz.h"
+#include "tmrg_quad.h"
 
 namespace tmrg {
 
@@ -95,25 +96,39 @@ static void make_basis(int o, HBasisT<double> &B) {
   }
 }
 
-// Element factors: V = sx sy sz, c_d = r^2 / s_d^2, s_d the half side of
-// the element in direction d (block box extent x 2^-level / 2).
-__global__ void k_h_geom(long long ne, const int *__restrict__ block,
+// Element factors: V = sx sy (sz), c_d = r^2 / s_d^2, s_d the half side of
+// the element in direction d (box extent x 2^-level / 2).  Boxes hold the
+// origin then the extent of each direction (6 values in 3-D, 4 in 2-D).
+__global__ void k_h_geom(long long ne, int dim, const int *__restrict__ block,
                          const int16_t *__restrict__ level,
                          const double *__restrict__ boxes, double r2, HGeoT<double> *geo,
                          HGeoT<float> *geo32) {
   long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ne) return;
-  const double *bx = boxes + 6LL * block[e];
+  const double *bx = boxes + 2LL * dim * block[e];
   int l = level[e];
-  double sx = ldexp(bx[3], -l - 1), sy = ldexp(bx[4], -l - 1), sz = ldexp(bx[5], -l - 1);
-  HGeoT<double> g{sx * sy * sz, r2 / (sx * sx), r2 / (sy * sy), r2 / (sz * sz)};
+  double sx = ldexp(bx[dim], -l - 1), sy = ldexp(bx[dim + 1], -l - 1);
+  HGeoT<double> g;
+  if (dim == 3) {
+    double sz = ldexp(bx[5], -l - 1);
+    g = HGeoT<double>{sx * sy * sz, r2 / (sx * sx), r2 / (sy * sy), r2 / (sz * sz)};
+  } else {
+    g = HGeoT<double>{sx * sy, r2 / (sx * sx), r2 / (sy * sy), 0.0};
+  }
   geo[e] = g;
   geo32[e] = HGeoT<float>{(float)g.x, (float)g.y, (float)g.z, (float)g.w};
 }
 
-// Element matrix entry K_e[a][b] (stiff) or M_e[a][b].
-__device__ __forceinline__ double h_entry(const HBasisT<double> &B, int o, HGeoT<double> G,
-                                          int a, int b, bool stiff) {
+// Element matrix entry K_e[a][b] (stiff) or M_e[a][b] of a dim-D element.
+__device__ __forceinline__ double h_entry(const HBasisT<double> &B, int o, int dim,
+                                          HGeoT<double> G, int a, int b, bool stiff) {
+  if (dim == 2) {
+    int ax = a % o, ay = a / o, bx = b % o, by = b / o;
+    double mx = B.M[ax][bx], my = B.M[ay][by];
+    double v = mx * my;
+    if (stiff) v += G.y * B.K[ax][bx] * my + G.z * mx * B.K[ay][by];
+    return G.x * v;
+  }
   int ax = a % o, ay = (a / o) % o, az = a / (o * o);
   int bx = b % o, by = (b / o) % o, bz = b / (o * o);
   double mx = B.M[ax][bx], my = B.M[ay][by], mz = B.M[az][bz];
@@ -189,7 +204,7 @@ __global__ void k_h_srowptr(long long nn, long long E, const uint64_t *__restric
 
 // Inverse Jacobi diagonal: diag_j = sum over elements e touching j of
 // sum_{(a,wa),(b,wb) in e} wa wb K_e[a][b].
-__global__ void k_h_diag(long long nn, long long ne, int o, HBasisT<double> B,
+__global__ void k_h_diag(long long nn, long long ne, int o, int dim, HBasisT<double> B,
                          const int *__restrict__ rp, const int *__restrict__ slot,
                          const double *__restrict__ w,
                          const HGeoT<double> *__restrict__ geo, double *dinv,
@@ -207,7 +222,7 @@ __global__ void k_h_diag(long long nn, long long ne, int o, HBasisT<double> B,
       int a = (int)((unsigned)slot[i] / (unsigned)ne);
       for (int k = p; k < q; k++) {
         int b = (int)((unsigned)slot[k] / (unsigned)ne);
-        d += w[i] * w[k] * h_entry(B, o, G, a, b, true);
+        d += w[i] * w[k] * h_entry(B, o, dim, G, a, b, true);
       }
     }
     p = q;
@@ -318,6 +333,59 @@ __global__ void __launch_bounds__(HM_THREADS)
   }
 }
 
+// 2-D element: y = V (cx Kx My + cy Mx Ky + Mx My) x by sum
+// factorisation (y direction, then x), slot-major output.
+template <int O, bool STIFF, typename T>
+__global__ void __launch_bounds__(HM_THREADS)
+    k_h_elem2(long long ne, int nvec, const int *__restrict__ econn,
+              const HGeoT<T> *__restrict__ geo, const T *__restrict__ x,
+              const T *__restrict__ xd, T *__restrict__ yE, HBasisT<T> B) {
+  constexpr int N = O * O;
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  int g[N];
+#pragma unroll
+  for (int a = 0; a < N; a++) g[a] = econn[e * N + a];
+  const HGeoT<T> G = geo[e];
+  for (int v = 0; v < nvec; v++) {
+    T u[N];
+#pragma unroll
+    for (int a = 0; a < N; a++)
+      u[a] = g[a] >= 0 ? __ldg(x + (long long)g[a] * nvec + v)
+                       : __ldg(xd + (long long)(-g[a] - 1) * nvec + v);
+    // y direction: ym = My u, in = cy Ky u + My u
+    T ym[N], in[N];
+#pragma unroll
+    for (int ix = 0; ix < O; ix++)
+#pragma unroll
+      for (int by = 0; by < O; by++) {
+        T sm = T(0), sk = T(0);
+#pragma unroll
+        for (int ay = 0; ay < O; ay++) {
+          sm = fma(B.M[by][ay], u[ix + O * ay], sm);
+          if (STIFF) sk = fma(B.K[by][ay], u[ix + O * ay], sk);
+        }
+        ym[ix + O * by] = sm;
+        in[ix + O * by] = STIFF ? fma(G.z, sk, sm) : sm;
+      }
+    // x direction: y = V (Mx in + cx Kx ym)
+#pragma unroll
+    for (int by = 0; by < O; by++)
+#pragma unroll
+      for (int bx = 0; bx < O; bx++) {
+        T sm = T(0), sk = T(0);
+#pragma unroll
+        for (int ax = 0; ax < O; ax++) {
+          sm = fma(B.M[bx][ax], in[ax + O * by], sm);
+          if (STIFF) sk = fma(B.K[bx][ax], ym[ax + O * by], sk);
+        }
+        const int b = bx + O * by;
+        T r = STIFF ? fma(G.y, sk, sm) : sm;
+        yE[((long long)b * ne + e) * nvec + v] = G.x * r;
+      }
+  }
+}
+
 // y_j = sum of w yE[slot] over j's scatter list; mode 0: out = y,
 // 1: out = b - y, 2: out -= y.
 template <typename T>
@@ -356,7 +424,7 @@ __global__ void k_h_csr(long long nrows, int nvec, const int *__restrict__ rp,
 // ---------------------------------------------------------------------
 // Coarsest level: dense matrix (thread per row), Gauss-Jordan inverse,
 // dense product.
-__global__ void k_h_dense(long long nn, long long ne, int o, HBasisT<double> B,
+__global__ void k_h_dense(long long nn, long long ne, int o, int dim, HBasisT<double> B,
                           const int *__restrict__ rp, const int *__restrict__ slot,
                           const double *__restrict__ w, const int *__restrict__ econn,
                           const int *__restrict__ dptr, const int *__restrict__ dconn,
@@ -364,14 +432,14 @@ __global__ void k_h_dense(long long nn, long long ne, int o, HBasisT<double> B,
                           const HGeoT<double> *__restrict__ geo, double *A) {
   long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nn) return;
-  const int npe = o * o * o;
+  const int npe = dim == 3 ? o * o * o : o * o;
   double *row = A + j * nn;
   for (int p = rp[j]; p < rp[j + 1]; p++) {
     unsigned e = (unsigned)slot[p] % (unsigned)ne;
     int a = (int)((unsigned)slot[p] / (unsigned)ne);
     HGeoT<double> G = geo[e];
     for (int b = 0; b < npe; b++) {
-      double kab = w[p] * h_entry(B, o, G, a, b, true);
+      double kab = w[p] * h_entry(B, o, dim, G, a, b, true);
       int g = econn[(long long)e * npe + b];
       if (g >= 0) {
         row[g] += kab;
@@ -647,7 +715,7 @@ static void h_apply(HLevel &L, bool stiff, int nvec, const T *x, T *y, const T *
   // FP64 operations of the sum factorisation (7 or 3 contractions of
   // o^4 multiply-adds, x2 flops)
   if constexpr (std::is_same<T, double>::value)
-    prof_flops((stiff ? 14LL : 6LL) * L.ne * npe * L.o * nvec);
+    prof_flops((stiff ? (L.dim == 3 ? 14LL : 8LL) : 2LL * L.dim) * L.ne * npe * L.o * nvec);
   const unsigned g = blocks_for(L.ne, HM_THREADS);
   const HGeoT<T> *geo = D::geo(L);
   const int *ec = L.econn.p;
@@ -656,7 +724,24 @@ static void h_apply(HLevel &L, bool stiff, int nvec, const T *x, T *y, const T *
 #define H_ELEM(O, ST, TT)                                                                  \
   launch((k_h_elem<O, ST, TT>), g, HM_THREADS, 0, s, L.ne, nvec, ec, geo, x, xd, yE, \
          D::bas(L))
-  if constexpr (std::is_same<T, double>::value) {
+#define H_ELEM2(O, ST, TT)                                                                 \
+  launch((k_h_elem2<O, ST, TT>), g, HM_THREADS, 0, s, L.ne, nvec, ec, geo, x, xd, yE, \
+         D::bas(L))
+  if (L.dim == 2) {
+    if constexpr (std::is_same<T, double>::value) {
+      if (L.o == 2) {
+        if (stiff) H_ELEM2(2, true, double); else H_ELEM2(2, false, double);
+      } else {
+        if (stiff) H_ELEM2(3, true, double); else H_ELEM2(3, false, double);
+      }
+    } else {
+      if (L.o == 2) {
+        if (stiff) H_ELEM2(2, true, float); else H_ELEM2(2, false, float);
+      } else {
+        if (stiff) H_ELEM2(3, true, float); else H_ELEM2(3, false, float);
+      }
+    }
+  } else if constexpr (std::is_same<T, double>::value) {
     if (L.o == 2) {
       if (stiff) H_ELEM(2, true, double); else H_ELEM(2, false, double);
     } else {
@@ -670,6 +755,7 @@ static void h_apply(HLevel &L, bool stiff, int nvec, const T *x, T *y, const T *
     }
   }
 #undef H_ELEM
+#undef H_ELEM2
   prof_bytes((4 + sz) * L.snnz + 4 * (L.nn + 1) + sz * L.snnz * nvec +
              sz * L.nn * nvec * (mode == 0 ? 1 : 2));
   const unsigned gs = blocks_for(L.nn * nvec, 256);
@@ -926,16 +1012,39 @@ static void solve(Helmholtz &H, int nvec, const double *b, double *x) {
 }
 
 // ---------------------------------------------------------------------
-static void build_level(Helmholtz &H, Forest &f, HLevel &L) {
-  cudaStream_t s = H.s;
+// What a level needs from an octree or quadtree filter forest.
+struct HSource {
+  int dim, order;
+  long long ne, nn, ndep, dnnz;
+  const int *econn, *dptr, *dconn;
+  const double *dw;
+  const int *block;
+  const int16_t *level;
+  const double *boxes;  // device, 2 dim values per block; null = no geometry
+};
+static HSource source_of(Forest &f) {
   if (!f.have_nodes) forest_create_nodes(f);
+  return HSource{3, f.order, f.n, f.num_owned, f.num_dep, f.dep_nnz, f.econn.p, f.dep_ptr.p,
+                 f.dep_conn.p, f.dep_w.p, f.block.p, f.level.p,
+                 (f.conn && !f.conn->boxes.empty()) ? f.conn->d_boxes.p : nullptr};
+}
+static HSource source_of(QForest &f) {
+  if (!f.have_nodes) qforest_create_nodes(f);
+  return HSource{2, f.order, f.n, f.num_owned, f.num_dep, f.dep_nnz, f.econn.p, f.dep_ptr.p,
+                 f.dep_conn.p, f.dep_w.p, f.block.p, f.level.p,
+                 (f.conn && !f.conn->boxes.empty()) ? f.conn->d_boxes.p : nullptr};
+}
+
+static void build_level(Helmholtz &H, const HSource &f, HLevel &L) {
+  cudaStream_t s = H.s;
   if (f.order != 2 && f.order != 3)
     throw Error(TMRG_ERR_UNSUPPORTED, "Helmholtz filter: forest order must be 2 or 3");
-  if (!f.conn || f.conn->boxes.empty())
+  if (!f.boxes)
     throw Error(TMRG_ERR_ARG,
                 "Helmholtz filter: the forest has no geometry (set the block boxes)");
+  L.dim = f.dim;
   L.o = f.order;
-  L.npe = f.order * f.order * f.order;
+  L.npe = f.dim == 3 ? f.order * f.order * f.order : f.order * f.order;
   make_basis(L.o, L.bas);
   L.bas32.o = L.o;
   for (int a = 0; a < 3; a++)
@@ -943,26 +1052,26 @@ static void build_level(Helmholtz &H, Forest &f, HLevel &L) {
       L.bas32.M[a][b] = (float)L.bas.M[a][b];
       L.bas32.K[a][b] = (float)L.bas.K[a][b];
     }
-  L.ne = f.n;
-  L.nn = f.num_owned;
-  L.ndep = f.num_dep;
-  L.dnnz = f.dep_nnz;
+  L.ne = f.ne;
+  L.nn = f.nn;
+  L.ndep = f.ndep;
+  L.dnnz = f.dnnz;
   if (L.ne * L.npe >= (1LL << 31))
     throw Error(TMRG_ERR_ARG, "Helmholtz filter: too many element slots");
   const long long nslot = L.ne * L.npe;
   L.econn.alloc(std::max(1LL, nslot), s);
-  TMRG_CUDA(cudaMemcpyAsync(L.econn.p, f.econn.p, sizeof(int) * nslot,
+  TMRG_CUDA(cudaMemcpyAsync(L.econn.p, f.econn, sizeof(int) * nslot,
                             cudaMemcpyDeviceToDevice, s));
   L.dptr.alloc(L.ndep + 1, s);
   L.dconn.alloc(std::max(1LL, L.dnnz), s);
   L.dw.alloc(std::max(1LL, L.dnnz), s);
   L.dw32.alloc(std::max(1LL, L.dnnz), s);
   if (L.ndep) {
-    TMRG_CUDA(cudaMemcpyAsync(L.dptr.p, f.dep_ptr.p, sizeof(int) * (L.ndep + 1),
+    TMRG_CUDA(cudaMemcpyAsync(L.dptr.p, f.dptr, sizeof(int) * (L.ndep + 1),
                               cudaMemcpyDeviceToDevice, s));
-    TMRG_CUDA(cudaMemcpyAsync(L.dconn.p, f.dep_conn.p, sizeof(int) * L.dnnz,
+    TMRG_CUDA(cudaMemcpyAsync(L.dconn.p, f.dconn, sizeof(int) * L.dnnz,
                               cudaMemcpyDeviceToDevice, s));
-    TMRG_CUDA(cudaMemcpyAsync(L.dw.p, f.dep_w.p, sizeof(double) * L.dnnz,
+    TMRG_CUDA(cudaMemcpyAsync(L.dw.p, f.dw, sizeof(double) * L.dnnz,
                               cudaMemcpyDeviceToDevice, s));
     launch((k_h_cvt<double, float>), blocks_for(L.dnnz, 256), 256, 0, s, L.dnnz,
            (const double *)L.dw.p, L.dw32.p);
@@ -971,9 +1080,8 @@ static void build_level(Helmholtz &H, Forest &f, HLevel &L) {
   }
   L.geo.alloc(4 * std::max(1LL, L.ne), s);
   L.geo32.alloc(4 * std::max(1LL, L.ne), s);
-  launch(k_h_geom, blocks_for(L.ne, 256), 256, 0, s, L.ne, (const int *)f.block.p,
-         (const int16_t *)f.level.p, (const double *)f.conn->d_boxes.p, H.r * H.r,
-         (HGeoT<double> *)L.geo.p, (HGeoT<float> *)L.geo32.p);
+  launch(k_h_geom, blocks_for(L.ne, 256), 256, 0, s, L.ne, L.dim, f.block, f.level, f.boxes,
+         H.r * H.r, (HGeoT<double> *)L.geo.p, (HGeoT<float> *)L.geo32.p);
   // scatter list
   DBuf<unsigned> cnt(nslot + 1, s);
   launch(k_h_scount, blocks_for(nslot, 256), 256, 0, s, nslot, (const int *)L.econn.p,
@@ -1006,7 +1114,7 @@ static void build_level(Helmholtz &H, Forest &f, HLevel &L) {
   err.zero();
   L.dinv.alloc(std::max(1LL, L.nn), s);
   L.dinv32.alloc(std::max(1LL, L.nn), s);
-  launch(k_h_diag, blocks_for(L.nn, 128), 128, 0, s, L.nn, L.ne, L.o, L.bas,
+  launch(k_h_diag, blocks_for(L.nn, 128), 128, 0, s, L.nn, L.ne, L.o, L.dim, L.bas,
          (const int *)L.srp.p, (const int *)L.sslot.p, (const double *)L.sw.p,
          (const HGeoT<double> *)L.geo.p, L.dinv.p, L.dinv32.p, err.p);
   if (read_scalar(err.p, s))
@@ -1014,8 +1122,10 @@ static void build_level(Helmholtz &H, Forest &f, HLevel &L) {
                               "(degenerate element geometry)");
 }
 
-void helmholtz_create(Forest *const *forests, int nlevels, double r, Helmholtz &H) {
-  Stage st("tmrg_helmholtz_create");
+// The levels and the P between consecutive forests (octree or quadtree).
+template <typename F, typename MakeP>
+static void helmholtz_levels(F *const *forests, int nlevels, double r, Helmholtz &H,
+                             MakeP &&make_p) {
   if (nlevels < 1) throw Error(TMRG_ERR_ARG, "Helmholtz filter: no forests");
   H.s = forests[0]->s;
   H.r = r;
@@ -1026,24 +1136,43 @@ void helmholtz_create(Forest *const *forests, int nlevels, double r, Helmholtz &
   H.sc.alloc(8 * HM_MAXVEC, s);
   for (int k = 0; k < nlevels; k++) {
     H.L.emplace_back(new HLevel);
-    build_level(H, *forests[k], *H.L.back());
+    build_level(H, source_of(*forests[k]), *H.L.back());
   }
   for (int k = 0; k + 1 < nlevels; k++) {
     H.P.emplace_back(new Interp);
     Interp &I = *H.P.back();
-    interp_create(*forests[k], *forests[k + 1], I);
+    make_p(*forests[k], *forests[k + 1], I);
     I.s = s;
     if (I.rows != H.L[k]->nn || I.cols != H.L[k + 1]->nn)
       throw Error(TMRG_ERR_INTERNAL, "Helmholtz filter: interpolation size mismatch");
     H.P32.emplace_back(new HInterp32);
-    HInterp32 &F = *H.P32.back();
-    F.p.alloc(std::max(1LL, I.nnz_nz), s);
-    F.pt.alloc(std::max(1LL, I.nnz_nz), s);
+    HInterp32 &P32 = *H.P32.back();
+    P32.p.alloc(std::max(1LL, I.nnz_nz), s);
+    P32.pt.alloc(std::max(1LL, I.nnz_nz), s);
     launch((k_h_cvt<double, float>), blocks_for(I.nnz_nz, 256), 256, 0, s, I.nnz_nz,
-           I.ap_vals(), F.p.p);
+           I.ap_vals(), P32.p.p);
     launch((k_h_cvt<double, float>), blocks_for(I.nnz_nz, 256), 256, 0, s, I.nnz_nz,
-           (const double *)I.t_vals.p, F.pt.p);
+           (const double *)I.t_vals.p, P32.pt.p);
   }
+}
+static void helmholtz_finish(Helmholtz &H);
+
+void helmholtz_create(Forest *const *forests, int nlevels, double r, Helmholtz &H) {
+  Stage st("tmrg_helmholtz_create");
+  helmholtz_levels(forests, nlevels, r, H,
+                   [](Forest &a, Forest &b, Interp &I) { interp_create(a, b, I); });
+  helmholtz_finish(H);
+}
+void helmholtz_create_quad(QForest *const *forests, int nlevels, double r, Helmholtz &H) {
+  Stage st("tmrg_helmholtz_create");
+  helmholtz_levels(forests, nlevels, r, H,
+                   [](QForest &a, QForest &b, Interp &I) { qinterp_create(a, b, I); });
+  helmholtz_finish(H);
+}
+
+static void helmholtz_finish(Helmholtz &H) {
+  const int nlevels = H.nlevels;
+  cudaStream_t s = H.s;
   // coarsest level
   HLevel &C = *H.L.back();
   H.nc = C.nn;
@@ -1052,7 +1181,7 @@ void helmholtz_create(Forest *const *forests, int nlevels, double r, Helmholtz &
     const long long n = C.nn;
     DBuf<double> A(std::max(1LL, n * n), s);
     A.zero();
-    launch(k_h_dense, blocks_for(n, 64), 64, 0, s, n, C.ne, C.o, C.bas, (const int *)C.srp.p,
+    launch(k_h_dense, blocks_for(n, 64), 64, 0, s, n, C.ne, C.o, C.dim, C.bas, (const int *)C.srp.p,
            (const int *)C.sslot.p, (const double *)C.sw.p, (const int *)C.econn.p,
            (const int *)C.dptr.p, (const int *)C.dconn.p, (const double *)C.dw.p,
            (const HGeoT<double> *)C.geo.p, A.p);

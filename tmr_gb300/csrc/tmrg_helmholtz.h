@@ -41,7 +41,7 @@ struct HWork {
 // preconditioner).
 struct HLevel {
   long long ne = 0, nn = 0, ndep = 0, dnnz = 0, snnz = 0;
-  int o = 2, npe = 8;
+  int dim = 3, o = 2, npe = 8;
   HBasisT<double> bas{};
   HBasisT<float> bas32{};
   DBuf<int> econn, dptr, dconn, srp, sslot;
@@ -85,6 +85,8 @@ struct Helmholtz {
 };
 
 void helmholtz_create(Forest *const *forests, int nlevels, double r, Helmholtz &H);
+struct QForest;
+void helmholtz_create_quad(QForest *const *forests, int nlevels, double r, Helmholtz &H);
 void helmholtz_apply(Helmholtz &H, bool transpose, int vpn, const double *in, double *out);
 void helmholtz_operator(Helmholtz &H, int level, bool stiff, int nvec, const double *in,
                         double *out);
