@@ -22,7 +22,7 @@ from oracle import build as ob  # noqa: E402
 from tests import pipeline  # noqa: E402
 
 CASES = ["c1_small", "brick_o2", "brick_o3", "rot_o2", "rot_o3", "rot_o4", "nocorner",
-         "uniform_o3", "mixed_o2"]
+         "uniform_o3", "mixed_o2", "gap_o2", "gap_o3"]
 
 
 def case_meta(case):
@@ -30,11 +30,11 @@ def case_meta(case):
     return json.dumps(meta, sort_keys=True)
 
 
-def main():
+def main(names=None):
     if ob.build_ref() is None:
         sys.exit("reference sources not found; set TMR_REFERENCE_SRC")
     allc = pipeline.cases()
-    for name in CASES:
+    for name in names or CASES:
         case = allc[name]
         r = pipeline.run_cpu(case, "ref")
         arrs = {
@@ -242,6 +242,9 @@ def make_quad_golden():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) > 1:  # only the named octree cases
+        main(sys.argv[1:])
+        sys.exit(0)
     main()
     make_api_golden()
     make_stl_golden()

@@ -26,6 +26,17 @@ def _csr_from_records(rows, ptr, cols, w, nrows):
     return interp_to_csr(rows, ptr, cols, w, nrows)
 
 
+def coarser(f, case):
+    """The next coarse forest: coarsen + balance, `coarse_steps` times
+    (two or more give fine elements several levels below their coarse
+    element)."""
+    c = f
+    for _ in range(case.get("coarse_steps", 1)):
+        c = c.coarsen()
+        c.balance(case.get("corner", 1))
+    return c
+
+
 def run_gpu(case):
     from tmr_gb300 import TMR
     order = case["order"]
@@ -43,8 +54,7 @@ def run_gpu(case):
     c = f
     forests = [f]
     for _ in range(case.get("coarse_levels", 1)):
-        cc = c.coarsen()
-        cc.balance(case.get("corner", 1))
+        cc = coarser(c, case)
         cc.createNodes()
         I = TMR.VecInterp()
         c.createInterpolation(cc, I)
@@ -78,8 +88,7 @@ def run_cpu(case, kind="oracle"):
                dep=f.getDepNodeConn(), sizes=f.nodeSizes(), levels=[])
     c = f
     for _ in range(case.get("coarse_levels", 1)):
-        cc = c.coarsen()
-        cc.balance(case.get("corner", 1))
+        cc = coarser(c, case)
         cc.createNodes()
         rows, ptr, cols, w = c.createInterpolation(cc)
         P = _csr_from_records(rows, ptr, cols, w, c.nodeSizes()["num_owned"])
@@ -185,6 +194,12 @@ def cases():
                          max_level=5, prob=0.3, seed=6, corner=0),
         "uniform_o3": dict(conn=W.brick(2, 1, 1), order=3, L0=2, passes=1, max_level=3,
                            prob=1.0, seed=1, interp=0),
+        # P across two or three levels (fine elements up to three levels
+        # below their coarse element)
+        "gap_o2": dict(conn=W.rotate_blocks(W.brick(2, 2, 1), 9), order=2, L0=1, passes=3,
+                       max_level=5, prob=0.4, seed=21, coarse_levels=1, coarse_steps=3),
+        "gap_o3": dict(conn=W.brick(2, 1, 1), order=3, L0=1, passes=3, max_level=5,
+                       prob=0.4, seed=22, coarse_levels=2, coarse_steps=2),
         # refinement arrays with -1 entries: coarsening inside refine
         "mixed_o2": dict(conn=W.rotate_blocks(W.brick(3, 2, 2), 8), order=2, L0=2, passes=3,
                          max_level=4, indicator="mixed", prob=0.35, coarsen_prob=0.3, seed=12,

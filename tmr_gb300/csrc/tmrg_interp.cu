@@ -31,6 +31,8 @@ struct InterpCtx {
   int fo, co;  // fine / coarse order
   double fk1[TMRG_MAX_ORDER], ck[TMRG_MAX_ORDER];  // 1 + fine knot, coarse knot
   double crk[TMRG_MAX_ORDER][TMRG_MAX_ORDER];     // 1/(ck_i - ck_j)
+  int fk1i[TMRG_MAX_ORDER];  // 1 + fine knot rounded to 0, 1 or 2 (orders 2, 3)
+  int fodd;                  // bit i: 1 + fine knot i is not that integer
   // fine octants
   const int *fb, *fx, *fy, *fz;
   const int16_t *fl;
@@ -48,6 +50,9 @@ struct InterpCtx {
   const uint8_t *ekind;
   const unsigned long long *rep;  // fine node -> element*npe + local index
   int *err;
+  // weight products by direction states (k_uvw_table), or null
+  const double *uvw;
+  int *wide;  // set when a fine element lies two or more levels below its coarse element
 };
 
 __global__ void k_pack_octs(long long n, const int *__restrict__ b,
@@ -290,6 +295,57 @@ __device__ __forceinline__ void dir_weights(const InterpCtx &I, int i, int range
   double u = __dadd_rn(-1.0, __dmul_rn(__dsub_rn(t, exact_double(ox)), two_ihc));
   lagrange3(I.co, u, I.ck, I.crk, n0, n1, n2);
 }
+
+// Direction states.  Fine orders 2 and 3 have 1 + k_i equal to 0, 1 or 2,
+// or (the middle Gauss-Lobatto knot -cos(pi/2)) 1 - 2^-53.  Where the fine
+// level lf is at most one below the coarse level lc and not above it when
+// a knot is of the second kind, the u that dir_weights computes is one of:
+//   s = 0..4: u = -1 + s/2 exactly.  With t = nx + 0.5 h (1 + k_i) exact
+//     (integers; for the inexact knot and nx >= h the 2^-53 term is below
+//     half an ulp of nx + h/2), num = 2 (nx - ox) + h (1 + k_i) - hc is a
+//     multiple of 2^(30 - max(lf, lc)) and u = num / hc.
+//   s = 6: the inexact knot at nx = ox = 0, lf = lc: u = -1 + (1 - 2^-53),
+//     which is -2^-53 whatever the level.  (At lf = lc + 1 the sum
+//     -1 + (1/2 - 2^-54) is a tie that rounds to -1/2, s = 1; the host
+//     checks it.)
+//   s = 5: an exact face hit (weights 1).
+// A row's three states index k_uvw_table's products, which repeat the
+// double sequence of dir_weights and the Nu Nv then Nw products on the same
+// u, so they are the same bits.
+__device__ __forceinline__ int dir_state(const InterpCtx &I, int i, int range, int32_t nx,
+                                         int32_t h, int lf, int32_t ox, int32_t hc, int lc) {
+  if (((range >> 2) - (range & 3)) == 1) return 5;
+  if (((I.fodd >> i) & 1) && nx == 0 && lf == lc) return 6;
+  const long long num = 2LL * (nx - ox) + (long long)h * I.fk1i[i] - hc;
+  const int lm = max(lf, lc);
+  const int m = (int)(num >> (TMRG_MAX_LEVEL - lm));
+  return m * (1 << (1 - (lm - lc))) + 2;
+}
+constexpr int UVW_DIR = 7, UVW_STATES = UVW_DIR * UVW_DIR * UVW_DIR;
+// tab[(su*49 + sv*7 + sw) * co^3 + ii + co*jj + co^2*kk] = (Nu[ii] Nv[jj]) Nw[kk];
+// fk1odd is 1 + the inexact fine knot (state 6).
+__global__ void k_uvw_table(InterpCtx I, double fk1odd, double *tab) {
+  const int co = I.co, cn3 = co * co * co;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= UVW_STATES * cn3) return;
+  const int st = t / cn3, li = t - st * cn3;
+  const int ss[3] = {st / (UVW_DIR * UVW_DIR), (st / UVW_DIR) % UVW_DIR, st % UVW_DIR};
+  const int ix[3] = {li % co, (li / co) % co, li / (co * co)};
+  double w[3];
+  for (int d = 0; d < 3; d++) {
+    double n[3] = {1.0, 1.0, 1.0};
+    if (ss[d] < 5) {
+      lagrange3(co, -1.0 + 0.5 * ss[d], I.ck, I.crk, n[0], n[1], n[2]);
+    } else if (ss[d] == 6) {
+      // dir_weights' sequence at nx = ox = 0, lf = lc = 10
+      const double tt = __dadd_rn(0.0, __dmul_rn(pow2(TMRG_MAX_LEVEL - 11), fk1odd));
+      const double u = __dadd_rn(-1.0, __dmul_rn(__dsub_rn(tt, 0.0), pow2(11 - TMRG_MAX_LEVEL)));
+      lagrange3(co, u, I.ck, I.crk, n[0], n[1], n[2]);
+    }
+    w[d] = n[ix[d]];
+  }
+  tab[t] = __dmul_rn(__dmul_rn(w[0], w[1]), w[2]);
+}
 // Bit l of the mask is set when local coarse node l = ii + jj*co + kk*co^2
 // lies in the row's box.
 __device__ __forceinline__ unsigned box_mask(int co, int rx, int ry, int rz) {
@@ -337,6 +393,10 @@ __global__ void k_interp_count(long long rows, InterpCtx I, int *trow, long long
   unsigned bm;
   long long t = row_box(I, row, node, info, cq, r, bm);
   trow[row] = (int)t;
+  if (I.wide && t >= 0) {
+    const int gap = node.level - (cq.x >> 26);
+    if ((gap > 1 || (gap < 0 && I.fodd)) && *(volatile int *)I.wide == 0) atomicOr(I.wide, 1);
+  }
   long long ne = 0;
   if (t >= 0) {
     const int kind = I.ekind[t];
@@ -378,14 +438,20 @@ __device__ __forceinline__ int nonzero_bits(double v) {
 // (row, column) in order and writes the run heads in order; the last run
 // of a non-final flush stays staged because it may continue.  *nzcount
 // gets the number of nonzero values written.
+//
+// TAB: the weight products come from the direction-state table (one FP64
+// multiply per staged entry, by its dependent weight or 1.0); phase A is
+// integer work.  The host picks it where every row's states exist.
 constexpr int IW_WARPS = 4;
 constexpr int IW_CAP = 256;  // staged entries per warp
+template <bool TAB>
 __global__ void __launch_bounds__(IW_WARPS * 32)
     k_interp_rows(long long rows, InterpCtx I, const int *__restrict__ trow,
                   const long long *__restrict__ roff, int *cols, double *vals,
                   unsigned long long *nzcount) {
-  __shared__ double s_uv[IW_WARPS][32][IMAX_CO * IMAX_CO];
-  __shared__ double s_nw[IW_WARPS][32][IMAX_CO];
+  __shared__ double s_uv[TAB ? 1 : IW_WARPS][32][IMAX_CO * IMAX_CO];
+  __shared__ double s_nw[TAB ? 1 : IW_WARPS][32][IMAX_CO];
+  __shared__ int s_st[IW_WARPS][32];  // TAB: the row's state * co^3
   __shared__ long long s_eo[IW_WARPS][32];
   __shared__ int s_vs[IW_WARPS][33];  // start of each row's list in the sequence
   __shared__ unsigned s_bm[IW_WARPS][32];
@@ -417,13 +483,19 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
         int4 cq = __ldg(I.c4 + t);
         int cl = cq.x >> 26;
         int32_t h = side_of(node.level), hc = side_of(cl);
-        const double half = pow2(TMRG_MAX_LEVEL - 1 - node.level);
-        const double two_ihc = pow2(cl + 1 - TMRG_MAX_LEVEL);
         int i = info % mo, j = (info % (mo * mo)) / mo, k = info / (mo * mo);
         int rx = dir_range(i, mo, co, node.x, h, cq.y, hc);
         int ry = dir_range(j, mo, co, node.y, h, cq.z, hc);
         int rz = dir_range(k, mo, co, node.z, h, cq.w, hc);
         bm = box_mask(co, rx, ry, rz);
+        if constexpr (TAB) {
+          const int su = dir_state(I, i, rx, node.x, h, node.level, cq.y, hc, cl);
+          const int sv = dir_state(I, j, ry, node.y, h, node.level, cq.z, hc, cl);
+          const int sw = dir_state(I, k, rz, node.z, h, node.level, cq.w, hc, cl);
+          s_st[warp][lane] = (su * UVW_DIR * UVW_DIR + sv * UVW_DIR + sw) * co * co2;
+        } else {
+        const double half = pow2(TMRG_MAX_LEVEL - 1 - node.level);
+        const double two_ihc = pow2(cl + 1 - TMRG_MAX_LEVEL);
         double u0, u1, u2, v0, v1, v2, w0, w1, w2;
         dir_weights(I, i, rx, node.x, half, cq.y, two_ihc, u0, u1, u2);
         dir_weights(I, j, ry, node.y, half, cq.z, two_ihc, v0, v1, v2);
@@ -437,6 +509,7 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
         s_nw[warp][lane][0] = w0;
         s_nw[warp][lane][1] = w1;
         s_nw[warp][lane][2] = w2;
+        }
       }
     }
     int incl = E;
@@ -468,8 +541,13 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
     for (int k = lane; k < end; k += 32) {
       const int sk = s_k[warp][k];
       const int q = sk >> 8;
-      s_v[warp][k] = __dmul_rn(__dmul_rn(s_uv[warp][q][sk & 15], s_nw[warp][q][(sk >> 4) & 15]),
-                               s_v[warp][k]);
+      if constexpr (TAB) {
+        const int li = ((sk >> 4) & 15) * co2 + (sk & 15);
+        s_v[warp][k] = __dmul_rn(__ldg(I.uvw + s_st[warp][q] + li), s_v[warp][k]);
+      } else {
+        s_v[warp][k] = __dmul_rn(
+            __dmul_rn(s_uv[warp][q][sk & 15], s_nw[warp][q][(sk >> 4) & 15]), s_v[warp][k]);
+      }
     }
     __syncwarp();
     // runs of equal (row, column) longer than one entry, listed densely so
@@ -870,6 +948,33 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
       c.crk[i][j] = (i != j && i < coarse.order && j < coarse.order)
                         ? 1.0 / (coarse.knots[i] - coarse.knots[j])
                         : 0.0;
+  // direction states (dir_state): fine orders 2 and 3, 1 + each fine knot
+  // within 2^-53 of 0, 1 or 2, at most one inexact, and the tie of an
+  // inexact knot one level below rounding to -1/2 as on the device
+  bool states = fine.order <= 3;
+  double fk1odd = 1.0;
+  c.fodd = 0;
+  for (int i = 0; i < TMRG_MAX_ORDER; i++) {
+    const double k1 = c.fk1[i];
+    const double r = k1 < 0.5 ? 0.0 : (k1 < 1.5 ? 1.0 : 2.0);
+    c.fk1i[i] = (int)r;
+    if (i >= fine.order) continue;
+    if (std::fabs(k1 - r) > std::ldexp(1.0, -53)) states = false;
+    if (k1 != r) {
+      c.fodd |= 1 << i;
+      fk1odd = k1;
+    }
+  }
+  if (__builtin_popcount((unsigned)c.fodd) > 1) states = false;
+  if (c.fodd) {
+    volatile double tt = std::ldexp(1.0, TMRG_MAX_LEVEL - 12) * fk1odd;  // lf = 11
+    volatile double x = tt * std::ldexp(1.0, 11 - TMRG_MAX_LEVEL);        // lc = 10
+    volatile double u = -1.0 + x;
+    if (u != -0.5) states = false;
+  }
+  DBuf<int> wide(1, s);
+  wide.zero();
+  c.wide = wide.p;
   // pass 1: enclosing octants and exact row lengths; pass 2: the rows
   DBuf<int> trow(rows + 1, s);
   DBuf<long long> roff(rows + 1, s);
@@ -877,6 +982,7 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   exclusive_scan<long long>(roff.p, roff.p, rows, s);
   const long long nnz = read_scalar(roff.p + rows, s);
   const int e = read_scalar(err.p, s);
+  states = states && read_scalar(wide.p, s) == 0;
   if (e == 2)
     throw Error(TMRG_ERR_INTERNAL,
                 "createInterpolation: a coarse element expands to more than 256 entries");
@@ -896,8 +1002,19 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   // compulsory traffic: the CSR entries written (12 B each) and per row
   // its first reference, element, and offset (20 B)
   prof_bytes(12 * nnz + 20 * rows);
-  launch(k_interp_rows, blocks_for(rows, IW_WARPS * 32), IW_WARPS * 32, 0, s, rows, c,
-         (const int *)trow.p, (const long long *)roff.p, I.colidx.p, I.vals.p, nzcount.p);
+  DBuf<double> uvw;
+  if (states) {
+    const int nt = UVW_STATES * cnpe;
+    uvw.alloc(nt, s);
+    launch(k_uvw_table, blocks_for(nt, 128), 128, 0, s, c, fk1odd, uvw.p);
+    c.uvw = uvw.p;
+    launch(k_interp_rows<true>, blocks_for(rows, IW_WARPS * 32), IW_WARPS * 32, 0, s, rows, c,
+           (const int *)trow.p, (const long long *)roff.p, I.colidx.p, I.vals.p, nzcount.p);
+  } else {
+    c.uvw = nullptr;
+    launch(k_interp_rows<false>, blocks_for(rows, IW_WARPS * 32), IW_WARPS * 32, 0, s, rows,
+           c, (const int *)trow.p, (const long long *)roff.p, I.colidx.p, I.vals.p, nzcount.p);
+  }
   trow.release();
   roff.release();
   EL = ElemLists();
