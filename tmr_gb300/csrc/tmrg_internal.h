@@ -80,15 +80,28 @@ struct Forest {
   OctKey oct_key() const;
 };
 
+// An entry the P / P^T applies keep: |w| >= 2^-49 (and Inf / NaN), from the
+// exponent bits (no FP64 compare).
+#ifdef __CUDACC__
+__device__ __forceinline__ int apply_keeps(double w) {
+  return (int)((__double_as_longlong(w) >> 52) & 0x7ff) >= 1023 - 49;
+}
+#endif
+
 struct Interp {
   cudaStream_t s = 0;
   long long rows = 0, cols = 0, nnz = 0;
   DBuf<int> rowptr, colidx;  // P, row-sorted CSR, every entry the reference keeps
   DBuf<double> vals;
-  // The applies run on P without its exactly-zero entries (with knots that
-  // are exact, a fine node on a coarse knot plane has zero weights for the
-  // other knots of that direction): same sums for finite inputs, fewer FP64
-  // operations.  Without zeros (nnz_nz == nnz) the applies use P itself.
+  // The applies run on P without its numerically-zero entries, |w| < 2^-49
+  // (apply_keeps): a fine node on a coarse knot plane has zero weights for
+  // the other knots of that direction, exactly 0 with exact knots and
+  // rounding residue below 4e-17 with the Gauss-Lobatto middle knot
+  // -cos(pi/2) = -6.1e-17 (about half of an order-3 P).  Leaving them out
+  // changes y_i = sum_j P_ij x_j by at most (dropped entries of row i)
+  // * 2^-49 * max |x_j|, below 1e-13 of max |x| for the row lengths of P;
+  // P itself (getCSR) keeps every entry.  Without such entries
+  // (nnz_nz == nnz) the applies use P itself.
   long long nnz_nz = 0;
   DBuf<int> nz_rowptr, nz_colidx;
   DBuf<double> nz_vals;

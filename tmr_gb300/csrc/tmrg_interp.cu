@@ -14,7 +14,7 @@
 // subsequence, so each coarse element's expansion is stably sorted by
 // column once, and a row is the in-box filter of that list with adjacent
 // equal columns summed in order.  Rows are written in two passes (exact
-// count, then write at the scanned offsets).  P^T is the zero-free matrix
+// count, then write at the scanned offsets).  P^T is the apply copy
 // re-sorted by (column, row), so transpose applies gather without atomics
 // and sum in a fixed order.
 #include <algorithm>
@@ -422,9 +422,6 @@ __global__ void k_interp_count(long long rows, InterpCtx I, int *trow, long long
   cnt[row] = ne;
 }
 
-__device__ __forceinline__ int nonzero_bits(double v) {
-  return (__double_as_longlong(v) << 1) != 0;
-}
 
 // Pass 2, 32 consecutive rows per warp; their entries form one contiguous
 // segment of the CSR.  Phase A, one lane per row: the element, its list
@@ -596,7 +593,7 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
         if (o < lim) {
           cols[o] = col;
           vals[o] = acc;
-          nzc += nonzero_bits(acc);
+          nzc += apply_keeps(acc);
         } else {
           atomicExch(I.err, 3);
         }
@@ -672,7 +669,7 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
   if (lane == 0 && nzc) atomicAdd(nzcount, (unsigned long long)nzc);
 }
 
-// Nonzero values per row (8 lanes per row).
+// Entries the applies keep, per row (8 lanes per row).
 __global__ void k_nz_count(long long rows, const int *__restrict__ rp,
                            const double *__restrict__ v, long long *cnt) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -680,7 +677,7 @@ __global__ void k_nz_count(long long rows, const int *__restrict__ rp,
   const int g8 = threadIdx.x & 7;
   int c = 0;
   if (r < rows)
-    for (int p = __ldg(rp + r) + g8; p < __ldg(rp + r + 1); p += 8) c += nonzero_bits(__ldg(v + p));
+    for (int p = __ldg(rp + r) + g8; p < __ldg(rp + r + 1); p += 8) c += apply_keeps(__ldg(v + p));
   c += __shfl_xor_sync(0xffffffffu, c, 1);
   c += __shfl_xor_sync(0xffffffffu, c, 2);
   c += __shfl_xor_sync(0xffffffffu, c, 4);
@@ -692,7 +689,7 @@ __global__ void k_ptr32(long long n, const long long *__restrict__ in, int *out)
   if (i <= n) out[i] = (int)in[i];
 }
 
-// Zero-free copy of P: 8 lanes per row keep the nonzero entries in order.
+// The apply copy of P: 8 lanes per row keep the apply_keeps entries in order.
 __global__ void k_nz_fill(long long rows, const int *__restrict__ rp,
                           const int *__restrict__ ci, const double *__restrict__ v,
                           const long long *__restrict__ nzoff, int *nrp, int *nci,
@@ -712,7 +709,7 @@ __global__ void k_nz_fill(long long rows, const int *__restrict__ rp,
     const int p = p0 + it * 8 + g8;
     const bool on = have && p < p1;
     const double w = on ? __ldg(v + p) : 0.0;
-    const bool nz = on && nonzero_bits(w);
+    const bool nz = on && apply_keeps(w);
     const unsigned mg = (__ballot_sync(0xffffffffu, nz) >> (grp * 8)) & 0xffu;
     if (nz) {
       const long long d = o + __popc(mg & ((1u << g8) - 1u));
@@ -1027,11 +1024,12 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
 }
 
 // The apply structures of a finished P (rows, cols, nnz, rowptr, colidx,
-// vals set): the zero-free copy when P has exact zeros, the length-ordered
+// vals set): the apply copy without numerically-zero entries, the length-ordered
 // row permutation and P^T.
 void interp_finish(Interp &I, long long nonzeros, cudaStream_t s) {
   const long long rows = I.rows, nnz = I.nnz;
-  // zero-free copy for the applies, when P has exact zeros  // worth a second copy only when zeros are a good part of P
+  // the apply copy (apply_keeps entries), worth a second copy only when the
+  // dropped entries are a good part of P
   I.nnz_nz = (nnz - nonzeros) * 8 >= nnz ? nonzeros : nnz;
   const long long nnz_nz = I.nnz_nz;
   if (I.nnz_nz < nnz) {

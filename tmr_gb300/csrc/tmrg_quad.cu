@@ -1361,7 +1361,7 @@ __global__ void k_q_row_fill(long long rows, QInterpCtx I, const int *__restrict
   if (r < rows) {
     int t = encl[r];
     int k = q_row<true>(I, r, &t, cols + rp[r], w + rp[r]);
-    for (int a = 0; a < k; a++) nz += (w[rp[r] + a] != 0.0);
+    for (int a = 0; a < k; a++) nz += apply_keeps(w[rp[r] + a]);
   }
   // one atomic per warp
   for (int o = 16; o; o >>= 1) nz += __shfl_xor_sync(0xffffffffu, nz, o);
