@@ -436,19 +436,16 @@ __global__ void k_interp_count(long long rows, InterpCtx I, int *trow, long long
 // of a non-final flush stays staged because it may continue.  *nzcount
 // gets the number of nonzero values written.
 //
-// TAB: the weight products come from the direction-state table (one FP64
-// multiply per staged entry, by its dependent weight or 1.0); phase A is
-// integer work.  The host picks it where every row's states exist.
+// This is the general kernel (any level gap, any knots of orders 2-3);
+// k_interp_elem covers the multigrid case with less work.
 constexpr int IW_WARPS = 4;
 constexpr int IW_CAP = 256;  // staged entries per warp
-template <bool TAB>
 __global__ void __launch_bounds__(IW_WARPS * 32)
     k_interp_rows(long long rows, InterpCtx I, const int *__restrict__ trow,
                   const long long *__restrict__ roff, int *cols, double *vals,
                   unsigned long long *nzcount) {
-  __shared__ double s_uv[TAB ? 1 : IW_WARPS][32][IMAX_CO * IMAX_CO];
-  __shared__ double s_nw[TAB ? 1 : IW_WARPS][32][IMAX_CO];
-  __shared__ int s_st[IW_WARPS][32];  // TAB: the row's state * co^3
+  __shared__ double s_uv[IW_WARPS][32][IMAX_CO * IMAX_CO];
+  __shared__ double s_nw[IW_WARPS][32][IMAX_CO];
   __shared__ long long s_eo[IW_WARPS][32];
   __shared__ int s_vs[IW_WARPS][33];  // start of each row's list in the sequence
   __shared__ unsigned s_bm[IW_WARPS][32];
@@ -485,12 +482,6 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
         int ry = dir_range(j, mo, co, node.y, h, cq.z, hc);
         int rz = dir_range(k, mo, co, node.z, h, cq.w, hc);
         bm = box_mask(co, rx, ry, rz);
-        if constexpr (TAB) {
-          const int su = dir_state(I, i, rx, node.x, h, node.level, cq.y, hc, cl);
-          const int sv = dir_state(I, j, ry, node.y, h, node.level, cq.z, hc, cl);
-          const int sw = dir_state(I, k, rz, node.z, h, node.level, cq.w, hc, cl);
-          s_st[warp][lane] = (su * UVW_DIR * UVW_DIR + sv * UVW_DIR + sw) * co * co2;
-        } else {
         const double half = pow2(TMRG_MAX_LEVEL - 1 - node.level);
         const double two_ihc = pow2(cl + 1 - TMRG_MAX_LEVEL);
         double u0, u1, u2, v0, v1, v2, w0, w1, w2;
@@ -506,7 +497,6 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
         s_nw[warp][lane][0] = w0;
         s_nw[warp][lane][1] = w1;
         s_nw[warp][lane][2] = w2;
-        }
       }
     }
     int incl = E;
@@ -538,13 +528,8 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
     for (int k = lane; k < end; k += 32) {
       const int sk = s_k[warp][k];
       const int q = sk >> 8;
-      if constexpr (TAB) {
-        const int li = ((sk >> 4) & 15) * co2 + (sk & 15);
-        s_v[warp][k] = __dmul_rn(__ldg(I.uvw + s_st[warp][q] + li), s_v[warp][k]);
-      } else {
-        s_v[warp][k] = __dmul_rn(
-            __dmul_rn(s_uv[warp][q][sk & 15], s_nw[warp][q][(sk >> 4) & 15]), s_v[warp][k]);
-      }
+      s_v[warp][k] = __dmul_rn(__dmul_rn(s_uv[warp][q][sk & 15], s_nw[warp][q][(sk >> 4) & 15]),
+                               s_v[warp][k]);
     }
     __syncwarp();
     // runs of equal (row, column) longer than one entry, listed densely so
@@ -667,6 +652,219 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) nzc += __shfl_xor_sync(0xffffffffu, nzc, o);
   if (lane == 0 && nzc) atomicAdd(nzcount, (unsigned long long)nzc);
+}
+
+// ---------------------------------------------------------------------
+// P rows grouped by coarse element (the direction-state case: every fine
+// element at most one level below its coarse element).  All rows whose
+// node lies in one coarse element filter the same sorted expansion list,
+// so one warp per coarse element loads the list into shared memory once
+// and handles its rows one after the other: a ballot compaction of the
+// in-box entries (list order kept), their weights (table product times the
+// dependent weight, as in k_interp_rows), and the in-order sums of equal
+// columns.  Same entries, same arithmetic, same bits as k_interp_rows.
+
+// Pass 1: each row's element (findEnclosing) and the rows per element.
+__global__ void k_interp_find(long long rows, InterpCtx I, int *trow, unsigned *ecnt) {
+  long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= rows) return;
+  const unsigned long long rr = I.rep[row];
+  const long long e = (long long)(rr >> 8);
+  const int info = (int)(rr & 255u);
+  const Oct node{I.fb[e], I.fx[e], I.fy[e], I.fz[e], I.fl[e]};
+  const long long t = find_enclosing(I, node, info);
+  trow[row] = (int)t;
+  if (t < 0) {
+    atomicExch(I.err, 1);
+    return;
+  }
+  atomicAdd(ecnt + t, 1u);
+  const int gap = node.level - (__ldg(I.c4 + t).x >> 26);
+  if ((gap > 1 || (gap < 0 && I.fodd)) && *(volatile int *)I.wide == 0) atomicOr(I.wide, 1);
+}
+// Rows by element: erows[estart[t] ..] lists the rows of element t (in no
+// particular order: each row's output place is fixed by its offset).
+__global__ void k_group_rows(long long rows, const int *__restrict__ trow,
+                             const unsigned *__restrict__ estart, unsigned *ecur, int *erows) {
+  long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= rows) return;
+  const int t = trow[row];
+  if (t < 0) return;
+  erows[estart[t] + atomicAdd(ecur + t, 1u)] = (int)row;
+}
+// Passes 2 (FILL = false: each row's merged length in cnt) and 3 (FILL:
+// the rows at roff, apply_keeps entries counted in *nzcount).  One warp per
+// coarse element, its rows 32 at a time, lane r <-> row r; the lanes walk
+// the element's sorted list in step (broadcast shared-memory reads):
+//   stage: the in-box (row, entry) pairs of list entries k0.. in list
+//     order, with each entry's rows mask and first pair;
+//   weights: the pairs' products on full warps (table value times the
+//     dependent weight, as in k_interp_rows);
+//   merge: lane r takes its pairs in list order and sums equal columns in
+//     that order; an add is issued only at list entries that repeat the
+//     previous entry's column (the list is sorted, so no other entry can
+//     continue a run).
+constexpr int EW_WARPS = 4;
+constexpr int EW_CAP = 256;  // staged pairs per warp
+template <bool FILL>
+__global__ void __launch_bounds__(EW_WARPS * 32)
+    k_interp_elem(long long n, InterpCtx I, const unsigned *__restrict__ estart,
+                  const int *__restrict__ erows, long long *cnt,
+                  const long long *__restrict__ roff, int *cols, double *vals,
+                  unsigned long long *nzcount) {
+  constexpr int FW = FILL ? EW_WARPS : 1;
+  __shared__ int s_col[EW_WARPS][IMAX_E];
+  __shared__ uint8_t s_key[EW_WARPS][IMAX_E];
+  __shared__ double s_dw[FW][IMAX_E];
+  __shared__ unsigned s_mk[FW][IMAX_E];   // rows (lanes) taking entry k
+  __shared__ uint16_t s_bk[FW][IMAX_E];   // staged position of its first pair
+  __shared__ uint8_t s_pr[FW][EW_CAP];    // staged pair: row lane
+  __shared__ uint8_t s_pk[FW][EW_CAP];    // staged pair: list entry
+  __shared__ double s_pv[FW][EW_CAP];     // staged pair: weight
+  __shared__ int s_st[FW][32];            // row state * co^3
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const long long t = (long long)blockIdx.x * EW_WARPS + warp;
+  if (t >= n) return;
+  const unsigned r0 = estart[t], r1 = estart[t + 1];
+  if (r0 == r1) return;
+  const long long eo = I.eoff[t];
+  const int E = (int)(I.eoff[t + 1] - eo);
+  if (E > IMAX_E) return;  // k_elist_fill flagged it; the host throws
+  const int kind = I.ekind[t];
+  for (int k = lane; k < E; k += 32) {
+    s_col[warp][k] = I.lcol[eo + k];
+    s_key[warp][k] = I.lkey[eo + k];
+    if (FILL) s_dw[FILL ? warp : 0][k] = I.ldw[eo + k];
+  }
+  const int fw = FILL ? warp : 0;
+  const int4 cq = __ldg(I.c4 + t);
+  const int cl = cq.x >> 26;
+  const int32_t hc = side_of(cl);
+  const int mo = I.fo, co = I.co, cn3 = co * co * co;
+  int nzc = 0;
+  for (unsigned b0 = r0; b0 < r1; b0 += 32) {
+    const int nb = (int)min(32u, r1 - b0);
+    const bool mine = lane < nb;
+    unsigned bm = 0;
+    int row = 0;
+    long long out = 0, lim = 0;
+    __syncwarp();
+    if (mine) {
+      row = erows[b0 + lane];
+      const unsigned long long rr = I.rep[row];
+      const long long e = (long long)(rr >> 8);
+      const int info = (int)(rr & 255u);
+      const int32_t nx = I.fx[e], ny = I.fy[e], nz = I.fz[e];
+      const int lf = I.fl[e];
+      const int32_t h = side_of(lf);
+      const int i = info % mo, j = (info % (mo * mo)) / mo, k = info / (mo * mo);
+      const int rx = dir_range(i, mo, co, nx, h, cq.y, hc);
+      const int ry = dir_range(j, mo, co, ny, h, cq.z, hc);
+      const int rz = dir_range(k, mo, co, nz, h, cq.w, hc);
+      bm = box_mask(co, rx, ry, rz);
+      if (FILL) {
+        int su = dir_state(I, i, rx, nx, h, lf, cq.y, hc, cl);
+        int sv = dir_state(I, j, ry, ny, h, lf, cq.z, hc, cl);
+        int sw = dir_state(I, k, rz, nz, h, lf, cq.w, hc, cl);
+        if ((unsigned)su >= UVW_DIR || (unsigned)sv >= UVW_DIR || (unsigned)sw >= UVW_DIR) {
+          atomicExch(I.err, 4);  // outside the table: reported, never read
+          su = sv = sw = 0;
+        }
+        s_st[fw][lane] = (su * UVW_DIR * UVW_DIR + sv * UVW_DIR + sw) * cn3;
+        out = roff[row];
+        lim = roff[row + 1];
+      }
+    }
+    if constexpr (!FILL) {
+      long long ne = 0;
+      if (kind == 0) {
+        ne = __popc(bm);
+      } else {
+        int pcol = -1;
+        for (int k = 0; k < E; k++) {
+          const int col = s_col[warp][k];
+          if ((bm >> (s_key[warp][k] & 31)) & 1u) {
+            ne += (kind == 1 || col != pcol);
+            pcol = col;
+          }
+        }
+      }
+      if (mine) cnt[row] = ne;
+    } else {
+      int pcol = -1;
+      double acc = 0.0;
+      for (int k0 = 0; k0 < E;) {
+        // stage entries k0..k1-1 (at most EW_CAP pairs)
+        int k1 = k0, nst = 0;
+        __syncwarp();
+        while (k1 < E && nst + 32 <= EW_CAP) {
+          const bool in = (bm >> (s_key[warp][k1] & 31)) & 1u;
+          const unsigned m = __ballot_sync(0xffffffffu, in);
+          if (in) {
+            const int p = nst + __popc(m & lt);
+            s_pr[fw][p] = (uint8_t)lane;
+            s_pk[fw][p] = (uint8_t)k1;
+          }
+          if (lane == 0) {
+            s_mk[fw][k1] = m;
+            s_bk[fw][k1] = (uint16_t)nst;
+          }
+          nst += __popc(m);
+          k1++;
+        }
+        __syncwarp();
+        for (int p = lane; p < nst; p += 32) {
+          const int k = s_pk[fw][p];
+          const double w = __ldg(I.uvw + s_st[fw][s_pr[fw][p]] + (s_key[warp][k] & 31));
+          s_pv[fw][p] = kind == 0 ? w : __dmul_rn(w, s_dw[fw][k]);
+        }
+        __syncwarp();
+        for (int k = k0; k < k1; k++) {
+          const unsigned m = s_mk[fw][k];
+          const int col = s_col[warp][k];
+          const bool in = (m >> lane) & 1u;
+          const bool cont = kind == 2 && k > 0 && s_col[warp][k - 1] == col;  // uniform
+          if (in) {
+            const double v = s_pv[fw][s_bk[fw][k] + __popc(m & lt)];
+            if (cont && col == pcol) {
+              acc = __dadd_rn(acc, v);
+            } else {
+              if (pcol >= 0) {
+                if (out < lim) {
+                  cols[out] = pcol;
+                  vals[out] = acc;
+                  nzc += apply_keeps(acc);
+                } else {
+                  atomicExch(I.err, 3);
+                }
+                out++;
+              }
+              pcol = col;
+              acc = v;
+            }
+          }
+        }
+        k0 = k1;
+      }
+      if (pcol >= 0) {
+        if (out < lim) {
+          cols[out] = pcol;
+          vals[out] = acc;
+          nzc += apply_keeps(acc);
+        } else {
+          atomicExch(I.err, 3);
+        }
+        out++;
+      }
+      if (mine && out != lim) atomicExch(I.err, 3);
+    }
+  }
+  if (FILL) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nzc += __shfl_xor_sync(0xffffffffu, nzc, o);
+    if (lane == 0 && nzc) atomicAdd(nzcount, (unsigned long long)nzc);
+  }
 }
 
 // Entries the applies keep, per row (8 lanes per row).
@@ -972,14 +1170,36 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   DBuf<int> wide(1, s);
   wide.zero();
   c.wide = wide.p;
-  // pass 1: enclosing octants and exact row lengths; pass 2: the rows
+  // enclosing octants and exact row lengths, then the rows: grouped by
+  // coarse element where the direction states cover every row, else one
+  // warp per 32 consecutive rows
   DBuf<int> trow(rows + 1, s);
   DBuf<long long> roff(rows + 1, s);
-  launch(k_interp_count, blocks_for(rows, 128), 128, 0, s, rows, c, trow.p, roff.p);
+  DBuf<unsigned> estart;
+  DBuf<int> erows;
+  if (states) {
+    estart.alloc(coarse.n + 1, s);
+    estart.zero();
+    launch(k_interp_find, blocks_for(rows, 128), 128, 0, s, rows, c, trow.p, estart.p);
+    states = read_scalar(wide.p, s) == 0 && read_scalar(err.p, s) == 0;
+  }
+  if (states) {
+    exclusive_scan<unsigned>(estart.p, estart.p, coarse.n, s);
+    DBuf<unsigned> ecur(coarse.n + 1, s);
+    ecur.zero();
+    erows.alloc(rows + 1, s);
+    launch(k_group_rows, blocks_for(rows, 256), 256, 0, s, rows, (const int *)trow.p,
+           (const unsigned *)estart.p, ecur.p, erows.p);
+    launch(k_interp_elem<false>, blocks_for(coarse.n, EW_WARPS), EW_WARPS * 32, 0, s, coarse.n,
+           c, (const unsigned *)estart.p, (const int *)erows.p, roff.p,
+           (const long long *)nullptr, (int *)nullptr, (double *)nullptr,
+           (unsigned long long *)nullptr);
+  } else {
+    launch(k_interp_count, blocks_for(rows, 128), 128, 0, s, rows, c, trow.p, roff.p);
+  }
   exclusive_scan<long long>(roff.p, roff.p, rows, s);
   const long long nnz = read_scalar(roff.p + rows, s);
   const int e = read_scalar(err.p, s);
-  states = states && read_scalar(wide.p, s) == 0;
   if (e == 2)
     throw Error(TMRG_ERR_INTERNAL,
                 "createInterpolation: a coarse element expands to more than 256 entries");
@@ -1005,20 +1225,26 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
     uvw.alloc(nt, s);
     launch(k_uvw_table, blocks_for(nt, 128), 128, 0, s, c, fk1odd, uvw.p);
     c.uvw = uvw.p;
-    launch(k_interp_rows<true>, blocks_for(rows, IW_WARPS * 32), IW_WARPS * 32, 0, s, rows, c,
-           (const int *)trow.p, (const long long *)roff.p, I.colidx.p, I.vals.p, nzcount.p);
+    launch(k_interp_elem<true>, blocks_for(coarse.n, EW_WARPS), EW_WARPS * 32, 0, s, coarse.n, c,
+           (const unsigned *)estart.p, (const int *)erows.p, (long long *)nullptr,
+           (const long long *)roff.p, I.colidx.p, I.vals.p, nzcount.p);
   } else {
     c.uvw = nullptr;
-    launch(k_interp_rows<false>, blocks_for(rows, IW_WARPS * 32), IW_WARPS * 32, 0, s, rows,
-           c, (const int *)trow.p, (const long long *)roff.p, I.colidx.p, I.vals.p, nzcount.p);
+    launch(k_interp_rows, blocks_for(rows, IW_WARPS * 32), IW_WARPS * 32, 0, s, rows, c,
+           (const int *)trow.p, (const long long *)roff.p, I.colidx.p, I.vals.p, nzcount.p);
   }
   trow.release();
   roff.release();
+  estart.release();
+  erows.release();
   EL = ElemLists();
   c4.release();
   rep.release();
   const long long nonzeros = (long long)read_scalar(nzcount.p, s);
-  if (read_scalar(err.p, s))
+  const int e2 = read_scalar(err.p, s);
+  if (e2 == 4)
+    throw Error(TMRG_ERR_INTERNAL, "createInterpolation: a direction state is out of range");
+  if (e2)
     throw Error(TMRG_ERR_INTERNAL, "createInterpolation: a row outgrew its counted length");
   interp_finish(I, nonzeros, s);
 }
