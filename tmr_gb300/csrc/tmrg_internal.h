@@ -140,7 +140,10 @@ void forest_balance(Forest &f, int corner);
 void forest_create_nodes(Forest &f);
 void interp_create(Forest &fine, Forest &coarse, Interp &I);
 void interp_apply(Interp &I, int which, const double *x, double *y, int nvec);
-void interp_finish(Interp &I, long long nonzeros, cudaStream_t s);
+// The apply structures of a finished P with `nonzeros` apply_keeps entries;
+// keepoff (optional, device) holds their exclusive per-row offsets.
+void interp_finish(Interp &I, long long nonzeros, cudaStream_t s,
+                   const long long *keepoff = nullptr);
 bool interp_apply_transpose_staged(Interp &I, int which, const double *xh, double *dx,
                                    double *y, int nvec);
 void topo_weights_create(Forest &filter, Forest &analysis, Interp &I);

@@ -693,7 +693,7 @@ __global__ void k_group_rows(long long rows, const int *__restrict__ trow,
   erows[estart[t] + atomicAdd(ecur + t, 1u)] = (int)row;
 }
 // Passes 2 (FILL = false: each row's merged length in cnt) and 3 (FILL:
-// the rows at roff, apply_keeps entries counted in *nzcount).  One warp per
+// the rows at roff, each row's apply_keeps entries counted in cnt).  One warp per
 // coarse element, its rows 32 at a time, lane r <-> row r; the lanes walk
 // the element's sorted list in step (broadcast shared-memory reads):
 //   stage: the in-box (row, entry) pairs of list entries k0.. in list
@@ -710,8 +710,7 @@ template <bool FILL>
 __global__ void __launch_bounds__(EW_WARPS * 32)
     k_interp_elem(long long n, InterpCtx I, const unsigned *__restrict__ estart,
                   const int *__restrict__ erows, long long *cnt,
-                  const long long *__restrict__ roff, int *cols, double *vals,
-                  unsigned long long *nzcount) {
+                  const long long *__restrict__ roff, int *cols, double *vals) {
   constexpr int FW = FILL ? EW_WARPS : 1;
   __shared__ int s_col[EW_WARPS][IMAX_E];
   __shared__ uint8_t s_key[EW_WARPS][IMAX_E];
@@ -742,10 +741,10 @@ __global__ void __launch_bounds__(EW_WARPS * 32)
   const int cl = cq.x >> 26;
   const int32_t hc = side_of(cl);
   const int mo = I.fo, co = I.co, cn3 = co * co * co;
-  int nzc = 0;
   for (unsigned b0 = r0; b0 < r1; b0 += 32) {
     const int nb = (int)min(32u, r1 - b0);
     const bool mine = lane < nb;
+    int nzc = 0;  // this lane's row: entries the applies keep
     unsigned bm = 0;
     int row = 0;
     long long out = 0, lim = 0;
@@ -858,12 +857,8 @@ __global__ void __launch_bounds__(EW_WARPS * 32)
         out++;
       }
       if (mine && out != lim) atomicExch(I.err, 3);
+      if (mine) cnt[row] = nzc;
     }
-  }
-  if (FILL) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) nzc += __shfl_xor_sync(0xffffffffu, nzc, o);
-    if (lane == 0 && nzc) atomicAdd(nzcount, (unsigned long long)nzc);
   }
 }
 
@@ -1077,7 +1072,7 @@ static void build_elists(Forest &coarse, ElemLists &L, int *err, cudaStream_t s)
          (const int *)coarse.dep_conn.p, (const double *)coarse.dep_w.p,
          (const long long *)L.eoff.p, L.lcol.p, L.ldw.p, L.lkey.p, L.ekind.p, err);
 }
-void interp_finish(Interp &I, long long nonzeros, cudaStream_t s);
+void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long long *keepoff);
 
 void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   Stage st("tmrg_create_interpolation");
@@ -1192,8 +1187,7 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
            (const unsigned *)estart.p, ecur.p, erows.p);
     launch(k_interp_elem<false>, blocks_for(coarse.n, EW_WARPS), EW_WARPS * 32, 0, s, coarse.n,
            c, (const unsigned *)estart.p, (const int *)erows.p, roff.p,
-           (const long long *)nullptr, (int *)nullptr, (double *)nullptr,
-           (unsigned long long *)nullptr);
+           (const long long *)nullptr, (int *)nullptr, (double *)nullptr);
   } else {
     launch(k_interp_count, blocks_for(rows, 128), 128, 0, s, rows, c, trow.p, roff.p);
   }
@@ -1220,14 +1214,16 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   // its first reference, element, and offset (20 B)
   prof_bytes(12 * nnz + 20 * rows);
   DBuf<double> uvw;
+  DBuf<long long> keep;  // per row: entries the applies keep
   if (states) {
     const int nt = UVW_STATES * cnpe;
     uvw.alloc(nt, s);
     launch(k_uvw_table, blocks_for(nt, 128), 128, 0, s, c, fk1odd, uvw.p);
     c.uvw = uvw.p;
+    keep.alloc(rows + 1, s);
     launch(k_interp_elem<true>, blocks_for(coarse.n, EW_WARPS), EW_WARPS * 32, 0, s, coarse.n, c,
-           (const unsigned *)estart.p, (const int *)erows.p, (long long *)nullptr,
-           (const long long *)roff.p, I.colidx.p, I.vals.p, nzcount.p);
+           (const unsigned *)estart.p, (const int *)erows.p, keep.p,
+           (const long long *)roff.p, I.colidx.p, I.vals.p);
   } else {
     c.uvw = nullptr;
     launch(k_interp_rows, blocks_for(rows, IW_WARPS * 32), IW_WARPS * 32, 0, s, rows, c,
@@ -1240,36 +1236,47 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   EL = ElemLists();
   c4.release();
   rep.release();
-  const long long nonzeros = (long long)read_scalar(nzcount.p, s);
+  long long nonzeros;
+  if (states) {
+    // the per-row counts become the apply copy's offsets
+    exclusive_scan<long long>(keep.p, keep.p, rows, s);
+    nonzeros = read_scalar(keep.p + rows, s);
+  } else {
+    nonzeros = (long long)read_scalar(nzcount.p, s);
+  }
   const int e2 = read_scalar(err.p, s);
   if (e2 == 4)
     throw Error(TMRG_ERR_INTERNAL, "createInterpolation: a direction state is out of range");
   if (e2)
     throw Error(TMRG_ERR_INTERNAL, "createInterpolation: a row outgrew its counted length");
-  interp_finish(I, nonzeros, s);
+  interp_finish(I, nonzeros, s, states ? keep.p : nullptr);
 }
 
 // The apply structures of a finished P (rows, cols, nnz, rowptr, colidx,
 // vals set): the apply copy without numerically-zero entries, the length-ordered
 // row permutation and P^T.
-void interp_finish(Interp &I, long long nonzeros, cudaStream_t s) {
+void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long long *keepoff) {
   const long long rows = I.rows, nnz = I.nnz;
   // the apply copy (apply_keeps entries), worth a second copy only when the
   // dropped entries are a good part of P
   I.nnz_nz = (nnz - nonzeros) * 8 >= nnz ? nonzeros : nnz;
   const long long nnz_nz = I.nnz_nz;
   if (I.nnz_nz < nnz) {
-    DBuf<long long> nzoff(rows + 1, s);
-    launch(k_nz_count, blocks_for(rows * 8, 256), 256, 0, s, rows, (const int *)I.rowptr.p,
-           (const double *)I.vals.p, nzoff.p);
-    exclusive_scan<long long>(nzoff.p, nzoff.p, rows, s);
+    DBuf<long long> nzoff;
+    if (!keepoff) {
+      nzoff.alloc(rows + 1, s);
+      launch(k_nz_count, blocks_for(rows * 8, 256), 256, 0, s, rows, (const int *)I.rowptr.p,
+             (const double *)I.vals.p, nzoff.p);
+      exclusive_scan<long long>(nzoff.p, nzoff.p, rows, s);
+      keepoff = nzoff.p;
+    }
     I.nz_rowptr.alloc(rows + 1, s);
     I.nz_colidx.alloc(nnz_nz + 1, s);
     I.nz_vals.alloc(nnz_nz + 1, s);
     if (rows == 0) TMRG_CUDA(cudaMemsetAsync(I.nz_rowptr.p, 0, sizeof(int), s));
     launch(k_nz_fill, blocks_for(((rows + 3) / 4) * 32, 256), 256, 0, s, rows,
            (const int *)I.rowptr.p, (const int *)I.colidx.p, (const double *)I.vals.p,
-           (const long long *)nzoff.p, I.nz_rowptr.p, I.nz_colidx.p, I.nz_vals.p);
+           keepoff, I.nz_rowptr.p, I.nz_colidx.p, I.nz_vals.p);
   }
 
   I.perm.alloc(rows + 1, s);
