@@ -173,7 +173,8 @@ def hierarchy(out):
     lv = [{"octants": fr.getNumOctants()} for fr in out["forests"]]
     for k, I in enumerate(out["interps"]):
         rows, cols, nnz = I.sizes()
-        lv[k].update({"P_rows": rows, "P_cols": cols, "P_nnz": nnz})
+        lv[k].update({"P_rows": rows, "P_cols": cols, "P_nnz": nnz,
+                      "P_apply_nnz": I.applyNnz()})
     return lv
 
 
@@ -418,6 +419,7 @@ def run_gpu(args):
     time.sleep(0.3)
     barrier()
     launches0 = TMR.kernel_launch_count()
+    syncs0 = TMR.host_sync_count()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record()
@@ -429,6 +431,7 @@ def run_gpu(args):
     barrier()
     clocks = clk.stop()
     launches = TMR.kernel_launch_count() - launches0
+    syncs = TMR.host_sync_count() - syncs0
     levels = hierarchy(last)
     del last
     def allreduce_max(v):
@@ -508,7 +511,8 @@ def run_gpu(args):
                        "hierarchy": levels,
                        "parallelism": "replicas x%d" % world,
                        "l2": "working set (GBs) larger than L2; no flush"},
-            "e2e": e2e, "gpu_launches": launches, "roofline": roof, "p_apply": p_apply,
+            "e2e": e2e, "gpu_launches": launches, "host_syncs": syncs,
+            "roofline": roof, "p_apply": p_apply,
             "filter_chain": chain,
             "cpu_baseline": cpu, "clocks": clocks, "kernels": kernels,
         }

@@ -245,6 +245,10 @@ int tmrg_topo_weights_create(tmrg_forest *filter, tmrg_forest *analysis,
                              tmrg_interp **out);
 /* out: {rows, cols, nnz} */
 int tmrg_interp_sizes(tmrg_interp *I, int64_t out3[3]);
+/* Entries the applies use: P without its numerically-zero weights
+   (|w| < 2^-49; for Gauss-Lobatto order 3 the rounding residue of the
+   middle knot -cos(pi/2)).  Equal to nnz when P has none. */
+int tmrg_interp_apply_nnz(tmrg_interp *I, int64_t *out);
 /* Row-sorted CSR of P, host copies. */
 int tmrg_interp_get_csr(tmrg_interp *I, int *rowptr, int *cols, double *w);
 /* The TACSBVecInterp applies used at TMRConformFilter.cpp:163 and
@@ -483,6 +487,9 @@ int tmrg_bump_indicator_device(tmrg_forest *f, const double *d_centres,
                                int min_level, int max_level, int *d_out);
 /* Number of kernels this library has launched in this process. */
 int64_t tmrg_kernel_launch_count(void);
+/* Number of device-to-host scalar reads that waited for a stream (sizes
+   the host needs before its next allocation). */
+int64_t tmrg_host_sync_count(void);
 /* Per-kernel timing for benchmarks (no counterpart in the reference, which
    has no GPU code): between begin and end every launch is bracketed by
    CUDA events on its stream.  end() writes a JSON object

@@ -31,6 +31,14 @@ def test_interp_applies_match_oracle(gpu_lib):
         rp, cols, vals = lev["P"]
         I = lev["I"]
         rows, ncols, nnz = I.sizes()
+        # the applies use the entries with |w| >= 2^-49 (a separate copy
+        # when at least 1/8 of P is below that: for Gauss-Lobatto order 3
+        # the rounding residue of the middle knot, about half of P); the
+        # products below still agree with the full P to 1e-13
+        kept = int((np.abs(vals) >= 2.0 ** -49).sum())
+        assert I.applyNnz() == (kept if (nnz - kept) * 8 >= nnz else nnz)
+        assert kept < 0.6 * nnz
+        assert np.abs(vals[np.abs(vals) < 2.0 ** -49]).max(initial=0.0) < 1e-15
         k = 16
         rng = np.random.default_rng(7)
         x = rng.standard_normal(ncols * k)

@@ -715,6 +715,14 @@ class VecInterp:
         call("tmrg_interp_sizes", self.ptr, _ptr(s))
         return int(s[0]), int(s[1]), int(s[2])
 
+    def applyNnz(self):
+        """Entries the applies use: P without its numerically-zero weights
+        (|w| < 2^-49), which changes no product by more than 1e-13 of
+        max |x|."""
+        n = ctypes.c_int64(0)
+        call("tmrg_interp_apply_nnz", self.ptr, ctypes.byref(n))
+        return int(n.value)
+
     def getCSR(self):
         rows, cols, nnz = self.sizes()
         rp = np.zeros(rows + 1, np.intc)
@@ -1118,6 +1126,10 @@ def _zeros_like(x, n):
 
 def kernel_launch_count():
     return int(lib().tmrg_kernel_launch_count())
+
+
+def host_sync_count():
+    return int(lib().tmrg_host_sync_count())
 
 
 def version():

@@ -21,6 +21,7 @@ _SIGS = {
     "tmrg_last_error": [],
     "tmrg_version": [],
     "tmrg_kernel_launch_count": [],
+    "tmrg_host_sync_count": [],
     "tmrg_profile_begin": [],
     "tmrg_profile_end": [c_vp, c_i64],
     "tmrg_measure_fp64_peak": [P(c_dbl)],
@@ -73,6 +74,7 @@ _SIGS = {
     "tmrg_interp_destroy": [c_vp],
     "tmrg_topo_weights_create": [c_vp, c_vp, P(c_vp)],
     "tmrg_interp_sizes": [c_vp, c_vp],
+    "tmrg_interp_apply_nnz": [c_vp, c_vp],
     "tmrg_interp_get_csr": [c_vp, c_vp, c_vp, c_vp],
     "tmrg_interp_mult": [c_vp, c_vp, c_vp, c_int],
     "tmrg_interp_mult_transpose": [c_vp, c_vp, c_vp, c_int],
@@ -135,6 +137,7 @@ _RESTYPE = {
     "tmrg_last_error": ctypes.c_char_p,
     "tmrg_version": ctypes.c_char_p,
     "tmrg_kernel_launch_count": c_i64,
+    "tmrg_host_sync_count": c_i64,
 }
 
 STATUS = {

@@ -269,6 +269,7 @@ extern "C" {
 const char *tmrg_last_error(void) { return g_last_error.c_str(); }
 const char *tmrg_version(void) { return "tmr_gb300 0.1 (sm_103a)"; }
 int64_t tmrg_kernel_launch_count(void) { return g_kernel_launches.load(); }
+int64_t tmrg_host_sync_count(void) { return g_host_syncs.load(); }
 
 // FP64 FMA throughput of the current device: 8 independent FMA chains per
 // thread over a grid of 8 blocks per SM; the denominator of the roofline of
@@ -983,6 +984,12 @@ int tmrg_interp_sizes(tmrg_interp *I, int64_t out3[3]) {
     out3[0] = I->I.rows;
     out3[1] = I->I.cols;
     out3[2] = I->I.nnz;
+  });
+}
+int tmrg_interp_apply_nnz(tmrg_interp *I, int64_t *out) {
+  return guarded([&] {
+    ARG(I && out, "NULL argument");
+    *out = I->I.nnz_nz;
   });
 }
 int tmrg_interp_get_csr(tmrg_interp *I, int *rowptr, int *cols, double *w) {

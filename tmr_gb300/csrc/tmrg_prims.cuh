@@ -23,6 +23,8 @@ struct Stage {
 };
 
 extern std::atomic<long long> g_kernel_launches;
+// device-to-host reads that wait for the stream (read_scalar)
+extern std::atomic<long long> g_host_syncs;
 
 // Optional per-kernel timing (tmrg_profile_begin/end): CUDA events recorded
 // on the launching stream around each launch, with the launch's
@@ -132,6 +134,7 @@ struct DBuf {
 template <typename T>
 inline T read_scalar(const T *d, cudaStream_t s) {
   T v;
+  g_host_syncs.fetch_add(1, std::memory_order_relaxed);
   TMRG_CUDA(cudaMemcpyAsync(&v, d, sizeof(T), cudaMemcpyDeviceToHost, s));
   TMRG_CUDA(cudaStreamSynchronize(s));
   return v;
