@@ -714,7 +714,6 @@ __global__ void __launch_bounds__(EW_WARPS * 32)
   constexpr int FW = FILL ? EW_WARPS : 1;
   __shared__ int s_col[EW_WARPS][IMAX_E];
   __shared__ uint8_t s_key[EW_WARPS][IMAX_E];
-  __shared__ double s_dw[FW][IMAX_E];
   __shared__ unsigned s_mk[FW][IMAX_E];   // rows (lanes) taking entry k
   __shared__ uint16_t s_bk[FW][IMAX_E];   // staged position of its first pair
   __shared__ uint8_t s_pr[FW][EW_CAP];    // staged pair: row lane
@@ -734,8 +733,8 @@ __global__ void __launch_bounds__(EW_WARPS * 32)
   for (int k = lane; k < E; k += 32) {
     s_col[warp][k] = I.lcol[eo + k];
     s_key[warp][k] = I.lkey[eo + k];
-    if (FILL) s_dw[FILL ? warp : 0][k] = I.ldw[eo + k];
   }
+  const double *ldw = I.ldw + eo;  // the element's dependent weights (L1)
   const int fw = FILL ? warp : 0;
   const int4 cq = __ldg(I.c4 + t);
   const int cl = cq.x >> 26;
@@ -816,7 +815,7 @@ __global__ void __launch_bounds__(EW_WARPS * 32)
         for (int p = lane; p < nst; p += 32) {
           const int k = s_pk[fw][p];
           const double w = __ldg(I.uvw + s_st[fw][s_pr[fw][p]] + (s_key[warp][k] & 31));
-          s_pv[fw][p] = kind == 0 ? w : __dmul_rn(w, s_dw[fw][k]);
+          s_pv[fw][p] = kind == 0 ? w : __dmul_rn(w, __ldg(ldw + k));
         }
         __syncwarp();
         for (int k = k0; k < k1; k++) {
