@@ -1171,6 +1171,10 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   DBuf<long long> roff(rows + 1, s);
   DBuf<unsigned> estart;
   DBuf<int> erows;
+  // a warp per coarse element pays off when the elements enclose enough
+  // rows to fill it (order 3: about 29 per element; order 2: about 8, where
+  // the per-row kernel is faster)
+  states = states && rows >= 16LL * coarse.n;
   if (states) {
     estart.alloc(coarse.n + 1, s);
     estart.zero();
