@@ -1379,8 +1379,9 @@ def filter_chain_metrics(TMR, steps=5):
     buf = ctypes.create_string_buffer(1 << 20)
     L.tmrg_profile_end(buf, len(buf))
     prof = json.loads(buf.value.decode())
-    fb = sum(v[2] for k, v in prof.items() if k.startswith("(k_fe_step") or k.startswith("k_fe_scale"))
-    fms = sum(v[1] for k, v in prof.items() if k.startswith("(k_fe_step") or k.startswith("k_fe_scale"))
+    fb = sum(v[2] for k, v in prof.items() if k.startswith("(k_fe_") or k.startswith("k_fe_"))
+    fms = sum(v[1] for k, v in prof.items() if k.startswith("(k_fe_") or k.startswith("k_fe_"))
+    ffl = sum(v[3] for k, v in prof.items() if k.startswith("(k_fe_") or k.startswith("k_fe_"))
     pb = sum(v[2] for k, v in prof.items() if "csr_apply" in k)
     pms = sum(v[1] for k, v in prof.items() if "csr_apply" in k)
     peak, _ = measured_peaks()
@@ -1388,6 +1389,28 @@ def filter_chain_metrics(TMR, steps=5):
     r32 = torch.empty_like(x32)
     F.applyFilter(x32, r32, vpn)
     err32 = float((r32.double() - rho).abs().max() / rho.abs().max())
+    # the FP32 filter forward + adjoint alone (HBM-bound: FP32 arithmetic is
+    # 64x the FP64 rate on GB300, so the FP64 filter at vpn 3 is bounded by
+    # the FP64 pipe at 0.5 flop per byte of M)
+    g32 = torch.empty_like(x32)
+    for _ in range(3):
+        F.applyFilter(x32, r32, vpn)
+        F.applyTranspose(r32, g32, vpn)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(steps):
+        F.applyFilter(x32, r32, vpn)
+        F.applyTranspose(r32, g32, vpn)
+    e1.record()
+    torch.cuda.synchronize()
+    ms32 = e0.elapsed_time(e1) / steps
+    L.tmrg_profile_begin()
+    F.applyFilter(x32, r32, vpn)
+    F.applyTranspose(r32, g32, vpn)
+    L.tmrg_profile_end(buf, len(buf))
+    prof32 = json.loads(buf.value.decode())
+    fb32 = sum(v[2] for k, v in prof32.items() if k.startswith("(k_fe_") or k.startswith("k_fe_"))
+    fms32 = sum(v[1] for k, v in prof32.items() if k.startswith("(k_fe_") or k.startswith("k_fe_"))
     return {
         "workload": FW["name"], "octants": fine.getNumOctants(),
         "filter_octants": coarse.getNumOctants(), "filter_nodes": n, "M_nnz": nnz_m,
@@ -1398,6 +1421,10 @@ def filter_chain_metrics(TMR, steps=5):
         "chain_gbs": (fb + pb) / (ms / 1e3) / 1e9,
         "chain_frac": ((fb + pb) / (ms / 1e3) / 1e9) / peak,
         "fp32_filter_rel_err": err32,
+        "filter_fp64_tflops": ffl / (fms / 1e3) / 1e12 if fms else None,
+        "filter32_fwd_adj_ms": ms32,
+        "filter32_gbs": fb32 / (fms32 / 1e3) / 1e9 if fms32 else None,
+        "filter32_frac": (fb32 / (fms32 / 1e3) / 1e9) / peak if fms32 else None,
     }
 
 

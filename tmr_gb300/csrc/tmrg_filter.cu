@@ -191,25 +191,69 @@ __global__ void k_fe_scale(long long n, int vpn, const T *__restrict__ s,
 //   forward:   y = B.(M x) + t1
 //   transpose: y = M(B.x) + t1
 // then y *= post (the final Tinv or Ainv) when post != nullptr.
+// ---------------------------------------------------------------------
+// Sliced-ELL copy of M (see Filter): per slice the longest row length,
+// then per position its row's entries at soff[slice] + 32 k + lane (CSR
+// order; the tail of a shorter row holds column = row, value 0, never
+// read).
+__global__ void k_sell_len(long long npos, long long n, const int *__restrict__ perm,
+                           const int *__restrict__ rp, int *srl, long long *ssz) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npos) return;
+  int len = 0;
+  if (p < n) {
+    const int row = perm[p];
+    len = rp[row + 1] - rp[row];
+  }
+  srl[p] = len;
+  // slice length: the longest row of the 32 positions (one warp)
+  int m = len;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((p & 31) == 0) ssz[p >> 5] = 32LL * m;
+}
+template <typename T>
+__global__ void k_sell_fill(long long npos, long long n, const int *__restrict__ perm,
+                            const int *__restrict__ rp, const int *__restrict__ cols,
+                            const T *__restrict__ vals, const long long *__restrict__ soff,
+                            int *scol, T *sval) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npos) return;
+  const long long sl = p >> 5;
+  const int L = (int)((soff[sl + 1] - soff[sl]) >> 5);
+  const long long base = soff[sl] + (p & 31);
+  const int row = p < n ? perm[p] : 0;
+  const int p0 = p < n ? rp[row] : 0, len = p < n ? rp[row + 1] - p0 : 0;
+  for (int k = 0; k < L; k++) {
+    scol[base + 32LL * k] = k < len ? cols[p0 + k] : row;
+    sval[base + 32LL * k] = k < len ? vals[p0 + k] : T(0);
+  }
+}
+
+// One Horner term on the sliced copy: thread p <-> row sperm[p], its
+// entries in CSR order (the same FMA sequence as k_fe_step).
 template <typename T, int VPN, bool TR>
 __global__ void __launch_bounds__(256)
-    k_fe_step(long long n, int vpn_rt, const int *__restrict__ rp,
-              const int *__restrict__ cols, const T *__restrict__ vals,
-              const T *__restrict__ B, const T *__restrict__ t1,
-              const T *__restrict__ x, T *__restrict__ y,
-              const T *__restrict__ post) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+    k_fe_sell(long long n, int vpn_rt, const int *__restrict__ perm, const int *__restrict__ srl,
+              const long long *__restrict__ soff, const int *__restrict__ scol,
+              const T *__restrict__ sval, const T *__restrict__ B, const T *__restrict__ t1,
+              const T *__restrict__ x, T *__restrict__ y, const T *__restrict__ post) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const long long i = perm[p];
+  const int len = srl[p];
+  const long long base = soff[p >> 5] + (p & 31);
   const int vpn = VPN > 0 ? VPN : vpn_rt;
   T acc[VPN > 0 ? VPN : 4];
   for (int c0 = 0; c0 < vpn; c0 += (VPN > 0 ? VPN : 4)) {
     const int nc = (VPN > 0) ? VPN : min(4, vpn - c0);
 #pragma unroll
     for (int v = 0; v < (VPN > 0 ? VPN : 4); v++) acc[v] = T(0);
-    for (int p = rp[i]; p < rp[i + 1]; p++) {
-      int j = __ldg(cols + p);
-      T m = __ldg(vals + p);
-      T bj = TR ? __ldg(B + j) : T(1);
+#pragma unroll 4
+    for (int k = 0; k < len; k++) {
+      const int j = __ldg(scol + base + 32LL * k);
+      const T m = __ldg(sval + base + 32LL * k);
+      const T bj = TR ? __ldg(B + j) : T(1);
 #pragma unroll
       for (int v = 0; v < (VPN > 0 ? VPN : 4); v++) {
         if (v < nc) {
@@ -219,12 +263,12 @@ __global__ void __launch_bounds__(256)
         }
       }
     }
-    T bi = TR ? T(1) : B[i];
-    T pi = post ? post[i] : T(1);
+    const T bi = TR ? T(1) : B[i];
+    const T pi = post ? post[i] : T(1);
 #pragma unroll
     for (int v = 0; v < (VPN > 0 ? VPN : 4); v++) {
       if (v < nc) {
-        long long o = i * vpn + c0 + v;
+        const long long o = i * vpn + c0 + v;
         T r = TR ? fadd(acc[v], t1[o]) : fadd(fmul(bi, acc[v]), t1[o]);
         if (post) r = fmul(r, pi);
         y[o] = r;
@@ -233,32 +277,41 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+template <typename T>
+static const T *sell_vals(const Filter &F);
+template <>
+const double *sell_vals<double>(const Filter &F) {
+  return F.sval.p;
+}
+template <>
+const float *sell_vals<float>(const Filter &F) {
+  return F.sval32.p;
+}
+
+// One Horner term (all vpn components) on the sliced copy of M.
 template <typename T, bool TR>
-static void launch_step(long long n, long long nnz, int vpn, const int *rp, const int *cols,
-                        const T *vals, const T *B, const T *t1, const T *x, T *y,
+static void launch_sell(const Filter &F, int vpn, const T *B, const T *t1, const T *x, T *y,
                         const T *post, cudaStream_t s) {
-  unsigned g = blocks_for(n, 256);
-  // compulsory traffic of one term: M (value + column), row pointers, B,
-  // t1, one read of x and one write of y (all vpn components)
-  prof_bytes((long long)(sizeof(T) + 4) * nnz + 4 * (n + 1) + (long long)sizeof(T) * n +
+  const long long n = F.n;
+  const unsigned g = blocks_for(n, 256);
+  // compulsory traffic of one term: M (value + column), B, t1, one read of
+  // x and one write of y (all vpn components)
+  prof_bytes((long long)(sizeof(T) + 4) * F.nnz + 4 * (n + 1) + (long long)sizeof(T) * n +
              3LL * sizeof(T) * n * vpn + (post ? (long long)sizeof(T) * n : 0));
-  prof_flops(2LL * vpn * nnz);
+  prof_flops(2LL * vpn * F.nnz);
+  const T *sv = sell_vals<T>(F);
+#define TMRG_SELL(V)                                                                         \
+  launch((k_fe_sell<T, V, TR>), g, 256, 0, s, n, vpn, (const int *)F.sperm.p,               \
+         (const int *)F.srl.p, (const long long *)F.soff.p, (const int *)F.scol.p, sv, B, t1, \
+         x, y, post)
   switch (vpn) {
-    case 1:
-      launch((k_fe_step<T, 1, TR>), g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
-      break;
-    case 2:
-      launch((k_fe_step<T, 2, TR>), g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
-      break;
-    case 3:
-      launch((k_fe_step<T, 3, TR>), g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
-      break;
-    case 4:
-      launch((k_fe_step<T, 4, TR>), g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
-      break;
-    default:
-      launch((k_fe_step<T, 0, TR>), g, 256, 0, s, n, vpn, rp, cols, vals, B, t1, x, y, post);
+    case 1: TMRG_SELL(1); break;
+    case 2: TMRG_SELL(2); break;
+    case 3: TMRG_SELL(3); break;
+    case 4: TMRG_SELL(4); break;
+    default: TMRG_SELL(0);
   }
+#undef TMRG_SELL
 }
 
 // applyFilter / applyTranspose (TMRMatrixFilter.cpp:191-235).
@@ -280,15 +333,14 @@ static void horner(Filter &F, bool tr, int vpn, const T *in, T *out,
   }
   // ping-pong so that the last term lands in `out`
   const T *x = t1.p;
+  (void)vals;
   for (int k = 0; k < F.N; k++) {
     bool last = (k == F.N - 1);
     T *y = ((F.N - 1 - k) % 2 == 0) ? out : tmp.p;
     if (tr)
-      launch_step<T, true>(n, F.nnz, vpn, F.rowptr.p, F.colidx.p, vals, B, t1.p, x, y,
-                           last ? post : nullptr, s);
+      launch_sell<T, true>(F, vpn, B, t1.p, x, y, last ? post : nullptr, s);
     else
-      launch_step<T, false>(n, F.nnz, vpn, F.rowptr.p, F.colidx.p, vals, B, t1.p, x, y,
-                            last ? post : nullptr, s);
+      launch_sell<T, false>(F, vpn, B, t1.p, x, y, last ? post : nullptr, s);
     x = y;
   }
 }
@@ -365,11 +417,9 @@ void filter_apply_static(Filter &F, bool tr, int vpn, const double *in, double *
     bool last = (k == F.N - 1);
     double *y = ((F.N - 1 - k) % 2 == 0) ? out : tmp;
     if (tr)
-      launch_step<double, true>(n, F.nnz, vpn, F.rowptr.p, F.colidx.p, F.vals.p,
-                                F.B.p, t1, x, y, last ? post : nullptr, s);
+      launch_sell<double, true>(F, vpn, F.B.p, t1, x, y, last ? post : nullptr, s);
     else
-      launch_step<double, false>(n, F.nnz, vpn, F.rowptr.p, F.colidx.p, F.vals.p,
-                                 F.B.p, t1, x, y, last ? post : nullptr, s);
+      launch_sell<double, false>(F, vpn, F.B.p, t1, x, y, last ? post : nullptr, s);
     x = y;
   }
 }
@@ -427,6 +477,24 @@ void filter_create(Forest &f, double len, double r, int N, Filter &F) {
   F.Tinv.alloc(n, s);
   launch(k_fe_scalings, blocks_for(n, 256), 256, 0, s, n, (const int *)F.rowptr.p,
          (const double *)F.vals.p, r, F.Ainv.p, F.B.p);
+  // the sliced-ELL copy the Horner steps read
+  {
+    const long long nsl = (n + 31) / 32;
+    F.npos = nsl * 32;
+    F.sperm.alloc(std::max(1LL, n), s);
+    F.srl.alloc(std::max(1LL, F.npos), s);
+    F.soff.alloc(nsl + 1, s);
+    if (n) len_order(n, (const int *)F.rowptr.p, F.sperm.p, s);
+    launch(k_sell_len, blocks_for(F.npos, 256), 256, 0, s, F.npos, n, (const int *)F.sperm.p,
+           (const int *)F.rowptr.p, F.srl.p, F.soff.p);
+    exclusive_scan<long long>(F.soff.p, F.soff.p, nsl, s);
+    F.nsell = read_scalar(F.soff.p + nsl, s);
+    F.scol.alloc(std::max(1LL, F.nsell), s);
+    F.sval.alloc(std::max(1LL, F.nsell), s);
+    launch((k_sell_fill<double>), blocks_for(F.npos, 256), 256, 0, s, F.npos, n,
+           (const int *)F.sperm.p, (const int *)F.rowptr.p, (const int *)F.colidx.p,
+           (const double *)F.vals.p, (const long long *)F.soff.p, F.scol.p, F.sval.p);
+  }
   // Tinv = 1 / (F~ 1) with Tinv = 1 during the evaluation.
   {
     DBuf<double> ones(n, s), y(n, s);
@@ -441,6 +509,9 @@ void filter_create(Forest &f, double len, double r, int N, Filter &F) {
     TMRG_CUDA(cudaStreamSynchronize(s));
   }
   F.vals32.alloc(nnz + 1, s);
+  F.sval32.alloc(std::max(1LL, F.nsell), s);
+  launch(k_to_f32<float>, blocks_for(F.nsell, 256), 256, 0, s, F.nsell,
+         (const double *)F.sval.p, F.sval32.p);
   F.Ainv32.alloc(n, s);
   F.B32.alloc(n, s);
   F.Tinv32.alloc(n, s);

@@ -127,6 +127,15 @@ struct Filter {
   DBuf<float> vals32;
   DBuf<double> Ainv, B, Tinv;
   DBuf<float> Ainv32, B32, Tinv32;
+  // M as sliced ELL for the Horner steps: rows in length order inside
+  // 4096-row windows (sperm, with each position's row length in srl),
+  // slices of 32 positions stored entry-major from soff[slice], so a warp
+  // reads its rows' k-th entries as one contiguous run
+  long long npos = 0, nsell = 0;
+  DBuf<int> sperm, srl, scol;
+  DBuf<long long> soff;
+  DBuf<double> sval;
+  DBuf<float> sval32;
 };
 
 // Operations (tmrg_forest.cu, tmrg_nodes.cu, tmrg_interp.cu,
@@ -148,6 +157,8 @@ bool interp_apply_transpose_staged(Interp &I, int which, const double *xh, doubl
                                    double *y, int nvec);
 void topo_weights_create(Forest &filter, Forest &analysis, Interp &I);
 void filter_create(Forest &f, double len, double r, int N, Filter &F);
+// Rows in length order inside 4096-row windows (perm[position] = row).
+void len_order(long long rows, const int *rp, int *perm, cudaStream_t s);
 void filter_apply(Filter &F, bool transpose, int vpn, const double *in,
                   double *out);
 void filter_apply_f32(Filter &F, bool transpose, int vpn, const float *in,

@@ -994,6 +994,11 @@ __global__ void __launch_bounds__(LO_THREADS)
       perm[w0 + atomicAdd(&s_off[b[k]], 1)] = list ? __ldg(list + r) : (int)r;
     }
 }
+void len_order(long long rows, const int *rp, int *perm, cudaStream_t s) {
+  launch(k_len_order, blocks_for(rows, LO_WIN), LO_THREADS, 0, s, rows, rp, (const int *)nullptr,
+         perm);
+}
+
 // P^T rows keyed by the input chunk holding their last (largest) input
 // row: chunk = last_row * TC_CHUNKS / n_in, empty rows in chunk 0.
 __global__ void k_t_chunk_keys(long long ncols, long long nin, const int *__restrict__ trp,
