@@ -280,6 +280,12 @@ int tmrg_interp_mult_weight_transpose_device(tmrg_interp *I, const double *x,
    assembled with dependent nodes condensed onto their independent nodes. */
 int tmrg_filter_create(tmrg_forest *f, double block_len, double r, int N,
                        tmrg_filter **out);
+/* The same filter on a quadtree forest (the TMRQuadForest constructor,
+   TMRMatrixFilter.cpp:39-46, and its 2-D scalings :133-137): bilinear
+   elements, every face a square of side `block_len`.  The applies and the
+   rest of the tmrg_filter_* calls are shared. */
+int tmrg_filter_create_quad(tmrg_qforest *f, double block_len, double r, int N,
+                            tmrg_filter **out);
 int tmrg_filter_destroy(tmrg_filter *F);
 /* out: {n (owned nodes), nnz of M} */
 int tmrg_filter_sizes(tmrg_filter *F, int64_t out2[2]);

@@ -124,3 +124,67 @@ def test_filter_interp_autograd_matches_fd(gpu_lib):
             fd = (obj(x + h * d) - obj(x - h * d)) / (2 * h)
         an = torch.dot(gx, d)
         assert abs(fd.item() - an.item()) <= 1e-6 * max(1.0, abs(an.item())), (k, fd.item(), an.item())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["brick_o2", "nocorner_o2"])
+def test_quad_filter_matches_restatement(gpu_lib, name):
+    """The matrix filter on a quadtree forest (TMRMatrixFilter's
+    TMRQuadForest constructor): M against the 2-D assembly of the Helmholtz
+    oracle (bilinear mass through the dependent weights), Ainv and B by the
+    reference's 2-D formulas (TMRMatrixFilter.cpp:133-137), and the apply
+    against its Horner recurrence (:191-211)."""
+    import scipy.sparse as sp
+
+    from oracle import helmholtz as HO
+    from tmr_gb300 import TMR
+    case = pipeline.quad_golden_case(name)
+    gold = pipeline.load_quad_golden(name)
+    f = TMR.QuadForest(order=2, interp=case.get("interp", 1))
+    f.setConnectivity(case["conn"])
+    f.createTrees(case["L0"])
+    for p in range(case["passes"]):
+        f.refine(pipeline.indicator(f.getQuadrantsArray(), case, p), 0, case["max_level"])
+        f.balance(case.get("corner", 1))
+    f.createNodes()
+    np.testing.assert_array_equal(f.getMeshConn(), gold["conn"])
+    c = f.coarsen()
+    c.balance(case.get("corner", 1))
+    c.createNodes()
+    F = TMR.MatrixFilter(R_FILTER, N_TERMS, None, [f, c])
+    n, nnz = F.size()
+    rp, cols, vals, A, B, T = F.getMatrix()
+    M = sp.csr_matrix((vals, cols, rp), shape=(n, n))
+    # square faces of side 1 (block_len): the box of face q is its own
+    # unit square, in its own frame
+    boxes = np.array([[0.0, 0.0, 1.0, 1.0]] * case["conn"].shape[0])
+    dp, dc, dw = gold["dep"]
+    _, Mo = HO.assemble2d(gold["quads"], gold["conn"], dp, dc, dw, n, 2,
+                          np.array([-1.0, 1.0]), boxes, 0.0)
+    assert abs(M - Mo).max() <= 1e-13 * abs(Mo).max()
+    D = np.asarray(Mo.sum(axis=1)).ravel()
+    r2 = R_FILTER * R_FILTER
+    Ao = 1.0 / (1.0 + r2 / D)
+    Bo = Ao * R_FILTER * R_FILTER / (D * D)
+    np.testing.assert_allclose(A, Ao, rtol=1e-13)
+    np.testing.assert_allclose(B, Bo, rtol=1e-13)
+
+    def horner(x, Tinv):
+        t1 = Ao * x
+        out = t1.copy()
+        for _ in range(N_TERMS):
+            out = Bo * (Mo @ out) + t1
+        return Tinv * out
+
+    To = 1.0 / horner(np.ones(n), np.ones(n))
+    np.testing.assert_allclose(T, To, rtol=1e-12)
+    x = np.random.default_rng(2).uniform(0.0, 1.0, n)
+    y = np.zeros(n)
+    F.applyFilter(x, y)
+    np.testing.assert_allclose(y, horner(x, To), rtol=1e-12)
+    F.applyFilter(np.ones(n), y)
+    np.testing.assert_allclose(y, 1.0, rtol=1e-12)
+    w = np.random.default_rng(3).standard_normal(n)
+    yt = np.zeros(n)
+    F.applyTranspose(w, yt)
+    assert w @ horner(x, To) == pytest.approx(yt @ x, rel=1e-11)

@@ -766,7 +766,8 @@ class MatrixFilter:
 
     ``MatrixFilter(r, N, assemblers, filters)`` as in the reference; the
     assemblers are ignored (no TACS) and the filter is built on
-    ``filters[0]``, whose blocks are cubes of side ``block_len``.  The
+    ``filters[0]`` (an OctForest whose blocks are cubes of side
+    ``block_len``, or a QuadForest whose faces are squares of that side).  The
     remaining forests form the restriction hierarchy used by
     ``setDesignVars`` (TMRConformFilter.cpp:75-91).
     """
@@ -775,8 +776,9 @@ class MatrixFilter:
         self.filters = list(filters)
         self.vpn = vpn
         h = _vp()
-        call("tmrg_filter_create", self.filters[0].ptr, float(block_len), float(r),
-             int(N), ctypes.byref(h))
+        name = ("tmrg_filter_create_quad" if isinstance(self.filters[0], QuadForest)
+                else "tmrg_filter_create")
+        call(name, self.filters[0].ptr, float(block_len), float(r), int(N), ctypes.byref(h))
         self.ptr = h
         self.interps = []
         for k in range(len(self.filters) - 1):

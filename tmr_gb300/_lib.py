@@ -83,6 +83,7 @@ _SIGS = {
     "tmrg_interp_mult_transpose_device": [c_vp, c_vp, c_vp, c_int],
     "tmrg_interp_mult_weight_transpose_device": [c_vp, c_vp, c_vp, c_int],
     "tmrg_filter_create": [c_vp, c_dbl, c_dbl, c_int, P(c_vp)],
+    "tmrg_filter_create_quad": [c_vp, c_dbl, c_dbl, c_int, P(c_vp)],
     "tmrg_filter_destroy": [c_vp],
     "tmrg_filter_sizes": [c_vp, c_vp],
     "tmrg_filter_get_matrix": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp],

@@ -1081,6 +1081,21 @@ int tmrg_filter_create(tmrg_forest *f, double block_len, double r, int N,
     *out = h;
   });
 }
+int tmrg_filter_create_quad(tmrg_qforest *f, double block_len, double r, int N,
+                            tmrg_filter **out) {
+  return guarded([&] {
+    ARG(f && out, "NULL argument");
+    ARG(block_len > 0.0 && r >= 0.0 && N >= 0, "bad filter parameters");
+    auto *h = new tmrg_filter;
+    try {
+      filter_create_quad(f->f, block_len, r, N, h->F);
+    } catch (...) {
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
 int tmrg_filter_destroy(tmrg_filter *F) {
   return guarded([&] {
     if (!F) return;

@@ -1,13 +1,14 @@
 // Matrix density filter (TMRMatrixFilter.cpp:30-235) on the GPU.
 //
-// Setup: the consistent mass matrix M of the trilinear elements of an
-// order-2 forest, with dependent nodes condensed onto the independent
-// nodes they interpolate.  Each element first merges its 8x8 element
+// Setup: the consistent mass matrix M of the trilinear (octree) or
+// bilinear (quadtree) elements of an order-2 forest, with dependent nodes
+// condensed onto the independent nodes they interpolate.  Each element
+// first merges its 8x8 (4x4) element
 // matrix, expanded through the dependent-node weights, into a dense
 // block over its distinct independent nodes; the blocks of all elements
 // are then sorted by (row, column) and summed in element order.  Then
-// D = M 1, Ainv = 1/(1 + r^2/D^(2/3)), B = Ainv r^2/(D^(2/3) D) and
-// Tinv = 1/(F~ 1).
+// D = M 1, Ainv = 1/(1 + r^2/D^(2/3)), B = Ainv r^2/(D^(2/3) D) (in 2-D
+// Ainv = 1/(1 + r^2/D), B = Ainv r^2/(D D)) and Tinv = 1/(F~ 1).
 //
 // Apply: Horner's recurrence out = B.(M out) + t1 (forward) or
 // out = M(B.out) + t1 (transpose), one fused CSR kernel per term over all
@@ -15,6 +16,7 @@
 #include <mutex>
 #include <string>
 
+#include "tmrg_quad.h"
 #include "tmrg_tree.cuh"
 
 namespace tmrg {
@@ -28,18 +30,20 @@ struct FilterCtx {
   double block_len;
   const int16_t *lev;
   int *err;
+  int npe, dim;  // 8 and 3 (octree) or 4 and 2 (quadtree)
 };
 
 // Merged element block: distinct nodes U[0..K) in first-appearance order
 // and L[u][v] summed over (a, b, p, q) in loop order.
 __device__ int element_block(const FilterCtx &c, long long e, int *U,
                              double (*L)[FMAXK]) {
-  const int *ec = c.conn + e * 8;
+  const int npe = c.npe;
+  const int *ec = c.conn + e * npe;
   int ni[8][4];
   double nw[8][4];
   int nc[8];
   int K = 0;
-  for (int a = 0; a < 8; a++) {
+  for (int a = 0; a < npe; a++) {
     int g = ec[a];
     if (g >= 0) {
       nc[a] = 1;
@@ -75,10 +79,14 @@ __device__ int element_block(const FilterCtx &c, long long e, int *U,
     for (int v = 0; v < K; v++) L[u][v] = 0.0;
   double side = c.block_len / (double)(1 << c.lev[e]);
   double s3 = __dmul_rn(__dmul_rn(side, side), side);
-  for (int a = 0; a < 8; a++)
-    for (int b = 0; b < 8; b++) {
+  const double s2 = __dmul_rn(side, side);
+  // exact mass of the linear element (corner a = i + 2j + 4k): the 1-D
+  // entries s/3 and s/6 multiplied over the directions, nd of which differ
+  for (int a = 0; a < npe; a++)
+    for (int b = 0; b < npe; b++) {
       int nd = ((a ^ b) & 1) + (((a ^ b) >> 1) & 1) + ((a ^ b) >> 2);
-      double mab = __ddiv_rn(s3, 27.0 * (double)(1 << nd));
+      double mab = c.dim == 3 ? __ddiv_rn(s3, 27.0 * (double)(1 << nd))
+                              : __ddiv_rn(s2, 9.0 * (double)(1 << nd));
       for (int p = 0; p < nc[a]; p++) {
         int u = 0;
         while (U[u] != ni[a][p]) u++;
@@ -140,7 +148,7 @@ __global__ void k_fe_first(long long E, const uint64_t *__restrict__ keys,
 }
 
 // D, Ainv, B (TMRMatrixFilter.cpp:121-147).
-__global__ void k_fe_scalings(long long n, const int *__restrict__ rp,
+__global__ void k_fe_scalings(long long n, int dim, const int *__restrict__ rp,
                               const double *__restrict__ vals, double r,
                               double *Ainv, double *B) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -150,6 +158,11 @@ __global__ void k_fe_scalings(long long n, const int *__restrict__ rp,
   if (D == 0.0) {
     Ainv[i] = 1.0;
     B[i] = 0.0;
+  } else if (dim == 2) {
+    double rr = __dmul_rn(r, r);
+    double a = __ddiv_rn(1.0, __dadd_rn(1.0, __ddiv_rn(rr, D)));
+    Ainv[i] = a;
+    B[i] = __ddiv_rn(__dmul_rn(__dmul_rn(a, r), r), __dmul_rn(D, D));
   } else {
     double t = pow(D, 2.0 / 3.0);
     double rr = __dmul_rn(r, r);
@@ -424,21 +437,46 @@ void filter_apply_static(Filter &F, bool tr, int vpn, const double *in, double *
   }
 }
 
+// What the filter needs from an octree or quadtree forest (nodes created).
+struct FSource {
+  cudaStream_t s;
+  int order, npe, dim;
+  long long ne, nn;
+  const int *econn, *dptr, *dconn;
+  const double *dw;
+  const int16_t *level;
+};
+static void filter_build(const FSource &f, double len, double r, int N, Filter &F);
+
 void filter_create(Forest &f, double len, double r, int N, Filter &F) {
   Stage st("tmrg_filter_create");
   if (f.order != 2)
     throw Error(TMRG_ERR_UNSUPPORTED, "matrix filter: order-2 forests only");
   forest_create_nodes(f);
+  filter_build(FSource{f.s, 2, 8, 3, f.n, f.num_owned, f.econn.p, f.dep_ptr.p, f.dep_conn.p,
+                       f.dep_w.p, f.level.p},
+               len, r, N, F);
+}
+void filter_create_quad(QForest &f, double len, double r, int N, Filter &F) {
+  Stage st("tmrg_filter_create");
+  if (f.order != 2)
+    throw Error(TMRG_ERR_UNSUPPORTED, "matrix filter: order-2 forests only");
+  qforest_create_nodes(f);
+  filter_build(FSource{f.s, 2, 4, 2, f.n, f.num_owned, f.econn.p, f.dep_ptr.p, f.dep_conn.p,
+                       f.dep_w.p, f.level.p},
+               len, r, N, F);
+}
+
+static void filter_build(const FSource &f, double len, double r, int N, Filter &F) {
   cudaStream_t s = f.s;
   F.s = s;
   F.N = N;
   F.r = r;
-  const long long n = f.num_owned, ne = f.n;
+  const long long n = f.nn, ne = f.ne;
   F.n = n;
   DBuf<int> err(1, s);
   err.zero();
-  FilterCtx c{f.econn.p, f.dep_ptr.p, f.dep_conn.p, f.dep_w.p, len,
-              f.level.p, err.p};
+  FilterCtx c{f.econn, f.dptr, f.dconn, f.dw, len, f.level, err.p, f.npe, f.dim};
   DBuf<unsigned> cnt(ne + 1, s);
   launch(k_fe_count, blocks_for(ne, 128), 128, 0, s, ne, c, cnt.p);
   exclusive_scan<unsigned>(cnt.p, cnt.p, ne, s);
@@ -475,7 +513,7 @@ void filter_create(Forest &f, double len, double r, int N, Filter &F) {
   F.Ainv.alloc(n, s);
   F.B.alloc(n, s);
   F.Tinv.alloc(n, s);
-  launch(k_fe_scalings, blocks_for(n, 256), 256, 0, s, n, (const int *)F.rowptr.p,
+  launch(k_fe_scalings, blocks_for(n, 256), 256, 0, s, n, f.dim, (const int *)F.rowptr.p,
          (const double *)F.vals.p, r, F.Ainv.p, F.B.p);
   // the sliced-ELL copy the Horner steps read
   {

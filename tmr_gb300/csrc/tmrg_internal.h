@@ -157,6 +157,8 @@ bool interp_apply_transpose_staged(Interp &I, int which, const double *xh, doubl
                                    double *y, int nvec);
 void topo_weights_create(Forest &filter, Forest &analysis, Interp &I);
 void filter_create(Forest &f, double len, double r, int N, Filter &F);
+struct QForest;
+void filter_create_quad(QForest &f, double len, double r, int N, Filter &F);
 // Rows in length order inside 4096-row windows (perm[position] = row).
 void len_order(long long rows, const int *rp, int *perm, cudaStream_t s);
 void filter_apply(Filter &F, bool transpose, int vpn, const double *in,
