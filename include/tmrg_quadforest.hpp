@@ -4,7 +4,8 @@
   (TMR_STLTools.h:44-77) and TMRHelmholtzFilter (TMRHelmholtzFilter.h:31-61)
   over the tmrg C ABI.  Header only; include after (or instead of)
   tmrg_octforest.hpp, whose TMRGEntity, TMRGVecInterp, TMRPoint and error
-  reporting it shares.
+  reporting it shares.  TMRMatrixFilter (TMRMatrixFilter.h:63-110) for
+  either forest type is here too.
 */
 #ifndef TMRG_QUADFOREST_HPP
 #define TMRG_QUADFOREST_HPP
@@ -263,6 +264,38 @@ class TMRHelmholtzFilter : public TMRGEntity {
 
  private:
   tmrg_helmholtz *H;
+};
+
+// TMRMatrixFilter (TMRMatrixFilter.h:63-110) over octree or quadtree filter
+// forests: the filter is built on filter[0] (order 2; blocks / faces are
+// cubes / squares of side block_len in place of the TACS assemblers'
+// geometry); applyFilter / applyTranspose on host vectors of vpn
+// interleaved components.  The restriction down the remaining forests
+// (setDesignVars) is the interpolation objects' multWeightTranspose.
+class TMRMatrixFilter : public TMRGEntity {
+ public:
+  TMRMatrixFilter(double r, int N, int nlevels, TMROctForest *filter[], double block_len = 1.0)
+      : F(nullptr) {
+    (void)nlevels;
+    tmrg_report(tmrg_filter_create(filter[0]->handle(), block_len, r, N, &F), "TMRMatrixFilter");
+  }
+  TMRMatrixFilter(double r, int N, int nlevels, TMRQuadForest *filter[], double block_len = 1.0)
+      : F(nullptr) {
+    (void)nlevels;
+    tmrg_report(tmrg_filter_create_quad(filter[0]->handle(), block_len, r, N, &F),
+                "TMRMatrixFilter");
+  }
+  ~TMRMatrixFilter() { tmrg_filter_destroy(F); }
+  void applyFilter(const double *in, double *out, int vpn = 1) {
+    tmrg_report(tmrg_filter_apply(F, vpn, in, out), "applyFilter");
+  }
+  void applyTranspose(const double *in, double *out, int vpn = 1) {
+    tmrg_report(tmrg_filter_apply_transpose(F, vpn, in, out), "applyTranspose");
+  }
+  tmrg_filter *handle() { return F; }
+
+ private:
+  tmrg_filter *F;
 };
 
 #endif

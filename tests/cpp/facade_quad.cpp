@@ -83,6 +83,24 @@ int main() {
     for (int k = 0; k < 3; k++) tsum += tris[i].p[k].x + tris[i].p[k].y + tris[i].p[k].z;
   delete[] tris;
   printf("stl_tris %d stl_sum %.17g local %d\n", ntris, tsum, nl);
+  // the matrix filter on an order-2 quadtree forest of the same faces
+  TMRQuadForest *q2 = new TMRQuadForest(0, 2, TMR_GAUSS_LOBATTO_POINTS);
+  q2->incref();
+  q2->setConnectivity((nx + 1) * (ny + 1), conn.data(), nx * ny);
+  q2->createTrees(3);
+  q2->createNodes();
+  int n2;
+  q2->getNodeConn(nullptr, nullptr, &n2);
+  TMRMatrixFilter *mf = new TMRMatrixFilter(0.1, 10, 1, &q2);
+  mf->incref();
+  std::vector<double> fx(n2), fy(n2);
+  for (int i = 0; i < n2; i++) fx[i] = (i % 5) * 0.25;
+  mf->applyFilter(fx.data(), fy.data());
+  double fsum = 0.0;
+  for (int i = 0; i < n2; i++) fsum += fy[i];
+  printf("filter_nodes %d filter_sum %.17g\n", n2, fsum);
+  mf->decref();
+  q2->decref();
   I->decref();
   c->decref();
   f->decref();

@@ -109,3 +109,15 @@ def test_quad_facade_matches_python_binding(gpu_lib, tmp_path):
     pts = TMR.getSTLTriangles(o, xv, offset=0, cutoff=0.4, vpn=1)
     assert int(vals["stl_tris"]) == len(pts) // 3 > 0
     assert float(vals["stl_sum"]) == pytest.approx(float(pts.sum()), rel=1e-13)
+    # the matrix filter facade on an order-2 quadtree forest = the binding
+    q2 = TMR.QuadForest(order=2)
+    q2.setConnectivity(W.brick2d(3, 2))
+    q2.createTrees(3)
+    q2.createNodes()
+    mf = TMR.MatrixFilter(0.1, 10, None, [q2])
+    n2 = mf.size()[0]
+    fx = (np.arange(n2) % 5) * 0.25
+    fy = np.zeros(n2)
+    mf.applyFilter(fx, fy)
+    assert int(vals["filter_nodes"]) == n2
+    assert float(vals["filter_sum"]) == pytest.approx(fy.sum(), rel=1e-12)
