@@ -329,8 +329,8 @@ static void launch_sell(const Filter &F, int vpn, const T *B, const T *t1, const
 
 // applyFilter / applyTranspose (TMRMatrixFilter.cpp:191-235).
 template <typename T>
-static void horner(Filter &F, bool tr, int vpn, const T *in, T *out,
-                   const T *vals, const T *Ainv, const T *B, const T *Tinv) {
+static void horner(Filter &F, bool tr, int vpn, const T *in, T *out, const T *Ainv,
+                   const T *B, const T *Tinv) {
   cudaStream_t s = F.s;
   long long n = F.n, len = n * vpn;
   if (n == 0) return;
@@ -346,7 +346,6 @@ static void horner(Filter &F, bool tr, int vpn, const T *in, T *out,
   }
   // ping-pong so that the last term lands in `out`
   const T *x = t1.p;
-  (void)vals;
   for (int k = 0; k < F.N; k++) {
     bool last = (k == F.N - 1);
     T *y = ((F.N - 1 - k) % 2 == 0) ? out : tmp.p;
@@ -360,11 +359,10 @@ static void horner(Filter &F, bool tr, int vpn, const T *in, T *out,
 
 void filter_apply(Filter &F, bool tr, int vpn, const double *in, double *out) {
   Stage st(tr ? "tmrg_filter_apply_transpose" : "tmrg_filter_apply");
-  horner<double>(F, tr, vpn, in, out, F.vals.p, F.Ainv.p, F.B.p, F.Tinv.p);
+  horner<double>(F, tr, vpn, in, out, F.Ainv.p, F.B.p, F.Tinv.p);
 }
 void filter_apply_f32(Filter &F, bool tr, int vpn, const float *in, float *out) {
-  horner<float>(F, tr, vpn, in, out, F.vals32.p, F.Ainv32.p, F.B32.p,
-                F.Tinv32.p);
+  horner<float>(F, tr, vpn, in, out, F.Ainv32.p, F.B32.p, F.Tinv32.p);
 }
 
 // ---------------------------------------------------------------------
@@ -546,15 +544,12 @@ static void filter_build(const FSource &f, double len, double r, int N, Filter &
            F.Tinv.p);
     TMRG_CUDA(cudaStreamSynchronize(s));
   }
-  F.vals32.alloc(nnz + 1, s);
   F.sval32.alloc(std::max(1LL, F.nsell), s);
   launch(k_to_f32<float>, blocks_for(F.nsell, 256), 256, 0, s, F.nsell,
          (const double *)F.sval.p, F.sval32.p);
   F.Ainv32.alloc(n, s);
   F.B32.alloc(n, s);
   F.Tinv32.alloc(n, s);
-  launch(k_to_f32<float>, blocks_for(nnz, 256), 256, 0, s, nnz,
-         (const double *)F.vals.p, F.vals32.p);
   launch(k_to_f32<float>, blocks_for(n, 256), 256, 0, s, n,
          (const double *)F.Ainv.p, F.Ainv32.p);
   launch(k_to_f32<float>, blocks_for(n, 256), 256, 0, s, n,

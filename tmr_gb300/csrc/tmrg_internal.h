@@ -124,7 +124,6 @@ struct Filter {
   double r = 0.0;
   DBuf<int> rowptr, colidx;
   DBuf<double> vals;
-  DBuf<float> vals32;
   DBuf<double> Ainv, B, Tinv;
   DBuf<float> Ainv32, B32, Tinv32;
   // M as sliced ELL for the Horner steps: rows in length order inside

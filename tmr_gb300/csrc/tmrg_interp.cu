@@ -393,10 +393,6 @@ __global__ void k_interp_count(long long rows, InterpCtx I, int *trow, long long
   unsigned bm;
   long long t = row_box(I, row, node, info, cq, r, bm);
   trow[row] = (int)t;
-  if (I.wide && t >= 0) {
-    const int gap = node.level - (cq.x >> 26);
-    if ((gap > 1 || (gap < 0 && I.fodd)) && *(volatile int *)I.wide == 0) atomicOr(I.wide, 1);
-  }
   long long ne = 0;
   if (t >= 0) {
     const int kind = I.ekind[t];
