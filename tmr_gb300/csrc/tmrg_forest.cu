@@ -455,19 +455,25 @@ __device__ __forceinline__ unsigned gen_family(const ConnDev &c, PosKey P,
   return cnt;
 }
 
-__global__ void k_gen_count(long long n, ConnDev c, PosKey P, int level,
-                            int corner, const uint64_t *__restrict__ cur,
+// n bounds the families; *m (device) is their number, so the count of the
+// families need not be read back first (entries past it count 0).
+__global__ void k_gen_count(long long n, const unsigned *__restrict__ m, ConnDev c, PosKey P,
+                            int level, int corner, const uint64_t *__restrict__ cur,
                             unsigned *cnt) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (i >= (long long)*m) {
+    cnt[i] = 0;
+    return;
+  }
   Oct q = P.decode(cur[i], level);
   cnt[i] = gen_family<false>(c, P, q, corner, nullptr);
 }
-__global__ void k_gen_write(long long n, ConnDev c, PosKey P, int level,
-                            int corner, const uint64_t *__restrict__ cur,
+__global__ void k_gen_write(long long n, const unsigned *__restrict__ m, ConnDev c, PosKey P,
+                            int level, int corner, const uint64_t *__restrict__ cur,
                             const unsigned *__restrict__ offs, uint64_t *out) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || i >= (long long)*m) return;
   Oct q = P.decode(cur[i], level);
   gen_family<true>(c, P, q, corner, out + offs[i]);
 }
@@ -592,9 +598,14 @@ void forest_balance(Forest &f, int corner) {
   std::vector<long long> Sn(L + 2, 0);
   DBuf<uint64_t> gen;
   long long ngen = 0;
+  // One wait per level: the level's distinct families stay counted on the
+  // device (S[l] sized by the level's input), the next level's generated
+  // families are counted over that bound, and both counts come back
+  // together.
   for (int l = L; l >= 0; l--) {
     long long nseed = hi[l] - lo[l];
     long long tot = nseed + ngen;
+    DBuf<unsigned> upos;  // unique positions; upos[tot] = Sn[l]
     if (tot > 0) {
       DBuf<uint64_t> cat(tot, s);
       if (nseed)
@@ -603,19 +614,34 @@ void forest_balance(Forest &f, int corner) {
       if (ngen)
         TMRG_CUDA(cudaMemcpyAsync(cat.p + nseed, gen.p, ngen * sizeof(uint64_t),
                                   cudaMemcpyDeviceToDevice, s));
-      Sn[l] = sort_unique(cat, tot, pbits, ~0ULL, S[l], s);
+      radix_sort(cat, nullptr, tot, pbits, s);
+      upos.alloc(tot + 1, s);
+      launch(k_unique_flags, blocks_for(tot, 256), 256, 0, s, tot, (const uint64_t *)cat.p,
+             upos.p);
+      exclusive_scan<unsigned>(upos.p, upos.p, tot, s);
+      S[l].alloc(tot, s);
+      launch(k_unique_emit, blocks_for(tot, 256), 256, 0, s, tot, (const uint64_t *)cat.p,
+             (const unsigned *)upos.p, ~0ULL, S[l].p);
     }
     gen.release();
     ngen = 0;
-    if (l >= 2 && Sn[l] > 0) {
-      DBuf<unsigned> cnt(Sn[l] + 1, s);
-      launch(k_gen_count, blocks_for(Sn[l], 128), 128, 0, s, Sn[l], c, P, l,
-             corner, (const uint64_t *)S[l].p, cnt.p);
-      exclusive_scan<unsigned>(cnt.p, cnt.p, Sn[l], s);
-      ngen = read_scalar(cnt.p + Sn[l], s);
+    Sn[l] = 0;
+    if (tot == 0) continue;
+    if (l >= 2) {
+      DBuf<unsigned> cnt(tot + 1, s);
+      launch(k_gen_count, blocks_for(tot, 128), 128, 0, s, tot, (const unsigned *)upos.p + tot,
+             c, P, l, corner, (const uint64_t *)S[l].p, cnt.p);
+      exclusive_scan<unsigned>(cnt.p, cnt.p, tot, s);
+      const unsigned *dv[2] = {upos.p + tot, cnt.p + tot};
+      unsigned hv[2];
+      read_scalars(dv, hv, s);
+      Sn[l] = hv[0];
+      ngen = hv[1];
       gen.alloc(ngen, s);
-      launch(k_gen_write, blocks_for(Sn[l], 128), 128, 0, s, Sn[l], c, P, l,
-             corner, (const uint64_t *)S[l].p, (const unsigned *)cnt.p, gen.p);
+      launch(k_gen_write, blocks_for(tot, 128), 128, 0, s, tot, (const unsigned *)upos.p + tot,
+             c, P, l, corner, (const uint64_t *)S[l].p, (const unsigned *)cnt.p, gen.p);
+    } else {
+      Sn[l] = read_scalar(upos.p + tot, s);
     }
   }
   seeds.release();

@@ -131,6 +131,15 @@ struct DBuf {
   }
 };
 
+// Several device scalars after one wait for the stream.
+template <typename T, int K>
+inline void read_scalars(const T *const (&d)[K], T (&h)[K], cudaStream_t s) {
+  g_host_syncs.fetch_add(1, std::memory_order_relaxed);
+  for (int k = 0; k < K; k++)
+    TMRG_CUDA(cudaMemcpyAsync(&h[k], d[k], sizeof(T), cudaMemcpyDeviceToHost, s));
+  TMRG_CUDA(cudaStreamSynchronize(s));
+}
+
 template <typename T>
 inline T read_scalar(const T *d, cudaStream_t s) {
   T v;
