@@ -681,17 +681,24 @@ __device__ __forceinline__ unsigned q_gen_family(const QConnDev &c, QPos P, cons
     }
   return cnt;
 }
-__global__ void k_q_gen_count(long long n, QConnDev c, QPos P, int level, int corner,
-                              const uint64_t *__restrict__ cur, unsigned *cnt) {
+// n bounds the families; *m (device) is their number (entries past it
+// count 0), so it need not be read back before the count.
+__global__ void k_q_gen_count(long long n, const unsigned *__restrict__ m, QConnDev c, QPos P,
+                              int level, int corner, const uint64_t *__restrict__ cur,
+                              unsigned *cnt) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (i >= (long long)*m) {
+    cnt[i] = 0;
+    return;
+  }
   cnt[i] = q_gen_family<false>(c, P, P.decode(cur[i], level), corner, nullptr);
 }
-__global__ void k_q_gen_write(long long n, QConnDev c, QPos P, int level, int corner,
-                              const uint64_t *__restrict__ cur, const unsigned *__restrict__ offs,
-                              uint64_t *out) {
+__global__ void k_q_gen_write(long long n, const unsigned *__restrict__ m, QConnDev c, QPos P,
+                              int level, int corner, const uint64_t *__restrict__ cur,
+                              const unsigned *__restrict__ offs, uint64_t *out) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || i >= (long long)*m) return;
   q_gen_family<true>(c, P, P.decode(cur[i], level), corner, out + offs[i]);
 }
 __global__ void k_q_leaves(long long n, QPos P, QKey K, int level, const uint64_t *__restrict__ cur,
@@ -795,9 +802,11 @@ void qforest_balance(QForest &f, int corner) {
   std::vector<long long> Sn(L + 2, 0);
   DBuf<uint64_t> gen;
   long long ngen = 0;
+  // one wait per level, as in the octree balance
   for (int l = L; l >= 0; l--) {
     const long long nseed = hi[l] - lo[l];
     const long long tot = nseed + ngen;
+    DBuf<unsigned> upos;  // unique positions; upos[tot] = Sn[l]
     if (tot > 0) {
       DBuf<uint64_t> cat(tot, s);
       if (nseed)
@@ -806,19 +815,35 @@ void qforest_balance(QForest &f, int corner) {
       if (ngen)
         TMRG_CUDA(cudaMemcpyAsync(cat.p + nseed, gen.p, ngen * sizeof(uint64_t),
                                   cudaMemcpyDeviceToDevice, s));
-      Sn[l] = q_sort_unique(cat, tot, pbits, ~0ULL, S[l], s);
+      radix_sort(cat, nullptr, tot, pbits, s);
+      upos.alloc(tot + 1, s);
+      launch(k_q_unique_flags, blocks_for(tot, 256), 256, 0, s, tot, (const uint64_t *)cat.p,
+             upos.p);
+      exclusive_scan<unsigned>(upos.p, upos.p, tot, s);
+      S[l].alloc(tot, s);
+      launch(k_q_unique_emit, blocks_for(tot, 256), 256, 0, s, tot, (const uint64_t *)cat.p,
+             (const unsigned *)upos.p, ~0ULL, S[l].p);
     }
     gen.release();
     ngen = 0;
-    if (l >= 2 && Sn[l] > 0) {
-      DBuf<unsigned> cnt(Sn[l] + 1, s);
-      launch(k_q_gen_count, blocks_for(Sn[l], 128), 128, 0, s, Sn[l], c, P, l, corner,
-             (const uint64_t *)S[l].p, cnt.p);
-      exclusive_scan<unsigned>(cnt.p, cnt.p, Sn[l], s);
-      ngen = read_scalar(cnt.p + Sn[l], s);
+    Sn[l] = 0;
+    if (tot == 0) continue;
+    if (l >= 2) {
+      DBuf<unsigned> cnt(tot + 1, s);
+      launch(k_q_gen_count, blocks_for(tot, 128), 128, 0, s, tot,
+             (const unsigned *)upos.p + tot, c, P, l, corner, (const uint64_t *)S[l].p, cnt.p);
+      exclusive_scan<unsigned>(cnt.p, cnt.p, tot, s);
+      const unsigned *dv[2] = {upos.p + tot, cnt.p + tot};
+      unsigned hv[2];
+      read_scalars(dv, hv, s);
+      Sn[l] = hv[0];
+      ngen = hv[1];
       gen.alloc(std::max(1LL, ngen), s);
-      launch(k_q_gen_write, blocks_for(Sn[l], 128), 128, 0, s, Sn[l], c, P, l, corner,
-             (const uint64_t *)S[l].p, (const unsigned *)cnt.p, gen.p);
+      launch(k_q_gen_write, blocks_for(tot, 128), 128, 0, s, tot,
+             (const unsigned *)upos.p + tot, c, P, l, corner, (const uint64_t *)S[l].p,
+             (const unsigned *)cnt.p, gen.p);
+    } else {
+      Sn[l] = read_scalar(upos.p + tot, s);
     }
   }
   seeds.release();
