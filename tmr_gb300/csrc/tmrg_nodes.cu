@@ -549,11 +549,15 @@ __global__ void k_dep_write(long long n, DepCtx d, Knots kn,
                             const int *__restrict__ lconn,
                             const int *__restrict__ dptr,
                             const unsigned long long *__restrict__ writer,
-                            int *dconn, double *dw) {
+                            const int *__restrict__ order, int *dconn, double *dw) {
   // One thread per dependent node: its winning writer (element, edge or
   // face, position) fixes the parent edge/face whose nodes form the row.
-  long long di = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (di >= n) return;
+  // Threads take the nodes in `order` (edge rows first, then face rows),
+  // so a warp runs one kind: an edge row takes `order` node lookups, a
+  // face row order^2, and a warp of both kinds would run both paths.
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const long long di = order[t];
   const int o = d.order;
   unsigned long long w = writer[di];
   if (w == 0ULL) return;  // no writer: the row has length 0
@@ -591,6 +595,25 @@ __global__ void k_dep_write(long long n, DepCtx d, Knots kn,
     lagrange(o, v, kn, Nv);
     for (int j = 0; j < o * o; j++) dw[ptr + j] = __dmul_rn(Nu[j % o], Nv[j / o]);
   }
+}
+
+// Edge rows (writer on a parent edge) first, then the others, each in node
+// order: flag, scan, then place.
+__global__ void k_dep_edge_flag(long long n, const unsigned long long *__restrict__ writer,
+                                unsigned *flag) {
+  const long long di = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (di >= n) return;
+  const unsigned long long w = writer[di];
+  flag[di] = (w != 0ULL && ((w >> 6) & 31) < 16) ? 1u : 0u;
+}
+__global__ void k_dep_order(long long n, const unsigned long long *__restrict__ writer,
+                            const unsigned *__restrict__ epos, int *order) {
+  const long long di = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (di >= n) return;
+  const unsigned long long w = writer[di];
+  const bool edge = w != 0ULL && ((w >> 6) & 31) < 16;
+  const long long k = edge ? (long long)epos[di] : (long long)epos[n] + (di - (long long)epos[di]);
+  order[k] = (int)di;
 }
 
 // ---------------------------------------------------------------------
@@ -803,12 +826,19 @@ void forest_create_nodes(Forest &f) {
     for (int j = 0; j < TMRG_MAX_ORDER; j++)
       kn.r[i][j] = (i != j && i < o && j < o) ? 1.0 / (f.knots[i] - f.knots[j]) : 0.0;
   }
+  DBuf<unsigned> epos(nd + 1, s);
+  DBuf<int> order(nd + 1, s);
+  launch(k_dep_edge_flag, blocks_for(nd, 256), 256, 0, s, nd,
+         (const unsigned long long *)writer.p, epos.p);
+  exclusive_scan<unsigned>(epos.p, epos.p, nd, s);
+  launch(k_dep_order, blocks_for(nd, 256), 256, 0, s, nd, (const unsigned long long *)writer.p,
+         (const unsigned *)epos.p, order.p);
   launch(k_dep_write, blocks_for(nd, 128), 128, 0, s, nd, d, kn,
          (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
          (const int *)f.z.p, (const int16_t *)f.level.p,
          (const int16_t *)f.info.p, (const int *)lconn.p,
          (const int *)f.dep_ptr.p, (const unsigned long long *)writer.p,
-         f.dep_conn.p, f.dep_w.p);
+         (const int *)order.p, f.dep_conn.p, f.dep_w.p);
 
   // 5. global numbers
   DBuf<int> num(nl + 1, s);
