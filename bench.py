@@ -347,6 +347,7 @@ def run_reference(args):
     import multiprocessing as mp
     from oracle import build as ob
     ob.build_oracle()
+    ob.build_ref()
     kind = cpu_kind()
     pk = "ref" if kind == "reference" else "oracle"
     ncores = os.cpu_count() or 1
@@ -360,6 +361,14 @@ def run_reference(args):
             res = pool.map(_cpu_sample_worker, [pk] * ncores)
             tot += sum(u for u, _ in res)
         dt = time.perf_counter() - t0
+        port = None
+        if kind == "reference":
+            # the C restatement on the same sample, one step, for continuity
+            # with lines measured where the reference could not be built
+            t1 = time.perf_counter()
+            res = pool.map(_cpu_sample_worker, ["oracle"] * ncores)
+            port = {"value": sum(u for u, _ in res) / (time.perf_counter() - t1),
+                    "unit": "octants/s", "cores": ncores, "kind": "port"}
     value = tot / dt
     line = {
         "impl": "reference", "metric": "balanced+numbered octants/s", "value": value,
@@ -377,7 +386,12 @@ def run_reference(args):
         "e2e": {"value": value, "unit": "octants/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+    if kind == "reference":
+        line["cpu_baseline"]["binary"] = "oracle/_ref/libtmrref.so (TMROctant.cpp, " \
+            "TMROctForest.cpp, TMRBase.cpp compiled from the reference sources, one rank)"
+        line["port_baseline"] = port
     print(json.dumps(line), flush=True)
+
 
 
 def run_gpu(args):
@@ -444,7 +458,7 @@ def run_gpu(args):
     # e2e through the host-buffer C ABI
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(TMR, conn, W, args, barrier, world, x_fine)
+        e2e = run_e2e(TMR, conn, W, args, barrier, world, x_fine, tot_units // args.steps)
 
     # roofline of the dominant kernel (separate untimed, event-profiled step)
     prof = profile_step(TMR, conn, W, x_fine)
@@ -1428,7 +1442,10 @@ def filter_chain_metrics(TMR, steps=5):
     }
 
 
-def run_e2e(TMR, conn, W, args, barrier, world, x_fine):
+E2E_MIN_STEPS = 10
+
+
+def run_e2e(TMR, conn, W, args, barrier, world, x_fine, units_per_step):
     import torch
 
     from tmr_gb300 import workloads as Wk
@@ -1454,11 +1471,17 @@ def run_e2e(TMR, conn, W, args, barrier, world, x_fine):
     xh[:] = x_fine.cpu().numpy()
     buf = [pin(x_fine.numel(), torch.float64), pin(x_fine.numel(), torch.float64)]
     pre = {"refine": refine, "x": xh, "buf": buf}
-    steps = max(1, min(args.steps, 3))
-    gpu_pipeline(TMR, conn, W, host=True, prefetched=pre)
+    steps = max(E2E_MIN_STEPS, args.steps)
+    u, _o = gpu_pipeline(TMR, conn, W, host=True, prefetched=pre)
+    del _o
+    # the host-buffer arm must build the same forests as the resident arm
+    # (host draws vs device draws of the same seeded indicator)
+    if u != units_per_step:
+        raise RuntimeError("e2e arm built %d octants per step, the resident arm %d"
+                           % (u, units_per_step))
     barrier()
+    link0 = host_link_rates(x_fine)
     each = []
-    units = 0
     h2d = d2h = 0
     for _ in range(steps):
         # every step bracketed by a barrier (host-synchronous API: the
@@ -1467,18 +1490,48 @@ def run_e2e(TMR, conn, W, args, barrier, world, x_fine):
         u, o = gpu_pipeline(TMR, conn, W, host=True, prefetched=pre)
         barrier()
         each.append(time.perf_counter() - t0)
-        units = u
+        if u != units_per_step:
+            raise RuntimeError("e2e step built %d octants, expected %d" % (u, units_per_step))
         h2d, d2h = o["h2d"], o["d2h"]
+        del o
+    link1 = host_link_rates(x_fine)
     if world > 1:
         t = torch.tensor(each, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         each = [float(v) for v in t.cpu()]
-    # the median step: the host link is shared with other jobs on the
-    # machine, so single steps can stall
-    dt = float(np.median(each))
-    return {"value": units * world / dt, "unit": "octants/s", "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "steps": steps, "ms_per_step": 1000 * dt,
-            "statistic": "median step", "ms_each": [round(1000 * v, 2) for v in each]}
+    dt = float(np.mean(each))
+    med = float(np.median(each))
+    return {"value": units_per_step * world / dt, "unit": "octants/s",
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": steps,
+            "ms_per_step": 1000 * dt, "statistic": "mean step",
+            "median_value": units_per_step * world / med, "median_ms": 1000 * med,
+            "ms_each": [round(1000 * v, 2) for v in each],
+            "units_match_resident_arm": True,
+            # pinned host<->device copy rates of the shared host link,
+            # measured just before and just after the timed e2e steps
+            "link_gbs": {"h2d_before": link0[0], "d2h_before": link0[1],
+                         "h2d_after": link1[0], "d2h_after": link1[1]}}
+
+
+def host_link_rates(x_dev, reps=3):
+    """Best-of-`reps` pinned host->device and device->host copy rates (GB/s)
+    of one buffer the size of the fine-level vectors."""
+    import torch
+    h = torch.empty(x_dev.numel(), dtype=x_dev.dtype, pin_memory=True)
+    d = torch.empty_like(x_dev)
+    nb = x_dev.numel() * x_dev.element_size()
+    out = []
+    for src, dst in ((h, d), (d, h)):
+        best = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            dst.copy_(src, non_blocking=True)
+            torch.cuda.synchronize()
+            dtc = time.perf_counter() - t0
+            best = dtc if best is None else min(best, dtc)
+        out.append(round(nb / best / 1e9, 1))
+    return out
 
 
 def main():

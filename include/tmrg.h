@@ -496,6 +496,10 @@ int64_t tmrg_kernel_launch_count(void);
 /* Number of device-to-host scalar reads that waited for a stream (sizes
    the host needs before its next allocation). */
 int64_t tmrg_host_sync_count(void);
+/* Number of device buffers this library has allocated in this process (its
+   stream-ordered pool allocations); no counterpart in the reference.  An
+   entry point that must not allocate leaves it unchanged. */
+int64_t tmrg_device_alloc_count(void);
 /* Per-kernel timing for benchmarks (no counterpart in the reference, which
    has no GPU code): between begin and end every launch is bracketed by
    CUDA events on its stream.  end() writes a JSON object

@@ -1481,6 +1481,85 @@ static void label_dependent(oo_forest *f, int *nodes) {
   }
 }
 
+/* eval_bernstein_weights (TMRInterpolation.h:309-439): the weights of the
+   coarse edge's Bernstein control points for the control point u of the two
+   refined half-edges, u in [-(order-1), order-1].  The reference lists the
+   de Casteljau subdivision at t = 1/2 for orders 2-5: control point r of the
+   left half (u = r - (order-1)) takes C(r, i) / 2^r of coarse point i <= r,
+   control point r of the right half (u = r) takes
+   C(order-1-r, i-r) / 2^(order-1-r) of coarse point i >= r.  Every value is
+   a short dyadic fraction, exact in double.  Returns 1 (and writes nothing,
+   as the reference writes nothing) for orders outside 2-5. */
+static int bernstein_dep_weights(int order, int u, double *N) {
+  if (order < 2 || order > 5) return 1;
+  int p = order - 1;
+  for (int i = 0; i < order; i++) N[i] = 0.0;
+  if (u <= 0) {
+    int r = u + p;
+    double c = 1.0;
+    for (int i = 0; i <= r; i++) {
+      N[i] = c / (double)(1 << r);
+      c = c * (r - i) / (i + 1);
+    }
+  } else {
+    int r = u, m = p - r;
+    double c = 1.0;
+    for (int i = 0; i <= m; i++) {
+      N[r + i] = c / (double)(1 << m);
+      c = c * (m - i) / (i + 1);
+    }
+  }
+  return 0;
+}
+
+/* eval_bernstein_interp_weights (TMRInterpolation.h:441-560): degree
+   elevation weights of fine control point u on a coarse element one order
+   lower, exactly as the reference tabulates them.  Note that for coarse
+   order 4 the reference's rows u = 2 and u = 3 are the natural elevation
+   rows of u = 3 and u = 2 (the table is reproduced as written).  Returns 1
+   when the orders differ by more than one or the coarse order is outside
+   2-5 (the reference leaves N unset then). */
+static int bernstein_interp_weights(int mo, int co, int u, double *N) {
+  if (mo - co != 1 || co < 2 || co > 5 || u < 0 || u > mo - 1) return 1;
+  for (int i = 0; i < co; i++) N[i] = 0.0;
+  if (u == 0) {
+    N[0] = 1.0;
+  } else if (u == mo - 1) {
+    N[co - 1] = 1.0;
+  } else if (co == 2) {
+    N[0] = 0.5; N[1] = 0.5;
+  } else if (co == 3) {
+    if (u == 1) { N[0] = 1. / 3; N[1] = 2. / 3; }
+    else { N[1] = 2. / 3; N[2] = 1. / 3; }
+  } else if (co == 4) {
+    if (u == 1) { N[0] = 0.25; N[1] = 0.75; }
+    else if (u == 2) { N[2] = 0.75; N[3] = 0.25; }
+    else { N[1] = 0.5; N[2] = 0.5; }
+  } else {
+    if (u == 1) { N[0] = 0.2; N[1] = 0.8; }
+    else if (u == 2) { N[1] = 0.4; N[2] = 0.6; }
+    else if (u == 3) { N[2] = 0.6; N[3] = 0.4; }
+    else { N[3] = 0.8; N[4] = 0.2; }
+  }
+  return 0;
+}
+
+/* bernstein_shape_functions (TMRInterpolation.h:164-177): the Bernstein
+   basis at u in [-1, 1] by the reference's triangular recurrence. */
+static void bernstein(int order, double u, double *N) {
+  double u1 = 0.5 * (1.0 - u), u2 = 0.5 * (u + 1.0);
+  N[0] = 1.0;
+  for (int j = 1; j < order; j++) {
+    double s = 0.0;
+    for (int k = 0; k < j; k++) {
+      double t = N[k];
+      N[k] = s + u1 * t;
+      s = u2 * t;
+    }
+    N[j] = s;
+  }
+}
+
 static void lagrange(int order, double u, const double *knots, double *N) {
   for (int i = 0; i < order; i++) {
     N[i] = 1.0;
@@ -1667,6 +1746,10 @@ static void create_dep_conn(oo_forest *f, const int *nn, const onodes *N) {
         int ptr = f->dep_ptr[d];
         for (int j = 0; j < o; j++) f->dep_conn[ptr + j] = pen[j];
         int s = (ei < 4) ? x : (ei < 8) ? y : z;
+        if (f->interp == 2) { /* TMROctForest.cpp:5364-5373 */
+          bernstein_dep_weights(o, (o - 1) * (s - 1) + k, &f->dep_w[ptr]);
+          continue;
+        }
         double u = 1.0 * (s - 1) + 0.5 * (1.0 + f->knots[k]);
         lagrange(o, u, f->knots, &f->dep_w[ptr]);
       }
@@ -1681,6 +1764,27 @@ static void create_dep_conn(oo_forest *f, const int *nn, const onodes *N) {
           if (d >= 0) continue;
           d = -d - 1;
           if (f->dep_ptr[d + 1] - f->dep_ptr[d] != o * o) continue;
+          if (f->interp == 2) { /* TMROctForest.cpp:5453-5473 */
+            int ub = -(o - 1) + ii, vb = -(o - 1) + jj;
+            if (fi < 2) {
+              ub += (o - 1) * y;
+              vb += (o - 1) * z;
+            } else if (fi < 4) {
+              ub += (o - 1) * x;
+              vb += (o - 1) * z;
+            } else {
+              ub += (o - 1) * x;
+              vb += (o - 1) * y;
+            }
+            bernstein_dep_weights(o, ub, Nu);
+            bernstein_dep_weights(o, vb, Nv);
+            int ptr = f->dep_ptr[d];
+            for (int j = 0; j < o * o; j++) {
+              f->dep_conn[ptr + j] = pfn[j];
+              f->dep_w[ptr + j] = Nu[j % o] * Nv[j / o];
+            }
+            continue;
+          }
           double u = -1.0 + 0.5 * (1.0 + f->knots[ii]);
           double v = -1.0 + 0.5 * (1.0 + f->knots[jj]);
           if (fi < 2) {
@@ -1713,8 +1817,9 @@ static int cmp_int(const void *a, const void *b) {
 /* createNodes (TMROctForest.cpp:4064-4268), one rank. */
 void oo_create_nodes(oo_forest *f) {
   if (f->have_nodes) return;
-  if (f->interp == 2) {
-    fprintf(stderr, "tmr_oracle: Bernstein interpolation not restated\n");
+  if (f->interp == 2 && f->order > 5) {
+    /* the reference's eval_bernstein_weights covers orders 2-5 only */
+    fprintf(stderr, "tmr_oracle: Bernstein dependent weights exist for orders 2-5\n");
     abort();
   }
   dep_faces_edges(f);
@@ -1903,7 +2008,27 @@ static int unique_sort_iw(oo_iw *a, int n) {
   return j;
 }
 
-/* computeElemInterp (TMROctForest.cpp:6396-6594), Lagrange branch. */
+/* The 1-D weights of one direction of computeElemInterp: the coarse
+   basis (Lagrange at the coarse knots, or Bernstein: the basis at u when
+   the orders agree, the degree-elevation table when they differ) at the
+   fine node's coordinate. */
+static void dir_basis(oo_forest *fine, oo_forest *coarse, int i, int32_t nx, int32_t h,
+                      int32_t ox, int32_t hc, double *N) {
+  int mo = fine->order, co = coarse->order;
+  const double *kn = fine->knots;
+  if (fine->interp == 2 && mo != co) {
+    bernstein_interp_weights(mo, co, i, N);
+    return;
+  }
+  double u = -1.0 + 2.0 * (nx + 0.5 * h * (1.0 + kn[i]) - ox) / hc;
+  if (fine->interp == 2)
+    bernstein(mo, u, N);
+  else
+    lagrange(co, u, coarse->knots, N);
+}
+
+/* computeElemInterp (TMROctForest.cpp:6396-6594), Lagrange and Bernstein
+   branches. */
 static int elem_interp(oo_forest *fine, const oo_oct *node, oo_forest *coarse,
                        const oo_oct *oct, oo_iw *w) {
   int mo = fine->order, co = coarse->order;
@@ -1912,15 +2037,13 @@ static int elem_interp(oo_forest *fine, const oo_oct *node, oo_forest *coarse,
   int32_t h = side(node->level), hc = side(oct->level);
   double Nu[OO_MAX_ORDER], Nv[OO_MAX_ORDER], Nw[OO_MAX_ORDER];
   int is = 0, ie = co, js = 0, je = co, ks = 0, ke = co;
-  const double *kn = fine->knots;
   if ((i == 0 && oct->x == node->x) || (i == mo - 1 && oct->x == node->x + h)) {
     is = 0; ie = 1; Nu[0] = 1.0;
   } else if ((i == 0 && oct->x + hc == node->x) ||
              (i == mo - 1 && oct->x + hc == node->x + h)) {
     is = co - 1; ie = co; Nu[is] = 1.0;
   } else {
-    double u = -1.0 + 2.0 * (node->x + 0.5 * h * (1.0 + kn[i]) - oct->x) / hc;
-    lagrange(co, u, coarse->knots, Nu);
+    dir_basis(fine, coarse, i, node->x, h, oct->x, hc, Nu);
   }
   if ((j == 0 && oct->y == node->y) || (j == mo - 1 && oct->y == node->y + h)) {
     js = 0; je = 1; Nv[0] = 1.0;
@@ -1928,8 +2051,7 @@ static int elem_interp(oo_forest *fine, const oo_oct *node, oo_forest *coarse,
              (j == mo - 1 && oct->y + hc == node->y + h)) {
     js = co - 1; je = co; Nv[js] = 1.0;
   } else {
-    double v = -1.0 + 2.0 * (node->y + 0.5 * h * (1.0 + kn[j]) - oct->y) / hc;
-    lagrange(co, v, coarse->knots, Nv);
+    dir_basis(fine, coarse, j, node->y, h, oct->y, hc, Nv);
   }
   if ((k == 0 && oct->z == node->z) || (k == mo - 1 && oct->z == node->z + h)) {
     ks = 0; ke = 1; Nw[0] = 1.0;
@@ -1937,8 +2059,7 @@ static int elem_interp(oo_forest *fine, const oo_oct *node, oo_forest *coarse,
              (k == mo - 1 && oct->z + hc == node->z + h)) {
     ks = co - 1; ke = co; Nw[ks] = 1.0;
   } else {
-    double wv = -1.0 + 2.0 * (node->z + 0.5 * h * (1.0 + kn[k]) - oct->z) / hc;
-    lagrange(co, wv, coarse->knots, Nw);
+    dir_basis(fine, coarse, k, node->z, h, oct->z, hc, Nw);
   }
   const int *c = &coarse->econn[(long)co * co * co * oct->tag];
   int n = 0;

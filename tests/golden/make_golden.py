@@ -22,7 +22,8 @@ from oracle import build as ob  # noqa: E402
 from tests import pipeline  # noqa: E402
 
 CASES = ["c1_small", "brick_o2", "brick_o3", "rot_o2", "rot_o3", "rot_o4", "nocorner",
-         "uniform_o3", "mixed_o2", "gap_o2", "gap_o3"]
+         "uniform_o3", "mixed_o2", "gap_o2", "gap_o3", "pcoarse_o3", "pcoarse_o4",
+         "coarse_o4", "bern_o3", "bern_p3", "bern_o4", "bern_o5"]
 
 
 def case_meta(case):
@@ -57,6 +58,20 @@ def main(names=None):
         out = os.path.join(HERE, name + ".npz")
         np.savez_compressed(out, **arrs)
         print(name, len(r["oct"]), "octants ->", out, os.path.getsize(out), "bytes")
+
+
+def make_digest_golden():
+    """tests/golden/digest_<case>.npz: checksums, samples and moments of the
+    reference's products on the configuration-size cases (pipeline.py
+    digest_cases), which are too large to store whole."""
+    for name, case in pipeline.digest_cases().items():
+        r = pipeline.run_cpu(case, "ref")
+        d = pipeline.digest(r)
+        d["meta"] = np.array(case_meta(case))
+        d["block_conn"] = case["conn"]
+        out = os.path.join(HERE, "digest_" + name + ".npz")
+        np.savez_compressed(out, **d)
+        print("digest", name, len(r["oct"]), "octants ->", os.path.getsize(out), "bytes")
 
 
 def make_api_golden():
@@ -242,10 +257,14 @@ def make_quad_golden():
 
 
 if __name__ == "__main__":
-    if len(sys.argv) > 1:  # only the named octree cases
-        main(sys.argv[1:])
+    if len(sys.argv) > 1:  # only the named octree cases (or "digest")
+        if sys.argv[1:] == ["digest"]:
+            make_digest_golden()
+        else:
+            main(sys.argv[1:])
         sys.exit(0)
     main()
+    make_digest_golden()
     make_api_golden()
     make_stl_golden()
     make_quad_golden()

@@ -26,10 +26,23 @@ def _csr_from_records(rows, ptr, cols, w, nrows):
     return interp_to_csr(rows, ptr, cols, w, nrows)
 
 
-def coarser(f, case):
-    """The next coarse forest: coarsen + balance, `coarse_steps` times
+def hierarchy_steps(case):
+    """The coarse levels of a case: "h" = coarsen + balance (the geometric
+    step), "p" = duplicate + setMeshOrder(order - 1) on the same octants
+    (the order step createTopoProblem takes while the order is above its
+    lowest, TopOptUtils.py:80-88)."""
+    return case.get("hier") or ["h"] * case.get("coarse_levels", 1)
+
+
+def coarser(f, case, step="h", order=None):
+    """The next coarse forest.  "h": coarsen + balance, `coarse_steps` times
     (two or more give fine elements several levels below their coarse
-    element)."""
+    element).  "p": duplicate + setMeshOrder(order - 1), same octants and
+    knot family, not re-balanced (as TopOptUtils.py:82-85 does)."""
+    if step == "p":
+        c = f.duplicate()
+        c.setMeshOrder(order - 1, case.get("interp", 1))
+        return c
     c = f
     for _ in range(case.get("coarse_steps", 1)):
         c = c.coarsen()
@@ -53,8 +66,8 @@ def run_gpu(case):
                sizes=_gpu_sizes(f), levels=[])
     c = f
     forests = [f]
-    for _ in range(case.get("coarse_levels", 1)):
-        cc = coarser(c, case)
+    for step in hierarchy_steps(case):
+        cc = coarser(c, case, step, c.getMeshOrder())
         cc.createNodes()
         I = TMR.VecInterp()
         c.createInterpolation(cc, I)
@@ -87,8 +100,10 @@ def run_cpu(case, kind="oracle"):
     out = dict(oct=f.getOctants(), conn=f.getMeshConn(order), nn=f.getNodeNumbers(),
                dep=f.getDepNodeConn(), sizes=f.nodeSizes(), levels=[])
     c = f
-    for _ in range(case.get("coarse_levels", 1)):
-        cc = coarser(c, case)
+    for step in hierarchy_steps(case):
+        cc = coarser(c, case, step, order)
+        if step == "p":
+            order -= 1
         cc.createNodes()
         rows, ptr, cols, w = c.createInterpolation(cc)
         P = _csr_from_records(rows, ptr, cols, w, c.nodeSizes()["num_owned"])
@@ -140,10 +155,103 @@ GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 def golden_cases():
     """Names of the pipeline fixtures in tests/golden (api*.npz hold the
-    single-call getters and the STL output and are read by their own
-    tests)."""
+    single-call getters and the STL output, digest_*.npz the checksummed
+    configuration-size cases; each is read by its own tests)."""
     return sorted(f[:-4] for f in os.listdir(GOLDEN_DIR)
-                  if f.endswith(".npz") and not f.startswith(("api", "quad_")))
+                  if f.endswith(".npz") and not f.startswith(("api", "quad_", "digest_")))
+
+
+# ---------------------------------------------------------------------------
+# Configuration-size cases: too large to store whole, so their fixtures hold
+# a digest of every product (tests/golden/digest_<case>.npz).
+def digest_cases():
+    return {
+        # the one-tree configuration exactly as specified: createTrees(4),
+        # 3 passes refining the octants whose centre lies within 0.3 of the
+        # cube centre (max level 7) + balance(1), order 2 GLL, one coarsened
+        # level and its P (about 237k octants)
+        "c1": dict(conn=W.brick(1, 1, 1), order=2, L0=4, passes=3, max_level=7,
+                   indicator="sphere", coarse_levels=1),
+    }
+
+
+def product_arrays(r):
+    """Every product of a pipeline result by name, integers as int64 and
+    weights as float64 (so GPU and CPU results hash alike)."""
+    s = r["sizes"]
+    out = {"octants": r["oct"], "conn": r["conn"], "node_numbers": r["nn"],
+           "dep_ptr": r["dep"][0], "dep_conn": r["dep"][1], "dep_w": r["dep"][2],
+           "sizes": [s[k] for k in ("num_local", "num_owned", "num_dep", "ext_pre",
+                                    "num_elements", "dep_nnz")]}
+    for k, lv in enumerate(r["levels"]):
+        out["L%d_octants" % k] = lv["oct"]
+        out["L%d_conn" % k] = lv["conn"]
+        out["L%d_P_rowptr" % k], out["L%d_P_cols" % k], out["L%d_P_vals" % k] = lv["P"]
+    norm = {}
+    for k, a in out.items():
+        a = np.asarray(a)
+        if hasattr(a, "dtype") and a.dtype.names:  # structured octants
+            a = np.stack([a[n] for n in a.dtype.names], 1)
+        a = np.ascontiguousarray(a, np.float64 if a.dtype.kind == "f" else np.int64)
+        norm[k] = a
+    return norm
+
+
+DIGEST_SAMPLES = 4096
+
+
+def _sample_index(n):
+    return np.unique(np.linspace(0, max(n - 1, 0), min(n, DIGEST_SAMPLES)).astype(np.int64))
+
+
+def digest(r):
+    """The fixture of a configuration-size case: per integer product its
+    shape, the SHA-256 of its bytes and an evenly spaced sample of its
+    entries (to locate a difference); weights are stored whole (they take
+    few distinct values and compress to a few KB)."""
+    import hashlib
+    d = {}
+    for k, a in product_arrays(r).items():
+        d[k + "__shape"] = np.array(a.shape, np.int64)
+        if a.dtype.kind == "f":
+            d[k + "__full"] = a
+            continue
+        d[k + "__sha"] = np.array(hashlib.sha256(a.tobytes()).hexdigest())
+        flat = a.reshape(a.shape[0], -1) if a.ndim > 1 else a
+        d[k + "__sample"] = flat[_sample_index(flat.shape[0])]
+    return d
+
+
+def compare_digest(r, z):
+    """Mismatches between a pipeline result and a digest fixture (empty when
+    they agree): integer products bit for bit (by hash), weights entry by
+    entry within RTOL."""
+    import hashlib
+    bad = []
+    arrs = product_arrays(r)
+    names = sorted({k.split("__")[0] for k in z.files if "__" in k})
+    if sorted(arrs) != names:
+        bad.append("products %s vs fixture %s" % (sorted(arrs), names))
+    for k in names:
+        if k not in arrs:
+            continue
+        a = arrs[k]
+        if tuple(a.shape) != tuple(z[k + "__shape"]):
+            bad.append("%s: shape %s vs %s" % (k, a.shape, tuple(z[k + "__shape"])))
+        elif a.dtype.kind == "f":
+            ref = z[k + "__full"]
+            if a.size and not np.allclose(a, ref, rtol=RTOL,
+                                          atol=RTOL * max(1.0, np.abs(ref).max())):
+                bad.append("%s: max abs diff %g" % (k, np.abs(a - ref).max()))
+        elif hashlib.sha256(a.tobytes()).hexdigest() != str(z[k + "__sha"]):
+            flat = a.reshape(a.shape[0], -1) if a.ndim > 1 else a
+            smp, ref = flat[_sample_index(flat.shape[0])], z[k + "__sample"]
+            diff = np.argwhere(smp != ref)
+            bad.append("%s: hash differs%s" % (k, "" if not len(diff) else
+                                                " (sample entry %s: %s vs %s)" % (
+                                                    tuple(diff[0]), smp[tuple(diff[0])],
+                                                    ref[tuple(diff[0])])))
+    return bad
 
 
 def load_golden(name):
@@ -200,6 +308,27 @@ def cases():
                        max_level=5, prob=0.4, seed=21, coarse_levels=1, coarse_steps=3),
         "gap_o3": dict(conn=W.brick(2, 1, 1), order=3, L0=1, passes=3, max_level=5,
                        prob=0.4, seed=22, coarse_levels=2, coarse_steps=2),
+        # the hierarchy createTopoProblem builds from an order-3 forest:
+        # 3 -> 2 on the same octants, then geometric coarsening at order 2
+        "pcoarse_o3": dict(conn=W.rotate_blocks(W.brick(3, 2, 2), 11), order=3, L0=1,
+                           passes=3, max_level=5, prob=0.3, seed=17, hier=["p", "h", "h"]),
+        # order 4: 4 -> 3 -> 2 on the same octants, then one geometric step
+        "pcoarse_o4": dict(conn=W.brick(2, 2, 1), order=4, L0=1, passes=2, max_level=4,
+                           prob=0.3, seed=18, hier=["p", "p", "h"]),
+        # geometric coarsening at order 4 (coarse elements of order 4)
+        "coarse_o4": dict(conn=W.rotate_blocks(W.brick(2, 1, 1), 13), order=4, L0=1,
+                          passes=2, max_level=3, prob=0.3, seed=19, coarse_levels=2),
+        # Bernstein elements (interp 2): dependent rows from the subdivision
+        # weights, P from the Bernstein basis (same order) or the degree
+        # elevation table (order one lower)
+        "bern_o3": dict(conn=W.rotate_blocks(W.brick(2, 2, 1), 14), order=3, L0=1, passes=3,
+                        max_level=4, prob=0.3, seed=23, interp=2, coarse_levels=2),
+        "bern_p3": dict(conn=W.brick(3, 2, 1), order=3, L0=1, passes=3, max_level=5,
+                        prob=0.3, seed=24, interp=2, hier=["p", "h"]),
+        "bern_o4": dict(conn=W.rotate_blocks(W.brick(2, 1, 1), 15), order=4, L0=1, passes=2,
+                        max_level=4, prob=0.3, seed=25, interp=2, hier=["h", "p", "h"]),
+        "bern_o5": dict(conn=W.brick(1, 1, 1), order=5, L0=1, passes=2, max_level=3,
+                        prob=0.3, seed=26, interp=2, hier=["p", "h"]),
         # refinement arrays with -1 entries: coarsening inside refine
         "mixed_o2": dict(conn=W.rotate_blocks(W.brick(3, 2, 2), 8), order=2, L0=2, passes=3,
                          max_level=4, indicator="mixed", prob=0.35, coarsen_prob=0.3, seed=12,

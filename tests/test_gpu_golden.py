@@ -19,3 +19,16 @@ def test_gpu_matches_reference_golden(gpu_lib, name):
     ref = pipeline.load_golden(name)
     bad = pipeline.compare(g, ref)
     assert not bad, "\n".join(bad)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(pipeline.digest_cases()))
+def test_gpu_matches_reference_digest(gpu_lib, name):
+    # the configuration-size case (C1 exactly as specified, ~237k octants)
+    # against the digest of the reference's own products
+    import numpy as np
+    case = pipeline.golden_case("digest_" + name)
+    g = pipeline.run_gpu(case)
+    z = np.load(os.path.join(pipeline.GOLDEN_DIR, "digest_%s.npz" % name))
+    bad = pipeline.compare_digest(g, z)
+    assert not bad, "\n".join(bad)

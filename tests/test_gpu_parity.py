@@ -76,3 +76,30 @@ def test_interp_applies_match_oracle(gpu_lib):
         a = np.dot(y_ref, xf)
         b = np.dot(x, yt_ref)
         assert abs(a - b) <= 1e-10 * max(1.0, abs(a))
+
+
+@pytest.mark.gpu
+def test_bench_sample_matches_oracle(gpu_lib):
+    # the multi-tree order-3 bench workload's CPU sample (its first 2 of 5
+    # refinement passes, 4-level hierarchy, ~140k octants), the case the
+    # CPU baseline times: GPU and oracle agree bit for bit on octants,
+    # conn, node numbers and the dependent CSR, P within 1e-13
+    import bench
+    case = bench.cpu_sample_case()
+    g = pipeline.run_gpu(case)
+    o = pipeline.run_cpu(case, "oracle")
+    assert len(g["oct"]) > 50000
+    bad = pipeline.compare(g, o)
+    assert not bad, "\n".join(bad)
+
+
+@pytest.mark.gpu
+def test_device_refinement_draws_match_host(gpu_lib):
+    # the bench's resident arm draws its refinement flags on the device, the
+    # host-buffer arm and every CPU checker on the host: the same bits
+    from tmr_gb300 import TMR
+    from tmr_gb300 import workloads as W
+    for n, seed, stream, prob in [(1, 7, 0, 0.3), (1000003, 7, 4, 0.3), (65536, 3, 1, 0.5),
+                                  (12345, 21, 2, 0.0), (777, 9, 3, 1.0)]:
+        d = TMR.random_refinement(n, seed, stream, prob).cpu().numpy()
+        np.testing.assert_array_equal(d, W.random_indicator(n, seed, stream, prob))

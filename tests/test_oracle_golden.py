@@ -30,6 +30,34 @@ def test_golden_cases_are_the_parity_cases():
         for k, v in allc[name].items():
             if k != "conn":
                 assert c[k] == v, (name, k)
+    for name, case in pipeline.digest_cases().items():
+        c = pipeline.golden_case("digest_" + name)
+        np.testing.assert_array_equal(c["conn"], case["conn"])
+        assert {k: v for k, v in c.items() if k != "conn"} == \
+            {k: v for k, v in case.items() if k != "conn"}
+
+
+@pytest.mark.parametrize("name", sorted(pipeline.digest_cases()))
+def test_oracle_matches_reference_digest(name):
+    # the configuration-size case (C1 as specified) against the digest of
+    # the reference's own products
+    case = pipeline.golden_case("digest_" + name)
+    o = pipeline.run_cpu(case, "oracle")
+    z = np.load(os.path.join(pipeline.GOLDEN_DIR, "digest_%s.npz" % name))
+    bad = pipeline.compare_digest(o, z)
+    assert not bad, "\n".join(bad)
+
+
+def test_digest_check_catches_planted_mistakes():
+    # a wrong weight (1e-9 off) and a wrong connectivity entry planted in the
+    # oracle's products are both reported
+    case = pipeline.golden_case("digest_c1")
+    o = pipeline.run_cpu(case, "oracle")
+    z = np.load(os.path.join(pipeline.GOLDEN_DIR, "digest_c1.npz"))
+    o["levels"][0]["P"][2][1234] += 1e-9
+    o["conn"][77, 3] += 1
+    bad = pipeline.compare_digest(o, z)
+    assert any("L0_P_vals" in b for b in bad) and any(b.startswith("conn") for b in bad)
 
 
 def test_golden_properties():

@@ -7,7 +7,9 @@ entry point: its work vectors live in a static device array of the library.
 This checks, through the C ABI, that it returns what the allocating
 tmrg_filter_apply_device returns (tolerance 1e-13 relative, the FP64
 tolerance of the other filter tests) on two calls in a row, forward and
-transpose, and that it rejects a problem larger than its fixed scratch.
+transpose, that those calls allocate no device memory (the library's
+allocation counter stays put), and that it rejects a problem larger than
+its fixed scratch.
 The file is named to be collected last."""
 import ctypes
 
@@ -38,11 +40,15 @@ def test_static_scratch_filter_apply_matches_allocating_apply(gpu_lib):
                                 ctypes.c_void_p(ref.data_ptr())) == 0
         for _ in range(2):  # two calls in a row share the static scratch
             out = torch.full_like(x, float("nan"))
+            torch.cuda.synchronize()
+            allocs = L.tmrg_device_alloc_count()
             rc = L.tmrg_filter_apply_static_device(F.ptr, transpose, vpn,
                                                    ctypes.c_void_p(x.data_ptr()),
                                                    ctypes.c_void_p(out.data_ptr()))
             assert rc == 0, L.tmrg_last_error()
             torch.cuda.synchronize()
+            # the property the entry point exists for: no device allocation
+            assert L.tmrg_device_alloc_count() == allocs
             np.testing.assert_allclose(out.cpu().numpy(), ref.cpu().numpy(),
                                        rtol=1e-13, atol=0.0)
     # nodes x vpn beyond the fixed scratch: rejected before any launch

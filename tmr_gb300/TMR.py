@@ -58,6 +58,43 @@ def _is_torch(a):
     return type(a).__module__.startswith("torch")
 
 
+def _check_vectors(what, x, y, nin, nout, dtypes):
+    """Validate an (x -> y) vector pair before its pointers reach the C ABI
+    and return the number of vectors per node.
+
+    x must hold nin * nvec values and y nout * nvec (nvec >= 1), both of one
+    dtype from `dtypes` (numpy dtype names), both contiguous, and both on
+    the same side: CUDA tensors for the device entry points, host arrays
+    otherwise.  A wrong size would make a kernel read or write past the end
+    of a buffer, so every mismatch raises ValueError instead."""
+    if nin <= 0 or nout <= 0:
+        raise ValueError("%s: empty operator (%d inputs, %d outputs)" % (what, nin, nout))
+    tx, ty = _is_torch(x), _is_torch(y)
+    if tx or ty:
+        if not (tx and ty and x.is_cuda and y.is_cuda):
+            raise ValueError("%s: x and y must both be CUDA tensors (or both host arrays)"
+                             % what)
+        if x.device != y.device:
+            raise ValueError("%s: x on %s, y on %s" % (what, x.device, y.device))
+        if x.dtype != y.dtype:
+            raise ValueError("%s: x is %s, y is %s" % (what, x.dtype, y.dtype))
+        name = str(x.dtype).replace("torch.", "")
+        if name not in dtypes:
+            raise ValueError("%s: dtype %s not supported (%s)" % (what, name, "/".join(dtypes)))
+        if not (x.is_contiguous() and y.is_contiguous()):
+            raise ValueError("%s: x and y must be contiguous" % what)
+        nx, ny = x.numel(), y.numel()
+    else:
+        nx, ny = np.size(x), np.size(y)
+    if nx == 0 or nx % nin != 0:
+        raise ValueError("%s: x holds %d values, not a multiple of %d" % (what, nx, nin))
+    nvec = nx // nin
+    if ny != nout * nvec:
+        raise ValueError("%s: y holds %d values, expected %d (%d x %d)"
+                         % (what, ny, nout * nvec, nout, nvec))
+    return nvec
+
+
 class _DeviceArray:
     """Exposes a borrowed device pointer through __cuda_array_interface__."""
 
@@ -735,14 +772,13 @@ class VecInterp:
         names = ("tmrg_interp_mult", "tmrg_interp_mult_transpose",
                  "tmrg_interp_mult_weight_transpose")
         rows, cols, _ = self.sizes()
-        nin = cols if which == 0 else rows
+        nin, nout = (cols, rows) if which == 0 else (rows, cols)
+        nvec = _check_vectors(names[which], x, y, nin, nout, ("float64",))
         if _is_torch(x):
-            nvec = x.numel() // max(nin, 1)
             call(names[which] + "_device", self.ptr, _vp(x.data_ptr()),
                  _vp(y.data_ptr()), nvec)
         else:
             x = np.ascontiguousarray(x, dtype=np.float64)
-            nvec = x.size // max(nin, 1)
             direct = (isinstance(y, np.ndarray) and y.dtype == np.float64
                       and y.flags.c_contiguous)
             out = y if direct else np.zeros(y.shape, np.float64)
@@ -813,6 +849,12 @@ class MatrixFilter:
 
     def _apply(self, transpose, x, y, vpn=None):
         vpn = vpn or self.vpn
+        n = self.size()[0]
+        what = "MatrixFilter.applyTranspose" if transpose else "MatrixFilter.applyFilter"
+        dts = ("float64", "float32") if _is_torch(x) else ("float64",)
+        if _check_vectors(what, x, y, n, n, dts) != vpn:
+            raise ValueError("%s: x holds %d values, expected %d nodes x vpn %d"
+                             % (what, np.size(x) if not _is_torch(x) else x.numel(), n, vpn))
         if _is_torch(x):
             import torch
             if x.dtype == torch.float32:
@@ -994,6 +1036,11 @@ class HelmholtzFilter(ConformFilter):
 
     def _apply(self, transpose, x, y, vpn=None):
         vpn = vpn or self.vpn
+        n = int(self.sizes()[0][0])
+        what = "HelmholtzFilter.applyTranspose" if transpose else "HelmholtzFilter.applyFilter"
+        if _check_vectors(what, x, y, n, n, ("float64",)) != vpn:
+            raise ValueError("%s: vectors hold %d nodes x %d values, vpn is %d"
+                             % (what, n, (x.numel() if _is_torch(x) else np.size(x)) // n, vpn))
         if _is_torch(x):
             name = ("tmrg_helmholtz_apply_transpose_device" if transpose
                     else "tmrg_helmholtz_apply_device")
@@ -1017,6 +1064,15 @@ class HelmholtzFilter(ConformFilter):
     def mult(self, level, which, x, y, nvec=1):
         """y = K x (which = 0) or M x (which = 1) on filter level `level`
         (torch CUDA tensors)."""
+        sz = self.sizes()
+        if not 0 <= level < len(sz):
+            raise ValueError("HelmholtzFilter.mult: level %d of %d" % (level, len(sz)))
+        n = int(sz[level][0])
+        if not (_is_torch(x) and _is_torch(y)):
+            raise ValueError("HelmholtzFilter.mult: x and y must be CUDA tensors")
+        if _check_vectors("HelmholtzFilter.mult", x, y, n, n, ("float64",)) != nvec:
+            raise ValueError("HelmholtzFilter.mult: vectors hold %d values, expected %d x %d"
+                             % (x.numel(), n, nvec))
         call("tmrg_helmholtz_mult_device", self.ptr, int(level), int(which), int(nvec),
              _vp(x.data_ptr()), _vp(y.data_ptr()))
         return y

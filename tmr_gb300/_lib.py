@@ -22,6 +22,7 @@ _SIGS = {
     "tmrg_version": [],
     "tmrg_kernel_launch_count": [],
     "tmrg_host_sync_count": [],
+    "tmrg_device_alloc_count": [],
     "tmrg_profile_begin": [],
     "tmrg_profile_end": [c_vp, c_i64],
     "tmrg_measure_fp64_peak": [P(c_dbl)],
@@ -139,6 +140,7 @@ _RESTYPE = {
     "tmrg_version": ctypes.c_char_p,
     "tmrg_kernel_launch_count": c_i64,
     "tmrg_host_sync_count": c_i64,
+    "tmrg_device_alloc_count": c_i64,
 }
 
 STATUS = {

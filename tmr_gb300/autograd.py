@@ -14,13 +14,19 @@ from .TMR import MatrixFilter, VecInterp
 class FilterInterp(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, filt: MatrixFilter, interp: VecInterp, vpn: int = 1):
+        if x.dtype != torch.float64:
+            raise TypeError("FilterInterp: the interpolation apply is FP64")
         x = x.contiguous()
         rows, cols, _ = interp.sizes()
+        n = filt.size()[0]
+        if n != cols:
+            raise ValueError("FilterInterp: filter has %d nodes, P has %d columns" % (n, cols))
+        if x.numel() != n * vpn:
+            raise ValueError("FilterInterp: x holds %d values, expected %d nodes x vpn %d"
+                             % (x.numel(), n, vpn))
         rho_f = torch.empty_like(x)
         filt.applyFilter(x, rho_f, vpn)
         y = torch.empty(rows * vpn, dtype=x.dtype, device=x.device)
-        if x.dtype != torch.float64:
-            raise TypeError("FilterInterp: the interpolation apply is FP64")
         interp.mult(rho_f, y)
         ctx.filt, ctx.interp, ctx.vpn = filt, interp, vpn
         ctx.ncols = cols

@@ -270,6 +270,7 @@ const char *tmrg_last_error(void) { return g_last_error.c_str(); }
 const char *tmrg_version(void) { return "tmr_gb300 0.1 (sm_103a)"; }
 int64_t tmrg_kernel_launch_count(void) { return g_kernel_launches.load(); }
 int64_t tmrg_host_sync_count(void) { return g_host_syncs.load(); }
+int64_t tmrg_device_alloc_count(void) { return g_device_allocs.load(); }
 
 // FP64 FMA throughput of the current device: 8 independent FMA chains per
 // thread over a grid of 8 blocks per SM; the denominator of the roofline of

@@ -340,6 +340,7 @@ static void horner(Filter &F, bool tr, int vpn, const T *in, T *out, const T *Ai
   prof_bytes(2LL * sizeof(T) * len + (long long)sizeof(T) * n);
   launch(k_fe_scale<T>, blocks_for(len, 256), 256, 0, s, n, vpn, pre, in, t1.p);
   if (F.N == 0) {
+    prof_bytes(2LL * sizeof(T) * len + (long long)sizeof(T) * n);
     launch(k_fe_scale<T>, blocks_for(len, 256), 256, 0, s, n, vpn, post,
            (const T *)t1.p, out);
     return;
@@ -411,14 +412,17 @@ void filter_apply_static(Filter &F, bool tr, int vpn, const double *in, double *
                 "allocation-free filter apply: " + std::to_string(len) +
                     " values (nodes x vpn) exceed the static scratch limit of " +
                     std::to_string(FILTER_STATIC_MAX));
+  Stage st(tr ? "tmrg_filter_apply_static_transpose" : "tmrg_filter_apply_static");
   double *t1 = filter_static_scratch();
   double *tmp = t1 + FILTER_STATIC_MAX;
   if (n == 0) return;
   cudaStream_t s = F.s;
   const double *pre = tr ? F.Tinv.p : F.Ainv.p;
   const double *post = tr ? F.Ainv.p : F.Tinv.p;
+  prof_bytes(2LL * sizeof(double) * len + (long long)sizeof(double) * n);
   launch(k_fe_scale<double>, blocks_for(len, 256), 256, 0, s, n, vpn, pre, in, t1);
   if (F.N == 0) {
+    prof_bytes(2LL * sizeof(double) * len + (long long)sizeof(double) * n);
     launch(k_fe_scale<double>, blocks_for(len, 256), 256, 0, s, n, vpn, post,
            (const double *)t1, out);
     return;

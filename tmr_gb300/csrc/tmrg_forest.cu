@@ -11,6 +11,7 @@ namespace tmrg {
 
 std::atomic<long long> g_kernel_launches{0};
 std::atomic<long long> g_host_syncs{0};
+std::atomic<long long> g_device_allocs{0};
 std::atomic<bool> g_profile_on{false};
 thread_local long long g_prof_bytes = 0;
 thread_local long long g_prof_flops = 0;

@@ -1049,6 +1049,349 @@ void forest_find_enclosing(Forest &f, int order, const double *knots,
   TMRG_CUDA(cudaStreamSynchronize(s));
 }
 
+void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long long *keepoff);
+
+// ---------------------------------------------------------------------
+// The general createInterpolation path: any fine and coarse order up to
+// TMRG_MAX_ORDER, Lagrange (uniform or Gauss-Lobatto knots) or Bernstein
+// elements.  The specialised kernels above cover coarse orders 2-3 with
+// Lagrange bases, the multigrid hierarchies that dominate the runtime;
+// this path serves the rest (coarse order 4+, the Bernstein element
+// hierarchies of the reference's topology-optimisation drivers).
+//
+// One warp per row, in two passes with the same row construction (count,
+// then write at the scanned offsets).  A row is built as computeElemInterp
+// builds it (TMROctForest.cpp:6396-6594): the three directions' 1-D weights
+// of the enclosing coarse element, the tensor-product entries in (kk, jj,
+// ii) order with each dependent coarse node expanded through its CSR row,
+// then uniqueSort (TMRBase.h:110-133): a stable sort by column and the
+// in-order sum of equal columns.
+struct GenInterp {
+  int bern;  // Bernstein elements
+  // eval_bernstein_interp_weights rows (fine order = coarse order + 1):
+  // bel[u] are the coarse weights of fine control point u
+  double bel[TMRG_MAX_ORDER][TMRG_MAX_ORDER];
+  int cnpe;
+  const int *conn, *dptr, *dconn;  // coarse element connectivity, dependent CSR
+  const double *dw;
+  int cap;  // staged entries per warp
+};
+
+// The direction's index range of computeElemInterp: [s, e) with the face
+// hits that keep a single coarse index.
+__device__ __forceinline__ void gen_range(int i, int mo, int co, int32_t nx, int32_t h,
+                                          int32_t ox, int32_t hc, int &s, int &e) {
+  if ((i == 0 && ox == nx) || (i == mo - 1 && ox == nx + h)) {
+    s = 0;
+    e = 1;
+  } else if ((i == 0 && ox + hc == nx) || (i == mo - 1 && ox + hc == nx + h)) {
+    s = co - 1;
+    e = co;
+  } else {
+    s = 0;
+    e = co;
+  }
+}
+
+// The direction's 1-D weights (N[s] = 1 at a face hit).  Lagrange:
+// lagrange_shape_functions (TMRInterpolation.h:40-52) at the coarse knots;
+// Bernstein: bernstein_shape_functions (:164-177) when the orders agree,
+// else the degree-elevation row of the fine index.  u as the reference
+// rounds it: 0.5 h and 2 / hc are powers of two, so those scalings are
+// exact.
+__device__ void gen_weights(const InterpCtx &I, const GenInterp &G, int i, int s, int e,
+                            int32_t nx, int32_t h, int32_t ox, int32_t hc, double *N) {
+  const int co = I.co;
+  if (e - s == 1) {
+    N[s] = 1.0;
+    return;
+  }
+  if (G.bern && I.fo != co) {
+    for (int a = 0; a < co; a++) N[a] = G.bel[i][a];
+    return;
+  }
+  const double t = __dadd_rn(exact_double(nx), __dmul_rn(0.5 * (double)h, I.fk1[i]));
+  const double u = __dadd_rn(-1.0, __dmul_rn(__dsub_rn(t, exact_double(ox)),
+                                             2.0 / (double)hc));
+  if (G.bern) {
+    const double u1 = __dmul_rn(0.5, __dsub_rn(1.0, u));
+    const double u2 = __dmul_rn(0.5, __dadd_rn(u, 1.0));
+    N[0] = 1.0;
+    for (int j = 1; j < co; j++) {
+      double sum = 0.0;
+      for (int k = 0; k < j; k++) {
+        const double tk = N[k];
+        N[k] = __dadd_rn(sum, __dmul_rn(u1, tk));
+        sum = __dmul_rn(u2, tk);
+      }
+      N[j] = sum;
+    }
+    return;
+  }
+  for (int a = 0; a < co; a++) {
+    double v = 1.0;
+    for (int b = 0; b < co; b++)
+      if (a != b) v = __dmul_rn(v, __dmul_rn(__dsub_rn(u, I.ck[b]), I.crk[a][b]));
+    N[a] = v;
+  }
+}
+
+// findEnclosing for every row (one thread per row).
+__global__ void k_gen_find(long long rows, InterpCtx I, int *trow) {
+  const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= rows) return;
+  const unsigned long long rr = I.rep[row];
+  const long long e = (long long)(rr >> 8);
+  const Oct node{I.fb[e], I.fx[e], I.fy[e], I.fz[e], I.fl[e]};
+  const long long t = find_enclosing(I, node, (int)(rr & 255u));
+  if (t < 0) atomicExch(I.err, 1);
+  trow[row] = (int)t;
+}
+
+// Element expansion length bound: the largest sum of dependent row lengths
+// over one coarse element's nodes.
+__global__ void k_gen_emax(long long n, int cnpe, const int *__restrict__ conn,
+                           const int *__restrict__ dptr, int *emax) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int *c = conn + t * cnpe;
+  int e = 0;
+  for (int l = 0; l < cnpe; l++) {
+    const int cv = __ldg(c + l);
+    e += (cv >= 0) ? 1 : (__ldg(dptr - cv) - __ldg(dptr - cv - 1));
+  }
+  atomicMax(emax, e);
+}
+
+// WRITE = false: cnt[row] = merged entries of the row.  WRITE = true: the
+// row's entries at off[row] (and nzcount += its apply_keeps entries).
+// Dynamic shared memory: per warp, 2 * cap (column, weight) slots.
+constexpr int GEN_WARPS = 4;
+template <bool WRITE>
+__global__ void __launch_bounds__(GEN_WARPS * 32)
+    k_gen_rows(long long rows, InterpCtx I, GenInterp G, const int *__restrict__ trow,
+               long long *cnt_off, int *cols, double *vals, unsigned long long *nzcount) {
+  extern __shared__ unsigned char gen_smem[];
+  __shared__ double s_N[GEN_WARPS][3][TMRG_MAX_ORDER];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long row = (long long)blockIdx.x * GEN_WARPS + warp;
+  if (row >= rows) return;
+  const int cap = G.cap;
+  int *c0 = (int *)gen_smem + (size_t)warp * 2 * cap;
+  int *c1 = c0 + cap;
+  double *w0 = (double *)((int *)gen_smem + (size_t)GEN_WARPS * 2 * cap) + (size_t)warp * 2 * cap;
+  double *w1 = w0 + cap;
+  const int t = trow[row];
+  if (t < 0) {
+    if (!WRITE && lane == 0) cnt_off[row] = 0;
+    return;
+  }
+  const int mo = I.fo, co = I.co;
+  const unsigned long long rr = I.rep[row];
+  const long long e = (long long)(rr >> 8);
+  const int info = (int)(rr & 255u);
+  const int32_t nx[3] = {I.fx[e], I.fy[e], I.fz[e]};
+  const int32_t h = side_of(I.fl[e]);
+  const int4 cq = __ldg(I.c4 + t);
+  const int32_t hc = side_of(cq.x >> 26);
+  const int32_t ox[3] = {cq.y, cq.z, cq.w};
+  const int idx[3] = {info % mo, (info % (mo * mo)) / mo, info / (mo * mo)};
+  int rs[3], re[3];
+  for (int d = 0; d < 3; d++) gen_range(idx[d], mo, co, nx[d], h, ox[d], hc, rs[d], re[d]);
+  if (lane < 3)
+    gen_weights(I, G, idx[lane], rs[lane], re[lane], nx[lane], h, ox[lane], hc,
+                s_N[warp][lane]);
+  __syncwarp();
+  // entries in computeElemInterp's loop order
+  const int ni = re[0] - rs[0], nj = re[1] - rs[1], nk = re[2] - rs[2];
+  const int npos = ni * nj * nk;
+  const int *cc = G.conn + (long long)t * G.cnpe;
+  int total = 0;
+  for (int q0 = 0; q0 < npos; q0 += 32) {
+    const int q = q0 + lane;
+    int cv = 0, len = 0, d0 = 0;
+    double w = 0.0;
+    if (q < npos) {
+      const int ii = rs[0] + q % ni, jj = rs[1] + (q / ni) % nj, kk = rs[2] + q / (ni * nj);
+      w = __dmul_rn(__dmul_rn(s_N[warp][0][ii], s_N[warp][1][jj]), s_N[warp][2][kk]);
+      cv = __ldg(cc + ii + jj * co + kk * co * co);
+      if (cv >= 0) {
+        len = 1;
+      } else {
+        d0 = __ldg(G.dptr - cv - 1);
+        len = __ldg(G.dptr - cv) - d0;
+      }
+    }
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int off = total + incl - len;
+    if (off + len <= cap) {
+      if (cv >= 0 && len) {
+        c0[off] = cv;
+        w0[off] = w;
+      } else {
+        for (int p = 0; p < len; p++) {
+          c0[off + p] = __ldg(G.dconn + d0 + p);
+          w0[off + p] = __dmul_rn(w, __ldg(G.dw + d0 + p));
+        }
+      }
+    }
+    total += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  if (total > cap) {
+    if (lane == 0) atomicExch(I.err, 5);
+    if (!WRITE && lane == 0) cnt_off[row] = 0;
+    return;
+  }
+  __syncwarp();
+  // stable rank sort by column
+  for (int a = lane; a < total; a += 32) {
+    const int col = c0[a];
+    int rk = 0;
+    for (int b = 0; b < total; b++) {
+      const int cb = c0[b];
+      rk += (cb < col) || (cb == col && b < a);
+    }
+    c1[rk] = col;
+    w1[rk] = w0[a];
+  }
+  __syncwarp();
+  // run heads, their rank among heads, and the in-order run sums
+  const long long base = WRITE ? cnt_off[row] : 0;
+  int heads = 0, kept = 0;
+  for (int a0 = 0; a0 < total; a0 += 32) {
+    const int a = a0 + lane;
+    const bool head = a < total && (a == 0 || c1[a] != c1[a - 1]);
+    const unsigned hb = __ballot_sync(0xffffffffu, head);
+    if (WRITE && head) {
+      double v = w1[a];
+      for (int b = a + 1; b < total && c1[b] == c1[a]; b++) v = __dadd_rn(v, w1[b]);
+      const long long o = base + heads + __popc(hb & ((1u << lane) - 1u));
+      cols[o] = c1[a];
+      vals[o] = v;
+      kept += apply_keeps(v);
+    }
+    heads += __popc(hb);
+  }
+  if (WRITE) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) kept += __shfl_xor_sync(0xffffffffu, kept, o);
+    if (lane == 0 && kept) atomicAdd(nzcount, (unsigned long long)kept);
+  } else if (lane == 0) {
+    cnt_off[row] = heads;
+  }
+}
+
+// eval_bernstein_interp_weights (TMRInterpolation.h:441-560) as the
+// reference tabulates it, for fine order = coarse order + 1, coarse orders
+// 2-5.  The coarse-order-4 rows for u = 2 and u = 3 are reproduced as the
+// reference writes them (they are the natural degree-elevation rows of
+// u = 3 and u = 2).
+static void bernstein_elevation(int mo, int co, double (*N)[TMRG_MAX_ORDER]) {
+  for (int u = 0; u < TMRG_MAX_ORDER; u++)
+    for (int i = 0; i < TMRG_MAX_ORDER; i++) N[u][i] = 0.0;
+  for (int u = 0; u < mo; u++) {
+    double *r = N[u];
+    if (u == 0) {
+      r[0] = 1.0;
+    } else if (u == mo - 1) {
+      r[co - 1] = 1.0;
+    } else if (co == 2) {
+      r[0] = 0.5;
+      r[1] = 0.5;
+    } else if (co == 3) {
+      r[u - 1] = (u == 1) ? 1. / 3 : 2. / 3;
+      r[u] = (u == 1) ? 2. / 3 : 1. / 3;
+    } else if (co == 4) {
+      if (u == 1) {
+        r[0] = 0.25;
+        r[1] = 0.75;
+      } else if (u == 2) {
+        r[2] = 0.75;
+        r[3] = 0.25;
+      } else {
+        r[1] = 0.5;
+        r[2] = 0.5;
+      }
+    } else {
+      const double a[4][2] = {{0.2, 0.8}, {0.4, 0.6}, {0.6, 0.4}, {0.8, 0.2}};
+      r[u - 1] = a[u - 1][0];
+      r[u] = a[u - 1][1];
+    }
+  }
+}
+
+// Rows of P by the general path (interp_create fills ctx `c` first).
+static void interp_rows_general(Forest &fine, Forest &coarse, Interp &I, InterpCtx &c,
+                                DBuf<int> &err, cudaStream_t s) {
+  const long long rows = I.rows;
+  GenInterp G{};
+  G.bern = fine.interp == TMRG_BERNSTEIN_POINTS;
+  if (G.bern) {
+    if (fine.order != coarse.order &&
+        (fine.order - coarse.order != 1 || coarse.order > 5))
+      throw Error(TMRG_ERR_UNSUPPORTED,
+                  "createInterpolation: Bernstein meshes must have equal orders or a "
+                  "fine order one above a coarse order of 2-5");
+    if (fine.order != coarse.order) bernstein_elevation(fine.order, coarse.order, G.bel);
+  }
+  G.cnpe = coarse.order * coarse.order * coarse.order;
+  G.conn = coarse.econn.p;
+  G.dptr = coarse.dep_ptr.p;
+  G.dconn = coarse.dep_conn.p;
+  G.dw = coarse.dep_w.p;
+  DBuf<int> emax(1, s);
+  emax.zero();
+  launch(k_gen_emax, blocks_for(coarse.n, 256), 256, 0, s, coarse.n, G.cnpe,
+         (const int *)coarse.econn.p, (const int *)coarse.dep_ptr.p, emax.p);
+  const int em = read_scalar(emax.p, s);
+  G.cap = std::max(32, (em + 31) / 32 * 32);
+  const size_t smem = (size_t)GEN_WARPS * 2 * G.cap * (sizeof(int) + sizeof(double));
+  if (smem > 200 * 1024)
+    throw Error(TMRG_ERR_UNSUPPORTED,
+                "createInterpolation: a coarse element expands to " + std::to_string(em) +
+                    " entries, beyond the general path's shared-memory stage");
+  TMRG_CUDA(cudaFuncSetAttribute(k_gen_rows<false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  TMRG_CUDA(cudaFuncSetAttribute(k_gen_rows<true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  DBuf<int> trow(rows + 1, s);
+  DBuf<long long> roff(rows + 1, s);
+  launch(k_gen_find, blocks_for(rows, 128), 128, 0, s, rows, c, trow.p);
+  launch(k_gen_rows<false>, blocks_for(rows, GEN_WARPS), GEN_WARPS * 32, smem, s, rows, c, G,
+         (const int *)trow.p, roff.p, (int *)nullptr, (double *)nullptr,
+         (unsigned long long *)nullptr);
+  exclusive_scan<long long>(roff.p, roff.p, rows, s);
+  const long long nnz = read_scalar(roff.p + rows, s);
+  const int e = read_scalar(err.p, s);
+  if (e == 5)
+    throw Error(TMRG_ERR_INTERNAL, "createInterpolation: a row outgrew its element bound");
+  if (e)
+    throw Error(TMRG_ERR_INTERNAL,
+                "createInterpolation: a fine node has no enclosing coarse octant");
+  if (nnz >= (1LL << 31) - 1)
+    throw Error(TMRG_ERR_ARG, "createInterpolation: more than 2^31 entries");
+  I.nnz = nnz;
+  I.rowptr.alloc(rows + 1, s);
+  launch(k_ptr32, blocks_for(rows + 1, 256), 256, 0, s, rows, (const long long *)roff.p,
+         I.rowptr.p);
+  I.colidx.alloc(nnz + 1, s);
+  I.vals.alloc(nnz + 1, s);
+  DBuf<unsigned long long> nzcount(1, s);
+  nzcount.zero();
+  prof_bytes(12 * nnz + 20 * rows);
+  launch(k_gen_rows<true>, blocks_for(rows, GEN_WARPS), GEN_WARPS * 32, smem, s, rows, c, G,
+         (const int *)trow.p, roff.p, I.colidx.p, I.vals.p, nzcount.p);
+  const long long nonzeros = (long long)read_scalar(nzcount.p, s);
+  trow.release();
+  roff.release();
+  interp_finish(I, nonzeros, s, nullptr);
+}
+
 // Sorted expansion lists of every element of `coarse` (k_elist_*).
 struct ElemLists {
   DBuf<long long> eoff;
@@ -1072,8 +1415,6 @@ static void build_elists(Forest &coarse, ElemLists &L, int *err, cudaStream_t s)
          (const int *)coarse.dep_conn.p, (const double *)coarse.dep_w.p,
          (const long long *)L.eoff.p, L.lcol.p, L.ldw.p, L.lkey.p, L.ekind.p, err);
 }
-void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long long *keepoff);
-
 void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   Stage st("tmrg_create_interpolation");
   if (&fine == &coarse)
@@ -1081,9 +1422,8 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   if (fine.interp != coarse.interp)
     throw Error(TMRG_ERR_ARG,
                 "Interpolation types between meshes are not identical");
-  if (coarse.order > IMAX_CO)
-    throw Error(TMRG_ERR_UNSUPPORTED,
-                "createInterpolation: coarse order > 3 is not built");
+  // coarse orders above 3 and Bernstein elements take the general path
+  const bool general = coarse.order > IMAX_CO || fine.interp == TMRG_BERNSTEIN_POINTS;
   forest_create_nodes(fine);
   forest_create_nodes(coarse);
   TMRG_CUDA(cudaStreamSynchronize(coarse.s));
@@ -1123,6 +1463,17 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
          (const int *)coarse.y.p, (const int *)coarse.z.p,
          (const int16_t *)coarse.level.p, c4.p);
   c.c4 = c4.p;
+  c.rep = rep.p;
+  c.err = err.p;
+  for (int i = 0; i < TMRG_MAX_ORDER; i++)
+    for (int j = 0; j < TMRG_MAX_ORDER; j++)
+      c.crk[i][j] = (i != j && i < coarse.order && j < coarse.order)
+                        ? 1.0 / (coarse.knots[i] - coarse.knots[j])
+                        : 0.0;
+  if (general) {
+    interp_rows_general(fine, coarse, I, c, err, s);
+    return;
+  }
   // sorted expansion list of every coarse element
   ElemLists EL;
   build_elists(coarse, EL, err.p, s);
@@ -1131,13 +1482,6 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   c.ldw = EL.ldw.p;
   c.lkey = EL.lkey.p;
   c.ekind = EL.ekind.p;
-  c.rep = rep.p;
-  c.err = err.p;
-  for (int i = 0; i < TMRG_MAX_ORDER; i++)
-    for (int j = 0; j < TMRG_MAX_ORDER; j++)
-      c.crk[i][j] = (i != j && i < coarse.order && j < coarse.order)
-                        ? 1.0 / (coarse.knots[i] - coarse.knots[j])
-                        : 0.0;
   // direction states (dir_state): fine orders 2 and 3, 1 + each fine knot
   // within 2^-53 of 0, 1 or 2, at most one inexact, and the tie of an
   // inexact knot one level below rounding to -1/2 as on the device

@@ -22,7 +22,35 @@ namespace tmrg {
 struct Knots {
   double k[TMRG_MAX_ORDER];
   double r[TMRG_MAX_ORDER][TMRG_MAX_ORDER];
+  // Bernstein elements: bt[u + order - 1] are the coarse-edge weights of
+  // refined control point u (bernstein_subdivision)
+  int bern;
+  double bt[2 * TMRG_MAX_ORDER - 1][TMRG_MAX_ORDER];
 };
+
+// Dependent-node weights of Bernstein elements (eval_bernstein_weights,
+// TMRInterpolation.h:309-439, used by createDependentConn at
+// TMROctForest.cpp:5364-5373 and 5453-5473): refined control point
+// u in [-(order-1), order-1] of the two half-edges, by de Casteljau
+// subdivision at t = 1/2.  Left half (u = r - (order-1)): C(r, i) / 2^r of
+// coarse point i <= r; right half (u = r): C(order-1-r, i-r) / 2^(order-1-r)
+// of coarse point i >= r.  Short dyadic fractions, exact in double, so they
+// equal the reference's tabulated literals.  The reference tabulates orders
+// 2-5; other orders are rejected before this is used.
+static void bernstein_subdivision(int order, Knots &kn) {
+  kn.bern = 1;
+  const int p = order - 1;
+  for (int u = -p; u <= p; u++) {
+    double *N = kn.bt[u + p];
+    for (int i = 0; i < TMRG_MAX_ORDER; i++) N[i] = 0.0;
+    const int r = u <= 0 ? u + p : u, m = u <= 0 ? r : p - r, first = u <= 0 ? 0 : r;
+    double c = 1.0;
+    for (int i = 0; i <= m; i++) {
+      N[first + i] = c / (double)(1 << m);
+      c = c * (m - i) / (i + 1);
+    }
+  }
+}
 
 // Labels distinguish node objects at one position for order > 3
 // (initLabel, TMROctForest.cpp:6798-6811).
@@ -573,11 +601,25 @@ __global__ void k_dep_write(long long n, DepCtx d, Knots kn,
     int ei = sub, k = pos;
     parent_edge_nodes(d, p, ei, dconn + ptr);
     int sb = (ei < 4) ? x : (ei < 8) ? y : z;
+    if (kn.bern) {
+      const double *N = kn.bt[(o - 1) * (sb - 1) + k + o - 1];
+      for (int j = 0; j < o; j++) dw[ptr + j] = N[j];
+      return;
+    }
     double u = __dadd_rn(1.0 * (sb - 1), __dmul_rn(0.5, __dadd_rn(1.0, kn.k[k])));
     lagrange(o, u, kn, &dw[ptr]);
   } else {
     int fi = sub - 16, ii = pos % o, jj = pos / o;
     parent_face_nodes(d, p, fi, dconn + ptr);
+    if (kn.bern) {
+      // u = -(order-1) + ii plus (order-1) times the child offset of the
+      // face's first direction, v likewise (both integers)
+      const int a = (fi < 2) ? y : x, b = (fi < 4) ? z : y;
+      const double *Nu = kn.bt[ii + (o - 1) * a];
+      const double *Nv = kn.bt[jj + (o - 1) * b];
+      for (int j = 0; j < o * o; j++) dw[ptr + j] = __dmul_rn(Nu[j % o], Nv[j / o]);
+      return;
+    }
     double u = __dadd_rn(-1.0, __dmul_rn(0.5, __dadd_rn(1.0, kn.k[ii])));
     double v = __dadd_rn(-1.0, __dmul_rn(0.5, __dadd_rn(1.0, kn.k[jj])));
     if (fi < 2) {
@@ -699,9 +741,10 @@ void forest_create_nodes(Forest &f) {
     throw Error(TMRG_ERR_STATE,
                 "Cannot call createNodes(), no octants have been created");
   if (f.have_nodes) return;
-  if (f.interp == TMRG_BERNSTEIN_POINTS && f.order >= 3)
+  if (f.interp == TMRG_BERNSTEIN_POINTS && f.order > 5)
     throw Error(TMRG_ERR_UNSUPPORTED,
-                "createNodes: Bernstein interpolation is not built");
+                "createNodes: Bernstein dependent weights exist for orders 2-5 "
+                "(eval_bernstein_weights)");
   cudaStream_t s = f.s;
   const long long n = f.n;
   const int o = f.order, npe = o * o * o;
@@ -820,12 +863,13 @@ void forest_create_nodes(Forest &f) {
          (const int *)f.dep_ptr.p, writer.p);
   f.dep_conn.alloc(dnnz + 1, s);
   f.dep_w.alloc(dnnz + 1, s);
-  Knots kn;
+  Knots kn{};
   for (int i = 0; i < TMRG_MAX_ORDER; i++) {
     kn.k[i] = f.knots[i];
     for (int j = 0; j < TMRG_MAX_ORDER; j++)
       kn.r[i][j] = (i != j && i < o && j < o) ? 1.0 / (f.knots[i] - f.knots[j]) : 0.0;
   }
+  if (f.interp == TMRG_BERNSTEIN_POINTS) bernstein_subdivision(o, kn);
   DBuf<unsigned> epos(nd + 1, s);
   DBuf<int> order(nd + 1, s);
   launch(k_dep_edge_flag, blocks_for(nd, 256), 256, 0, s, nd,

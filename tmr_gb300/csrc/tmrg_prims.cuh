@@ -25,6 +25,8 @@ struct Stage {
 extern std::atomic<long long> g_kernel_launches;
 // device-to-host reads that wait for the stream (read_scalar)
 extern std::atomic<long long> g_host_syncs;
+// Device allocations made through DBuf (the library's only device allocator).
+extern std::atomic<long long> g_device_allocs;
 
 // Optional per-kernel timing (tmrg_profile_begin/end): CUDA events recorded
 // on the launching stream around each launch, with the launch's
@@ -101,6 +103,7 @@ struct DBuf {
     s = st;
     n = count;
     if (count) {
+      g_device_allocs.fetch_add(1, std::memory_order_relaxed);
       cudaError_t e = cudaMallocAsync((void **)&p, count * sizeof(T), s);
       if (e != cudaSuccess) {
         p = nullptr;
