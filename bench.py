@@ -93,13 +93,16 @@ def aggregate(ms_local, units_local, world, allreduce_max):
 
 # ---------------------------------------------------------------------------
 # GPU pipeline
-def gpu_pipeline(TMR, conn, W, x_fine=None, host=False, prefetched=None):
-    """Returns (units, products).  host=True uses host buffers throughout."""
+def gpu_pipeline(TMR, conn, W, x_fine=None, host=False, prefetched=None, mark=None):
+    """Returns (units, products).  host=True uses host buffers throughout.
+    mark(stage) (optional) is called after each stage is queued."""
     import torch
+    mark = mark or (lambda name: None)
     f = TMR.OctForest(order=W["order"], interp=TMR.GAUSS_LOBATTO_POINTS)
     f.setConnectivity(conn)
     f.createTrees(W["L0"])
     h2d = d2h = 0
+    passes = []
     for p in range(W["passes"]):
         n = f.getNumOctants()
         if host:
@@ -109,21 +112,26 @@ def gpu_pipeline(TMR, conn, W, x_fine=None, host=False, prefetched=None):
         else:
             f.refine(TMR.random_refinement(n, W["seed"], p, W["prob"]), 0, W["max_level"])
         f.balance(W["corner"])
+        passes.append((n, f.getNumOctants()))
+    mark("refine+balance")
     f.createNodes()
+    mark("createNodes")
     forests = [f]
     for _ in range(W["levels"] - 1):
         c = forests[-1].coarsen()
         c.balance(W["corner"])
         c.createNodes()
         forests.append(c)
+    mark("coarse levels")
     interps = []
     for k in range(W["levels"] - 1):
         I = TMR.VecInterp()
         forests[k].createInterpolation(forests[k + 1], I)
         interps.append(I)
+    mark("createInterpolation")
     units = sum(fr.getNumOctants() for fr in forests)
     nv = W["nvec"]
-    out = {}
+    out = {"passes": passes}
     if host:
         x = prefetched["x"]
         bufs = prefetched["buf"]
@@ -161,6 +169,7 @@ def gpu_pipeline(TMR, conn, W, x_fine=None, host=False, prefetched=None):
             I.mult(x, y)
             x = y
         out["y"] = x
+        mark("P^T/P applies")
     out["forests"] = forests
     out["interps"] = interps
     out["h2d"] = h2d
@@ -242,6 +251,82 @@ def measured_peaks():
             d = json.load(fp)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def pipeline_roofline(TMR, conn, W, x_fine, peak):
+    """Compulsory HBM bytes of one whole step (every stage's input read and
+    output written once, nothing else) against its time, with a per-stage
+    split timed by CUDA events on the stream the library runs on.  Bytes:
+    16 per octant read and written by each refine+balance pass and each
+    coarsen+balance; per forest 4 * order^3 per element (conn),
+    4 + 12 r_d per dependent node (CSR row of mean length r_d), 4 per owned
+    node (numbers); per P 12 per entry + 4 per row; per apply 12 per entry
+    used + 4 per output row + 8 per input and output vector value."""
+    import torch
+    evs = []
+
+    def mark(name):
+        e = torch.cuda.Event(enable_timing=True)
+        e.record()
+        evs.append((name, e))
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    _u, o = gpu_pipeline(TMR, conn, W, x_fine, mark=mark)
+    torch.cuda.synchronize()
+    stages, prev = {}, e0
+    for name, e in evs:
+        stages[name] = round(prev.elapsed_time(e), 3)
+        prev = e
+    total_ms = e0.elapsed_time(evs[-1][1])
+    order, nv = W["order"], W["nvec"]
+    b = {"refine+balance": 0, "createNodes": 0, "coarse levels": 0, "createInterpolation": 0,
+         "P^T/P applies": 0}
+    n0 = W["nx"] * W["ny"] * W["nz"] * 8 ** W["L0"]
+    b["refine+balance"] += 16 * n0  # createTrees writes the first octants
+    for nin, nout in o["passes"]:
+        b["refine+balance"] += 16 * (nin + nout)
+
+    def node_bytes(fr):
+        s = fr._sizes()  # num_local, num_owned, num_dep, ext_pre, elements, dep_nnz
+        return 4 * int(s[4]) * order ** 3 + 4 * int(s[2]) + 12 * int(s[5]) + 4 * int(s[1])
+    b["createNodes"] += node_bytes(o["forests"][0])
+    for k in range(1, len(o["forests"])):
+        b["coarse levels"] += 16 * (o["forests"][k - 1].getNumOctants() +
+                                    o["forests"][k].getNumOctants())
+        b["coarse levels"] += node_bytes(o["forests"][k])
+    for I in o["interps"]:
+        rows, cols, nnz = I.sizes()
+        ap = I.applyNnz()
+        b["createInterpolation"] += 12 * nnz + 4 * (rows + 1)
+        # one P^T and one P per level
+        b["P^T/P applies"] += 2 * (12 * ap + 8 * nv * (rows + cols)) + 4 * (rows + 1) + \
+            4 * (cols + 1)
+    tot = sum(b.values())
+    del o
+    return {"bytes_per_step": tot, "ms_per_step": total_ms,
+            "achieved_gbs": tot / (total_ms / 1e3) / 1e9,
+            "frac": tot / (total_ms / 1e3) / 1e9 / peak,
+            "peak_gbs": peak,
+            "stages": {k: {"ms": stages.get(k), "bytes": b[k],
+                           "gbs": round(b[k] / (stages[k] / 1e3) / 1e9, 1)
+                           if stages.get(k) else None} for k in b}}
+
+
+TUNE_KINDS = {1: "P apply", 2: "P^T apply", 3: "filter vpn3 FP32", 4: "filter vpn3 FP64"}
+
+
+def autotune_report(TMR):
+    """The autotuner's choices so far (made during the warm-up steps): per
+    size class the candidate chosen and every candidate's time."""
+    buf = ctypes.create_string_buffer(1 << 16)
+    if TMR.lib().tmrg_tune_report(buf, len(buf)) != 0:
+        return None
+    out = []
+    for e in json.loads(buf.value.decode()):
+        e["kind"] = TUNE_KINDS.get(e["kind"], e["kind"])
+        out.append(e)
+    return out
 
 
 def profile_step(TMR, conn, W, x_fine):
@@ -499,6 +584,9 @@ def run_gpu(args):
                           "gbs": round(v[2] / (v[1] / 1e3) / 1e9, 1) if v[2] and v[1] else None,
                           "tflops": round(v[3] / (v[1] / 1e3) / 1e12, 3) if v[3] and v[1] else None}
 
+    pipe_roof = pipeline_roofline(TMR, conn, W, x_fine, peak)
+    tuned = autotune_report(TMR)
+
     chain = None
     if rank == 0 and not args.no_filter:
         try:
@@ -526,7 +614,8 @@ def run_gpu(args):
                        "parallelism": "replicas x%d" % world,
                        "l2": "working set (GBs) larger than L2; no flush"},
             "e2e": e2e, "gpu_launches": launches, "host_syncs": syncs,
-            "roofline": roof, "p_apply": p_apply,
+            "roofline": roof, "p_apply": p_apply, "pipeline_roofline": pipe_roof,
+            "autotune": tuned,
             "filter_chain": chain,
             "cpu_baseline": cpu, "clocks": clocks, "kernels": kernels,
         }

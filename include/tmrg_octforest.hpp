@@ -336,6 +336,52 @@ class TMROctForest : public TMRGEntity {
     for (int e = 0; e < ne; e++) fprintf(fp, "%d\n", 12);
     fclose(fp);
   }
+  // Axis-aligned box (origin xyz, extent xyz) of every block: the stand-in
+  // for the topology's volumes that getPoints and writeForestToVTK map
+  // through (tmrg_forest_set_block_boxes).
+  void setBlockBoxes(const double *boxes, int nblocks) {
+    if (tmrg_report(tmrg_forest_set_block_boxes(f, boxes, nblocks), "setBlockBoxes"))
+      boxes_.assign(boxes, boxes + (size_t)(boxes ? 6 * nblocks : 0));
+  }
+  // writeForestToVTK (TMROctForest.cpp:1317-1384): every octant as a
+  // hexahedron with its own eight corners (x fastest) mapped through its
+  // block's box, and the block index as the cell scalar entity_index.
+  // Like the reference without a topology, nothing is written when no
+  // block boxes are set.
+  void writeForestToVTK(const char *filename) {
+    if (boxes_.empty()) return;
+    TMROctantArray *arr = nullptr;
+    getOctants(&arr);
+    if (!arr) return;
+    FILE *fp = filename ? fopen(filename, "w") : nullptr;
+    if (!fp) return;
+    const int n = (int)arr->n;
+    const TMROctant *o = arr->ptr;
+    const double hmax = (double)(1 << 30);
+    fprintf(fp, "# vtk DataFile Version 3.0\nvtk output\nASCII\n");
+    fprintf(fp, "DATASET UNSTRUCTURED_GRID\nPOINTS %d float\n", 8 * n);
+    for (int k = 0; k < n; k++) {
+      const int32_t h = 1 << (30 - o[k].level);
+      const double *b = &boxes_[6 * (size_t)o[k].block];
+      for (int kk = 0; kk < 2; kk++)
+        for (int jj = 0; jj < 2; jj++)
+          for (int ii = 0; ii < 2; ii++) {
+            const double u = 1.0 * (o[k].x + ii * h) / hmax;
+            const double v = 1.0 * (o[k].y + jj * h) / hmax;
+            const double w = 1.0 * (o[k].z + kk * h) / hmax;
+            fprintf(fp, "%e %e %e\n", b[0] + b[3] * u, b[1] + b[4] * v, b[2] + b[5] * w);
+          }
+    }
+    fprintf(fp, "\nCELLS %d %d\n", n, 9 * n);
+    for (int k = 0; k < n; k++)
+      fprintf(fp, "8 %d %d %d %d %d %d %d %d\n", 8 * k, 8 * k + 1, 8 * k + 3, 8 * k + 2,
+              8 * k + 4, 8 * k + 5, 8 * k + 7, 8 * k + 6);
+    fprintf(fp, "\nCELL_TYPES %d\n", n);
+    for (int k = 0; k < n; k++) fprintf(fp, "12\n");
+    fprintf(fp, "CELL_DATA %d\nSCALARS entity_index float 1\nLOOKUP_TABLE default\n", n);
+    for (int k = 0; k < n; k++) fprintf(fp, "%e\n", 1.0 * o[k].block);
+    fclose(fp);
+  }
   int getExtPreOffset() {
     int64_t s[6] = {0};
     tmrg_forest_node_sizes(f, s);
@@ -369,6 +415,7 @@ class TMROctForest : public TMRGEntity {
   std::vector<int> nn_;
   std::vector<TMRPoint> points_;
   std::vector<double> knots_;
+  std::vector<double> boxes_;
   int range_[2];
 };
 

@@ -2207,13 +2207,13 @@ double oo_uniform(uint64_t seed, uint64_t stream, uint64_t index) {
 /* ------------------------------------------------------------------ */
 /* Matrix density filter (TMRMatrixFilter.cpp:30-235).  Parity unpinned:
    the mass matrix is assembled by TACS in the reference (absent here).
-   Restatement: trilinear elements (TMRMatrixCreator.h:79-80) on blocks that
-   are cubes of side block_len; the exact element mass matrix of a cube of
-   side a is M_ab = a^3 / (27 * 2^k), k = number of local coordinates in
-   which corners a and b differ.  Dependent nodes are condensed: each
-   element merges its expanded 8x8 block over its distinct independent
-   nodes (first-appearance order; products summed in (a, b, p, q) loop
-   order), and the element blocks are summed in element order. */
+   Restatement: trilinear elements for order 2, quadratic and cubic
+   Bernstein hexahedra for orders 3 and 4 (TMRMatrixCreator.h:76-92), on
+   blocks that are cubes of side block_len (elem_mass).  Dependent nodes
+   are condensed: each element merges its expanded block over its distinct
+   independent nodes (first-appearance order; products summed in
+   (a, b, p, q) loop order), and the element blocks are summed in element
+   order. */
 struct oo_filter {
   int n, nnz, N;
   double r;
@@ -2265,61 +2265,96 @@ static void filter_horner(oo_filter *F, int tr, int vpn, const double *in,
   free(nxt);
 }
 
+/* 1-D Bernstein mass of degree p on [0, 1]:
+   int B_i B_j = C(p, i) C(p, j) / ((2p + 1) C(2p, i + j)), one division. */
+static double bern_mass_1d(int p, int i, int j) {
+  double ci = 1.0, cj = 1.0, c2 = 1.0;
+  for (int k = 1; k <= i; k++) ci = ci * (p - k + 1) / k;
+  for (int k = 1; k <= j; k++) cj = cj * (p - k + 1) / k;
+  for (int k = 1; k <= i + j; k++) c2 = c2 * (2 * p - k + 1) / k;
+  return (ci * cj) / ((2 * p + 1) * c2);
+}
+
+/* Element mass of an order-o element on a cube of side `side`
+   (TMRMatrixCreator.h:76-92): the trilinear element for order 2, the
+   quadratic and cubic Bernstein hexahedra for orders 3 and 4, whose
+   consistent mass matrices are tensor products of the 1-D Bernstein
+   masses (TACS integrates them exactly on axis-aligned cubes).  Order 2
+   keeps the exact form s^3 / (27 * 2^k) (k = coordinates in which the two
+   corners differ); orders 3-4 form ((s^3 m_x) m_y) m_z. */
+static double elem_mass(int o, double s3, int a, int b) {
+  if (o == 2) {
+    int x = a ^ b;
+    int k = (x & 1) + ((x >> 1) & 1) + (x >> 2);
+    return s3 / (27.0 * (double)(1 << k));
+  }
+  int p = o - 1;
+  int ia = a % o, ja = (a / o) % o, ka = a / (o * o);
+  int ib = b % o, jb = (b / o) % o, kb = b / (o * o);
+  return ((s3 * bern_mass_1d(p, ia, ib)) * bern_mass_1d(p, ja, jb)) * bern_mass_1d(p, ka, kb);
+}
+
 oo_filter *oo_filter_create(oo_forest *f, double block_len, double r, int N) {
-  if (f->order != 2) return NULL;
+  if (f->order < 2 || f->order > 4) return NULL;
   oo_create_nodes(f);
   oo_filter *F = (oo_filter *)calloc(1, sizeof(oo_filter));
   F->n = f->num_owned;
   F->N = N;
   F->r = r;
+  const int o = f->order, npe = o * o * o, mx = o * o; /* dependent rows <= o^2 */
   long cap = 1 << 16, ne = 0;
   oo_fent *E = (oo_fent *)malloc(sizeof(oo_fent) * (size_t)cap);
+  int *ni = (int *)malloc(sizeof(int) * (size_t)npe * mx);
+  double *nw = (double *)malloc(sizeof(double) * (size_t)npe * mx);
+  int *nc = (int *)malloc(sizeof(int) * (size_t)npe);
+  int *U = (int *)malloc(sizeof(int) * (size_t)npe * mx);
+  double *L = NULL;
+  long Lcap = 0;
   for (long e = 0; e < f->noct; e++) {
-    const int *ec = &f->econn[8 * e];
-    int ni[8][4], nc[8], U[27], K = 0;
-    double nw[8][4];
-    for (int a = 0; a < 8; a++) {
+    const int *ec = &f->econn[(long)npe * e];
+    int K = 0;
+    for (int a = 0; a < npe; a++) {
       int g = ec[a];
       if (g >= 0) {
         nc[a] = 1;
-        ni[a][0] = g;
-        nw[a][0] = 1.0;
+        ni[a * mx] = g;
+        nw[a * mx] = 1.0;
       } else {
         int d = -g - 1;
         nc[a] = f->dep_ptr[d + 1] - f->dep_ptr[d];
         for (int p = 0; p < nc[a]; p++) {
-          ni[a][p] = f->dep_conn[f->dep_ptr[d] + p];
-          nw[a][p] = f->dep_w[f->dep_ptr[d] + p];
+          ni[a * mx + p] = f->dep_conn[f->dep_ptr[d] + p];
+          nw[a * mx + p] = f->dep_w[f->dep_ptr[d] + p];
         }
       }
       for (int p = 0; p < nc[a]; p++) {
         int u = 0;
-        while (u < K && U[u] != ni[a][p]) u++;
-        if (u == K) U[K++] = ni[a][p];
+        while (u < K && U[u] != ni[a * mx + p]) u++;
+        if (u == K) U[K++] = ni[a * mx + p];
       }
     }
-    double L[27][27];
-    for (int u = 0; u < K; u++)
-      for (int v = 0; v < K; v++) L[u][v] = 0.0;
+    if ((long)K * K > Lcap) {
+      Lcap = (long)K * K;
+      L = (double *)realloc(L, sizeof(double) * (size_t)Lcap);
+    }
+    for (long u = 0; u < (long)K * K; u++) L[u] = 0.0;
     double side = block_len / (double)(1 << f->octs[e].level);
     double s3 = side * side * side;
-    for (int a = 0; a < 8; a++)
-      for (int b = 0; b < 8; b++) {
-        int x = a ^ b;
-        int k = (x & 1) + ((x >> 1) & 1) + (x >> 2);
-        double mab = s3 / (27.0 * (double)(1 << k));
+    for (int a = 0; a < npe; a++)
+      for (int b = 0; b < npe; b++) {
+        double mab = elem_mass(o, s3, a, b);
         for (int p = 0; p < nc[a]; p++) {
           int u = 0;
-          while (U[u] != ni[a][p]) u++;
-          double t = mab * nw[a][p];
+          while (U[u] != ni[a * mx + p]) u++;
+          double t = mab * nw[a * mx + p];
           for (int q = 0; q < nc[b]; q++) {
             int v = 0;
-            while (U[v] != ni[b][q]) v++;
-            L[u][v] = L[u][v] + t * nw[b][q];
+            while (U[v] != ni[b * mx + q]) v++;
+            L[(long)u * K + v] = L[(long)u * K + v] + t * nw[b * mx + q];
           }
         }
       }
-    while (ne + K * K > cap) {
+    while (ne + (long)K * K > cap) {
       cap *= 2;
       E = (oo_fent *)realloc(E, sizeof(oo_fent) * (size_t)cap);
     }
@@ -2327,10 +2362,15 @@ oo_filter *oo_filter_create(oo_forest *f, double block_len, double r, int N) {
       for (int v = 0; v < K; v++) {
         E[ne].key = (long)U[u] * (long)F->n + U[v];
         E[ne].seq = ne;
-        E[ne].v = L[u][v];
+        E[ne].v = L[(long)u * K + v];
         ne++;
       }
   }
+  free(ni);
+  free(nw);
+  free(nc);
+  free(U);
+  free(L);
   qsort(E, (size_t)ne, sizeof(oo_fent), cmp_fent);
   F->rowptr = (int *)calloc((size_t)F->n + 1, sizeof(int));
   F->cols = (int *)malloc(sizeof(int) * (size_t)(ne ? ne : 1));

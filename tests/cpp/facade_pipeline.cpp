@@ -9,7 +9,7 @@
 
 #include "tmrg_octforest.hpp"
 
-int main() {
+int main(int argc, char **argv) {
   const int nx = 3, ny = 2, nz = 2;
   std::vector<int> conn;
   for (int k = 0; k < nz; k++)
@@ -87,6 +87,14 @@ int main() {
   corner.x = corner.y = corner.z = 0;
   int rev = -1, fid = -1;
   f->transformNode(&corner, -1, &rev, &fid);
+  // the forest outline through unit block boxes (writeForestToVTK)
+  std::vector<double> boxes(6 * nb);
+  for (int b = 0; b < nb; b++) {
+    boxes[6 * b + 0] = b, boxes[6 * b + 1] = 0.0, boxes[6 * b + 2] = 0.0;
+    boxes[6 * b + 3] = boxes[6 * b + 4] = boxes[6 * b + 5] = 1.0;
+  }
+  f->setBlockBoxes(boxes.data(), nb);
+  f->writeForestToVTK(argc > 1 ? argv[1] : "/dev/null");
   printf("elements %d owned %d dep %d conn_sum %lld P_rows %lld P_nnz %lld P1_sum %.12f "
          "blocks %d faces %d edges %d nodes %d node_refs %d local_ok %d pu %.15f du %.15f "
          "enclosed_self %d corner_block %d\n",

@@ -169,10 +169,10 @@ def make_api_golden():
     # design -> analysis weights: analysis forest = a refined forest, filter
     # forest = its coarsened forest (orders 2 and 3)
     L.tmrref_topo_weights.restype = ctypes.c_long
-    for name in ("brick_o2", "rot_o3"):
+    for name in ("brick_o2", "rot_o3", "bern_o3", "coarse_o4"):
         case = dict(pipeline.cases()[name])
         case["passes"] = 2
-        ana = RefForest(case["order"], 1)
+        ana = RefForest(case["order"], case.get("interp", 1))
         ana.setConnectivity(case["conn"])
         ana.createTrees(case["L0"])
         for p in range(case["passes"]):

@@ -191,15 +191,16 @@ def test_forest_eval_interp_matches_reference(gpu_lib):
                 np.testing.assert_array_equal(d2[:10], z[key + "_d2"][:10])
 
 
-@pytest.mark.parametrize("name", ["brick_o2", "rot_o3"])
+@pytest.mark.parametrize("name", ["brick_o2", "rot_o3", "bern_o3", "coarse_o4"])
 def test_topo_weights_match_reference(gpu_lib, name):
     """Design -> analysis weights of every element against the reference's
-    computeWeights steps run on the reference forests."""
+    computeWeights steps run on the reference forests (Lagrange filters of
+    orders 2-4 and a Bernstein filter)."""
     from tmr_gb300 import TMR
     z = _golden()
     case = json.loads(str(z["tw_%s_case" % name]))
     case["conn"] = z["tw_%s_conn" % name]
-    ana = TMR.OctForest(order=case["order"])
+    ana = TMR.OctForest(order=case["order"], interp=case.get("interp", 1))
     ana.setConnectivity(case["conn"])
     ana.createTrees(case["L0"])
     for p in range(case["passes"]):
@@ -213,7 +214,7 @@ def test_topo_weights_match_reference(gpu_lib, name):
     rp, ci, w = W_.getCSR()
     np.testing.assert_array_equal(rp, z["tw_%s_rowptr" % name])
     np.testing.assert_array_equal(ci, z["tw_%s_cols" % name])
-    np.testing.assert_array_equal(w, z["tw_%s_w" % name])
+    np.testing.assert_allclose(w, z["tw_%s_w" % name], rtol=1e-13, atol=1e-13)
     # the element values of a constant design field are that constant
     rows, cols, _ = W_.sizes()
     y = np.zeros(rows)
@@ -239,3 +240,39 @@ def test_interpolate_design_vec_keeps_constants(gpu_lib):
     y = np.zeros(2 * ng)
     TMR.interpolateDesignVec(f, x, g, y)
     np.testing.assert_allclose(y.reshape(-1, 2), np.tile([1.5, -2.0], (ng, 1)), rtol=1e-12)
+
+
+def test_write_forest_to_vtk(gpu_lib, tmp_path):
+    """writeForestToVTK: eight corner points per octant (x fastest) through
+    the block boxes, the reference's corner order in CELLS, the block index
+    as entity_index; nothing is written without block boxes (the
+    reference's behaviour without a topology)."""
+    from tmr_gb300 import TMR
+    case = pipeline.cases()["brick_o2"]
+    f = TMR.OctForest(order=2)
+    f.setConnectivity(case["conn"])
+    f.createTrees(1)
+    f.refine(W.random_indicator(f.getNumOctants(), 5, 0, 0.4), 0, 3)
+    f.balance(1)
+    fn = tmp_path / "forest.vtk"
+    f.writeForestToVTK(str(fn))
+    assert not fn.exists()
+    boxes = pipeline.brick_boxes(3, 2, 2, ext=(2.0, 1.0, 0.5))
+    f.setBlockBoxes(boxes)
+    f.writeForestToVTK(str(fn))
+    lines = fn.read_text().split("\n")
+    o = f.getOctantsArray()
+    n = len(o)
+    i = lines.index("POINTS %d float" % (8 * n))
+    pts = np.array([[float(v) for v in ln.split()] for ln in lines[i + 1:i + 1 + 8 * n]])
+    h = (1 << (30 - o[:, 5].astype(np.int64))) / 2.0 ** 30
+    for k in (0, n // 2, n - 1):
+        b = boxes[o[k, 0]]
+        for c in range(8):
+            u = o[k, 1:4] / 2.0 ** 30 + h[k] * np.array([c & 1, (c >> 1) & 1, c >> 2])
+            np.testing.assert_allclose(pts[8 * k + c], b[:3] + b[3:] * u, rtol=1e-6)
+    j = lines.index("CELLS %d %d" % (n, 9 * n))
+    assert lines[j + 1] == "8 0 1 3 2 4 5 7 6"
+    e = lines.index("SCALARS entity_index float 1")
+    ent = np.array([float(v) for v in lines[e + 2:e + 2 + n]])
+    np.testing.assert_array_equal(ent, o[:, 0])

@@ -38,11 +38,32 @@ def test_error_statuses_and_recovery(gpu_lib):
     assert f.getMeshConn().shape == (f.getNumOctants(), 8)
     with pytest.raises(ValueError):
         f.createInterpolation(f, TMR.VecInterp())
-    b = TMR.OctForest(order=3, interp=TMR.BERNSTEIN_POINTS)
+    # Bernstein elements of order 6: the reference tabulates dependent
+    # weights for orders 2-5 only (eval_bernstein_weights)
+    b = TMR.OctForest(order=6, interp=TMR.BERNSTEIN_POINTS)
     b.setConnectivity(W.brick(1, 1, 1))
     b.createTrees(1)
     with pytest.raises(TMRGError) as e:
         b.createNodes()
+    assert e.value.status == 6
+    # Bernstein meshes two orders apart (the reference's degree-elevation
+    # table covers one order)
+    b4 = TMR.OctForest(order=4, interp=TMR.BERNSTEIN_POINTS)
+    b4.setConnectivity(W.brick(1, 1, 1))
+    b4.createTrees(1)
+    b4.createNodes()
+    b2 = b4.duplicate()
+    b2.setMeshOrder(2, TMR.BERNSTEIN_POINTS)
+    b2.createNodes()
+    with pytest.raises(TMRGError) as e:
+        b4.createInterpolation(b2, TMR.VecInterp())
+    assert e.value.status == 6
+    # matrix filter on an order-5 forest (no element basis in the reference)
+    f5 = TMR.OctForest(order=5)
+    f5.setConnectivity(W.brick(1, 1, 1))
+    f5.createTrees(1)
+    with pytest.raises(TMRGError) as e:
+        TMR.MatrixFilter(0.1, 10, None, [f5])
     assert e.value.status == 6
 
 

@@ -34,8 +34,10 @@ def _p(a):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["brick_o2", "rot_o2", "c1_small"])
+@pytest.mark.parametrize("name", ["brick_o2", "rot_o2", "c1_small", "brick_o3", "rot_o4"])
 def test_filter_matches_oracle(gpu_lib, name):
+    # orders 3 and 4 use the quadratic / cubic Bernstein element mass and a
+    # different (blocked) summation order on the GPU: M agrees to rounding
     import torch
 
     from tmr_gb300 import TMR
@@ -55,7 +57,7 @@ def test_filter_matches_oracle(gpu_lib, name):
     L.oo_filter_get_matrix(ctypes.c_void_p(OF), _p(orp), _p(oc), _p(ov), _p(oA), _p(oB), _p(oT))
     np.testing.assert_array_equal(rp, orp)
     np.testing.assert_array_equal(cols, oc)
-    np.testing.assert_allclose(vals, ov, rtol=1e-13)
+    np.testing.assert_allclose(vals, ov, rtol=1e-13, atol=1e-14 * np.abs(ov).max())
     np.testing.assert_allclose(A, oA, rtol=1e-13)
     np.testing.assert_allclose(B, oB, rtol=1e-13)
     np.testing.assert_allclose(T, oT, rtol=1e-13)
@@ -188,3 +190,76 @@ def test_quad_filter_matches_restatement(gpu_lib, name):
     yt = np.zeros(n)
     F.applyTranspose(w, yt)
     assert w @ horner(x, To) == pytest.approx(yt @ x, rel=1e-11)
+
+
+@pytest.mark.gpu
+def test_filter_chain_c3_shape_fd_1000_directions(gpu_lib):
+    """The differentiable filter -> prolongation chain on a reduced copy of
+    the 16x8x8-brick, 16-bump configuration (vpn 3, r = 2 h_min, N = 10):
+    the gradient of sum w rho^3 against central differences (h = 1e-6) in
+    1000 seeded directions, and the backward pass (P^T then F^T) against
+    the oracle's CSR transpose followed by the reference's applyTranspose
+    recurrence restated in numpy on the library's M, Ainv, B, Tinv (M
+    itself is checked against the oracle in test_filter_matches_oracle)."""
+    import torch
+
+    import bench
+    from oracle.oracle import _lib
+    from tmr_gb300 import TMR
+    from tmr_gb300.autograd import filter_interp
+    FW = dict(bench.FILTER_WORKLOAD, target=400_000, max_level=8)
+    fine, coarse, I, F, r = bench.build_filter_chain(TMR, FW)
+    vpn = FW["vpn"]
+    n, _ = F.size()
+    rows, cols, _ = I.sizes()
+    assert cols == n and rows > 100_000
+    gen = torch.Generator(device="cpu").manual_seed(11)
+    x = torch.rand(n * vpn, generator=gen, dtype=torch.float64).cuda().requires_grad_(True)
+    w = torch.rand(rows * vpn, generator=gen, dtype=torch.float64).cuda()
+
+    def obj(v):
+        return (w * filter_interp(v, F, I, vpn) ** 3).sum()
+
+    J = obj(x)
+    J.backward()
+    gx = x.grad.detach()
+    h = 1e-6
+    # the central difference carries the roundoff of two sums of
+    # rows * vpn terms: about eps * sum |w rho^3| / h, on top of the
+    # O(h^2) truncation of the cubic objective
+    with torch.no_grad():
+        S = (w * filter_interp(x.detach(), F, I, vpn).abs() ** 3).sum().item()
+    fd_noise = 4.0 * 2.2e-16 * S / h
+    worst = 0.0
+    with torch.no_grad():
+        for k in range(1000):
+            d = torch.randn(n * vpn, generator=gen, dtype=torch.float64).cuda()
+            fd = ((obj(x + h * d) - obj(x - h * d)) / (2 * h)).item()
+            an = torch.dot(gx, d).item()
+            worst = max(worst, abs(fd - an) / (1e-7 * abs(an) + fd_noise))
+    assert worst <= 1.0, worst
+    # backward pass against the oracle: g = F^T (P^T gy)
+    L = _lib("oracle").lib
+    P_ = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    rp, pc, pv = I.getCSR()
+    gy = (3.0 * w * filter_interp(x.detach(), F, I, vpn) ** 2).cpu().numpy()
+    gp = np.zeros(cols * vpn)
+    L.oo_csr_mult_t(rows, cols, P_(rp), P_(pc), P_(pv), vpn, P_(gy), P_(gp))
+    frp, fc, fv, fA, fB, fT = F.getMatrix()
+    gx_ref = _horner_t(frp, fc, fv, fA, fB, fT, N_TERMS, gp, vpn)
+    np.testing.assert_allclose(gx.cpu().numpy(), gx_ref, rtol=1e-13,
+                               atol=1e-13 * np.abs(gx_ref).max())
+
+
+def _horner_t(rp, cols, vals, A, B, T, N, x, vpn):
+    """TMRMatrixFilter::applyTranspose (TMRMatrixFilter.cpp:216-235) on the
+    given matrices: t1 = T x, out = M (B out) + t1 N times, then A out."""
+    import scipy.sparse as sp
+    n = len(A)
+    M = sp.csr_matrix((vals, cols, rp), shape=(n, n))
+    X = x.reshape(n, vpn)
+    t1 = T[:, None] * X
+    out = t1.copy()
+    for _ in range(N):
+        out = M @ (B[:, None] * out) + t1
+    return (A[:, None] * out).ravel()

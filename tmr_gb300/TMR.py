@@ -359,11 +359,13 @@ class OctForest:
         geometry getPoints maps node positions through; None removes it."""
         if boxes is None:
             call("tmrg_forest_set_block_boxes", self.ptr, None, 0)
+            self._boxes = None
             return
         b = np.ascontiguousarray(boxes, dtype=np.float64)
         if b.ndim != 2 or b.shape[1] != 6:
             raise ValueError("Expected array of shape (n, 6)")
         call("tmrg_forest_set_block_boxes", self.ptr, _ptr(b), b.shape[0])
+        self._boxes = b.copy()
 
     def getPoints(self):
         """Node locations (num_local_nodes, 3) (TMROctForest::getPoints):
@@ -485,6 +487,45 @@ class OctForest:
                 fp.write("8 " + " ".join(str(8 * i + k) for k in range(8)) + "\n")
             fp.write("CELL_TYPES %d\n" % len(o))
             fp.write("12\n" * len(o))
+
+
+    def writeForestToVTK(self, fname):
+        """writeForestToVTK (TMROctForest.cpp:1317-1384): every octant as a
+        hexahedron with its own eight corner points (x fastest), mapped
+        through the block's volume, and the block index as the cell scalar
+        `entity_index`.  The block boxes (setBlockBoxes) stand in for the
+        topology's volumes; like the reference without a topology, nothing
+        is written when no boxes are set."""
+        boxes = getattr(self, "_boxes", None)
+        if boxes is None:
+            return
+        o = self.getOctantsArray()
+        n = len(o)
+        h = (1 << (30 - o[:, 5].astype(np.int64)))
+        hmax = float(1 << 30)
+        with open(fname, "w") as fp:
+            fp.write("# vtk DataFile Version 3.0\nvtk output\nASCII\n")
+            fp.write("DATASET UNSTRUCTURED_GRID\nPOINTS %d float\n" % (8 * n))
+            for r, hh in zip(o, h):
+                b = boxes[r[0]]
+                for kk in range(2):
+                    for jj in range(2):
+                        for ii in range(2):
+                            u = 1.0 * (r[1] + ii * hh) / hmax
+                            v = 1.0 * (r[2] + jj * hh) / hmax
+                            w = 1.0 * (r[3] + kk * hh) / hmax
+                            fp.write("%e %e %e\n" % (b[0] + b[3] * u, b[1] + b[4] * v,
+                                                     b[2] + b[5] * w))
+            fp.write("\nCELLS %d %d\n" % (n, 9 * n))
+            for k in range(n):
+                c = 8 * k
+                fp.write("8 %d %d %d %d %d %d %d %d\n" % (c, c + 1, c + 3, c + 2, c + 4, c + 5,
+                                                          c + 7, c + 6))
+            fp.write("\nCELL_TYPES %d\n" % n)
+            fp.write("12\n" * n)
+            fp.write("CELL_DATA %d\nSCALARS entity_index float 1\nLOOKUP_TABLE default\n" % n)
+            for r in o:
+                fp.write("%e\n" % (1.0 * r[0]))
 
 
 class Quadrant:

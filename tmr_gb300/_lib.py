@@ -23,6 +23,8 @@ _SIGS = {
     "tmrg_kernel_launch_count": [],
     "tmrg_host_sync_count": [],
     "tmrg_device_alloc_count": [],
+    "tmrg_tune_reset": [c_int],
+    "tmrg_tune_report": [c_vp, c_i64],
     "tmrg_profile_begin": [],
     "tmrg_profile_end": [c_vp, c_i64],
     "tmrg_measure_fp64_peak": [P(c_dbl)],

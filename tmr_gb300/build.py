@@ -26,6 +26,7 @@ SOURCES = [
     "tmrg_stl.cu",
     "tmrg_quad.cu",
     "tmrg_capi.cu",
+    "tmrg_tune.cu",
 ]
 
 NVCC_FLAGS = [

@@ -240,6 +240,12 @@ __global__ void k_h_cvt(long long n, const A *__restrict__ a, B *b) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) b[i] = (B)a[i];
 }
+// FP32 weights of P from its (hi, lo) apply copy: hi is the weight rounded
+// to float.
+__global__ void k_h_hi(long long n, const float2 *__restrict__ a, float *b) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i].x;
+}
 
 // ---------------------------------------------------------------------
 // Operator: xd = dependent values, yE = element products, y = scatter.
@@ -1149,10 +1155,10 @@ static void helmholtz_levels(F *const *forests, int nlevels, double r, Helmholtz
     HInterp32 &P32 = *H.P32.back();
     P32.p.alloc(std::max(1LL, I.nnz_nz), s);
     P32.pt.alloc(std::max(1LL, I.nnz_nz), s);
-    launch((k_h_cvt<double, float>), blocks_for(I.nnz_nz, 256), 256, 0, s, I.nnz_nz,
-           I.ap_vals(), P32.p.p);
-    launch((k_h_cvt<double, float>), blocks_for(I.nnz_nz, 256), 256, 0, s, I.nnz_nz,
-           (const double *)I.t_vals.p, P32.pt.p);
+    launch(k_h_hi, blocks_for(I.nnz_nz, 256), 256, 0, s, I.nnz_nz,
+           (const float2 *)I.ap_w.p, P32.p.p);
+    launch(k_h_hi, blocks_for(I.nnz_nz, 256), 256, 0, s, I.nnz_nz,
+           (const float2 *)I.t_w.p, P32.pt.p);
   }
 }
 static void helmholtz_finish(Helmholtz &H);

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <memory>
 #include <vector>
 
@@ -11,6 +12,19 @@
 #include "tmrg_prims.cuh"
 
 namespace tmrg {
+
+// Autotuner (tmrg_tune.cu): a size class of an operation with `ncand`
+// candidate shapes.  tune_run runs the operation with the class's chosen
+// candidate, timing all of them the first time the class is seen on the
+// device; tune_lookup returns the cached choice (or the fallback).
+struct TuneKey {
+  int kind, a, b, c, d;
+  int fallback;
+};
+enum TuneKind { TUNE_P = 1, TUNE_PT = 2, TUNE_FILTER3_F32 = 3, TUNE_FILTER3_F64 = 4 };
+int tune_run(const TuneKey &k, int ncand, const std::function<void(int)> &run,
+             cudaStream_t s);
+int tune_lookup(const TuneKey &k);
 
 // Device view of the block connectivity tables.  CSR entries hold
 // 8*block+corner, 12*block+edge, 6*block+face; the first entry of each
@@ -101,18 +115,24 @@ struct Interp {
   // changes y_i = sum_j P_ij x_j by at most (dropped entries of row i)
   // * 2^-49 * max |x_j|, below 1e-13 of max |x| for the row lengths of P;
   // P itself (getCSR) keeps every entry.  Without such entries
-  // (nnz_nz == nnz) the applies use P itself.
+  // (nnz_nz == nnz) the applies use P's structure.
   long long nnz_nz = 0;
   DBuf<int> nz_rowptr, nz_colidx;
-  DBuf<double> nz_vals;
   const int *ap_rowptr() const { return nnz_nz < nnz ? nz_rowptr.p : rowptr.p; }
   const int *ap_colidx() const { return nnz_nz < nnz ? nz_colidx.p : colidx.p; }
-  const double *ap_vals() const { return nnz_nz < nnz ? nz_vals.p : vals.p; }
+  // The apply copy's weights as double-float pairs (hi, lo): w = hi + lo to
+  // 2^-48 |w| (df_split).  The applies run in double-float arithmetic on the
+  // FP32 pipe (GB300 issues FP64 at 1/64 of its FP32 rate), same 8 bytes
+  // per weight as an FP64 copy.
+  DBuf<float2> ap_w;
   DBuf<int> perm;  // apply rows ordered by length inside windows
   DBuf<int> t_rowptr, t_colidx;  // P^T (zero-free) as CSR, rows = coarse nodes
   DBuf<int> t_perm;  // P^T rows by input chunk of their last entry, then length
   std::vector<long long> t_chunk;  // t_perm range of each input chunk
-  DBuf<double> t_vals;
+  DBuf<float2> t_w;  // P^T weights (hi, lo)
+  // dfflag[0]: a weight outside the double-float window (the applies then
+  // run in FP64); dfflag[1]: the same for the input vector of one apply
+  DBuf<int> dfflag;
   bool have_colsum = false;
   DBuf<double> colsum;  // P^T 1 (column sums of P), made on first use
 };

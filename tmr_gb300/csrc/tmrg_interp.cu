@@ -877,11 +877,102 @@ __global__ void k_ptr32(long long n, const long long *__restrict__ in, int *out)
   if (i <= n) out[i] = (int)in[i];
 }
 
+// ---------------------------------------------------------------------
+// Double-float arithmetic for the applies.  A value v is carried as two
+// floats, hi = v rounded to 24 bits and lo = v - hi rounded to 24 bits
+// (|v - hi - lo| <= 2^-48 |v|), and a CSR product sum as a pair (sh, sl)
+// updated with an exact product (TwoProduct by FMA) and an exact sum
+// (TwoSum), renormalised every four terms.  Measured against exact sums
+// on order-3 Gauss-Lobatto prolongations (rows up to 27 entries, transpose
+// rows up to 616) the error stays below 3e-14 of max(1, |y|), inside the
+// 1e-13 bar, for about 13 FP32 operations per entry and vector instead of
+// one FP64 FMA: GB300 issues FP64 at 1/64 of its FP32 rate, which bounds
+// an FP64 apply at 2 FMAs per 12 bytes of matrix far below its HBM rate.
+//
+// The split takes the exponent and mantissa bits apart with integer
+// operations (no FP64 instruction).  Values are represented when their
+// biased exponent lies in [emin, emin + erange) or they are zero; the
+// windows below keep every partial product and sum a normal float.
+constexpr unsigned DF_X_EMIN = 1023 - 40, DF_X_ERANGE = 100;  // 2^-40 <= |x| < 2^60
+constexpr unsigned DF_W_EMIN = 1023 - 49, DF_W_ERANGE = 66;   // 2^-49 <= |w| < 2^17
+__device__ __forceinline__ bool df_split(double v, unsigned emin, unsigned erange, float &hi,
+                                         float &lo) {
+  const unsigned h = (unsigned)__double2hiint(v), l = (unsigned)__double2loint(v);
+  const unsigned E = (h >> 20) & 0x7ffu, sgn = h & 0x80000000u;
+  const bool zero = ((h & 0x7fffffffu) | l) == 0u;
+  const bool in = (E - emin) < erange;
+  // top 24 bits rounded (a carry into the exponent is the correct rounding)
+  const unsigned rb = (l >> 28) & 1u;
+  const unsigned hb = (sgn | ((((h & 0x7fffffffu) - (896u << 20)) << 3) | (l >> 29))) + rb;
+  // the remainder v - hi: the low 29 mantissa bits, less 2^29 when rounded
+  // up, in units of 2^(E - 1075)
+  const int m = (int)(l & 0x1fffffffu) - (int)(rb << 29);
+  const float sc = __uint_as_float(sgn | ((E - 948u) << 23));
+  hi = in ? __uint_as_float(hb) : 0.0f;
+  lo = in ? __fmul_rn(__int2float_rn(m), sc) : 0.0f;
+  return in || zero;
+}
+// A weight of the apply copy: weights below the window (< 2^-49, the
+// apply_keeps residue kept when P has few of them) become 0, which changes
+// a row by at most 2^-49 |x| per such entry; weights above it (or Inf/NaN)
+// set the flag that sends the applies to FP64.
+__device__ __forceinline__ float2 df_weight(double w, int *flag) {
+  float hi, lo;
+  if (!df_split(w, DF_W_EMIN, DF_W_ERANGE, hi, lo) &&
+      ((unsigned)(__double2hiint(w) >> 20) & 0x7ffu) >= DF_W_EMIN + DF_W_ERANGE)
+    atomicOr(flag, 1);
+  return make_float2(hi, lo);
+}
+// (sh, sl) += (wh + wl)(xh + xl), the wl xl term (below 2^-48 |w x|) left out.
+__device__ __forceinline__ void df_fma(float wh, float wl, float xh, float xl, float &sh,
+                                       float &sl) {
+  const float p = __fmul_rn(wh, xh);
+  const float e = __fmaf_rn(wh, xh, -p);
+  const float c = __fmaf_rn(wh, xl, __fmaf_rn(wl, xh, e));
+  const float t = __fadd_rn(sh, p);
+  const float bp = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  sl = __fadd_rn(sl, __fadd_rn(err, c));
+  sh = t;
+}
+__device__ __forceinline__ void df_renorm(float &sh, float &sl) {
+  const float t = __fadd_rn(sh, sl);
+  sl = __fsub_rn(sl, __fsub_rn(t, sh));
+  sh = t;
+}
+// (sh, sl) += (oh, ol)
+__device__ __forceinline__ void df_add(float &sh, float &sl, float oh, float ol) {
+  const float t = __fadd_rn(sh, oh);
+  const float bp = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(oh, bp));
+  sl = __fadd_rn(sl, __fadd_rn(err, ol));
+  sh = t;
+  df_renorm(sh, sl);
+}
+__device__ __forceinline__ double df_value(float sh, float sl) {
+  return __dadd_rn((double)sh, (double)sl);
+}
+
+// The apply copy's weights when it shares P's structure (nnz_nz == nnz).
+__global__ void k_df_weights(long long n, const double *__restrict__ v, float2 *w, int *flag) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) w[i] = df_weight(__ldg(v + i), flag);
+}
+// An apply's input vector as (hi, lo) pairs; flag set when a value lies
+// outside the window (that apply then runs in FP64).
+__global__ void k_df_split_x(long long n, const double *__restrict__ x, float2 *xs, int *flag) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float hi, lo;
+  if (!df_split(__ldg(x + i), DF_X_EMIN, DF_X_ERANGE, hi, lo)) atomicOr(flag, 1);
+  xs[i] = make_float2(hi, lo);
+}
+
 // The apply copy of P: 8 lanes per row keep the apply_keeps entries in order.
 __global__ void k_nz_fill(long long rows, const int *__restrict__ rp,
                           const int *__restrict__ ci, const double *__restrict__ v,
                           const long long *__restrict__ nzoff, int *nrp, int *nci,
-                          double *nv) {
+                          float2 *nw, int *flag) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long r = t >> 3;
   const int lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
@@ -903,7 +994,7 @@ __global__ void k_nz_fill(long long rows, const int *__restrict__ rp,
       const long long d = o + __popc(mg & ((1u << g8) - 1u));
       if (d < lim) {
         nci[d] = __ldg(ci + p);
-        nv[d] = w;
+        nw[d] = df_weight(w, flag);
       }
     }
     o += __popc(mg);
@@ -930,8 +1021,8 @@ __global__ void k_t_keys(long long rows, const int *__restrict__ rowptr,
 }
 __global__ void k_t_fill(long long nnz, const uint64_t *__restrict__ keys,
                          const uint32_t *__restrict__ perm,
-                         const double *__restrict__ vals, int *tcols,
-                         double *tvals, int *trowptr) {
+                         const float2 *__restrict__ vals, int *tcols,
+                         float2 *tvals, int *trowptr) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nnz) return;
   uint64_t k = keys[i];
@@ -1007,11 +1098,14 @@ __global__ void k_t_chunk_keys(long long ncols, long long nin, const int *__rest
   vals[c] = (uint32_t)c;
 }
 __global__ void k_rowsum(long long rows, const int *__restrict__ rowptr,
-                         const double *__restrict__ vals, double *sum) {
+                         const float2 *__restrict__ vals, double *sum) {
   long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= rows) return;
   double s = 0.0;
-  for (int p = rowptr[r]; p < rowptr[r + 1]; p++) s = __dadd_rn(s, vals[p]);
+  for (int p = rowptr[r]; p < rowptr[r + 1]; p++) {
+    const float2 w = vals[p];
+    s = __dadd_rn(s, __dadd_rn((double)w.x, (double)w.y));
+  }
   sum[r] = s;
 }
 
@@ -1068,6 +1162,9 @@ void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long lon
 // in-order sum of equal columns.
 struct GenInterp {
   int bern;  // Bernstein elements
+  // design -> analysis weights (computeWeights): the Bernstein basis is
+  // evaluated at u whatever the two orders (evalInterp)
+  int topo;
   // eval_bernstein_interp_weights rows (fine order = coarse order + 1):
   // bel[u] are the coarse weights of fine control point u
   double bel[TMRG_MAX_ORDER][TMRG_MAX_ORDER];
@@ -1106,7 +1203,7 @@ __device__ void gen_weights(const InterpCtx &I, const GenInterp &G, int i, int s
     N[s] = 1.0;
     return;
   }
-  if (G.bern && I.fo != co) {
+  if (G.bern && !G.topo && I.fo != co) {
     for (int a = 0; a < co; a++) N[a] = G.bel[i][a];
     return;
   }
@@ -1325,20 +1422,12 @@ static void bernstein_elevation(int mo, int co, double (*N)[TMRG_MAX_ORDER]) {
   }
 }
 
-// Rows of P by the general path (interp_create fills ctx `c` first).
-static void interp_rows_general(Forest &fine, Forest &coarse, Interp &I, InterpCtx &c,
+// Rows of P by the general path: I.rows rows whose (element, local node)
+// are in c.rep, the coarse forest's elements in c; G.bern, G.topo and
+// G.bel set by the caller.
+static void interp_rows_general(Forest &coarse, Interp &I, InterpCtx &c, GenInterp G,
                                 DBuf<int> &err, cudaStream_t s) {
   const long long rows = I.rows;
-  GenInterp G{};
-  G.bern = fine.interp == TMRG_BERNSTEIN_POINTS;
-  if (G.bern) {
-    if (fine.order != coarse.order &&
-        (fine.order - coarse.order != 1 || coarse.order > 5))
-      throw Error(TMRG_ERR_UNSUPPORTED,
-                  "createInterpolation: Bernstein meshes must have equal orders or a "
-                  "fine order one above a coarse order of 2-5");
-    if (fine.order != coarse.order) bernstein_elevation(fine.order, coarse.order, G.bel);
-  }
   G.cnpe = coarse.order * coarse.order * coarse.order;
   G.conn = coarse.econn.p;
   G.dptr = coarse.dep_ptr.p;
@@ -1471,7 +1560,16 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
                         ? 1.0 / (coarse.knots[i] - coarse.knots[j])
                         : 0.0;
   if (general) {
-    interp_rows_general(fine, coarse, I, c, err, s);
+    GenInterp G{};
+    G.bern = fine.interp == TMRG_BERNSTEIN_POINTS;
+    if (G.bern && fine.order != coarse.order) {
+      if (fine.order - coarse.order != 1 || coarse.order > 5)
+        throw Error(TMRG_ERR_UNSUPPORTED,
+                    "createInterpolation: Bernstein meshes must have equal orders or a "
+                    "fine order one above a coarse order of 2-5");
+      bernstein_elevation(fine.order, coarse.order, G.bel);
+    }
+    interp_rows_general(coarse, I, c, G, err, s);
     return;
   }
   // sorted expansion list of every coarse element
@@ -1609,6 +1707,12 @@ void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long lon
   // dropped entries are a good part of P
   I.nnz_nz = (nnz - nonzeros) * 8 >= nnz ? nonzeros : nnz;
   const long long nnz_nz = I.nnz_nz;
+  I.dfflag.alloc(2, s);
+  I.dfflag.zero();
+  I.ap_w.alloc(nnz_nz + 1, s);
+  if (I.nnz_nz == nnz)
+    launch(k_df_weights, blocks_for(nnz, 256), 256, 0, s, nnz, (const double *)I.vals.p,
+           I.ap_w.p, I.dfflag.p);
   if (I.nnz_nz < nnz) {
     DBuf<long long> nzoff;
     if (!keepoff) {
@@ -1620,11 +1724,10 @@ void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long lon
     }
     I.nz_rowptr.alloc(rows + 1, s);
     I.nz_colidx.alloc(nnz_nz + 1, s);
-    I.nz_vals.alloc(nnz_nz + 1, s);
     if (rows == 0) TMRG_CUDA(cudaMemsetAsync(I.nz_rowptr.p, 0, sizeof(int), s));
     launch(k_nz_fill, blocks_for(((rows + 3) / 4) * 32, 256), 256, 0, s, rows,
            (const int *)I.rowptr.p, (const int *)I.colidx.p, (const double *)I.vals.p,
-           keepoff, I.nz_rowptr.p, I.nz_colidx.p, I.nz_vals.p);
+           keepoff, I.nz_rowptr.p, I.nz_colidx.p, I.ap_w.p, I.dfflag.p);
   }
 
   I.perm.alloc(rows + 1, s);
@@ -1634,7 +1737,7 @@ void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long lon
   // P^T by a stable sort on the column (rows stay ascending per column).
   Stage st_t("tmrg_transpose");
   I.t_colidx.alloc(nnz_nz + 1, s);
-  I.t_vals.alloc(nnz_nz + 1, s);
+  I.t_w.alloc(nnz_nz + 1, s);
   I.t_rowptr.alloc(I.cols + 1, s);
   const int cbits = bits_for(I.cols + 1);
   DBuf<uint64_t> tk(nnz_nz, s);
@@ -1643,7 +1746,7 @@ void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long lon
          I.ap_rowptr(), I.ap_colidx(), tk.p, tp.p);
   radix_sort(tk, &tp, nnz_nz, cbits, s);
   launch(k_t_fill, blocks_for(nnz_nz, 256), 256, 0, s, nnz_nz, (const uint64_t *)tk.p,
-         (const uint32_t *)tp.p, I.ap_vals(), I.t_colidx.p, I.t_vals.p,
+         (const uint32_t *)tp.p, (const float2 *)I.ap_w.p, I.t_colidx.p, I.t_w.p,
          I.t_rowptr.p);
   launch(k_t_tail, blocks_for(I.cols + 1, 256), 256, 0, s, I.cols, nnz_nz,
          (const uint64_t *)tk.p, I.t_rowptr.p);
@@ -1752,13 +1855,66 @@ __global__ void k_tw_rows(long long n, InterpCtx I, const int *__restrict__ ax,
   }
 }
 
+// Element centre of every analysis element as (element << 8 | 13): local
+// node 13 of an order-3 element with knots -1, 0, 1.
+__global__ void k_tw_rep(long long n, unsigned long long *rep) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) rep[e] = ((unsigned long long)e << 8) | 13u;
+}
+
 void topo_weights_create(Forest &filter, Forest &analysis, Interp &I) {
   Stage st("tmrg_topo_weights");
-  if (filter.order > IMAX_CO)
-    throw Error(TMRG_ERR_UNSUPPORTED, "topo weights: filter order > 3 is not built");
-  if (filter.interp == TMRG_BERNSTEIN_POINTS)
-    throw Error(TMRG_ERR_UNSUPPORTED, "topo weights: Bernstein filter is not built");
   if (!analysis.have_octs) throw Error(TMRG_ERR_STATE, "topo weights: no analysis octants");
+  if (filter.order > IMAX_CO || filter.interp == TMRG_BERNSTEIN_POINTS) {
+    // filter orders above 3 and Bernstein filters: the general row kernel,
+    // with the analysis element centres as the fine nodes (the centre never
+    // lies on a filter octant face, so every row takes the full order^3
+    // loop of computeWeights)
+    forest_create_nodes(filter);
+    if (filter.conn->nb >= (1 << 26))
+      throw Error(TMRG_ERR_KEY_RANGE, "topo weights: more than 2^26 blocks");
+    cudaStream_t s = analysis.s;
+    TMRG_CUDA(cudaStreamSynchronize(filter.s));
+    I.s = s;
+    I.have_colsum = false;
+    I.colsum.release();
+    I.rows = analysis.n;
+    I.cols = filter.num_owned;
+    DBuf<int> err(1, s);
+    err.zero();
+    DBuf<unsigned long long> rep(analysis.n + 1, s);
+    launch(k_tw_rep, blocks_for(analysis.n, 256), 256, 0, s, analysis.n, rep.p);
+    InterpCtx c{};
+    c.fo = 3;
+    c.fk1[0] = 0.0;
+    c.fk1[1] = 1.0;
+    c.fk1[2] = 2.0;
+    c.co = filter.order;
+    for (int i = 0; i < TMRG_MAX_ORDER; i++) c.ck[i] = filter.knots[i];
+    for (int i = 0; i < TMRG_MAX_ORDER; i++)
+      for (int j = 0; j < TMRG_MAX_ORDER; j++)
+        c.crk[i][j] = (i != j && i < filter.order && j < filter.order)
+                          ? 1.0 / (filter.knots[i] - filter.knots[j])
+                          : 0.0;
+    c.fb = analysis.block.p;
+    c.fx = analysis.x.p;
+    c.fy = analysis.y.p;
+    c.fz = analysis.z.p;
+    c.fl = analysis.level.p;
+    c.cn = filter.n;
+    DBuf<int4> c4(filter.n + 1, s);
+    launch(k_pack_octs, blocks_for(filter.n, 256), 256, 0, s, filter.n,
+           (const int *)filter.block.p, (const int *)filter.x.p, (const int *)filter.y.p,
+           (const int *)filter.z.p, (const int16_t *)filter.level.p, c4.p);
+    c.c4 = c4.p;
+    c.rep = rep.p;
+    c.err = err.p;
+    GenInterp G{};
+    G.bern = filter.interp == TMRG_BERNSTEIN_POINTS;
+    G.topo = 1;
+    interp_rows_general(filter, I, c, G, err, s);
+    return;
+  }
   forest_create_nodes(filter);
   if (filter.conn->nb >= (1 << 26))
     throw Error(TMRG_ERR_KEY_RANGE, "topo weights: more than 2^26 blocks");
@@ -1833,108 +1989,93 @@ static void interp_colsum(Interp &I) {
   if (I.have_colsum) return;
   I.colsum.alloc(I.cols + 1, I.s);
   launch(k_rowsum, blocks_for(I.cols, 256), 256, 0, I.s, I.cols,
-         (const int *)I.t_rowptr.p, (const double *)I.t_vals.p, I.colsum.p);
+         (const int *)I.t_rowptr.p, (const float2 *)I.t_w.p, I.colsum.p);
   I.have_colsum = true;
 }
 
 // ---------------------------------------------------------------------
-// CSR apply over node-major multi-vectors: G lanes per row, lane v
-// accumulates vectors v, v+G, ... in entry order.  With `scale` the
-// result is divided by scale[row] (weight-normalised transpose).
+// CSR applies over node-major multi-vectors, in double-float arithmetic
+// (df_fma; weights and inputs as (hi, lo) pairs), or in FP64 when
+// flags[0] | flags[1] says a weight or an input lies outside the
+// double-float window (a uniform branch; the FP64 branch reads the FP64
+// input and rebuilds each weight as hi + lo).  With `scale` the result is
+// divided by scale[row] (weight-normalised transpose).
+
+// G lanes per row, lane v accumulates vectors v, v+G, ... in entry order
+// (any number of vectors).
 __global__ void __launch_bounds__(256)
-    k_csr_apply(long long rows, int G, int nvec, const int *__restrict__ rowptr,
-                const int *__restrict__ cols, const double *__restrict__ vals,
-                const double *__restrict__ x, double *__restrict__ y,
-                const double *__restrict__ scale) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long r = t / G;
-  int lane = (int)(t - r * G);
+    k_df_apply(long long rows, int G, int nvec, const int *__restrict__ rowptr,
+               const int *__restrict__ cols, const float2 *__restrict__ w,
+               const float2 *__restrict__ xs, const double *__restrict__ x,
+               double *__restrict__ y, const double *__restrict__ scale,
+               const int *__restrict__ flags) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long r = t / G;
+  const int lane = (int)(t - r * G);
   if (r >= rows) return;
-  int p0 = rowptr[r], p1 = rowptr[r + 1];
+  const bool f64 = (__ldg(flags) | __ldg(flags + 1)) != 0;
+  const int p0 = __ldg(rowptr + r), p1 = __ldg(rowptr + r + 1);
   for (int v = lane; v < nvec; v += G) {
     double acc = 0.0;
-    for (int p = p0; p < p1; p++)
-      acc = __fma_rn(__ldg(vals + p), __ldg(x + (long long)__ldg(cols + p) * nvec + v), acc);
+    if (f64) {
+      for (int p = p0; p < p1; p++) {
+        const float2 wv = __ldg(w + p);
+        acc = __fma_rn(__dadd_rn((double)wv.x, (double)wv.y),
+                       __ldg(x + (long long)__ldg(cols + p) * nvec + v), acc);
+      }
+    } else {
+      float sh = 0.0f, sl = 0.0f;
+      int p = p0;
+      for (; p + 4 <= p1; p += 4) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const float2 wv = __ldg(w + p + k);
+          const float2 xv = __ldg(xs + (long long)__ldg(cols + p + k) * nvec + v);
+          df_fma(wv.x, wv.y, xv.x, xv.y, sh, sl);
+        }
+        df_renorm(sh, sl);
+      }
+      for (; p < p1; p++) {
+        const float2 wv = __ldg(w + p);
+        const float2 xv = __ldg(xs + (long long)__ldg(cols + p) * nvec + v);
+        df_fma(wv.x, wv.y, xv.x, xv.y, sh, sl);
+      }
+      df_renorm(sh, sl);
+      acc = df_value(sh, sl);
+    }
     if (scale) {
-      double sc = scale[r];
+      const double sc = scale[r];
       acc = (sc != 0.0) ? __ddiv_rn(acc, sc) : 0.0;
     }
     y[r * nvec + v] = acc;
   }
 }
 
-// Paired-vector form for an even number of vectors: lane l of a row owns
-// vectors 2l, 2l+1 (16-byte loads), LPR lanes per row.  Column indices and
-// weights of 8 entries are loaded ahead of their 8 independent gathers;
-// the accumulation still runs entry by entry in CSR order.
-template <int LPR>
+// Vector pairs: LPR lanes per row, lane v holds PPL consecutive vector
+// pairs (16-byte loads of (hi, lo, hi, lo) each), and NG groups of LPR
+// lanes split a row's entries; the warp runs one trip count with per-entry
+// predicates (a masked entry adds an exact 0), and group sums combine in a
+// fixed tree order.  With `perm` the rows sharing a warp come from the
+// length-ordered permutation, so they have equal trip counts.  Each trip
+// group issues the column, weight and input loads of four entries before
+// their arithmetic, so a warp waits for two memory round trips per four
+// entries; more pairs per lane (PPL) give each wait more arithmetic.
+template <int LPR, int NG, int PPL>
 __global__ void __launch_bounds__(256)
-    k_csr_apply2(long long rows, int nvec2, const int *__restrict__ rowptr,
-                 const int *__restrict__ cols, const double *__restrict__ vals,
-                 const double2 *__restrict__ x, double2 *__restrict__ y,
-                 const double *__restrict__ scale) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long r = t / LPR;
-  int lane = (int)(t & (LPR - 1));
-  if (r >= rows) return;
-  const int p0 = __ldg(rowptr + r), p1 = __ldg(rowptr + r + 1);
-  for (int v = lane; v < nvec2; v += LPR) {
-    double ax = 0.0, ay = 0.0;
-    int p = p0;
-    for (; p + 8 <= p1; p += 8) {
-      int c[8];
-      double w[8];
-      double2 xv[8];
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        c[k] = __ldg(cols + p + k);
-        w[k] = __ldg(vals + p + k);
-      }
-#pragma unroll
-      for (int k = 0; k < 8; k++) xv[k] = __ldg(x + (long long)c[k] * nvec2 + v);
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        ax = __fma_rn(w[k], xv[k].x, ax);
-        ay = __fma_rn(w[k], xv[k].y, ay);
-      }
-    }
-    for (; p < p1; p++) {
-      double2 xv = __ldg(x + (long long)__ldg(cols + p) * nvec2 + v);
-      double w = __ldg(vals + p);
-      ax = __fma_rn(w, xv.x, ax);
-      ay = __fma_rn(w, xv.y, ay);
-    }
-    if (scale) {
-      double sc = scale[r];
-      ax = (sc != 0.0) ? __ddiv_rn(ax, sc) : 0.0;
-      ay = (sc != 0.0) ? __ddiv_rn(ay, sc) : 0.0;
-    }
-    y[r * nvec2 + v] = make_double2(ax, ay);
-  }
-}
-
-// Split-row form: NG groups of LPR lanes share one row (RPW = 32/(LPR*NG)
-// rows per warp); group g takes entries g, g+NG, ...  The warp runs one
-// trip count (the longest row it holds) with per-entry predicates, so no
-// lane diverges: on GB300 the FP64 pipe is the bound and a diverged or
-// half-masked warp instruction costs the pipe as much as a full one.
-// Group partial sums are combined in a fixed tree order.  With `perm` the
-// warp takes rows perm[slot] (rows ordered by length inside windows, so the
-// rows sharing a warp have equal trip counts).
-template <int LPR, int NG>
-__global__ void __launch_bounds__(256)
-    k_csr_apply_split(long long rows, int nvec2, const int *__restrict__ rowptr,
-                      const int *__restrict__ cols, const double *__restrict__ vals,
-                      const double2 *__restrict__ x, double2 *__restrict__ y,
-                      const double *__restrict__ scale, const int *__restrict__ perm) {
+    k_df_apply2(long long rows, int nvec2, const int *__restrict__ rowptr,
+                const int *__restrict__ cols, const float2 *__restrict__ w,
+                const float4 *__restrict__ xs, const double2 *__restrict__ x,
+                double2 *__restrict__ y, const double *__restrict__ scale,
+                const int *__restrict__ perm, const int *__restrict__ flags) {
   constexpr int RPW = 32 / (LPR * NG);
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int sub = lane / (LPR * NG);       // row slot in the warp
-  const int g = (lane / LPR) % NG;         // group in the row
-  const int v = lane % LPR;                // vector pair
+  const int sub = lane / (LPR * NG);  // row slot in the warp
+  const int g = (lane / LPR) % NG;    // group in the row
+  const int v = lane % LPR;           // lane in the group
   const long long slot = warp * RPW + sub;
-  if (warp * RPW >= rows) return;          // uniform per warp
+  if (warp * RPW >= rows) return;     // uniform per warp
+  const bool f64 = (__ldg(flags) | __ldg(flags + 1)) != 0;
   const bool have = slot < rows;
   const long long r = (have && perm) ? (long long)__ldg(perm + slot) : slot;
   const int p0 = have ? __ldg(rowptr + r) : 0;
@@ -1942,65 +2083,195 @@ __global__ void __launch_bounds__(256)
   int trips = (p1 - p0 + NG - 1) / NG;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) trips = max(trips, __shfl_xor_sync(0xffffffffu, trips, o));
-  for (int vb = 0; vb < nvec2; vb += LPR) {
-    const bool act = have && (vb + v < nvec2);
-    double ax = 0.0, ay = 0.0;
-#pragma unroll 4
-    for (int t = 0; t < trips; t++) {
-      int p = p0 + g + t * NG;
-      bool on = act && p < p1;
-      int c = on ? __ldg(cols + p) : 0;
-      double w = on ? __ldg(vals + p) : 0.0;
-      double2 xv = on ? __ldg(x + (long long)c * nvec2 + vb + v) : make_double2(0.0, 0.0);
-      ax = __fma_rn(w, xv.x, ax);
-      ay = __fma_rn(w, xv.y, ay);
-    }
+  for (int vb = 0; vb < nvec2; vb += LPR * PPL) {
+    const int q0 = vb + v * PPL;  // this lane's first pair
+    bool act[PPL];
 #pragma unroll
-    for (int o = (NG / 2) * LPR; o >= LPR; o >>= 1) {
-      ax = __dadd_rn(ax, __shfl_down_sync(0xffffffffu, ax, o));
-      ay = __dadd_rn(ay, __shfl_down_sync(0xffffffffu, ay, o));
-    }
-    if (act && g == 0) {
-      if (scale) {
-        double sc = scale[r];
-        ax = (sc != 0.0) ? __ddiv_rn(ax, sc) : 0.0;
-        ay = (sc != 0.0) ? __ddiv_rn(ay, sc) : 0.0;
+    for (int j = 0; j < PPL; j++) act[j] = have && (q0 + j < nvec2);
+    double ax[PPL], ay[PPL];
+    if (f64) {
+#pragma unroll
+      for (int j = 0; j < PPL; j++) ax[j] = ay[j] = 0.0;
+      for (int t = 0; t < trips; t++) {
+        const int p = p0 + g + t * NG;
+        const bool on = have && p < p1;
+        const int c = on ? __ldg(cols + p) : 0;
+        const float2 wv = on ? __ldg(w + p) : make_float2(0.0f, 0.0f);
+        const double wd = __dadd_rn((double)wv.x, (double)wv.y);
+#pragma unroll
+        for (int j = 0; j < PPL; j++) {
+          const double2 xv = (on && act[j]) ? __ldg(x + (long long)c * nvec2 + q0 + j)
+                                            : make_double2(0.0, 0.0);
+          ax[j] = __fma_rn(wd, xv.x, ax[j]);
+          ay[j] = __fma_rn(wd, xv.y, ay[j]);
+        }
       }
-      y[r * nvec2 + vb + v] = make_double2(ax, ay);
+#pragma unroll
+      for (int o = (NG / 2) * LPR; o >= LPR; o >>= 1)
+#pragma unroll
+        for (int j = 0; j < PPL; j++) {
+          ax[j] = __dadd_rn(ax[j], __shfl_down_sync(0xffffffffu, ax[j], o));
+          ay[j] = __dadd_rn(ay[j], __shfl_down_sync(0xffffffffu, ay[j], o));
+        }
+    } else {
+      float ah[PPL], al[PPL], bh[PPL], bl[PPL];
+#pragma unroll
+      for (int j = 0; j < PPL; j++) ah[j] = al[j] = bh[j] = bl[j] = 0.0f;
+      int t = 0;
+      for (; t + 4 <= trips; t += 4) {
+        int c[4];
+        float2 wv[4];
+        float4 xv[4][PPL];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const int p = p0 + g + (t + k) * NG;
+          const bool on = have && p < p1;
+          c[k] = on ? __ldg(cols + p) : -1;
+          wv[k] = on ? __ldg(w + p) : make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+#pragma unroll
+          for (int j = 0; j < PPL; j++)
+            xv[k][j] = (c[k] >= 0 && act[j]) ? __ldg(xs + (long long)c[k] * nvec2 + q0 + j)
+                                             : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+#pragma unroll
+          for (int j = 0; j < PPL; j++) {
+            df_fma(wv[k].x, wv[k].y, xv[k][j].x, xv[k][j].y, ah[j], al[j]);
+            df_fma(wv[k].x, wv[k].y, xv[k][j].z, xv[k][j].w, bh[j], bl[j]);
+          }
+#pragma unroll
+        for (int j = 0; j < PPL; j++) {
+          df_renorm(ah[j], al[j]);
+          df_renorm(bh[j], bl[j]);
+        }
+      }
+      for (; t < trips; t++) {
+        const int p = p0 + g + t * NG;
+        const bool on = have && p < p1;
+        const int c = on ? __ldg(cols + p) : 0;
+        const float2 wv = on ? __ldg(w + p) : make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int j = 0; j < PPL; j++) {
+          const float4 xv = (on && act[j]) ? __ldg(xs + (long long)c * nvec2 + q0 + j)
+                                           : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+          df_fma(wv.x, wv.y, xv.x, xv.y, ah[j], al[j]);
+          df_fma(wv.x, wv.y, xv.z, xv.w, bh[j], bl[j]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < PPL; j++) {
+        df_renorm(ah[j], al[j]);
+        df_renorm(bh[j], bl[j]);
+      }
+#pragma unroll
+      for (int o = (NG / 2) * LPR; o >= LPR; o >>= 1)
+#pragma unroll
+        for (int j = 0; j < PPL; j++) {
+          const float oah = __shfl_down_sync(0xffffffffu, ah[j], o);
+          const float oal = __shfl_down_sync(0xffffffffu, al[j], o);
+          const float obh = __shfl_down_sync(0xffffffffu, bh[j], o);
+          const float obl = __shfl_down_sync(0xffffffffu, bl[j], o);
+          df_add(ah[j], al[j], oah, oal);
+          df_add(bh[j], bl[j], obh, obl);
+        }
+#pragma unroll
+      for (int j = 0; j < PPL; j++) {
+        ax[j] = df_value(ah[j], al[j]);
+        ay[j] = df_value(bh[j], bl[j]);
+      }
+    }
+    if (g == 0) {
+      const double sc = scale && have ? scale[r] : 1.0;
+#pragma unroll
+      for (int j = 0; j < PPL; j++) {
+        if (!act[j]) continue;
+        double a = ax[j], b = ay[j];
+        if (scale) {
+          a = (sc != 0.0) ? __ddiv_rn(a, sc) : 0.0;
+          b = (sc != 0.0) ? __ddiv_rn(b, sc) : 0.0;
+        }
+        y[r * nvec2 + q0 + j] = make_double2(a, b);
+      }
     }
   }
 }
 
-template <int LPR>
-static void apply2(long long rows, long long nnz, int nvec2, const int *rp,
-                   const int *ci, const double *v, const double *x, double *y,
-                   const double *scale, const int *perm, cudaStream_t s) {
-  // with rows ordered by length: four rows per warp, one group of 8 lanes
-  // each (no partial sums to combine); otherwise long rows take a whole
-  // warp and short rows two rows per warp
-  double avg = rows ? (double)nnz / (double)rows : 0.0;
-  if (LPR == 8) {
-    if (perm)
-      launch((k_csr_apply_split<8, 1>), blocks_for((rows + 3) / 4 * 32, 256), 256, 0, s,
-             rows, nvec2, rp, ci, v, (const double2 *)x, (double2 *)y, scale, perm);
-    else if (avg >= 24)
-      launch((k_csr_apply_split<8, 4>), blocks_for(rows * 32, 256), 256, 0, s, rows,
-             nvec2, rp, ci, v, (const double2 *)x, (double2 *)y, scale,
-             (const int *)nullptr);
+// Launch shapes for vector pairs (the autotuner's candidates): LPR lanes per
+// row holding PPL pairs each, NG groups of LPR lanes splitting a row's
+// entries, 32 / (LPR NG) rows per warp; with `perm` the rows sharing a warp
+// come from the length-ordered permutation.
+struct DF2Shape {
+  int lpr, ng, ppl;
+};
+// 8 or more pairs (16+ vectors)
+constexpr DF2Shape DF2_WIDE[] = {{8, 1, 1}, {8, 2, 1}, {8, 4, 1}, {4, 1, 2}, {2, 1, 4}};
+// fewer pairs: LPR = pairs rounded down to a power of two
+constexpr int DF2_SHAPES_WIDE = 5, DF2_SHAPES_NARROW = 2;
+static void df_apply2(int shape, long long rows, int nvec2, const int *rp, const int *ci,
+                      const float2 *w, const float2 *xs, const double *x, double *y,
+                      const double *scale, const int *perm, const int *flags, cudaStream_t s) {
+  const float4 *x4 = (const float4 *)xs;
+  const double2 *x2 = (const double2 *)x;
+  double2 *y2 = (double2 *)y;
+#define TMRG_DF2(L, N, P)                                                                  \
+  launch((k_df_apply2<L, N, P>),                                                           \
+         blocks_for(((rows + 32 / ((L) * (N)) - 1) / (32 / ((L) * (N)))) * 32, 256), 256, 0, s, \
+         rows, nvec2, rp, ci, w, x4, x2, y2, scale, perm, flags)
+  if (nvec2 >= 8) {
+    switch (shape) {
+      case 0: TMRG_DF2(8, 1, 1); break;
+      case 1: TMRG_DF2(8, 2, 1); break;
+      case 2: TMRG_DF2(8, 4, 1); break;
+      case 3: TMRG_DF2(4, 1, 2); break;
+      default: TMRG_DF2(2, 1, 4);
+    }
+  } else if (nvec2 >= 4) {
+    if (shape == 0)
+      TMRG_DF2(4, 1, 1);
     else
-      launch((k_csr_apply_split<8, 2>), blocks_for((rows + 1) / 2 * 32, 256), 256, 0, s,
-             rows, nvec2, rp, ci, v, (const double2 *)x, (double2 *)y, scale, perm);
-    return;
+      TMRG_DF2(4, 2, 1);
+  } else if (nvec2 >= 2) {
+    if (shape == 0)
+      TMRG_DF2(2, 1, 1);
+    else
+      TMRG_DF2(2, 2, 1);
+  } else {
+    if (shape == 0)
+      TMRG_DF2(1, 1, 1);
+    else
+      TMRG_DF2(1, 2, 1);
   }
-  launch(k_csr_apply2<LPR>, blocks_for(rows * LPR, 256), 256, 0, s, rows, nvec2,
-         rp, ci, v, (const double2 *)x, (double2 *)y, scale);
+#undef TMRG_DF2
+}
+// Size class of an apply: direction, vector pairs (8 = 8 or more), log2 of
+// the rows, mean row length in quarters (capped).
+static TuneKey df_key(int which, long long rows, long long nnz, int nvec2) {
+  int lr = 0;
+  while ((1LL << (lr + 1)) <= rows) lr++;
+  const int q = rows ? (int)std::min(4096LL, (4 * nnz) / rows) : 0;
+  return TuneKey{which == 0 ? TUNE_P : TUNE_PT, std::min(nvec2, 8), lr, q, 0, 0};
+}
+
+// The input as (hi, lo) pairs in pool memory, with its window flag.
+static void df_split_input(Interp &I, const double *x, long long n, DBuf<float2> &xs,
+                           cudaStream_t s) {
+  if (n <= 0) return;
+  prof_bytes(16 * n);
+  launch(k_df_split_x, blocks_for(n, 256), 256, 0, s, n, x, xs.p, I.dfflag.p + 1);
 }
 
 // Transpose apply with the input in host memory: the input rows are copied
-// in TC_CHUNKS pieces on a second stream, and after piece k arrives the
-// output rows whose inputs all lie in pieces <= k are computed (t_perm
-// holds the rows grouped that way), so the copy of the next piece overlaps
-// them.  Same kernel, rows and summation order as the single apply.
+// in TC_CHUNKS pieces on a second stream, and after piece k arrives (and is
+// split into (hi, lo) pairs) the output rows whose inputs all lie in pieces
+// <= k are computed (t_perm holds the rows grouped that way), so the copy
+// of the next piece overlaps them.  Same kernel, rows and summation order
+// as the single apply; a piece with a value outside the double-float window
+// sends that piece's rows and every later piece's rows to FP64 (each row
+// only reads pieces already split, so a row never runs in double-float on
+// an input that was not represented).
 // Returns false (nothing done) where the grouped kernel does not apply.
 bool interp_apply_transpose_staged(Interp &I, int which, const double *xh, double *dx,
                                    double *y, int nvec) {
@@ -2011,6 +2282,9 @@ bool interp_apply_transpose_staged(Interp &I, int which, const double *xh, doubl
   Stage st("tmrg_interp_mult_transpose_staged");
   cudaStream_t s = I.s;
   if (which == 2) interp_colsum(I);
+  const long long nin = I.rows;
+  DBuf<float2> xs(nin * nvec + 1, s);
+  TMRG_CUDA(cudaMemsetAsync(I.dfflag.p + 1, 0, sizeof(int), s));
   cudaStream_t cs;
   TMRG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
   cudaEvent_t ev[TC_CHUNKS + 1];
@@ -2019,22 +2293,28 @@ bool interp_apply_transpose_staged(Interp &I, int which, const double *xh, doubl
   // the copies start after the work already queued on the forest stream
   TMRG_CUDA(cudaEventRecord(ev[TC_CHUNKS], s));
   TMRG_CUDA(cudaStreamWaitEvent(cs, ev[TC_CHUNKS], 0));
-  const long long nin = I.rows;
+  long long r0s[TC_CHUNKS + 1];
+  for (int k = 0; k <= TC_CHUNKS; k++) r0s[k] = (k * nin + TC_CHUNKS - 1) / TC_CHUNKS;
   for (int k = 0; k < TC_CHUNKS; k++) {
-    const long long r0 = (k * nin + TC_CHUNKS - 1) / TC_CHUNKS;
-    const long long r1 = ((k + 1) * nin + TC_CHUNKS - 1) / TC_CHUNKS;
+    const long long r0 = r0s[k], r1 = r0s[k + 1];
     if (r1 > r0)
       TMRG_CUDA(cudaMemcpyAsync(dx + r0 * nvec, xh + r0 * nvec, sizeof(double) * (r1 - r0) * nvec,
                                 cudaMemcpyHostToDevice, cs));
     TMRG_CUDA(cudaEventRecord(ev[k], cs));
   }
   const double *sc = which == 2 ? (const double *)I.colsum.p : (const double *)nullptr;
+  // the tuned shape of the whole apply's class (the pieces are not tuned)
+  const int shape = tune_lookup(df_key(1, I.cols, I.nnz_nz, nvec / 2));
   for (int k = 0; k < TC_CHUNKS; k++) {
     TMRG_CUDA(cudaStreamWaitEvent(s, ev[k], 0));
+    const long long r0 = r0s[k], r1 = r0s[k + 1];
+    if (r1 > r0)
+      launch(k_df_split_x, blocks_for((r1 - r0) * nvec, 256), 256, 0, s, (r1 - r0) * nvec,
+             (const double *)(dx + r0 * nvec), xs.p + r0 * nvec, I.dfflag.p + 1);
     const long long a = I.t_chunk[k], n = I.t_chunk[k + 1] - a;
     if (n > 0)
-      apply2<8>(n, I.nnz_nz, nvec / 2, I.t_rowptr.p, I.t_colidx.p, I.t_vals.p, dx, y, sc,
-                I.t_perm.p + a, s);
+      df_apply2(shape, n, nvec / 2, I.t_rowptr.p, I.t_colidx.p, I.t_w.p, xs.p, dx, y, sc,
+                I.t_perm.p + a, I.dfflag.p, s);
   }
   TMRG_CUDA(cudaStreamSynchronize(s));
   for (int k = 0; k <= TC_CHUNKS; k++) cudaEventDestroy(ev[k]);
@@ -2051,33 +2331,31 @@ void interp_apply(Interp &I, int which, const double *x, double *y, int nvec) {
   const long long nout = (which == 0) ? I.rows : I.cols;
   const int *rp = which == 0 ? I.ap_rowptr() : I.t_rowptr.p;
   const int *ci = which == 0 ? I.ap_colidx() : I.t_colidx.p;
-  const double *v = which == 0 ? I.ap_vals() : I.t_vals.p;
+  const float2 *w = which == 0 ? (const float2 *)I.ap_w.p : (const float2 *)I.t_w.p;
   const double *sc = which == 2 ? (const double *)I.colsum.p : (const double *)nullptr;
   const int *perm = which == 0 ? (const int *)I.perm.p : (const int *)I.t_perm.p;
+  DBuf<float2> xs(nin * nvec + 1, s);
+  TMRG_CUDA(cudaMemsetAsync(I.dfflag.p + 1, 0, sizeof(int), s));
+  df_split_input(I, x, nin * nvec, xs, s);
   // compulsory traffic: 12 B per nonzero entry, the row pointers, one read
-  // of the input and one write of the output vectors
+  // of the input (its (hi, lo) copy) and one write of the output vectors
   const long long bytes = 12 * I.nnz_nz + 4 * (nout + 1) + 8LL * nvec * (nin + nout) +
                           (which == 2 ? 8 * nout : 0);
+  prof_bytes(bytes);
+  prof_flops(2LL * nvec * I.nnz_nz);
   if (nvec % 2 == 0 && ((uintptr_t)x % 16) == 0 && ((uintptr_t)y % 16) == 0) {
-    prof_bytes(bytes);
-    prof_flops(2LL * nvec * I.nnz_nz);
-    int n2 = nvec / 2;
-    if (n2 >= 8)
-      apply2<8>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, perm, s);
-    else if (n2 >= 4)
-      apply2<4>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, perm, s);
-    else if (n2 >= 2)
-      apply2<2>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, perm, s);
-    else
-      apply2<1>(nout, I.nnz_nz, n2, rp, ci, v, x, y, sc, perm, s);
+    const int n2 = nvec / 2;
+    tune_run(df_key(which, nout, I.nnz_nz, n2), n2 >= 8 ? DF2_SHAPES_WIDE : DF2_SHAPES_NARROW,
+             [&](int shape) {
+               df_apply2(shape, nout, n2, rp, ci, w, xs.p, x, y, sc, perm, I.dfflag.p, s);
+             },
+             s);
     return;
   }
   int G = 1;
   while (G < nvec && G < 32) G <<= 1;
-  prof_bytes(bytes);
-  prof_flops(2LL * nvec * I.nnz_nz);
-  launch(k_csr_apply, blocks_for(nout * G, 256), 256, 0, s, nout, G, nvec, rp, ci, v, x,
-         y, sc);
+  launch(k_df_apply, blocks_for(nout * G, 256), 256, 0, s, nout, G, nvec, rp, ci, w,
+         (const float2 *)xs.p, x, y, sc, (const int *)I.dfflag.p);
 }
 
 }  // namespace tmrg

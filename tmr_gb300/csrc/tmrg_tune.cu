@@ -1,0 +1,135 @@
+// Project-written autotuner for the launch shapes of the streaming kernels.
+//
+// A tuned operation presents a few candidate shapes (launch geometry, sparse
+// format) that compute the same result, and a size class (operation kind,
+// vectors, log2 of its rows, rounded mean row length, ...).  The first time
+// a class is seen on a device every candidate is run once to warm up and then
+// timed over TUNE_REPS launches with CUDA events on the operation's stream;
+// the fastest is cached for the process and used for every later operation of
+// the class.  Tuning synchronises the stream, so it happens once per class
+// (in a benchmark, during its warm-up steps).  tmrg_tune_reset() clears the
+// cache and tmrg_tune_report() lists the choices.
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+
+#include "tmrg_internal.h"
+
+namespace tmrg {
+
+namespace {
+constexpr int TUNE_REPS = 3;
+struct Entry {
+  int choice;
+  std::vector<float> ms;  // per candidate, mean of TUNE_REPS launches
+};
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int, int, int>, Entry> g_tune;
+bool g_tune_on = true;
+}  // namespace
+
+int tune_run(const TuneKey &k, int ncand, const std::function<void(int)> &run,
+             cudaStream_t s) {
+  int dev = 0;
+  TMRG_CUDA(cudaGetDevice(&dev));
+  const auto key = std::make_tuple(dev, k.kind, k.a, k.b, k.c, k.d);
+  int choice = -1;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    if (!g_tune_on || ncand <= 1) {
+      choice = ncand <= 1 ? 0 : k.fallback;
+    } else {
+      auto it = g_tune.find(key);
+      if (it != g_tune.end()) choice = it->second.choice;
+    }
+  }
+  if (choice >= 0) {
+    run(choice);
+    return choice;
+  }
+  // not yet tuned: time every candidate on this operation
+  Entry e;
+  e.ms.assign(ncand, 0.0f);
+  cudaEvent_t a, b;
+  TMRG_CUDA(cudaEventCreate(&a));
+  TMRG_CUDA(cudaEventCreate(&b));
+  int best = 0;
+  for (int c = 0; c < ncand; c++) {
+    run(c);  // warm-up
+    TMRG_CUDA(cudaEventRecord(a, s));
+    for (int r = 0; r < TUNE_REPS; r++) run(c);
+    TMRG_CUDA(cudaEventRecord(b, s));
+    TMRG_CUDA(cudaEventSynchronize(b));
+    float ms = 0.0f;
+    TMRG_CUDA(cudaEventElapsedTime(&ms, a, b));
+    e.ms[c] = ms / TUNE_REPS;
+    if (e.ms[c] < e.ms[best]) best = c;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  e.choice = best;
+  // candidates may differ in summation order (rounding): the result left in
+  // place is the chosen candidate's, as on every later call of the class
+  if (best != ncand - 1) run(best);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune.emplace(key, e);
+  return best;
+}
+
+int tune_lookup(const TuneKey &k) {
+  int dev = 0;
+  TMRG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (!g_tune_on) return k.fallback;
+  auto it = g_tune.find(std::make_tuple(dev, k.kind, k.a, k.b, k.c, k.d));
+  return it != g_tune.end() ? it->second.choice : k.fallback;
+}
+
+void tune_set_enabled(bool on) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_on = on;
+}
+
+}  // namespace tmrg
+
+using namespace tmrg;
+
+extern "C" {
+
+int tmrg_tune_reset(int enabled) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune.clear();
+  g_tune_on = enabled != 0;
+  return TMRG_OK;
+}
+
+// JSON list of the tuned classes: [{"device", "kind", "key": [a, b, c, d],
+// "choice", "ms": [...]}, ...]
+int tmrg_tune_report(char *json, int64_t cap) {
+  if (!json || cap <= 0) return TMRG_ERR_ARG;
+  std::string out = "[";
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  bool first = true;
+  for (const auto &kv : g_tune) {
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s{\"device\": %d, \"kind\": %d, \"key\": [%d, %d, %d, %d], "
+                               "\"choice\": %d, \"ms\": [",
+             first ? "" : ", ", std::get<0>(kv.first), std::get<1>(kv.first),
+             std::get<2>(kv.first), std::get<3>(kv.first), std::get<4>(kv.first),
+             std::get<5>(kv.first), kv.second.choice);
+    out += buf;
+    for (size_t c = 0; c < kv.second.ms.size(); c++) {
+      snprintf(buf, sizeof(buf), "%s%.4f", c ? ", " : "", kv.second.ms[c]);
+      out += buf;
+    }
+    out += "]}";
+    first = false;
+  }
+  out += "]";
+  if ((int64_t)out.size() + 1 > cap) return TMRG_ERR_ARG;
+  memcpy(json, out.c_str(), out.size() + 1);
+  return TMRG_OK;
+}
+
+}  // extern "C"
