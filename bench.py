@@ -501,9 +501,15 @@ def run_gpu(args):
         gpu_pipeline(TMR, conn, W, x_fine)
     torch.cuda.synchronize()
     if args.profile_step:
+        # only the steps after the warm-up (where the autotuner made its
+        # choices) are visible to a profiler started with
+        # --profile-from-start off
+        torch.cuda.synchronize()
+        torch.cuda.cudart().cudaProfilerStart()
         for _ in range(args.steps):
             _u, o = gpu_pipeline(TMR, conn, W, x_fine)
         torch.cuda.synchronize()
+        torch.cuda.cudart().cudaProfilerStop()
         if rank == 0:
             print(json.dumps({"workload": W["name"], "hierarchy": hierarchy(o)}), flush=True)
         return

@@ -949,8 +949,35 @@ __device__ __forceinline__ void df_add(float &sh, float &sl, float oh, float ol)
   sh = t;
   df_renorm(sh, sl);
 }
+// sh + sl as a double, from the bits with integer operations (the FP64 pipe
+// carries no work of the applies but rare special cases).  (sh, sl) is
+// normalised, |sl| <= ulp(sh) / 2, so sl lies 24 or more binades below sh:
+// the double of sh plus sl in units of the double ulp at sh's exponent
+// (exact up to a gap of 29 binades, rounded half away from zero beyond;
+// when sh is a power of two and sl has the other sign the result falls
+// into the binade below, whose ulp is half as large).
 __device__ __forceinline__ double df_value(float sh, float sl) {
-  return __dadd_rn((double)sh, (double)sl);
+  const unsigned bh = __float_as_uint(sh), bl = __float_as_uint(sl);
+  const int eh = (int)((bh >> 23) & 0xffu), el = (int)((bl >> 23) & 0xffu);
+  if (eh == 0 || eh == 255 || (el == 0 && (bl & 0x7fffffffu) != 0u) || el == 255)
+    return __dadd_rn((double)sh, (double)sl);  // zeros/subnormal sh, Inf, NaN
+  const unsigned long long hd = ((unsigned long long)(bh & 0x80000000u) << 32) |
+                                ((unsigned long long)(eh + 896) << 52) |
+                                ((unsigned long long)(bh & 0x7fffffu) << 29);
+  if (el == 0) return __longlong_as_double((long long)hd);  // sl = +-0
+  const int g = eh - el;
+  const bool neg = ((bh ^ bl) >> 31) != 0u;
+  const bool pow2 = (bh & 0x7fffffu) == 0u;
+  const int sft = (neg && pow2 ? 30 : 29) - g;
+  const unsigned long long ml = (unsigned long long)((bl & 0x7fffffu) | 0x800000u);
+  unsigned long long d;
+  if (sft >= 0)
+    d = ml << sft;
+  else if (sft > -26)
+    d = (ml + (1ULL << (-sft - 1))) >> (-sft);
+  else
+    d = 0;
+  return __longlong_as_double((long long)(neg ? hd - d : hd + d));
 }
 
 // The apply copy's weights when it shares P's structure (nnz_nz == nnz).
@@ -2057,9 +2084,10 @@ __global__ void __launch_bounds__(256)
 // predicates (a masked entry adds an exact 0), and group sums combine in a
 // fixed tree order.  With `perm` the rows sharing a warp come from the
 // length-ordered permutation, so they have equal trip counts.  Each trip
-// group issues the column, weight and input loads of four entries before
-// their arithmetic, so a warp waits for two memory round trips per four
-// entries; more pairs per lane (PPL) give each wait more arithmetic.
+// group issues the column, weight and input loads of four entries (two
+// with four pairs per lane) before their arithmetic, so a warp waits for
+// two memory round trips per group; more pairs per lane (PPL) give each
+// wait more arithmetic.
 template <int LPR, int NG, int PPL>
 __global__ void __launch_bounds__(256)
     k_df_apply2(long long rows, int nvec2, const int *__restrict__ rowptr,
@@ -2117,26 +2145,28 @@ __global__ void __launch_bounds__(256)
       float ah[PPL], al[PPL], bh[PPL], bl[PPL];
 #pragma unroll
       for (int j = 0; j < PPL; j++) ah[j] = al[j] = bh[j] = bl[j] = 0.0f;
+      // entries per batch: four, two with four pairs per lane (registers)
+      constexpr int UB = PPL >= 4 ? 2 : 4;
       int t = 0;
-      for (; t + 4 <= trips; t += 4) {
-        int c[4];
-        float2 wv[4];
-        float4 xv[4][PPL];
+      for (; t + UB <= trips; t += UB) {
+        int c[UB];
+        float2 wv[UB];
+        float4 xv[UB][PPL];
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
+        for (int k = 0; k < UB; k++) {
           const int p = p0 + g + (t + k) * NG;
           const bool on = have && p < p1;
           c[k] = on ? __ldg(cols + p) : -1;
           wv[k] = on ? __ldg(w + p) : make_float2(0.0f, 0.0f);
         }
 #pragma unroll
-        for (int k = 0; k < 4; k++)
+        for (int k = 0; k < UB; k++)
 #pragma unroll
           for (int j = 0; j < PPL; j++)
             xv[k][j] = (c[k] >= 0 && act[j]) ? __ldg(xs + (long long)c[k] * nvec2 + q0 + j)
                                              : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll
-        for (int k = 0; k < 4; k++)
+        for (int k = 0; k < UB; k++)
 #pragma unroll
           for (int j = 0; j < PPL; j++) {
             df_fma(wv[k].x, wv[k].y, xv[k][j].x, xv[k][j].y, ah[j], al[j]);
