@@ -996,10 +996,13 @@ __global__ void k_df_split_x(long long n, const double *__restrict__ x, float2 *
 }
 
 // The apply copy of P: 8 lanes per row keep the apply_keeps entries in order.
+// Each kept entry also gets its transpose sort record: key = column,
+// value = its position in the copy, erow = its row (k_t_keys' output).
 __global__ void k_nz_fill(long long rows, const int *__restrict__ rp,
                           const int *__restrict__ ci, const double *__restrict__ v,
                           const long long *__restrict__ nzoff, int *nrp, int *nci,
-                          float2 *nw, int *flag) {
+                          float2 *nw, int *flag, uint32_t *tkeys, uint32_t *tvals,
+                          int *erow) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long r = t >> 3;
   const int lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
@@ -1020,8 +1023,12 @@ __global__ void k_nz_fill(long long rows, const int *__restrict__ rp,
     if (nz) {
       const long long d = o + __popc(mg & ((1u << g8) - 1u));
       if (d < lim) {
-        nci[d] = __ldg(ci + p);
+        const int c = __ldg(ci + p);
+        nci[d] = c;
         nw[d] = df_weight(w, flag);
+        tkeys[d] = (uint32_t)c;
+        tvals[d] = (uint32_t)d;
+        erow[d] = (int)r;
       }
     }
     o += __popc(mg);
@@ -1035,36 +1042,37 @@ __global__ void k_nz_fill(long long rows, const int *__restrict__ rp,
 // column (the entries arrive row-major) with a third of the passes a full
 // (column, row) key would take.  8 lanes per row write its entries.
 __global__ void k_t_keys(long long rows, const int *__restrict__ rowptr,
-                         const int *__restrict__ cols, uint64_t *keys,
-                         uint32_t *vals) {
+                         const int *__restrict__ cols, uint32_t *keys, uint32_t *vals,
+                         int *erow) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long r = t >> 3;
   if (r >= rows) return;
   int lane = (int)(t & 7);
   for (int p = rowptr[r] + lane; p < rowptr[r + 1]; p += 8) {
-    keys[p] = ((uint64_t)r << 32) | (uint64_t)(uint32_t)cols[p];
+    keys[p] = (uint32_t)cols[p];
     vals[p] = (uint32_t)p;
+    erow[p] = (int)r;
   }
 }
-__global__ void k_t_fill(long long nnz, const uint64_t *__restrict__ keys,
-                         const uint32_t *__restrict__ perm,
-                         const float2 *__restrict__ vals, int *tcols,
-                         float2 *tvals, int *trowptr) {
+__global__ void k_t_fill(long long nnz, const uint32_t *__restrict__ keys,
+                         const uint32_t *__restrict__ perm, const int *__restrict__ erow,
+                         const float2 *__restrict__ vals, int *tcols, float2 *tvals,
+                         int *trowptr) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nnz) return;
-  uint64_t k = keys[i];
-  tcols[i] = (int)(k >> 32);
-  tvals[i] = vals[perm[i]];
+  const uint32_t p = perm[i];
+  tcols[i] = erow[p];
+  tvals[i] = vals[p];
   // column starts: every column in (previous column, this column] begins here
-  int c = (int)(k & 0xffffffffu);
-  int cprev = (i == 0) ? -1 : (int)(keys[i - 1] & 0xffffffffu);
+  int c = (int)keys[i];
+  int cprev = (i == 0) ? -1 : (int)keys[i - 1];
   for (int j = cprev + 1; j <= c; j++) trowptr[j] = (int)i;
 }
-__global__ void k_t_tail(long long ncols, long long nnz, const uint64_t *__restrict__ keys,
+__global__ void k_t_tail(long long ncols, long long nnz, const uint32_t *__restrict__ keys,
                          int *trowptr) {
   // columns after the last entry's column are empty
   long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  int clast = nnz ? (int)(keys[nnz - 1] & 0xffffffffu) : -1;
+  int clast = nnz ? (int)keys[nnz - 1] : -1;
   if (j > clast && j <= ncols) trowptr[j] = (int)nnz;
 }
 // Rows ordered by length inside windows of LO_WIN rows (one block per
@@ -1510,6 +1518,7 @@ static void interp_rows_general(Forest &coarse, Interp &I, InterpCtx &c, GenInte
 
 // Sorted expansion lists of every element of `coarse` (k_elist_*).
 struct ElemLists {
+  long long total = 0;  // entries of all lists
   DBuf<long long> eoff;
   DBuf<int> lcol;
   DBuf<double> ldw;
@@ -1522,6 +1531,7 @@ static void build_elists(Forest &coarse, ElemLists &L, int *err, cudaStream_t s)
          (const int *)coarse.econn.p, (const int *)coarse.dep_ptr.p, L.eoff.p);
   exclusive_scan<long long>(L.eoff.p, L.eoff.p, coarse.n, s);
   const long long ne = read_scalar(L.eoff.p + coarse.n, s);
+  L.total = ne;
   L.lcol.alloc(ne + 1, s);
   L.ldw.alloc(ne + 1, s);
   L.lkey.alloc(ne + 1, s);
@@ -1658,6 +1668,10 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
     erows.alloc(rows + 1, s);
     launch(k_group_rows, blocks_for(rows, 256), 256, 0, s, rows, (const int *)trow.p,
            (const unsigned *)estart.p, ecur.p, erows.p);
+    // compulsory traffic of the count pass: per row its group slot,
+    // reference, octant and count (34 B); per coarse element its row range,
+    // list offset, octant and kind (29 B) and its list's columns and keys
+    prof_bytes(34 * rows + 29 * coarse.n + 5 * EL.total);
     launch(k_interp_elem<false>, blocks_for(coarse.n, EW_WARPS), EW_WARPS * 32, 0, s, coarse.n,
            c, (const unsigned *)estart.p, (const int *)erows.p, roff.p,
            (const long long *)nullptr, (int *)nullptr, (double *)nullptr);
@@ -1683,9 +1697,6 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   I.vals.alloc(nnz + 1, s);
   DBuf<unsigned long long> nzcount(1, s);
   nzcount.zero();
-  // compulsory traffic: the CSR entries written (12 B each) and per row
-  // its first reference, element, and offset (20 B)
-  prof_bytes(12 * nnz + 20 * rows);
   DBuf<double> uvw;
   DBuf<long long> keep;  // per row: entries the applies keep
   if (states) {
@@ -1694,11 +1705,17 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
     launch(k_uvw_table, blocks_for(nt, 128), 128, 0, s, c, fk1odd, uvw.p);
     c.uvw = uvw.p;
     keep.alloc(rows + 1, s);
+    // compulsory traffic of the fill: the CSR entries written (12 B each);
+    // per row its group slot, reference, octant, offsets and kept count
+    // (46 B); per coarse element 29 B and its list (column, key, dependent
+    // weight: 13 B an entry)
+    prof_bytes(12 * nnz + 46 * rows + 29 * coarse.n + 13 * EL.total);
     launch(k_interp_elem<true>, blocks_for(coarse.n, EW_WARPS), EW_WARPS * 32, 0, s, coarse.n, c,
            (const unsigned *)estart.p, (const int *)erows.p, keep.p,
            (const long long *)roff.p, I.colidx.p, I.vals.p);
   } else {
     c.uvw = nullptr;
+    prof_bytes(12 * nnz + 20 * rows);
     launch(k_interp_rows, blocks_for(rows, IW_WARPS * 32), IW_WARPS * 32, 0, s, rows, c,
            (const int *)trow.p, (const long long *)roff.p, I.colidx.p, I.vals.p, nzcount.p);
   }
@@ -1737,9 +1754,16 @@ void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long lon
   I.dfflag.alloc(2, s);
   I.dfflag.zero();
   I.ap_w.alloc(nnz_nz + 1, s);
-  if (I.nnz_nz == nnz)
+  // transpose sort records (column key, position, row) of every apply entry
+  DBuf<uint32_t> tk(nnz_nz + 1, s);
+  DBuf<uint32_t> tp(nnz_nz + 1, s);
+  DBuf<int> erow(nnz_nz + 1, s);
+  if (I.nnz_nz == nnz) {
     launch(k_df_weights, blocks_for(nnz, 256), 256, 0, s, nnz, (const double *)I.vals.p,
            I.ap_w.p, I.dfflag.p);
+    launch(k_t_keys, blocks_for(rows * 8, 256), 256, 0, s, rows, (const int *)I.rowptr.p,
+           (const int *)I.colidx.p, tk.p, tp.p, erow.p);
+  }
   if (I.nnz_nz < nnz) {
     DBuf<long long> nzoff;
     if (!keepoff) {
@@ -1754,7 +1778,7 @@ void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long lon
     if (rows == 0) TMRG_CUDA(cudaMemsetAsync(I.nz_rowptr.p, 0, sizeof(int), s));
     launch(k_nz_fill, blocks_for(((rows + 3) / 4) * 32, 256), 256, 0, s, rows,
            (const int *)I.rowptr.p, (const int *)I.colidx.p, (const double *)I.vals.p,
-           keepoff, I.nz_rowptr.p, I.nz_colidx.p, I.ap_w.p, I.dfflag.p);
+           keepoff, I.nz_rowptr.p, I.nz_colidx.p, I.ap_w.p, I.dfflag.p, tk.p, tp.p, erow.p);
   }
 
   I.perm.alloc(rows + 1, s);
@@ -1766,17 +1790,17 @@ void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long lon
   I.t_colidx.alloc(nnz_nz + 1, s);
   I.t_w.alloc(nnz_nz + 1, s);
   I.t_rowptr.alloc(I.cols + 1, s);
+  // the column bits only: a stable LSD sort keeps rows ascending per column
   const int cbits = bits_for(I.cols + 1);
-  DBuf<uint64_t> tk(nnz_nz, s);
-  DBuf<uint32_t> tp(nnz_nz, s);
-  launch(k_t_keys, blocks_for(rows * 8, 256), 256, 0, s, rows,
-         I.ap_rowptr(), I.ap_colidx(), tk.p, tp.p);
   radix_sort(tk, &tp, nnz_nz, cbits, s);
-  launch(k_t_fill, blocks_for(nnz_nz, 256), 256, 0, s, nnz_nz, (const uint64_t *)tk.p,
-         (const uint32_t *)tp.p, (const float2 *)I.ap_w.p, I.t_colidx.p, I.t_w.p,
-         I.t_rowptr.p);
+  launch(k_t_fill, blocks_for(nnz_nz, 256), 256, 0, s, nnz_nz, (const uint32_t *)tk.p,
+         (const uint32_t *)tp.p, (const int *)erow.p, (const float2 *)I.ap_w.p, I.t_colidx.p,
+         I.t_w.p, I.t_rowptr.p);
   launch(k_t_tail, blocks_for(I.cols + 1, 256), 256, 0, s, I.cols, nnz_nz,
-         (const uint64_t *)tk.p, I.t_rowptr.p);
+         (const uint32_t *)tk.p, I.t_rowptr.p);
+  tk.release();
+  tp.release();
+  erow.release();
   // P^T rows ordered by the input chunk their last entry needs (stable),
   // then by length inside 4096-row windows of each chunk
   {
@@ -2145,7 +2169,8 @@ __global__ void __launch_bounds__(256)
       float ah[PPL], al[PPL], bh[PPL], bl[PPL];
 #pragma unroll
       for (int j = 0; j < PPL; j++) ah[j] = al[j] = bh[j] = bl[j] = 0.0f;
-      // entries per batch: four, two with four pairs per lane (registers)
+      // entries per batch: four, two with four or more pairs per lane
+      // (registers)
       constexpr int UB = PPL >= 4 ? 2 : 4;
       int t = 0;
       for (; t + UB <= trips; t += UB) {
@@ -2233,13 +2258,9 @@ __global__ void __launch_bounds__(256)
 // row holding PPL pairs each, NG groups of LPR lanes splitting a row's
 // entries, 32 / (LPR NG) rows per warp; with `perm` the rows sharing a warp
 // come from the length-ordered permutation.
-struct DF2Shape {
-  int lpr, ng, ppl;
-};
-// 8 or more pairs (16+ vectors)
-constexpr DF2Shape DF2_WIDE[] = {{8, 1, 1}, {8, 2, 1}, {8, 4, 1}, {4, 1, 2}, {2, 1, 4}};
-// fewer pairs: LPR = pairs rounded down to a power of two
-constexpr int DF2_SHAPES_WIDE = 5, DF2_SHAPES_NARROW = 2;
+// 8 or more pairs (16+ vectors): {8,1,1} {8,2,1} {8,4,1} {4,1,2} {2,1,4}
+// {1,1,8}; fewer pairs: LPR = pairs rounded down to a power of two, NG 1 or 2
+constexpr int DF2_SHAPES_WIDE = 6, DF2_SHAPES_NARROW = 2;
 static void df_apply2(int shape, long long rows, int nvec2, const int *rp, const int *ci,
                       const float2 *w, const float2 *xs, const double *x, double *y,
                       const double *scale, const int *perm, const int *flags, cudaStream_t s) {
@@ -2256,7 +2277,8 @@ static void df_apply2(int shape, long long rows, int nvec2, const int *rp, const
       case 1: TMRG_DF2(8, 2, 1); break;
       case 2: TMRG_DF2(8, 4, 1); break;
       case 3: TMRG_DF2(4, 1, 2); break;
-      default: TMRG_DF2(2, 1, 4);
+      case 4: TMRG_DF2(2, 1, 4); break;
+      default: TMRG_DF2(1, 1, 8);
     }
   } else if (nvec2 >= 4) {
     if (shape == 0)

@@ -274,8 +274,9 @@ constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_ITEMS = 8;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 
-static __global__ void __launch_bounds__(RS_THREADS)
-    k_radix_hist(const uint64_t *__restrict__ kin, long long n, int shift,
+template <typename K>
+__global__ void __launch_bounds__(RS_THREADS)
+    k_radix_hist(const K *__restrict__ kin, long long n, int shift,
                  uint32_t *__restrict__ hist, unsigned nblocks) {
   __shared__ uint32_t wh[RS_WARPS][256];
   for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) (&wh[0][0])[i] = 0;
@@ -298,31 +299,32 @@ static __global__ void __launch_bounds__(RS_THREADS)
 // registers a thread, two blocks per SM).  Ranks inside the tile come from
 // __match_any_sync per warp-row and per-warp digit counters; keys (and
 // values) are staged in tile order of their digit and written out as one
-// contiguous run per digit.
-template <bool VALS>
+// contiguous run per digit.  K: 64-bit keys, or 32-bit keys where the
+// sorted bits fit (half the key traffic of every pass).
+template <typename K, bool VALS>
 __global__ void __launch_bounds__(RS_THREADS, 2)
-    k_radix_scatter(const uint64_t *__restrict__ kin,
-                    const uint32_t *__restrict__ vin, uint64_t *__restrict__ kout,
+    k_radix_scatter(const K *__restrict__ kin,
+                    const uint32_t *__restrict__ vin, K *__restrict__ kout,
                     uint32_t *__restrict__ vout, long long n, int shift,
                     const uint32_t *__restrict__ offs, unsigned nblocks) {
   __shared__ uint16_t wcnt[RS_WARPS][256];
   __shared__ uint32_t tile_off[256];
   __shared__ uint32_t gbase[256];
   __shared__ uint32_t wsum[8];
-  __shared__ uint64_t stage[RS_TILE];
+  __shared__ K stage[RS_TILE];
   __shared__ uint8_t stage_d[RS_TILE];
   for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) (&wcnt[0][0])[i] = 0;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const long long base = (long long)blockIdx.x * RS_TILE + (long long)warp * 32 * RS_ITEMS;
-  uint64_t k[RS_ITEMS];
+  K k[RS_ITEMS];
   uint32_t v[RS_ITEMS];
   uint32_t rank[RS_ITEMS];
 #pragma unroll
   for (int j = 0; j < RS_ITEMS; j++) {
     long long idx = base + j * 32 + lane;
-    k[j] = (idx < n) ? kin[idx] : 0ULL;
+    k[j] = (idx < n) ? kin[idx] : K(0);
     if (VALS) v[j] = (idx < n) ? vin[idx] : 0u;
   }
 #pragma unroll
@@ -405,29 +407,31 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
 // Sorts keys[0..n) (and vals alongside, if given) by bits [0, nbits).
 // Buffers are swapped with internal scratch, so the sorted data ends in
 // `keys`/`vals`.  n < 2^32.
-inline void radix_sort(DBuf<uint64_t> &keys, DBuf<uint32_t> *vals, long long n,
-                       int nbits, cudaStream_t s) {
+template <typename K>
+inline void radix_sort(DBuf<K> &keys, DBuf<uint32_t> *vals, long long n, int nbits,
+                       cudaStream_t s) {
+  static_assert(sizeof(K) == 4 || sizeof(K) == 8, "radix sort keys are 32 or 64 bits");
   if (n <= 1 || nbits <= 0) return;
   if (n >= (1LL << 32)) throw Error(TMRG_ERR_ARG, "radix sort size >= 2^32");
+  if (nbits > 8 * (int)sizeof(K)) throw Error(TMRG_ERR_ARG, "radix sort: bits beyond the key");
   unsigned nb = blocks_for(n, RS_TILE);
-  DBuf<uint64_t> k2(n, s);
+  DBuf<K> k2(n, s);
   DBuf<uint32_t> v2;
   if (vals) v2.alloc(n, s);
   DBuf<uint32_t> hist((size_t)256 * nb + 1, s);
+  constexpr long long KB = sizeof(K);
   for (int shift = 0; shift < nbits; shift += 8) {
-    prof_bytes(8LL * n);
-    launch(k_radix_hist, nb, RS_THREADS, 0, s, (const uint64_t *)keys.p, n,
-           shift, hist.p, nb);
+    prof_bytes(KB * n);
+    launch(k_radix_hist<K>, nb, RS_THREADS, 0, s, (const K *)keys.p, n, shift, hist.p, nb);
     exclusive_scan<uint32_t>(hist.p, hist.p, (long long)256 * nb, s);
-    prof_bytes((vals ? 24LL : 16LL) * n);
+    prof_bytes((vals ? 2 * KB + 8 : 2 * KB) * n);
     if (vals)
-      launch(k_radix_scatter<true>, nb, RS_THREADS, 0, s,
-             (const uint64_t *)keys.p, (const uint32_t *)vals->p, k2.p, v2.p, n,
-             shift, (const uint32_t *)hist.p, nb);
+      launch((k_radix_scatter<K, true>), nb, RS_THREADS, 0, s, (const K *)keys.p,
+             (const uint32_t *)vals->p, k2.p, v2.p, n, shift, (const uint32_t *)hist.p, nb);
     else
-      launch(k_radix_scatter<false>, nb, RS_THREADS, 0, s,
-             (const uint64_t *)keys.p, (const uint32_t *)nullptr, k2.p,
-             (uint32_t *)nullptr, n, shift, (const uint32_t *)hist.p, nb);
+      launch((k_radix_scatter<K, false>), nb, RS_THREADS, 0, s, (const K *)keys.p,
+             (const uint32_t *)nullptr, k2.p, (uint32_t *)nullptr, n, shift,
+             (const uint32_t *)hist.p, nb);
     keys.swap(k2);
     if (vals) vals->swap(v2);
   }
