@@ -2394,7 +2394,6 @@ void interp_apply(Interp &I, int which, const double *x, double *y, int nvec) {
   const long long bytes = 12 * I.nnz_nz + 4 * (nout + 1) + 8LL * nvec * (nin + nout) +
                           (which == 2 ? 8 * nout : 0);
   prof_bytes(bytes);
-  prof_flops(2LL * nvec * I.nnz_nz);
   if (nvec % 2 == 0 && ((uintptr_t)x % 16) == 0 && ((uintptr_t)y % 16) == 0) {
     const int n2 = nvec / 2;
     tune_run(df_key(which, nout, I.nnz_nz, n2), n2 >= 8 ? DF2_SHAPES_WIDE : DF2_SHAPES_NARROW,

@@ -295,6 +295,49 @@ __global__ void __launch_bounds__(RS_THREADS)
   }
 }
 
+// Per digit (one block each): the exclusive scan of its row of tile counts
+// in place (the tile's offset inside the digit's run) and the digit's
+// total.  One launch per pass instead of a multi-level scan of the whole
+// digit-major table.
+constexpr int RS_SCAN_THREADS = 1024;
+static __global__ void __launch_bounds__(RS_SCAN_THREADS)
+    k_radix_scan_digits(uint32_t *__restrict__ hist, unsigned nblocks,
+                        uint32_t *__restrict__ dtot) {
+  __shared__ uint32_t wsum[RS_SCAN_THREADS / 32];
+  uint32_t *row = hist + (size_t)blockIdx.x * nblocks;
+  const unsigned per = (nblocks + RS_SCAN_THREADS - 1) / RS_SCAN_THREADS;
+  const unsigned a = threadIdx.x * per, b = min(nblocks, a + per);
+  uint32_t sum = 0;
+  for (unsigned i = a; i < b; i++) sum += row[i];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = wsum[lane];
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    wsum[lane] = wi - w;
+    if (lane == 31) dtot[blockIdx.x] = wi;
+  }
+  __syncthreads();
+  uint32_t run = wsum[warp] + incl - sum;
+  for (unsigned i = a; i < b; i++) {
+    const uint32_t c = row[i];
+    row[i] = run;
+    run += c;
+  }
+}
+
 // One tile of RS_TILE keys per block, 16 warps x 8 keys per lane (64
 // registers a thread, two blocks per SM).  Ranks inside the tile come from
 // __match_any_sync per warp-row and per-warp digit counters; keys (and
@@ -306,11 +349,13 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
     k_radix_scatter(const K *__restrict__ kin,
                     const uint32_t *__restrict__ vin, K *__restrict__ kout,
                     uint32_t *__restrict__ vout, long long n, int shift,
-                    const uint32_t *__restrict__ offs, unsigned nblocks) {
+                    const uint32_t *__restrict__ offs, const uint32_t *__restrict__ dtot,
+                    unsigned nblocks) {
   __shared__ uint16_t wcnt[RS_WARPS][256];
   __shared__ uint32_t tile_off[256];
   __shared__ uint32_t gbase[256];
   __shared__ uint32_t wsum[8];
+  __shared__ uint32_t dsum[8];
   __shared__ K stage[RS_TILE];
   __shared__ uint8_t stage_d[RS_TILE];
   for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) (&wcnt[0][0])[i] = 0;
@@ -346,7 +391,8 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
   __syncthreads();
   // Per digit (threads 0..255): prefix over warps, then the tile's digit
   // offsets (exclusive scan over digits) and the digit's global base.
-  uint32_t run = 0, incl = 0;
+  // The digit's global base: the exclusive prefix of the digit totals.
+  uint32_t run = 0, incl = 0, dt = 0, dincl = 0;
   if (threadIdx.x < 256) {
     const int d = threadIdx.x;
     for (int w = 0; w < RS_WARPS; w++) {
@@ -355,19 +401,22 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
       run += c;
     }
     incl = run;
+    dt = dtot[d];
+    dincl = dt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
+      uint32_t z = __shfl_up_sync(0xffffffffu, dincl, o);
+      if (lane >= o) incl += y, dincl += z;
     }
-    if (lane == 31) wsum[warp] = incl;
+    if (lane == 31) wsum[warp] = incl, dsum[warp] = dincl;
   }
   __syncthreads();
   if (threadIdx.x < 256) {
-    uint32_t pre = 0;
-    for (int w = 0; w < warp; w++) pre += wsum[w];
+    uint32_t pre = 0, dpre = 0;
+    for (int w = 0; w < warp; w++) pre += wsum[w], dpre += dsum[w];
     tile_off[threadIdx.x] = pre + incl - run;
-    gbase[threadIdx.x] = offs[(size_t)threadIdx.x * nblocks + blockIdx.x];
+    gbase[threadIdx.x] = dpre + dincl - dt + offs[(size_t)threadIdx.x * nblocks + blockIdx.x];
   }
   __syncthreads();
   const long long tile_base = (long long)blockIdx.x * RS_TILE;
@@ -418,20 +467,23 @@ inline void radix_sort(DBuf<K> &keys, DBuf<uint32_t> *vals, long long n, int nbi
   DBuf<K> k2(n, s);
   DBuf<uint32_t> v2;
   if (vals) v2.alloc(n, s);
-  DBuf<uint32_t> hist((size_t)256 * nb + 1, s);
+  DBuf<uint32_t> hist((size_t)256 * nb + 256, s);
+  uint32_t *dtot = hist.p + (size_t)256 * nb;
   constexpr long long KB = sizeof(K);
   for (int shift = 0; shift < nbits; shift += 8) {
     prof_bytes(KB * n);
     launch(k_radix_hist<K>, nb, RS_THREADS, 0, s, (const K *)keys.p, n, shift, hist.p, nb);
-    exclusive_scan<uint32_t>(hist.p, hist.p, (long long)256 * nb, s);
+    prof_bytes(8LL * 256 * nb);
+    launch(k_radix_scan_digits, 256, RS_SCAN_THREADS, 0, s, hist.p, nb, dtot);
     prof_bytes((vals ? 2 * KB + 8 : 2 * KB) * n);
     if (vals)
       launch((k_radix_scatter<K, true>), nb, RS_THREADS, 0, s, (const K *)keys.p,
-             (const uint32_t *)vals->p, k2.p, v2.p, n, shift, (const uint32_t *)hist.p, nb);
+             (const uint32_t *)vals->p, k2.p, v2.p, n, shift, (const uint32_t *)hist.p,
+             (const uint32_t *)dtot, nb);
     else
       launch((k_radix_scatter<K, false>), nb, RS_THREADS, 0, s, (const K *)keys.p,
              (const uint32_t *)nullptr, k2.p, (uint32_t *)nullptr, n, shift,
-             (const uint32_t *)hist.p, nb);
+             (const uint32_t *)hist.p, (const uint32_t *)dtot, nb);
     keys.swap(k2);
     if (vals) vals->swap(v2);
   }
