@@ -136,21 +136,23 @@ def gpu_pipeline(TMR, conn, W, x_fine=None, host=False, prefetched=None, mark=No
         x = prefetched["x"]
         bufs = prefetched["buf"]
         k = 0
-        for I in interps:  # restriction P^T, fine -> coarse (host buffers)
+        for lv, I in enumerate(interps):  # restriction P^T, fine -> coarse
             rows, cols, _ = I.sizes()
             y = bufs[k % 2][: cols * nv]
             I.multTranspose(x[: rows * nv], y)
             h2d += rows * nv * 8
             d2h += cols * nv * 8
             x, k = y, k + 1
-        for I in reversed(interps):  # prolongation P, coarse -> fine
+            mark("P^T L%d" % lv)
+        for lv in reversed(range(len(interps))):  # prolongation P, coarse -> fine
+            I = interps[lv]
             rows, cols, _ = I.sizes()
             y = bufs[k % 2][: rows * nv]
             I.mult(x[: cols * nv], y)
             h2d += cols * nv * 8
             d2h += rows * nv * 8
             x, k = y, k + 1
-        mark("P^T/P applies")
+            mark("P L%d" % lv)
         # the reference getters' borrowed views (TMROctForest::getOctants,
         # getNodeConn): page-locked host copies owned by the forest
         octs = f.getOctants()

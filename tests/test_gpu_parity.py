@@ -103,3 +103,46 @@ def test_device_refinement_draws_match_host(gpu_lib):
                                   (12345, 21, 2, 0.0), (777, 9, 3, 1.0)]:
         d = TMR.random_refinement(n, seed, stream, prob).cpu().numpy()
         np.testing.assert_array_equal(d, W.random_indicator(n, seed, stream, prob))
+
+
+@pytest.mark.gpu
+def test_host_buffer_applies_in_pieces(gpu_lib):
+    # the host-buffer prolongation computed in row pieces whose copies back
+    # overlap the next piece (P with more than 16 x 4096 rows), and the
+    # restriction whose input arrives in pieces: the same values as the
+    # device-pointer applies (same kernel and shape) and the oracle's CSR
+    import ctypes
+
+    import bench
+    import torch
+
+    from oracle.oracle import _lib
+    case = bench.cpu_sample_case()
+    g = pipeline.run_gpu(dict(case, coarse_levels=1))
+    I = g["levels"][0]["I"]
+    rows, ncols, _ = I.sizes()
+    assert rows > 16 * 4096
+    k = 16
+    rng = np.random.default_rng(12)
+    x = rng.standard_normal(ncols * k)
+    xd = torch.tensor(x, device="cuda")
+    yd = torch.empty(rows * k, dtype=torch.float64, device="cuda")
+    I.mult(xd, yd)  # the device apply (tunes the shape of this size class)
+    yh = torch.empty(rows * k, dtype=torch.float64, pin_memory=True).numpy()
+    I.mult(x, yh)
+    np.testing.assert_array_equal(yh, yd.cpu().numpy())
+    y_pageable = np.zeros(rows * k)
+    I.mult(x, y_pageable)
+    np.testing.assert_array_equal(y_pageable, yh)
+    rp, cols, vals = I.getCSR()
+    L = _lib("oracle").lib
+    P_ = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    y_ref = np.zeros(rows * k)
+    L.oo_csr_mult(rows, P_(rp), P_(cols), P_(vals), k, P_(x), P_(y_ref))
+    np.testing.assert_allclose(yh, y_ref, rtol=1e-13, atol=1e-13)
+    xf = rng.standard_normal(rows * k)
+    yt_ref = np.zeros(ncols * k)
+    L.oo_csr_mult_t(rows, ncols, P_(rp), P_(cols), P_(vals), k, P_(xf), P_(yt_ref))
+    yt = np.zeros(ncols * k)
+    I.multTranspose(xf, yt)
+    np.testing.assert_allclose(yt, yt_ref, rtol=1e-13, atol=1e-13)

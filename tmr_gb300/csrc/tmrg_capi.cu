@@ -1021,6 +1021,9 @@ static int interp_host(tmrg_interp *I, int which, const double *x, double *y,
         return;
       }
     }
+    // prolongation: rows computed in pieces, each piece copied back while
+    // the next one computes
+    if (which == 0 && interp_apply_forward_staged(P, x, dx.p, y, nvec)) return;
     TMRG_CUDA(cudaMemcpyAsync(dx.p, x, sizeof(double) * nin,
                               cudaMemcpyHostToDevice, P.s));
     if (ym) {

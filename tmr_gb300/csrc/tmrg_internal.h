@@ -174,6 +174,8 @@ void interp_finish(Interp &I, long long nonzeros, cudaStream_t s,
                    const long long *keepoff = nullptr);
 bool interp_apply_transpose_staged(Interp &I, int which, const double *xh, double *dx,
                                    double *y, int nvec);
+bool interp_apply_forward_staged(Interp &I, const double *xh, double *dx, double *yh,
+                                 int nvec);
 void topo_weights_create(Forest &filter, Forest &analysis, Interp &I);
 void filter_create(Forest &f, double len, double r, int N, Filter &F);
 struct QForest;

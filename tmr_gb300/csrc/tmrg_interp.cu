@@ -2374,6 +2374,59 @@ bool interp_apply_transpose_staged(Interp &I, int which, const double *xh, doubl
   return true;
 }
 
+// Prolongation with the output in host memory: the input (coarse values)
+// is copied first, then the rows are computed in FC_CHUNKS pieces of whole
+// 4096-row windows (the length-ordered permutation stays inside a window,
+// so a piece of slots is exactly a piece of rows) into device memory, and
+// each piece is copied to the host on a second stream while the next piece
+// computes.  One bulk copy per piece runs the host link at its copy rate
+// (the kernel writing host memory directly ran it at less than half).
+// Same kernel, rows and summation order as the single apply.  Returns
+// false (nothing done) where the pair kernel does not apply.
+constexpr int FC_CHUNKS = 16;
+bool interp_apply_forward_staged(Interp &I, const double *xh, double *dx, double *yh,
+                                 int nvec) {
+  if (nvec % 2 != 0 || ((uintptr_t)dx % 16) != 0 || I.rows < (long long)LO_WIN * FC_CHUNKS)
+    return false;
+  Stage st("tmrg_interp_mult_staged");
+  cudaStream_t s = I.s;
+  const long long nin = I.cols, rows = I.rows;
+  TMRG_CUDA(cudaMemcpyAsync(dx, xh, sizeof(double) * nin * nvec, cudaMemcpyHostToDevice, s));
+  DBuf<float2> xs(nin * nvec + 1, s);
+  TMRG_CUDA(cudaMemsetAsync(I.dfflag.p + 1, 0, sizeof(int), s));
+  df_split_input(I, dx, nin * nvec, xs, s);
+  DBuf<double> dy(rows * nvec + 2, s);
+  double *y = dy.p;
+  if ((uintptr_t)y % 16) y++;
+  const int n2 = nvec / 2;
+  const int shape = tune_lookup(df_key(0, rows, I.nnz_nz, n2));
+  cudaStream_t cs;
+  TMRG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaEvent_t ev[FC_CHUNKS];
+  for (int k = 0; k < FC_CHUNKS; k++)
+    TMRG_CUDA(cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming));
+  const long long nwin = (rows + LO_WIN - 1) / LO_WIN;
+  for (int k = 0; k < FC_CHUNKS; k++) {
+    const long long r0 = std::min(rows, (nwin * k / FC_CHUNKS) * LO_WIN);
+    const long long r1 = std::min(rows, (nwin * (k + 1) / FC_CHUNKS) * LO_WIN);
+    if (r1 > r0) {
+      prof_bytes(12 * I.nnz_nz * (r1 - r0) / rows + 4 * (r1 - r0) + 8LL * nvec * (r1 - r0));
+      df_apply2(shape, r1 - r0, n2, I.ap_rowptr(), I.ap_colidx(), I.ap_w.p, xs.p, dx, y,
+                nullptr, I.perm.p + r0, I.dfflag.p, s);
+    }
+    TMRG_CUDA(cudaEventRecord(ev[k], s));
+    TMRG_CUDA(cudaStreamWaitEvent(cs, ev[k], 0));
+    if (r1 > r0)
+      TMRG_CUDA(cudaMemcpyAsync(yh + r0 * nvec, y + r0 * nvec, sizeof(double) * (r1 - r0) * nvec,
+                                cudaMemcpyDeviceToHost, cs));
+  }
+  TMRG_CUDA(cudaStreamSynchronize(cs));
+  TMRG_CUDA(cudaStreamSynchronize(s));
+  for (int k = 0; k < FC_CHUNKS; k++) cudaEventDestroy(ev[k]);
+  cudaStreamDestroy(cs);
+  return true;
+}
+
 void interp_apply(Interp &I, int which, const double *x, double *y, int nvec) {
   Stage st(which == 0 ? "tmrg_interp_mult" : "tmrg_interp_mult_transpose");
   if (nvec <= 0) throw Error(TMRG_ERR_ARG, "interp apply: nvec <= 0");
