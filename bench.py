@@ -317,7 +317,8 @@ def pipeline_roofline(TMR, conn, W, x_fine, peak):
                            if stages.get(k) else None} for k in b}}
 
 
-TUNE_KINDS = {1: "P apply", 2: "P^T apply", 3: "filter vpn3 FP32", 4: "filter vpn3 FP64"}
+TUNE_KINDS = {1: "P apply", 2: "P^T apply", 3: "filter vpn3 FP32", 4: "filter vpn3 FP64",
+              5: "radix scatter (key bytes, values, log2 n)"}
 
 
 def autotune_report(TMR):
@@ -529,18 +530,18 @@ def run_gpu(args):
     barrier()
     launches0 = TMR.kernel_launch_count()
     syncs0 = TMR.host_sync_count()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev0, ev1 = evs[0], evs[-1]
     ev0.record()
     tot_units = 0
     last = None
-    for _ in range(args.steps):
+    for i in range(args.steps):
         # the previous step's hierarchy is released before the next one is
         # built (its destruction stays inside the timed region)
         last = None
         u, last = gpu_pipeline(TMR, conn, W, x_fine)
         tot_units += u
-    ev1.record()
+        evs[i + 1].record()
     barrier()
     clocks = clk.stop()
     launches = TMR.kernel_launch_count() - launches0
@@ -553,6 +554,7 @@ def run_gpu(args):
         return float(t.item())
 
     value, ms = aggregate(ev0.elapsed_time(ev1), tot_units, world, allreduce_max)
+    ms_each = [round(evs[i].elapsed_time(evs[i + 1]), 2) for i in range(args.steps)]
 
     # e2e through the host-buffer C ABI
     e2e = None
@@ -617,7 +619,8 @@ def run_gpu(args):
         line = {
             "metric": "balanced+numbered octants/s", "value": value, "unit": "octants/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": ms / args.steps, "ms_each": ms_each,
+            "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic (seeded)",
             "config": {"workload": W["name"], "trees": W["nx"] * W["ny"] * W["nz"],
                        "octants_per_step": tot_units // args.steps,

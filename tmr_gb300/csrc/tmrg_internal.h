@@ -13,18 +13,8 @@
 
 namespace tmrg {
 
-// Autotuner (tmrg_tune.cu): a size class of an operation with `ncand`
-// candidate shapes.  tune_run runs the operation with the class's chosen
-// candidate, timing all of them the first time the class is seen on the
-// device; tune_lookup returns the cached choice (or the fallback).
-struct TuneKey {
-  int kind, a, b, c, d;
-  int fallback;
-};
-enum TuneKind { TUNE_P = 1, TUNE_PT = 2, TUNE_FILTER3_F32 = 3, TUNE_FILTER3_F64 = 4 };
-int tune_run(const TuneKey &k, int ncand, const std::function<void(int)> &run,
-             cudaStream_t s);
-int tune_lookup(const TuneKey &k);
+// The autotuner's interface (TuneKey, tune_run, tune_lookup) is declared
+// in tmrg_prims.cuh, beside the radix sort that uses it.
 
 // Device view of the block connectivity tables.  CSR entries hold
 // 8*block+corner, 12*block+edge, 6*block+face; the first entry of each

@@ -660,8 +660,12 @@ __global__ void __launch_bounds__(IW_WARPS * 32)
 // dependent weight, as in k_interp_rows), and the in-order sums of equal
 // columns.  Same entries, same arithmetic, same bits as k_interp_rows.
 
-// Pass 1: each row's element (findEnclosing) and the rows per element.
-__global__ void k_interp_find(long long rows, InterpCtx I, int *trow, unsigned *ecnt) {
+// Pass 1: each row's element (findEnclosing), the rows per element, and
+// the row's box mask and direction states packed as bm | state << 32
+// (state = su*49 + sv*7 + sw, or 0xffff where the states do not cover the
+// row: its element is too coarse, and the host takes the per-row kernel).
+__global__ void k_interp_find(long long rows, InterpCtx I, int *trow, unsigned *ecnt,
+                              unsigned long long *rinfo) {
   long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= rows) return;
   const unsigned long long rr = I.rep[row];
@@ -675,27 +679,58 @@ __global__ void k_interp_find(long long rows, InterpCtx I, int *trow, unsigned *
     return;
   }
   atomicAdd(ecnt + t, 1u);
-  const int gap = node.level - (__ldg(I.c4 + t).x >> 26);
-  if ((gap > 1 || (gap < 0 && I.fodd)) && *(volatile int *)I.wide == 0) atomicOr(I.wide, 1);
+  const int4 cq = __ldg(I.c4 + t);
+  const int cl = cq.x >> 26;
+  const int gap = node.level - cl;
+  const bool wide = gap > 1 || (gap < 0 && I.fodd);
+  if (wide && *(volatile int *)I.wide == 0) atomicOr(I.wide, 1);
+  const int mo = I.fo, co = I.co;
+  const int32_t h = side_of(node.level), hc = side_of(cl);
+  const int i = info % mo, j = (info % (mo * mo)) / mo, k = info / (mo * mo);
+  const int rx = dir_range(i, mo, co, node.x, h, cq.y, hc);
+  const int ry = dir_range(j, mo, co, node.y, h, cq.z, hc);
+  const int rz = dir_range(k, mo, co, node.z, h, cq.w, hc);
+  unsigned sidx = 0xffffu;
+  if (!wide) {
+    const int su = dir_state(I, i, rx, node.x, h, node.level, cq.y, hc, cl);
+    const int sv = dir_state(I, j, ry, node.y, h, node.level, cq.z, hc, cl);
+    const int sw = dir_state(I, k, rz, node.z, h, node.level, cq.w, hc, cl);
+    if ((unsigned)su < UVW_DIR && (unsigned)sv < UVW_DIR && (unsigned)sw < UVW_DIR)
+      sidx = (unsigned)((su * UVW_DIR + sv) * UVW_DIR + sw);
+  }
+  rinfo[row] = (unsigned long long)box_mask(co, rx, ry, rz) |
+               ((unsigned long long)sidx << 32);
 }
 // Rows by element: erows[estart[t] ..] lists the rows of element t (in no
-// particular order: each row's output place is fixed by its offset).
+// particular order: each row's output place is fixed by its offset), with
+// their packed box mask and states beside them in einfo.
 __global__ void k_group_rows(long long rows, const int *__restrict__ trow,
-                             const unsigned *__restrict__ estart, unsigned *ecur, int *erows) {
+                             const unsigned long long *__restrict__ rinfo,
+                             const unsigned *__restrict__ estart, unsigned *ecur, int *erows,
+                             unsigned long long *einfo) {
   long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= rows) return;
   const int t = trow[row];
   if (t < 0) return;
-  erows[estart[t] + atomicAdd(ecur + t, 1u)] = (int)row;
+  const unsigned pos = estart[t] + atomicAdd(ecur + t, 1u);
+  erows[pos] = (int)row;
+  einfo[pos] = rinfo[row];
 }
 // Passes 2 (FILL = false: each row's merged length in cnt) and 3 (FILL:
 // the rows at roff, each row's apply_keeps entries counted in cnt).  One warp per
-// coarse element, its rows 32 at a time, lane r <-> row r; the lanes walk
-// the element's sorted list in step (broadcast shared-memory reads):
+// coarse element, its rows 32 at a time, lane r <-> row r for the set-up
+// (box mask, direction states, CSR offsets).
+// An element of kind 0 (co^3 distinct independent nodes: each entry's
+// weight is the table value itself) emits its rows one after another, lane
+// j <-> list entry j: the in-box lanes write consecutive CSR slots, so a
+// row is one contiguous store, with no FP64 instruction.
+// Other elements walk the sorted list in step (broadcast shared-memory
+// reads), lane r <-> row r:
 //   stage: the in-box (row, entry) pairs of list entries k0.. in list
 //     order, with each entry's rows mask and first pair;
 //   weights: the pairs' products on full warps (table value times the
-//     dependent weight, as in k_interp_rows);
+//     dependent weight, as in k_interp_rows; a masked FP64 warp
+//     instruction costs the GB300 FP64 pipe as much as a full one);
 //   merge: lane r takes its pairs in list order and sums equal columns in
 //     that order; an add is issued only at list entries that repeat the
 //     previous entry's column (the list is sorted, so no other entry can
@@ -705,8 +740,9 @@ constexpr int EW_CAP = 256;  // staged pairs per warp
 template <bool FILL>
 __global__ void __launch_bounds__(EW_WARPS * 32)
     k_interp_elem(long long n, InterpCtx I, const unsigned *__restrict__ estart,
-                  const int *__restrict__ erows, long long *cnt,
-                  const long long *__restrict__ roff, int *cols, double *vals) {
+                  const int *__restrict__ erows, const unsigned long long *__restrict__ einfo,
+                  long long *cnt, const long long *__restrict__ roff, int *cols,
+                  double *vals) {
   constexpr int FW = FILL ? EW_WARPS : 1;
   __shared__ int s_col[EW_WARPS][IMAX_E];
   __shared__ uint8_t s_key[EW_WARPS][IMAX_E];
@@ -732,10 +768,7 @@ __global__ void __launch_bounds__(EW_WARPS * 32)
   }
   const double *ldw = I.ldw + eo;  // the element's dependent weights (L1)
   const int fw = FILL ? warp : 0;
-  const int4 cq = __ldg(I.c4 + t);
-  const int cl = cq.x >> 26;
-  const int32_t hc = side_of(cl);
-  const int mo = I.fo, co = I.co, cn3 = co * co * co;
+  const int co = I.co, cn3 = co * co * co;
   for (unsigned b0 = r0; b0 < r1; b0 += 32) {
     const int nb = (int)min(32u, r1 - b0);
     const bool mine = lane < nb;
@@ -746,30 +779,20 @@ __global__ void __launch_bounds__(EW_WARPS * 32)
     __syncwarp();
     if (mine) {
       row = erows[b0 + lane];
-      const unsigned long long rr = I.rep[row];
-      const long long e = (long long)(rr >> 8);
-      const int info = (int)(rr & 255u);
-      const int32_t nx = I.fx[e], ny = I.fy[e], nz = I.fz[e];
-      const int lf = I.fl[e];
-      const int32_t h = side_of(lf);
-      const int i = info % mo, j = (info % (mo * mo)) / mo, k = info / (mo * mo);
-      const int rx = dir_range(i, mo, co, nx, h, cq.y, hc);
-      const int ry = dir_range(j, mo, co, ny, h, cq.z, hc);
-      const int rz = dir_range(k, mo, co, nz, h, cq.w, hc);
-      bm = box_mask(co, rx, ry, rz);
+      const unsigned long long inf = einfo[b0 + lane];
+      bm = (unsigned)inf;
       if (FILL) {
-        int su = dir_state(I, i, rx, nx, h, lf, cq.y, hc, cl);
-        int sv = dir_state(I, j, ry, ny, h, lf, cq.z, hc, cl);
-        int sw = dir_state(I, k, rz, nz, h, lf, cq.w, hc, cl);
-        if ((unsigned)su >= UVW_DIR || (unsigned)sv >= UVW_DIR || (unsigned)sw >= UVW_DIR) {
+        unsigned sidx = (unsigned)(inf >> 32);
+        if (sidx >= (unsigned)UVW_STATES) {
           atomicExch(I.err, 4);  // outside the table: reported, never read
-          su = sv = sw = 0;
+          sidx = 0;
         }
-        s_st[fw][lane] = (su * UVW_DIR * UVW_DIR + sv * UVW_DIR + sw) * cn3;
+        s_st[fw][lane] = (int)sidx * cn3;
         out = roff[row];
         lim = roff[row + 1];
       }
     }
+    __syncwarp();
     if constexpr (!FILL) {
       long long ne = 0;
       if (kind == 0) {
@@ -785,6 +808,34 @@ __global__ void __launch_bounds__(EW_WARPS * 32)
         }
       }
       if (mine) cnt[row] = ne;
+    } else if (kind == 0) {
+      // E == co^3 <= 27: one list entry per lane
+      const int ekey = lane < E ? (s_key[warp][lane] & 31) : 0;
+      const int ecol = lane < E ? s_col[warp][lane] : 0;
+      for (int r = 0; r < nb; r++) {
+        const unsigned rbm = __shfl_sync(0xffffffffu, bm, r);
+        const int rs = s_st[fw][r];
+        const long long o = __shfl_sync(0xffffffffu, out, r);
+        const long long rlim = __shfl_sync(0xffffffffu, lim, r);
+        const bool in = lane < E && ((rbm >> ekey) & 1u);
+        const unsigned m = __ballot_sync(0xffffffffu, in);
+        double v = 0.0;
+        if (in) {
+          v = __ldg(I.uvw + rs + ekey);
+          const long long p = o + __popc(m & lt);
+          if (p < rlim) {
+            cols[p] = ecol;
+            vals[p] = v;
+          } else {
+            atomicExch(I.err, 3);
+          }
+        }
+        const int kept = __popc(__ballot_sync(0xffffffffu, in && apply_keeps(v)));
+        if (lane == r) {
+          if (o + __popc(m) != rlim) atomicExch(I.err, 3);
+          cnt[row] = kept;
+        }
+      }
     } else {
       int pcol = -1;
       double acc = 0.0;
@@ -1651,6 +1702,7 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   DBuf<long long> roff(rows + 1, s);
   DBuf<unsigned> estart;
   DBuf<int> erows;
+  DBuf<unsigned long long> rinfo, einfo;  // per row: box mask | states << 32
   // a warp per coarse element pays off when the elements enclose enough
   // rows to fill it (order 3: about 29 per element; order 2: about 8, where
   // the per-row kernel is faster)
@@ -1658,7 +1710,9 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   if (states) {
     estart.alloc(coarse.n + 1, s);
     estart.zero();
-    launch(k_interp_find, blocks_for(rows, 128), 128, 0, s, rows, c, trow.p, estart.p);
+    rinfo.alloc(rows + 1, s);
+    launch(k_interp_find, blocks_for(rows, 128), 128, 0, s, rows, c, trow.p, estart.p,
+           rinfo.p);
     states = read_scalar(wide.p, s) == 0 && read_scalar(err.p, s) == 0;
   }
   if (states) {
@@ -1666,15 +1720,19 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
     DBuf<unsigned> ecur(coarse.n + 1, s);
     ecur.zero();
     erows.alloc(rows + 1, s);
+    einfo.alloc(rows + 1, s);
     launch(k_group_rows, blocks_for(rows, 256), 256, 0, s, rows, (const int *)trow.p,
-           (const unsigned *)estart.p, ecur.p, erows.p);
-    // compulsory traffic of the count pass: per row its group slot,
-    // reference, octant and count (34 B); per coarse element its row range,
-    // list offset, octant and kind (29 B) and its list's columns and keys
-    prof_bytes(34 * rows + 29 * coarse.n + 5 * EL.total);
+           (const unsigned long long *)rinfo.p, (const unsigned *)estart.p, ecur.p, erows.p,
+           einfo.p);
+    rinfo.release();
+    // compulsory traffic of the count pass: per row its group slot, box
+    // and count (20 B); per coarse element its row range, list offset and
+    // kind (13 B) and its list's columns and keys
+    prof_bytes(20 * rows + 13 * coarse.n + 5 * EL.total);
     launch(k_interp_elem<false>, blocks_for(coarse.n, EW_WARPS), EW_WARPS * 32, 0, s, coarse.n,
-           c, (const unsigned *)estart.p, (const int *)erows.p, roff.p,
-           (const long long *)nullptr, (int *)nullptr, (double *)nullptr);
+           c, (const unsigned *)estart.p, (const int *)erows.p,
+           (const unsigned long long *)einfo.p, roff.p, (const long long *)nullptr,
+           (int *)nullptr, (double *)nullptr);
   } else {
     launch(k_interp_count, blocks_for(rows, 128), 128, 0, s, rows, c, trow.p, roff.p);
   }
@@ -1706,13 +1764,14 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
     c.uvw = uvw.p;
     keep.alloc(rows + 1, s);
     // compulsory traffic of the fill: the CSR entries written (12 B each);
-    // per row its group slot, reference, octant, offsets and kept count
-    // (46 B); per coarse element 29 B and its list (column, key, dependent
+    // per row its group slot, box and states, offsets and kept count
+    // (36 B); per coarse element 13 B and its list (column, key, dependent
     // weight: 13 B an entry)
-    prof_bytes(12 * nnz + 46 * rows + 29 * coarse.n + 13 * EL.total);
+    prof_bytes(12 * nnz + 36 * rows + 13 * coarse.n + 13 * EL.total);
     launch(k_interp_elem<true>, blocks_for(coarse.n, EW_WARPS), EW_WARPS * 32, 0, s, coarse.n, c,
-           (const unsigned *)estart.p, (const int *)erows.p, keep.p,
-           (const long long *)roff.p, I.colidx.p, I.vals.p);
+           (const unsigned *)estart.p, (const int *)erows.p,
+           (const unsigned long long *)einfo.p, keep.p, (const long long *)roff.p, I.colidx.p,
+           I.vals.p);
   } else {
     c.uvw = nullptr;
     prof_bytes(12 * nnz + 20 * rows);
@@ -1723,6 +1782,7 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
   roff.release();
   estart.release();
   erows.release();
+  einfo.release();
   EL = ElemLists();
   c4.release();
   rep.release();

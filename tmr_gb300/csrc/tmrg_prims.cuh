@@ -9,6 +9,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
+#include <functional>
 #include <utility>
 
 #include "tmrg_common.cuh"
@@ -338,42 +339,46 @@ static __global__ void __launch_bounds__(RS_SCAN_THREADS)
   }
 }
 
-// One tile of RS_TILE keys per block, 16 warps x 8 keys per lane (64
-// registers a thread, two blocks per SM).  Ranks inside the tile come from
-// __match_any_sync per warp-row and per-warp digit counters; keys (and
-// values) are staged in tile order of their digit and written out as one
-// contiguous run per digit.  K: 64-bit keys, or 32-bit keys where the
-// sorted bits fit (half the key traffic of every pass).
-template <typename K, bool VALS>
-__global__ void __launch_bounds__(RS_THREADS, 2)
+// One tile of RS_TILE keys per block of THREADS threads, RS_TILE / THREADS
+// keys per lane, at least MINB blocks per SM (the launch shapes the
+// autotuner picks from: 512 x 8 keys at 2 or 3 blocks, 1024 x 4 keys at 2).
+// Ranks inside the tile come from __match_any_sync per warp-row and
+// per-warp digit counters; keys (and values) are staged in tile order of
+// their digit and written out as one contiguous run per digit.  K: 64-bit
+// keys, or 32-bit keys where the sorted bits fit (half the key traffic of
+// every pass).
+template <typename K, bool VALS, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB)
     k_radix_scatter(const K *__restrict__ kin,
                     const uint32_t *__restrict__ vin, K *__restrict__ kout,
                     uint32_t *__restrict__ vout, long long n, int shift,
                     const uint32_t *__restrict__ offs, const uint32_t *__restrict__ dtot,
                     unsigned nblocks) {
-  __shared__ uint16_t wcnt[RS_WARPS][256];
+  constexpr int NW = THREADS / 32, ITEMS = RS_TILE / THREADS;
+  static_assert(THREADS >= 256 && RS_TILE % THREADS == 0, "scatter shape");
+  __shared__ uint16_t wcnt[NW][256];
   __shared__ uint32_t tile_off[256];
   __shared__ uint32_t gbase[256];
   __shared__ uint32_t wsum[8];
   __shared__ uint32_t dsum[8];
   __shared__ K stage[RS_TILE];
   __shared__ uint8_t stage_d[RS_TILE];
-  for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) (&wcnt[0][0])[i] = 0;
+  for (int i = threadIdx.x; i < NW * 256; i += THREADS) (&wcnt[0][0])[i] = 0;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  const long long base = (long long)blockIdx.x * RS_TILE + (long long)warp * 32 * RS_ITEMS;
-  K k[RS_ITEMS];
-  uint32_t v[RS_ITEMS];
-  uint32_t rank[RS_ITEMS];
+  const long long base = (long long)blockIdx.x * RS_TILE + (long long)warp * 32 * ITEMS;
+  K k[ITEMS];
+  uint32_t v[ITEMS];
+  uint32_t rank[ITEMS];
 #pragma unroll
-  for (int j = 0; j < RS_ITEMS; j++) {
+  for (int j = 0; j < ITEMS; j++) {
     long long idx = base + j * 32 + lane;
     k[j] = (idx < n) ? kin[idx] : K(0);
     if (VALS) v[j] = (idx < n) ? vin[idx] : 0u;
   }
 #pragma unroll
-  for (int j = 0; j < RS_ITEMS; j++) {
+  for (int j = 0; j < ITEMS; j++) {
     long long idx = base + j * 32 + lane;
     bool ok = idx < n;
     uint32_t d = ok ? ((uint32_t)(k[j] >> shift) & 0xFFu) : (256u + lane);
@@ -395,7 +400,7 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
   uint32_t run = 0, incl = 0, dt = 0, dincl = 0;
   if (threadIdx.x < 256) {
     const int d = threadIdx.x;
-    for (int w = 0; w < RS_WARPS; w++) {
+    for (int w = 0; w < NW; w++) {
       uint32_t c = wcnt[w][d];
       wcnt[w][d] = (uint16_t)run;
       run += c;
@@ -422,7 +427,7 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
   const long long tile_base = (long long)blockIdx.x * RS_TILE;
   const int cnt = (int)min((long long)RS_TILE, n - tile_base);
 #pragma unroll
-  for (int j = 0; j < RS_ITEMS; j++) {
+  for (int j = 0; j < ITEMS; j++) {
     long long idx = base + j * 32 + lane;
     if (idx < n) {
       uint32_t d = (uint32_t)(k[j] >> shift) & 0xFFu;
@@ -433,7 +438,7 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
     }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < cnt; i += RS_THREADS) {
+  for (int i = threadIdx.x; i < cnt; i += THREADS) {
     uint32_t d = stage_d[i];
     kout[gbase[d] + (i - tile_off[d])] = stage[i];
   }
@@ -441,15 +446,53 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
     __syncthreads();
     uint32_t *vstage = reinterpret_cast<uint32_t *>(stage);
 #pragma unroll
-    for (int j = 0; j < RS_ITEMS; j++) {
+    for (int j = 0; j < ITEMS; j++) {
       long long idx = base + j * 32 + lane;
       if (idx < n) vstage[rank[j]] = v[j];
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < cnt; i += RS_THREADS) {
+    for (int i = threadIdx.x; i < cnt; i += THREADS) {
       uint32_t d = stage_d[i];
       vout[gbase[d] + (i - tile_off[d])] = vstage[i];
     }
+  }
+}
+
+// Autotuner (tmrg_tune.cu): a size class of an operation with `ncand`
+// candidate shapes.  tune_run runs the operation with the class's chosen
+// candidate, timing all of them the first time the class is seen on the
+// device; tune_lookup returns the cached choice (or the fallback).
+struct TuneKey {
+  int kind, a, b, c, d;
+  int fallback;
+};
+enum TuneKind {
+  TUNE_P = 1,
+  TUNE_PT = 2,
+  TUNE_FILTER3_F32 = 3,
+  TUNE_FILTER3_F64 = 4,
+  TUNE_RADIX = 5
+};
+int tune_run(const TuneKey &k, int ncand, const std::function<void(int)> &run,
+             cudaStream_t s);
+int tune_lookup(const TuneKey &k);
+
+template <typename K, bool VALS>
+inline void radix_scatter_shape(int shape, unsigned nb, cudaStream_t s, const K *kin,
+                                const uint32_t *vin, K *kout, uint32_t *vout, long long n,
+                                int shift, const uint32_t *offs, const uint32_t *dtot) {
+  switch (shape) {
+    case 1:
+      launch((k_radix_scatter<K, VALS, 512, 3>), nb, 512, 0, s, kin, vin, kout, vout, n, shift,
+             offs, dtot, nb);
+      break;
+    case 2:
+      launch((k_radix_scatter<K, VALS, 1024, 2>), nb, 1024, 0, s, kin, vin, kout, vout, n, shift,
+             offs, dtot, nb);
+      break;
+    default:
+      launch((k_radix_scatter<K, VALS, 512, 2>), nb, 512, 0, s, kin, vin, kout, vout, n, shift,
+             offs, dtot, nb);
   }
 }
 
@@ -475,15 +518,20 @@ inline void radix_sort(DBuf<K> &keys, DBuf<uint32_t> *vals, long long n, int nbi
     launch(k_radix_hist<K>, nb, RS_THREADS, 0, s, (const K *)keys.p, n, shift, hist.p, nb);
     prof_bytes(8LL * 256 * nb);
     launch(k_radix_scan_digits, 256, RS_SCAN_THREADS, 0, s, hist.p, nb, dtot);
-    prof_bytes((vals ? 2 * KB + 8 : 2 * KB) * n);
-    if (vals)
-      launch((k_radix_scatter<K, true>), nb, RS_THREADS, 0, s, (const K *)keys.p,
-             (const uint32_t *)vals->p, k2.p, v2.p, n, shift, (const uint32_t *)hist.p,
-             (const uint32_t *)dtot, nb);
-    else
-      launch((k_radix_scatter<K, false>), nb, RS_THREADS, 0, s, (const K *)keys.p,
-             (const uint32_t *)nullptr, k2.p, (uint32_t *)nullptr, n, shift,
-             (const uint32_t *)hist.p, (const uint32_t *)dtot, nb);
+    // the scatter is out of place and every shape writes the same result,
+    // so the first pass of a size class times the shapes on its own data
+    const TuneKey tk{TUNE_RADIX, (int)KB, vals ? 1 : 0, bits_for(n), 0, 0};
+    tune_run(tk, 3, [&](int shape) {
+      prof_bytes((vals ? 2 * KB + 8 : 2 * KB) * n);
+      if (vals)
+        radix_scatter_shape<K, true>(shape, nb, s, (const K *)keys.p, (const uint32_t *)vals->p,
+                                     k2.p, v2.p, n, shift, (const uint32_t *)hist.p,
+                                     (const uint32_t *)dtot);
+      else
+        radix_scatter_shape<K, false>(shape, nb, s, (const K *)keys.p, nullptr, k2.p, nullptr,
+                                      n, shift, (const uint32_t *)hist.p,
+                                      (const uint32_t *)dtot);
+    }, s);
     keys.swap(k2);
     if (vals) vals->swap(v2);
   }
