@@ -23,7 +23,8 @@ from tests import pipeline  # noqa: E402
 
 CASES = ["c1_small", "brick_o2", "brick_o3", "rot_o2", "rot_o3", "rot_o4", "nocorner",
          "uniform_o3", "mixed_o2", "gap_o2", "gap_o3", "pcoarse_o3", "pcoarse_o4",
-         "coarse_o4", "bern_o3", "bern_p3", "bern_o4", "bern_o5"]
+         "coarse_o4", "bern_o3", "bern_p3", "bern_o4", "bern_o5", "deep_o2", "deep_o3",
+         "deep_l29", "deep_l30"]
 
 
 def case_meta(case):
@@ -38,6 +39,12 @@ def main(names=None):
     for name in names or CASES:
         case = allc[name]
         r = pipeline.run_cpu(case, "ref")
+        if r.get("octants_only"):
+            out = os.path.join(HERE, name + ".npz")
+            np.savez_compressed(out, meta=np.array(case_meta(case)), block_conn=case["conn"],
+                                octants=r["oct"])
+            print(name, len(r["oct"]), "octants ->", out, os.path.getsize(out), "bytes")
+            continue
         arrs = {
             "meta": np.array(case_meta(case)),
             "block_conn": case["conn"],

@@ -15,6 +15,8 @@ RTOL = 1e-13  # FP64 tolerance for weights and applies (relative)
 def indicator(octs, case, p):
     if case.get("indicator", "random") == "sphere":
         return W.sphere_indicator(octs)
+    if case.get("indicator") == "point":
+        return W.point_indicator(octs, case["point"])
     if case.get("indicator") == "mixed":
         return W.mixed_indicator(len(octs), case.get("seed", 0), p, case.get("prob", 0.3),
                                  case.get("coarsen_prob", 0.3))
@@ -60,6 +62,8 @@ def run_gpu(case):
         o = f.getOctantsArray()
         f.refine(indicator(o, case, p), 0, case["max_level"])
         f.balance(case.get("corner", 1))
+    if case.get("octants_only"):
+        return dict(oct=f.getOctantsArray(), octants_only=True, forests=[f])
     f.createNodes()
     out = dict(oct=f.getOctantsArray(), conn=f.getMeshConn(),
                nn=f.getNodeNumbers(), dep=f.getDepNodeConn(),
@@ -96,6 +100,8 @@ def run_cpu(case, kind="oracle"):
         o = f.getOctants()
         f.refine(indicator(o, case, p), 0, case["max_level"])
         f.balance(case.get("corner", 1))
+    if case.get("octants_only"):
+        return dict(oct=f.getOctants(), octants_only=True)
     f.createNodes()
     out = dict(oct=f.getOctants(), conn=f.getMeshConn(order), nn=f.getNodeNumbers(),
                dep=f.getDepNodeConn(), sizes=f.nodeSizes(), levels=[])
@@ -134,6 +140,8 @@ def compare(a, b):
             bad.append("%s: max abs diff %g" % (name, np.abs(x - y).max()))
 
     ints("octants", a["oct"], b["oct"])
+    if a.get("octants_only") or b.get("octants_only"):
+        return bad
     if a["sizes"] != b["sizes"]:
         bad.append("sizes %s vs %s" % (a["sizes"], b["sizes"]))
     ints("conn", a["conn"], b["conn"])
@@ -259,6 +267,8 @@ def load_golden(name):
     (tests/golden/<name>.npz, written by tests/golden/make_golden.py), in
     the format run_gpu/run_cpu return."""
     z = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
+    if "sizes" not in z:
+        return dict(oct=z["octants"], octants_only=True)
     s = z["sizes"]
     out = dict(oct=z["octants"], conn=z["conn"], nn=z["node_numbers"],
                dep=(z["dep_ptr"], z["dep_conn"], z["dep_w"]),
@@ -318,6 +328,24 @@ def cases():
         # geometric coarsening at order 4 (coarse elements of order 4)
         "coarse_o4": dict(conn=W.rotate_blocks(W.brick(2, 1, 1), 13), order=4, L0=1,
                           passes=2, max_level=3, prob=0.3, seed=19, coarse_levels=2),
+        # forests deeper than 64-bit keys hold (octant keys of bb + 3W + 5
+        # bits, node keys of bb + 3(W + 1) + label bits): refinement paths
+        # toward one block-local point, the coarse levels crossing back
+        # to 64-bit keys
+        "deep_o2": dict(conn=W.brick(1, 1, 1), order=2, L0=1, passes=22, max_level=23,
+                        indicator="point", point=[0.3, 0.6, 0.45], coarse_levels=2),
+        "deep_o3": dict(conn=W.rotate_blocks(W.brick(2, 1, 1), 27), order=3, L0=1, passes=20,
+                        max_level=21, indicator="point", point=[1.0 - 2.0 ** -25, 0.37, 0.61],
+                        coarse_levels=3),
+        "deep_l29": dict(conn=W.brick(1, 1, 1), order=2, L0=0, passes=29, max_level=29,
+                         indicator="point", point=[0.7, 0.2, 0.55], coarse_levels=1),
+        # refine + balance down to level 30 (side 1); octants only: the
+        # reference's element connectivity takes a half side of
+        # 1 << (TMR_MAX_LEVEL - level - 1) (TMROctForest.cpp:4693), a negative
+        # shift at level 30, so its nodes there have no defined value
+        "deep_l30": dict(conn=W.rotate_blocks(W.brick(2, 1, 1), 31), order=2, L0=0, passes=30,
+                         max_level=30, indicator="point", point=[0.999, 0.2, 0.55],
+                         octants_only=True),
         # Bernstein elements (interp 2): dependent rows from the subdivision
         # weights, P from the Bernstein basis (same order) or the degree
         # elevation table (order one lower)

@@ -235,38 +235,107 @@ HD uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) {
   return (spread3(x) << 2) | (spread3(y) << 1) | spread3(z);
 }
 
+// 128-bit keys for forests whose octant or node keys outgrow 64 bits
+// (deep levels times many blocks).  Only the operations the key kernels
+// use: shifts, or, and, compare, and the low words.
+struct alignas(16) U128 {
+  uint64_t lo, hi;
+  HD U128() : lo(0), hi(0) {}
+  HD U128(uint64_t v) : lo(v), hi(0) {}
+  HD U128(uint64_t h, uint64_t l) : lo(l), hi(h) {}
+};
+HD U128 operator|(U128 a, U128 b) { return U128(a.hi | b.hi, a.lo | b.lo); }
+HD U128 operator&(U128 a, U128 b) { return U128(a.hi & b.hi, a.lo & b.lo); }
+HD bool operator==(U128 a, U128 b) { return a.lo == b.lo && a.hi == b.hi; }
+HD bool operator!=(U128 a, U128 b) { return !(a == b); }
+HD bool operator<(U128 a, U128 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+HD bool operator<=(U128 a, U128 b) { return !(b < a); }
+HD U128 operator<<(U128 a, int s) {
+  if (s <= 0) return a;
+  if (s >= 128) return U128();
+  if (s >= 64) return U128(a.lo << (s - 64), 0);
+  return U128((a.hi << s) | (a.lo >> (64 - s)), a.lo << s);
+}
+HD U128 operator>>(U128 a, int s) {
+  if (s <= 0) return a;
+  if (s >= 128) return U128();
+  if (s >= 64) return U128(0, a.hi >> (s - 64));
+  return U128(a.hi >> s, (a.lo >> s) | (a.hi << (64 - s)));
+}
+HD uint64_t klo64(uint64_t k) { return k; }
+HD uint64_t klo64(U128 k) { return k.lo; }
+// all ones in the low `bits` bits
+template <typename K>
+HD K kmask(int bits);
+template <>
+HD uint64_t kmask<uint64_t>(int bits) {
+  return bits >= 64 ? ~0ULL : ((1ULL << bits) - 1ULL);
+}
+template <>
+HD U128 kmask<U128>(int bits) {
+  if (bits >= 128) return U128(~0ULL, ~0ULL);
+  if (bits >= 64) return U128(kmask<uint64_t>(bits - 64), ~0ULL);
+  return U128(0, kmask<uint64_t>(bits));
+}
+// Morton code of coordinates of up to 21 (uint64_t) or 30 (U128) bits.
+template <typename K>
+HD K kmorton3(uint32_t x, uint32_t y, uint32_t z);
+template <>
+HD uint64_t kmorton3<uint64_t>(uint32_t x, uint32_t y, uint32_t z) {
+  return morton3(x, y, z);
+}
+template <>
+HD U128 kmorton3<U128>(uint32_t x, uint32_t y, uint32_t z) {
+  const uint32_t m21 = 0x1fffffu;
+  return U128(morton3(x & m21, y & m21, z & m21)) |
+         (U128(morton3(x >> 21, y >> 21, z >> 21)) << 63);
+}
+// Every third bit of v (from bit 0), compacted.
+HD uint32_t kcompact3(uint64_t v) { return compact3(v); }
+HD uint32_t kcompact3(U128 v) {
+  return compact3(v.lo & 0x7fffffffffffffffULL) | (compact3((v >> 63).lo) << 21);
+}
+// 16-byte aligned read-only load
+__device__ __forceinline__ uint64_t kldg(const uint64_t *p) { return __ldg(p); }
+__device__ __forceinline__ U128 kldg(const U128 *p) {
+  const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2 *>(p));
+  return U128(v.y, v.x);
+}
+
 // Key layout for octants: [block | morton(3W) | level(5)], W = bits per
 // coordinate (the finest level present).  Element order = key order.
-struct OctKey {
+// K = uint64_t where bb + 3W + 5 <= 64, else U128.
+template <typename K>
+struct OctKeyT {
   int W;  // coordinate bits
   int bb; // block bits
   HD int total_bits() const { return bb + 3 * W + 5; }
-  HD uint64_t make(int32_t block, int32_t x, int32_t y, int32_t z,
-                   int level) const {
+  HD K make(int32_t block, int32_t x, int32_t y, int32_t z, int level) const {
     int s = TMRG_MAX_LEVEL - W;
-    uint64_t m = morton3((uint32_t)x >> s, (uint32_t)y >> s, (uint32_t)z >> s);
-    return ((uint64_t)(uint32_t)block << (3 * W + 5)) | (m << 5) |
-           (uint64_t)level;
+    K m = kmorton3<K>((uint32_t)x >> s, (uint32_t)y >> s, (uint32_t)z >> s);
+    return (K((uint64_t)(uint32_t)block) << (3 * W + 5)) | (m << 5) | K((uint64_t)level);
   }
-  HD uint64_t pos(uint64_t key) const { return key >> 5; }
-  HD Oct decode(uint64_t key) const {
+  HD K pos(K key) const { return key >> 5; }
+  HD Oct decode(K key) const {
     Oct o;
     int s = TMRG_MAX_LEVEL - W;
-    o.level = (int)(key & 31);
-    uint64_t m = (key >> 5) & ((W >= 21) ? ~0ULL : ((1ULL << (3 * W)) - 1));
-    o.x = (int32_t)(compact3(m >> 2) << s);
-    o.y = (int32_t)(compact3(m >> 1) << s);
-    o.z = (int32_t)(compact3(m) << s);
-    o.block = (int32_t)(key >> (3 * W + 5));
+    o.level = (int)(klo64(key) & 31);
+    K m = (key >> 5) & kmask<K>(3 * W);
+    o.x = (int32_t)(kcompact3(m >> 2) << s);
+    o.y = (int32_t)(kcompact3(m >> 1) << s);
+    o.z = (int32_t)(kcompact3(m) << s);
+    o.block = (int32_t)klo64(key >> (3 * W + 5));
     return o;
   }
 };
+using OctKey = OctKeyT<uint64_t>;
 
 // Key layout for node objects: [block | morton(3Wn) | label(lb)].  Node
 // coordinates are multiples of 2^(30-Lg) or the truncated boundary value
 // hmax-1; they map to 2c/s and to all-ones, which keeps the order of the
 // truncated 30-bit coordinates (TMROctForest.cpp:4029-4037).
-struct NodeKey {
+template <typename K>
+struct NodeKeyT {
   int Lg;  // node grid level
   int bb;  // block bits
   int lb;  // label bits (0 or 2)
@@ -276,13 +345,13 @@ struct NodeKey {
     if (c == TMRG_HMAX - 1) return (1u << (Lg + 1)) - 1u;
     return ((uint32_t)c >> (TMRG_MAX_LEVEL - Lg)) << 1;
   }
-  HD uint64_t make(int32_t block, int32_t x, int32_t y, int32_t z,
-                   int label) const {
-    uint64_t m = morton3(map(x), map(y), map(z));
-    return ((uint64_t)(uint32_t)block << (3 * (Lg + 1) + lb)) | (m << lb) |
-           (uint64_t)label;
+  HD K make(int32_t block, int32_t x, int32_t y, int32_t z, int label) const {
+    K m = kmorton3<K>(map(x), map(y), map(z));
+    return (K((uint64_t)(uint32_t)block) << (3 * (Lg + 1) + lb)) | (m << lb) |
+           K((uint64_t)label);
   }
 };
+using NodeKey = NodeKeyT<uint64_t>;
 
 HD int bits_for(long long n) {  // bits to hold values 0..n-1 (>= 1)
   int b = 1;

@@ -35,15 +35,20 @@ void Forest::set_order(int o, int it) {
   }
 }
 
+// The octant key layout; the kernels take 64-bit keys where it fits and
+// 128-bit keys (U128) otherwise.
 OctKey Forest::oct_key() const {
   OctKey k;
   k.W = std::max(maxlev, 1);
   k.bb = conn->block_bits;
-  if (k.total_bits() > 64)
+  if (k.total_bits() > 128)
     throw Error(TMRG_ERR_KEY_RANGE,
-                "octant key needs " + std::to_string(k.total_bits()) +
-                    " bits (blocks x levels too large for 64-bit keys)");
+                "octant key needs " + std::to_string(k.total_bits()) + " bits");
   return k;
+}
+template <typename Key>
+static OctKeyT<Key> key_as(const OctKey &k) {
+  return OctKeyT<Key>{k.W, k.bb};
 }
 
 static void alloc_octs(Forest &f, long long n) {
@@ -136,13 +141,14 @@ __global__ void k_refine_count(long long n, RefineArgs a,
 }
 
 // Payload: source index; bit 31 set when the octant keeps its info.
-__global__ void k_refine_emit(long long n, RefineArgs a, OctKey K,
+template <typename Key>
+__global__ void k_refine_emit(long long n, RefineArgs a, OctKeyT<Key> K,
                               const int *__restrict__ blk,
                               const int *__restrict__ xs,
                               const int *__restrict__ ys,
                               const int *__restrict__ zs,
                               const int16_t *__restrict__ lev,
-                              const unsigned *__restrict__ offs, uint64_t *keys,
+                              const unsigned *__restrict__ offs, Key *keys,
                               uint32_t *vals) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -171,11 +177,12 @@ __global__ void k_refine_emit(long long n, RefineArgs a, OctKey K,
 
 // Keep entry i of the sorted keys if it opens its run of equal keys and
 // that run is the last (finest) one at its position.
-__global__ void k_dedupe_flags(long long n, const uint64_t *__restrict__ keys,
+template <typename Key>
+__global__ void k_dedupe_flags(long long n, const Key *__restrict__ keys,
                                unsigned *__restrict__ flag) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  uint64_t k = keys[i];
+  const Key k = keys[i];
   unsigned keep = 0;
   if (i == 0 || keys[i - 1] != k) {
     long long e = i;
@@ -185,8 +192,9 @@ __global__ void k_dedupe_flags(long long n, const uint64_t *__restrict__ keys,
   flag[i] = keep;
 }
 
-__global__ void k_compact_octs(long long n, OctKey K,
-                               const uint64_t *__restrict__ keys,
+template <typename Key>
+__global__ void k_compact_octs(long long n, OctKeyT<Key> K,
+                               const Key *__restrict__ keys,
                                const uint32_t *__restrict__ vals,
                                const unsigned *__restrict__ pos,
                                const int16_t *__restrict__ old_info, int *blk,
@@ -205,6 +213,31 @@ __global__ void k_compact_octs(long long n, OctKey K,
   uint32_t v = vals ? vals[i] : 0u;
   info[o] = (vals && old_info && (v & 0x80000000u)) ? old_info[v & 0x7fffffffu]
                                                    : (int16_t)0;
+}
+
+template <typename Key>
+static void refine_sort_compact(Forest &f, const RefineArgs &a, const OctKeyT<Key> &K,
+                                const DBuf<unsigned> &cnt, unsigned total) {
+  cudaStream_t s = f.s;
+  const long long n = f.n;
+  DBuf<Key> keys(total, s);
+  DBuf<uint32_t> vals(total, s);
+  launch(k_refine_emit<Key>, blocks_for(n, 256), 256, 0, s, n, a, K,
+         (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
+         (const int *)f.z.p, (const int16_t *)f.level.p, (const unsigned *)cnt.p,
+         keys.p, vals.p);
+  sort_keys(keys, &vals, total, K.total_bits(), s);
+  DBuf<unsigned> pos(total + 1, s);
+  launch(k_dedupe_flags<Key>, blocks_for(total, 256), 256, 0, s, (long long)total,
+         (const Key *)keys.p, pos.p);
+  exclusive_scan<unsigned>(pos.p, pos.p, total, s);
+  unsigned m = read_scalar(pos.p + total, s);
+  DBuf<int16_t> old_info = std::move(f.info);
+  alloc_octs(f, m);
+  launch(k_compact_octs<Key>, blocks_for(total, 256), 256, 0, s, (long long)total, K,
+         (const Key *)keys.p, (const uint32_t *)vals.p,
+         (const unsigned *)pos.p, (const int16_t *)old_info.p, f.block.p, f.x.p,
+         f.y.p, f.z.p, f.level.p, f.info.p);
 }
 
 void forest_refine(Forest &f, const int *d_ref, long long nref, int min_level,
@@ -232,25 +265,11 @@ void forest_refine(Forest &f, const int *d_ref, long long nref, int min_level,
   unsigned total = read_scalar(cnt.p + n, s);
   int newmax = read_scalar(ml.p, s);
   f.maxlev = std::max(newmax, 0);
-  OctKey K = f.oct_key();
-  DBuf<uint64_t> keys(total, s);
-  DBuf<uint32_t> vals(total, s);
-  launch(k_refine_emit, blocks_for(n, 256), 256, 0, s, n, a, K,
-         (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
-         (const int *)f.z.p, (const int16_t *)f.level.p, (const unsigned *)cnt.p,
-         keys.p, vals.p);
-  radix_sort(keys, &vals, total, K.total_bits(), s);
-  DBuf<unsigned> pos(total + 1, s);
-  launch(k_dedupe_flags, blocks_for(total, 256), 256, 0, s, (long long)total,
-         (const uint64_t *)keys.p, pos.p);
-  exclusive_scan<unsigned>(pos.p, pos.p, total, s);
-  unsigned m = read_scalar(pos.p + total, s);
-  DBuf<int16_t> old_info = std::move(f.info);
-  alloc_octs(f, m);
-  launch(k_compact_octs, blocks_for(total, 256), 256, 0, s, (long long)total, K,
-         (const uint64_t *)keys.p, (const uint32_t *)vals.p,
-         (const unsigned *)pos.p, (const int16_t *)old_info.p, f.block.p, f.x.p,
-         f.y.p, f.z.p, f.level.p, f.info.p);
+  const OctKey K = f.oct_key();
+  if (K.total_bits() > 64)
+    refine_sort_compact<U128>(f, a, key_as<U128>(K), cnt, total);
+  else
+    refine_sort_compact<uint64_t>(f, a, K, cnt, total);
 }
 
 // ---------------------------------------------------------------------
@@ -357,72 +376,73 @@ void forest_duplicate(Forest &f, Forest &out) {
 // finest-per-position sort leave.
 
 // Position key of a family: [block | morton(3W)].
+template <typename Key>
 struct PosKey {
   int W, bb;
-  __device__ __forceinline__ uint64_t make(int32_t b, int32_t x, int32_t y,
-                                           int32_t z) const {
+  __device__ __forceinline__ Key make(int32_t b, int32_t x, int32_t y, int32_t z) const {
     int s = TMRG_MAX_LEVEL - W;
-    return ((uint64_t)(uint32_t)b << (3 * W)) |
-           morton3((uint32_t)x >> s, (uint32_t)y >> s, (uint32_t)z >> s);
+    return (Key((uint64_t)(uint32_t)b) << (3 * W)) |
+           kmorton3<Key>((uint32_t)x >> s, (uint32_t)y >> s, (uint32_t)z >> s);
   }
-  __device__ __forceinline__ Oct decode(uint64_t k, int level) const {
+  __device__ __forceinline__ Oct decode(Key k, int level) const {
     int s = TMRG_MAX_LEVEL - W;
-    uint64_t m = k & ((1ULL << (3 * W)) - 1);
+    Key m = k & kmask<Key>(3 * W);
     Oct o;
-    o.block = (int32_t)(k >> (3 * W));
-    o.x = (int32_t)(compact3(m >> 2) << s);
-    o.y = (int32_t)(compact3(m >> 1) << s);
-    o.z = (int32_t)(compact3(m) << s);
+    o.block = (int32_t)klo64(k >> (3 * W));
+    o.x = (int32_t)(kcompact3(m >> 2) << s);
+    o.y = (int32_t)(kcompact3(m >> 1) << s);
+    o.z = (int32_t)(kcompact3(m) << s);
     o.level = level;
     return o;
   }
 };
 
 // Seeds: the child-0 of every octant, keyed level-major.
-__global__ void k_seed_keys(long long n, PosKey P, const int *__restrict__ blk,
+template <typename Key>
+__global__ void k_seed_keys(long long n, PosKey<Key> P, const int *__restrict__ blk,
                             const int *__restrict__ xs,
                             const int *__restrict__ ys,
                             const int *__restrict__ zs,
-                            const int16_t *__restrict__ lev, uint64_t *keys) {
+                            const int16_t *__restrict__ lev, Key *keys) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   Oct o{blk[i], xs[i], ys[i], zs[i], lev[i]};
   Oct q = sibling(o, 0);
-  keys[i] = ((uint64_t)o.level << (P.bb + 3 * P.W)) | P.make(q.block, q.x, q.y, q.z);
+  keys[i] = (Key((uint64_t)o.level) << (P.bb + 3 * P.W)) | P.make(q.block, q.x, q.y, q.z);
 }
 
 // Unique flags over sorted keys (first of each run).
-__global__ void k_unique_flags(long long n, const uint64_t *__restrict__ keys,
-                               unsigned *flag) {
+template <typename Key>
+__global__ void k_unique_flags(long long n, const Key *__restrict__ keys, unsigned *flag) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   flag[i] = (i == 0 || keys[i - 1] != keys[i]) ? 1u : 0u;
 }
-__global__ void k_unique_emit(long long n, const uint64_t *__restrict__ keys,
-                              const unsigned *__restrict__ pos, uint64_t mask,
-                              uint64_t *out) {
+template <typename Key>
+__global__ void k_unique_emit(long long n, const Key *__restrict__ keys,
+                              const unsigned *__restrict__ pos, Key mask, Key *out) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || pos[i + 1] == pos[i]) return;
   out[pos[i]] = keys[i] & mask;
 }
-__global__ void k_mask_copy(long long n, const uint64_t *__restrict__ in,
-                            uint64_t mask, uint64_t *out) {
+template <typename Key>
+__global__ void k_mask_copy(long long n, const Key *__restrict__ in, Key mask, Key *out) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = in[i] & mask;
 }
-__global__ void k_level_starts(long long n, const uint64_t *__restrict__ keys,
-                               int shift, long long *starts) {
+template <typename Key>
+__global__ void k_level_starts(long long n, const Key *__restrict__ keys, int shift,
+                               long long *starts) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  int l = (int)(keys[i] >> shift);
-  if (i == 0 || (int)(keys[i - 1] >> shift) != l) starts[l] = i;
+  int l = (int)klo64(keys[i] >> shift);
+  if (i == 0 || (int)klo64(keys[i - 1] >> shift) != l) starts[l] = i;
 }
 
 // Children-0 of the parent's neighbours of family q (level L >= 2).
-template <bool WRITE>
-__device__ __forceinline__ unsigned gen_family(const ConnDev &c, PosKey P,
-                                               const Oct &q, int corner,
-                                               uint64_t *out) {
+template <bool WRITE, typename Key>
+__device__ __forceinline__ unsigned gen_family(const ConnDev &c, PosKey<Key> P,
+                                               const Oct &q, int corner, Key *out) {
   unsigned cnt = 0;
   Oct p = parent_of(q);
   int32_t bs = 2 * side_of(p.level);  // side of the generated family's box
@@ -458,8 +478,9 @@ __device__ __forceinline__ unsigned gen_family(const ConnDev &c, PosKey P,
 
 // n bounds the families; *m (device) is their number, so the count of the
 // families need not be read back first (entries past it count 0).
-__global__ void k_gen_count(long long n, const unsigned *__restrict__ m, ConnDev c, PosKey P,
-                            int level, int corner, const uint64_t *__restrict__ cur,
+template <typename Key>
+__global__ void k_gen_count(long long n, const unsigned *__restrict__ m, ConnDev c,
+                            PosKey<Key> P, int level, int corner, const Key *__restrict__ cur,
                             unsigned *cnt) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -468,33 +489,34 @@ __global__ void k_gen_count(long long n, const unsigned *__restrict__ m, ConnDev
     return;
   }
   Oct q = P.decode(cur[i], level);
-  cnt[i] = gen_family<false>(c, P, q, corner, nullptr);
+  cnt[i] = gen_family<false, Key>(c, P, q, corner, nullptr);
 }
-__global__ void k_gen_write(long long n, const unsigned *__restrict__ m, ConnDev c, PosKey P,
-                            int level, int corner, const uint64_t *__restrict__ cur,
-                            const unsigned *__restrict__ offs, uint64_t *out) {
+template <typename Key>
+__global__ void k_gen_write(long long n, const unsigned *__restrict__ m, ConnDev c,
+                            PosKey<Key> P, int level, int corner, const Key *__restrict__ cur,
+                            const unsigned *__restrict__ offs, Key *out) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || i >= (long long)*m) return;
   Oct q = P.decode(cur[i], level);
-  gen_family<true>(c, P, q, corner, out + offs[i]);
+  gen_family<true, Key>(c, P, q, corner, out + offs[i]);
 }
 
 // Leaves of level L: siblings of each family in S_L whose anchor does not
 // hold a finer family (or the root itself at level 0).
-__global__ void k_leaves(long long n, PosKey P, OctKey K, int level,
-                         const uint64_t *__restrict__ cur,
-                         const uint64_t *__restrict__ finer, long long nfiner,
-                         uint64_t *out, unsigned long long *counter) {
+template <typename Key>
+__global__ void k_leaves(long long n, PosKey<Key> P, OctKeyT<Key> K, int level,
+                         const Key *__restrict__ cur, const Key *__restrict__ finer,
+                         long long nfiner, Key *out, unsigned long long *counter) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t mine[8];
+  Key mine[8];
   int m = 0;
   if (i < n) {
     Oct q = P.decode(cur[i], level);
     int ns = (level == 0) ? 1 : 8;
     for (int j = 0; j < ns; j++) {
       Oct sb = (level == 0) ? q : sibling(q, j);
-      uint64_t pk = P.make(sb.block, sb.x, sb.y, sb.z);
-      if (!contains_u64(finer, nfiner, pk))
+      const Key pk = P.make(sb.block, sb.x, sb.y, sb.z);
+      if (!contains_key(finer, nfiner, pk))
         mine[m++] = K.make(sb.block, sb.x, sb.y, sb.z, level);
     }
   }
@@ -513,8 +535,9 @@ __global__ void k_leaves(long long n, PosKey P, OctKey K, int level,
   for (int j = 0; j < m; j++) out[o + j] = mine[j];
 }
 
-__global__ void k_decode_octs(long long n, OctKey K,
-                              const uint64_t *__restrict__ keys, int *blk,
+template <typename Key>
+__global__ void k_decode_octs(long long n, OctKeyT<Key> K, const Key *__restrict__ keys,
+                              int *blk,
                               int *xs, int *ys, int *zs, int16_t *lev,
                               int16_t *info) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -529,52 +552,46 @@ __global__ void k_decode_octs(long long n, OctKey K,
 }
 
 // Sort `keys` (n entries, nbits) and keep one of each value (masked).
-static long long sort_unique(DBuf<uint64_t> &keys, long long n, int nbits,
-                             uint64_t mask, DBuf<uint64_t> &out,
+template <typename Key>
+static long long sort_unique(DBuf<Key> &keys, long long n, int nbits, Key mask, DBuf<Key> &out,
                              cudaStream_t s) {
   if (n == 0) {
     out.release();
     return 0;
   }
-  radix_sort(keys, nullptr, n, nbits, s);
+  sort_keys(keys, nullptr, n, nbits, s);
   DBuf<unsigned> pos(n + 1, s);
-  launch(k_unique_flags, blocks_for(n, 256), 256, 0, s, n,
-         (const uint64_t *)keys.p, pos.p);
+  launch(k_unique_flags<Key>, blocks_for(n, 256), 256, 0, s, n, (const Key *)keys.p, pos.p);
   exclusive_scan<unsigned>(pos.p, pos.p, n, s);
   long long m = read_scalar(pos.p + n, s);
   out.alloc(m, s);
-  launch(k_unique_emit, blocks_for(n, 256), 256, 0, s, n,
-         (const uint64_t *)keys.p, (const unsigned *)pos.p, mask, out.p);
+  launch(k_unique_emit<Key>, blocks_for(n, 256), 256, 0, s, n, (const Key *)keys.p,
+         (const unsigned *)pos.p, mask, out.p);
   return m;
 }
 
-void forest_balance(Forest &f, int corner) {
-  Stage stage("tmrg_balance");
-  if (!f.have_octs)
-    throw Error(TMRG_ERR_STATE,
-                "Cannot call balance(), no octants have been created");
-  f.free_nodes();
-  long long n = f.n;
-  if (n == 0) return;
+template <typename Key>
+static void balance_impl(Forest &f, int corner, const OctKeyT<Key> K) {
+  const long long n = f.n;
   cudaStream_t s = f.s;
-  OctKey K = f.oct_key();
-  PosKey P{K.W, K.bb};
+  PosKey<Key> P{K.W, K.bb};
   const int pbits = K.bb + 3 * K.W;
-  const uint64_t pmask = (pbits >= 64) ? ~0ULL : ((1ULL << pbits) - 1);
+  const Key pmask = kmask<Key>(pbits);
+  const Key all = kmask<Key>(8 * (int)sizeof(Key));
   ConnDev c = f.conn->dev;
 
   // Seeds, unique, grouped by level.
-  DBuf<uint64_t> sk(n, s);
-  launch(k_seed_keys, blocks_for(n, 256), 256, 0, s, n, P, (const int *)f.block.p,
+  DBuf<Key> sk(n, s);
+  launch(k_seed_keys<Key>, blocks_for(n, 256), 256, 0, s, n, P, (const int *)f.block.p,
          (const int *)f.x.p, (const int *)f.y.p, (const int *)f.z.p,
          (const int16_t *)f.level.p, sk.p);
-  DBuf<uint64_t> seeds;
-  long long ns = sort_unique(sk, n, pbits + 5, ~0ULL, seeds, s);
+  DBuf<Key> seeds;
+  long long ns = sort_unique<Key>(sk, n, pbits + 5, all, seeds, s);
   sk.release();
   DBuf<long long> starts(TMRG_MAX_LEVEL + 2, s);
   starts.fill_bytes(0xff);
-  launch(k_level_starts, blocks_for(ns, 256), 256, 0, s, ns,
-         (const uint64_t *)seeds.p, pbits, starts.p);
+  launch(k_level_starts<Key>, blocks_for(ns, 256), 256, 0, s, ns, (const Key *)seeds.p, pbits,
+         starts.p);
   std::vector<long long> st(TMRG_MAX_LEVEL + 2);
   TMRG_CUDA(cudaMemcpyAsync(st.data(), starts.p, st.size() * sizeof(long long),
                             cudaMemcpyDeviceToHost, s));
@@ -595,9 +612,9 @@ void forest_balance(Forest &f, int corner) {
   }
 
   // Fixed point, finest level first.
-  std::vector<DBuf<uint64_t>> S(L + 2);
+  std::vector<DBuf<Key>> S(L + 2);
   std::vector<long long> Sn(L + 2, 0);
-  DBuf<uint64_t> gen;
+  DBuf<Key> gen;
   long long ngen = 0;
   // One wait per level: the level's distinct families stay counted on the
   // device (S[l] sized by the level's input), the next level's generated
@@ -608,21 +625,21 @@ void forest_balance(Forest &f, int corner) {
     long long tot = nseed + ngen;
     DBuf<unsigned> upos;  // unique positions; upos[tot] = Sn[l]
     if (tot > 0) {
-      DBuf<uint64_t> cat(tot, s);
+      DBuf<Key> cat(tot, s);
       if (nseed)
-        launch(k_mask_copy, blocks_for(nseed, 256), 256, 0, s, nseed,
-               (const uint64_t *)(seeds.p + lo[l]), pmask, cat.p);
+        launch(k_mask_copy<Key>, blocks_for(nseed, 256), 256, 0, s, nseed,
+               (const Key *)(seeds.p + lo[l]), pmask, cat.p);
       if (ngen)
-        TMRG_CUDA(cudaMemcpyAsync(cat.p + nseed, gen.p, ngen * sizeof(uint64_t),
+        TMRG_CUDA(cudaMemcpyAsync(cat.p + nseed, gen.p, ngen * sizeof(Key),
                                   cudaMemcpyDeviceToDevice, s));
-      radix_sort(cat, nullptr, tot, pbits, s);
+      sort_keys(cat, nullptr, tot, pbits, s);
       upos.alloc(tot + 1, s);
-      launch(k_unique_flags, blocks_for(tot, 256), 256, 0, s, tot, (const uint64_t *)cat.p,
+      launch(k_unique_flags<Key>, blocks_for(tot, 256), 256, 0, s, tot, (const Key *)cat.p,
              upos.p);
       exclusive_scan<unsigned>(upos.p, upos.p, tot, s);
       S[l].alloc(tot, s);
-      launch(k_unique_emit, blocks_for(tot, 256), 256, 0, s, tot, (const uint64_t *)cat.p,
-             (const unsigned *)upos.p, ~0ULL, S[l].p);
+      launch(k_unique_emit<Key>, blocks_for(tot, 256), 256, 0, s, tot, (const Key *)cat.p,
+             (const unsigned *)upos.p, all, S[l].p);
     }
     gen.release();
     ngen = 0;
@@ -630,8 +647,8 @@ void forest_balance(Forest &f, int corner) {
     if (tot == 0) continue;
     if (l >= 2) {
       DBuf<unsigned> cnt(tot + 1, s);
-      launch(k_gen_count, blocks_for(tot, 128), 128, 0, s, tot, (const unsigned *)upos.p + tot,
-             c, P, l, corner, (const uint64_t *)S[l].p, cnt.p);
+      launch(k_gen_count<Key>, blocks_for(tot, 128), 128, 0, s, tot,
+             (const unsigned *)upos.p + tot, c, P, l, corner, (const Key *)S[l].p, cnt.p);
       exclusive_scan<unsigned>(cnt.p, cnt.p, tot, s);
       const unsigned *dv[2] = {upos.p + tot, cnt.p + tot};
       unsigned hv[2];
@@ -639,8 +656,9 @@ void forest_balance(Forest &f, int corner) {
       Sn[l] = hv[0];
       ngen = hv[1];
       gen.alloc(ngen, s);
-      launch(k_gen_write, blocks_for(tot, 128), 128, 0, s, tot, (const unsigned *)upos.p + tot,
-             c, P, l, corner, (const uint64_t *)S[l].p, (const unsigned *)cnt.p, gen.p);
+      launch(k_gen_write<Key>, blocks_for(tot, 128), 128, 0, s, tot,
+             (const unsigned *)upos.p + tot, c, P, l, corner, (const Key *)S[l].p,
+             (const unsigned *)cnt.p, gen.p);
     } else {
       Sn[l] = read_scalar(upos.p + tot, s);
     }
@@ -650,22 +668,34 @@ void forest_balance(Forest &f, int corner) {
   // Leaves of every level, then one sort into element order.
   long long cap = 0;
   for (int l = 0; l <= L; l++) cap += (l == 0 ? 1 : 8) * Sn[l];
-  DBuf<uint64_t> leaves(cap, s);
+  DBuf<Key> leaves(cap, s);
   DBuf<unsigned long long> counter(1, s);
   counter.zero();
   for (int l = 0; l <= L; l++) {
     if (!Sn[l]) continue;
-    launch(k_leaves, blocks_for(Sn[l], 256), 256, 0, s, Sn[l], P, K, l,
-           (const uint64_t *)S[l].p, (const uint64_t *)S[l + 1].p, Sn[l + 1],
-           leaves.p, counter.p);
+    launch(k_leaves<Key>, blocks_for(Sn[l], 256), 256, 0, s, Sn[l], P, K, l,
+           (const Key *)S[l].p, (const Key *)S[l + 1].p, Sn[l + 1], leaves.p, counter.p);
   }
   long long m = (long long)read_scalar(counter.p, s);
   S.clear();
-  radix_sort(leaves, nullptr, m, K.total_bits(), s);
+  sort_keys(leaves, nullptr, m, K.total_bits(), s);
   alloc_octs(f, m);
-  launch(k_decode_octs, blocks_for(m, 256), 256, 0, s, m, K,
-         (const uint64_t *)leaves.p, f.block.p, f.x.p, f.y.p, f.z.p, f.level.p,
-         f.info.p);
+  launch(k_decode_octs<Key>, blocks_for(m, 256), 256, 0, s, m, K, (const Key *)leaves.p,
+         f.block.p, f.x.p, f.y.p, f.z.p, f.level.p, f.info.p);
+}
+
+void forest_balance(Forest &f, int corner) {
+  Stage stage("tmrg_balance");
+  if (!f.have_octs)
+    throw Error(TMRG_ERR_STATE,
+                "Cannot call balance(), no octants have been created");
+  f.free_nodes();
+  if (f.n == 0) return;
+  const OctKey K = f.oct_key();
+  if (K.total_bits() > 64)
+    balance_impl<U128>(f, corner, key_as<U128>(K));
+  else
+    balance_impl<uint64_t>(f, corner, K);
 }
 
 // ---------------------------------------------------------------------
@@ -696,8 +726,9 @@ __global__ void k_random_refinement(uint64_t seed, uint64_t stream, double prob,
 // level, sorted, and made unique on position keeping the finest (the
 // reference's TMROctantArray::sort).  The reference draws from libc rand();
 // here octant i of block b draws U(seed, b, 4i + k), k = 0..3.
+template <typename Key>
 __global__ void k_random_octs(long long total, int nrand, int min_level, int max_level,
-                              uint64_t seed, OctKey K, uint64_t *keys) {
+                              uint64_t seed, OctKeyT<Key> K, Key *keys) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= total) return;
   const unsigned tu = (unsigned)t;  // total < 2^32
@@ -716,6 +747,25 @@ __global__ void k_random_octs(long long total, int nrand, int min_level, int max
   keys[t] = K.make(b, c[0], c[1], c[2], level);
 }
 
+template <typename Key>
+static void random_sort_compact(Forest &f, long long total, int nrand, int min_level,
+                                int max_level, uint64_t seed, const OctKeyT<Key> &K) {
+  cudaStream_t s = f.s;
+  DBuf<Key> keys(total, s);
+  launch(k_random_octs<Key>, blocks_for(total, 256), 256, 0, s, total, nrand, min_level,
+         max_level, seed, K, keys.p);
+  sort_keys(keys, nullptr, total, K.total_bits(), s);
+  DBuf<unsigned> pos(total + 1, s);
+  launch(k_dedupe_flags<Key>, blocks_for(total, 256), 256, 0, s, total, (const Key *)keys.p,
+         pos.p);
+  exclusive_scan<unsigned>(pos.p, pos.p, total, s);
+  const unsigned m = total ? read_scalar(pos.p + total, s) : 0u;
+  alloc_octs(f, m);
+  launch(k_compact_octs<Key>, blocks_for(total, 256), 256, 0, s, total, K, (const Key *)keys.p,
+         (const uint32_t *)nullptr, (const unsigned *)pos.p, (const int16_t *)nullptr,
+         f.block.p, f.x.p, f.y.p, f.z.p, f.level.p, f.info.p);
+}
+
 void forest_create_random_trees(Forest &f, int nrand, int min_level, int max_level,
                                 uint64_t seed) {
   Stage st("tmrg_create_random_trees");
@@ -729,20 +779,11 @@ void forest_create_random_trees(Forest &f, int nrand, int min_level, int max_lev
   const long long total = (long long)f.conn->nb * nrand;
   if (total >= (1LL << 32)) throw Error(TMRG_ERR_ARG, "createRandomTrees: too many octants");
   f.maxlev = max_level;
-  OctKey K = f.oct_key();
-  DBuf<uint64_t> keys(total, s);
-  launch(k_random_octs, blocks_for(total, 256), 256, 0, s, total, nrand, min_level,
-         max_level, seed, K, keys.p);
-  radix_sort(keys, nullptr, total, K.total_bits(), s);
-  DBuf<unsigned> pos(total + 1, s);
-  launch(k_dedupe_flags, blocks_for(total, 256), 256, 0, s, total, (const uint64_t *)keys.p,
-         pos.p);
-  exclusive_scan<unsigned>(pos.p, pos.p, total, s);
-  const unsigned m = total ? read_scalar(pos.p + total, s) : 0u;
-  alloc_octs(f, m);
-  launch(k_compact_octs, blocks_for(total, 256), 256, 0, s, total, K,
-         (const uint64_t *)keys.p, (const uint32_t *)nullptr, (const unsigned *)pos.p,
-         (const int16_t *)nullptr, f.block.p, f.x.p, f.y.p, f.z.p, f.level.p, f.info.p);
+  const OctKey K = f.oct_key();
+  if (K.total_bits() > 64)
+    random_sort_compact<U128>(f, total, nrand, min_level, max_level, seed, key_as<U128>(K));
+  else
+    random_sort_compact<uint64_t>(f, total, nrand, min_level, max_level, seed, K);
   f.have_octs = true;
   TMRG_CUDA(cudaStreamSynchronize(s));
 }

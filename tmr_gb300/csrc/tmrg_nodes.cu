@@ -72,16 +72,18 @@ static Labels make_labels(int order, int interp) {
 
 // ---------------------------------------------------------------------
 // 1. Hanging flags.
-__global__ void k_oct_keys(long long n, OctKey K, const int *__restrict__ blk,
+template <typename Key>
+__global__ void k_oct_keys(long long n, OctKeyT<Key> K, const int *__restrict__ blk,
                            const int *__restrict__ xs, const int *__restrict__ ys,
                            const int *__restrict__ zs,
-                           const int16_t *__restrict__ lev, uint64_t *keys) {
+                           const int16_t *__restrict__ lev, Key *keys) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) keys[i] = K.make(blk[i], xs[i], ys[i], zs[i], lev[i]);
 }
 
-__global__ void k_dep_info(long long n, ConnDev c, OctKey K,
-                           const uint64_t *__restrict__ keys,
+template <typename Key>
+__global__ void k_dep_info(long long n, ConnDev c, OctKeyT<Key> K,
+                           const Key *__restrict__ keys,
                            const int *__restrict__ blk,
                            const int *__restrict__ xs, const int *__restrict__ ys,
                            const int *__restrict__ zs,
@@ -95,7 +97,7 @@ __global__ void k_dep_info(long long n, ConnDev c, OctKey K,
   }
   const int32_t hmax = TMRG_HMAX;
   auto exists = [&](const Oct &q) {
-    return contains_u64(keys, n, K.make(q.block, q.x, q.y, q.z, q.level));
+    return contains_key(keys, n, K.make(q.block, q.x, q.y, q.z, q.level));
   };
   int id = child_id(o);
   Oct p = parent_of(o);
@@ -192,11 +194,12 @@ __device__ __forceinline__ void object_of(const NodeGen &g, const Oct &e, int j,
   }
 }
 
+template <typename Key>
 __global__ void k_node_keys(long long n, ConnDev c, NodeGen g,
                             const int *__restrict__ blk,
                             const int *__restrict__ xs, const int *__restrict__ ys,
                             const int *__restrict__ zs,
-                            const int16_t *__restrict__ lev, uint64_t *keys,
+                            const int16_t *__restrict__ lev, Key *keys,
                             uint32_t *vals) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * g.nobj) return;
@@ -209,25 +212,26 @@ __global__ void k_node_keys(long long n, ConnDev c, NodeGen g,
   int label, mult, ed;
   object_of(g, o, j, x, y, z, label, mult, ed);
   transform_node(c, b, x, y, z, -1, nullptr, nullptr);
-  keys[t] = g.NK.make(b, x, y, z, label);
+  keys[t] = NodeKeyT<Key>{g.NK.Lg, g.NK.bb, g.NK.lb}.make(b, x, y, z, label);
   vals[t] = (uint32_t)t;
 }
 
 // Sorted node-object keys -> run index per (element, object) and the
 // unique keys/multiplicities.
-__global__ void k_node_unique(long long m, const uint64_t *__restrict__ keys,
+template <typename Key>
+__global__ void k_node_unique(long long m, const Key *__restrict__ keys,
                               const uint32_t *__restrict__ vals,
                               const unsigned *__restrict__ pos, int lab_bits,
-                              int order, uint64_t *ukeys, unsigned *umult,
+                              int order, Key *ukeys, unsigned *umult,
                               unsigned *obj_of) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   unsigned idx = pos[i + 1] - 1;  // inclusive count - 1
   obj_of[vals[i]] = idx;
   if (pos[i + 1] != pos[i]) {
-    uint64_t k = keys[i];
+    const Key k = keys[i];
     ukeys[idx] = k;
-    int label = lab_bits ? (int)(k & 3) : 0;
+    int label = lab_bits ? (int)(klo64(k) & 3) : 0;
     int mm = order - 2;
     unsigned mult = (label == 0) ? 1u : (label == 1) ? mm : (label == 2) ? mm * mm : mm * mm * mm;
     umult[idx] = mult;
@@ -235,8 +239,8 @@ __global__ void k_node_unique(long long m, const uint64_t *__restrict__ keys,
 }
 
 // Flags for the unique pass (first entry of each run).
-__global__ void k_first_of_run(long long m, const uint64_t *__restrict__ keys,
-                               unsigned *flag) {
+template <typename Key>
+__global__ void k_first_of_run(long long m, const Key *__restrict__ keys, unsigned *flag) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < m) flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
 }
@@ -376,11 +380,14 @@ __global__ void k_label_dep(long long n, int order, int bern,
 struct DepCtx {
   int order;
   Labels lab;
-  NodeKey NK;
+  NodeKey NK;  // the node key layout; 128-bit keys where wide
   ConnDev c;
+  int wide;
   const uint64_t *ukeys;
+  const U128 *ukeys_w;
   long long nobj;
   SampledKeys idx;
+  SampledKeysT<U128> idx_w;
   const unsigned *noff;
   const unsigned *deprank;  // exclusive scan of dependent flags
   const unsigned *depflag;
@@ -397,9 +404,18 @@ __device__ __forceinline__ int find_object(const DepCtx &d, int32_t b, int32_t x
                                            int32_t y, int32_t z, int label,
                                            int edge_dir, int *rev, int *fid) {
   transform_node(d.c, b, x, y, z, edge_dir, rev, fid);
-  uint64_t k = d.NK.make(b, x, y, z, label);
-  long long i = d.idx.lower_bound(k);
-  if (i >= d.nobj || d.ukeys[i] != k) {
+  long long i;
+  bool found;
+  if (d.wide) {
+    const U128 k = NodeKeyT<U128>{d.NK.Lg, d.NK.bb, d.NK.lb}.make(b, x, y, z, label);
+    i = d.idx_w.lower_bound(k);
+    found = i < d.nobj && d.ukeys_w[i] == k;
+  } else {
+    const uint64_t k = d.NK.make(b, x, y, z, label);
+    i = d.idx.lower_bound(k);
+    found = i < d.nobj && d.ukeys[i] == k;
+  }
+  if (!found) {
     atomicExch(d.err, 1);
     return 0;
   }
@@ -735,6 +751,45 @@ void forest_get_points(Forest &f, const double *d_boxes, double *d_X) {
   TMRG_CUDA(cudaStreamSynchronize(s));
 }
 
+// Hanging-face/edge flags of every octant (section 1 of createNodes).
+template <typename Key>
+static void hanging_flags(Forest &f, const OctKeyT<Key> &K) {
+  cudaStream_t s = f.s;
+  const long long n = f.n;
+  DBuf<Key> okeys(n, s);
+  launch(k_oct_keys<Key>, blocks_for(n, 256), 256, 0, s, n, K, (const int *)f.block.p,
+         (const int *)f.x.p, (const int *)f.y.p, (const int *)f.z.p,
+         (const int16_t *)f.level.p, okeys.p);
+  launch(k_dep_info<Key>, blocks_for(n, 128), 128, 0, s, n, f.conn->dev, K,
+         (const Key *)okeys.p, (const int *)f.block.p, (const int *)f.x.p,
+         (const int *)f.y.p, (const int *)f.z.p, (const int16_t *)f.level.p, f.info.p);
+}
+
+// The distinct node objects (section 2): their sorted keys, multiplicities
+// (in noff) and each (element, object)'s index.  Returns their number.
+template <typename Key>
+static long long node_objects(Forest &f, const NodeGen &g, long long m, DBuf<Key> &ukeys,
+                              DBuf<unsigned> &noff, DBuf<unsigned> &obj_of) {
+  cudaStream_t s = f.s;
+  const long long n = f.n;
+  DBuf<Key> keys(m, s);
+  DBuf<uint32_t> vals(m, s);
+  launch(k_node_keys<Key>, blocks_for(m, 256), 256, 0, s, n, f.conn->dev, g,
+         (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
+         (const int *)f.z.p, (const int16_t *)f.level.p, keys.p, vals.p);
+  sort_keys(keys, &vals, m, g.NK.total_bits(), s);
+  DBuf<unsigned> pos(m + 1, s);
+  launch(k_first_of_run<Key>, blocks_for(m, 256), 256, 0, s, m, (const Key *)keys.p, pos.p);
+  exclusive_scan<unsigned>(pos.p, pos.p, m, s);
+  const long long nobj = read_scalar(pos.p + m, s);
+  ukeys.alloc(nobj, s);
+  noff.alloc(nobj + 1, s);
+  launch(k_node_unique<Key>, blocks_for(m, 256), 256, 0, s, m, (const Key *)keys.p,
+         (const uint32_t *)vals.p, (const unsigned *)pos.p, g.lab.bits, g.order, ukeys.p,
+         noff.p, obj_of.p);
+  return nobj;
+}
+
 void forest_create_nodes(Forest &f) {
   Stage st("tmrg_create_nodes");
   if (!f.have_octs)
@@ -749,19 +804,13 @@ void forest_create_nodes(Forest &f) {
   const long long n = f.n;
   const int o = f.order, npe = o * o * o;
   ConnDev c = f.conn->dev;
-  OctKey K = f.oct_key();
 
   // 1. hanging flags
-  {
-    DBuf<uint64_t> okeys(n, s);
-    launch(k_oct_keys, blocks_for(n, 256), 256, 0, s, n, K,
-           (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
-           (const int *)f.z.p, (const int16_t *)f.level.p, okeys.p);
-    launch(k_dep_info, blocks_for(n, 128), 128, 0, s, n, c, K,
-           (const uint64_t *)okeys.p, (const int *)f.block.p, (const int *)f.x.p,
-           (const int *)f.y.p, (const int *)f.z.p, (const int16_t *)f.level.p,
-           f.info.p);
-  }
+  const OctKey K = f.oct_key();
+  if (K.total_bits() > 64)
+    hanging_flags<U128>(f, OctKeyT<U128>{K.W, K.bb});
+  else
+    hanging_flags<uint64_t>(f, K);
 
   // 2. node objects
   NodeGen g;
@@ -771,32 +820,26 @@ void forest_create_nodes(Forest &f) {
   g.NK.Lg = f.maxlev + (o == 2 ? 0 : 1);
   g.NK.bb = f.conn->block_bits;
   g.NK.lb = g.lab.bits;
-  if (g.NK.total_bits() > 64)
+  if (g.NK.total_bits() > 128)
     throw Error(TMRG_ERR_KEY_RANGE, "node key needs " +
                                         std::to_string(g.NK.total_bits()) +
                                         " bits");
+  if (o > 2 && f.maxlev >= TMRG_MAX_LEVEL)
+    throw Error(TMRG_ERR_ARG, "createNodes: an order > 2 element at level " +
+                                  std::to_string(TMRG_MAX_LEVEL) +
+                                  " has no integer half-side for its nodes");
   const long long m = n * g.nobj;
   if (m >= (1LL << 32)) throw Error(TMRG_ERR_ARG, "createNodes: too many node objects");
-  DBuf<uint64_t> keys(m, s);
-  DBuf<uint32_t> vals(m, s);
-  launch(k_node_keys, blocks_for(m, 256), 256, 0, s, n, c, g,
-         (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
-         (const int *)f.z.p, (const int16_t *)f.level.p, keys.p, vals.p);
-  radix_sort(keys, &vals, m, g.NK.total_bits(), s);
-  DBuf<unsigned> pos(m + 1, s);
-  launch(k_first_of_run, blocks_for(m, 256), 256, 0, s, m,
-         (const uint64_t *)keys.p, pos.p);
-  exclusive_scan<unsigned>(pos.p, pos.p, m, s);
-  const long long nobj = read_scalar(pos.p + m, s);
-  DBuf<uint64_t> ukeys(nobj, s);
-  DBuf<unsigned> noff(nobj + 1, s);
+  const bool wide = g.NK.total_bits() > 64;
+  DBuf<uint64_t> ukeys;
+  DBuf<U128> ukeys_w;
+  DBuf<unsigned> noff;
   DBuf<unsigned> obj_of(m, s);
-  launch(k_node_unique, blocks_for(m, 256), 256, 0, s, m,
-         (const uint64_t *)keys.p, (const uint32_t *)vals.p,
-         (const unsigned *)pos.p, g.lab.bits, o, ukeys.p, noff.p, obj_of.p);
-  keys.release();
-  vals.release();
-  pos.release();
+  long long nobj;
+  if (wide)
+    nobj = node_objects<U128>(f, g, m, ukeys_w, noff, obj_of);
+  else
+    nobj = node_objects<uint64_t>(f, g, m, ukeys, noff, obj_of);
   exclusive_scan<unsigned>(noff.p, noff.p, nobj, s);
   const long long nl = read_scalar(noff.p + nobj, s);
   f.num_local = nl;
@@ -830,14 +873,27 @@ void forest_create_nodes(Forest &f) {
   d.lab = g.lab;
   d.NK = g.NK;
   d.c = c;
+  d.wide = wide ? 1 : 0;
   d.ukeys = ukeys.p;
+  d.ukeys_w = ukeys_w.p;
   d.nobj = nobj;
   const int S = 6;
   const long long ntop = (nobj + (1LL << S) - 1) >> S;
-  DBuf<uint64_t> top(ntop, s);
-  launch(k_sample_keys, blocks_for(ntop, 256), 256, 0, s, ntop, S,
-         (const uint64_t *)ukeys.p, top.p);
-  d.idx = SampledKeys{ukeys.p, nobj, top.p, ntop, S};
+  DBuf<uint64_t> top;
+  DBuf<U128> top_w;
+  d.idx = SampledKeys{nullptr, 0, nullptr, 0, S};
+  d.idx_w = SampledKeysT<U128>{nullptr, 0, nullptr, 0, S};
+  if (wide) {
+    top_w.alloc(ntop, s);
+    launch(k_sample_keys<U128>, blocks_for(ntop, 256), 256, 0, s, ntop, S,
+           (const U128 *)ukeys_w.p, top_w.p);
+    d.idx_w = SampledKeysT<U128>{ukeys_w.p, nobj, top_w.p, ntop, S};
+  } else {
+    top.alloc(ntop, s);
+    launch(k_sample_keys<uint64_t>, blocks_for(ntop, 256), 256, 0, s, ntop, S,
+           (const uint64_t *)ukeys.p, top.p);
+    d.idx = SampledKeys{ukeys.p, nobj, top.p, ntop, S};
+  }
   d.noff = noff.p;
   d.deprank = deprank.p;
   d.depflag = depflag.p;

@@ -8,6 +8,7 @@
 
 #include <nvtx3/nvToolsExt.h>
 
+#include <algorithm>
 #include <atomic>
 #include <functional>
 #include <utility>
@@ -534,6 +535,57 @@ inline void radix_sort(DBuf<K> &keys, DBuf<uint32_t> *vals, long long n, int nbi
     }, s);
     keys.swap(k2);
     if (vals) vals->swap(v2);
+  }
+}
+
+// Key sort over the two key widths: 64-bit keys go straight to the radix
+// sort; 128-bit keys are sorted as two stable LSD stages (the low word,
+// then the high word's remaining bits) that carry a permutation, which then
+// gathers the keys and values.
+inline void sort_keys(DBuf<uint64_t> &keys, DBuf<uint32_t> *vals, long long n, int nbits,
+                      cudaStream_t s) {
+  radix_sort(keys, vals, n, nbits, s);
+}
+static __global__ void k_split128(long long n, const U128 *__restrict__ k, uint64_t *lo,
+                                  uint64_t *hi, uint32_t *perm) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const U128 v = k[i];
+  lo[i] = v.lo;
+  hi[i] = v.hi;
+  perm[i] = (uint32_t)i;
+}
+template <typename T>
+__global__ void k_gather_perm(long long n, const uint32_t *__restrict__ perm,
+                              const T *__restrict__ in, T *out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = in[perm[i]];
+}
+inline void sort_keys(DBuf<U128> &keys, DBuf<uint32_t> *vals, long long n, int nbits,
+                      cudaStream_t s) {
+  if (n <= 1 || nbits <= 0) return;
+  if (n >= (1LL << 32)) throw Error(TMRG_ERR_ARG, "radix sort size >= 2^32");
+  DBuf<uint64_t> lo(n, s), hi(n, s);
+  DBuf<uint32_t> perm(n, s);
+  launch(k_split128, blocks_for(n, 256), 256, 0, s, n, (const U128 *)keys.p, lo.p, hi.p,
+         perm.p);
+  radix_sort(lo, &perm, n, std::min(nbits, 64), s);
+  if (nbits > 64) {
+    launch(k_gather_perm<uint64_t>, blocks_for(n, 256), 256, 0, s, n,
+           (const uint32_t *)perm.p, (const uint64_t *)hi.p, lo.p);
+    radix_sort(lo, &perm, n, nbits - 64, s);
+  }
+  lo.release();
+  hi.release();
+  DBuf<U128> k2(n, s);
+  launch(k_gather_perm<U128>, blocks_for(n, 256), 256, 0, s, n, (const uint32_t *)perm.p,
+         (const U128 *)keys.p, k2.p);
+  keys.swap(k2);
+  if (vals) {
+    DBuf<uint32_t> v2(n, s);
+    launch(k_gather_perm<uint32_t>, blocks_for(n, 256), 256, 0, s, n, (const uint32_t *)perm.p,
+           (const uint32_t *)vals->p, v2.p);
+    vals->swap(v2);
   }
 }
 

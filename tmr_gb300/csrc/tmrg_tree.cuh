@@ -251,9 +251,9 @@ __device__ __forceinline__ void transform_node(const ConnDev &c, int32_t &block,
   if (z == hmax) z = hmax - 1;
 }
 
-// lower_bound over a sorted u64 array.
-__device__ __forceinline__ long long lower_bound_u64(const uint64_t *a,
-                                                     long long n, uint64_t v) {
+// lower_bound over a sorted key array (uint64_t or U128).
+template <typename K>
+__device__ __forceinline__ long long lower_bound_key(const K *a, long long n, K v) {
   long long lo = 0, hi = n;
   while (lo < hi) {
     long long mid = (lo + hi) >> 1;
@@ -264,27 +264,35 @@ __device__ __forceinline__ long long lower_bound_u64(const uint64_t *a,
   }
   return lo;
 }
-__device__ __forceinline__ bool contains_u64(const uint64_t *a, long long n,
-                                             uint64_t v) {
-  long long i = lower_bound_u64(a, n, v);
+template <typename K>
+__device__ __forceinline__ bool contains_key(const K *a, long long n, K v) {
+  long long i = lower_bound_key(a, n, v);
   return i < n && a[i] == v;
+}
+__device__ __forceinline__ long long lower_bound_u64(const uint64_t *a, long long n,
+                                                     uint64_t v) {
+  return lower_bound_key(a, n, v);
+}
+__device__ __forceinline__ bool contains_u64(const uint64_t *a, long long n, uint64_t v) {
+  return contains_key(a, n, v);
 }
 
 // Two-level search over a large sorted array: `top` samples every
 // 2^S-th key (small enough to stay in L2), so a lookup touches the big
 // array only inside one 2^S-key segment.
-struct SampledKeys {
-  const uint64_t *keys;
+template <typename K>
+struct SampledKeysT {
+  const K *keys;
   long long n;
-  const uint64_t *top;
+  const K *top;
   long long ntop;
   int S;
-  __device__ __forceinline__ long long lower_bound(uint64_t v) const {
+  __device__ __forceinline__ long long lower_bound(K v) const {
     // last sample <= v
     long long lo = 0, hi = ntop;
     while (lo < hi) {
       long long mid = (lo + hi) >> 1;
-      if (__ldg(top + mid) <= v)
+      if (kldg(top + mid) <= v)
         lo = mid + 1;
       else
         hi = mid;
@@ -294,7 +302,7 @@ struct SampledKeys {
     long long a = seg << S, b = min(n, (seg + 1) << S);
     while (a < b) {
       long long mid = (a + b) >> 1;
-      if (__ldg(keys + mid) < v)
+      if (kldg(keys + mid) < v)
         a = mid + 1;
       else
         b = mid;
@@ -302,10 +310,10 @@ struct SampledKeys {
     return a;
   }
 };
+using SampledKeys = SampledKeysT<uint64_t>;
 
-static __global__ void k_sample_keys(long long ntop, int S,
-                                     const uint64_t *__restrict__ keys,
-                                     uint64_t *top) {
+template <typename K>
+__global__ void k_sample_keys(long long ntop, int S, const K *__restrict__ keys, K *top) {
   long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (j < ntop) top[j] = keys[j << S];
 }

@@ -90,6 +90,17 @@ def sphere_indicator(octs, centre=(0.5, 0.5, 0.5), radius=0.3):
     return ((((c - np.asarray(centre)) ** 2).sum(1)) < radius * radius).astype(np.intc)
 
 
+def point_indicator(octs, point):
+    """1 where the octant contains the block-local point (in [0, 1)^3, on
+    the 2^30 integer grid), in every block: one refinement path per block
+    down to any depth."""
+    p = np.floor(np.asarray(point, np.float64) * HMAX).astype(np.int64)
+    h = (np.int64(1) << (30 - octs[:, 5].astype(np.int64)))
+    xyz = octs[:, 1:4].astype(np.int64)
+    inside = ((xyz <= p[None, :]) & (p[None, :] < xyz + h[:, None])).all(1)
+    return inside.astype(np.intc)
+
+
 def random_indicator(n, seed, stream, prob):
     return (uniform(seed, stream, n) < prob).astype(np.intc)
 
