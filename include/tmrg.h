@@ -507,14 +507,19 @@ int64_t tmrg_device_alloc_count(void);
    json[cap]. */
 int tmrg_profile_begin(void);
 int tmrg_profile_end(char *json, int64_t cap);
-/* Autotuner of the applies' launch shapes and the filter's layout (no
-   counterpart in the reference): the first operation of each size class
-   on a device times every candidate shape once and the fastest is used
-   from then on.  reset clears the choices (enabled = 0 turns tuning off:
-   fixed default shapes); report writes a JSON list of the tuned classes
-   {"device", "kind", "key", "choice", "ms"} into json[cap]. */
+/* Autotuner of the applies' launch shapes, the filter's layout and the
+   radix scatter's shape (no counterpart in the reference): the first
+   operation of each size class on a device times every candidate shape
+   once and the fastest is used from then on.  reset clears the choices and
+   any forced candidate (enabled = 0 turns tuning off: fixed default
+   shapes); report writes a JSON list of the tuned classes {"device",
+   "kind", "key", "choice", "ms"} into json[cap]; force makes every
+   operation of `kind` (1 P apply, 2 P^T apply, 3/4 three-component filter
+   FP32/FP64, 5 radix scatter) run candidate `choice` (< 0: tuned again),
+   for tests that check each candidate. */
 int tmrg_tune_reset(int enabled);
 int tmrg_tune_report(char *json, int64_t cap);
+int tmrg_tune_force(int kind, int choice);
 /* FP64 FMA throughput of the current GPU in TFLOP/s (independent FMA
    chains, ~20 ms): the roofline denominator for FP64-pipe-bound kernels.
    No counterpart in the reference. */

@@ -146,3 +146,60 @@ def test_host_buffer_applies_in_pieces(gpu_lib):
     yt = np.zeros(ncols * k)
     I.multTranspose(xf, yt)
     np.testing.assert_allclose(yt, yt_ref, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.gpu
+def test_every_apply_shape_matches_oracle(gpu_lib):
+    # each launch shape the autotuner may pick, forced on the P and P^T
+    # applies (device pointers and the host-buffer pieces): the oracle's CSR
+    # products to 1e-13, and the TMA-staged shape (6) the same bits as the
+    # shape whose entry order it follows (4: 2 lanes x 4 pairs)
+    import ctypes
+
+    import bench
+    import torch
+
+    from oracle.oracle import _lib
+    from tmr_gb300 import TMR
+    case = bench.cpu_sample_case()
+    g = pipeline.run_gpu(dict(case, coarse_levels=1))
+    I = g["levels"][0]["I"]
+    rows, ncols, _ = I.sizes()
+    k = 16
+    rng = np.random.default_rng(31)
+    x = rng.standard_normal(ncols * k)
+    xf = rng.standard_normal(rows * k)
+    rp, cols, vals = I.getCSR()
+    L = _lib("oracle").lib
+    P_ = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    y_ref = np.zeros(rows * k)
+    L.oo_csr_mult(rows, P_(rp), P_(cols), P_(vals), k, P_(x), P_(y_ref))
+    yt_ref = np.zeros(ncols * k)
+    L.oo_csr_mult_t(rows, ncols, P_(rp), P_(cols), P_(vals), k, P_(xf), P_(yt_ref))
+    lib = TMR.lib()
+    xd = torch.tensor(x, device="cuda")
+    xfd = torch.tensor(xf, device="cuda")
+    out = {}
+    try:
+        for shape in range(7):
+            assert lib.tmrg_tune_force(1, shape) == 0 and lib.tmrg_tune_force(2, shape) == 0
+            yd = torch.empty(rows * k, dtype=torch.float64, device="cuda")
+            I.mult(xd, yd)
+            ytd = torch.empty(ncols * k, dtype=torch.float64, device="cuda")
+            I.multTranspose(xfd, ytd)
+            yh = np.zeros(rows * k)
+            I.mult(x, yh)  # pieces with copies back
+            yth = np.zeros(ncols * k)
+            I.multTranspose(xf, yth)  # input in pieces
+            y, yt = yd.cpu().numpy(), ytd.cpu().numpy()
+            np.testing.assert_allclose(y, y_ref, rtol=1e-13, atol=1e-13, err_msg="P %d" % shape)
+            np.testing.assert_allclose(yt, yt_ref, rtol=1e-13, atol=1e-13,
+                                       err_msg="PT %d" % shape)
+            np.testing.assert_array_equal(yh, y)
+            np.testing.assert_allclose(yth, yt_ref, rtol=1e-13, atol=1e-13)
+            out[shape] = (y, yt)
+    finally:
+        lib.tmrg_tune_force(1, -1)
+        lib.tmrg_tune_force(2, -1)
+    np.testing.assert_array_equal(out[6][0], out[4][0])
+    np.testing.assert_array_equal(out[6][1], out[4][1])

@@ -25,6 +25,7 @@ _SIGS = {
     "tmrg_device_alloc_count": [],
     "tmrg_tune_reset": [c_int],
     "tmrg_tune_report": [c_vp, c_i64],
+    "tmrg_tune_force": [c_int, c_int],
     "tmrg_profile_begin": [],
     "tmrg_profile_end": [c_vp, c_i64],
     "tmrg_measure_fp64_peak": [P(c_dbl)],

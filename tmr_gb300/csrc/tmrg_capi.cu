@@ -1031,11 +1031,13 @@ static int interp_host(tmrg_interp *I, int which, const double *x, double *y,
       // it computes, instead of a copy after it
       interp_apply(P, which, dx.p, ym, nvec);
       TMRG_CUDA(cudaStreamSynchronize(P.s));
+      interp_check_apply(P);
       return;
     }
     DBuf<double> dy(nout, P.s);
     interp_apply(P, which, dx.p, dy.p, nvec);
     copy_d2h(y, dy.p, sizeof(double) * nout, P.s);
+    interp_check_apply(P);
   });
 }
 static int interp_dev(tmrg_interp *I, int which, const double *x, double *y,

@@ -162,6 +162,7 @@ void interp_apply(Interp &I, int which, const double *x, double *y, int nvec);
 // keepoff (optional, device) holds their exclusive per-row offsets.
 void interp_finish(Interp &I, long long nonzeros, cudaStream_t s,
                    const long long *keepoff = nullptr);
+void interp_check_apply(Interp &I);
 bool interp_apply_transpose_staged(Interp &I, int which, const double *xh, double *dx,
                                    double *y, int nvec);
 bool interp_apply_forward_staged(Interp &I, const double *xh, double *dx, double *yh,

@@ -17,6 +17,8 @@
 // count, then write at the scanned offsets).  P^T is the apply copy
 // re-sorted by (column, row), so transpose applies gather without atomics
 // and sum in a fixed order.
+#include <cuda.h>  // CUtensorMap (the encoder is fetched from the driver at run time)
+
 #include <algorithm>
 
 #include "tmrg_tree.cuh"
@@ -1811,7 +1813,7 @@ void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long lon
   // dropped entries are a good part of P
   I.nnz_nz = (nnz - nonzeros) * 8 >= nnz ? nonzeros : nnz;
   const long long nnz_nz = I.nnz_nz;
-  I.dfflag.alloc(2, s);
+  I.dfflag.alloc(3, s);  // [0] weights, [1] inputs outside the double-float window, [2] TMA wait
   I.dfflag.zero();
   I.ap_w.alloc(nnz_nz + 1, s);
   // transpose sort records (column key, position, row) of every apply entry
@@ -2314,16 +2316,249 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ---------------------------------------------------------------------
+// The same apply (2 lanes per row, 4 vector pairs per lane: 16 vectors) with
+// the input rows staged in shared memory by the Tensor Memory Accelerator:
+// per warp a ring of TG_STAGES batches, a batch being entry b of the warp's
+// 16 rows (16 input rows of 128 bytes, four `cp.async.bulk.tensor ...
+// tile::gather4` copies of 4 rows each, completion counted on the stage's
+// mbarrier).  The warp issues the gathers TG_STAGES - 1 batches ahead of the
+// batch it sums, so the input latency is covered without registers; the
+// entry order and the renormalisation points are those of k_df_apply2<2, 1,
+// 4>, so the results are the same bits.  Every wait is bounded: a stage that
+// does not complete sets flags[2] (the host reports it) and the warp drains
+// the gathers it issued (bounded again) before it leaves.
+constexpr int TG_WARPS = 8, TG_STAGES = 4, TG_ROWB = 128, TG_BATCH = 16 * TG_ROWB;
+constexpr int TG_SMEM = TG_WARPS * TG_STAGES * TG_BATCH + TG_WARPS * TG_STAGES * 8;
+constexpr long long TG_WAIT_LIMIT = 1LL << 20;  // try_wait rounds before giving up
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *b, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_addr(b)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *b, unsigned parity) {
+  for (long long it = 0; it < TG_WAIT_LIMIT; it++)
+    if (mbar_try_wait(b, parity)) return true;
+  return false;
+}
+// Rows r0..r3 (columns from c0) of the 2-D tensor `map` to 4 consecutive
+// rows of shared memory at dst.
+__device__ __forceinline__ void tma_gather4(void *dst, const CUtensorMap *map, int c0, int r0,
+                                            int r1, int r2, int r3, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(r0), "r"(r1), "r"(r2), "r"(r3),
+      "r"(smem_addr(bar))
+      : "memory");
+}
+
+__global__ void __launch_bounds__(TG_WARPS * 32)
+    k_df_apply_tma(const __grid_constant__ CUtensorMap xmap, long long rows,
+                   const int *__restrict__ rowptr, const int *__restrict__ cols,
+                   const float2 *__restrict__ w, const double2 *__restrict__ x,
+                   double2 *__restrict__ y, const double *__restrict__ scale,
+                   const int *__restrict__ perm, int *flags) {
+  extern __shared__ __align__(128) uint8_t tg_smem[];
+  constexpr int PPL = 4, NV2 = 8;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint8_t *buf = tg_smem + warp * (TG_STAGES * TG_BATCH);
+  uint64_t *bar =
+      reinterpret_cast<uint64_t *>(tg_smem + TG_WARPS * TG_STAGES * TG_BATCH) + warp * TG_STAGES;
+  const long long slot0 = ((long long)blockIdx.x * TG_WARPS + warp) * 16;
+  if (slot0 >= rows) return;  // uniform per warp
+  const int i = lane >> 1, half = lane & 1;
+  const long long slot = slot0 + i;
+  const bool have = slot < rows;
+  const long long r = (have && perm) ? (long long)__ldg(perm + slot) : slot;
+  const int p0 = have ? __ldg(rowptr + r) : 0;
+  const int p1 = have ? __ldg(rowptr + r + 1) : 0;
+  int trips = p1 - p0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) trips = max(trips, __shfl_xor_sync(0xffffffffu, trips, o));
+  const int q0 = half * PPL;  // this lane's first pair
+  const bool f64 = (__ldg(flags) | __ldg(flags + 1)) != 0;
+  double ax[PPL], ay[PPL];
+  if (f64) {
+    // values outside the double-float window: the FP64 sums of k_df_apply2
+#pragma unroll
+    for (int j = 0; j < PPL; j++) ax[j] = ay[j] = 0.0;
+    for (int t = 0; t < trips; t++) {
+      const int p = p0 + t;
+      const bool on = have && p < p1;
+      const int c = on ? __ldg(cols + p) : 0;
+      const float2 wv = on ? __ldg(w + p) : make_float2(0.0f, 0.0f);
+      const double wd = __dadd_rn((double)wv.x, (double)wv.y);
+#pragma unroll
+      for (int j = 0; j < PPL; j++) {
+        const double2 xv = on ? __ldg(x + (long long)c * NV2 + q0 + j) : make_double2(0.0, 0.0);
+        ax[j] = __fma_rn(wd, xv.x, ax[j]);
+        ay[j] = __fma_rn(wd, xv.y, ay[j]);
+      }
+    }
+  } else {
+    if (lane < TG_STAGES) mbar_init(&bar[lane], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncwarp();
+    // lanes 0..15 hold the entry range of row `lane` for the gathers
+    const int g0 = __shfl_sync(0xffffffffu, p0, 2 * (lane & 15));
+    const int g1 = __shfl_sync(0xffffffffu, p1, 2 * (lane & 15));
+    auto issue = [&](int b) {
+      const int st = b % TG_STAGES;
+      const int c = (lane < 16 && g0 + b < g1) ? __ldg(cols + g0 + b) : 0;
+      const int c1 = __shfl_down_sync(0xffffffffu, c, 1);
+      const int c2 = __shfl_down_sync(0xffffffffu, c, 2);
+      const int c3 = __shfl_down_sync(0xffffffffu, c, 3);
+      if (lane == 0) mbar_expect_tx(&bar[st], TG_BATCH);
+      __syncwarp();
+      if (lane < 16 && (lane & 3) == 0)
+        tma_gather4(buf + st * TG_BATCH + lane * TG_ROWB, &xmap, 0, c, c1, c2, c3, &bar[st]);
+    };
+    const int pre = min(trips, TG_STAGES);
+    for (int b = 0; b < pre; b++) issue(b);
+    int issued = pre;
+    float ah[PPL], al[PPL], bh[PPL], bl[PPL];
+#pragma unroll
+    for (int j = 0; j < PPL; j++) ah[j] = al[j] = bh[j] = bl[j] = 0.0f;
+    int b = 0;
+    for (; b < trips; b++) {
+      const int st = b % TG_STAGES;
+      if (!mbar_wait_bounded(&bar[st], (unsigned)(b / TG_STAGES) & 1u)) {
+        if (lane == 0) atomicExch(flags + 2, 1);
+        break;
+      }
+      const int p = p0 + b;
+      const float2 wv = (have && p < p1) ? __ldg(w + p) : make_float2(0.0f, 0.0f);
+      const float4 *xr =
+          reinterpret_cast<const float4 *>(buf + st * TG_BATCH + i * TG_ROWB + half * 64);
+#pragma unroll
+      for (int j = 0; j < PPL; j++) {
+        const float4 xv = xr[j];
+        df_fma(wv.x, wv.y, xv.x, xv.y, ah[j], al[j]);
+        df_fma(wv.x, wv.y, xv.z, xv.w, bh[j], bl[j]);
+      }
+      if (b & 1) {  // k_df_apply2 renormalises after every two entries
+#pragma unroll
+        for (int j = 0; j < PPL; j++) {
+          df_renorm(ah[j], al[j]);
+          df_renorm(bh[j], bl[j]);
+        }
+      }
+      // this stage's reads are done before the gathers refill it
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (issued < trips) {
+        issue(issued);
+        issued++;
+      }
+    }
+    if (b < trips) {
+      // a stage timed out: wait (bounded) for the other gathers in flight
+      for (int bb = b + 1; bb < issued; bb++)
+        mbar_wait_bounded(&bar[bb % TG_STAGES], (unsigned)(bb / TG_STAGES) & 1u);
+    }
+#pragma unroll
+    for (int j = 0; j < PPL; j++) {
+      df_renorm(ah[j], al[j]);
+      df_renorm(bh[j], bl[j]);
+      ax[j] = df_value(ah[j], al[j]);
+      ay[j] = df_value(bh[j], bl[j]);
+    }
+  }
+  if (have) {
+    const double sc = scale ? scale[r] : 1.0;
+#pragma unroll
+    for (int j = 0; j < PPL; j++) {
+      double a = ax[j], bv = ay[j];
+      if (scale) {
+        a = (sc != 0.0) ? __ddiv_rn(a, sc) : 0.0;
+        bv = (sc != 0.0) ? __ddiv_rn(bv, sc) : 0.0;
+      }
+      y[r * NV2 + q0 + j] = make_double2(a, bv);
+    }
+  }
+}
+
+// The tensor map of the split input (rows of 16 float2 = 128 bytes) for the
+// gathers: UINT32 elements, box 32 x 1 (a gather4 box is one row high).
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(f);
+  }();
+  return fn;
+}
+static bool tma_apply(long long rows, long long nin, const int *rp, const int *ci,
+                      const float2 *w, const float2 *xs, const double *x, double *y,
+                      const double *scale, const int *perm, int *flags, cudaStream_t s) {
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc || nin <= 0 || nin >= (1LL << 31) || ((uintptr_t)xs % 16) != 0) return false;
+  CUtensorMap map;
+  const cuuint64_t dims[2] = {32, (cuuint64_t)nin};
+  const cuuint64_t strides[1] = {TG_ROWB};
+  const cuuint32_t box[2] = {32, 1};
+  const cuuint32_t estr[2] = {1, 1};
+  if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<float2 *>(xs), dims, strides, box,
+          estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  static bool attr = false;
+  if (!attr) {
+    TMRG_CUDA(cudaFuncSetAttribute(k_df_apply_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   TG_SMEM));
+    attr = true;
+  }
+  const long long rows_per_block = 16LL * TG_WARPS;
+  launch(k_df_apply_tma, (unsigned)((rows + rows_per_block - 1) / rows_per_block),
+         TG_WARPS * 32, TG_SMEM, s, map, rows, rp, ci, w, (const double2 *)x, (double2 *)y,
+         scale, perm, flags);
+  return true;
+}
+
 // Launch shapes for vector pairs (the autotuner's candidates): LPR lanes per
 // row holding PPL pairs each, NG groups of LPR lanes splitting a row's
 // entries, 32 / (LPR NG) rows per warp; with `perm` the rows sharing a warp
 // come from the length-ordered permutation.
 // 8 or more pairs (16+ vectors): {8,1,1} {8,2,1} {8,4,1} {4,1,2} {2,1,4}
-// {1,1,8}; fewer pairs: LPR = pairs rounded down to a power of two, NG 1 or 2
-constexpr int DF2_SHAPES_WIDE = 6, DF2_SHAPES_NARROW = 2;
+// {1,1,8}, and for exactly 8 pairs {2,1,4} with TMA-staged inputs
+// (k_df_apply_tma); fewer pairs: LPR = pairs rounded down to a power of
+// two, NG 1 or 2
+constexpr int DF2_SHAPES_WIDE = 7, DF2_SHAPES_NARROW = 2;
 static void df_apply2(int shape, long long rows, int nvec2, const int *rp, const int *ci,
                       const float2 *w, const float2 *xs, const double *x, double *y,
-                      const double *scale, const int *perm, const int *flags, cudaStream_t s) {
+                      const double *scale, const int *perm, int *flags, cudaStream_t s,
+                      long long nin) {
+  if (shape == 6 && nvec2 == 8 &&
+      tma_apply(rows, nin, rp, ci, w, xs, x, y, scale, perm, flags, s))
+    return;
   const float4 *x4 = (const float4 *)xs;
   const double2 *x2 = (const double2 *)x;
   double2 *y2 = (double2 *)y;
@@ -2337,8 +2572,8 @@ static void df_apply2(int shape, long long rows, int nvec2, const int *rp, const
       case 1: TMRG_DF2(8, 2, 1); break;
       case 2: TMRG_DF2(8, 4, 1); break;
       case 3: TMRG_DF2(4, 1, 2); break;
-      case 4: TMRG_DF2(2, 1, 4); break;
-      default: TMRG_DF2(1, 1, 8);
+      case 5: TMRG_DF2(1, 1, 8); break;
+      default: TMRG_DF2(2, 1, 4);  // 4, and 6 where the staged kernel does not apply
     }
   } else if (nvec2 >= 4) {
     if (shape == 0)
@@ -2385,6 +2620,15 @@ static void df_split_input(Interp &I, const double *x, long long n, DBuf<float2>
 // only reads pieces already split, so a row never runs in double-float on
 // an input that was not represented).
 // Returns false (nothing done) where the grouped kernel does not apply.
+// Reports (and clears) a TMA input stage of k_df_apply_tma that did not
+// complete within its wait limit; read where the host already waits.
+void interp_check_apply(Interp &I) {
+  if (read_scalar(I.dfflag.p + 2, I.s)) {
+    TMRG_CUDA(cudaMemsetAsync(I.dfflag.p + 2, 0, sizeof(int), I.s));
+    throw Error(TMRG_ERR_INTERNAL, "P apply: a staged input batch did not arrive");
+  }
+}
+
 bool interp_apply_transpose_staged(Interp &I, int which, const double *xh, double *dx,
                                    double *y, int nvec) {
   if ((which != 1 && which != 2) || nvec % 2 != 0 || nvec / 2 < 8 ||
@@ -2426,11 +2670,12 @@ bool interp_apply_transpose_staged(Interp &I, int which, const double *xh, doubl
     const long long a = I.t_chunk[k], n = I.t_chunk[k + 1] - a;
     if (n > 0)
       df_apply2(shape, n, nvec / 2, I.t_rowptr.p, I.t_colidx.p, I.t_w.p, xs.p, dx, y, sc,
-                I.t_perm.p + a, I.dfflag.p, s);
+                I.t_perm.p + a, I.dfflag.p, s, nin);
   }
   TMRG_CUDA(cudaStreamSynchronize(s));
   for (int k = 0; k <= TC_CHUNKS; k++) cudaEventDestroy(ev[k]);
   cudaStreamDestroy(cs);
+  interp_check_apply(I);
   return true;
 }
 
@@ -2472,7 +2717,7 @@ bool interp_apply_forward_staged(Interp &I, const double *xh, double *dx, double
     if (r1 > r0) {
       prof_bytes(12 * I.nnz_nz * (r1 - r0) / rows + 4 * (r1 - r0) + 8LL * nvec * (r1 - r0));
       df_apply2(shape, r1 - r0, n2, I.ap_rowptr(), I.ap_colidx(), I.ap_w.p, xs.p, dx, y,
-                nullptr, I.perm.p + r0, I.dfflag.p, s);
+                nullptr, I.perm.p + r0, I.dfflag.p, s, nin);
     }
     TMRG_CUDA(cudaEventRecord(ev[k], s));
     TMRG_CUDA(cudaStreamWaitEvent(cs, ev[k], 0));
@@ -2484,6 +2729,7 @@ bool interp_apply_forward_staged(Interp &I, const double *xh, double *dx, double
   TMRG_CUDA(cudaStreamSynchronize(s));
   for (int k = 0; k < FC_CHUNKS; k++) cudaEventDestroy(ev[k]);
   cudaStreamDestroy(cs);
+  interp_check_apply(I);
   return true;
 }
 
@@ -2511,7 +2757,7 @@ void interp_apply(Interp &I, int which, const double *x, double *y, int nvec) {
     const int n2 = nvec / 2;
     tune_run(df_key(which, nout, I.nnz_nz, n2), n2 >= 8 ? DF2_SHAPES_WIDE : DF2_SHAPES_NARROW,
              [&](int shape) {
-               df_apply2(shape, nout, n2, rp, ci, w, xs.p, x, y, sc, perm, I.dfflag.p, s);
+               df_apply2(shape, nout, n2, rp, ci, w, xs.p, x, y, sc, perm, I.dfflag.p, s, nin);
              },
              s);
     return;

@@ -27,6 +27,7 @@ struct Entry {
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int, int, int, int>, Entry> g_tune;
 bool g_tune_on = true;
+std::map<int, int> g_force;  // kind -> candidate every operation of the kind uses
 }  // namespace
 
 int tune_run(const TuneKey &k, int ncand, const std::function<void(int)> &run,
@@ -37,7 +38,10 @@ int tune_run(const TuneKey &k, int ncand, const std::function<void(int)> &run,
   int choice = -1;
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    if (!g_tune_on || ncand <= 1) {
+    auto f = g_force.find(k.kind);
+    if (f != g_force.end() && f->second < ncand) {
+      choice = f->second;
+    } else if (!g_tune_on || ncand <= 1) {
       choice = ncand <= 1 ? 0 : k.fallback;
     } else {
       auto it = g_tune.find(key);
@@ -81,6 +85,8 @@ int tune_lookup(const TuneKey &k) {
   int dev = 0;
   TMRG_CUDA(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto f = g_force.find(k.kind);
+  if (f != g_force.end()) return f->second;
   if (!g_tune_on) return k.fallback;
   auto it = g_tune.find(std::make_tuple(dev, k.kind, k.a, k.b, k.c, k.d));
   return it != g_tune.end() ? it->second.choice : k.fallback;
@@ -100,7 +106,20 @@ extern "C" {
 int tmrg_tune_reset(int enabled) {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tune.clear();
+  g_force.clear();
   g_tune_on = enabled != 0;
+  return TMRG_OK;
+}
+
+// Every operation of `kind` runs candidate `choice` (choice < 0: back to
+// the tuned choice); a candidate index beyond the operation's count is
+// ignored.  For tests that check each candidate against the oracle.
+int tmrg_tune_force(int kind, int choice) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (choice < 0)
+    g_force.erase(kind);
+  else
+    g_force[kind] = choice;
   return TMRG_OK;
 }
 
