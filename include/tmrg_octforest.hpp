@@ -343,6 +343,48 @@ class TMROctForest : public TMRGEntity {
     if (tmrg_report(tmrg_forest_set_block_boxes(f, boxes, nblocks), "setBlockBoxes"))
       boxes_.assign(boxes, boxes + (size_t)(boxes ? 6 * nblocks : 0));
   }
+  // writeToTecplot (TMROctForest.cpp:1233-1311): the block mesh as one
+  // Tecplot FEBRICK zone, each connectivity node at its owner block's
+  // corner (the lowest-numbered block touching it) mapped through the
+  // block's box, and the block index as a cell-centred variable.  Nothing
+  // is written when no block boxes are set (the reference needs a topology).
+  void writeToTecplot(const char *filename) {
+    if (boxes_.empty()) return;
+    int nb = 0, nf = 0, ne = 0, nn = 0;
+    const int *bc = nullptr, *bf = nullptr, *be = nullptr, *fid = nullptr;
+    getConnectivity(&nb, &nf, &ne, &nn, &bc, &bf, &be, &fid);
+    if (!bc) return;
+    FILE *fp = filename ? fopen(filename, "w") : nullptr;
+    if (!fp) return;
+    std::vector<int> owner(nn, nb);
+    for (int b = 0; b < nb; b++)
+      for (int c = 0; c < 8; c++)
+        if (b < owner[bc[8 * b + c]]) owner[bc[8 * b + c]] = b;
+    std::vector<double> X(3 * (size_t)nn, 0.0);
+    for (int k = 0; k < nn; k++) {
+      const int b = owner[k];
+      if (b >= nb) continue;
+      int corner = 0;
+      while (corner < 8 && bc[8 * b + corner] != k) corner++;
+      const double uvw[3] = {1.0 * (corner & 1), 1.0 * ((corner >> 1) & 1),
+                             1.0 * (corner >> 2)};
+      for (int d = 0; d < 3; d++)
+        X[3 * k + d] = boxes_[6 * b + d] + boxes_[6 * b + 3 + d] * uvw[d];
+    }
+    fprintf(fp, "Variables = X,Y,Z,block\n");
+    fprintf(fp, "Zone N = %d E = %d ", nn, nb);
+    fprintf(fp, "DATAPACKING=BLOCK, ZONETYPE=FEBRICK\n");
+    fprintf(fp, "VARLOCATION = ([4]=CELLCENTERED)\n");
+    for (int d = 0; d < 3; d++)
+      for (int k = 0; k < nn; k++) fprintf(fp, "%e\n", X[3 * k + d]);
+    for (int k = 0; k < nb; k++) fprintf(fp, "%e\n", 1.0 * k);
+    for (int k = 0; k < nb; k++) {
+      const int *c = bc + 8 * k;
+      fprintf(fp, "%d %d %d %d %d %d %d %d\n", c[0] + 1, c[1] + 1, c[3] + 1, c[2] + 1,
+              c[4] + 1, c[5] + 1, c[7] + 1, c[6] + 1);
+    }
+    fclose(fp);
+  }
   // writeForestToVTK (TMROctForest.cpp:1317-1384): every octant as a
   // hexahedron with its own eight corners (x fastest) mapped through its
   // block's box, and the block index as the cell scalar entity_index.

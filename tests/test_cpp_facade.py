@@ -31,7 +31,9 @@ def test_facade_compiles_and_links(tmp_path):
 @pytest.mark.gpu
 def test_facade_matches_python_binding(gpu_lib, tmp_path):
     exe = _build(tmp_path)
-    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
+    vtk, tec = str(tmp_path / "cpp.vtk"), str(tmp_path / "cpp.dat")
+    out = subprocess.run([exe, vtk, tec], check=True, capture_output=True,
+                         text=True).stdout.split()
     vals = dict(zip(out[0::2], out[1::2]))
     from tmr_gb300 import TMR
     from tmr_gb300 import workloads as W
@@ -66,6 +68,16 @@ def test_facade_matches_python_binding(gpu_lib, tmp_path):
     assert float(vals["du"]) == pytest.approx(0.0, abs=1e-13)
     assert int(vals["enclosed_self"]) == 1
     assert int(vals["corner_block"]) == 0
+    # the same files from the Python binding with the same block boxes
+    nb = bc.shape[0]
+    boxes = np.zeros((nb, 6))
+    boxes[:, 0] = np.arange(nb)
+    boxes[:, 3:] = 1.0
+    f.setBlockBoxes(boxes)
+    f.writeForestToVTK(str(tmp_path / "py.vtk"))
+    f.writeToTecplot(str(tmp_path / "py.dat"))
+    assert open(tec).read() == (tmp_path / "py.dat").read_text()
+    assert open(vtk).read() == (tmp_path / "py.vtk").read_text()
 
 
 @pytest.mark.gpu

@@ -276,3 +276,36 @@ def test_write_forest_to_vtk(gpu_lib, tmp_path):
     e = lines.index("SCALARS entity_index float 1")
     ent = np.array([float(v) for v in lines[e + 2:e + 2 + n]])
     np.testing.assert_array_equal(ent, o[:, 0])
+
+
+def test_write_to_tecplot(gpu_lib, tmp_path):
+    """writeToTecplot: the block mesh, each connectivity node at its owner
+    block's corner (lowest-numbered block touching it) through the block
+    boxes, the block index cell-centred, corners in the reference's
+    (0 1 3 2 4 5 7 6) order counted from 1; nothing without block boxes."""
+    from tmr_gb300 import TMR
+    conn = W.rotate_blocks(W.brick(3, 2, 2), 8)
+    f = TMR.OctForest(order=2)
+    f.setConnectivity(conn)
+    fn = tmp_path / "blocks.dat"
+    f.writeToTecplot(str(fn))
+    assert not fn.exists()
+    boxes = pipeline.brick_boxes(3, 2, 2, ext=(2.0, 1.0, 0.5))
+    f.setBlockBoxes(boxes)
+    f.writeToTecplot(str(fn))
+    lines = fn.read_text().split("\n")
+    nb, nn = conn.shape[0], int(conn.max()) + 1
+    assert lines[0] == "Variables = X,Y,Z,block"
+    assert lines[1] == "Zone N = %d E = %d DATAPACKING=BLOCK, ZONETYPE=FEBRICK" % (nn, nb)
+    assert lines[2] == "VARLOCATION = ([4]=CELLCENTERED)"
+    vals = np.array([float(v) for v in lines[3:3 + 3 * nn + nb]])
+    X = vals[:3 * nn].reshape(3, nn).T
+    for k in range(nn):
+        b = min(np.argwhere(conn == k)[:, 0])
+        c = int(np.argwhere(conn[b] == k)[0, 0])
+        uvw = np.array([c & 1, (c >> 1) & 1, c >> 2], np.float64)
+        np.testing.assert_allclose(X[k], boxes[b, :3] + boxes[b, 3:] * uvw, rtol=1e-6)
+    np.testing.assert_array_equal(vals[3 * nn:], np.arange(nb))
+    cells = np.array([[int(v) for v in ln.split()] for ln in lines[3 + 3 * nn + nb:3 + 3 * nn + 2 * nb]])
+    np.testing.assert_array_equal(cells, conn[:, [0, 1, 3, 2, 4, 5, 7, 6]] + 1)
+

@@ -489,6 +489,42 @@ class OctForest:
             fp.write("12\n" * len(o))
 
 
+    def writeToTecplot(self, fname):
+        """writeToTecplot (TMROctForest.cpp:1233-1311): the block mesh as one
+        Tecplot FEBRICK zone, each block connectivity node at its owner
+        block's corner (the lowest-numbered block touching it) mapped
+        through that block's volume, and the block index as a cell-centred
+        variable.  The block boxes (setBlockBoxes) stand in for the
+        topology's volumes; nothing is written when no boxes are set."""
+        boxes = getattr(self, "_boxes", None)
+        if boxes is None:
+            return
+        bc = self.getConnectivity()[0]
+        nb = bc.shape[0]
+        nn = int(bc.max()) + 1 if nb else 0
+        owner = np.full(nn, nb, np.int64)
+        np.minimum.at(owner, bc.ravel(), np.repeat(np.arange(nb), 8))
+        X = np.zeros((nn, 3))
+        for k in range(nn):
+            b = owner[k]
+            corner = next(c for c in range(8) if bc[b, c] == k)
+            uvw = np.array([corner & 1, (corner >> 1) & 1, corner >> 2], np.float64)
+            X[k] = boxes[b, :3] + boxes[b, 3:] * uvw
+        with open(fname, "w") as fp:
+            fp.write("Variables = X,Y,Z,block\n")
+            fp.write("Zone N = %d E = %d " % (nn, nb))
+            fp.write("DATAPACKING=BLOCK, ZONETYPE=FEBRICK\n")
+            fp.write("VARLOCATION = ([4]=CELLCENTERED)\n")
+            for d in range(3):
+                for k in range(nn):
+                    fp.write("%e\n" % X[k, d])
+            for k in range(nb):
+                fp.write("%e\n" % (1.0 * k))
+            for k in range(nb):
+                c = bc[k] + 1
+                fp.write("%d %d %d %d %d %d %d %d\n" % (c[0], c[1], c[3], c[2], c[4], c[5],
+                                                         c[7], c[6]))
+
     def writeForestToVTK(self, fname):
         """writeForestToVTK (TMROctForest.cpp:1317-1384): every octant as a
         hexahedron with its own eight corner points (x fastest), mapped
