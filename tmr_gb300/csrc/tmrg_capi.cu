@@ -2,9 +2,14 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <unistd.h>
+
+#include <algorithm>
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "tmrg_internal.h"
@@ -150,6 +155,7 @@ static int guarded(Fn &&fn) {
 
 // Device-usable address of page-locked host memory (cudaMallocHost,
 // cudaHostAlloc, registered), or null for any other pointer.
+static std::atomic<unsigned> g_warm_sink{0};
 static void *host_mapped(void *p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -158,8 +164,41 @@ static void *host_mapped(void *p) {
   }
   return (a.type == cudaMemoryTypeHost) ? a.devicePointer : nullptr;
 }
+// One read per OS page of a large page-locked host buffer, on a few host
+// threads, before the copy engine moves it.  On guests whose kernel samples
+// page accesses in the background (clearing the pages' accessed state),
+// page-locked memory last touched by the CPU some seconds earlier was
+// measured to copy at 31-91 GB/s instead of the link's 210, and a CPU read
+// pass over it restored the full rate; the pass costs a few milliseconds
+// against the ~36 ms a 7.7 GB copy takes.  Pageable memory is skipped (the
+// driver stages it through the CPU anyway).
+static void host_warm(const void *p, size_t bytes) {
+  if (!p || bytes < ((size_t)16 << 20) || !host_mapped(const_cast<void *>(p))) return;
+  static const size_t pg = [] {
+    long v = sysconf(_SC_PAGESIZE);
+    return v > 0 ? (size_t)v : (size_t)4096;
+  }();
+  const volatile unsigned char *c = (const volatile unsigned char *)p;
+  const size_t npg = (bytes + pg - 1) / pg;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const unsigned nt = bytes >= ((size_t)256 << 20) ? std::min(8u, hw) : 1u;
+  std::vector<unsigned> sums(nt, 0u);
+  auto run = [&](unsigned t) {
+    unsigned acc = 0;
+    for (size_t i = t; i < npg; i += nt) acc += c[std::min(i * pg, bytes - 1)];
+    sums[t] = acc;
+  };
+  std::vector<std::thread> th;
+  for (unsigned t = 1; t < nt; t++) th.emplace_back(run, t);
+  run(0);
+  for (auto &x : th) x.join();
+  unsigned tot = 0;
+  for (unsigned v : sums) tot += v;
+  g_warm_sink.fetch_add(tot, std::memory_order_relaxed);
+}
 static void copy_d2h(void *dst, const void *src, size_t bytes, cudaStream_t s) {
   if (!bytes) return;
+  host_warm(dst, bytes);
   TMRG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
   TMRG_CUDA(cudaStreamSynchronize(s));
 }
@@ -726,6 +765,7 @@ int tmrg_forest_octants_host(tmrg_forest *f, const tmrg_octant **octs, int64_t *
              (const int *)F.block.p, (const int *)F.x.p, (const int *)F.y.p,
              (const int *)F.z.p, (const int16_t *)F.level.p, (const int16_t *)F.info.p,
              d.p);
+      host_warm(f->m.octs.p, sizeof(tmrg_octant) * (size_t)F.n);
       if (F.n)
         TMRG_CUDA(cudaMemcpyAsync(f->m.octs.p, d.p, sizeof(tmrg_octant) * (size_t)F.n,
                                   cudaMemcpyDeviceToHost, F.s));
@@ -743,6 +783,7 @@ static void conn_mirror(tmrg_forest *f) {
   f->m.conn_gen = ~0ULL;
   const size_t nconn = (size_t)F.n * F.order * F.order * F.order;
   pin_ensure(f->m.conn, sizeof(int) * nconn);
+  host_warm(f->m.conn.p, sizeof(int) * nconn);
   if (nconn)
     TMRG_CUDA(cudaMemcpyAsync(f->m.conn.p, F.econn.p, sizeof(int) * nconn,
                               cudaMemcpyDeviceToHost, F.s));
@@ -760,6 +801,8 @@ static void dep_mirror(tmrg_forest *f) {
   TMRG_CUDA(cudaMemcpyAsync(f->m.dptr.p, F.dep_ptr.p, sizeof(int) * ((size_t)F.num_dep + 1),
                             cudaMemcpyDeviceToHost, F.s));
   if (F.dep_nnz) {
+    host_warm(f->m.dconn.p, sizeof(int) * (size_t)F.dep_nnz);
+    host_warm(f->m.dw.p, sizeof(double) * (size_t)F.dep_nnz);
     TMRG_CUDA(cudaMemcpyAsync(f->m.dconn.p, F.dep_conn.p, sizeof(int) * (size_t)F.dep_nnz,
                               cudaMemcpyDeviceToHost, F.s));
     TMRG_CUDA(cudaMemcpyAsync(f->m.dw.p, F.dep_w.p, sizeof(double) * (size_t)F.dep_nnz,
@@ -1011,6 +1054,8 @@ static int interp_host(tmrg_interp *I, int which, const double *x, double *y,
     long long nout = (which == 0 ? P.rows : P.cols) * nvec;
     DBuf<double> dx(nin, P.s);
     double *ym = (double *)host_mapped(y);
+    host_warm(x, sizeof(double) * nin);
+    host_warm(y, sizeof(double) * nout);
     if (which != 0) {
       // restriction: copy the input in pieces overlapped with the rows
       // they complete
@@ -1137,6 +1182,7 @@ static int filter_host(tmrg_filter *F, bool tr, int vpn, const double *in,
     Filter &M = F->F;
     long long len = M.n * vpn;
     DBuf<double> a(len, M.s), b(len, M.s);
+    host_warm(in, sizeof(double) * len);
     TMRG_CUDA(cudaMemcpyAsync(a.p, in, sizeof(double) * len,
                               cudaMemcpyHostToDevice, M.s));
     filter_apply(M, tr, vpn, a.p, b.p);
