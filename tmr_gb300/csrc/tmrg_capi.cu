@@ -1323,6 +1323,7 @@ int tmrg_qforest_refine(tmrg_qforest *f, const int *refine, int64_t n, int min_l
     }
     DBuf<int> d(std::max<int64_t>(n, 1), F.s);
     if (n)
+      host_warm(refine, sizeof(int) * n);
       TMRG_CUDA(cudaMemcpyAsync(d.p, refine, sizeof(int) * n, cudaMemcpyHostToDevice, F.s));
     qforest_refine(F, d.p, n, min_level, max_level);
   });
