@@ -17,6 +17,8 @@ def indicator(octs, case, p):
         return W.sphere_indicator(octs)
     if case.get("indicator") == "point":
         return W.point_indicator(octs, case["point"])
+    if case.get("indicator") == "qpoint":
+        return W.quad_point_indicator(octs, case["point"])
     if case.get("indicator") == "mixed":
         return W.mixed_indicator(len(octs), case.get("seed", 0), p, case.get("prob", 0.3),
                                  case.get("coarsen_prob", 0.3))
@@ -426,6 +428,13 @@ def quad_cases():
         "mixed_o2": dict(conn=W.rotate_faces(W.brick2d(4, 3), 6), order=2, L0=2, passes=3,
                          max_level=6, indicator="mixed", prob=0.35, coarsen_prob=0.3, seed=13,
                          coarse_levels=2),
+        # deeper than 64-bit keys hold (quadrant keys of face bits + 2W + 5
+        # bits, node keys of face bits + 2(W + 1)): refinement paths toward
+        # one face-local point, the coarse levels crossing back to 64-bit keys
+        "deep_o2": dict(conn=W.rotate_faces(W.brick2d(8, 4), 14), order=2, L0=0, passes=29,
+                        max_level=29, indicator="qpoint", point=[0.999, 0.31], coarse_levels=2),
+        "deep_o3": dict(conn=W.brick2d(8, 4), order=3, L0=0, passes=28, max_level=28,
+                        indicator="qpoint", point=[0.42, 0.0001], coarse_levels=2),
     }
 
 

@@ -95,38 +95,43 @@ HD int cmp_position2(int32_t ab, int32_t ax, int32_t ay, int32_t bb, int32_t bx,
   return d > 0 ? 1 : (d < 0 ? -1 : 0);
 }
 
+// Keys are 64-bit where the face bits and levels fit and 128-bit (U128)
+// otherwise; the Morton part (2 x 31 bits at most) always fits one word.
 // [face | morton(2W) | level(5)]
-struct QKey {
+template <typename Key>
+struct QKeyT {
   int W, bb;
   HD int total_bits() const { return bb + 2 * W + 5; }
-  HD uint64_t make(int32_t b, int32_t x, int32_t y, int level) const {
+  HD Key make(int32_t b, int32_t x, int32_t y, int level) const {
     int s = TMRG_MAX_LEVEL - W;
-    return ((uint64_t)(uint32_t)b << (2 * W + 5)) |
-           (morton2((uint32_t)x >> s, (uint32_t)y >> s) << 5) | (uint64_t)level;
+    return (Key((uint64_t)(uint32_t)b) << (2 * W + 5)) |
+           (Key(morton2((uint32_t)x >> s, (uint32_t)y >> s)) << 5) | Key((uint64_t)level);
   }
-  HD Quad decode(uint64_t k) const {
+  HD Quad decode(Key k) const {
     int s = TMRG_MAX_LEVEL - W;
     Quad q;
-    q.level = (int)(k & 31);
-    uint64_t m = (k >> 5) & ((1ULL << (2 * W)) - 1);
+    q.level = (int)(klo64(k) & 31);
+    const uint64_t m = klo64((k >> 5) & kmask<Key>(2 * W));
     q.x = (int32_t)(compact2(m >> 1) << s);
     q.y = (int32_t)(compact2(m) << s);
-    q.block = (int32_t)(k >> (2 * W + 5));
+    q.block = (int32_t)klo64(k >> (2 * W + 5));
     return q;
   }
 };
 // family position [face | morton(2W)]
+template <typename Key>
 struct QPos {
   int W, bb;
-  HD uint64_t make(int32_t b, int32_t x, int32_t y) const {
+  HD Key make(int32_t b, int32_t x, int32_t y) const {
     int s = TMRG_MAX_LEVEL - W;
-    return ((uint64_t)(uint32_t)b << (2 * W)) | morton2((uint32_t)x >> s, (uint32_t)y >> s);
+    return (Key((uint64_t)(uint32_t)b) << (2 * W)) |
+           Key(morton2((uint32_t)x >> s, (uint32_t)y >> s));
   }
-  HD Quad decode(uint64_t k, int level) const {
+  HD Quad decode(Key k, int level) const {
     int s = TMRG_MAX_LEVEL - W;
-    uint64_t m = k & ((1ULL << (2 * W)) - 1);
+    const uint64_t m = klo64(k & kmask<Key>(2 * W));
     Quad q;
-    q.block = (int32_t)(k >> (2 * W));
+    q.block = (int32_t)klo64(k >> (2 * W));
     q.x = (int32_t)(compact2(m >> 1) << s);
     q.y = (int32_t)(compact2(m) << s);
     q.level = level;
@@ -135,21 +140,31 @@ struct QPos {
 };
 // node objects [face | morton(2(Lg+1))], coordinates on the node grid with
 // hmax - 1 mapped to all ones (TMRQuadrant::compareNode order).
-struct QNodeKey {
+template <typename Key>
+struct QNodeKeyT {
   int Lg, bb;
   HD uint32_t map(int32_t c) const {
     if (c == TMRG_HMAX - 1) return (1u << (Lg + 1)) - 1u;
     return ((uint32_t)c >> (TMRG_MAX_LEVEL - Lg)) << 1;
   }
   HD int total_bits() const { return bb + 2 * (Lg + 1); }
-  HD uint64_t make(int32_t b, int32_t x, int32_t y) const {
-    return ((uint64_t)(uint32_t)b << (2 * (Lg + 1))) | morton2(map(x), map(y));
+  HD Key make(int32_t b, int32_t x, int32_t y) const {
+    return (Key((uint64_t)(uint32_t)b) << (2 * (Lg + 1))) | Key(morton2(map(x), map(y)));
   }
 };
+using QNodeKey = QNodeKeyT<uint64_t>;
 
 QKey QForest::key() const {
   int W = std::max(maxlev, 1);
-  return QKey{W, conn ? conn->block_bits : 1};
+  QKey k{W, conn ? conn->block_bits : 1};
+  if (k.total_bits() > 128)
+    throw Error(TMRG_ERR_KEY_RANGE,
+                "quadrant key needs " + std::to_string(k.total_bits()) + " bits");
+  return k;
+}
+template <typename Key>
+static QKeyT<Key> qkey_as(const QKey &k) {
+  return QKeyT<Key>{k.W, k.bb};
 }
 
 // ---------------------------------------------------------------------
@@ -450,11 +465,11 @@ __global__ void k_q_refine_count(long long n, QRefineArgs a, const int16_t *__re
   for (int o = 16; o > 0; o >>= 1) ml = max(ml, __shfl_down_sync(0xffffffffu, ml, o));
   if ((threadIdx.x & 31) == 0 && ml > 0) atomicMax(maxlev, ml);
 }
-__global__ void k_q_refine_emit(long long n, QRefineArgs a, QKey K, const int *__restrict__ blk,
-                                const int *__restrict__ xs, const int *__restrict__ ys,
-                                const int16_t *__restrict__ lev,
-                                const unsigned *__restrict__ offs, uint64_t *keys,
-                                uint32_t *vals) {
+template <typename Key>
+__global__ void k_q_refine_emit(long long n, QRefineArgs a, QKeyT<Key> K,
+                                const int *__restrict__ blk, const int *__restrict__ xs,
+                                const int *__restrict__ ys, const int16_t *__restrict__ lev,
+                                const unsigned *__restrict__ offs, Key *keys, uint32_t *vals) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int level = lev[i];
@@ -476,10 +491,11 @@ __global__ void k_q_refine_emit(long long n, QRefineArgs a, QKey K, const int *_
     }
 }
 // first of a run of equal keys, if that run is the finest at its position
-__global__ void k_q_dedupe(long long n, const uint64_t *__restrict__ keys, unsigned *flag) {
+template <typename Key>
+__global__ void k_q_dedupe(long long n, const Key *__restrict__ keys, unsigned *flag) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  uint64_t k = keys[i];
+  const Key k = keys[i];
   unsigned keep = 0;
   if (i == 0 || keys[i - 1] != k) {
     long long e = i;
@@ -488,7 +504,8 @@ __global__ void k_q_dedupe(long long n, const uint64_t *__restrict__ keys, unsig
   }
   flag[i] = keep;
 }
-__global__ void k_q_compact(long long n, QKey K, const uint64_t *__restrict__ keys,
+template <typename Key>
+__global__ void k_q_compact(long long n, QKeyT<Key> K, const Key *__restrict__ keys,
                             const uint32_t *__restrict__ vals, const unsigned *__restrict__ pos,
                             const int16_t *__restrict__ old_info, int *blk, int *xs, int *ys,
                             int16_t *lev, int16_t *info) {
@@ -502,6 +519,29 @@ __global__ void k_q_compact(long long n, QKey K, const uint64_t *__restrict__ ke
   lev[o] = (int16_t)q.level;
   uint32_t v = vals ? vals[i] : 0u;
   info[o] = (vals && old_info && (v & 0x80000000u)) ? old_info[v & 0x7fffffffu] : (int16_t)0;
+}
+
+template <typename Key>
+static void q_refine_sort_compact(QForest &f, const QRefineArgs &a, const QKeyT<Key> &K,
+                                  const DBuf<unsigned> &cnt, unsigned total) {
+  cudaStream_t s = f.s;
+  const long long n = f.n;
+  DBuf<Key> keys(total, s);
+  DBuf<uint32_t> vals(total, s);
+  launch(k_q_refine_emit<Key>, blocks_for(n, 256), 256, 0, s, n, a, K, (const int *)f.block.p,
+         (const int *)f.x.p, (const int *)f.y.p, (const int16_t *)f.level.p,
+         (const unsigned *)cnt.p, keys.p, vals.p);
+  sort_keys(keys, &vals, total, K.total_bits(), s);
+  DBuf<unsigned> pos(total + 1, s);
+  launch(k_q_dedupe<Key>, blocks_for(total, 256), 256, 0, s, (long long)total,
+         (const Key *)keys.p, pos.p);
+  exclusive_scan<unsigned>(pos.p, pos.p, total, s);
+  const unsigned m = read_scalar(pos.p + total, s);
+  DBuf<int16_t> old_info = std::move(f.info);
+  q_alloc(f, m);
+  launch(k_q_compact<Key>, blocks_for(total, 256), 256, 0, s, (long long)total, K,
+         (const Key *)keys.p, (const uint32_t *)vals.p, (const unsigned *)pos.p,
+         (const int16_t *)old_info.p, f.block.p, f.x.p, f.y.p, f.level.p, f.info.p);
 }
 
 void qforest_refine(QForest &f, const int *d_ref, long long nref, int min_level,
@@ -527,23 +567,11 @@ void qforest_refine(QForest &f, const int *d_ref, long long nref, int min_level,
   exclusive_scan<unsigned>(cnt.p, cnt.p, n, s);
   const unsigned total = read_scalar(cnt.p + n, s);
   f.maxlev = std::max(f.maxlev, std::max(read_scalar(ml.p, s), 0));
-  QKey K = f.key();
-  DBuf<uint64_t> keys(total, s);
-  DBuf<uint32_t> vals(total, s);
-  launch(k_q_refine_emit, blocks_for(n, 256), 256, 0, s, n, a, K, (const int *)f.block.p,
-         (const int *)f.x.p, (const int *)f.y.p, (const int16_t *)f.level.p,
-         (const unsigned *)cnt.p, keys.p, vals.p);
-  radix_sort(keys, &vals, total, K.total_bits(), s);
-  DBuf<unsigned> pos(total + 1, s);
-  launch(k_q_dedupe, blocks_for(total, 256), 256, 0, s, (long long)total,
-         (const uint64_t *)keys.p, pos.p);
-  exclusive_scan<unsigned>(pos.p, pos.p, total, s);
-  const unsigned m = read_scalar(pos.p + total, s);
-  DBuf<int16_t> old_info = std::move(f.info);
-  q_alloc(f, m);
-  launch(k_q_compact, blocks_for(total, 256), 256, 0, s, (long long)total, K,
-         (const uint64_t *)keys.p, (const uint32_t *)vals.p, (const unsigned *)pos.p,
-         (const int16_t *)old_info.p, f.block.p, f.x.p, f.y.p, f.level.p, f.info.p);
+  const QKey K = f.key();
+  if (K.total_bits() > 64)
+    q_refine_sort_compact<U128>(f, a, qkey_as<U128>(K), cnt, total);
+  else
+    q_refine_sort_compact<uint64_t>(f, a, K, cnt, total);
 }
 
 // coarsen (TMRQuadForest.cpp:1594-1640)
@@ -622,41 +650,45 @@ void qforest_duplicate(QForest &f, QForest &out) {
 // 2:1 balance (TMRQuadForest.cpp:2137-2410): the child-0 families closed
 // level by level from the finest down, S_L = seeds_L U gen(S_{L+1}), then
 // the siblings of every family that are not themselves refined.
-__global__ void k_q_seed_keys(long long n, QPos P, const int *__restrict__ blk,
+template <typename Key>
+__global__ void k_q_seed_keys(long long n, QPos<Key> P, const int *__restrict__ blk,
                               const int *__restrict__ xs, const int *__restrict__ ys,
-                              const int16_t *__restrict__ lev, uint64_t *keys) {
+                              const int16_t *__restrict__ lev, Key *keys) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   Quad o{blk[i], xs[i], ys[i], lev[i]};
   Quad q = q_sibling(o, 0);
-  keys[i] = ((uint64_t)o.level << (P.bb + 2 * P.W)) | P.make(q.block, q.x, q.y);
+  keys[i] = (Key((uint64_t)o.level) << (P.bb + 2 * P.W)) | P.make(q.block, q.x, q.y);
 }
-__global__ void k_q_unique_flags(long long n, const uint64_t *__restrict__ keys, unsigned *flag) {
+template <typename Key>
+__global__ void k_q_unique_flags(long long n, const Key *__restrict__ keys, unsigned *flag) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) flag[i] = (i == 0 || keys[i - 1] != keys[i]) ? 1u : 0u;
 }
-__global__ void k_q_unique_emit(long long n, const uint64_t *__restrict__ keys,
-                                const unsigned *__restrict__ pos, uint64_t mask, uint64_t *out) {
+template <typename Key>
+__global__ void k_q_unique_emit(long long n, const Key *__restrict__ keys,
+                                const unsigned *__restrict__ pos, Key mask, Key *out) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || pos[i + 1] == pos[i]) return;
   out[pos[i]] = keys[i] & mask;
 }
-__global__ void k_q_mask_copy(long long n, const uint64_t *__restrict__ in, uint64_t mask,
-                              uint64_t *out) {
+template <typename Key>
+__global__ void k_q_mask_copy(long long n, const Key *__restrict__ in, Key mask, Key *out) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = in[i] & mask;
 }
-__global__ void k_q_level_starts(long long n, const uint64_t *__restrict__ keys, int shift,
+template <typename Key>
+__global__ void k_q_level_starts(long long n, const Key *__restrict__ keys, int shift,
                                  long long *starts) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  int l = (int)(keys[i] >> shift);
-  if (i == 0 || (int)(keys[i - 1] >> shift) != l) starts[l] = i;
+  int l = (int)klo64(keys[i] >> shift);
+  if (i == 0 || (int)klo64(keys[i - 1] >> shift) != l) starts[l] = i;
 }
 // children-0 of the parent's edge (and corner) neighbours of family q
-template <bool WRITE>
-__device__ __forceinline__ unsigned q_gen_family(const QConnDev &c, QPos P, const Quad &q,
-                                                 int corner, uint64_t *out) {
+template <bool WRITE, typename Key>
+__device__ __forceinline__ unsigned q_gen_family(const QConnDev &c, QPos<Key> P, const Quad &q,
+                                                 int corner, Key *out) {
   unsigned cnt = 0;
   Quad p = q_parent(q);
   const int32_t bs = 2 * side_of(p.level);
@@ -683,8 +715,9 @@ __device__ __forceinline__ unsigned q_gen_family(const QConnDev &c, QPos P, cons
 }
 // n bounds the families; *m (device) is their number (entries past it
 // count 0), so it need not be read back before the count.
-__global__ void k_q_gen_count(long long n, const unsigned *__restrict__ m, QConnDev c, QPos P,
-                              int level, int corner, const uint64_t *__restrict__ cur,
+template <typename Key>
+__global__ void k_q_gen_count(long long n, const unsigned *__restrict__ m, QConnDev c,
+                              QPos<Key> P, int level, int corner, const Key *__restrict__ cur,
                               unsigned *cnt) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -692,27 +725,29 @@ __global__ void k_q_gen_count(long long n, const unsigned *__restrict__ m, QConn
     cnt[i] = 0;
     return;
   }
-  cnt[i] = q_gen_family<false>(c, P, P.decode(cur[i], level), corner, nullptr);
+  cnt[i] = q_gen_family<false, Key>(c, P, P.decode(cur[i], level), corner, nullptr);
 }
-__global__ void k_q_gen_write(long long n, const unsigned *__restrict__ m, QConnDev c, QPos P,
-                              int level, int corner, const uint64_t *__restrict__ cur,
-                              const unsigned *__restrict__ offs, uint64_t *out) {
+template <typename Key>
+__global__ void k_q_gen_write(long long n, const unsigned *__restrict__ m, QConnDev c,
+                              QPos<Key> P, int level, int corner, const Key *__restrict__ cur,
+                              const unsigned *__restrict__ offs, Key *out) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || i >= (long long)*m) return;
-  q_gen_family<true>(c, P, P.decode(cur[i], level), corner, out + offs[i]);
+  q_gen_family<true, Key>(c, P, P.decode(cur[i], level), corner, out + offs[i]);
 }
-__global__ void k_q_leaves(long long n, QPos P, QKey K, int level, const uint64_t *__restrict__ cur,
-                           const uint64_t *__restrict__ finer, long long nfiner, uint64_t *out,
-                           unsigned long long *counter) {
+template <typename Key>
+__global__ void k_q_leaves(long long n, QPos<Key> P, QKeyT<Key> K, int level,
+                           const Key *__restrict__ cur, const Key *__restrict__ finer,
+                           long long nfiner, Key *out, unsigned long long *counter) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  uint64_t mine[4];
+  Key mine[4];
   int m = 0;
   if (i < n) {
     Quad q = P.decode(cur[i], level);
     int ns = (level == 0) ? 1 : 4;
     for (int j = 0; j < ns; j++) {
       Quad sb = (level == 0) ? q : q_sibling(q, j);
-      if (!contains_u64(finer, nfiner, P.make(sb.block, sb.x, sb.y)))
+      if (!contains_key(finer, nfiner, P.make(sb.block, sb.x, sb.y)))
         mine[m++] = K.make(sb.block, sb.x, sb.y, level);
     }
   }
@@ -729,7 +764,8 @@ __global__ void k_q_leaves(long long n, QPos P, QKey K, int level, const uint64_
   unsigned long long o = base + (incl - m);
   for (int j = 0; j < m; j++) out[o + j] = mine[j];
 }
-__global__ void k_q_decode(long long n, QKey K, const uint64_t *__restrict__ keys, int *blk,
+template <typename Key>
+__global__ void k_q_decode(long long n, QKeyT<Key> K, const Key *__restrict__ keys, int *blk,
                            int *xs, int *ys, int16_t *lev, int16_t *info) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -740,45 +776,42 @@ __global__ void k_q_decode(long long n, QKey K, const uint64_t *__restrict__ key
   lev[i] = (int16_t)q.level;
   info[i] = 0;
 }
-static long long q_sort_unique(DBuf<uint64_t> &keys, long long n, int nbits, uint64_t mask,
-                               DBuf<uint64_t> &out, cudaStream_t s) {
+template <typename Key>
+static long long q_sort_unique(DBuf<Key> &keys, long long n, int nbits, Key mask,
+                               DBuf<Key> &out, cudaStream_t s) {
   if (n == 0) {
     out.release();
     return 0;
   }
-  radix_sort(keys, nullptr, n, nbits, s);
+  sort_keys(keys, nullptr, n, nbits, s);
   DBuf<unsigned> pos(n + 1, s);
-  launch(k_q_unique_flags, blocks_for(n, 256), 256, 0, s, n, (const uint64_t *)keys.p, pos.p);
+  launch(k_q_unique_flags<Key>, blocks_for(n, 256), 256, 0, s, n, (const Key *)keys.p, pos.p);
   exclusive_scan<unsigned>(pos.p, pos.p, n, s);
   long long m = read_scalar(pos.p + n, s);
   out.alloc(std::max(1LL, m), s);
-  launch(k_q_unique_emit, blocks_for(n, 256), 256, 0, s, n, (const uint64_t *)keys.p,
+  launch(k_q_unique_emit<Key>, blocks_for(n, 256), 256, 0, s, n, (const Key *)keys.p,
          (const unsigned *)pos.p, mask, out.p);
   return m;
 }
 
-void qforest_balance(QForest &f, int corner) {
-  Stage stage("tmrg_quad_balance");
-  if (!f.have_quads)
-    throw Error(TMRG_ERR_STATE, "Cannot call balance(), no quadrants have been created");
-  f.free_nodes();
+template <typename Key>
+static void q_balance_impl(QForest &f, int corner, const QKeyT<Key> K) {
   const long long n = f.n;
-  if (n == 0) return;
   cudaStream_t s = f.s;
-  QKey K = f.key();
-  QPos P{K.W, K.bb};
+  QPos<Key> P{K.W, K.bb};
   const int pbits = K.bb + 2 * K.W;
-  const uint64_t pmask = (pbits >= 64) ? ~0ULL : ((1ULL << pbits) - 1);
+  const Key pmask = kmask<Key>(pbits);
+  const Key all = kmask<Key>(8 * (int)sizeof(Key));
   QConnDev c = f.conn->dev;
-  DBuf<uint64_t> sk(n, s);
-  launch(k_q_seed_keys, blocks_for(n, 256), 256, 0, s, n, P, (const int *)f.block.p,
+  DBuf<Key> sk(n, s);
+  launch(k_q_seed_keys<Key>, blocks_for(n, 256), 256, 0, s, n, P, (const int *)f.block.p,
          (const int *)f.x.p, (const int *)f.y.p, (const int16_t *)f.level.p, sk.p);
-  DBuf<uint64_t> seeds;
-  const long long ns = q_sort_unique(sk, n, pbits + 5, ~0ULL, seeds, s);
+  DBuf<Key> seeds;
+  const long long ns = q_sort_unique<Key>(sk, n, pbits + 5, all, seeds, s);
   sk.release();
   DBuf<long long> starts(TMRG_MAX_LEVEL + 2, s);
   starts.fill_bytes(0xff);
-  launch(k_q_level_starts, blocks_for(ns, 256), 256, 0, s, ns, (const uint64_t *)seeds.p, pbits,
+  launch(k_q_level_starts<Key>, blocks_for(ns, 256), 256, 0, s, ns, (const Key *)seeds.p, pbits,
          starts.p);
   std::vector<long long> st(TMRG_MAX_LEVEL + 2);
   TMRG_CUDA(cudaMemcpyAsync(st.data(), starts.p, st.size() * sizeof(long long),
@@ -798,9 +831,9 @@ void qforest_balance(QForest &f, int corner) {
       }
     }
   }
-  std::vector<DBuf<uint64_t>> S(L + 2);
+  std::vector<DBuf<Key>> S(L + 2);
   std::vector<long long> Sn(L + 2, 0);
-  DBuf<uint64_t> gen;
+  DBuf<Key> gen;
   long long ngen = 0;
   // one wait per level, as in the octree balance
   for (int l = L; l >= 0; l--) {
@@ -808,21 +841,21 @@ void qforest_balance(QForest &f, int corner) {
     const long long tot = nseed + ngen;
     DBuf<unsigned> upos;  // unique positions; upos[tot] = Sn[l]
     if (tot > 0) {
-      DBuf<uint64_t> cat(tot, s);
+      DBuf<Key> cat(tot, s);
       if (nseed)
-        launch(k_q_mask_copy, blocks_for(nseed, 256), 256, 0, s, nseed,
-               (const uint64_t *)(seeds.p + lo[l]), pmask, cat.p);
+        launch(k_q_mask_copy<Key>, blocks_for(nseed, 256), 256, 0, s, nseed,
+               (const Key *)(seeds.p + lo[l]), pmask, cat.p);
       if (ngen)
-        TMRG_CUDA(cudaMemcpyAsync(cat.p + nseed, gen.p, ngen * sizeof(uint64_t),
+        TMRG_CUDA(cudaMemcpyAsync(cat.p + nseed, gen.p, ngen * sizeof(Key),
                                   cudaMemcpyDeviceToDevice, s));
-      radix_sort(cat, nullptr, tot, pbits, s);
+      sort_keys(cat, nullptr, tot, pbits, s);
       upos.alloc(tot + 1, s);
-      launch(k_q_unique_flags, blocks_for(tot, 256), 256, 0, s, tot, (const uint64_t *)cat.p,
+      launch(k_q_unique_flags<Key>, blocks_for(tot, 256), 256, 0, s, tot, (const Key *)cat.p,
              upos.p);
       exclusive_scan<unsigned>(upos.p, upos.p, tot, s);
       S[l].alloc(tot, s);
-      launch(k_q_unique_emit, blocks_for(tot, 256), 256, 0, s, tot, (const uint64_t *)cat.p,
-             (const unsigned *)upos.p, ~0ULL, S[l].p);
+      launch(k_q_unique_emit<Key>, blocks_for(tot, 256), 256, 0, s, tot, (const Key *)cat.p,
+             (const unsigned *)upos.p, all, S[l].p);
     }
     gen.release();
     ngen = 0;
@@ -830,8 +863,8 @@ void qforest_balance(QForest &f, int corner) {
     if (tot == 0) continue;
     if (l >= 2) {
       DBuf<unsigned> cnt(tot + 1, s);
-      launch(k_q_gen_count, blocks_for(tot, 128), 128, 0, s, tot,
-             (const unsigned *)upos.p + tot, c, P, l, corner, (const uint64_t *)S[l].p, cnt.p);
+      launch(k_q_gen_count<Key>, blocks_for(tot, 128), 128, 0, s, tot,
+             (const unsigned *)upos.p + tot, c, P, l, corner, (const Key *)S[l].p, cnt.p);
       exclusive_scan<unsigned>(cnt.p, cnt.p, tot, s);
       const unsigned *dv[2] = {upos.p + tot, cnt.p + tot};
       unsigned hv[2];
@@ -839,8 +872,8 @@ void qforest_balance(QForest &f, int corner) {
       Sn[l] = hv[0];
       ngen = hv[1];
       gen.alloc(std::max(1LL, ngen), s);
-      launch(k_q_gen_write, blocks_for(tot, 128), 128, 0, s, tot,
-             (const unsigned *)upos.p + tot, c, P, l, corner, (const uint64_t *)S[l].p,
+      launch(k_q_gen_write<Key>, blocks_for(tot, 128), 128, 0, s, tot,
+             (const unsigned *)upos.p + tot, c, P, l, corner, (const Key *)S[l].p,
              (const unsigned *)cnt.p, gen.p);
     } else {
       Sn[l] = read_scalar(upos.p + tot, s);
@@ -849,35 +882,50 @@ void qforest_balance(QForest &f, int corner) {
   seeds.release();
   long long cap = 0;
   for (int l = 0; l <= L; l++) cap += (l == 0 ? 1 : 4) * Sn[l];
-  DBuf<uint64_t> leaves(std::max(1LL, cap), s);
+  DBuf<Key> leaves(std::max(1LL, cap), s);
   DBuf<unsigned long long> counter(1, s);
   counter.zero();
   for (int l = 0; l <= L; l++) {
     if (!Sn[l]) continue;
-    launch(k_q_leaves, blocks_for(Sn[l], 256), 256, 0, s, Sn[l], P, K, l,
-           (const uint64_t *)S[l].p, (const uint64_t *)S[l + 1].p, Sn[l + 1], leaves.p,
-           counter.p);
+    launch(k_q_leaves<Key>, blocks_for(Sn[l], 256), 256, 0, s, Sn[l], P, K, l,
+           (const Key *)S[l].p, (const Key *)S[l + 1].p, Sn[l + 1], leaves.p, counter.p);
   }
   const long long m = (long long)read_scalar(counter.p, s);
   S.clear();
-  radix_sort(leaves, nullptr, m, K.total_bits(), s);
+  sort_keys(leaves, nullptr, m, K.total_bits(), s);
   q_alloc(f, m);
-  launch(k_q_decode, blocks_for(m, 256), 256, 0, s, m, K, (const uint64_t *)leaves.p, f.block.p,
+  launch(k_q_decode<Key>, blocks_for(m, 256), 256, 0, s, m, K, (const Key *)leaves.p, f.block.p,
          f.x.p, f.y.p, f.level.p, f.info.p);
 }
+
+void qforest_balance(QForest &f, int corner) {
+  Stage stage("tmrg_quad_balance");
+  if (!f.have_quads)
+    throw Error(TMRG_ERR_STATE, "Cannot call balance(), no quadrants have been created");
+  f.free_nodes();
+  if (f.n == 0) return;
+  const QKey K = f.key();
+  if (K.total_bits() > 64)
+    q_balance_impl<U128>(f, corner, qkey_as<U128>(K));
+  else
+    q_balance_impl<uint64_t>(f, corner, K);
+}
+
 
 // ---------------------------------------------------------------------
 // createNodes (TMRQuadForest.cpp:2996-3860).
 // 1. hanging edges: bit e of info when the quadrant's edge e lies on its
 //    parent's edge e and the parent's neighbour across it is a leaf
 //    (computeDepEdges :2658-2726, seen from the finer side).
-__global__ void k_q_keys(long long n, QKey K, const int *__restrict__ blk,
+template <typename Key>
+__global__ void k_q_keys(long long n, QKeyT<Key> K, const int *__restrict__ blk,
                          const int *__restrict__ xs, const int *__restrict__ ys,
-                         const int16_t *__restrict__ lev, uint64_t *keys) {
+                         const int16_t *__restrict__ lev, Key *keys) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) keys[i] = K.make(blk[i], xs[i], ys[i], lev[i]);
 }
-__global__ void k_q_dep_info(long long n, QConnDev c, QKey K, const uint64_t *__restrict__ keys,
+template <typename Key>
+__global__ void k_q_dep_info(long long n, QConnDev c, QKeyT<Key> K, const Key *__restrict__ keys,
                              const int *__restrict__ blk, const int *__restrict__ xs,
                              const int *__restrict__ ys, const int16_t *__restrict__ lev,
                              int16_t *info) {
@@ -889,7 +937,7 @@ __global__ void k_q_dep_info(long long n, QConnDev c, QKey K, const uint64_t *__
     return;
   }
   auto exists = [&](const Quad &q) {
-    return contains_u64(keys, n, K.make(q.block, q.x, q.y, q.level));
+    return contains_key(keys, n, K.make(q.block, q.x, q.y, q.level));
   };
   const int32_t h = side_of(o.level);
   const int id = ((o.x & h) ? 1 : 0) | ((o.y & h) ? 2 : 0);
@@ -926,10 +974,11 @@ __device__ __forceinline__ void q_object(int order, const Quad &e, int j, int32_
     y = e.y + h * (j / 3);
   }
 }
-__global__ void k_q_node_keys(long long n, QConnDev c, QNodeKey NK, int order,
+template <typename Key>
+__global__ void k_q_node_keys(long long n, QConnDev c, QNodeKeyT<Key> NK, int order,
                               const int *__restrict__ blk, const int *__restrict__ xs,
                               const int *__restrict__ ys, const int16_t *__restrict__ lev,
-                              uint64_t *keys, uint32_t *vals) {
+                              Key *keys, uint32_t *vals) {
   const int npe = order * order;
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * npe) return;
@@ -944,9 +993,10 @@ __global__ void k_q_node_keys(long long n, QConnDev c, QNodeKey NK, int order,
   vals[t] = (uint32_t)t;
 }
 // sorted object keys -> run index of every (element, local node) entry
-__global__ void k_q_node_runs(long long m, const uint64_t *__restrict__ keys,
+template <typename Key>
+__global__ void k_q_node_runs(long long m, const Key *__restrict__ keys,
                               const uint32_t *__restrict__ vals, const unsigned *__restrict__ pos,
-                              uint64_t *ukeys, int *lconn) {
+                              Key *ukeys, int *lconn) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   unsigned idx = pos[i + 1] - 1;
@@ -1005,16 +1055,17 @@ struct QKnots {
   double k[3];
   double r[3][3];
 };
-__device__ __forceinline__ long long q_find_node(const uint64_t *ukeys, long long nl,
-                                                 uint64_t key) {
-  long long i = lower_bound_u64(ukeys, nl, key);
+template <typename Key>
+__device__ __forceinline__ long long q_find_node(const Key *ukeys, long long nl, Key key) {
+  long long i = lower_bound_key(ukeys, nl, key);
   return (i < nl && ukeys[i] == key) ? i : -1;
 }
-__global__ void k_q_dep_rows(long long n, QConnDev c, QNodeKey NK, int order, QKnots kn,
+template <typename Key>
+__global__ void k_q_dep_rows(long long n, QConnDev c, QNodeKeyT<Key> NK, int order, QKnots kn,
                              const int *__restrict__ blk, const int *__restrict__ xs,
                              const int *__restrict__ ys, const int16_t *__restrict__ lev,
                              const int16_t *__restrict__ info, const int *__restrict__ lconn,
-                             const int *__restrict__ num, const uint64_t *__restrict__ ukeys,
+                             const int *__restrict__ num, const Key *__restrict__ ukeys,
                              long long nl, int *dconn, double *dw, int *err) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || !info[i]) return;
@@ -1038,7 +1089,7 @@ __global__ void k_q_dep_rows(long long n, QConnDev c, QNodeKey NK, int order, QK
         y = p.y + 2 * h * (e % 2);
       }
       q_transform_node(c, b, x, y);
-      long long t = q_find_node(ukeys, nl, NK.make(b, x, y));
+      long long t = q_find_node<Key>(ukeys, nl, NK.make(b, x, y));
       if (t < 0) {
         atomicExch(err, 1);
         return;
@@ -1063,41 +1114,42 @@ __global__ void k_q_dep_rows(long long n, QConnDev c, QNodeKey NK, int order, QK
   }
 }
 
-void qforest_create_nodes(QForest &f) {
-  Stage st("tmrg_quad_create_nodes");
-  if (!f.have_quads)
-    throw Error(TMRG_ERR_STATE, "Cannot call createNodes(), no quadrants have been created");
-  if (f.have_nodes) return;
+// Hanging-edge flags (section 1 of createNodes).
+template <typename Key>
+static void q_hanging(QForest &f, const QKeyT<Key> &K) {
   cudaStream_t s = f.s;
   const long long n = f.n;
-  const int o = f.order, npe = o * o;
+  DBuf<Key> qk(std::max(1LL, n), s);
+  launch(k_q_keys<Key>, blocks_for(n, 256), 256, 0, s, n, K, (const int *)f.block.p,
+         (const int *)f.x.p, (const int *)f.y.p, (const int16_t *)f.level.p, qk.p);
+  launch(k_q_dep_info<Key>, blocks_for(n, 128), 128, 0, s, n, f.conn->dev, K,
+         (const Key *)qk.p, (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
+         (const int16_t *)f.level.p, f.info.p);
+}
+
+// Node objects, numbering and the dependent rows (the node keys are 64- or
+// 128-bit).
+template <typename Key>
+static void q_nodes(QForest &f, const QNodeKeyT<Key> &NK) {
+  cudaStream_t s = f.s;
+  const long long n = f.n;
+  const int o = f.order;
   QConnDev c = f.conn->dev;
-  QKey K = f.key();
-  {
-    DBuf<uint64_t> qk(std::max(1LL, n), s);
-    launch(k_q_keys, blocks_for(n, 256), 256, 0, s, n, K, (const int *)f.block.p,
-           (const int *)f.x.p, (const int *)f.y.p, (const int16_t *)f.level.p, qk.p);
-    launch(k_q_dep_info, blocks_for(n, 128), 128, 0, s, n, c, K, (const uint64_t *)qk.p,
-           (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
-           (const int16_t *)f.level.p, f.info.p);
-  }
-  const long long m = n * npe;
-  if (m >= (1LL << 32)) throw Error(TMRG_ERR_ARG, "createNodes: too many element nodes");
-  QNodeKey NK{f.maxlev + (o == 3 ? 1 : 0), f.conn->block_bits};
-  if (NK.total_bits() > 64) throw Error(TMRG_ERR_KEY_RANGE, "createNodes: node key range");
-  DBuf<uint64_t> keys(std::max(1LL, m), s);
+  const long long m = n * o * o;
+  DBuf<Key> keys(std::max(1LL, m), s);
   DBuf<uint32_t> vals(std::max(1LL, m), s);
-  launch(k_q_node_keys, blocks_for(m, 256), 256, 0, s, n, c, NK, o, (const int *)f.block.p,
-         (const int *)f.x.p, (const int *)f.y.p, (const int16_t *)f.level.p, keys.p, vals.p);
-  radix_sort(keys, &vals, m, NK.total_bits(), s);
+  launch(k_q_node_keys<Key>, blocks_for(m, 256), 256, 0, s, n, c, NK, o,
+         (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
+         (const int16_t *)f.level.p, keys.p, vals.p);
+  sort_keys(keys, &vals, m, NK.total_bits(), s);
   DBuf<unsigned> pos(m + 1, s);
-  launch(k_q_unique_flags, blocks_for(m, 256), 256, 0, s, m, (const uint64_t *)keys.p, pos.p);
+  launch(k_q_unique_flags<Key>, blocks_for(m, 256), 256, 0, s, m, (const Key *)keys.p, pos.p);
   // pos[i + 1] - 1 is then the run (node) index of entry i
   exclusive_scan<unsigned>(pos.p, pos.p, m, s);
   const long long nl = read_scalar(pos.p + m, s);
-  DBuf<uint64_t> ukeys(std::max(1LL, nl), s);
+  DBuf<Key> ukeys(std::max(1LL, nl), s);
   DBuf<int> lconn(std::max(1LL, m), s);
-  launch(k_q_node_runs, blocks_for(m, 256), 256, 0, s, m, (const uint64_t *)keys.p,
+  launch(k_q_node_runs<Key>, blocks_for(m, 256), 256, 0, s, m, (const Key *)keys.p,
          (const uint32_t *)vals.p, (const unsigned *)pos.p, ukeys.p, lconn.p);
   keys.release();
   vals.release();
@@ -1139,16 +1191,41 @@ void qforest_create_nodes(QForest &f) {
   DBuf<int> err(1, s);
   err.zero();
   if (ndep)
-    launch(k_q_dep_rows, blocks_for(n, 128), 128, 0, s, n, c, NK, o, kn, (const int *)f.block.p,
-           (const int *)f.x.p, (const int *)f.y.p, (const int16_t *)f.level.p,
-           (const int16_t *)f.info.p, (const int *)lconn.p, (const int *)num.p,
-           (const uint64_t *)ukeys.p, nl, f.dep_conn.p, f.dep_w.p, err.p);
+    launch(k_q_dep_rows<Key>, blocks_for(n, 128), 128, 0, s, n, c, NK, o, kn,
+           (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
+           (const int16_t *)f.level.p, (const int16_t *)f.info.p, (const int *)lconn.p,
+           (const int *)num.p, (const Key *)ukeys.p, nl, f.dep_conn.p, f.dep_w.p, err.p);
   if (read_scalar(err.p, s))
     throw Error(TMRG_ERR_INTERNAL, "createNodes: a parent edge node is missing");
-  f.node_keys = std::move(ukeys);
   f.node_num = std::move(num);
   f.have_nodes = true;
   TMRG_CUDA(cudaStreamSynchronize(s));
+}
+
+void qforest_create_nodes(QForest &f) {
+  Stage st("tmrg_quad_create_nodes");
+  if (!f.have_quads)
+    throw Error(TMRG_ERR_STATE, "Cannot call createNodes(), no quadrants have been created");
+  if (f.have_nodes) return;
+  const long long n = f.n;
+  const int o = f.order;
+  const QKey K = f.key();
+  if (K.total_bits() > 64)
+    q_hanging<U128>(f, qkey_as<U128>(K));
+  else
+    q_hanging<uint64_t>(f, K);
+  if (n * o * o >= (1LL << 32))
+    throw Error(TMRG_ERR_ARG, "createNodes: too many element nodes");
+  if (o == 3 && f.maxlev >= TMRG_MAX_LEVEL)
+    throw Error(TMRG_ERR_ARG, "createNodes: an order-3 element at level " +
+                                  std::to_string(TMRG_MAX_LEVEL) +
+                                  " has no integer half-side for its nodes");
+  const QNodeKey NK{f.maxlev + (o == 3 ? 1 : 0), f.conn->block_bits};
+  if (NK.total_bits() > 128) throw Error(TMRG_ERR_KEY_RANGE, "createNodes: node key range");
+  if (NK.total_bits() > 64)
+    q_nodes<U128>(f, QNodeKeyT<U128>{NK.Lg, NK.bb});
+  else
+    q_nodes<uint64_t>(f, NK);
 }
 
 // ---------------------------------------------------------------------

@@ -8,7 +8,9 @@
 
 namespace tmrg {
 
-struct QKey;
+template <typename Key>
+struct QKeyT;
+using QKey = QKeyT<uint64_t>;
 
 // Device view of the face connectivity: CSR entries hold 4*face+corner and
 // 4*face+edge; the first entry of each list is the lowest-numbered face,
@@ -48,7 +50,6 @@ struct QForest {
   long long num_local = 0, num_owned = 0, num_dep = 0, dep_nnz = 0;
   DBuf<int> econn, dep_ptr, dep_conn;
   DBuf<double> dep_w;
-  DBuf<uint64_t> node_keys;  // sorted node keys (local node order)
   DBuf<int> node_num;        // node number of each local node
   void free_nodes() {
     have_nodes = false;
@@ -56,7 +57,6 @@ struct QForest {
     dep_ptr.release();
     dep_conn.release();
     dep_w.release();
-    node_keys.release();
     node_num.release();
     num_local = num_owned = num_dep = dep_nnz = 0;
   }

@@ -101,6 +101,16 @@ def point_indicator(octs, point):
     return inside.astype(np.intc)
 
 
+def quad_point_indicator(quads, point):
+    """The 2-D point_indicator over an (n, 6) {face, x, y, tag, level, info}
+    quadrant array: 1 where the quadrant contains the face-local point."""
+    p = np.floor(np.asarray(point, np.float64) * HMAX).astype(np.int64)
+    h = (np.int64(1) << (30 - quads[:, 4].astype(np.int64)))
+    xy = quads[:, 1:3].astype(np.int64)
+    inside = ((xy <= p[None, :]) & (p[None, :] < xy + h[:, None])).all(1)
+    return inside.astype(np.intc)
+
+
 def random_indicator(n, seed, stream, prob):
     return (uniform(seed, stream, n) < prob).astype(np.intc)
 
