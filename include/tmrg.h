@@ -346,6 +346,12 @@ int tmrg_qforest_get_mesh_order(tmrg_qforest *f, int *order, int *interp, double
    refines every quadrant by one level), coarsen (:1594-1640), duplicate
    (:1572-1592), balance (:2237-2410), createNodes (:2996-3216). */
 int tmrg_qforest_create_trees(tmrg_qforest *f, int level);
+/* createRandomTrees (TMRQuadForest.cpp:1327-1407): nrand quadrants per face
+   at random levels in [min_level, max_level] and random anchors, sorted and
+   made unique on position (finest kept), with the seeded generator
+   U(seed, face, 3i + k) in place of libc rand(). */
+int tmrg_qforest_create_random_trees(tmrg_qforest *f, int nrand, int min_level, int max_level,
+                                     uint64_t seed);
 int tmrg_qforest_refine(tmrg_qforest *f, const int *refine, int64_t n, int min_level,
                         int max_level);
 int tmrg_qforest_refine_device(tmrg_qforest *f, const int *d_refine, int64_t n, int min_level,

@@ -304,36 +304,30 @@ class TMROctForest : public TMRGEntity {
                                             edge_dir, edge_reversed, src_face_id),
                 "transformNode");
   }
-  // Legacy VTK unstructured grid of the elements' corner points
-  // (writeToVTK, TMROctForest.cpp), from getPoints and getNodeConn.
+  // writeToVTK (TMROctForest.cpp:1149-1228): the block mesh as VTK
+  // hexahedra, each connectivity node at its owner block's corner through
+  // the block boxes (the reference evaluates the topology's volumes), the
+  // block index as the cell scalar entity_index.  Nothing is written when no
+  // block boxes are set (the reference needs a topology).
   void writeToVTK(const char *filename) {
-    TMRPoint *X = nullptr;
-    int np = getPoints(&X);
-    const int *conn = nullptr;
-    int ne = 0;
-    getNodeConn(&conn, &ne);
-    int64_t s[6] = {0};
-    tmrg_forest_node_sizes(f, s);
-    const int o = getMeshOrder(), nd = (int)s[2];
+    int nb = 0, nn = 0;
+    const int *bc = nullptr;
+    std::vector<double> X;
+    if (!blockNodePoints(&nb, &nn, &bc, X)) return;
     FILE *fp = filename ? fopen(filename, "w") : nullptr;
-    if (!fp || !conn) {
-      if (fp) fclose(fp);
-      fprintf(stderr, "TMROctForest: writeToVTK failed for %s\n", filename ? filename : "(null)");
-      return;
+    if (!fp) return;
+    fprintf(fp, "# vtk DataFile Version 3.0\nvtk output\nASCII\n");
+    fprintf(fp, "DATASET UNSTRUCTURED_GRID\nPOINTS %d float\n", nn);
+    for (int k = 0; k < nn; k++) fprintf(fp, "%e %e %e\n", X[3 * k], X[3 * k + 1], X[3 * k + 2]);
+    fprintf(fp, "\nCELLS %d %d\n", nb, 9 * nb);
+    for (int k = 0; k < nb; k++) {
+      const int *c = bc + 8 * k;
+      fprintf(fp, "8 %d %d %d %d %d %d %d %d\n", c[0], c[1], c[3], c[2], c[4], c[5], c[7], c[6]);
     }
-    fprintf(fp, "# vtk DataFile Version 3.0\nvtk output\nASCII\nDATASET UNSTRUCTURED_GRID\n");
-    fprintf(fp, "POINTS %d float\n", np);
-    for (int i = 0; i < np; i++) fprintf(fp, "%e %e %e\n", X[i].x, X[i].y, X[i].z);
-    fprintf(fp, "CELLS %d %d\n", ne, 9 * ne);
-    const int c[8] = {0, o - 1, o * o - 1, o * (o - 1), o * o * (o - 1),
-                      o * o * (o - 1) + o - 1, o * o * o - 1, o * o * o - o};
-    for (int e = 0; e < ne; e++) {
-      fprintf(fp, "8");
-      for (int k = 0; k < 8; k++) fprintf(fp, " %d", conn[o * o * o * e + c[k]] + nd);
-      fprintf(fp, "\n");
-    }
-    fprintf(fp, "CELL_TYPES %d\n", ne);
-    for (int e = 0; e < ne; e++) fprintf(fp, "%d\n", 12);
+    fprintf(fp, "\nCELL_TYPES %d\n", nb);
+    for (int k = 0; k < nb; k++) fprintf(fp, "12\n");
+    fprintf(fp, "CELL_DATA %d\nSCALARS entity_index float 1\nLOOKUP_TABLE default\n", nb);
+    for (int k = 0; k < nb; k++) fprintf(fp, "%e\n", 1.0 * k);
     fclose(fp);
   }
   // Axis-aligned box (origin xyz, extent xyz) of every block: the stand-in
@@ -349,28 +343,12 @@ class TMROctForest : public TMRGEntity {
   // block's box, and the block index as a cell-centred variable.  Nothing
   // is written when no block boxes are set (the reference needs a topology).
   void writeToTecplot(const char *filename) {
-    if (boxes_.empty()) return;
-    int nb = 0, nf = 0, ne = 0, nn = 0;
-    const int *bc = nullptr, *bf = nullptr, *be = nullptr, *fid = nullptr;
-    getConnectivity(&nb, &nf, &ne, &nn, &bc, &bf, &be, &fid);
-    if (!bc) return;
+    int nb = 0, nn = 0;
+    const int *bc = nullptr;
+    std::vector<double> X;
+    if (!blockNodePoints(&nb, &nn, &bc, X)) return;
     FILE *fp = filename ? fopen(filename, "w") : nullptr;
     if (!fp) return;
-    std::vector<int> owner(nn, nb);
-    for (int b = 0; b < nb; b++)
-      for (int c = 0; c < 8; c++)
-        if (b < owner[bc[8 * b + c]]) owner[bc[8 * b + c]] = b;
-    std::vector<double> X(3 * (size_t)nn, 0.0);
-    for (int k = 0; k < nn; k++) {
-      const int b = owner[k];
-      if (b >= nb) continue;
-      int corner = 0;
-      while (corner < 8 && bc[8 * b + corner] != k) corner++;
-      const double uvw[3] = {1.0 * (corner & 1), 1.0 * ((corner >> 1) & 1),
-                             1.0 * (corner >> 2)};
-      for (int d = 0; d < 3; d++)
-        X[3 * k + d] = boxes_[6 * b + d] + boxes_[6 * b + 3 + d] * uvw[d];
-    }
     fprintf(fp, "Variables = X,Y,Z,block\n");
     fprintf(fp, "Zone N = %d E = %d ", nn, nb);
     fprintf(fp, "DATAPACKING=BLOCK, ZONETYPE=FEBRICK\n");
@@ -384,6 +362,32 @@ class TMROctForest : public TMRGEntity {
               c[4] + 1, c[5] + 1, c[7] + 1, c[6] + 1);
     }
     fclose(fp);
+  }
+  // Each block connectivity node at its owner block's corner (the
+  // lowest-numbered block touching it, node_block_owners) through the
+  // block boxes; false without boxes.
+  bool blockNodePoints(int *nb, int *nn, const int **bc, std::vector<double> &X) {
+    if (boxes_.empty()) return false;
+    int nf = 0, ne = 0;
+    const int *bf = nullptr, *be = nullptr, *fid = nullptr;
+    getConnectivity(nb, &nf, &ne, nn, bc, &bf, &be, &fid);
+    if (!*bc) return false;
+    std::vector<int> owner(*nn, *nb);
+    for (int b = 0; b < *nb; b++)
+      for (int c = 0; c < 8; c++)
+        if (b < owner[(*bc)[8 * b + c]]) owner[(*bc)[8 * b + c]] = b;
+    X.assign(3 * (size_t)*nn, 0.0);
+    for (int k = 0; k < *nn; k++) {
+      const int b = owner[k];
+      if (b >= *nb) continue;
+      int corner = 0;
+      while (corner < 8 && (*bc)[8 * b + corner] != k) corner++;
+      const double uvw[3] = {1.0 * (corner & 1), 1.0 * ((corner >> 1) & 1),
+                             1.0 * (corner >> 2)};
+      for (int d = 0; d < 3; d++)
+        X[3 * k + d] = boxes_[6 * b + d] + boxes_[6 * b + 3 + d] * uvw[d];
+    }
+    return true;
   }
   // writeForestToVTK (TMROctForest.cpp:1317-1384): every octant as a
   // hexahedron with its own eight corners (x fastest) mapped through its

@@ -93,6 +93,15 @@ class TMRQuadForest : public TMRGEntity {
   void createTrees(int refine_level) {
     tmrg_report(tmrg_qforest_create_trees(f, refine_level), "createTrees");
   }
+  // createRandomTrees (TMRQuadForest.cpp:1327-1407) with the seeded
+  // generator U(seed, face, 3i + k) in place of libc rand().
+  void createRandomTrees(int nrand = 10, int min_level = 0, int max_level = 8,
+                         uint64_t seed = 0) {
+    tmrg_report(tmrg_qforest_create_random_trees(f, nrand, min_level, max_level, seed),
+                "createRandomTrees");
+  }
+  // repartition: the forest lives on one GPU, nothing to redistribute.
+  void repartition() {}
   void refine(const int refinement[] = nullptr, int min_level = 0,
               int max_level = TMR_MAX_LEVEL) {
     int64_t n = 0;
@@ -173,6 +182,83 @@ class TMRQuadForest : public TMRGEntity {
                 "createInterpolation");
   }
   tmrg_qforest *handle() { return f; }
+  // A box (origin x, y, extent x, y) per face: the stand-in for the
+  // topology's surfaces that getPoints and the VTK writers map through
+  // (tmrg_qforest_set_face_boxes).
+  void setFaceBoxes(const double *boxes, int nfaces) {
+    if (tmrg_report(tmrg_qforest_set_face_boxes(f, boxes, nfaces), "setFaceBoxes"))
+      boxes_.assign(boxes, boxes + (size_t)(boxes ? 4 * nfaces : 0));
+  }
+  // writeToVTK (TMRQuadForest.cpp:651-720): the face mesh as VTK
+  // quadrilaterals, each connectivity node at its owner face's corner (the
+  // lowest-numbered face touching it) through the face boxes, the face
+  // index as the cell scalar entity_index; nothing without face boxes.
+  void writeToVTK(const char *filename) {
+    if (boxes_.empty()) return;
+    int nf = 0, ne = 0, nn = 0;
+    const int *fc = nullptr, *fe = nullptr;
+    getConnectivity(&nf, &ne, &nn, &fc, &fe);
+    FILE *fp = filename ? fopen(filename, "w") : nullptr;
+    if (!fp) return;
+    std::vector<int> owner(nn, nf);
+    for (int q = 0; q < nf; q++)
+      for (int c = 0; c < 4; c++)
+        if (q < owner[fc[4 * q + c]]) owner[fc[4 * q + c]] = q;
+    fprintf(fp, "# vtk DataFile Version 3.0\nvtk output\nASCII\n");
+    fprintf(fp, "DATASET UNSTRUCTURED_GRID\nPOINTS %d float\n", nn);
+    for (int k = 0; k < nn; k++) {
+      const int q = owner[k];
+      double x = 0.0, y = 0.0;
+      if (q < nf) {
+        int corner = 0;
+        while (corner < 4 && fc[4 * q + corner] != k) corner++;
+        x = boxes_[4 * q] + boxes_[4 * q + 2] * (1.0 * (corner & 1));
+        y = boxes_[4 * q + 1] + boxes_[4 * q + 3] * (1.0 * (corner >> 1));
+      }
+      fprintf(fp, "%e %e %e\n", x, y, 0.0);
+    }
+    fprintf(fp, "\nCELLS %d %d\n", nf, 5 * nf);
+    for (int q = 0; q < nf; q++)
+      fprintf(fp, "4 %d %d %d %d\n", fc[4 * q], fc[4 * q + 1], fc[4 * q + 3], fc[4 * q + 2]);
+    fprintf(fp, "\nCELL_TYPES %d\n", nf);
+    for (int q = 0; q < nf; q++) fprintf(fp, "9\n");
+    fprintf(fp, "CELL_DATA %d\nSCALARS entity_index float 1\nLOOKUP_TABLE default\n", nf);
+    for (int q = 0; q < nf; q++) fprintf(fp, "%e\n", 1.0 * q);
+    fclose(fp);
+  }
+  // writeForestToVTK (TMRQuadForest.cpp:809-870): every quadrant as a
+  // quadrilateral with its own four corners (x fastest) through its face's
+  // box, the face index as entity_index; nothing without face boxes.
+  void writeForestToVTK(const char *filename) {
+    if (boxes_.empty()) return;
+    TMRQuadrantArray *arr = nullptr;
+    getQuadrants(&arr);
+    FILE *fp = filename ? fopen(filename, "w") : nullptr;
+    if (!fp) return;
+    const int n = (int)arr->quads.size();
+    const double hmax = (double)(1 << 30);
+    fprintf(fp, "# vtk DataFile Version 3.0\nvtk output\nASCII\n");
+    fprintf(fp, "DATASET UNSTRUCTURED_GRID\nPOINTS %d float\n", 4 * n);
+    for (int k = 0; k < n; k++) {
+      const TMRQuadrant &q = arr->quads[k];
+      const int32_t h = 1 << (30 - q.level);
+      const double *b = &boxes_[4 * (size_t)q.face];
+      for (int jj = 0; jj < 2; jj++)
+        for (int ii = 0; ii < 2; ii++) {
+          const double u = 1.0 * (q.x + ii * h) / hmax;
+          const double v = 1.0 * (q.y + jj * h) / hmax;
+          fprintf(fp, "%e %e %e\n", b[0] + b[2] * u, b[1] + b[3] * v, 0.0);
+        }
+    }
+    fprintf(fp, "\nCELLS %d %d\n", n, 5 * n);
+    for (int k = 0; k < n; k++)
+      fprintf(fp, "4 %d %d %d %d\n", 4 * k, 4 * k + 1, 4 * k + 3, 4 * k + 2);
+    fprintf(fp, "\nCELL_TYPES %d\n", n);
+    for (int k = 0; k < n; k++) fprintf(fp, "9\n");
+    fprintf(fp, "CELL_DATA %d\nSCALARS entity_index float 1\nLOOKUP_TABLE default\n", n);
+    for (int k = 0; k < n; k++) fprintf(fp, "%e\n", 1.0 * arr->quads[k].face);
+    fclose(fp);
+  }
 
  private:
   TMRQuadForest *derived(int (*fn)(tmrg_qforest *, tmrg_qforest **), const char *w) {
@@ -186,7 +272,7 @@ class TMRQuadForest : public TMRGEntity {
   void *stream;
   TMRQuadrantArray quads_;
   std::vector<int> fc_, fe_, conn_, dptr_, dconn_;
-  std::vector<double> dw_, knots_;
+  std::vector<double> dw_, knots_, boxes_;
   int range_[2];
 };
 

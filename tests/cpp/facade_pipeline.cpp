@@ -96,6 +96,7 @@ int main(int argc, char **argv) {
   f->setBlockBoxes(boxes.data(), nb);
   f->writeForestToVTK(argc > 1 ? argv[1] : "/dev/null");
   f->writeToTecplot(argc > 2 ? argv[2] : "/dev/null");
+  f->writeToVTK(argc > 3 ? argv[3] : "/dev/null");
   printf("elements %d owned %d dep %d conn_sum %lld P_rows %lld P_nnz %lld P1_sum %.12f "
          "blocks %d faces %d edges %d nodes %d node_refs %d local_ok %d pu %.15f du %.15f "
          "enclosed_self %d corner_block %d\n",

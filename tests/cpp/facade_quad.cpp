@@ -8,7 +8,7 @@
 
 #include "tmrg_quadforest.hpp"
 
-int main() {
+int main(int argc, char **argv) {
   const int nx = 3, ny = 2;
   std::vector<int> conn;
   for (int j = 0; j < ny; j++)
@@ -59,6 +59,30 @@ int main() {
   printf("elements %d owned %d dep %d conn_sum %lld P_rows %lld P_nnz %lld P1_sum %.17g "
          "faces %d edges %d nodes %d\n",
          ne, nown, nd, csum, (long long)rows, (long long)nnz, s, nfaces, nedges, nnodes);
+  // the face mesh and the quadrants through face boxes (x offset = face)
+  std::vector<double> boxes(4 * nfaces);
+  for (int k = 0; k < nfaces; k++) {
+    boxes[4 * k] = k, boxes[4 * k + 1] = 0.0;
+    boxes[4 * k + 2] = boxes[4 * k + 3] = 1.0;
+  }
+  f->setFaceBoxes(boxes.data(), nfaces);
+  f->writeToVTK(argc > 1 ? argv[1] : "/dev/null");
+  f->writeForestToVTK(argc > 2 ? argv[2] : "/dev/null");
+  // seeded random trees
+  TMRQuadForest *r = new TMRQuadForest(0, 2, TMR_GAUSS_LOBATTO_POINTS);
+  r->incref();
+  r->setConnectivity((nx + 1) * (ny + 1), conn.data(), nx * ny);
+  r->createRandomTrees(25, 1, 6, 5);
+  r->repartition();
+  TMRQuadrantArray *rq;
+  r->getQuadrants(&rq);
+  int nr;
+  TMRQuadrant *ra;
+  rq->getArray(&ra, &nr);
+  long long rsum = 0;
+  for (int i = 0; i < nr; i++) rsum += (long long)ra[i].x + 3LL * ra[i].y + ra[i].level;
+  printf("rand_quads %d rand_sum %lld\n", nr, rsum);
+  r->decref();
   // STL tools on a one-block octree forest with a linear field in x
   std::vector<int> bconn = {0, 1, 2, 3, 4, 5, 6, 7};
   TMROctForest *o = new TMROctForest(0, 2, TMR_GAUSS_LOBATTO_POINTS);

@@ -31,8 +31,9 @@ def test_facade_compiles_and_links(tmp_path):
 @pytest.mark.gpu
 def test_facade_matches_python_binding(gpu_lib, tmp_path):
     exe = _build(tmp_path)
-    vtk, tec = str(tmp_path / "cpp.vtk"), str(tmp_path / "cpp.dat")
-    out = subprocess.run([exe, vtk, tec], check=True, capture_output=True,
+    vtk, tec, bvtk = (str(tmp_path / "cpp.vtk"), str(tmp_path / "cpp.dat"),
+                      str(tmp_path / "cpp_blocks.vtk"))
+    out = subprocess.run([exe, vtk, tec, bvtk], check=True, capture_output=True,
                          text=True).stdout.split()
     vals = dict(zip(out[0::2], out[1::2]))
     from tmr_gb300 import TMR
@@ -76,14 +77,18 @@ def test_facade_matches_python_binding(gpu_lib, tmp_path):
     f.setBlockBoxes(boxes)
     f.writeForestToVTK(str(tmp_path / "py.vtk"))
     f.writeToTecplot(str(tmp_path / "py.dat"))
+    f.writeToVTK(str(tmp_path / "py_blocks.vtk"))
     assert open(tec).read() == (tmp_path / "py.dat").read_text()
     assert open(vtk).read() == (tmp_path / "py.vtk").read_text()
+    assert open(bvtk).read() == (tmp_path / "py_blocks.vtk").read_text()
 
 
 @pytest.mark.gpu
 def test_quad_facade_matches_python_binding(gpu_lib, tmp_path):
     exe = _build(tmp_path, SRC_QUAD)
-    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
+    fvtk, qvtk = str(tmp_path / "cpp_faces.vtk"), str(tmp_path / "cpp_quads.vtk")
+    out = subprocess.run([exe, fvtk, qvtk], check=True, capture_output=True,
+                         text=True).stdout.split()
     vals = dict(zip(out[0::2], out[1::2]))
     from tmr_gb300 import TMR
     from tmr_gb300 import workloads as W
@@ -111,6 +116,22 @@ def test_quad_facade_matches_python_binding(gpu_lib, tmp_path):
     assert int(vals["P_rows"]) == rows and int(vals["P_nnz"]) == nnz
     assert float(vals["P1_sum"]) == pytest.approx(y.sum(), rel=1e-12)
     assert (int(vals["faces"]), int(vals["edges"]), int(vals["nodes"])) == (6, 17, 12)
+    # the VTK writers through the same face boxes, and seeded random trees
+    boxes = np.zeros((6, 4))
+    boxes[:, 0] = np.arange(6)
+    boxes[:, 2:] = 1.0
+    f.setFaceBoxes(boxes)
+    f.writeToVTK(str(tmp_path / "py_faces.vtk"))
+    f.writeForestToVTK(str(tmp_path / "py_quads.vtk"))
+    assert open(fvtk).read() == (tmp_path / "py_faces.vtk").read_text()
+    assert open(qvtk).read() == (tmp_path / "py_quads.vtk").read_text()
+    r = TMR.QuadForest(order=2)
+    r.setConnectivity(W.brick2d(3, 2))
+    r.createRandomTrees(25, 1, 6, 5)
+    r.repartition()
+    rq = r.getQuadrantsArray().astype(np.int64)
+    assert int(vals["rand_quads"]) == len(rq)
+    assert int(vals["rand_sum"]) == int((rq[:, 1] + 3 * rq[:, 2] + rq[:, 4]).sum())
     # STL tools through the facade = the Python binding
     o = TMR.OctForest(order=2)
     o.setConnectivity(np.arange(8, dtype=np.intc).reshape(1, 8))

@@ -309,3 +309,32 @@ def test_write_to_tecplot(gpu_lib, tmp_path):
     cells = np.array([[int(v) for v in ln.split()] for ln in lines[3 + 3 * nn + nb:3 + 3 * nn + 2 * nb]])
     np.testing.assert_array_equal(cells, conn[:, [0, 1, 3, 2, 4, 5, 7, 6]] + 1)
 
+
+
+def test_write_to_vtk_blocks(gpu_lib, tmp_path):
+    """writeToVTK: the block mesh (as the reference writes it): each
+    connectivity node at its owner block's corner through the block boxes,
+    hexahedra in the (0 1 3 2 4 5 7 6) corner order, the block index as
+    entity_index; nothing without block boxes."""
+    from tmr_gb300 import TMR
+    conn = W.rotate_blocks(W.brick(3, 2, 2), 8)
+    f = TMR.OctForest(order=2)
+    f.setConnectivity(conn)
+    fn = tmp_path / "blocks.vtk"
+    f.writeToVTK(str(fn))
+    assert not fn.exists()
+    boxes = pipeline.brick_boxes(3, 2, 2, ext=(2.0, 1.0, 0.5))
+    f.setBlockBoxes(boxes)
+    f.writeToVTK(str(fn))
+    lines = fn.read_text().split("\n")
+    nb, nn = conn.shape[0], int(conn.max()) + 1
+    i = lines.index("POINTS %d float" % nn)
+    pts = np.array([[float(v) for v in ln.split()] for ln in lines[i + 1:i + 1 + nn]])
+    for k in range(nn):
+        b = min(np.argwhere(conn == k)[:, 0])
+        c = int(np.argwhere(conn[b] == k)[0, 0])
+        uvw = np.array([c & 1, (c >> 1) & 1, c >> 2], np.float64)
+        np.testing.assert_allclose(pts[k], boxes[b, :3] + boxes[b, 3:] * uvw, rtol=1e-6)
+    j = lines.index("CELLS %d %d" % (nb, 9 * nb))
+    cells = np.array([[int(v) for v in ln.split()] for ln in lines[j + 1:j + 1 + nb]])
+    np.testing.assert_array_equal(cells[:, 1:], conn[:, [0, 1, 3, 2, 4, 5, 7, 6]])

@@ -144,6 +144,17 @@ class OctantArray:
             return a["block"], a["x"], a["y"], a["z"], a["tag"], a["level"], a["info"]
         return tuple(a[:, j] for j in range(7))
 
+    def findIndex(self, oc, use_nodes=False):
+        """findIndex (TMR.pyx OctantArray, over TMROctantArray::contains,
+        TMROctant.cpp:404-424): the index of the octant with oc's block,
+        position and level (position alone with use_nodes), or None."""
+        b, x, y, z, _tag, lev, _info = self._fields()
+        m = (b == oc.block) & (x == oc.x) & (y == oc.y) & (z == oc.z)
+        if not use_nodes:
+            m &= lev == oc.level
+        idx = np.flatnonzero(m)
+        return int(idx[0]) if len(idx) else None
+
     def asArray7(self):
         """(n, 7) int32 copy {block, x, y, z, tag, level, info}."""
         if not self.array.dtype.names:
@@ -469,36 +480,15 @@ class OctForest:
             raise ValueError("Cannot interpolate between the same object")
         vec._create(self, forest)
 
-    def writeToVTK(self, fname):
-        """Legacy-VTK unstructured grid of the octants (one hexahedron each,
-        block-local integer coordinates)."""
-        o = self.getOctantsArray()
-        h = (1 << (30 - o[:, 5].astype(np.int64)))
-        with open(fname, "w") as fp:
-            fp.write("# vtk DataFile Version 3.0\ntmr_gb300 forest\nASCII\n")
-            fp.write("DATASET UNSTRUCTURED_GRID\nPOINTS %d double\n" % (8 * len(o)))
-            for r, hh in zip(o, h):
-                for c in (0, 1, 3, 2, 4, 5, 7, 6):
-                    fp.write("%g %g %g\n" % ((r[1] + hh * (c & 1)) / 2.0 ** 30 + r[0],
-                                             (r[2] + hh * ((c >> 1) & 1)) / 2.0 ** 30,
-                                             (r[3] + hh * (c >> 2)) / 2.0 ** 30))
-            fp.write("CELLS %d %d\n" % (len(o), 9 * len(o)))
-            for i in range(len(o)):
-                fp.write("8 " + " ".join(str(8 * i + k) for k in range(8)) + "\n")
-            fp.write("CELL_TYPES %d\n" % len(o))
-            fp.write("12\n" * len(o))
-
-
-    def writeToTecplot(self, fname):
-        """writeToTecplot (TMROctForest.cpp:1233-1311): the block mesh as one
-        Tecplot FEBRICK zone, each block connectivity node at its owner
+    def _block_node_points(self):
+        """(block_conn, X): each block connectivity node at its owner
         block's corner (the lowest-numbered block touching it) mapped
-        through that block's volume, and the block index as a cell-centred
-        variable.  The block boxes (setBlockBoxes) stand in for the
-        topology's volumes; nothing is written when no boxes are set."""
+        through that block's box, as the reference evaluates the owner's
+        volume (node_block_owners, TMROctForest.cpp:1090-1143); None
+        without block boxes."""
         boxes = getattr(self, "_boxes", None)
         if boxes is None:
-            return
+            return None
         bc = self.getConnectivity()[0]
         nb = bc.shape[0]
         nn = int(bc.max()) + 1 if nb else 0
@@ -510,6 +500,46 @@ class OctForest:
             corner = next(c for c in range(8) if bc[b, c] == k)
             uvw = np.array([corner & 1, (corner >> 1) & 1, corner >> 2], np.float64)
             X[k] = boxes[b, :3] + boxes[b, 3:] * uvw
+        return bc, X
+
+    def writeToVTK(self, fname):
+        """writeToVTK (TMROctForest.cpp:1149-1228): the block mesh as VTK
+        hexahedra, each connectivity node at its owner block's corner
+        through the block boxes (the topology's volumes in the reference),
+        the block index as the cell scalar entity_index; nothing is written
+        when no boxes are set (the reference needs a topology)."""
+        bx = self._block_node_points()
+        if bx is None:
+            return
+        bc, X = bx
+        nb = bc.shape[0]
+        with open(fname, "w") as fp:
+            fp.write("# vtk DataFile Version 3.0\nvtk output\nASCII\n")
+            fp.write("DATASET UNSTRUCTURED_GRID\nPOINTS %d float\n" % X.shape[0])
+            for p in X:
+                fp.write("%e %e %e\n" % (p[0], p[1], p[2]))
+            fp.write("\nCELLS %d %d\n" % (nb, 9 * nb))
+            for c in bc:
+                fp.write("8 %d %d %d %d %d %d %d %d\n" % (c[0], c[1], c[3], c[2], c[4], c[5],
+                                                          c[7], c[6]))
+            fp.write("\nCELL_TYPES %d\n" % nb)
+            fp.write("12\n" * nb)
+            fp.write("CELL_DATA %d\nSCALARS entity_index float 1\nLOOKUP_TABLE default\n" % nb)
+            for k in range(nb):
+                fp.write("%e\n" % (1.0 * k))
+
+    def writeToTecplot(self, fname):
+        """writeToTecplot (TMROctForest.cpp:1233-1311): the block mesh as one
+        Tecplot FEBRICK zone, each block connectivity node at its owner
+        block's corner (the lowest-numbered block touching it) mapped
+        through that block's volume, and the block index as a cell-centred
+        variable.  The block boxes (setBlockBoxes) stand in for the
+        topology's volumes; nothing is written when no boxes are set."""
+        bx = self._block_node_points()
+        if bx is None:
+            return
+        bc, X = bx
+        nb, nn = bc.shape[0], X.shape[0]
         with open(fname, "w") as fp:
             fp.write("Variables = X,Y,Z,block\n")
             fp.write("Zone N = %d E = %d " % (nn, nb))
@@ -594,6 +624,17 @@ class QuadrantArray:
             raise IndexError("Quadrant array index %d out of range [0,%d)" % (k, n))
         return Quadrant(*(int(v) for v in self.array[k]))
 
+    def findIndex(self, quad, use_nodes=False):
+        """findIndex (TMR.pyx QuadrantArray, over TMRQuadrantArray::contains):
+        the index of the quadrant with quad's face, position and level
+        (position alone with use_nodes), or None."""
+        a = self.array
+        m = (a[:, 0] == quad.face) & (a[:, 1] == quad.x) & (a[:, 2] == quad.y)
+        if not use_nodes:
+            m &= a[:, 4] == quad.level
+        idx = np.flatnonzero(m)
+        return int(idx[0]) if len(idx) else None
+
 
 class QuadForest:
     """Forest of quadtrees on one GPU (TMRQuadForest, TMR.pyx QuadForest):
@@ -667,6 +708,16 @@ class QuadForest:
         fe = np.zeros((sz[0], 4), np.intc)
         call("tmrg_qforest_get_connectivity", self.ptr, _ptr(sz), _ptr(fc), _ptr(fe))
         return fc, fe, int(sz[2]), int(sz[1])
+
+    def createRandomTrees(self, nrand=10, min_lev=0, max_lev=8, seed=0):
+        """TMRQuadForest::createRandomTrees (TMRQuadForest.cpp:1327-1407) with a
+        seeded generator in place of libc rand()."""
+        call("tmrg_qforest_create_random_trees", self.ptr, nrand, min_lev, max_lev, seed)
+
+    def repartition(self):
+        """TMRQuadForest::repartition: the forest lives on one GPU, nothing
+        to redistribute."""
+        return None
 
     def createTrees(self, depth=0):
         call("tmrg_qforest_create_trees", self.ptr, depth)
@@ -764,6 +815,70 @@ class QuadForest:
         if b.ndim != 2 or b.shape[1] != 4:
             raise ValueError("Expected array of shape (n, 4)")
         call("tmrg_qforest_set_face_boxes", self.ptr, _ptr(b), b.shape[0])
+        self._boxes = b.copy()
+
+    def writeToVTK(self, fname):
+        """writeToVTK (TMRQuadForest.cpp:651-720): the face mesh as VTK
+        quadrilaterals, each connectivity node at its owner face's corner
+        (the lowest-numbered face touching it) through the face boxes (the
+        topology's surfaces in the reference), the face index as the cell
+        scalar entity_index; nothing is written when no boxes are set."""
+        boxes = getattr(self, "_boxes", None)
+        if boxes is None:
+            return
+        fc = self.getConnectivity()[0]
+        nf = fc.shape[0]
+        nn = int(fc.max()) + 1 if nf else 0
+        owner = np.full(nn, nf, np.int64)
+        np.minimum.at(owner, fc.ravel(), np.repeat(np.arange(nf), 4))
+        with open(fname, "w") as fp:
+            fp.write("# vtk DataFile Version 3.0\nvtk output\nASCII\n")
+            fp.write("DATASET UNSTRUCTURED_GRID\nPOINTS %d float\n" % nn)
+            for k in range(nn):
+                f = owner[k]
+                corner = next(c for c in range(4) if fc[f, c] == k)
+                p = boxes[f, :2] + boxes[f, 2:] * np.array([corner & 1, corner >> 1], np.float64)
+                fp.write("%e %e %e\n" % (p[0], p[1], 0.0))
+            fp.write("\nCELLS %d %d\n" % (nf, 5 * nf))
+            for c in fc:
+                fp.write("4 %d %d %d %d\n" % (c[0], c[1], c[3], c[2]))
+            fp.write("\nCELL_TYPES %d\n" % nf)
+            fp.write("9\n" * nf)
+            fp.write("CELL_DATA %d\nSCALARS entity_index float 1\nLOOKUP_TABLE default\n" % nf)
+            for k in range(nf):
+                fp.write("%e\n" % (1.0 * k))
+
+    def writeForestToVTK(self, fname):
+        """writeForestToVTK (TMRQuadForest.cpp:809-870): every quadrant as a
+        quadrilateral with its own four corners (x fastest) through its
+        face's box, the face index as the cell scalar entity_index; nothing
+        is written when no boxes are set."""
+        boxes = getattr(self, "_boxes", None)
+        if boxes is None:
+            return
+        q = self.getQuadrantsArray()
+        n = len(q)
+        h = (1 << (30 - q[:, 4].astype(np.int64)))
+        hmax = float(1 << 30)
+        with open(fname, "w") as fp:
+            fp.write("# vtk DataFile Version 3.0\nvtk output\nASCII\n")
+            fp.write("DATASET UNSTRUCTURED_GRID\nPOINTS %d float\n" % (4 * n))
+            for r, hh in zip(q, h):
+                b = boxes[r[0]]
+                for jj in range(2):
+                    for ii in range(2):
+                        u = 1.0 * (r[1] + ii * hh) / hmax
+                        v = 1.0 * (r[2] + jj * hh) / hmax
+                        fp.write("%e %e %e\n" % (b[0] + b[2] * u, b[1] + b[3] * v, 0.0))
+            fp.write("\nCELLS %d %d\n" % (n, 5 * n))
+            for k in range(n):
+                c = 4 * k
+                fp.write("4 %d %d %d %d\n" % (c, c + 1, c + 3, c + 2))
+            fp.write("\nCELL_TYPES %d\n" % n)
+            fp.write("9\n" * n)
+            fp.write("CELL_DATA %d\nSCALARS entity_index float 1\nLOOKUP_TABLE default\n" % n)
+            for r in q:
+                fp.write("%e\n" % (1.0 * r[0]))
 
     def getPoints(self):
         s = self._sizes()

@@ -106,6 +106,7 @@ _SIGS = {
     "tmrg_qforest_set_mesh_order": [c_vp, c_int, c_int],
     "tmrg_qforest_get_mesh_order": [c_vp, c_vp, c_vp, c_vp],
     "tmrg_qforest_create_trees": [c_vp, c_int],
+    "tmrg_qforest_create_random_trees": [c_vp, c_int, c_int, c_int, c_u64],
     "tmrg_qforest_refine": [c_vp, c_vp, c_i64, c_int, c_int],
     "tmrg_qforest_refine_device": [c_vp, c_vp, c_i64, c_int, c_int],
     "tmrg_qforest_coarsen": [c_vp, P(c_vp)],

@@ -1313,6 +1313,10 @@ int tmrg_qforest_get_mesh_order(tmrg_qforest *f, int *order, int *interp, double
 int tmrg_qforest_create_trees(tmrg_qforest *f, int level) {
   return guarded([&] { qforest_create_trees(QF(f), level); });
 }
+int tmrg_qforest_create_random_trees(tmrg_qforest *f, int nrand, int min_level, int max_level,
+                                     uint64_t seed) {
+  return guarded([&] { qforest_create_random_trees(QF(f), nrand, min_level, max_level, seed); });
+}
 int tmrg_qforest_refine(tmrg_qforest *f, const int *refine, int64_t n, int min_level,
                         int max_level) {
   return guarded([&] {

@@ -699,20 +699,6 @@ void forest_balance(Forest &f, int corner) {
 }
 
 // ---------------------------------------------------------------------
-// Seeded uniform U(seed, stream, i) in [0, 1): splitmix64 of the seed and
-// stream, mixed with the index (same function as oo_uniform and
-// workloads.uniform).
-__device__ __forceinline__ double seeded_uniform(uint64_t seed, uint64_t stream, uint64_t i) {
-  auto sm = [](uint64_t x) {
-    x += 0x9E3779B97F4A7C15ULL;
-    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
-    x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
-    return x ^ (x >> 31);
-  };
-  uint64_t r = sm(sm(seed * 0x100000001B3ULL + stream) ^ (i * 0xD6E8FEB86659FD93ULL));
-  return (double)(r >> 11) * (1.0 / 9007199254740992.0);
-}
-
 __global__ void k_random_refinement(uint64_t seed, uint64_t stream, double prob,
                                     int *out, long long n) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;

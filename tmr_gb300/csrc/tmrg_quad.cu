@@ -574,6 +574,68 @@ void qforest_refine(QForest &f, const int *d_ref, long long nref, int min_level,
     q_refine_sort_compact<uint64_t>(f, a, K, cnt, total);
 }
 
+// createRandomTrees (TMRQuadForest.cpp:1327-1407): nrand quadrants per face
+// at a random level in [min_level, max_level] and a random anchor of that
+// level, sorted, and made unique on position keeping the finest (the
+// reference's TMRQuadrantArray::sort).  The reference draws from libc
+// rand(); here quadrant i of face f draws U(seed, f, 3i + k), k = 0..2.
+template <typename Key>
+__global__ void k_q_random_quads(long long total, int nrand, int min_level, int max_level,
+                                 uint64_t seed, QKeyT<Key> K, Key *keys) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const unsigned tu = (unsigned)t;  // total < 2^32
+  const int b = (int)(tu / (unsigned)nrand), i = (int)(tu - (unsigned)b * (unsigned)nrand);
+  const uint64_t base = 3ULL * (uint64_t)i;
+  int level = min_level + (int)(seeded_uniform(seed, b, base) * (max_level - min_level + 1));
+  if (level > max_level) level = max_level;
+  const int32_t h = side_of(level);
+  const double cells = (double)(1 << level);
+  int32_t c[2];
+  for (int k = 0; k < 2; k++) {
+    int32_t q = (int32_t)(seeded_uniform(seed, b, base + 1 + k) * cells);
+    if (q >= (1 << level)) q = (1 << level) - 1;
+    c[k] = h * q;
+  }
+  keys[t] = K.make(b, c[0], c[1], level);
+}
+template <typename Key>
+static void q_random_sort_compact(QForest &f, long long total, int nrand, int min_level,
+                                  int max_level, uint64_t seed, const QKeyT<Key> &K) {
+  cudaStream_t s = f.s;
+  DBuf<Key> keys(std::max(1LL, total), s);
+  launch(k_q_random_quads<Key>, blocks_for(total, 256), 256, 0, s, total, nrand, min_level,
+         max_level, seed, K, keys.p);
+  sort_keys(keys, nullptr, total, K.total_bits(), s);
+  DBuf<unsigned> pos(total + 1, s);
+  launch(k_q_dedupe<Key>, blocks_for(total, 256), 256, 0, s, total, (const Key *)keys.p, pos.p);
+  exclusive_scan<unsigned>(pos.p, pos.p, total, s);
+  const unsigned m = total ? read_scalar(pos.p + total, s) : 0u;
+  q_alloc(f, m);
+  launch(k_q_compact<Key>, blocks_for(total, 256), 256, 0, s, total, K, (const Key *)keys.p,
+         (const uint32_t *)nullptr, (const unsigned *)pos.p, (const int16_t *)nullptr, f.block.p,
+         f.x.p, f.y.p, f.level.p, f.info.p);
+}
+void qforest_create_random_trees(QForest &f, int nrand, int min_level, int max_level,
+                                 uint64_t seed) {
+  Stage st("tmrg_quad_create_random_trees");
+  if (!f.conn) throw Error(TMRG_ERR_STATE, "createRandomTrees: no connectivity");
+  if (nrand < 0) throw Error(TMRG_ERR_ARG, "createRandomTrees: nrand < 0");
+  if (min_level < 0) min_level = 0;
+  if (max_level >= TMRG_MAX_LEVEL) max_level = TMRG_MAX_LEVEL - 1;
+  if (min_level > max_level) min_level = max_level;
+  f.free_nodes();
+  const long long total = (long long)f.conn->nf * nrand;
+  if (total >= (1LL << 32)) throw Error(TMRG_ERR_ARG, "createRandomTrees: too many quadrants");
+  f.maxlev = max_level;
+  const QKey K = f.key();
+  if (K.total_bits() > 64)
+    q_random_sort_compact<U128>(f, total, nrand, min_level, max_level, seed, qkey_as<U128>(K));
+  else
+    q_random_sort_compact<uint64_t>(f, total, nrand, min_level, max_level, seed, K);
+  TMRG_CUDA(cudaStreamSynchronize(f.s));
+}
+
 // coarsen (TMRQuadForest.cpp:1594-1640)
 __global__ void k_q_coarsen_flags(long long n, const int *__restrict__ xs,
                                   const int *__restrict__ ys, const int16_t *__restrict__ lev,

@@ -65,6 +65,8 @@ struct QForest {
 };
 
 void qforest_create_trees(QForest &f, int level);
+void qforest_create_random_trees(QForest &f, int nrand, int min_level, int max_level,
+                                 uint64_t seed);
 void qforest_refine(QForest &f, const int *d_ref, long long nref, int min_level, int max_level);
 void qforest_coarsen(QForest &f, QForest &out);
 void qforest_duplicate(QForest &f, QForest &out);
