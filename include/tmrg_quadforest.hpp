@@ -226,6 +226,61 @@ class TMRQuadForest : public TMRGEntity {
     for (int q = 0; q < nf; q++) fprintf(fp, "%e\n", 1.0 * q);
     fclose(fp);
   }
+  // writeToTecplot (TMRQuadForest.cpp:729-804): the face mesh as one
+  // Tecplot FEQUADRILATERAL zone, nodes at their owner face's corner through
+  // the face boxes, the face index cell-centred; nothing without face boxes.
+  void writeToTecplot(const char *filename) {
+    if (boxes_.empty()) return;
+    int nf = 0, ne = 0, nn = 0;
+    const int *fc = nullptr, *fe = nullptr;
+    getConnectivity(&nf, &ne, &nn, &fc, &fe);
+    FILE *fp = filename ? fopen(filename, "w") : nullptr;
+    if (!fp) return;
+    std::vector<int> owner(nn, nf);
+    for (int q = 0; q < nf; q++)
+      for (int c = 0; c < 4; c++)
+        if (q < owner[fc[4 * q + c]]) owner[fc[4 * q + c]] = q;
+    std::vector<double> X(3 * (size_t)nn, 0.0);
+    for (int k = 0; k < nn; k++) {
+      const int q = owner[k];
+      if (q >= nf) continue;
+      int corner = 0;
+      while (corner < 4 && fc[4 * q + corner] != k) corner++;
+      X[3 * k] = boxes_[4 * q] + boxes_[4 * q + 2] * (1.0 * (corner & 1));
+      X[3 * k + 1] = boxes_[4 * q + 1] + boxes_[4 * q + 3] * (1.0 * (corner >> 1));
+    }
+    fprintf(fp, "Variables = X,Y,Z,face\n");
+    fprintf(fp, "Zone N = %d E = %d ", nn, nf);
+    fprintf(fp, "DATAPACKING=BLOCK, ZONETYPE=FEQUADRILATERAL\n");
+    fprintf(fp, "VARLOCATION = ([4]=CELLCENTERED)\n");
+    for (int d = 0; d < 3; d++)
+      for (int k = 0; k < nn; k++) fprintf(fp, "%e\n", X[3 * k + d]);
+    for (int q = 0; q < nf; q++) fprintf(fp, "%e\n", 1.0 * q);
+    for (int q = 0; q < nf; q++)
+      fprintf(fp, "%d %d %d %d\n", fc[4 * q] + 1, fc[4 * q + 1] + 1, fc[4 * q + 3] + 1,
+              fc[4 * q + 2] + 1);
+    fclose(fp);
+  }
+  // getNodeNumbers / getLocalNodeNumber / getExtPreOffset (TMRQuadForest.h):
+  // the local nodes are numbered -num_dep .. -1, then the owned nodes.
+  int getNodeNumbers(const int **nodes) {
+    int64_t sz[6] = {0};
+    tmrg_qforest_sizes(f, sz);
+    nums_.resize((size_t)(sz[1] + sz[2]));
+    for (int64_t i = 0; i < sz[1] + sz[2]; i++) nums_[i] = (int)(i - sz[2]);
+    if (nodes) *nodes = nums_.data();
+    return (int)(sz[1] + sz[2]);
+  }
+  int getLocalNodeNumber(int node) {
+    int64_t sz[6] = {0};
+    tmrg_qforest_sizes(f, sz);
+    return (node >= -sz[2] && node < sz[1]) ? (int)(node + sz[2]) : -1;
+  }
+  int getExtPreOffset() {
+    int64_t sz[6] = {0};
+    tmrg_qforest_sizes(f, sz);
+    return (int)sz[3];
+  }
   // writeForestToVTK (TMRQuadForest.cpp:809-870): every quadrant as a
   // quadrilateral with its own four corners (x fastest) through its face's
   // box, the face index as entity_index; nothing without face boxes.
@@ -271,7 +326,7 @@ class TMRQuadForest : public TMRGEntity {
   tmrg_qforest *f;
   void *stream;
   TMRQuadrantArray quads_;
-  std::vector<int> fc_, fe_, conn_, dptr_, dconn_;
+  std::vector<int> fc_, fe_, conn_, dptr_, dconn_, nums_;
   std::vector<double> dw_, knots_, boxes_;
   int range_[2];
 };

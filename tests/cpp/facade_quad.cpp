@@ -68,6 +68,11 @@ int main(int argc, char **argv) {
   f->setFaceBoxes(boxes.data(), nfaces);
   f->writeToVTK(argc > 1 ? argv[1] : "/dev/null");
   f->writeForestToVTK(argc > 2 ? argv[2] : "/dev/null");
+  f->writeToTecplot(argc > 3 ? argv[3] : "/dev/null");
+  const int *qnums = nullptr;
+  const int nnum = f->getNodeNumbers(&qnums);
+  printf("node_numbers %d first %d local_of_first %d ext_pre %d\n", nnum, nnum ? qnums[0] : 0,
+         nnum ? f->getLocalNodeNumber(qnums[0]) : -1, f->getExtPreOffset());
   // seeded random trees
   TMRQuadForest *r = new TMRQuadForest(0, 2, TMR_GAUSS_LOBATTO_POINTS);
   r->incref();

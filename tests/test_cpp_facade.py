@@ -86,8 +86,9 @@ def test_facade_matches_python_binding(gpu_lib, tmp_path):
 @pytest.mark.gpu
 def test_quad_facade_matches_python_binding(gpu_lib, tmp_path):
     exe = _build(tmp_path, SRC_QUAD)
-    fvtk, qvtk = str(tmp_path / "cpp_faces.vtk"), str(tmp_path / "cpp_quads.vtk")
-    out = subprocess.run([exe, fvtk, qvtk], check=True, capture_output=True,
+    fvtk, qvtk, tec = (str(tmp_path / "cpp_faces.vtk"), str(tmp_path / "cpp_quads.vtk"),
+                       str(tmp_path / "cpp_faces.dat"))
+    out = subprocess.run([exe, fvtk, qvtk, tec], check=True, capture_output=True,
                          text=True).stdout.split()
     vals = dict(zip(out[0::2], out[1::2]))
     from tmr_gb300 import TMR
@@ -125,6 +126,12 @@ def test_quad_facade_matches_python_binding(gpu_lib, tmp_path):
     f.writeForestToVTK(str(tmp_path / "py_quads.vtk"))
     assert open(fvtk).read() == (tmp_path / "py_faces.vtk").read_text()
     assert open(qvtk).read() == (tmp_path / "py_quads.vtk").read_text()
+    f.writeToTecplot(str(tmp_path / "py_faces.dat"))
+    assert open(tec).read() == (tmp_path / "py_faces.dat").read_text()
+    nums = f.getNodeNumbers()
+    assert int(vals["node_numbers"]) == len(nums) and int(vals["first"]) == int(nums[0])
+    assert int(vals["local_of_first"]) == f.getLocalNodeNumber(int(nums[0])) == 0
+    assert int(vals["ext_pre"]) == f.getExtPreOffset()
     r = TMR.QuadForest(order=2)
     r.setConnectivity(W.brick2d(3, 2))
     r.createRandomTrees(25, 1, 6, 5)

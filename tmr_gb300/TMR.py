@@ -848,6 +848,38 @@ class QuadForest:
             for k in range(nf):
                 fp.write("%e\n" % (1.0 * k))
 
+    def writeToTecplot(self, fname):
+        """writeToTecplot (TMRQuadForest.cpp:729-804): the face mesh as one
+        Tecplot FEQUADRILATERAL zone, nodes at their owner face's corner
+        through the face boxes, the face index cell-centred; nothing is
+        written when no boxes are set."""
+        boxes = getattr(self, "_boxes", None)
+        if boxes is None:
+            return
+        fc = self.getConnectivity()[0]
+        nf = fc.shape[0]
+        nn = int(fc.max()) + 1 if nf else 0
+        owner = np.full(nn, nf, np.int64)
+        np.minimum.at(owner, fc.ravel(), np.repeat(np.arange(nf), 4))
+        X = np.zeros((nn, 3))
+        for k in range(nn):
+            f = owner[k]
+            corner = next(c for c in range(4) if fc[f, c] == k)
+            X[k, :2] = boxes[f, :2] + boxes[f, 2:] * np.array([corner & 1, corner >> 1],
+                                                              np.float64)
+        with open(fname, "w") as fp:
+            fp.write("Variables = X,Y,Z,face\n")
+            fp.write("Zone N = %d E = %d " % (nn, nf))
+            fp.write("DATAPACKING=BLOCK, ZONETYPE=FEQUADRILATERAL\n")
+            fp.write("VARLOCATION = ([4]=CELLCENTERED)\n")
+            for d in range(3):
+                for k in range(nn):
+                    fp.write("%e\n" % X[k, d])
+            for k in range(nf):
+                fp.write("%e\n" % (1.0 * k))
+            for c in fc:
+                fp.write("%d %d %d %d\n" % (c[0] + 1, c[1] + 1, c[3] + 1, c[2] + 1))
+
     def writeForestToVTK(self, fname):
         """writeForestToVTK (TMRQuadForest.cpp:809-870): every quadrant as a
         quadrilateral with its own four corners (x fastest) through its
