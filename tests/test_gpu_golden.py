@@ -32,3 +32,27 @@ def test_gpu_matches_reference_digest(gpu_lib, name):
     z = np.load(os.path.join(pipeline.GOLDEN_DIR, "digest_%s.npz" % name))
     bad = pipeline.compare_digest(g, z)
     assert not bad, "\n".join(bad)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cand", range(3))
+def test_every_radix_candidate_matches_reference(gpu_lib, cand):
+    # every radix-scatter shape the autotuner may pick gives the reference's
+    # products: the one-tree configuration at full size (hundreds of tiles
+    # per sort), a rotated multi-block forest and a level-29 forest (128-bit
+    # keys, sorted as two 64-bit stages)
+    import numpy as np
+    from tmr_gb300 import TMR
+    lib = TMR.lib()
+    assert lib.tmrg_tune_force(5, cand) == 0
+    try:
+        case = pipeline.golden_case("digest_c1")
+        z = np.load(os.path.join(pipeline.GOLDEN_DIR, "digest_c1.npz"))
+        bad = pipeline.compare_digest(pipeline.run_gpu(case), z)
+        assert not bad, "\n".join(bad)
+        for name in ("rot_o3", "deep_l29"):
+            g = pipeline.run_gpu(pipeline.golden_case(name))
+            bad = pipeline.compare(g, pipeline.load_golden(name))
+            assert not bad, name + "\n" + "\n".join(bad)
+    finally:
+        lib.tmrg_tune_force(5, -1)
