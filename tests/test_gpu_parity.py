@@ -203,3 +203,52 @@ def test_every_apply_shape_matches_oracle(gpu_lib):
         lib.tmrg_tune_force(2, -1)
     np.testing.assert_array_equal(out[6][0], out[4][0])
     np.testing.assert_array_equal(out[6][1], out[4][1])
+
+
+@pytest.mark.gpu
+def test_applies_outside_double_float_window(gpu_lib):
+    # inputs the double-float pairs cannot hold (|x| < 2^-40 or >= 2^60) send
+    # the applies to FP64: device and host-buffer P and P^T still match the
+    # oracle's CSR within 1e-13, including the host-buffer paths that split
+    # their input in pieces (a piece with such a value switches the rows
+    # computed after it)
+    import ctypes
+
+    import bench
+    import torch
+
+    from oracle.oracle import _lib
+    case = bench.cpu_sample_case()
+    g = pipeline.run_gpu(dict(case, coarse_levels=1))
+    I = g["levels"][0]["I"]
+    rows, ncols, _ = I.sizes()
+    assert rows > 16 * 4096
+    k = 16
+    rp, cols, vals = I.getCSR()
+    L = _lib("oracle").lib
+    P_ = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    rng = np.random.default_rng(31)
+    for scale, tiny in ((1.0, True), (1e30, False)):
+        x = rng.standard_normal(ncols * k) * scale
+        xf = rng.standard_normal(rows * k) * scale
+        if tiny:
+            # a few values below the window in the last input pieces
+            x[-5 * k::k] = 1e-20
+            xf[-7 * k::k] = -3e-19
+        y_ref = np.zeros(rows * k)
+        L.oo_csr_mult(rows, P_(rp), P_(cols), P_(vals), k, P_(x), P_(y_ref))
+        yt_ref = np.zeros(ncols * k)
+        L.oo_csr_mult_t(rows, ncols, P_(rp), P_(cols), P_(vals), k, P_(xf), P_(yt_ref))
+        yd = torch.empty(rows * k, dtype=torch.float64, device="cuda")
+        I.mult(torch.tensor(x, device="cuda"), yd)
+        ytd = torch.empty(ncols * k, dtype=torch.float64, device="cuda")
+        I.multTranspose(torch.tensor(xf, device="cuda"), ytd)
+        yh = torch.empty(rows * k, dtype=torch.float64, pin_memory=True).numpy()
+        I.mult(x, yh)
+        yth = np.zeros(ncols * k)
+        I.multTranspose(xf, yth)
+        for got, ref, what in ((yd.cpu().numpy(), y_ref, "P device"), (yh, y_ref, "P host"),
+                               (ytd.cpu().numpy(), yt_ref, "PT device"),
+                               (yth, yt_ref, "PT host")):
+            np.testing.assert_allclose(got / scale, ref / scale, rtol=1e-13, atol=1e-13,
+                                       err_msg="%s, scale %g" % (what, scale))

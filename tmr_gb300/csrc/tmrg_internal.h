@@ -119,6 +119,9 @@ struct Interp {
   DBuf<int> t_rowptr, t_colidx;  // P^T (zero-free) as CSR, rows = coarse nodes
   DBuf<int> t_perm;  // P^T rows by input chunk of their last entry, then length
   std::vector<long long> t_chunk;  // t_perm range of each input chunk
+  // largest column read by each LO_WIN-row window of the apply copy (host
+  // copy, made by the first host-buffer prolongation)
+  std::vector<int> win_maxcol;
   DBuf<float2> t_w;  // P^T weights (hi, lo)
   // dfflag[0]: a weight outside the double-float window (the applies then
   // run in FP64); dfflag[1]: the same for the input vector of one apply

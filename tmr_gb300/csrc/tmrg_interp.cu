@@ -2679,15 +2679,36 @@ bool interp_apply_transpose_staged(Interp &I, int which, const double *xh, doubl
   return true;
 }
 
-// Prolongation with the output in host memory: the input (coarse values)
-// is copied first, then the rows are computed in FC_CHUNKS pieces of whole
-// 4096-row windows (the length-ordered permutation stays inside a window,
-// so a piece of slots is exactly a piece of rows) into device memory, and
-// each piece is copied to the host on a second stream while the next piece
-// computes.  One bulk copy per piece runs the host link at its copy rate
-// (the kernel writing host memory directly ran it at less than half).
-// Same kernel, rows and summation order as the single apply.  Returns
-// false (nothing done) where the pair kernel does not apply.
+// Largest column of each LO_WIN-row window of a column-sorted CSR (the last
+// entry of each row), -1 for a window of empty rows; wmax starts at -1.
+__global__ void k_win_maxcol(long long rows, const int *__restrict__ rp,
+                             const int *__restrict__ ci, int *wmax) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int m = -1;
+  if (r < rows) {
+    const int a = rp[r], b = rp[r + 1];
+    if (b > a) m = ci[b - 1];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  // a warp's 32 rows lie in one window (LO_WIN is a multiple of 32)
+  if ((threadIdx.x & 31) == 0 && r < rows && m >= 0) atomicMax(wmax + r / LO_WIN, m);
+}
+
+// Prolongation with the input and the output in host memory: the input
+// (coarse values) is copied in FC_CHUNKS column ranges on a second stream,
+// and the rows are computed in FC_CHUNKS pieces of whole 4096-row windows
+// (the length-ordered permutation stays inside a window, so a piece of
+// slots is exactly a piece of rows) into device memory, each piece as soon
+// as the input range holding its largest column has arrived and been split
+// (rows and columns follow the same node order, so piece k mostly needs
+// the first ranges), and each piece is copied to the host on a third
+// stream while the next piece computes.  One bulk copy per piece runs the
+// host link at its copy rate (the kernel writing host memory directly ran
+// it at less than half).  Same kernel, rows and summation order as the
+// single apply; as in the transpose, a range with a value outside the
+// double-float window sends the rows computed after its split to FP64.
+// Returns false (nothing done) where the pair kernel does not apply.
 constexpr int FC_CHUNKS = 16;
 bool interp_apply_forward_staged(Interp &I, const double *xh, double *dx, double *yh,
                                  int nvec) {
@@ -2696,24 +2717,69 @@ bool interp_apply_forward_staged(Interp &I, const double *xh, double *dx, double
   Stage st("tmrg_interp_mult_staged");
   cudaStream_t s = I.s;
   const long long nin = I.cols, rows = I.rows;
-  TMRG_CUDA(cudaMemcpyAsync(dx, xh, sizeof(double) * nin * nvec, cudaMemcpyHostToDevice, s));
+  const long long nwin = (rows + LO_WIN - 1) / LO_WIN;
+  if ((long long)I.win_maxcol.size() != nwin) {
+    DBuf<int> wm(nwin, s);
+    TMRG_CUDA(cudaMemsetAsync(wm.p, 0xff, sizeof(int) * nwin, s));
+    launch(k_win_maxcol, blocks_for(rows, 256), 256, 0, s, rows, I.ap_rowptr(), I.ap_colidx(),
+           wm.p);
+    I.win_maxcol.resize(nwin);
+    TMRG_CUDA(cudaMemcpyAsync(I.win_maxcol.data(), wm.p, sizeof(int) * nwin,
+                              cudaMemcpyDeviceToHost, s));
+    TMRG_CUDA(cudaStreamSynchronize(s));
+    g_host_syncs.fetch_add(1, std::memory_order_relaxed);
+  }
   DBuf<float2> xs(nin * nvec + 1, s);
   TMRG_CUDA(cudaMemsetAsync(I.dfflag.p + 1, 0, sizeof(int), s));
-  df_split_input(I, dx, nin * nvec, xs, s);
   DBuf<double> dy(rows * nvec + 2, s);
   double *y = dy.p;
   if ((uintptr_t)y % 16) y++;
   const int n2 = nvec / 2;
   const int shape = tune_lookup(df_key(0, rows, I.nnz_nz, n2));
-  cudaStream_t cs;
+  cudaStream_t is, cs;
+  TMRG_CUDA(cudaStreamCreateWithFlags(&is, cudaStreamNonBlocking));
   TMRG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-  cudaEvent_t ev[FC_CHUNKS];
+  cudaEvent_t iev[FC_CHUNKS + 1], ev[FC_CHUNKS];
+  for (int k = 0; k <= FC_CHUNKS; k++)
+    TMRG_CUDA(cudaEventCreateWithFlags(&iev[k], cudaEventDisableTiming));
   for (int k = 0; k < FC_CHUNKS; k++)
     TMRG_CUDA(cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming));
-  const long long nwin = (rows + LO_WIN - 1) / LO_WIN;
+  // input ranges: columns [c0[j], c0[j + 1]), copied in order after the work
+  // already queued on the forest stream
+  long long c0[FC_CHUNKS + 1];
+  for (int j = 0; j <= FC_CHUNKS; j++) c0[j] = nin * j / FC_CHUNKS;
+  TMRG_CUDA(cudaEventRecord(iev[FC_CHUNKS], s));
+  TMRG_CUDA(cudaStreamWaitEvent(is, iev[FC_CHUNKS], 0));
+  for (int j = 0; j < FC_CHUNKS; j++) {
+    if (c0[j + 1] > c0[j])
+      TMRG_CUDA(cudaMemcpyAsync(dx + c0[j] * nvec, xh + c0[j] * nvec,
+                                sizeof(double) * (c0[j + 1] - c0[j]) * nvec,
+                                cudaMemcpyHostToDevice, is));
+    TMRG_CUDA(cudaEventRecord(iev[j], is));
+  }
+  int split = 0;  // input ranges [0, split) are on the device and split
   for (int k = 0; k < FC_CHUNKS; k++) {
-    const long long r0 = std::min(rows, (nwin * k / FC_CHUNKS) * LO_WIN);
-    const long long r1 = std::min(rows, (nwin * (k + 1) / FC_CHUNKS) * LO_WIN);
+    const long long w0 = nwin * k / FC_CHUNKS, w1 = nwin * (k + 1) / FC_CHUNKS;
+    const long long r0 = std::min(rows, w0 * LO_WIN), r1 = std::min(rows, w1 * LO_WIN);
+    int need = -1;  // largest column the piece reads
+    for (long long w = w0; w < w1; w++) need = std::max(need, I.win_maxcol[w]);
+    // ranges up to the one holding `need` (all of them if a column were
+    // out of range)
+    int upto = need < 0 ? 0 : FC_CHUNKS;
+    for (int j = 0; j < FC_CHUNKS && need >= 0; j++)
+      if (need < c0[j + 1]) {
+        upto = j + 1;
+        break;
+      }
+    for (; split < upto; split++) {
+      TMRG_CUDA(cudaStreamWaitEvent(s, iev[split], 0));
+      const long long a = c0[split], b = c0[split + 1];
+      if (b > a) {
+        prof_bytes(16 * (b - a) * nvec);
+        launch(k_df_split_x, blocks_for((b - a) * nvec, 256), 256, 0, s, (b - a) * nvec,
+               (const double *)(dx + a * nvec), xs.p + a * nvec, I.dfflag.p + 1);
+      }
+    }
     if (r1 > r0) {
       prof_bytes(12 * I.nnz_nz * (r1 - r0) / rows + 4 * (r1 - r0) + 8LL * nvec * (r1 - r0));
       df_apply2(shape, r1 - r0, n2, I.ap_rowptr(), I.ap_colidx(), I.ap_w.p, xs.p, dx, y,
@@ -2725,9 +2791,13 @@ bool interp_apply_forward_staged(Interp &I, const double *xh, double *dx, double
       TMRG_CUDA(cudaMemcpyAsync(yh + r0 * nvec, y + r0 * nvec, sizeof(double) * (r1 - r0) * nvec,
                                 cudaMemcpyDeviceToHost, cs));
   }
+  // every input range is waited for before the call returns
+  for (; split < FC_CHUNKS; split++) TMRG_CUDA(cudaStreamWaitEvent(s, iev[split], 0));
   TMRG_CUDA(cudaStreamSynchronize(cs));
   TMRG_CUDA(cudaStreamSynchronize(s));
+  for (int k = 0; k <= FC_CHUNKS; k++) cudaEventDestroy(iev[k]);
   for (int k = 0; k < FC_CHUNKS; k++) cudaEventDestroy(ev[k]);
+  cudaStreamDestroy(is);
   cudaStreamDestroy(cs);
   interp_check_apply(I);
   return true;
