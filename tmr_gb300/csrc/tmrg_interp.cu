@@ -1134,7 +1134,7 @@ __global__ void k_t_tail(long long ncols, long long nnz, const uint32_t *__restr
 constexpr int LO_WIN = 4096, LO_BUCKETS = 256, LO_THREADS = 256;
 // input chunks of a host-buffer transpose apply: the copy of chunk k+1
 // overlaps the rows whose inputs lie in chunks <= k
-constexpr int TC_CHUNKS = 8;
+constexpr int TC_CHUNKS = 16;
 __global__ void __launch_bounds__(LO_THREADS)
     k_len_order(long long rows, const int *__restrict__ rp, const int *__restrict__ list,
                 int *perm) {
