@@ -26,7 +26,39 @@ struct Knots {
   // refined control point u (bernstein_subdivision)
   int bern;
   double bt[2 * TMRG_MAX_ORDER - 1][TMRG_MAX_ORDER];
+  // Lagrange elements: the 1-D weights of the dependent rows, by knot and
+  // child side (lagrange_tables): le[k + order * side] for an edge node,
+  // lf[k + order * side] for either direction of a face node
+  double le[2 * TMRG_MAX_ORDER][TMRG_MAX_ORDER];
+  double lf[2 * TMRG_MAX_ORDER][TMRG_MAX_ORDER];
 };
+
+// The Lagrange basis at u (TMRInterpolation.h:40-52): N_i the product over
+// j != i, ascending, of (u - k_j) * (1 / (k_i - k_j)), in IEEE double
+// without contraction, so the host values equal a device evaluation.
+static void host_lagrange(int order, double u, const Knots &kn, double *N) {
+  for (int i = 0; i < order; i++) {
+    double v = 1.0;
+    for (int j = 0; j < order; j++)
+      if (i != j) v = v * ((u - kn.k[j]) * kn.r[i][j]);
+    N[i] = v;
+  }
+}
+
+// The 1-D weights of the dependent rows (createDependentConn,
+// TMROctForest.cpp:5337-5519 with the knots of TMRInterpolation): an edge
+// node at knot k of the half-edge on `side` (0 or 1) of its parent edge
+// sits at u = (side - 1) + (1 + k_k) / 2 of the parent's [-1, 1]; a face
+// node at u = (-1 + (1 + k_k) / 2) + side in each face direction.  The row
+// kernel reads them instead of evaluating the basis per row.
+static void lagrange_tables(int order, Knots &kn) {
+  for (int side = 0; side < 2; side++)
+    for (int k = 0; k < order; k++) {
+      const double h = 0.5 * (1.0 + kn.k[k]);
+      host_lagrange(order, (double)(side - 1) + h, kn, kn.le[k + order * side]);
+      host_lagrange(order, (-1.0 + h) + (double)side, kn, kn.lf[k + order * side]);
+    }
+}
 
 // Dependent-node weights of Bernstein elements (eval_bernstein_weights,
 // TMRInterpolation.h:309-439, used by createDependentConn at
@@ -513,17 +545,6 @@ __device__ void parent_face_nodes(const DepCtx &d, const Oct &p, int fi,
     }
 }
 
-__device__ __forceinline__ void lagrange(int order, double u, const Knots &kn,
-                                         double *N) {
-  for (int i = 0; i < order; i++) {
-    double v = 1.0;
-    for (int j = 0; j < order; j++) {
-      if (i != j) v = __dmul_rn(v, __dmul_rn(__dsub_rn(u, kn.k[j]), kn.r[i][j]));
-    }
-    N[i] = v;
-  }
-}
-
 // Pass A: which dependent nodes sit on a hanging edge (row length order)
 // or only on a hanging face (order^2).  Pass B: last writer per row, as
 // (element+1) << 11 | (0..11 for an edge, 16..21 for a face) << 6 | position of
@@ -617,40 +638,16 @@ __global__ void k_dep_write(long long n, DepCtx d, Knots kn,
     int ei = sub, k = pos;
     parent_edge_nodes(d, p, ei, dconn + ptr);
     int sb = (ei < 4) ? x : (ei < 8) ? y : z;
-    if (kn.bern) {
-      const double *N = kn.bt[(o - 1) * (sb - 1) + k + o - 1];
-      for (int j = 0; j < o; j++) dw[ptr + j] = N[j];
-      return;
-    }
-    double u = __dadd_rn(1.0 * (sb - 1), __dmul_rn(0.5, __dadd_rn(1.0, kn.k[k])));
-    lagrange(o, u, kn, &dw[ptr]);
+    const double *N = kn.bern ? kn.bt[(o - 1) * (sb - 1) + k + o - 1] : kn.le[k + o * sb];
+    for (int j = 0; j < o; j++) dw[ptr + j] = N[j];
   } else {
     int fi = sub - 16, ii = pos % o, jj = pos / o;
     parent_face_nodes(d, p, fi, dconn + ptr);
-    if (kn.bern) {
-      // u = -(order-1) + ii plus (order-1) times the child offset of the
-      // face's first direction, v likewise (both integers)
-      const int a = (fi < 2) ? y : x, b = (fi < 4) ? z : y;
-      const double *Nu = kn.bt[ii + (o - 1) * a];
-      const double *Nv = kn.bt[jj + (o - 1) * b];
-      for (int j = 0; j < o * o; j++) dw[ptr + j] = __dmul_rn(Nu[j % o], Nv[j / o]);
-      return;
-    }
-    double u = __dadd_rn(-1.0, __dmul_rn(0.5, __dadd_rn(1.0, kn.k[ii])));
-    double v = __dadd_rn(-1.0, __dmul_rn(0.5, __dadd_rn(1.0, kn.k[jj])));
-    if (fi < 2) {
-      u = __dadd_rn(u, 1.0 * y);
-      v = __dadd_rn(v, 1.0 * z);
-    } else if (fi < 4) {
-      u = __dadd_rn(u, 1.0 * x);
-      v = __dadd_rn(v, 1.0 * z);
-    } else {
-      u = __dadd_rn(u, 1.0 * x);
-      v = __dadd_rn(v, 1.0 * y);
-    }
-    double Nu[TMRG_MAX_ORDER], Nv[TMRG_MAX_ORDER];
-    lagrange(o, u, kn, Nu);
-    lagrange(o, v, kn, Nv);
+    // the child offsets of the face's two directions; Bernstein: u =
+    // -(order-1) + ii plus (order-1) times the offset, v likewise
+    const int a = (fi < 2) ? y : x, b = (fi < 4) ? z : y;
+    const double *Nu = kn.bern ? kn.bt[ii + (o - 1) * a] : kn.lf[ii + o * a];
+    const double *Nv = kn.bern ? kn.bt[jj + (o - 1) * b] : kn.lf[jj + o * b];
     for (int j = 0; j < o * o; j++) dw[ptr + j] = __dmul_rn(Nu[j % o], Nv[j / o]);
   }
 }
@@ -925,7 +922,10 @@ void forest_create_nodes(Forest &f) {
     for (int j = 0; j < TMRG_MAX_ORDER; j++)
       kn.r[i][j] = (i != j && i < o && j < o) ? 1.0 / (f.knots[i] - f.knots[j]) : 0.0;
   }
-  if (f.interp == TMRG_BERNSTEIN_POINTS) bernstein_subdivision(o, kn);
+  if (f.interp == TMRG_BERNSTEIN_POINTS)
+    bernstein_subdivision(o, kn);
+  else
+    lagrange_tables(o, kn);
   DBuf<unsigned> epos(nd + 1, s);
   DBuf<int> order(nd + 1, s);
   launch(k_dep_edge_flag, blocks_for(nd, 256), 256, 0, s, nd,
