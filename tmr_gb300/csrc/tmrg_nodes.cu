@@ -604,7 +604,7 @@ __global__ void k_dep_len(long long nd, int o, const unsigned *__restrict__ he,
   if (i < nd) len[i] = he[i] ? o : (hf[i] ? o * o : 0);
 }
 
-__global__ void k_dep_write(long long n, DepCtx d, Knots kn,
+__global__ void __launch_bounds__(128, 12) k_dep_write(long long n, DepCtx d, Knots kn,
                             const int *__restrict__ blk,
                             const int *__restrict__ xs,
                             const int *__restrict__ ys,
