@@ -99,7 +99,7 @@ __global__ void k_elist_count(long long n, int cnpe, const int *__restrict__ con
 // + kk*co^2, so lanes run in computeElemInterp's loop order) into shared
 // memory, then a stable rank sort by column writes the list.
 constexpr int EL_WARPS = 4;
-__global__ void __launch_bounds__(EL_WARPS * 32)
+__global__ void __launch_bounds__(EL_WARPS * 32, 16)
     k_elist_fill(long long n, int cnpe, const int *__restrict__ conn,
                  const int *__restrict__ dptr, const int *__restrict__ dconn,
                  const double *__restrict__ dw, const long long *__restrict__ eoff,
