@@ -279,6 +279,17 @@ __global__ void k_first_of_run(long long m, const Key *__restrict__ keys, unsign
 
 // Element connectivity in local node numbers (createLocalConn,
 // TMROctForest.cpp:4660-4867).
+// Orders 2 and 3 (one node per object, objects in local-node order): conn
+// entry i of the element-major array is the number of object i, one thread
+// per entry so the object reads and conn writes are contiguous.
+__global__ void k_local_conn_flat(long long m, const unsigned *__restrict__ obj_of,
+                                  const unsigned *__restrict__ noff, int *lconn) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) lconn[i] = (int)noff[obj_of[i]];
+}
+
+// Order >= 4: one thread per element expands its edge/face/interior
+// objects with the owner frame's edge reversal and face orientation.
 __global__ void k_local_conn(long long n, ConnDev c, NodeGen g,
                              const int *__restrict__ blk,
                              const int *__restrict__ xs,
@@ -293,16 +304,6 @@ __global__ void k_local_conn(long long n, ConnDev c, NodeGen g,
   const int npe = o * o * o;
   int *out = lconn + e * npe;
   const unsigned *ob = obj_of + e * g.nobj;
-  if (o == 2) {
-    for (int j = 0; j < 8; j++) out[j] = (int)noff[ob[j]];
-    return;
-  }
-  if (g.lab.bits == 0) {  // order 3 with one node per object
-    for (int j = 0; j < 27; j++) out[j] = (int)noff[ob[j]];
-    return;
-  }
-  // order >= 4: expand edge/face/interior objects with the owner frame's
-  // edge reversal and face orientation.
   Oct el{blk[e], xs[e], ys[e], zs[e], lev[e]};
   int rev[27], fid[27];
   for (int j = 0; j < 27; j++) {
@@ -842,10 +843,14 @@ void forest_create_nodes(Forest &f) {
   f.num_local = nl;
 
   DBuf<int> lconn((size_t)n * npe, s);
-  launch(k_local_conn, blocks_for(n, 128), 128, 0, s, n, c, g,
-         (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
-         (const int *)f.z.p, (const int16_t *)f.level.p,
-         (const unsigned *)obj_of.p, (const unsigned *)noff.p, lconn.p);
+  if (o == 2 || g.lab.bits == 0)  // g.nobj == npe
+    launch(k_local_conn_flat, blocks_for(n * npe, 256), 256, 0, s, n * npe,
+           (const unsigned *)obj_of.p, (const unsigned *)noff.p, lconn.p);
+  else
+    launch(k_local_conn, blocks_for(n, 128), 128, 0, s, n, c, g,
+           (const int *)f.block.p, (const int *)f.x.p, (const int *)f.y.p,
+           (const int *)f.z.p, (const int16_t *)f.level.p,
+           (const unsigned *)obj_of.p, (const unsigned *)noff.p, lconn.p);
   obj_of.release();
 
   // 3. labels and numbering
