@@ -25,7 +25,9 @@ Multi-GPU: replicas only (one independent pipeline per rank, no
 collectives on the data path); the reported time is the max over ranks.
 """
 import argparse
+import contextlib
 import ctypes
+import gc
 import json
 import os
 import subprocess
@@ -93,6 +95,24 @@ def aggregate(ms_local, units_local, world, allreduce_max):
 
 # ---------------------------------------------------------------------------
 # GPU pipeline
+@contextlib.contextmanager
+def gc_paused():
+    """Python's cyclic garbage collector collected before and paused during
+    the timed steps (as the timeit module does): a full collection of a
+    process holding torch walks every Python object for ~0.1 s at an
+    arbitrary step.  The library's objects hold no reference cycles, so
+    reference counting still frees every step's forests, P and host views
+    inside the step that drops them."""
+    gc.collect()
+    was = gc.isenabled()
+    gc.disable()
+    try:
+        yield
+    finally:
+        if was:
+            gc.enable()
+
+
 def gpu_pipeline(TMR, conn, W, x_fine=None, host=False, prefetched=None, mark=None):
     """Returns (units, products).  host=True uses host buffers throughout.
     mark(stage) (optional) is called after each stage is queued."""
@@ -532,17 +552,18 @@ def run_gpu(args):
     syncs0 = TMR.host_sync_count()
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     ev0, ev1 = evs[0], evs[-1]
-    ev0.record()
     tot_units = 0
     last = None
-    for i in range(args.steps):
-        # the previous step's hierarchy is released before the next one is
-        # built (its destruction stays inside the timed region)
-        last = None
-        u, last = gpu_pipeline(TMR, conn, W, x_fine)
-        tot_units += u
-        evs[i + 1].record()
-    barrier()
+    with gc_paused():
+        ev0.record()
+        for i in range(args.steps):
+            # the previous step's hierarchy is released before the next one
+            # is built (its destruction stays inside the timed region)
+            last = None
+            u, last = gpu_pipeline(TMR, conn, W, x_fine)
+            tot_units += u
+            evs[i + 1].record()
+        barrier()
     clocks = clk.stop()
     launches = TMR.kernel_launch_count() - launches0
     syncs = TMR.host_sync_count() - syncs0
@@ -1590,17 +1611,19 @@ def run_e2e(TMR, conn, W, args, barrier, world, x_fine, units_per_step):
     link0 = host_link_rates(x_fine)
     each = []
     h2d = d2h = 0
-    for _ in range(steps):
-        # every step bracketed by a barrier (host-synchronous API: the
-        # results are in host memory when the call returns)
-        t0 = time.perf_counter()
-        u, o = gpu_pipeline(TMR, conn, W, host=True, prefetched=pre)
-        barrier()
-        each.append(time.perf_counter() - t0)
-        if u != units_per_step:
-            raise RuntimeError("e2e step built %d octants, expected %d" % (u, units_per_step))
-        h2d, d2h = o["h2d"], o["d2h"]
-        del o
+    with gc_paused():
+        for _ in range(steps):
+            # every step bracketed by a barrier (host-synchronous API: the
+            # results are in host memory when the call returns)
+            t0 = time.perf_counter()
+            u, o = gpu_pipeline(TMR, conn, W, host=True, prefetched=pre)
+            barrier()
+            each.append(time.perf_counter() - t0)
+            if u != units_per_step:
+                raise RuntimeError("e2e step built %d octants, expected %d"
+                                   % (u, units_per_step))
+            h2d, d2h = o["h2d"], o["d2h"]
+            del o
     link1 = host_link_rates(x_fine)
     # one more step split by stage (host clock: the host-buffer calls
     # return with their results in host memory)
