@@ -1135,6 +1135,7 @@ constexpr int LO_WIN = 4096, LO_BUCKETS = 256, LO_THREADS = 256;
 // input chunks of a host-buffer transpose apply: the copy of chunk k+1
 // overlaps the rows whose inputs lie in chunks <= k
 constexpr int TC_CHUNKS = 16;
+static_assert(TC_CHUNKS < 32, "k_chunk_bounds runs one warp");
 __global__ void __launch_bounds__(LO_THREADS)
     k_len_order(long long rows, const int *__restrict__ rp, const int *__restrict__ list,
                 int *perm) {
@@ -1184,6 +1185,19 @@ __global__ void k_t_chunk_keys(long long ncols, long long nin, const int *__rest
   const long long last = p1 > p0 ? tci[p1 - 1] : 0;
   keys[c] = (uint64_t)((last * TC_CHUNKS) / (nin > 0 ? nin : 1));
   vals[c] = (uint32_t)c;
+}
+// Start of each chunk's run in the sorted chunk keys: bounds[k] = the first
+// position whose key is >= k (lower bound), for k = 0..nk.
+__global__ void k_chunk_bounds(long long n, const uint64_t *__restrict__ keys, int nk,
+                               long long *bounds) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k > nk) return;
+  long long lo = 0, hi = n;
+  while (lo < hi) {
+    const long long mid = (lo + hi) >> 1;
+    if (keys[mid] < (uint64_t)k) lo = mid + 1; else hi = mid;
+  }
+  bounds[k] = lo;
 }
 __global__ void k_rowsum(long long rows, const int *__restrict__ rowptr,
                          const float2 *__restrict__ vals, double *sum) {
@@ -1871,14 +1885,14 @@ void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long lon
     launch(k_t_chunk_keys, blocks_for(I.cols, 256), 256, 0, s, I.cols, rows,
            (const int *)I.t_rowptr.p, (const int *)I.t_colidx.p, ck.p, cv.p);
     radix_sort(ck, &cv, I.cols, bits_for(TC_CHUNKS), s);
-    std::vector<uint64_t> hk(I.cols > 0 ? I.cols : 1);
-    if (I.cols)
-      TMRG_CUDA(cudaMemcpyAsync(hk.data(), ck.p, sizeof(uint64_t) * I.cols,
-                                cudaMemcpyDeviceToHost, s));
-    TMRG_CUDA(cudaStreamSynchronize(s));
+    // the chunk boundaries in the sorted keys, found on the device (only
+    // TC_CHUNKS + 1 numbers come back)
+    DBuf<long long> cb(TC_CHUNKS + 1, s);
+    launch(k_chunk_bounds, 1, 32, 0, s, I.cols, (const uint64_t *)ck.p, TC_CHUNKS, cb.p);
     I.t_chunk.assign(TC_CHUNKS + 1, 0);
-    for (int k = 0; k <= TC_CHUNKS; k++)
-      I.t_chunk[k] = std::lower_bound(hk.begin(), hk.begin() + I.cols, (uint64_t)k) - hk.begin();
+    TMRG_CUDA(cudaMemcpyAsync(I.t_chunk.data(), cb.p, sizeof(long long) * (TC_CHUNKS + 1),
+                              cudaMemcpyDeviceToHost, s));
+    TMRG_CUDA(cudaStreamSynchronize(s));
     I.t_perm.alloc(I.cols + 1, s);
     for (int k = 0; k < TC_CHUNKS; k++) {
       const long long a = I.t_chunk[k], n = I.t_chunk[k + 1] - a;
