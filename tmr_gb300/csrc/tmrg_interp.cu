@@ -1823,6 +1823,7 @@ void interp_create(Forest &fine, Forest &coarse, Interp &I) {
 // row permutation and P^T.
 void interp_finish(Interp &I, long long nonzeros, cudaStream_t s, const long long *keepoff) {
   const long long rows = I.rows, nnz = I.nnz;
+  I.win_maxcol.clear();  // made again by the first host-buffer prolongation
   // the apply copy (apply_keeps entries), worth a second copy only when the
   // dropped entries are a good part of P
   I.nnz_nz = (nnz - nonzeros) * 8 >= nnz ? nonzeros : nnz;
