@@ -311,7 +311,6 @@ __global__ void __launch_bounds__(FG_WARPS * 32)
   const int r = fg_stage(c, g, e, sm, L);
   const int K = r & 0xffff, total = r >> 16;
   if (K == 0) return;
-  const int *s_node = (const int *)(sm + L.node);
   const double *s_w = (const double *)(sm + L.w);
   const uint8_t *s_a = (const uint8_t *)(sm + L.a);
   const uint16_t *s_u = (const uint16_t *)(sm + L.u);
@@ -335,7 +334,6 @@ __global__ void __launch_bounds__(FG_WARPS * 32)
       T[a * K + v] = __fma_rn(mab, wb, T[a * K + v]);
     }
   }
-  (void)s_node;
   // entries ordered by distinct node (stable), and each node's first slot
   for (int i = lane; i < total; i += 32) {
     const int ui = s_u[i];
@@ -684,7 +682,7 @@ template <typename T>
 static void horner(Filter &F, bool tr, int vpn, const T *in, T *out, const T *Ainv,
                    const T *B, const T *Tinv) {
   cudaStream_t s = F.s;
-  long long n = F.n, len = n * vpn;
+  const long long n = F.n;
   if (n == 0) return;
   if (vpn == 3 && F.N > 0) {
     // three components: padded (candidate 0) or sliced-ELL with three
